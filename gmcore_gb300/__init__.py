@@ -1,0 +1,234 @@
+"""GB300 GMCORE dynamics step: Python host side over the C ABI.
+
+The library (``lib/libgmcore_gpu.so``, built from ``csrc/`` for sm_103a)
+replaces the reference's ``time_integrate`` (src/dynamics/gmcore_mod.F90:577)
+behind the functions of ``include/gmcore_gpu.h``.  This module loads it with
+ctypes and mirrors the Fortran driver's sequence: set the initial state,
+``prepare`` (the run prologue, gmcore_mod.F90:97-135), ``step`` (the time
+loop body) and ``diagnose`` (gmcore_mod.F90:213-341).
+
+There is no CPU fallback: every compute call goes through the CUDA library
+and fails with an exception when it is missing or has no GPU.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (Config, Diag, View, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
+                  TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, LIMITER_NONE,
+                  LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
+                  VCOORD_WRF_L64, PREC_FP64, PREC_MIXED)
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libgmcore_gpu.so")
+
+EXPORTED = (
+    "gmc_config_default", "gmc_create", "gmc_lon_halo_width", "gmc_set_field", "gmc_set_tracer",
+    "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
+    "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
+)
+
+_lib = None
+
+
+class GmcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(build_if_missing=True):
+    """Load the CUDA library (building it in-tree on first use)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise OSError(f"{LIB_PATH} is missing; run python -m gmcore_gb300.build")
+        from .build import build
+        build()
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    lib.gmc_config_default.argtypes = [P(Config)]
+    lib.gmc_config_default.restype = None
+    lib.gmc_create.argtypes = [P(Config), P(C.c_void_p)]
+    lib.gmc_lon_halo_width.argtypes = [C.c_void_p, P(C.c_int32)]
+    lib.gmc_set_field.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, P(View)]
+    lib.gmc_get_field.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, P(View)]
+    lib.gmc_set_tracer.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View)]
+    lib.gmc_get_tracer.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View)]
+    lib.gmc_prepare.argtypes = [C.c_void_p]
+    lib.gmc_step.argtypes = [C.c_void_p, C.c_int32]
+    lib.gmc_diagnose.argtypes = [C.c_void_p, C.c_int32, P(Diag)]
+    lib.gmc_time_step.argtypes = [C.c_void_p, P(C.c_int64)]
+    lib.gmc_last_error.argtypes = [C.c_void_p]
+    lib.gmc_last_error.restype = C.c_char_p
+    lib.gmc_destroy.argtypes = [C.c_void_p]
+    lib.gmc_destroy.restype = None
+    lib.gmc_mesh_metric.argtypes = [P(Config), C.c_char_p, P(C.c_double), C.c_size_t]
+    lib.gmc_filter_taps.argtypes = [P(Config), C.c_int32, C.c_int32, P(C.c_int32), C.c_size_t]
+    lib.gmc_make_ic.argtypes = [P(Config), C.c_int32, C.c_uint64, C.c_double] + [P(C.c_double)] * 6
+    _lib = lib
+    return lib
+
+
+def _dptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def view_of(a, nk=None):
+    """gmc_view over a C-ordered [k][j][i] (or [j][i]) float64 array whose
+    Fortran index space is i = 1..ni, j = 1..nj, k = 1..nk."""
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("view needs a C-contiguous float64 array")
+    v = View()
+    v.data = _dptr(a)
+    shape = a.shape if a.ndim == 3 else (1,) + a.shape
+    v.lb[0], v.lb[1], v.lb[2] = 1, 1, 1
+    v.ub[0], v.ub[1], v.ub[2] = shape[2], shape[1], shape[0]
+    return v
+
+
+def field_shape(cfg, name):
+    nlon, nlat, nlev = cfg.nlon, cfg.nlat, cfg.nlev
+    if name in ("v_lat", "v_f", "mfy_lat", "pv", "pv_lat"):
+        return (nlev, nlat - 1, nlon)
+    if name in ("phs", "phs_f", "gzs", "gz", "gz_f"):
+        return (nlat, nlon)
+    if name == "we_lev":
+        return (nlev + 1, nlat, nlon)
+    return (nlev, nlat, nlon)
+
+
+def mesh_metric(cfg, name):
+    lib = load()
+    n = cfg.nlat - 1 if name.startswith("half") or name.startswith("area_lat") or name in (
+        "area_vtx", "de_lat", "le_lat") else cfg.nlat
+    out = np.zeros(n)
+    rc = lib.gmc_mesh_metric(C.byref(cfg), name.encode(), _dptr(out), n)
+    if rc:
+        raise GmcError(rc, f"metric {name}")
+    return out
+
+
+def filter_taps(cfg, which, lat):
+    lib = load()
+    n = cfg.nlat - 1 if lat else cfg.nlat
+    out = np.zeros(n, dtype=np.int32)
+    rc = lib.gmc_filter_taps(C.byref(cfg), which, lat, out.ctypes.data_as(C.POINTER(C.c_int32)), n)
+    if rc:
+        raise GmcError(rc, "filter taps")
+    return out
+
+
+def make_ic(cfg, kind, seed, noise_k=1.0):
+    """Seeded synthetic initial state (host side, no GPU).  Returns a dict of
+    C-ordered float64 arrays."""
+    lib = load()
+    nlon, nlat, nlev = cfg.nlon, cfg.nlat, cfg.nlev
+    u = np.zeros((nlev, nlat, nlon))
+    v = np.zeros((nlev, nlat - 1, nlon))
+    gzs = np.zeros((nlat, nlon))
+    if kind == 1:
+        h = np.zeros((nlat, nlon))
+        rc = lib.gmc_make_ic(C.byref(cfg), 1, seed, noise_k, _dptr(u), _dptr(v), _dptr(h), None, _dptr(gzs), None)
+        out = {"u_lon": u, "v_lat": v, "gz": h, "gzs": gzs}
+    else:
+        pt = np.zeros((nlev, nlat, nlon))
+        phs = np.zeros((nlat, nlon))
+        q = np.zeros((max(cfg.ntracer, 0), nlev, nlat, nlon))
+        rc = lib.gmc_make_ic(C.byref(cfg), 2, seed, noise_k, _dptr(u), _dptr(v), _dptr(pt), _dptr(phs), _dptr(gzs),
+                             _dptr(q) if cfg.ntracer > 0 else None)
+        out = {"u_lon": u, "v_lat": v, "pt": pt, "phs": phs, "gzs": gzs}
+        if cfg.ntracer > 0:
+            out["q"] = q
+    if rc:
+        raise GmcError(rc, "make_ic")
+    return out
+
+
+class Model:
+    """One GPU context of the dynamics step (all ensemble members)."""
+
+    def __init__(self, cfg):
+        self.lib = load()
+        self.cfg = cfg
+        h = C.c_void_p()
+        rc = self.lib.gmc_create(C.byref(cfg), C.byref(h))
+        self.h = h.value
+        if rc:
+            msg = self.lib.gmc_last_error(self.h).decode() if self.h else "no context"
+            if self.h:
+                self.lib.gmc_destroy(self.h)
+                self.h = None
+            raise GmcError(rc, msg)
+
+    def _check(self, rc):
+        if rc:
+            raise GmcError(rc, self.lib.gmc_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def lon_halo_width(self):
+        out = C.c_int32()
+        self._check(self.lib.gmc_lon_halo_width(self.h, C.byref(out)))
+        return out.value
+
+    def set_field(self, name, a, member=0):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(field_shape(self.cfg, name))
+        self._check(self.lib.gmc_set_field(self.h, member, name.encode(), C.byref(view_of(a))))
+
+    def get_field(self, name, member=0):
+        out = np.zeros(field_shape(self.cfg, name))
+        self._check(self.lib.gmc_get_field(self.h, member, name.encode(), C.byref(view_of(out))))
+        return out
+
+    def set_tracer(self, l, q, member=0):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.cfg.nlev, self.cfg.nlat, self.cfg.nlon)
+        self._check(self.lib.gmc_set_tracer(self.h, member, l, C.byref(view_of(q))))
+
+    def get_tracer(self, l, member=0):
+        out = np.zeros((self.cfg.nlev, self.cfg.nlat, self.cfg.nlon))
+        self._check(self.lib.gmc_get_tracer(self.h, member, l, C.byref(view_of(out))))
+        return out
+
+    def set_state(self, state, member=0):
+        for name, a in state.items():
+            if name == "q":
+                for l in range(a.shape[0]):
+                    self.set_tracer(l, a[l], member)
+            else:
+                self.set_field(name, a, member)
+
+    def prepare(self):
+        self._check(self.lib.gmc_prepare(self.h))
+
+    def step(self, n=1):
+        self._check(self.lib.gmc_step(self.h, n))
+
+    def diagnose(self, member=0):
+        d = Diag()
+        self._check(self.lib.gmc_diagnose(self.h, member, C.byref(d)))
+        return d.as_dict()
+
+    @property
+    def time_step(self):
+        out = C.c_int64()
+        self._check(self.lib.gmc_time_step(self.h, C.byref(out)))
+        return out.value

@@ -1,0 +1,125 @@
+// Device-side common definitions for the GB300 GMCORE step.
+//
+// Layout in HBM: every field is stored without halos, level-major,
+// [k][j][i] with i (longitude) fastest and a row pitch of nlon elements.
+// Full-latitude fields have nlat rows (both pole rows included), half-latitude
+// fields nlat-1 rows, half-level fields nlev+1 levels.  Halo points of the
+// reference arrays are produced by index arithmetic instead of copies:
+//   - longitude: periodic wrap;
+//   - latitude beyond a pole: the row on the other side of the pole, rotated
+//     by nlon/2 for interior columns, which is what the single-rank
+//     fill_halo writes (src/utils/parallel_mod.F90:529-563);
+//   - level ghost values of potential temperature and tracers: the linear
+//     extrapolation / copy the reference stores in its level halo
+//     (operators_mod.F90:1085-1090, adv_mod.F90:260-265), recomputed on load.
+// Indices in kernels are the reference's 1-based Fortran indices.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gmcore_gpu.h"
+
+namespace gmc {
+
+// Error word bits set by kernels (read by the host after a step).
+enum : unsigned {
+  ERR_CFLX = 1u, ERR_CFLY = 2u, ERR_CFLZ = 4u, ERR_NONMONO = 8u, ERR_NEGTRACER = 16u, ERR_NAN = 32u,
+};
+
+struct FilterDev {
+  const int *ntaps_full;   // [nlat], row j at [j-1]
+  const int *ntaps_half;   // [nhalf]
+  const int *off_full;     // weight offsets
+  const int *off_half;
+  const double *wgt;
+  int max_taps;
+};
+
+// Grid constants and 1-D metric tables (device pointers).  Row tables are
+// indexed [j + 1] for j = -1 .. n+2 (j = 0 and j = n+1 hold the reference's
+// halo values), level tables [k - 1].
+struct DGrid {
+  int nlon, nlat, nhalf, nlev, hx, half;
+  int baroclinic;
+  double radius, g, Rd, cpd, p0, kappa, p0h, ptop, dlon;
+  int ke_scheme;
+  double ke_cell_wgt;
+  int pv_scheme, upwind_order_pv, pv_pole_stokes, coriolis_scheme, limiter;
+  double upwind_wgt_pv;
+  const double *area_cell, *area_subcell1, *area_subcell2;
+  const double *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
+  const double *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
+  const double *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
+  const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat;
+  const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
+  const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
+  const double *lon_damp_full;                                     // [j-1]
+  FilterDev big, small1, small2;
+  unsigned *err;                                                   // device error word
+};
+
+#define ROW(t, j) ((t)[(j) + 1])
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); }
+
+__device__ __forceinline__ size_t ix3(int nrow, int nlon, int i, int j, int k) {
+  return ((size_t)(k - 1) * nrow + (j - 1)) * nlon + (i - 1);
+}
+
+// Read a full-latitude field at any (i, j) the reference's stencils touch.
+template <class T>
+__device__ __forceinline__ T rd_full(const T *a, const DGrid &g, int i, int j, int k) {
+  if (j < 1 || j > g.nlat) {
+    bool lon_halo = i < 1 || i > g.nlon;
+    if (lon_halo) {
+      j = j < 1 ? j + 3 : j - 3;   // halo columns keep the unrotated rows
+    } else {
+      j = j < 1 ? 2 - j : 2 * g.nlat - j;
+      i += g.half;
+    }
+  }
+  return a[ix3(g.nlat, g.nlon, wrap(i, g.nlon), j, k)];
+}
+
+// Same for half-latitude fields.
+template <class T>
+__device__ __forceinline__ T rd_half(const T *a, const DGrid &g, int i, int j, int k) {
+  if (j < 1 || j > g.nhalf) {
+    bool lon_halo = i < 1 || i > g.nlon;
+    if (lon_halo) {
+      j = j < 1 ? j + 2 : j - 2;
+    } else {
+      j = j < 1 ? 1 - j : 2 * g.nhalf + 1 - j;
+      i += g.half;
+    }
+  }
+  return a[ix3(g.nhalf, g.nlon, wrap(i, g.nlon), j, k)];
+}
+
+// Fixed-order block sum (deterministic for a given blockDim).  All threads
+// receive the result.
+__device__ __forceinline__ double block_sum(double v, double *smem) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (l == 0) smem[w] = v;
+  __syncthreads();
+  double s = 0;
+  for (int t = 0; t < nw; ++t) s += smem[t];
+  __syncthreads();
+  return s;
+}
+
+// Sum of f(i) over a latitude ring i = 1..nlon by one block.
+template <class F>
+__device__ __forceinline__ double ring_sum(int nlon, double *smem, F f) {
+  double s = 0;
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) s += f(i);
+  return block_sum(s, smem);
+}
+
+__device__ __forceinline__ double fsign(double a, double b) { return copysign(fabs(a), b); }
+__device__ __forceinline__ float fsign(float a, float b) { return copysignf(fabsf(a), b); }
+
+}  // namespace gmc

@@ -1,0 +1,865 @@
+// Dynamics kernels of one forward-backward stage on the lat-lon C-grid.
+//
+// Most kernels run one thread block per latitude row and level (grid
+// = rows x levels): a row is contiguous in HBM, pole rows reduce their ring
+// inside the block, and row filters keep the whole row in shared memory.
+// Column kernels (vertical sweeps) run one thread per (i, j) column.
+// Reference routines are cited per kernel.
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+#include "stencil.cuh"
+
+namespace gmc {
+
+namespace {
+
+template <class R>
+__device__ __forceinline__ MassField<R> mass_of(const DGrid &g, const Slot<R> &s) {
+  return MassField<R>{s.phs_f, s.gz, s.gzs};
+}
+
+// ---------------------------------------------------------------------------
+// calc_mf (operators_mod.F90:545-583): mfx_lon = m_lon u, mfy_lat = m_lat v
+// with m_lon, m_lat the edge averages of the cell mass
+// (interp_mod.F90:233-275).  Pole rows of mfx_lon stay zero.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void k_mass_flux(DGrid g, Slot<R> s) {
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const MassField<R> M = mass_of(g, s);
+  if (j == 1 || j == g.nlat) {
+    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) s.mfx_lon[ix3(g.nlat, g.nlon, i, j, k)] = (R)0;
+  } else {
+    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
+      R m_lon = (M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * (R)0.5;
+      size_t o = ix3(g.nlat, g.nlon, i, j, k);
+      s.mfx_lon[o] = m_lon * s.u_f[o];
+    }
+  }
+  if (j <= g.nhalf) {
+    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
+      R m_lat = (M.at(g, i, j, k) + M.at(g, i, j + 1, k)) * (R)0.5;
+      size_t o = ix3(g.nhalf, g.nlon, i, j, k);
+      s.mfy_lat[o] = m_lat * s.v_f[o];
+    }
+  }
+}
+
+// Tangential mass fluxes and winds (operators_mod.F90:585-605).
+template <class R>
+__global__ void k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const MassField<R> M = mass_of(g, s);
+  if (j <= g.nhalf) {
+    const R w1 = (R)ROW(g.htw1, j), w2 = (R)ROW(g.htw2, j);
+    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
+      const int im = wrap(i - 1, g.nlon);
+      R mfx_lat = w1 * (s.mfx_lon[ix3(g.nlat, g.nlon, im, j, k)] + s.mfx_lon[ix3(g.nlat, g.nlon, i, j, k)]) +
+                  w2 * (s.mfx_lon[ix3(g.nlat, g.nlon, im, j + 1, k)] + s.mfx_lon[ix3(g.nlat, g.nlon, i, j + 1, k)]);
+      R m_lat = (M.at(g, i, j, k) + M.at(g, i, j + 1, k)) * (R)0.5;
+      w.u_lat[ix3(g.nhalf, g.nlon, i, j, k)] = mfx_lat / m_lat;
+    }
+  }
+  if (j == 1 || j == g.nlat) {
+    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) w.v_lon[ix3(g.nlat, g.nlon, i, j, k)] = (R)0;
+  } else {
+    const R w1 = (R)ROW(g.ftw1, j), w2 = (R)ROW(g.ftw2, j);
+    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
+      const int ip = wrap(i + 1, g.nlon);
+      R mfy_lon = w1 * (s.mfy_lat[ix3(g.nhalf, g.nlon, i, j - 1, k)] + s.mfy_lat[ix3(g.nhalf, g.nlon, ip, j - 1, k)]) +
+                  w2 * (s.mfy_lat[ix3(g.nhalf, g.nlon, i, j, k)] + s.mfy_lat[ix3(g.nhalf, g.nlon, ip, j, k)]);
+      R m_lon = (M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * (R)0.5;
+      w.v_lon[ix3(g.nlat, g.nlon, i, j, k)] = mfy_lon / m_lon;
+    }
+  }
+}
+
+// calc_ke (operators_mod.F90:234-352): cell KE, optionally blended with the
+// four vertex KEs (ke_scheme 2); pole cells take the ring mean of v^2.
+template <class R>
+__global__ void k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
+  __shared__ double red[32];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const R *u = s.u_f, *v = s.v_f;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  if (j == 1 || j == nlat) {
+    const int jv = j == 1 ? 1 : nhalf;
+    double p = ring_sum(nlon, red, [&](int i) {
+      double x = (double)v[ix3(nhalf, nlon, i, jv, k)];
+      return x * x;
+    });
+    p = p / nlon;
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) w.ke[ix3(nlat, nlon, i, j, k)] = (R)p;
+    return;
+  }
+  auto U = [&](int i, int jj) { return u[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
+  auto V = [&](int i, int jj) { return v[ix3(nhalf, nlon, wrap(i, nlon), jj, k)]; };
+  auto sq = [](R x) { return x * x; };
+  const R alw = (R)ROW(g.area_lon_west, j), ale = (R)ROW(g.area_lon_east, j);
+  const R aln = (R)ROW(g.area_lat_north, j - 1), als = (R)ROW(g.area_lat_south, j), ac = (R)ROW(g.area_cell, j);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    R ke = (alw * sq(U(i - 1, j)) + ale * sq(U(i, j)) + aln * sq(V(i, j - 1)) + als * sq(V(i, j))) / ac;
+    if (g.ke_scheme == 2) {
+      const R cw = (R)g.ke_cell_wgt;
+      R k1 = ((R)ROW(g.area_lat_east, j) * sq(V(i - 1, j)) + (R)ROW(g.area_lat_west, j) * sq(V(i, j)) +
+              (R)ROW(g.area_lon_north, j) * sq(U(i - 1, j)) + (R)ROW(g.area_lon_south, j + 1) * sq(U(i - 1, j + 1))) /
+             (R)ROW(g.area_vtx, j);
+      R k2 = ((R)ROW(g.area_lat_east, j - 1) * sq(V(i - 1, j - 1)) + (R)ROW(g.area_lat_west, j - 1) * sq(V(i, j - 1)) +
+              (R)ROW(g.area_lon_north, j - 1) * sq(U(i - 1, j - 1)) + (R)ROW(g.area_lon_south, j) * sq(U(i - 1, j))) /
+             (R)ROW(g.area_vtx, j - 1);
+      R k3 = ((R)ROW(g.area_lat_east, j - 1) * sq(V(i, j - 1)) + (R)ROW(g.area_lat_west, j - 1) * sq(V(i + 1, j - 1)) +
+              (R)ROW(g.area_lon_north, j - 1) * sq(U(i, j - 1)) + (R)ROW(g.area_lon_south, j) * sq(U(i, j))) /
+             (R)ROW(g.area_vtx, j - 1);
+      R k4 = ((R)ROW(g.area_lat_east, j) * sq(V(i, j)) + (R)ROW(g.area_lat_west, j) * sq(V(i + 1, j)) +
+              (R)ROW(g.area_lon_north, j) * sq(U(i, j)) + (R)ROW(g.area_lon_south, j + 1) * sq(U(i, j + 1))) /
+             (R)ROW(g.area_vtx, j);
+      ke = ((R)1 - cw) * ((k1 + k4) * (R)ROW(g.area_subcell2, j) + (k2 + k3) * (R)ROW(g.area_subcell1, j)) / ac + cw * ke;
+    }
+    w.ke[ix3(nlat, nlon, i, j, k)] = ke;
+  }
+}
+
+// calc_vor + calc_pv (operators_mod.F90:612-703) with the vertex mass of
+// interp_cell_to_vtx (interp_mod.F90:438-463).
+template <class R>
+__global__ void k_pv(DGrid g, Slot<R> s, Work<R> w) {
+  __shared__ double red[32];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const MassField<R> M = mass_of(g, s);
+  const bool pole = g.pv_pole_stokes && (j == 1 || j == nhalf);
+  double pole_vor = 0;
+  if (pole) {
+    const double le = ROW(g.le_lat, j);
+    const double sgn = j == 1 ? -1.0 : 1.0;
+    double p = ring_sum(nlon, red, [&](int i) { return sgn * (double)w.u_lat[ix3(nhalf, nlon, i, j, k)] * le; });
+    pole_vor = p / nlon / ROW(g.area_cell, j == 1 ? 1 : nhalf + 1);
+  }
+  const R dl0 = (R)ROW(g.de_lon, j), dl1 = (R)ROW(g.de_lon, j + 1), dt = (R)ROW(g.de_lat, j), av = (R)ROW(g.area_vtx, j);
+  const R as2 = (R)ROW(g.area_subcell2, j), as1 = (R)ROW(g.area_subcell1, j + 1), f = (R)ROW(g.half_f, j);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    const int ip = wrap(i + 1, nlon);
+    R vor;
+    if (pole) {
+      vor = (R)pole_vor;
+    } else {
+      vor = (s.u_f[ix3(nlat, nlon, i, j, k)] * dl0 - s.u_f[ix3(nlat, nlon, i, j + 1, k)] * dl1 +
+             s.v_f[ix3(nhalf, nlon, ip, j, k)] * dt - s.v_f[ix3(nhalf, nlon, i, j, k)] * dt) / av;
+    }
+    R m_vtx = ((M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * as2 + (M.at(g, i, j + 1, k) + M.at(g, i + 1, j + 1, k)) * as1) / av;
+    s.pv[ix3(nhalf, nlon, i, j, k)] = (vor + f) / m_vtx;
+  }
+}
+
+template <class R>
+__device__ __forceinline__ R upwind3(R dir, R wgt, R f1, R f2, R f3, R f4) {
+  const R c31 = (R)(7.0 / 12.0), c32 = (R)(-1.0 / 12.0), c33 = (R)(1.0 / 12.0);
+  return c31 * (f3 + f2) + c32 * (f4 + f1) + c33 * (f4 - f1 - (R)3 * (f3 - f2)) * wgt * dir;
+}
+template <class R>
+__device__ __forceinline__ R upwind1(R dir, R wgt, R f1, R f2) {
+  return (R)0.5 * (f2 + f1) + (R)(-0.5) * (f2 - f1) * wgt * dir;
+}
+
+// interp_pv_midpoint / interp_pv_upwind (operators_mod.F90:705-795).
+template <class R>
+__global__ void k_pv_edges(DGrid g, Slot<R> s, Work<R> w) {
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const R eps = (R)2.220446049250313e-16;
+  const R wgt = (R)g.upwind_wgt_pv;
+  const R *pv = s.pv;
+  auto P = [&](int i, int jj) { return rd_half(pv, g, i, jj, k); };
+  if (j == 1 || j == nlat) {
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) s.pv_lon[ix3(nlat, nlon, i, j, k)] = (R)0;
+  } else {
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      size_t o = ix3(nlat, nlon, i, j, k);
+      R mid = P(i, j - 1) + P(i, j);
+      R val;
+      if (g.pv_scheme == GMC_PV_MIDPOINT) {
+        val = (R)0.5 * (P(i, j) + P(i, j - 1));
+      } else {
+        R un = s.u_f[o], vt = w.v_lon[o];
+        R b = fabs(vt) / (sqrt(un * un + vt * vt) + eps);
+        R dir = fsign((R)1, vt);
+        R up = g.upwind_order_pv == 3 ? upwind3(dir, wgt, P(i, j - 2), P(i, j - 1), P(i, j), P(i, j + 1))
+                                      : upwind1(dir, wgt, P(i, j - 1), P(i, j));
+        val = b * up + ((R)1 - b) * (R)0.5 * mid;
+      }
+      s.pv_lon[o] = val;
+    }
+  }
+  if (j <= nhalf) {
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      size_t o = ix3(nhalf, nlon, i, j, k);
+      R val;
+      if (g.pv_scheme == GMC_PV_MIDPOINT) {
+        val = (R)0.5 * (P(i - 1, j) + P(i, j));
+      } else {
+        R ut = w.u_lat[o], vn = s.v_f[o];
+        R b = fabs(ut) / (sqrt(ut * ut + vn * vn) + eps);
+        R dir = fsign((R)1, ut);
+        R up = g.upwind_order_pv == 3 ? upwind3(dir, wgt, P(i - 2, j), P(i - 1, j), P(i, j), P(i + 1, j))
+                                      : upwind1(dir, wgt, P(i - 1, j), P(i, j));
+        val = b * up + ((R)1 - b) * (R)0.5 * (P(i - 1, j) + P(i, j));
+      }
+      s.pv_lat[o] = val;
+    }
+  }
+}
+
+// adv_batch_accum_uv_cell, CFL part (adv_batch_mod.F90:252-373): RK4
+// departure points along each axis give the Courant numbers; divx/divy are
+// the axis-split divergences (pole rows: ring sums).
+template <class R>
+__global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt_) {
+  __shared__ double red[32];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const double radius = g.radius, dlon = g.dlon;
+  auto half_lon = [&](int i) { double f = 0.0 + (i - 1) * dlon; return f + 0.5 * dlon; };
+  if (j == 1 || j == nlat) {
+    const int jv = j == 1 ? 1 : nhalf;
+    const double sgn = j == 1 ? 1.0 : -1.0;
+    double p = ring_sum(nlon, red, [&](int i) { return sgn * (double)v[ix3(nhalf, nlon, i, jv, k)]; });
+    p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      size_t o = ix3(nlat, nlon, i, j, k);
+      divy[o] = (R)p;
+      divx[o] = (R)0;
+    }
+  } else {
+    const double dx = ROW(g.de_lon, j), cl = ROW(g.full_cos_lat, j);
+    const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      auto Ul = [&](int l) {   // any l: a corrupted wind must not index out of the row
+        int lw = ((l - 1) % nlon + nlon) % nlon + 1;
+        return (double)u[ix3(nlat, nlon, lw, j, k)];
+      };
+      double x0 = radius * half_lon(i) * cl;
+      double u1 = Ul(i);
+      double x1 = x0 + dt_ / 2 * u1;
+      int l = (int)floor(i + (x1 - x0) / dx);
+      double u2 = ((radius * half_lon(l + 1) * cl - x1) * Ul(l) + (x1 - radius * half_lon(l) * cl) * Ul(l + 1)) / dx;
+      double x2 = x0 + dt_ / 2 * u2;
+      l = (int)floor(i + (x2 - x0) / dx);
+      double u3 = ((radius * half_lon(l + 1) * cl - x2) * Ul(l) + (x2 - radius * half_lon(l) * cl) * Ul(l + 1)) / dx;
+      double x3 = x0 + dt_ * u3;
+      l = (int)floor(i + (x3 - x0) / dx);
+      double u4 = ((radius * half_lon(l + 1) * cl - x3) * Ul(l) + (x3 - radius * half_lon(l) * cl) * Ul(l + 1)) / dx;
+      double c = (u1 + 2 * u2 + 2 * u3 + u4) / 6 * dt_ / dx;
+      if (!(fabs(c) <= (double)g.hx)) atomicOr(g.err, ERR_CFLX);
+      size_t o = ix3(nlat, nlon, i, j, k);
+      cflx[o] = (R)c;
+      double uw = Ul(i - 1);
+      divx[o] = (R)((u1 - uw) * lel / ac);
+      double vn = (double)v[ix3(nhalf, nlon, i, j, k)], vs = (double)v[ix3(nhalf, nlon, i, j - 1, k)];
+      divy[o] = (R)((vn * la0 - vs * la1) / ac);
+    }
+  }
+  if (j <= nhalf) {
+    const double dy = ROW(g.de_lat, j);
+    const double y0 = radius * ROW(g.half_lat, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      auto Vl = [&](int l) { return (double)v[ix3(nhalf, nlon, i, l, k)]; };
+      auto interp = [&](int l, double y) {
+        return ((radius * ROW(g.half_lat, l + 1) - y) * Vl(l) + (y - radius * ROW(g.half_lat, l)) * Vl(l + 1)) / dy;
+      };
+      double v1 = Vl(j);
+      double y1 = y0 + dt_ / 2 * v1;
+      int l = (int)floor(j + (y1 - y0) / dy);
+      double v2 = (l < 1 || l > nhalf - 1) ? v1 : interp(l, y1);
+      double y2 = y0 + dt_ / 2 * v2;
+      l = (int)floor(j + (y2 - y0) / dy);
+      double v3 = (l < 1 || l > nhalf - 1) ? v1 : interp(l, y2);
+      double y3 = y0 + dt_ * v3;
+      l = (int)floor(j + (y3 - y0) / dy);
+      double v4 = (l < 1 || l > nhalf - 1) ? v1 : interp(l, y3);
+      double c = (v1 + 2 * v2 + 2 * v3 + v4) / 6 * dt_ / dy;
+      if (!(fabs(c) <= 1.0)) atomicOr(g.err, ERR_CFLY);
+      cfly[ix3(nhalf, nlon, i, j, k)] = (R)c;
+    }
+  }
+}
+
+// Vertical RK4 departure in eta and its Courant number
+// (adv_batch_accum_we_lev, adv_batch_mod.F90:525-628).  we and ml hold the
+// column's vertical mass flux and half-level mass, index [k-1].
+__device__ __forceinline__ double cflz_of(const DGrid &g, const double *we, const double *ml, int k, double dt_, bool &bad) {
+  const int nlev = g.nlev;
+  const double *HL = g.half_lev, *HD = g.half_dlev, *FD = g.full_dlev;   // [k-1]
+  auto locate = [&](double w, double z) {
+    int l;
+    if (w > 0) {
+      for (l = k; l <= nlev; ++l)
+        if (HL[l - 1] <= z && z <= HL[l]) break;
+      if (l == nlev + 1) { bad = true; l = nlev; }
+    } else {
+      for (l = k - 1; l >= 1; --l)
+        if (HL[l - 1] <= z && z <= HL[l]) break;
+      if (l == 0) { bad = true; l = 1; }
+    }
+    return l;
+  };
+  auto interp = [&](int l, double z) {
+    return ((HL[l] - z) * we[l - 1] / ml[l - 1] * HD[l - 1] + (z - HL[l - 1]) * we[l] / ml[l] * HD[l]) / FD[l - 1];
+  };
+  double z0 = HL[k - 1];
+  double w1 = we[k - 1] / ml[k - 1] * HD[k - 1];
+  double z1 = z0 + dt_ / 2 * w1;
+  double w2 = interp(locate(w1, z1), z1);
+  double z2 = z0 + dt_ / 2 * w2;
+  double w3 = interp(locate(w2, z2), z2);
+  double z3 = z0 + dt_ * w3;
+  double w4 = interp(locate(w3, z3), z3);
+  double deta = (w1 + 2 * w2 + 2 * w3 + w4) / 6 * dt_;
+  int ks, ke, s;
+  if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
+  deta = fabs(deta);
+  for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s) {
+    deta = deta - FD[l - 1];
+    if (deta < 0) return s * ((1 + deta / FD[l - 1]) + abs(l - ks));
+  }
+  return NAN;   // departure left the column: the reference keeps the previous value
+}
+
+// calc_grad_mf + calc_dphsdt + calc_we_lev + the mass batch's accum_we_lev
+// for one column (operators_mod.F90:939-1006, 1120-1143, 192-226).
+template <class R>
+__global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
+  extern __shared__ double sh[];
+  double *red = sh, *ring = sh + 32;
+  const int j = blockIdx.y + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
+  const bool pole = j == 1 || j == nlat;
+  if (pole) {
+    const int jv = j == 1 ? 1 : nhalf;
+    const double sgn = j == 1 ? 1.0 : -1.0;
+    for (int k = 1; k <= nlev; ++k) {
+      double p = ring_sum(nlon, red, [&](int ii) { return sgn * (double)s.mfy_lat[ix3(nhalf, nlon, ii, jv, k)]; });
+      if (threadIdx.x == 0) ring[k - 1] = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
+    }
+    __syncthreads();
+  }
+  if (i > nlon) return;
+  double mfp[66];
+  double we[66], ml[66];
+  const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
+  const int im = wrap(i - 1, nlon);
+  double dphs = 0, mf = 0;
+  for (int k = 1; k <= nlev; ++k) {
+    double dlon, dlat;
+    if (pole) {
+      dlon = 0;
+      dlat = ring[k - 1];
+    } else {
+      dlon = ((double)s.mfx_lon[ix3(nlat, nlon, i, j, k)] - (double)s.mfx_lon[ix3(nlat, nlon, im, j, k)]) * lel / ac;
+      dlat = ((double)s.mfy_lat[ix3(nhalf, nlon, i, j, k)] * la0 - (double)s.mfy_lat[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
+    }
+    dphs = dphs - dlon - dlat;
+    mf = mf + dlon + dlat;
+    mfp[k - 1] = mf;
+  }
+  const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
+  w.dphs[c2] = dphs;
+  we[0] = 0;
+  for (int k = 2; k <= nlev; ++k) we[k - 1] = -(g.hybi[k - 1] * dphs) - mfp[k - 2];
+  we[nlev] = 0;
+  for (int k = 1; k <= nlev + 1; ++k) s.we_lev[ix3(nlat, nlon, i, j, k)] = we[k - 1];
+  // half-level mass from the hybrid pressures (calc_m, operators_mod.F90:505-525)
+  const double phs = s.phs_f[c2];
+  double plo = ph_lev(g, 1, phs), ph_prev = 0;
+  for (int k = 1; k <= nlev; ++k) {
+    double phi = ph_lev(g, k + 1, phs);
+    double ph = 0.5 * (plo + phi);
+    ml[k - 1] = k == 1 ? ph - plo : ph - ph_prev;
+    ph_prev = ph;
+    plo = phi;
+  }
+  ml[nlev] = plo - ph_prev;
+  bool bad = false;
+  for (int k = 2; k <= nlev; ++k) {
+    double c = cflz_of(g, we, ml, k, dt, bad);
+    size_t o = ix3(nlat, nlon, i, j, k);
+    if (c == c) w.cflz[o] = (R)c;
+  }
+  if (bad) atomicOr(g.err, ERR_CFLZ);
+}
+
+// Momentum tendencies of the forward pass (gmcore_mod.F90:478-490 / 507-518):
+// du = qhv - dke/dlon - we du/dlev, dv = -qhu - dke/dlat - we dv/dlev with the
+// energy-conserving Coriolis term (calc_coriolis, operators_mod.F90:846-906),
+// the KE gradient (:908-937) and SB81 vertical advection (:1145-1216).
+template <class R>
+__global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
+  const MassField<R> M = mass_of(g, s);
+  auto MFX = [&](int i, int jj) { return s.mfx_lon[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
+  auto MFY = [&](int i, int jj) { return s.mfy_lat[ix3(nhalf, nlon, wrap(i, nlon), jj, k)]; };
+  auto PVLON = [&](int i, int jj) { return s.pv_lon[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
+  auto PVLAT = [&](int i, int jj) { return s.pv_lat[ix3(nhalf, nlon, wrap(i, nlon), jj, k)]; };
+  if (j != 1 && j != nlat) {
+    const R t1 = (R)ROW(g.ftw1, j), t2 = (R)ROW(g.ftw2, j), de = (R)ROW(g.de_lon, j);
+    const R aw = (R)ROW(g.area_lon_west, j), ae = (R)ROW(g.area_lon_east, j), al = (R)ROW(g.area_lon, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      const size_t o = ix3(nlat, nlon, i, j, k);
+      const R pl = s.pv_lon[o];
+      R qhv;
+      if (g.coriolis_scheme == 1) {
+        qhv = (t1 * (MFY(i, j - 1) * (pl + PVLAT(i, j - 1)) + MFY(i + 1, j - 1) * (pl + PVLAT(i + 1, j - 1))) +
+               t2 * (MFY(i, j) * (pl + PVLAT(i, j)) + MFY(i + 1, j) * (pl + PVLAT(i + 1, j)))) * (R)0.5;
+      } else {
+        R mfy_lon = t1 * (MFY(i, j - 1) + MFY(i + 1, j - 1)) + t2 * (MFY(i, j) + MFY(i + 1, j));
+        qhv = mfy_lon * pl;
+      }
+      R dkedlon = (w.ke[ix3(nlat, nlon, wrap(i + 1, nlon), j, k)] - w.ke[o]) / de;
+      R du = qhv - dkedlon;
+      if (g.baroclinic) {
+        auto WEL = [&](int kk) {
+          double a = s.we_lev[ix3(nlat, nlon, i, j, kk)], b = s.we_lev[ix3(nlat, nlon, wrap(i + 1, nlon), j, kk)];
+          return (R)(((double)aw * a + (double)ae * b) / (double)al);
+        };
+        auto Uk = [&](int kk) { return s.u_f[ix3(nlat, nlon, i, j, kk)]; };
+        R m_lon = (M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * (R)0.5;
+        R wd;
+        if (k == 1)
+          wd = (WEL(k + 1) * (Uk(k + 1) - Uk(k))) / m_lon / (R)2;
+        else if (k == nlev)
+          wd = (WEL(k) * (Uk(k) - Uk(k - 1))) / m_lon / (R)2;
+        else
+          wd = (WEL(k + 1) * (Uk(k + 1) - Uk(k)) + WEL(k) * (Uk(k) - Uk(k - 1))) / m_lon / (R)2;
+        du = du - wd;
+      }
+      w.du[o] = du;
+    }
+  }
+  if (j <= nhalf) {
+    const R t1 = (R)ROW(g.htw1, j), t2 = (R)ROW(g.htw2, j), de = (R)ROW(g.de_lat, j);
+    const R an = (R)ROW(g.area_lat_north, j), as = (R)ROW(g.area_lat_south, j), al = (R)ROW(g.area_lat, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      const size_t o = ix3(nhalf, nlon, i, j, k);
+      const R pl = s.pv_lat[o];
+      R qhu;
+      if (g.coriolis_scheme == 1) {
+        qhu = (t1 * (MFX(i - 1, j) * (pl + PVLON(i - 1, j)) + MFX(i, j) * (pl + PVLON(i, j))) +
+               t2 * (MFX(i - 1, j + 1) * (pl + PVLON(i - 1, j + 1)) + MFX(i, j + 1) * (pl + PVLON(i, j + 1)))) * (R)0.5;
+      } else {
+        R mfx_lat = t1 * (MFX(i - 1, j) + MFX(i, j)) + t2 * (MFX(i - 1, j + 1) + MFX(i, j + 1));
+        qhu = mfx_lat * pl;
+      }
+      R dkedlat = (w.ke[ix3(nlat, nlon, i, j + 1, k)] - w.ke[ix3(nlat, nlon, i, j, k)]) / de;
+      R dv = -qhu - dkedlat;
+      if (g.baroclinic) {
+        auto WEL = [&](int kk) {
+          double a = s.we_lev[ix3(nlat, nlon, i, j + 1, kk)], b = s.we_lev[ix3(nlat, nlon, i, j, kk)];
+          return (R)(((double)an * a + (double)as * b) / (double)al);
+        };
+        auto Vk = [&](int kk) { return s.v_f[ix3(nhalf, nlon, i, j, kk)]; };
+        R m_lat = (M.at(g, i, j, k) + M.at(g, i, j + 1, k)) * (R)0.5;
+        R wd;
+        if (k == 1)
+          wd = (WEL(k + 1) * (Vk(k + 1) - Vk(k))) / m_lat / (R)2;
+        else if (k == nlev)
+          wd = (WEL(k) * (Vk(k) - Vk(k - 1))) / m_lat / (R)2;
+        else
+          wd = (WEL(k + 1) * (Vk(k + 1) - Vk(k)) + WEL(k) * (Vk(k) - Vk(k - 1))) / m_lat / (R)2;
+        dv = dv - wd;
+      }
+      w.dv[o] = dv;
+    }
+  }
+}
+
+// Shallow-water thickness tendency dgz = -(dmf/dlon + dmf/dlat) g
+// (gmcore_mod.F90:520-524) with the pole ring of calc_grad_mf.
+template <class R>
+__global__ void k_swm_dgz(DGrid g, Slot<R> s, Work<R> w) {
+  __shared__ double red[32];
+  const int j = blockIdx.x + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  if (j == 1 || j == nlat) {
+    const int jv = j == 1 ? 1 : nhalf;
+    const double sgn = j == 1 ? 1.0 : -1.0;
+    double p = ring_sum(nlon, red, [&](int i) { return sgn * (double)s.mfy_lat[ix3(nhalf, nlon, i, jv, 1)]; });
+    p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) w.dgz[ix3(nlat, nlon, i, j, 1)] = (R)(-(0.0 + p) * g.g);
+    return;
+  }
+  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    R dlon = (s.mfx_lon[ix3(nlat, nlon, i, j, 1)] - s.mfx_lon[ix3(nlat, nlon, wrap(i - 1, nlon), j, 1)]) * lel / ac;
+    R dlat = (s.mfy_lat[ix3(nhalf, nlon, i, j, 1)] * la0 - s.mfy_lat[ix3(nhalf, nlon, i, j - 1, 1)] * la1) / ac;
+    w.dgz[ix3(nlat, nlon, i, j, 1)] = -(dlon + dlat) * (R)g.g;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// update_state (time_schemes_mod.F90:120-242): row updates fused with the
+// polar filters.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T *smem_rows(double *base, int nlon, int which) {
+  return reinterpret_cast<T *>(base) + (size_t)which * nlon;
+}
+
+// phs = phs_old + dt dphs; phs_f = big filter(phs)   (:134-143)
+template <class R>
+__global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  extern __shared__ double sh[];
+  const int j = blockIdx.x + 1, nlon = g.nlon;
+  double *row = sh, *ext = sh + nlon;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    size_t c = (size_t)(j - 1) * nlon + i;
+    double v = o.phs[c] + dt * w.dphs[c];
+    n.phs[c] = v;
+    row[i] = v;
+  }
+  filter_row<double>(g.big, true, j, nlon, row, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.phs_f[(size_t)(j - 1) * nlon + i] = row[i];
+}
+
+// pt = small1 filter(pt_old m_old + dt dpt) / m_new   (:153-173)
+template <class R>
+__global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  extern __shared__ double sh[];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1, nlon = g.nlon, nlat = g.nlat;
+  R *row = reinterpret_cast<R *>(sh), *ext = row + nlon;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    size_t c = ix3(nlat, nlon, i + 1, j, k);
+    R m_old = Mass<R>::layer(g, k, o.phs_f[(size_t)(j - 1) * nlon + i]);
+    row[i] = o.pt[c] * m_old + (R)dt * w.dpt[c];
+  }
+  filter_row<R>(g.small1, true, j, nlon, row, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    size_t c = ix3(nlat, nlon, i + 1, j, k);
+    R m_new = Mass<R>::layer(g, k, n.phs_f[(size_t)(j - 1) * nlon + i]);
+    n.pt[c] = row[i] / m_new;
+  }
+}
+
+// Shallow water: gz = gz_old + dt dgz; gz_f = big(gz); gz = small1(gz) (:178-192)
+template <class R>
+__global__ void k_update_gz(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  extern __shared__ double sh[];
+  const int j = blockIdx.x + 1, nlon = g.nlon;
+  R *row = reinterpret_cast<R *>(sh), *row2 = row + nlon, *ext = row2 + nlon;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    size_t c = (size_t)(j - 1) * nlon + i;
+    R v = o.gz[c] + (R)dt * w.dgz[c];
+    row[i] = v;
+    row2[i] = v;
+  }
+  filter_row<R>(g.big, true, j, nlon, row2, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.gz_f[(size_t)(j - 1) * nlon + i] = row2[i];
+  filter_row<R>(g.small1, true, j, nlon, row, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.gz[(size_t)(j - 1) * nlon + i] = row[i];
+}
+
+// Backward-pass column sweep (operators_prepare_2 backward,
+// operators_mod.F90:124-131): hybrid pressures and their Exner power
+// (calc_ph :136-168), temperature (calc_t :170-190) and the hydrostatic
+// geopotential integrated upward from the surface (calc_gz_lev :433-469).
+template <class R>
+__global__ void k_column_backward(DGrid g, Slot<R> n, Work<R> w) {
+  const int j = blockIdx.y + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
+  if (i > nlon) return;
+  const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
+  const double phs = n.phs_f[c2];
+  double pl[66];
+  for (int k = 1; k <= nlev + 1; ++k) {
+    pl[k - 1] = ph_lev(g, k, phs);
+    w.ph_exn_lev[ix3(nlat, nlon, i, j, k)] = pow(pl[k - 1], g.kappa);
+  }
+  double acc = 0;
+  const double gzs = n.gzs[c2];
+  w.gz_lev[ix3(nlat, nlon, i, j, nlev + 1)] = gzs;
+  for (int k = nlev; k >= 1; --k) {
+    double ph = 0.5 * (pl[k - 1] + pl[k]);
+    double t = (double)n.pt[ix3(nlat, nlon, i, j, k)] * pow(ph / g.p0, g.kappa);
+    acc = g.Rd * t * log(pl[k] / pl[k - 1]) + acc;
+    w.gz_lev[ix3(nlat, nlon, i, j, k)] = gzs + acc;
+  }
+}
+
+// u, v = old + dt (du_fwd - pgf); small2 filter (baroclinic); v blended next
+// to the poles; big filter into u_f, v_f   (time_schemes_mod.F90:198-238,
+// pgf_lin97_run pgf_lin97_mod.F90:59-105, pgf_swm_run pgf_swm_mod.F90:18-46,
+// backward pass gmcore_mod.F90:529-571).
+template <class R>
+__device__ __forceinline__ R pgf_lon(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k) {
+  const int nlat = g.nlat, nlon = g.nlon;
+  const int ip = wrap(i + 1, nlon);
+  if (g.baroclinic) {
+    const double *pe = w.ph_exn_lev, *gz = w.gz_lev;
+    double dph1 = pe[ix3(nlat, nlon, ip, j, k + 1)] - pe[ix3(nlat, nlon, i, j, k)];
+    double dph2 = pe[ix3(nlat, nlon, i, j, k + 1)] - pe[ix3(nlat, nlon, ip, j, k)];
+    double dgz1 = gz[ix3(nlat, nlon, i, j, k + 1)] - gz[ix3(nlat, nlon, ip, j, k)];
+    double dgz2 = gz[ix3(nlat, nlon, i, j, k)] - gz[ix3(nlat, nlon, ip, j, k + 1)];
+    return (R)(-(dph1 * dgz1 + dph2 * dgz2) / ROW(g.de_lon, j) / (dph1 + dph2));
+  }
+  return (n.gz_f[ix3(nlat, nlon, ip, j, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / (R)ROW(g.de_lon, j);
+}
+template <class R>
+__device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k) {
+  const int nlat = g.nlat, nlon = g.nlon;
+  if (g.baroclinic) {
+    const double *pe = w.ph_exn_lev, *gz = w.gz_lev;
+    double dph1 = pe[ix3(nlat, nlon, i, j + 1, k + 1)] - pe[ix3(nlat, nlon, i, j, k)];
+    double dph2 = pe[ix3(nlat, nlon, i, j, k + 1)] - pe[ix3(nlat, nlon, i, j + 1, k)];
+    double dgz1 = gz[ix3(nlat, nlon, i, j, k + 1)] - gz[ix3(nlat, nlon, i, j + 1, k)];
+    double dgz2 = gz[ix3(nlat, nlon, i, j, k)] - gz[ix3(nlat, nlon, i, j + 1, k + 1)];
+    return (R)(-(dph1 * dgz1 + dph2 * dgz2) / ROW(g.de_lat, j) / (dph1 + dph2));
+  }
+  return (n.gz_f[ix3(nlat, nlon, i, j + 1, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / (R)ROW(g.de_lat, j);
+}
+
+template <class R>
+__global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  extern __shared__ double sh[];
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const int k = blockIdx.y + 1;
+  R *row = reinterpret_cast<R *>(sh), *nb = row + nlon, *ext = nb + nlon;
+  if ((int)blockIdx.x < nlat) {
+    const int j = blockIdx.x + 1;
+    if (j == 1 || j == nlat) {   // pole rows are not updated; the big filter copies them
+      for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+        size_t c = ix3(nlat, nlon, i + 1, j, k);
+        n.u_f[c] = n.u_lon[c];
+      }
+      return;
+    }
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      size_t c = ix3(nlat, nlon, i + 1, j, k);
+      row[i] = o.u_lon[c] + (R)dt * (w.du[c] - pgf_lon(g, n, w, i + 1, j, k));
+    }
+    if (g.baroclinic) filter_row<R>(g.small2, true, j, nlon, row, ext);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_lon[ix3(nlat, nlon, i + 1, j, k)] = row[i];
+    filter_row<R>(g.big, true, j, nlon, row, ext);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_f[ix3(nlat, nlon, i + 1, j, k)] = row[i];
+    return;
+  }
+  const int j = blockIdx.x - nlat + 1;
+  auto load_v = [&](int jj, R *dst) {
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      size_t c = ix3(nhalf, nlon, i + 1, jj, k);
+      dst[i] = o.v_lat[c] + (R)dt * (w.dv[c] - pgf_lat(g, n, w, i + 1, jj, k));
+    }
+    if (g.baroclinic) filter_row<R>(g.small2, false, jj, nlon, dst, ext);
+    __syncthreads();
+  };
+  load_v(j, row);
+  if (j == 1 || j == nhalf) {
+    load_v(j == 1 ? 2 : nhalf - 1, nb);
+    const R wgt = (R)0.6;
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) row[i] = ((R)1 - wgt) * row[i] + wgt * nb[i];
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_lat[ix3(nhalf, nlon, i + 1, j, k)] = row[i];
+  filter_row<R>(g.big, false, j, nlon, row, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_f[ix3(nhalf, nlon, i + 1, j, k)] = row[i];
+}
+
+// Run-prologue filters (gmcore_mod.F90:112-122): u_f, v_f, phs_f | gz_f.
+template <class R, class T>
+__global__ void k_filter_copy(DGrid g, const T *src, T *dst, int which, int full_lat, int nrow) {
+  extern __shared__ double sh[];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1, nlon = g.nlon;
+  const FilterDev &f = which == 0 ? g.big : which == 1 ? g.small1 : g.small2;
+  T *row = reinterpret_cast<T *>(sh), *ext = row + nlon;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) row[i] = src[ix3(nrow, nlon, i + 1, j, k)];
+  filter_row<T>(f, full_lat != 0, j, nlon, row, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) dst[ix3(nrow, nlon, i + 1, j, k)] = row[i];
+}
+
+// ---------------------------------------------------------------------------
+// diagnose (gmcore_mod.F90:213-341): block partial sums with compensated
+// (Neumaier) accumulation, reduced by one block in fixed order.
+// ---------------------------------------------------------------------------
+struct KSum {
+  double s = 0, c = 0;
+  __device__ void add(double x) {
+    double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x; else c += (x - t) + s;
+    s = t;
+  }
+  __device__ double value() const { return s + c; }
+};
+
+template <class R>
+__global__ void k_diag_partial(DGrid g, Slot<R> s, double *partial) {
+  __shared__ double red[32];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const MassField<R> M = mass_of(g, s);
+  KSum tm, teke, teie, tepe, tav, tpe, tpt;
+  const double ac = ROW(g.area_cell, j);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    const size_t o = ix3(nlat, nlon, i, j, k);
+    const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
+    double m = (double)M.at(g, i, j, k);
+    tm.add(m * ac);
+    if (j != 1 && j != nlat) teke.add((double)s.mfx_lon[o] * 0.5 * (double)s.u_lon[o] * ROW(g.area_lon, j) * 2);
+    if (g.baroclinic) {
+      double pl0 = ph_lev(g, k, s.phs_f[c2]), pl1 = ph_lev(g, k + 1, s.phs_f[c2]);
+      double ph = 0.5 * (pl0 + pl1);
+      double t = (double)s.pt[o] * pow(ph / g.p0, g.kappa);
+      teie.add(m * g.cpd * t * ac);
+      tpt.add(m * (double)s.pt[o] * ac);
+      if (k == 1) tepe.add(s.gzs[c2] * s.phs[c2] * ac);
+    } else {
+      tepe.add((m * m * g.g * 0.5 + m * s.gzs[c2]) * ac);
+    }
+    if (j != 1 && j != nlat) {
+      double m_lon = 0.5 * ((double)M.at(g, i, j, k) + (double)M.at(g, i + 1, j, k));
+      double pl = (double)s.pv_lon[o];
+      tpe.add(m_lon * (pl * pl) * 0.5 * ROW(g.area_lon, j));
+    }
+    if (j <= nhalf) {
+      const size_t oh = ix3(nhalf, nlon, i, j, k);
+      teke.add((double)s.mfy_lat[oh] * 0.5 * (double)s.v_lat[oh] * ROW(g.area_lat, j) * 2);
+      tav.add((double)s.pv[oh] * ROW(g.area_vtx, j));
+      double m_lat = 0.5 * ((double)M.at(g, i, j, k) + (double)M.at(g, i, j + 1, k));
+      double pl = (double)s.pv_lat[oh];
+      tpe.add(m_lat * (pl * pl) * 0.5 * ROW(g.area_lat, j));
+    }
+  }
+  double vals[7] = {tm.value(), teke.value(), teie.value(), tepe.value(), tav.value(), tpe.value(), tpt.value()};
+  const size_t b = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+  for (int q = 0; q < 7; ++q) {
+    double t = block_sum(vals[q], red);
+    if (threadIdx.x == 0) partial[(size_t)q * gridDim.x * gridDim.y + b] = t;
+  }
+}
+
+__global__ void k_diag_final(const double *partial, int nblk, double *out) {
+  __shared__ double red[32];
+  for (int q = 0; q < 7; ++q) {
+    KSum acc;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc.add(partial[(size_t)q * nblk + b]);
+    // combine the per-thread compensated sums in fixed order
+    double s = block_sum(acc.s, red), c = block_sum(acc.c, red);
+    if (threadIdx.x == 0) out[q] = s + c;
+  }
+}
+
+inline size_t filter_smem(const DGrid &g, int rows, size_t elem) {
+  int hmax = (g.big.max_taps - 1) / 2;
+  return (size_t)(rows * g.nlon + g.nlon + 2 * hmax + 8) * elem;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+template <class R>
+void launch_mass_flux(const DGrid &g, const Launch &L, const Slot<R> &s) {
+  k_mass_flux<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s);
+}
+template <class R>
+void launch_tangent_winds(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  k_tangent_winds<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+}
+template <class R>
+void launch_kinetic_energy(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  k_kinetic_energy<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+}
+template <class R>
+void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  k_pv<R><<<dim3(g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+}
+template <class R>
+void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  k_pv_edges<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+}
+template <class R>
+void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt) {
+  k_batch_cfl<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, u, v, cflx, cfly, divx, divy, dt);
+}
+template <class R>
+void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
+  const int bt = 64;
+  size_t smem = (32 + g.nlev + 2) * sizeof(double);
+  k_column_mass<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, s, w, dt);
+}
+template <class R>
+void launch_momentum_tend(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  k_momentum_tend<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+}
+template <class R>
+void launch_swm_dgz(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  k_swm_dgz<R><<<dim3(g.nlat, 1), L.threads, 0, L.stream>>>(g, s, w);
+}
+template <class R>
+void launch_update_phs(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  k_update_phs<R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 1, sizeof(double)), L.stream>>>(g, o, n, w, dt);
+}
+template <class R>
+void launch_update_pt(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  k_update_pt<R><<<dim3(g.nlat, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, o, n, w, dt);
+}
+template <class R>
+void launch_update_gz(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  k_update_gz<R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt);
+}
+template <class R>
+void launch_column_backward(const DGrid &g, const Launch &L, const Slot<R> &n, const Work<R> &w) {
+  const int bt = 64;
+  k_column_backward<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, n, w);
+}
+template <class R>
+void launch_update_uv(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  k_update_uv<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt);
+}
+template <class R>
+void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s) {
+  k_filter_copy<R, R><<<dim3(g.nlat, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, s.u_lon, s.u_f, 0, 1, g.nlat);
+  k_filter_copy<R, R><<<dim3(g.nhalf, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, s.v_lat, s.v_f, 0, 0, g.nhalf);
+  if (g.baroclinic)
+    k_filter_copy<R, double><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 1, sizeof(double)), L.stream>>>(g, s.phs, s.phs_f, 0, 1, g.nlat);
+  else
+    k_filter_copy<R, R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, s.gz, s.gz_f, 0, 1, g.nlat);
+}
+template <class R>
+void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out) {
+  (void)w;
+  k_diag_partial<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, partial);
+  k_diag_final<<<1, 256, 0, L.stream>>>(partial, g.nlat * g.nlev, out);
+}
+
+#define INSTANTIATE(R)                                                                                              \
+  template void launch_mass_flux<R>(const DGrid &, const Launch &, const Slot<R> &);                              \
+  template void launch_tangent_winds<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);         \
+  template void launch_kinetic_energy<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);        \
+  template void launch_pv<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);                    \
+  template void launch_pv_edges<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);              \
+  template void launch_batch_cfl<R>(const DGrid &, const Launch &, const R *, const R *, R *, R *, R *, R *, double); \
+  template void launch_column_mass<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &, double);   \
+  template void launch_momentum_tend<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);         \
+  template void launch_swm_dgz<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);               \
+  template void launch_update_phs<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double); \
+  template void launch_update_pt<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
+  template void launch_update_gz<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
+  template void launch_column_backward<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);       \
+  template void launch_update_uv<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
+  template void launch_filter_prologue<R>(const DGrid &, const Launch &, const Slot<R> &);                        \
+  template void launch_diagnose<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &, double *, double *);
+
+INSTANTIATE(double)
+INSTANTIATE(float)
+
+}  // namespace gmc

@@ -1,0 +1,773 @@
+// C ABI of the GB300 GMCORE dynamics step: context set-up, state transfer,
+// the time loop (time_integrate, gmcore_mod.F90:577-591) and diagnostics.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gmcore_gpu.h"
+#include "grid.hpp"
+#include "kernels.hpp"
+
+using namespace gmc;
+
+namespace {
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct CudaError {
+  std::string msg;
+  explicit CudaError(std::string m) : msg(std::move(m)) {}
+};
+struct ApiError {
+  int code;
+  std::string msg;
+};
+
+// Bump allocator over one device allocation.
+struct Arena {
+  char *base = nullptr;
+  size_t size = 0, used = 0;
+  void reserve(size_t bytes) {
+    size = bytes;
+    cudaError_t e = cudaMalloc(&base, bytes);
+    if (e != cudaSuccess) {
+      base = nullptr;
+      throw ApiError{GMC_ENOMEM, std::string("device allocation of ") + std::to_string(bytes) + " bytes failed: " +
+                                     cudaGetErrorString(e)};
+    }
+    CK(cudaMemset(base, 0, bytes));
+  }
+  template <class T>
+  T *take(size_t n) {
+    size_t off = (used + 255) & ~(size_t)255;
+    size_t bytes = n * sizeof(T);
+    if (off + bytes > size) throw ApiError{GMC_ENOMEM, "arena overflow"};
+    used = off + bytes;
+    return reinterpret_cast<T *>(base + off);
+  }
+  void release() {
+    if (base) cudaFree(base);
+    base = nullptr;
+  }
+};
+
+// Size of a request: run the same sequence of takes on a counting arena.
+struct Counter {
+  size_t used = 0;
+  template <class T>
+  T *take(size_t n) {
+    used = ((used + 255) & ~(size_t)255) + n * sizeof(T);
+    return nullptr;
+  }
+};
+
+enum FieldKind { FULL3, HALF3, LEV3, TWO_D };
+
+struct FieldInfo {
+  FieldKind kind;
+  int nrow, nk;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Engine: one precision instantiation of the step.
+// ---------------------------------------------------------------------------
+struct EngineBase {
+  virtual ~EngineBase() {}
+  virtual void set_field(int member, const std::string &name, const double *src) = 0;
+  virtual void get_field(int member, const std::string &name, double *dst) = 0;
+  virtual void prepare() = 0;
+  virtual void step(int nsteps) = 0;
+  virtual void diagnose(int member, gmc_diag *out) = 0;
+  virtual unsigned read_error() = 0;
+  long time_step = 0;
+};
+
+template <class R>
+struct Engine : EngineBase {
+  Grid grid;
+  DGrid dg{};
+  Arena tables, arena;
+  cudaStream_t stream = nullptr;
+  Launch L{};
+  int nm = 1;
+  std::vector<Slot<R>> slots;   // [member * 3 + s]
+  std::vector<Work<R>> work;    // [member]
+  std::vector<double *> gzs;    // [member]
+  unsigned *err = nullptr;
+  double *diag_partial = nullptr, *diag_out = nullptr;
+  int old_i = 0, new_i = 1;
+  bool prepared = false;
+  double *pinned = nullptr;
+  size_t pinned_n = 0;
+  R *staging = nullptr;
+
+  size_t full3() const { return (size_t)grid.nlev * grid.nlat * grid.nlon; }
+  size_t half3() const { return (size_t)grid.nlev * grid.nhalf * grid.nlon; }
+  size_t lev3() const { return (size_t)(grid.nlev + 1) * grid.nlat * grid.nlon; }
+  size_t two_d() const { return (size_t)grid.nlat * grid.nlon; }
+
+  template <class A>
+  void carve(A &a, Slot<R> &s, bool baroclinic) {
+    s.u_lon = a.template take<R>(full3());
+    s.v_lat = a.template take<R>(half3());
+    s.u_f = a.template take<R>(full3());
+    s.v_f = a.template take<R>(half3());
+    s.mfx_lon = a.template take<R>(full3());
+    s.mfy_lat = a.template take<R>(half3());
+    s.pv = a.template take<R>(half3());
+    s.pv_lon = a.template take<R>(full3());
+    s.pv_lat = a.template take<R>(half3());
+    if (baroclinic) {
+      s.pt = a.template take<R>(full3());
+      s.phs = a.template take<double>(two_d());
+      s.phs_f = a.template take<double>(two_d());
+      s.we_lev = a.template take<double>(lev3());
+      s.gz = s.gz_f = nullptr;
+    } else {
+      s.gz = a.template take<R>(two_d());
+      s.gz_f = a.template take<R>(two_d());
+      s.pt = nullptr;
+      s.phs = s.phs_f = nullptr;
+      s.we_lev = nullptr;
+    }
+  }
+  template <class A>
+  void carve(A &a, Work<R> &w, bool baroclinic) {
+    w.u_lat = a.template take<R>(half3());
+    w.v_lon = a.template take<R>(full3());
+    w.ke = a.template take<R>(full3());
+    w.du = a.template take<R>(full3());
+    w.dv = a.template take<R>(half3());
+    if (baroclinic) {
+      w.cflx = a.template take<R>(full3());
+      w.cfly = a.template take<R>(half3());
+      w.cflz = a.template take<R>(lev3());
+      w.divx = a.template take<R>(full3());
+      w.divy = a.template take<R>(full3());
+      w.qmfx = a.template take<R>(full3());
+      w.qmfy = a.template take<R>(half3());
+      w.qx = a.template take<R>(full3());
+      w.qy = a.template take<R>(full3());
+      w.ptf_lon = a.template take<R>(full3());
+      w.ptf_lat = a.template take<R>(half3());
+      w.dpt = a.template take<R>(full3());
+      w.dphs = a.template take<double>(two_d());
+      w.ph_exn_lev = a.template take<double>(lev3());
+      w.gz_lev = a.template take<double>(lev3());
+      w.dgz = nullptr;
+    } else {
+      w.dgz = a.template take<R>(two_d());
+      w.cflx = w.cfly = w.cflz = w.divx = w.divy = nullptr;
+      w.qmfx = w.qmfy = w.qx = w.qy = w.ptf_lon = w.ptf_lat = w.dpt = nullptr;
+      w.dphs = w.ph_exn_lev = w.gz_lev = nullptr;
+    }
+  }
+
+  template <class A>
+  void carve_member(A &a, int m, bool baroclinic) {
+    double *z = a.template take<double>(two_d());
+    for (int s = 0; s < 3; ++s) {
+      Slot<R> &sl = slots[m * 3 + s];
+      carve(a, sl, baroclinic);
+      sl.gzs = z;
+    }
+    carve(a, work[m], baroclinic);
+    work[m].gzs = z;
+    gzs[m] = z;
+  }
+
+  explicit Engine(const gmc_config &cfg) {
+    std::string e = grid.build(cfg);
+    if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    nm = cfg.n_members;
+    const bool bc = cfg.baroclinic != 0;
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    L.stream = stream;
+    L.threads = grid.nlon >= 512 ? 256 : 128;
+    upload_tables();
+    slots.resize(3 * nm);
+    work.resize(nm);
+    gzs.resize(nm);
+    Counter cnt;
+    {
+      std::vector<Slot<R>> s2(3 * nm);
+      std::swap(s2, slots);
+      for (int m = 0; m < nm; ++m) carve_member(cnt, m, bc);
+      std::swap(s2, slots);
+    }
+    size_t nblk = (size_t)grid.nlat * grid.nlev;
+    cnt.take<double>(8 * nblk + 64);
+    cnt.take<unsigned>(64);
+    cnt.take<R>(std::max(lev3(), full3()));
+    arena.reserve(cnt.used + 4096);
+    for (int m = 0; m < nm; ++m) carve_member(arena, m, bc);
+    diag_partial = arena.take<double>(8 * nblk);
+    diag_out = arena.take<double>(64);
+    err = arena.take<unsigned>(64);
+    staging = arena.take<R>(std::max(lev3(), full3()));
+    dg.err = err;
+    pinned_n = std::max(lev3(), full3());
+    CK(cudaMallocHost(&pinned, pinned_n * sizeof(double)));
+  }
+
+  ~Engine() override {
+    if (stream) cudaStreamSynchronize(stream);
+    arena.release();
+    tables.release();
+    if (pinned) cudaFreeHost(pinned);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void upload_tables() {
+    const Grid &g = grid;
+    std::vector<char> host;
+    auto push = [&](const void *p, size_t bytes) {
+      size_t off = (host.size() + 255) & ~(size_t)255;
+      host.resize(off + bytes);
+      std::memcpy(host.data() + off, p, bytes);
+      return off;
+    };
+    struct Fix { size_t off; const void **dst; };
+    std::vector<Fix> fixes;
+    auto row = [&](const RowTable &t, const double **dst) { fixes.push_back({push(t.v.data(), t.v.size() * 8), (const void **)dst}); };
+    auto vec = [&](const std::vector<double> &t, const double **dst) {
+      fixes.push_back({push(t.data(), t.size() * 8), (const void **)dst});
+    };
+    row(g.area_cell, &dg.area_cell); row(g.area_subcell1, &dg.area_subcell1); row(g.area_subcell2, &dg.area_subcell2);
+    row(g.area_lon, &dg.area_lon); row(g.area_lon_west, &dg.area_lon_west); row(g.area_lon_east, &dg.area_lon_east);
+    row(g.area_lon_north, &dg.area_lon_north); row(g.area_lon_south, &dg.area_lon_south);
+    row(g.area_lat, &dg.area_lat); row(g.area_lat_west, &dg.area_lat_west); row(g.area_lat_east, &dg.area_lat_east);
+    row(g.area_lat_north, &dg.area_lat_north); row(g.area_lat_south, &dg.area_lat_south);
+    row(g.area_vtx, &dg.area_vtx); row(g.de_lon, &dg.de_lon); row(g.le_lon, &dg.le_lon); row(g.de_lat, &dg.de_lat);
+    row(g.le_lat, &dg.le_lat); row(g.full_f, &dg.full_f); row(g.half_f, &dg.half_f);
+    row(g.full_tangent_wgt1, &dg.ftw1); row(g.full_tangent_wgt2, &dg.ftw2);
+    row(g.half_tangent_wgt1, &dg.htw1); row(g.half_tangent_wgt2, &dg.htw2);
+    row(g.full_cos_lat, &dg.full_cos_lat); row(g.half_lat, &dg.half_lat);
+    vec(g.hyai, &dg.hyai); vec(g.hybi, &dg.hybi); vec(g.half_lev, &dg.half_lev); vec(g.half_dlev, &dg.half_dlev);
+    vec(g.full_dlev, &dg.full_dlev); vec(g.lon_damp_wgt_full, &dg.lon_damp_full);
+    // FP32 layer-mass coefficients
+    std::vector<float> dA(g.nlev + 1, 0.f), dB(g.nlev + 1, 0.f);
+    for (int k = 0; k < g.nlev && g.cfg.baroclinic; ++k) {
+      dA[k] = (float)((g.hyai[k + 1] - g.hyai[k]) * (g.cfg.hybrid_coord_p0 - g.local_ptop));
+      dB[k] = (float)(g.hybi[k + 1] - g.hybi[k]);
+    }
+    size_t offA = push(dA.data(), dA.size() * 4), offB = push(dB.data(), dB.size() * 4);
+    // filters
+    struct FFix { size_t nf, nh, of, oh, w; FilterDev *d; int maxt; };
+    std::vector<FFix> ff;
+    for (const Filter *f : {&g.big, &g.small1, &g.small2}) {
+      std::vector<int> of(g.nlat), oh(g.nhalf);
+      std::vector<double> w;
+      for (int j = 0; j < g.nlat; ++j) { of[j] = (int)w.size(); w.insert(w.end(), f->wgt_full[j].begin(), f->wgt_full[j].end()); }
+      for (int j = 0; j < g.nhalf; ++j) { oh[j] = (int)w.size(); w.insert(w.end(), f->wgt_half[j].begin(), f->wgt_half[j].end()); }
+      w.push_back(0.0);
+      FFix x;
+      x.nf = push(f->ngrid_full.data(), f->ngrid_full.size() * 4);
+      x.nh = push(f->ngrid_half.data(), f->ngrid_half.size() * 4);
+      x.of = push(of.data(), of.size() * 4);
+      x.oh = push(oh.data(), oh.size() * 4);
+      x.w = push(w.data(), w.size() * 8);
+      x.d = f == &g.big ? &dg.big : f == &g.small1 ? &dg.small1 : &dg.small2;
+      x.maxt = f->max_taps();
+      ff.push_back(x);
+    }
+    tables.reserve(host.size() + 256);
+    CK(cudaMemcpy(tables.base, host.data(), host.size(), cudaMemcpyHostToDevice));
+    for (const Fix &f : fixes) *f.dst = tables.base + f.off;
+    dg.dmA = reinterpret_cast<const float *>(tables.base + offA);
+    dg.dmB = reinterpret_cast<const float *>(tables.base + offB);
+    for (const FFix &x : ff) {
+      x.d->ntaps_full = reinterpret_cast<const int *>(tables.base + x.nf);
+      x.d->ntaps_half = reinterpret_cast<const int *>(tables.base + x.nh);
+      x.d->off_full = reinterpret_cast<const int *>(tables.base + x.of);
+      x.d->off_half = reinterpret_cast<const int *>(tables.base + x.oh);
+      x.d->wgt = reinterpret_cast<const double *>(tables.base + x.w);
+      x.d->max_taps = x.maxt;
+    }
+    const gmc_config &c = g.cfg;
+    dg.nlon = g.nlon; dg.nlat = g.nlat; dg.nhalf = g.nhalf; dg.nlev = g.nlev; dg.hx = g.lon_halo_width;
+    dg.half = g.nlon / 2;
+    dg.baroclinic = c.baroclinic;
+    dg.radius = c.radius; dg.g = c.g; dg.Rd = c.Rd; dg.cpd = c.cpd; dg.p0 = c.p0; dg.kappa = c.Rd / c.cpd;
+    dg.p0h = c.hybrid_coord_p0; dg.ptop = g.local_ptop; dg.dlon = g.dlon;
+    dg.ke_scheme = c.ke_scheme; dg.ke_cell_wgt = c.ke_cell_wgt;
+    dg.pv_scheme = c.pv_scheme; dg.upwind_order_pv = c.upwind_order_pv; dg.pv_pole_stokes = c.pv_pole_stokes;
+    dg.coriolis_scheme = c.coriolis_scheme; dg.limiter = c.limiter_type; dg.upwind_wgt_pv = c.upwind_wgt_pv;
+  }
+
+  FieldInfo info(const std::string &name) const {
+    const int nlat = grid.nlat, nhalf = grid.nhalf, nlev = grid.nlev;
+    if (name == "u_lon" || name == "u_f" || name == "pt" || name == "mfx_lon" || name == "pv_lon")
+      return {FULL3, nlat, nlev};
+    if (name == "v_lat" || name == "v_f" || name == "mfy_lat" || name == "pv" || name == "pv_lat")
+      return {HALF3, nhalf, nlev};
+    if (name == "we_lev") return {LEV3, nlat, nlev + 1};
+    return {TWO_D, nlat, 1};
+  }
+
+  // Device pointer of a named field of a slot (R or double flavour).
+  void locate(const Slot<R> &s, int m, const std::string &name, R **pr, double **pd) {
+    *pr = nullptr;
+    *pd = nullptr;
+    const bool bc = grid.cfg.baroclinic != 0;
+    if (name == "u_lon") *pr = s.u_lon;
+    else if (name == "v_lat") *pr = s.v_lat;
+    else if (name == "u_f") *pr = s.u_f;
+    else if (name == "v_f") *pr = s.v_f;
+    else if (name == "mfx_lon") *pr = s.mfx_lon;
+    else if (name == "mfy_lat") *pr = s.mfy_lat;
+    else if (name == "pv") *pr = s.pv;
+    else if (name == "pv_lon") *pr = s.pv_lon;
+    else if (name == "pv_lat") *pr = s.pv_lat;
+    else if (name == "pt" && bc) *pr = s.pt;
+    else if (name == "gz" && !bc) *pr = s.gz;
+    else if (name == "gz_f" && !bc) *pr = s.gz_f;
+    else if (name == "phs" && bc) *pd = s.phs;
+    else if (name == "phs_f" && bc) *pd = s.phs_f;
+    else if (name == "we_lev" && bc) *pd = s.we_lev;
+    else if (name == "gzs") *pd = gzs[m];
+    if (!*pr && !*pd) throw ApiError{GMC_EINVAL, "unknown field '" + name + "' for this model"};
+  }
+
+  size_t count(const FieldInfo &f) const { return (size_t)f.nk * f.nrow * grid.nlon; }
+
+  void set_field(int m, const std::string &name, const double *src) override {
+    FieldInfo f = info(name);
+    R *pr;
+    double *pd;
+    locate(slots[m * 3 + old_i], m, name, &pr, &pd);
+    const size_t n = count(f);
+    if (pd) {
+      CK(cudaMemcpyAsync(pd, src, n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    } else {
+      R *host = reinterpret_cast<R *>(pinned);
+      for (size_t t = 0; t < n; ++t) host[t] = (R)src[t];
+      CK(cudaMemcpyAsync(pr, host, n * sizeof(R), cudaMemcpyHostToDevice, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    prepared = false;
+  }
+
+  void get_field(int m, const std::string &name, double *dst) override {
+    FieldInfo f = info(name);
+    R *pr;
+    double *pd;
+    locate(slots[m * 3 + old_i], m, name, &pr, &pd);
+    const size_t n = count(f);
+    if (pd) {
+      CK(cudaMemcpyAsync(dst, pd, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+    } else {
+      R *host = reinterpret_cast<R *>(pinned);
+      CK(cudaMemcpyAsync(host, pr, n * sizeof(R), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      for (size_t t = 0; t < n; ++t) dst[t] = (double)host[t];
+    }
+  }
+
+  // operators_prepare forward list (operators_mod.F90:117-122)
+  void forward_prepare(int m, const Slot<R> &s) {
+    Work<R> &w = work[m];
+    launch_mass_flux<R>(dg, L, s);
+    launch_tangent_winds<R>(dg, L, s, w);
+    launch_kinetic_energy<R>(dg, L, s, w);
+    launch_pv<R>(dg, L, s, w);
+    launch_pv_edges<R>(dg, L, s, w);
+  }
+
+  // space_operators forward pass (gmcore_mod.F90:467-528)
+  void forward(int m, const Slot<R> &s, double dt) {
+    Work<R> &w = work[m];
+    forward_prepare(m, s);
+    if (grid.cfg.baroclinic) {
+      launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt);
+      launch_column_mass<R>(dg, L, s, w, dt);
+      BatchView<R> b{};
+      b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
+      b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
+      launch_ffsl_hflx<R>(dg, L, b, s.pt, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt);
+      launch_pt_tendency<R>(dg, L, s, w);
+    } else {
+      launch_swm_dgz<R>(dg, L, s, w);
+    }
+    launch_momentum_tend<R>(dg, L, s, w);
+  }
+
+  // step_forward_backward (time_schemes_mod.F90:102-118)
+  void stage(int m, int o, int s, int n, double dt) {
+    const Slot<R> &O = slots[m * 3 + o], &S = slots[m * 3 + s], &N = slots[m * 3 + n];
+    Work<R> &w = work[m];
+    forward(m, S, dt);
+    if (grid.cfg.baroclinic) {
+      launch_update_phs<R>(dg, L, O, N, w, dt);
+      launch_update_pt<R>(dg, L, O, N, w, dt);
+      launch_column_backward<R>(dg, L, N, w);
+    } else {
+      launch_update_gz<R>(dg, L, O, N, w, dt);
+    }
+    launch_update_uv<R>(dg, L, O, N, w, dt);
+  }
+
+  void prepare() override {
+    for (int m = 0; m < nm; ++m) {
+      const Slot<R> &s = slots[m * 3 + old_i];
+      launch_filter_prologue<R>(dg, L, s);
+      forward_prepare(m, s);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    prepared = true;
+    time_step = 0;
+  }
+
+  void step(int nsteps) override {
+    if (!prepared) throw ApiError{GMC_ESTATE, "gmc_prepare must be called after setting the state"};
+    const double dt = grid.cfg.dt_dyn;
+    for (int it = 0; it < nsteps; ++it) {
+      const int o = old_i, n = new_i, t3 = 3 - o - n;
+      for (int m = 0; m < nm; ++m) {
+        switch (grid.cfg.time_scheme) {
+          case GMC_TIME_EULER:
+            stage(m, o, o, n, dt);
+            break;
+          case GMC_TIME_PC2:
+            stage(m, o, o, n, dt / 2.0);
+            stage(m, o, n, t3, dt / 2.0);
+            stage(m, o, t3, n, dt);
+            break;
+          default:
+            stage(m, o, o, n, dt / 3.0);
+            stage(m, o, n, t3, dt / 2.0);
+            stage(m, o, t3, n, dt);
+            break;
+        }
+      }
+      std::swap(old_i, new_i);
+      ++time_step;
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  void diagnose(int m, gmc_diag *out) override {
+    const Slot<R> &s = slots[m * 3 + old_i];
+    launch_diagnose<R>(dg, L, s, work[m], diag_partial, diag_out);
+    double h[8];
+    CK(cudaMemcpyAsync(h, diag_out, 7 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    out->tm = h[0];
+    out->te_ke = h[1];
+    out->te_ie = h[2];
+    out->te_pe = h[3];
+    out->tav = h[4];
+    out->tpe = h[5];
+    out->tpt = h[6];
+    out->te = out->te_ke + out->te_ie + out->te_pe;
+  }
+
+  unsigned read_error() override {
+    unsigned h = 0;
+    CK(cudaMemcpyAsync(&h, err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (h) CK(cudaMemsetAsync(err, 0, sizeof(unsigned), stream));
+    return h;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// The C ABI
+// ---------------------------------------------------------------------------
+struct gmc_ctx {
+  gmc_config cfg;
+  std::unique_ptr<EngineBase> eng;
+  std::string last_error;
+  int lon_halo_width = 0;
+};
+
+namespace {
+
+int fail(gmc_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+template <class F>
+int guarded(gmc_ctx *ctx, F f) {
+  try {
+    return f();
+  } catch (const ApiError &e) {
+    return fail(ctx, e.code, e.msg);
+  } catch (const CudaError &e) {
+    return fail(ctx, GMC_ECUDA, e.msg);
+  } catch (const std::bad_alloc &) {
+    return fail(ctx, GMC_ENOMEM, "host allocation failed");
+  }
+}
+
+int error_word_status(gmc_ctx *ctx, unsigned w) {
+  if (!w) return GMC_OK;
+  if (w & ERR_NAN) return fail(ctx, GMC_ENAN, "non-finite value in the state");
+  if (w & ERR_NONMONO) return fail(ctx, GMC_ENONMONO, "The pressure levels are not monotonic!");
+  if (w & ERR_CFLX) return fail(ctx, GMC_ECFL, "cflx exceeds mesh%lon_halo_width");
+  if (w & ERR_CFLY) return fail(ctx, GMC_ECFL, "cfly exceeds 1");
+  if (w & ERR_CFLZ) return fail(ctx, GMC_ECFL, "cflz exceeds range");
+  if (w & ERR_NEGTRACER) return fail(ctx, GMC_ENEGTRACER, "Negative tracer!");
+  return fail(ctx, GMC_ECUDA, "unknown device error word");
+}
+
+gmc_config normalised(const gmc_config &c) {
+  gmc_config n = c;
+  // parse_namelist (namelist_mod.F90:227-249)
+  if (!n.baroclinic) n.ke_scheme = 1;
+  if (!(n.dt_adv > 0)) n.dt_adv = n.dt_dyn;
+  return n;
+}
+
+// Copy the interior of a Fortran-bounded view into a packed [k][j][i] array.
+bool unpack_view(const gmc_view *v, int nlon, int nrow, int nk, std::vector<double> &out, std::string &err) {
+  if (!v || !v->data) { err = "null view"; return false; }
+  for (int d = 0; d < 3; ++d)
+    if (v->ub[d] < v->lb[d]) { err = "view bounds are empty"; return false; }
+  if (v->lb[0] > 1 || v->ub[0] < nlon || v->lb[1] > 1 || v->ub[1] < nrow || v->lb[2] > 1 || v->ub[2] < nk) {
+    err = "view does not cover the interior (" + std::to_string(nlon) + "x" + std::to_string(nrow) + "x" +
+          std::to_string(nk) + ")";
+    return false;
+  }
+  const long n0 = v->ub[0] - v->lb[0] + 1, n1 = v->ub[1] - v->lb[1] + 1;
+  out.resize((size_t)nlon * nrow * nk);
+  size_t o = 0;
+  for (int k = 1; k <= nk; ++k)
+    for (int j = 1; j <= nrow; ++j) {
+      const double *src = v->data + (size_t)(1 - v->lb[0]) + (size_t)n0 * ((size_t)(j - v->lb[1]) + (size_t)n1 * (k - v->lb[2]));
+      std::memcpy(&out[o], src, nlon * sizeof(double));
+      o += nlon;
+    }
+  return true;
+}
+
+bool pack_view(const gmc_view *v, int nlon, int nrow, int nk, const std::vector<double> &in, std::string &err) {
+  std::vector<double> dummy;
+  if (!v || !v->data) { err = "null view"; return false; }
+  if (v->lb[0] > 1 || v->ub[0] < nlon || v->lb[1] > 1 || v->ub[1] < nrow || v->lb[2] > 1 || v->ub[2] < nk) {
+    err = "view does not cover the interior";
+    return false;
+  }
+  const long n0 = v->ub[0] - v->lb[0] + 1, n1 = v->ub[1] - v->lb[1] + 1;
+  size_t o = 0;
+  for (int k = 1; k <= nk; ++k)
+    for (int j = 1; j <= nrow; ++j) {
+      double *dst = v->data + (size_t)(1 - v->lb[0]) + (size_t)n0 * ((size_t)(j - v->lb[1]) + (size_t)n1 * (k - v->lb[2]));
+      std::memcpy(dst, &in[o], nlon * sizeof(double));
+      o += nlon;
+    }
+  return true;
+}
+
+void field_dims(const gmc_config &c, const std::string &name, int &nrow, int &nk) {
+  nrow = c.nlat;
+  nk = c.nlev;
+  if (name == "v_lat" || name == "v_f" || name == "mfy_lat" || name == "pv" || name == "pv_lat") nrow = c.nlat - 1;
+  if (name == "phs" || name == "phs_f" || name == "gzs" || name == "gz" || name == "gz_f") nk = 1;
+  if (name == "we_lev") nk = c.nlev + 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gmc_config_default(gmc_config *c) {
+  std::memset(c, 0, sizeof(*c));
+  c->nlon = 360; c->nlat = 180; c->nlev = 1;
+  c->baroclinic = 0;
+  c->time_scheme = GMC_TIME_WRFRK3;
+  c->dt_dyn = 60.0; c->dt_adv = 0.0;
+  c->ke_scheme = 2; c->ke_cell_wgt = 0.5;
+  c->pv_scheme = GMC_PV_UPWIND; c->upwind_order_pv = 3; c->upwind_wgt_pv = 1.0; c->pv_pole_stokes = 1;
+  c->coriolis_scheme = 1;
+  c->ffsl_flux_type = GMC_FLUX_PPM; c->limiter_type = GMC_LIMITER_MONO;
+  c->use_div_damp = 0; c->div_damp_order = 2; c->div_damp_coef2 = 1.0 / 128.0;
+  c->vert_coord_template = GMC_VCOORD_NONE;
+  c->ptop = 2.194e2; c->hybrid_coord_p0 = 1.0e5;
+  c->max_wave_speed = 300; c->max_cfl = 0.5;
+  c->filter_coef_a = 1.0; c->filter_coef_b = 0.4; c->filter_coef_c = 0.2; c->filter_coef_d = 0.375; c->filter_coef_e = 0.16;
+  c->lon_halo_width = 2;
+  c->ntracer = 0;
+  c->precision = GMC_PREC_FP64;
+  c->n_members = 1;
+  const double pi = std::atan(1.0) * 4.0;
+  c->radius = 6.37122e6; c->omega = 2 * pi / 86400.0; c->g = 9.80616; c->Rd = 287.04; c->cpd = 1004.0; c->p0 = 1.0e5;
+}
+
+int gmc_create(const gmc_config *cfg, gmc_ctx **out) {
+  if (!cfg || !out) return GMC_EINVAL;
+  *out = nullptr;
+  gmc_ctx *ctx = new gmc_ctx();
+  ctx->cfg = normalised(*cfg);
+  int rc = guarded(ctx, [&]() {
+    std::string e = validate_config(ctx->cfg);
+    if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    if (ctx->cfg.ntracer > 0) throw ApiError{GMC_EINVAL, "tracer batches are not available in this build"};
+    if (ctx->cfg.precision == GMC_PREC_FP64)
+      ctx->eng.reset(new Engine<double>(ctx->cfg));
+    else
+      ctx->eng.reset(new Engine<float>(ctx->cfg));
+    ctx->lon_halo_width = ctx->cfg.precision == GMC_PREC_FP64 ? static_cast<Engine<double> *>(ctx->eng.get())->grid.lon_halo_width
+                                                              : static_cast<Engine<float> *>(ctx->eng.get())->grid.lon_halo_width;
+    return GMC_OK;
+  });
+  if (rc != GMC_OK) {
+    // keep the context so the caller can read the message
+    *out = ctx;
+    ctx->eng.reset();
+    return rc;
+  }
+  *out = ctx;
+  return GMC_OK;
+}
+
+int gmc_lon_halo_width(const gmc_ctx *ctx, int32_t *out) {
+  if (!ctx || !out || !ctx->eng) return GMC_EINVAL;
+  *out = ctx->lon_halo_width;
+  return GMC_OK;
+}
+
+int gmc_set_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view *v) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!name) return fail(ctx, GMC_EINVAL, "null field name");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  return guarded(ctx, [&]() {
+    int nrow, nk;
+    std::string n(name), err;
+    field_dims(ctx->cfg, n, nrow, nk);
+    std::vector<double> buf;
+    if (!unpack_view(v, ctx->cfg.nlon, nrow, nk, buf, err)) throw ApiError{GMC_EINVAL, err};
+    ctx->eng->set_field(member, n, buf.data());
+    return GMC_OK;
+  });
+}
+
+int gmc_set_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v) {
+  (void)member; (void)tracer; (void)v;
+  if (!ctx) return GMC_EINVAL;
+  return fail(ctx, GMC_EINVAL, "this context has no tracers");
+}
+
+int gmc_get_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v) {
+  (void)member; (void)tracer; (void)v;
+  if (!ctx) return GMC_EINVAL;
+  return fail(ctx, GMC_EINVAL, "this context has no tracers");
+}
+
+int gmc_prepare(gmc_ctx *ctx) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  return guarded(ctx, [&]() {
+    ctx->eng->prepare();
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
+}
+
+int gmc_step(gmc_ctx *ctx, int32_t nsteps) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (nsteps < 0) return fail(ctx, GMC_EINVAL, "nsteps < 0");
+  return guarded(ctx, [&]() {
+    ctx->eng->step(nsteps);
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
+}
+
+int gmc_get_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view *v) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!name) return fail(ctx, GMC_EINVAL, "null field name");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  return guarded(ctx, [&]() {
+    int nrow, nk;
+    std::string n(name), err;
+    field_dims(ctx->cfg, n, nrow, nk);
+    std::vector<double> buf((size_t)ctx->cfg.nlon * nrow * nk);
+    ctx->eng->get_field(member, n, buf.data());
+    if (!pack_view(v, ctx->cfg.nlon, nrow, nk, buf, err)) throw ApiError{GMC_EINVAL, err};
+    return GMC_OK;
+  });
+}
+
+int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out) {
+  if (!ctx || !out) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  return guarded(ctx, [&]() {
+    ctx->eng->diagnose(member, out);
+    return GMC_OK;
+  });
+}
+
+int gmc_time_step(const gmc_ctx *ctx, int64_t *out) {
+  if (!ctx || !out || !ctx->eng) return GMC_EINVAL;
+  *out = ctx->eng->time_step;
+  return GMC_OK;
+}
+
+const char *gmc_last_error(const gmc_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+void gmc_destroy(gmc_ctx *ctx) { delete ctx; }
+
+int gmc_mesh_metric(const gmc_config *cfg, const char *name, double *out, size_t n) {
+  if (!cfg || !name || !out) return GMC_EINVAL;
+  try {
+    Grid g;
+    if (!g.build(normalised(*cfg)).empty()) return GMC_EINVAL;
+    const RowTable *t = g.metric(name);
+    if (!t) return GMC_EINVAL;
+    size_t len = t->v.size() - 4;
+    if (n != len) return GMC_EINVAL;
+    for (size_t j = 1; j <= len; ++j) out[j - 1] = (*t)[(int)j];
+    return GMC_OK;
+  } catch (...) {
+    return GMC_EINVAL;
+  }
+}
+
+int gmc_filter_taps(const gmc_config *cfg, int32_t which, int32_t lat, int32_t *out, size_t n) {
+  if (!cfg || !out || which < 0 || which > 2) return GMC_EINVAL;
+  try {
+    Grid g;
+    if (!g.build(normalised(*cfg)).empty()) return GMC_EINVAL;
+    const Filter &f = which == 0 ? g.big : which == 1 ? g.small1 : g.small2;
+    const std::vector<int> &v = lat ? f.ngrid_half : f.ngrid_full;
+    if (n != v.size()) return GMC_EINVAL;
+    for (size_t j = 0; j < n; ++j) out[j] = v[j];
+    return GMC_OK;
+  } catch (...) {
+    return GMC_EINVAL;
+  }
+}
+
+int gmc_make_ic(const gmc_config *cfg, int32_t kind, uint64_t seed, double noise_k, double *u_lon, double *v_lat,
+                double *pt_or_gz, double *phs, double *gzs, double *q) {
+  if (!cfg) return GMC_EINVAL;
+  try {
+    Grid g;
+    if (!g.build(normalised(*cfg)).empty()) return GMC_EINVAL;
+    std::string e = make_ic(g, kind, seed, noise_k, u_lon, v_lat, pt_or_gz, phs, gzs, q);
+    return e.empty() ? GMC_OK : GMC_EINVAL;
+  } catch (...) {
+    return GMC_EINVAL;
+  }
+}
+
+}  // extern "C"

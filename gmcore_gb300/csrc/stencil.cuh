@@ -1,0 +1,114 @@
+// Device helpers shared by the dynamics and advection kernels: layer mass,
+// PPM reconstruction, polar-filter row convolution.
+#pragma once
+
+#include "common.cuh"
+
+namespace gmc {
+
+// ---------------------------------------------------------------------------
+// Layer mass m = ph_lev(k+1) - ph_lev(k) from the filtered surface pressure
+// (calc_ph + calc_m, operators_mod.F90:136-168, 471-503).  The FP64 form
+// evaluates the reference's hybrid formula term by term; the FP32 form uses
+// per-layer coefficients dA_k + dB_k (phs - ptop).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double ph_lev(const DGrid &g, int k, double phs) {
+  return g.hyai[k - 1] * (g.p0h - g.ptop) + g.hybi[k - 1] * (phs - g.ptop) + g.ptop;
+}
+
+template <class R>
+struct Mass;
+
+template <>
+struct Mass<double> {
+  static __device__ __forceinline__ double layer(const DGrid &g, int k, double phs) {
+    return ph_lev(g, k + 1, phs) - ph_lev(g, k, phs);
+  }
+};
+template <>
+struct Mass<float> {
+  static __device__ __forceinline__ float layer(const DGrid &g, int k, double phs) {
+    return fmaf(g.dmB[k - 1], (float)(phs - g.ptop), g.dmA[k - 1]);
+  }
+};
+
+// Cell mass at (i, j, k): baroclinic from phs_f, shallow water (gz - gzs)/g.
+template <class R>
+struct MassField {
+  const double *phs_f;   // baroclinic
+  const R *gz;           // shallow water
+  const double *gzs;
+  __device__ __forceinline__ R at(const DGrid &g, int i, int j, int k) const {
+    i = wrap(i, g.nlon);
+    size_t o = (size_t)(j - 1) * g.nlon + (i - 1);
+    if (g.baroclinic) return Mass<R>::layer(g, k, phs_f[o]);
+    return (R)(((double)gz[o] - gzs[o]) / g.g);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// PPM sub-grid reconstruction with slope limiter (ffsl_mod.F90:1147-1205).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ R slope(int limiter, R fm1, R f, R fp1) {
+  R df = (fp1 - fm1) * (R)0.5;
+  if (limiter == GMC_LIMITER_NONE) return df;
+  if (limiter == GMC_LIMITER_PD) return fsign(fmin(fabs(df), (R)2 * f), df);
+  R dmin = (R)2 * (f - fmin(fmin(fm1, f), fp1));
+  R dmax = (R)2 * (fmax(fmax(fm1, f), fp1) - f);
+  return fsign(fmin(fmin(fabs(df), dmin), dmax), df);
+}
+
+template <class R>
+__device__ __forceinline__ void ppm(int limiter, R fm2, R fm1, R f, R fp1, R fp2, R &fl, R &df, R &f6) {
+  R dfl = slope(limiter, fm2, fm1, f);
+  df = slope(limiter, fm1, f, fp1);
+  R dfr = slope(limiter, f, fp1, fp2);
+  fl = (R)0.5 * (fm1 + f) + (dfl - df) / (R)6;
+  R fr = (R)0.5 * (fp1 + f) + (df - dfr) / (R)6;
+  fl = f - fsign(fmin(fabs(df), fabs(fl - f)), df);
+  fr = f + fsign(fmin(fabs(df), fabs(fr - f)), df);
+  f6 = (R)6 * f - (R)3 * (fl + fr);
+  df = fr - fl;
+}
+
+// Whole-cell sum plus the integral of the parabola over the upwind fraction
+// [s1, s2] of the departure cell, the common tail of hflx_ppm_cell and
+// vflx_ppm_cell (ffsl_mod.F90:833-875, 917-935).
+template <class R>
+__device__ __forceinline__ R ppm_tail(R sum, R fl, R df, R f6, R s1, R s2) {
+  R ds1 = s2 - s1;
+  R ds2 = s2 * s2 - s1 * s1;
+  R ds3 = s2 * s2 * s2 - s1 * s1 * s1;
+  return sum + fl * ds1 + (R)0.5 * df * ds2 + f6 * (ds2 / (R)2 - ds3 / (R)3);
+}
+
+// ---------------------------------------------------------------------------
+// Polar filter of one latitude row (filter_mod.F90:25-163): Gaussian
+// convolution with periodic wrap.  The row lives in shared memory; `ext`
+// receives the row extended by hn points on each side.  Returns false when
+// the row is not filtered (ngrid <= 1).  Accumulation is in FP64.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, int j, int nlon, R *row, R *ext) {
+  const int n = full_lat ? f.ntaps_full[j - 1] : f.ntaps_half[j - 1];
+  if (n <= 1) return false;
+  const int hn = (n - 1) / 2;
+  const double *w = f.wgt + (full_lat ? f.off_full[j - 1] : f.off_half[j - 1]);
+  __syncthreads();
+  for (int t = threadIdx.x; t < nlon + 2 * hn; t += blockDim.x) {
+    int i = t - hn + 1;
+    i = i < 1 ? i + nlon : (i > nlon ? i - nlon : i);
+    ext[t] = row[i - 1];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    double s = 0;
+    for (int t = 0; t < n; ++t) s = s + w[t] * (double)ext[i + t];
+    row[i] = (R)s;
+  }
+  __syncthreads();
+  return true;
+}
+
+}  // namespace gmc

@@ -1,0 +1,196 @@
+/*
+ * gmcore_gpu.h -- C ABI of the GB300 dynamics step for the GMCORE
+ * latitude-longitude C-grid model.
+ *
+ * The library replaces one call of the reference model:
+ *
+ *   time_integrate(dt_dyn, blocks)      src/dynamics/gmcore_mod.F90:577-591
+ *
+ * together with the run prologue that prepares the first step
+ * (src/dynamics/gmcore_mod.F90:97-135) and the conservation monitor
+ * `diagnose` (src/dynamics/gmcore_mod.F90:213-341).  A Fortran host keeps
+ * its namelist, initial conditions, output and restart code and calls these
+ * functions through iso_c_binding (see INTEGRATION.md for the shim).
+ *
+ * Conventions
+ *  - Every function returns an int status: GMC_OK (0) or a negative code.
+ *    A message for the last failure is available from gmc_last_error().
+ *    The library never aborts the process (the reference stops through
+ *    log_error / MPI_ABORT instead).
+ *  - Host arrays are described by gmc_view: a base pointer plus Fortran
+ *    lower/upper bounds per dimension, column-major (i fastest), so a
+ *    Fortran array with halos can be passed as c_loc(a) with lbound/ubound.
+ *    Only interior points are read or written; halos are left untouched.
+ *  - The caller owns host memory; the library never keeps host pointers.
+ *    The library owns device memory; model state stays resident in HBM
+ *    between calls.
+ *  - One host thread per context at a time.  All calls are synchronous.
+ */
+#ifndef GMCORE_GPU_H
+#define GMCORE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GMC_OK           0
+#define GMC_EINVAL      -1   /* malformed argument or unsupported option      */
+#define GMC_ECFL        -2   /* |cflx| > lon halo width or |cfly| > 1 or cflz out of range
+                                (adv_batch_mod.F90:284-287, 331-333, 538-601) */
+#define GMC_ENONMONO    -3   /* pressure levels not monotonic (operators_mod.F90:493-500) */
+#define GMC_ENEGTRACER  -4   /* negative tracer not fixable (adv_mod.F90:251-253, 290-292) */
+#define GMC_ENAN        -5   /* non-finite value in the prognostic state     */
+#define GMC_ETIMEDOUT   -6   /* a bounded device wait gave up                */
+#define GMC_ECUDA       -7   /* CUDA runtime error                           */
+#define GMC_ENOMEM      -8   /* device allocation failed                     */
+#define GMC_ESTATE      -9   /* call out of order (e.g. step before prepare) */
+
+/* ---- option enums (namelist strings of src/utils/namelist_mod.F90) ------ */
+#define GMC_TIME_EULER    0  /* time_scheme = 'euler'  */
+#define GMC_TIME_PC2      1  /* time_scheme = 'pc2'    */
+#define GMC_TIME_WRFRK3   2  /* time_scheme = 'wrfrk3' */
+
+#define GMC_PV_MIDPOINT   0  /* pv_scheme = 'midpoint' */
+#define GMC_PV_UPWIND     1  /* pv_scheme = 'upwind'   */
+
+#define GMC_FLUX_PPM      0  /* ffsl_flux_type = 'ppm' */
+
+#define GMC_LIMITER_NONE  0  /* limiter_type = 'none'  */
+#define GMC_LIMITER_MONO  1  /* limiter_type = 'mono'  */
+#define GMC_LIMITER_PD    2  /* limiter_type = 'pd'    */
+
+#define GMC_VCOORD_NONE       0   /* shallow water                           */
+#define GMC_VCOORD_TEST_L26  26   /* hybrid_coord_test_l26 (hybrid_coord_test_mod.F90:78)  */
+#define GMC_VCOORD_WRF_L32   32   /* hybrid_coord_wrf_l32  (hybrid_coord_test_mod.F90:565) */
+#define GMC_VCOORD_WRF_L64   64   /* hybrid_coord_wrf_l64  (hybrid_coord_test_mod.F90:734) */
+
+#define GMC_PREC_FP64     0  /* FP64 everywhere                               */
+#define GMC_PREC_MIXED    1  /* FP32 bulk stencils/advection, FP64 pole rings,
+                                column sweeps, integrals and filter weights   */
+
+/* ---- configuration: the namelist fields the step depends on ------------- */
+typedef struct gmc_config {
+  int32_t nlon, nlat, nlev;        /* num_lon, num_lat (both pole rows), num_lev  */
+  int32_t baroclinic;              /* 0: shallow water (nlev must be 1)          */
+  int32_t time_scheme;             /* GMC_TIME_*                                 */
+  double  dt_dyn;                  /* s                                          */
+  double  dt_adv;                  /* s; <= 0 means dt_dyn                       */
+  int32_t ke_scheme;               /* 1 or 2                                     */
+  double  ke_cell_wgt;
+  int32_t pv_scheme;               /* GMC_PV_*                                   */
+  int32_t upwind_order_pv;         /* 1 or 3                                     */
+  double  upwind_wgt_pv;
+  int32_t pv_pole_stokes;          /* logical                                    */
+  int32_t coriolis_scheme;         /* 1 or 2                                     */
+  int32_t ffsl_flux_type;          /* GMC_FLUX_*                                 */
+  int32_t limiter_type;            /* GMC_LIMITER_*                              */
+  int32_t use_div_damp;            /* divergence damping after each step         */
+  int32_t div_damp_order;          /* 2 (4 is not supported)                     */
+  double  div_damp_coef2;          /* namelist div_damp_coef2                    */
+  int32_t vert_coord_template;     /* GMC_VCOORD_*                               */
+  double  ptop;                    /* Pa (namelist ptop)                         */
+  double  hybrid_coord_p0;         /* Pa                                         */
+  double  max_wave_speed, max_cfl; /* polar filter                               */
+  double  filter_coef_a, filter_coef_b, filter_coef_c, filter_coef_d, filter_coef_e;
+  int32_t lon_halo_width;          /* namelist minimum; widened by the filter    */
+  int32_t ntracer;                 /* tracers of one FFSL batch (0: none)        */
+  int32_t precision;               /* GMC_PREC_*                                 */
+  int32_t n_members;               /* ensemble members sharing this grid         */
+  double  radius, omega, g, Rd, cpd, p0;   /* const_mod.F90:51-85 ('earth')     */
+} gmc_config;
+
+/* Diagnostics of gmcore_mod.F90:213-341 (FP64, compensated sums). */
+typedef struct gmc_diag {
+  double tm, te, te_ke, te_ie, te_pe, tav, tpe, tpt;
+} gmc_diag;
+
+/* Host array view: data(i,j,k) = data[(i-lb0) + n0*((j-lb1) + n1*(k-lb2))],
+ * n0 = ub0-lb0+1, n1 = ub1-lb1+1.  2-D fields use lb[2] = ub[2] = 1. */
+typedef struct gmc_view {
+  double *data;
+  int32_t lb[3];
+  int32_t ub[3];
+} gmc_view;
+
+typedef struct gmc_ctx gmc_ctx;
+
+/* Fill cfg with the reference defaults (namelist_mod.F90:10-113, earth). */
+void gmc_config_default(gmc_config *cfg);
+
+/* Build mesh metrics, vertical coordinate, polar filters and device state.
+ * Replaces gmcore_init's block set-up (gmcore_mod.F90:45-95). */
+int gmc_create(const gmc_config *cfg, gmc_ctx **out);
+
+/* Longitude halo width the reference would use for this configuration
+ * (process_mod.F90:208-213): max(namelist width, (big-filter taps - 1)/2). */
+int gmc_lon_halo_width(const gmc_ctx *ctx, int32_t *out);
+
+/* Set one prognostic field of one member, interior points only.
+ * Names: "u_lon" (i=1..nlon half lon, j=1..nlat, k=1..nlev),
+ *        "v_lat" (i=1..nlon, j=1..nlat-1, k=1..nlev),
+ *        "pt"    (baroclinic) or "gz" (shallow water), full cells,
+ *        "phs"   (baroclinic, 2-D), "gzs" (static surface geopotential, 2-D),
+ *        "q"     (tracer t: pass k-range 1..nlev, tracer index via gmc_set_tracer).
+ * Mirrors the assignments a set_ic routine makes (e.g.
+ * tests/swm/steady_geostrophic_flow_test_mod.F90:20-67). */
+int gmc_set_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view *v);
+int gmc_set_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v);
+
+/* Run prologue: filters of u, v, phs|gz, mass-batch set-up, all-pass
+ * operators_prepare (gmcore_mod.F90:97-135). */
+int gmc_prepare(gmc_ctx *ctx);
+
+/* Advance nsteps dynamics steps: time_integrate x nsteps, including tracer
+ * advection (adv_run) and the old/new swap of time_advance.  Returns after
+ * the device error word was checked. */
+int gmc_step(gmc_ctx *ctx, int32_t nsteps);
+
+/* Copy a field of the current (old) state to the host, interior only.
+ * Names: those of gmc_set_field plus "u_f", "v_f", "phs_f", "gz_f", "m",
+ * "t", "pv", "ke". */
+int gmc_get_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view *v);
+int gmc_get_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v);
+
+/* Global integrals of the current state (gmcore_mod.F90:213-341). */
+int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out);
+
+/* Number of steps taken since gmc_prepare. */
+int gmc_time_step(const gmc_ctx *ctx, int64_t *out);
+
+const char *gmc_last_error(const gmc_ctx *ctx);
+void gmc_destroy(gmc_ctx *ctx);
+
+/* ---- host-side set-up helpers (no device work) -------------------------
+ * A host without the reference's Fortran initialisation can obtain the same
+ * 1-D metrics and seeded synthetic initial states from these. */
+
+/* 1-D mesh metric by name ("full_lat", "half_lat", "area_cell", "area_lon",
+ * "area_lat", "area_vtx", "le_lon", "de_lon", "le_lat", "de_lat",
+ * "full_f", "half_f", "full_cos_lat", "half_cos_lat", "area_subcell1", ...)
+ * of mesh_mod.F90:134-447; n must equal the metric's length. */
+int gmc_mesh_metric(const gmc_config *cfg, const char *name, double *out, size_t n);
+
+/* Polar-filter tap counts per latitude row: which = 0 big, 1 small1,
+ * 2 small2; lat = 0 full latitudes (nlat), 1 half latitudes (nlat-1). */
+int gmc_filter_taps(const gmc_config *cfg, int32_t which, int32_t lat, int32_t *out, size_t n);
+
+/* Seeded synthetic initial state of a benchmark configuration.
+ *  kind 1: shallow water, 8000 m + degree<=8 harmonics, Gaussian hill,
+ *          geostrophic winds (u, v, gz, gzs filled; phs, pt, q ignored);
+ *  kind 2: dry baroclinic, 300 K + N(0, noise_k) noise, 35 m/s jet,
+ *          Gaussian-blob tracers (u, v, pt, phs, gzs, q filled).
+ * Arrays are interior-only, C order [k][j][i] (Fortran (i,j,k)); q is
+ * [tracer][k][j][i].  A NULL pointer skips that field. */
+int gmc_make_ic(const gmc_config *cfg, int32_t kind, uint64_t seed, double noise_k,
+                double *u_lon, double *v_lat, double *pt_or_gz, double *phs,
+                double *gzs, double *q);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GMCORE_GPU_H */

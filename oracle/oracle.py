@@ -1,0 +1,147 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes wrapper of the FP64 CPU restatement in gmcore_oracle.cpp.  Only the
+tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+load it; the product library never does.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from gmcore_gb300.abi import Config
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBS = {}
+
+
+def build(variant="parity", quiet=True):
+    """Compile the oracle with its Makefile (seconds)."""
+    target = "_build/liboracle.so" if variant == "parity" else "_build/liboracle_omp.so"
+    out = subprocess.run(["make", "-s", target], cwd=HERE, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return os.path.join(HERE, target)
+
+
+def load(variant="parity"):
+    if variant in _LIBS:
+        return _LIBS[variant]
+    path = build(variant)
+    lib = C.CDLL(path)
+    lib.orc_create.restype = C.c_void_p
+    lib.orc_create.argtypes = [C.POINTER(Config), C.c_char_p, C.c_int]
+    lib.orc_destroy.argtypes = [C.c_void_p]
+    lib.orc_lon_halo_width.argtypes = [C.c_void_p]
+    for name in ("orc_set_field", "orc_get_field"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+    for name in ("orc_set_tracer", "orc_get_tracer"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    lib.orc_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    lib.orc_step.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
+    lib.orc_diagnose.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.orc_metric.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int]
+    lib.orc_filter_taps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    _LIBS[variant] = lib
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+FIELD_SHAPES = {
+    # name: (lat kind, lev kind)  lat: 0 full, 1 half; lev: 0 full, 1 half-levels, 2 two-d
+    "u_lon": (0, 0), "v_lat": (1, 0), "u_f": (0, 0), "v_f": (1, 0), "pt": (0, 0), "gz": (0, 0),
+    "gz_f": (0, 0), "phs": (0, 2), "phs_f": (0, 2), "gzs": (0, 2), "m": (0, 0), "t": (0, 0),
+    "pv": (1, 0), "ke": (0, 0), "pv_lon": (0, 0), "pv_lat": (1, 0), "mfx_lon": (0, 0),
+    "mfy_lat": (1, 0), "u_lat": (1, 0), "v_lon": (0, 0), "we_lev": (0, 1), "m_lev": (0, 1),
+    "gz_lev": (0, 1), "ph_lev": (0, 1), "ph_exn_lev": (0, 1), "vor": (1, 0),
+}
+
+
+def field_shape(cfg, name):
+    lat, lev = FIELD_SHAPES[name]
+    nrow = cfg.nlat - 1 if lat else cfg.nlat
+    if lev == 2:
+        return (nrow, cfg.nlon)
+    nk = cfg.nlev + 1 if lev == 1 else cfg.nlev
+    return (nk, nrow, cfg.nlon)
+
+
+class Oracle:
+    """One model instance of the restatement (one ensemble member)."""
+
+    def __init__(self, cfg, variant="parity"):
+        self.lib = load(variant)
+        self.cfg = cfg
+        err = C.create_string_buffer(512)
+        self.h = self.lib.orc_create(C.byref(cfg), err, 512)
+        if not self.h:
+            raise ValueError(err.value.decode())
+
+    def close(self):
+        if self.h:
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def lon_halo_width(self):
+        return self.lib.orc_lon_halo_width(self.h)
+
+    def set_field(self, name, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(field_shape(self.cfg, name))
+        rc = self.lib.orc_set_field(self.h, name.encode(), _ptr(a))
+        if rc:
+            raise KeyError(name)
+
+    def get_field(self, name):
+        out = np.empty(field_shape(self.cfg, name))
+        rc = self.lib.orc_get_field(self.h, name.encode(), _ptr(out))
+        if rc:
+            raise KeyError(name)
+        return out
+
+    def set_tracer(self, l, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.cfg.nlev, self.cfg.nlat, self.cfg.nlon)
+        if self.lib.orc_set_tracer(self.h, l, _ptr(q)):
+            raise IndexError(l)
+
+    def get_tracer(self, l):
+        out = np.empty((self.cfg.nlev, self.cfg.nlat, self.cfg.nlon))
+        if self.lib.orc_get_tracer(self.h, l, _ptr(out)):
+            raise IndexError(l)
+        return out
+
+    def prepare(self):
+        err = C.create_string_buffer(512)
+        rc = self.lib.orc_prepare(self.h, err, 512)
+        if rc:
+            raise RuntimeError(f"oracle prepare failed ({rc}): {err.value.decode()}")
+
+    def step(self, n=1):
+        err = C.create_string_buffer(512)
+        rc = self.lib.orc_step(self.h, n, err, 512)
+        if rc:
+            raise RuntimeError(f"oracle step failed ({rc}): {err.value.decode()}")
+
+    def diagnose(self):
+        out = np.zeros(8)
+        self.lib.orc_diagnose(self.h, _ptr(out))
+        return dict(zip(("tm", "te", "te_ke", "te_ie", "te_pe", "tav", "tpe", "tpt"), out))
+
+    def metric(self, name, n):
+        out = np.zeros(n)
+        if self.lib.orc_metric(self.h, name.encode(), _ptr(out), n):
+            raise KeyError(name)
+        return out
+
+    def filter_taps(self, which, lat):
+        n = self.cfg.nlat - 1 if lat else self.cfg.nlat
+        out = np.zeros(n, dtype=np.int32)
+        self.lib.orc_filter_taps(self.h, which, lat, out.ctypes.data_as(C.POINTER(C.c_int)))
+        return out
