@@ -1,0 +1,372 @@
+"""Benchmark of the GMCORE dynamics step on GB300.
+
+Workload (the headline configuration): hydrostatic dry baroclinic core at
+0.5 degrees (720 x 360), 32 hybrid levels (wrf_l32), 4 FFSL tracers,
+dt = 180 s, seeded synthetic initial state (isothermal 300 K, 35 m/s
+balanced jet, 1 K temperature noise, Gaussian-blob tracers).  A step is one
+time_integrate (three forward-backward stages, divergence-free default
+options, tracer advection).
+
+Metric: simulated days per wall-clock day (SDPD) of the mixed FP32/FP64 form,
+with the FP64 form, their ratio and the surface-pressure difference reported
+beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas (one per GPU, launched by torchrun); the
+value is the whole-job total.  `--impl reference` times the FP64 CPU
+restatement of the reference on the host cores instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+RANK = int(os.environ.get("RANK", "0"))
+if WORLD > 1:
+    # one GPU per rank; the library uses the first visible device
+    _vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    _phys = _vis.split(",")[LOCAL_RANK] if _vis else str(LOCAL_RANK)
+    os.environ["CUDA_VISIBLE_DEVICES"] = _phys
+    PHYS_GPU = _phys
+else:
+    _vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    PHYS_GPU = _vis.split(",")[0] if _vis else "0"
+for _p in (ROOT, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+SEED = 20240601
+DT = 180.0
+NTRACER = 4
+METRIC = "sim days/wall-day at 0.5°L32: mixed vs FP64 GPU at stated err; adjoint/fwd cost"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload_config(precision):
+    from gmcore_gb300 import abi
+    # time_scheme wrfrk3 (the reference default) and a 400 m/s polar-filter
+    # design speed: an isothermal 300 K atmosphere carries Lamb waves at
+    # ~347 m/s, faster than the default 300 m/s the filter widths assume.
+    return abi.default_config(nlon=720, nlat=360, nlev=32, baroclinic=1, dt_dyn=DT,
+                              vert_coord_template=abi.VCOORD_WRF_L32, time_scheme=abi.TIME_WRFRK3,
+                              max_wave_speed=400.0, ntracer=NTRACER, precision=precision)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# Algorithmic (compulsory) bytes of one launch of each kernel group, in units
+# of N s (N = nlon nlat nlev cells, s = bytes of a bulk value), N 8 (FP64
+# level fields) and H 8 (FP64 surface fields).  Each entry counts the bulk
+# fields a kernel must read and write once.
+KERNEL_BYTES = {
+    "mass_flux": (4, 0, 1), "tangent_winds": (4, 0, 1), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 1),
+    "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (3, 1, 2), "ffsl_hflx_pt": (22, 0, 0),
+    "pt_tendency": (5, 1, 0), "momentum_tend": (9, 1, 1), "update_phs": (0, 0, 4), "update_pt": (3, 0, 2),
+    "column_backward": (1, 2, 2), "update_uv": (8, 2, 0), "div_damp": (7, 0, 0), "tracer_accum": (2, 1, 1),
+    "tracer_batch_cfl": (6, 0, 0), "tracer_batch_cflz": (1, 2, 0), "ffsl_hflx_tracer": (22, 0, 0),
+    "tracer_horizontal": (4, 0, 2), "tracer_vertical": (3, 1, 1), "tracer_lon_damp": (0.3, 0, 0),
+}
+
+
+def algorithmic_bytes(name, cfg, s):
+    n = cfg.nlon * cfg.nlat * cfg.nlev
+    h = cfg.nlon * cfg.nlat
+    a, b, c = KERNEL_BYTES.get(name, (0, 0, 0))
+    return a * n * s + b * n * 8 + c * h * 8
+
+
+def state_bytes(state):
+    return sum(a.nbytes for a in state.values())
+
+
+def run_ours(args):
+    import gmcore_gb300 as g
+    from gmcore_gb300 import abi
+
+    dist = None
+    if WORLD > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(0)
+        dist.init_process_group("nccl")
+
+    cfg = workload_config(abi.PREC_MIXED)
+    cfg64 = workload_config(abi.PREC_FP64)
+    st = g.make_ic(cfg, 2, SEED, 1.0)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident timing of the mixed form ----
+    model = g.Model(cfg)
+    model.set_state(st)
+    model.prepare()
+    model.step(args.warmup)
+    clocks = ClockSampler(PHYS_GPU)
+    barrier()
+    clocks.start()
+    model.step(args.steps)            # synchronous; CUDA events on the context stream
+    barrier()
+    clk = clocks.stop()
+    stats = model.stats()
+    dev_ms = max_over_ranks(stats["step_ms"])
+    ms_per_step = dev_ms / args.steps
+    sdpd_rank = DT * args.steps / (dev_ms / 1000.0)
+    value = sdpd_rank * WORLD
+    launches_per_step = stats["kernel_launches"] / args.steps
+
+    # ---- end to end through the C ABI with host buffers ----
+    host = {k: np.ascontiguousarray(v) for k, v in st.items()}
+    out = {k: np.empty_like(v) for k, v in host.items() if k != "q"}
+    qout = np.empty_like(host["q"])
+    e2e_steps = max(2, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for name in ("u_lon", "v_lat", "pt", "phs"):
+            model.set_field(name, host[name])
+        for l in range(NTRACER):
+            model.set_tracer(l, host["q"][l])
+        model.step(1)
+        for name in ("u_lon", "v_lat", "pt", "phs"):
+            out[name][...] = model.get_field(name)
+        for l in range(NTRACER):
+            qout[l] = model.get_tracer(l)
+        host["u_lon"], host["v_lat"], host["pt"], host["phs"] = out["u_lon"], out["v_lat"], out["pt"], out["phs"]
+        host["q"] = qout
+        out = {k: np.empty_like(v) for k, v in out.items()}
+        qout = np.empty_like(qout)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    h2d = sum(host[k].nbytes for k in ("u_lon", "v_lat", "pt", "phs", "q"))
+    e2e_value = DT * e2e_steps / e2e_s * WORLD
+
+    # ---- per-kernel device timing for the roofline ----
+    model.set_profiling(True)
+    model.step(3)
+    prof = model.kernel_profile()
+    model.set_profiling(False)
+    total = sum(ms for ms, _ in prof.values())
+    top = max(prof.items(), key=lambda kv: kv[1][0])
+    top_name, (top_ms, top_n) = top
+    per_launch_ms = top_ms / top_n
+    alg = algorithmic_bytes(top_name, cfg, 4)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (per_launch_ms / 1000.0) / 1e9
+    ps_mixed = model.get_field("phs")
+    model.close()
+
+    # ---- FP64 form on the same initial state ----
+    m64 = g.Model(cfg64)
+    m64.set_state(st)
+    m64.prepare()
+    m64.step(args.warmup)
+    barrier()
+    m64.step(args.steps)
+    barrier()
+    ms64 = max_over_ranks(m64.stats()["step_ms"]) / args.steps
+    ps64 = m64.get_field("phs")
+    m64.close()
+    ps_rms_hpa = float(np.sqrt(np.mean((ps_mixed - ps64) ** 2)) / 100.0)
+
+    cpu = None
+    if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, sample_steps=1)
+
+    if RANK == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "sim days/wall-day",
+            "n_gpus": WORLD,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_per_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 bulk + f64 (rings, column sweeps, integrals, filter weights)",
+            "data": "synthetic (seeded isothermal 300 K + balanced 35 m/s jet + 1 K noise, 4 Gaussian-blob tracers)",
+            "config": {"workload": "hydrostatic baroclinic 0.5deg 720x360 L32 (wrf_l32), 4 FFSL tracers, dt=180 s",
+                       "time_scheme": "wrfrk3", "max_wave_speed": 400.0, "precision": "mixed",
+                       "parallelism": f"replicas x{WORLD}" if WORLD > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (state ~1.5 GB)"},
+            "fp64": {"ms_per_step": ms64, "value": DT / (ms64 / 1000.0) * WORLD,
+                     "mixed_speedup": ms64 / ms_per_step, "ps_rms_diff_hpa_after_steps": ps_rms_hpa,
+                     "steps_compared": args.warmup + args.steps},
+            "e2e": {"value": e2e_value, "unit": "sim days/wall-day", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": h2d, "steps": e2e_steps,
+                    "path": "gmc_set_field/gmc_set_tracer + gmc_step(1) + gmc_get_field/gmc_get_tracer, host float64"},
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": alg, "avg_launch_ms": per_launch_ms,
+                         "share_of_step": top_ms / total if total else None},
+            "kernel_ms_per_step": {k: round(v[0] / 3.0, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+            "clocks": clk,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, sample_steps=1, warm=0):
+    """FP64 CPU restatement of the reference (the oracle, OpenMP build) on
+    the same workload, timed on the host cores."""
+    import gmcore_gb300 as g
+    from gmcore_gb300 import abi
+    import oracle as orc_mod
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cfg = workload_config(abi.PREC_FP64)
+    st = g.make_ic(cfg, 2, SEED, 1.0)
+    o = orc_mod.Oracle(cfg, variant="omp")
+    for name, a in st.items():
+        if name == "q":
+            for l in range(a.shape[0]):
+                o.set_tracer(l, a[l])
+        else:
+            o.set_field(name, a)
+    o.prepare()
+    if warm:
+        o.step(warm)
+    t0 = time.perf_counter()
+    o.step(sample_steps)
+    dt_s = time.perf_counter() - t0
+    o.close()
+    return {"value": DT * sample_steps / dt_s, "unit": "sim days/wall-day", "cores": int(os.environ["OMP_NUM_THREADS"]),
+            "kind": "port", "sample": f"{sample_steps} step(s) of the same 0.5deg L32 4-tracer workload after the run prologue",
+            "s_per_step": dt_s / sample_steps}
+
+
+def run_reference(args):
+    if RANK != 0:
+        return
+    cpu = cpu_baseline(args, sample_steps=args.steps, warm=args.warmup)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": cpu["value"],
+        "unit": "sim days/wall-day",
+        "n_gpus": WORLD,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": cpu["s_per_step"] * 1000.0,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded isothermal 300 K + balanced 35 m/s jet + 1 K noise, 4 Gaussian-blob tracers)",
+        "config": {"workload": "hydrostatic baroclinic 0.5deg 720x360 L32 (wrf_l32), 4 FFSL tracers, dt=180 s",
+                   "time_scheme": "wrfrk3", "max_wave_speed": 400.0, "precision": "fp64",
+                   "implementation": "FP64 C++ restatement of the reference (the reference's Fortran/MPI build "
+                                     "cannot be compiled here)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": "sim days/wall-day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if args.steps > 3:
+            log("reference arm: each step of the CPU restatement takes seconds; timing", args.steps, "steps")
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

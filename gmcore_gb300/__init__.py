@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .abi import (Config, Diag, View, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
+from .abi import (Config, Diag, View, Stats, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
                   TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, LIMITER_NONE,
                   LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
                   VCOORD_WRF_L64, PREC_FP64, PREC_MIXED)
@@ -27,6 +27,7 @@ EXPORTED = (
     "gmc_config_default", "gmc_create", "gmc_lon_halo_width", "gmc_set_field", "gmc_set_tracer",
     "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
+    "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile",
 )
 
 _lib = None
@@ -69,6 +70,9 @@ def load(build_if_missing=True):
     lib.gmc_mesh_metric.argtypes = [P(Config), C.c_char_p, P(C.c_double), C.c_size_t]
     lib.gmc_filter_taps.argtypes = [P(Config), C.c_int32, C.c_int32, P(C.c_int32), C.c_size_t]
     lib.gmc_make_ic.argtypes = [P(Config), C.c_int32, C.c_uint64, C.c_double] + [P(C.c_double)] * 6
+    lib.gmc_get_stats.argtypes = [C.c_void_p, P(Stats)]
+    lib.gmc_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
     _lib = lib
     return lib
 
@@ -226,6 +230,25 @@ class Model:
         d = Diag()
         self._check(self.lib.gmc_diagnose(self.h, member, C.byref(d)))
         return d.as_dict()
+
+    def stats(self):
+        """Device time (CUDA events on the context stream) and kernel count of
+        the last step() call."""
+        st = Stats()
+        self._check(self.lib.gmc_get_stats(self.h, C.byref(st)))
+        return {"step_ms": st.step_ms, "steps": st.steps, "kernel_launches": st.kernel_launches}
+
+    def set_profiling(self, on):
+        self._check(self.lib.gmc_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_profile(self):
+        out, i = {}, 0
+        name = C.create_string_buffer(64)
+        ms, n = C.c_double(), C.c_int64()
+        while self.lib.gmc_kernel_profile(self.h, i, name, 64, C.byref(ms), C.byref(n)) == 0:
+            out[name.value.decode()] = (ms.value, n.value)
+            i += 1
+        return out
 
     @property
     def time_step(self):

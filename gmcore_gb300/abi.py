@@ -68,6 +68,10 @@ class Diag(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class Stats(C.Structure):
+    _fields_ = [("step_ms", C.c_double), ("steps", C.c_int64), ("kernel_launches", C.c_int64)]
+
+
 class View(C.Structure):
     _fields_ = [("data", C.POINTER(C.c_double)), ("lb", C.c_int32 * 3), ("ub", C.c_int32 * 3)]
 

@@ -9,6 +9,8 @@
 // order.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.hpp"
 #include "stencil.cuh"
 
@@ -209,6 +211,216 @@ __global__ void k_pt_tendency(DGrid g, Slot<R> s, Work<R> w) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Tracer batch (adv_run, adv_mod.F90:152-312)
+// ---------------------------------------------------------------------------
+
+// adv_batch_accum_*: copy (mode 0), add (1) or average (2) a field.
+template <class T>
+__global__ void k_accum(T *dst, const T *src, size_t n, int mode, double divisor) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    T s = src ? src[t] : (T)0;
+    if (mode == 0) dst[t] = s;
+    else if (mode == 1) dst[t] = dst[t] + s;
+    else dst[t] = (T)((dst[t] + s) / (T)divisor);
+  }
+}
+
+// Half-level mass m_lev of calc_m (operators_mod.F90:505-525) folded into
+// the batch accumulator.
+__global__ void k_half_level_mass(DGrid g, const double *phs_f, double *m_lev, int mode, double divisor) {
+  const int j = blockIdx.y + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
+  if (i > nlon) return;
+  double ml[66];
+  if (phs_f) {
+    const double phs = phs_f[(size_t)(j - 1) * nlon + (i - 1)];
+    double plo = ph_lev(g, 1, phs), ph_prev = 0;
+    for (int k = 1; k <= nlev; ++k) {
+      double phi = ph_lev(g, k + 1, phs);
+      double ph = 0.5 * (plo + phi);
+      ml[k - 1] = k == 1 ? ph - plo : ph - ph_prev;
+      ph_prev = ph;
+      plo = phi;
+    }
+    ml[nlev] = plo - ph_prev;
+  } else {
+    for (int k = 0; k <= nlev; ++k) ml[k] = 0;
+  }
+  for (int k = 1; k <= nlev + 1; ++k) {
+    size_t o = ix3(nlat, nlon, i, j, k);
+    if (mode == 0) m_lev[o] = ml[k - 1];
+    else if (mode == 1) m_lev[o] = m_lev[o] + ml[k - 1];
+    else m_lev[o] = (m_lev[o] + ml[k - 1]) / divisor;
+  }
+}
+
+template <class R>
+__global__ void k_batch_cflz(DGrid g, const double *we_in, const double *ml_in, R *cflz, double dt) {
+  const int j = blockIdx.y + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
+  if (i > nlon) return;
+  double we[66], ml[66];
+  for (int k = 1; k <= nlev + 1; ++k) {
+    size_t o = ix3(nlat, nlon, i, j, k);
+    we[k - 1] = we_in[o];
+    ml[k - 1] = ml_in[o];
+  }
+  bool bad = false;
+  for (int k = 2; k <= nlev; ++k) {
+    double c = cflz_of(g, we, ml, k, dt, bad);
+    if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = (R)c;
+  }
+  if (bad) atomicOr(g.err, ERR_CFLZ);
+}
+
+// q_new = (old_m q_old - dt div(qmf)) / m, then the zonal negative fixer,
+// which walks the row in order and borrows from the neighbours; at the ends
+// it reads the longitude halo of q_new as the reference leaves it (the row's
+// values before this update, wrapped).
+template <class R>
+__global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *fx, const R *fy, const double *old_phs_f,
+                                    const double *phs_f, double dt_adv) {
+  extern __shared__ double sh[];
+  double *red = sh;
+  R *row = reinterpret_cast<R *>(sh + 32);
+  R *mrow = row + g.nlon + 2;
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  if (threadIdx.x == 0) {
+    row[0] = q_new[ix3(nlat, nlon, nlon, j, k)];
+    row[nlon + 1] = q_new[ix3(nlat, nlon, 1, j, k)];
+  }
+  __syncthreads();
+  double pole = 0;
+  const bool is_pole = j == 1 || j == nlat;
+  if (is_pole) {
+    const int jv = j == 1 ? 1 : nhalf;
+    double p = ring_sum(nlon, red, [&](int i) { return (double)fy[ix3(nhalf, nlon, i, jv, k)]; });
+    pole = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j) * dt_adv;
+  }
+  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  const R dta = (R)dt_adv;
+  bool neg = false;
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    const size_t o = ix3(nlat, nlon, i, j, k);
+    const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
+    R om = Mass<R>::layer(g, k, old_phs_f[c2]);
+    R m = Mass<R>::layer(g, k, phs_f[c2]);
+    R qn;
+    if (!is_pole) {
+      R a = (fx[o] - fx[ix3(nlat, nlon, wrap(i - 1, nlon), j, k)]) * lel;
+      R b = fy[ix3(nhalf, nlon, i, j, k)] * la0 - fy[ix3(nhalf, nlon, i, j - 1, k)] * la1;
+      qn = om * q_old[o] - (a + b) / ac * dta;
+    } else if (j == 1) {
+      qn = om * q_old[o] - (R)pole;
+    } else {
+      qn = om * q_old[o] + (R)pole;
+    }
+    qn = qn / m;
+    row[i] = qn;
+    mrow[i] = m;
+    neg |= qn < 0;
+  }
+  if (threadIdx.x == 0) {
+    mrow[0] = Mass<R>::layer(g, k, phs_f[(size_t)(j - 1) * nlon + (nlon - 1)]);
+    mrow[nlon + 1] = Mass<R>::layer(g, k, phs_f[(size_t)(j - 1) * nlon]);
+  }
+  if (__syncthreads_or(neg) && threadIdx.x == 0) {
+    for (int i = 1; i <= nlon; ++i) {
+      if (row[i] < 0) {
+        R qm0 = row[i] * mrow[i], qm1 = row[i - 1] * mrow[i - 1], qm2 = row[i + 1] * mrow[i + 1];
+        R qm0_half = (R)0.5 * qm0;
+        if (qm1 >= qm0_half && qm2 >= qm0_half) {
+          row[i - 1] = (qm1 - qm0_half) / mrow[i - 1];
+          row[i + 1] = (qm2 - qm0_half) / mrow[i + 1];
+        } else if (qm1 > qm0) {
+          row[i - 1] = (qm1 - qm0) / mrow[i - 1];
+        } else if (qm2 > qm0) {
+          row[i + 1] = (qm2 - qm0) / mrow[i + 1];
+        } else {
+          atomicOr(g.err, ERR_NEGTRACER);
+        }
+        row[i] = 0;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) q_new[ix3(nlat, nlon, i, j, k)] = row[i];
+}
+
+// Vertical FFSL of the tracer column with copied ghost levels, then the
+// vertical negative fixer (adv_mod.F90:259-297).
+template <class R>
+__global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const double *we, const double *phs_f, double dt_adv) {
+  const int j = blockIdx.y + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
+  if (i > nlon) return;
+  R col[70], mz[66], m[66];
+  for (int k = 1; k <= nlev; ++k) col[k + 1] = q[ix3(nlat, nlon, i, j, k)];
+  col[1] = col[0] = col[2];
+  col[nlev + 2] = col[nlev + 3] = col[nlev + 1];
+  const double phs = phs_f[(size_t)(j - 1) * nlon + (i - 1)];
+  for (int k = 1; k <= nlev; ++k) m[k - 1] = Mass<R>::layer(g, k, phs);
+  mz[0] = 0;
+  mz[nlev] = 0;
+  for (int k = 2; k <= nlev; ++k) {
+    size_t o = ix3(nlat, nlon, i, j, k);
+    mz[k - 1] = vflx_at<R>(g, col, k, cflz[o], (R)we[o]);
+  }
+  R *qc = col + 1;   // qc[k] = q(k)
+  const R dta = (R)dt_adv;
+  for (int k = 1; k <= nlev; ++k) qc[k] = qc[k] - ((mz[k] - mz[k - 1]) * dta) / m[k - 1];
+  for (int k = 1; k <= nlev; ++k) {
+    if (qc[k] < 0) {
+      R qm0 = qc[k] * m[k - 1];
+      R qm1 = k > 1 ? qc[k - 1] * m[k - 2] : (R)0;
+      R qm2 = k < nlev ? qc[k + 1] * m[k] : (R)0;
+      R qm0_half = (R)0.5 * qm0;
+      if (qm1 >= qm0_half && qm2 >= qm0_half) {
+        if (qm1 > 0) qc[k - 1] = (qm1 - qm0_half) / m[k - 2];
+        if (qm2 > 0) qc[k + 1] = (qm2 - qm0_half) / m[k];
+      } else if (qm1 > qm0) {
+        if (qm1 > 0) qc[k - 1] = (qm1 - qm0) / m[k - 2];
+      } else if (qm2 > qm0) {
+        if (qm2 > 0) qc[k + 1] = (qm2 - qm0) / m[k];
+      } else {
+        atomicOr(g.err, ERR_NEGTRACER);
+      }
+      qc[k] = 0;
+    }
+  }
+  for (int k = 1; k <= nlev; ++k) q[ix3(nlat, nlon, i, j, k)] = qc[k];
+}
+
+// Order-2 zonal smoother applied three times (lon_damp_1d, lon_damp_mod.F90:200-241).
+template <class R>
+__global__ void k_tracer_lon_damp(DGrid g, R *q) {
+  extern __shared__ double sh[];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1, nlon = g.nlon, nlat = g.nlat;
+  if (j == 1 || j == nlat) return;
+  const double wgt = g.lon_damp_full[j - 1];
+  if (wgt == 0) return;
+  R *f = reinterpret_cast<R *>(sh), *gw = f + nlon;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) f[i] = q[ix3(nlat, nlon, i + 1, j, k)];
+  const R w = (R)wgt, c = (R)0.25;
+  for (int pass = 0; pass < 3; ++pass) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      R fm = f[i == 0 ? nlon - 1 : i - 1], fc = f[i], fp = f[i == nlon - 1 ? 0 : i + 1];
+      gw[i] = w * (fc + c * (fm - (R)2 * fc + fp)) + ((R)1 - w) * fc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) f[i] = gw[i];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) q[ix3(nlat, nlon, i + 1, j, k)] = f[i];
+}
+
 }  // namespace
 
 template <class R>
@@ -233,5 +445,57 @@ template void launch_ffsl_hflx<float>(const DGrid &, const Launch &, const Batch
                                       float *, float *, float *, float *, float *, double);
 template void launch_pt_tendency<double>(const DGrid &, const Launch &, const Slot<double> &, const Work<double> &);
 template void launch_pt_tendency<float>(const DGrid &, const Launch &, const Slot<float> &, const Work<float> &);
+
+}  // namespace gmc
+
+namespace gmc {
+
+template <class T>
+void launch_accum(const Launch &L, T *dst, const T *src, size_t n, int mode, double divisor) {
+  int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  k_accum<T><<<blocks, 256, 0, L.stream>>>(dst, src, n, mode, divisor);
+}
+template void launch_accum<double>(const Launch &, double *, const double *, size_t, int, double);
+template void launch_accum<float>(const Launch &, float *, const float *, size_t, int, double);
+
+void launch_half_level_mass(const DGrid &g, const Launch &L, const double *phs_f, double *m_lev, int mode, double divisor) {
+  const int bt = 64;
+  k_half_level_mass<<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, phs_f, m_lev, mode, divisor);
+}
+
+template <class R>
+void launch_batch_cflz(const DGrid &g, const Launch &L, const double *we, const double *m_lev, R *cflz, double dt) {
+  const int bt = 64;
+  k_batch_cflz<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, we, m_lev, cflz, dt);
+}
+
+template <class R>
+void launch_tracer_horizontal(const DGrid &g, const Launch &L, const R *q_old, R *q_new, const R *fx, const R *fy,
+                              const double *old_phs_f, const double *phs_f, double dt_adv) {
+  size_t smem = 32 * sizeof(double) + 2 * (g.nlon + 2) * sizeof(R) + 16;
+  k_tracer_horizontal<R><<<dim3(g.nlat, g.nlev), L.threads, smem, L.stream>>>(g, q_old, q_new, fx, fy, old_phs_f, phs_f, dt_adv);
+}
+
+template <class R>
+void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const double *we, const double *phs_f,
+                            double dt_adv) {
+  const int bt = 64;
+  k_tracer_vertical<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, q, cflz, we, phs_f, dt_adv);
+}
+
+template <class R>
+void launch_tracer_lon_damp(const DGrid &g, const Launch &L, R *q) {
+  k_tracer_lon_damp<R><<<dim3(g.nlat, g.nlev), L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, q);
+}
+
+#define INST_TRACER(R)                                                                                              \
+  template void launch_batch_cflz<R>(const DGrid &, const Launch &, const double *, const double *, R *, double); \
+  template void launch_tracer_horizontal<R>(const DGrid &, const Launch &, const R *, R *, const R *, const R *,  \
+                                            const double *, const double *, double);                             \
+  template void launch_tracer_vertical<R>(const DGrid &, const Launch &, R *, const R *, const double *,           \
+                                          const double *, double);                                               \
+  template void launch_tracer_lon_damp<R>(const DGrid &, const Launch &, R *);
+INST_TRACER(double)
+INST_TRACER(float)
 
 }  // namespace gmc

@@ -55,6 +55,7 @@ struct DGrid {
   const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
   const double *lon_damp_full;                                     // [j-1]
+  const double *div_c_lon, *div_c_lat;                             // [(k-1)*n + j-1]
   FilterDev big, small1, small2;
   unsigned *err;                                                   // device error word
 };

@@ -284,47 +284,6 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
   }
 }
 
-// Vertical RK4 departure in eta and its Courant number
-// (adv_batch_accum_we_lev, adv_batch_mod.F90:525-628).  we and ml hold the
-// column's vertical mass flux and half-level mass, index [k-1].
-__device__ __forceinline__ double cflz_of(const DGrid &g, const double *we, const double *ml, int k, double dt_, bool &bad) {
-  const int nlev = g.nlev;
-  const double *HL = g.half_lev, *HD = g.half_dlev, *FD = g.full_dlev;   // [k-1]
-  auto locate = [&](double w, double z) {
-    int l;
-    if (w > 0) {
-      for (l = k; l <= nlev; ++l)
-        if (HL[l - 1] <= z && z <= HL[l]) break;
-      if (l == nlev + 1) { bad = true; l = nlev; }
-    } else {
-      for (l = k - 1; l >= 1; --l)
-        if (HL[l - 1] <= z && z <= HL[l]) break;
-      if (l == 0) { bad = true; l = 1; }
-    }
-    return l;
-  };
-  auto interp = [&](int l, double z) {
-    return ((HL[l] - z) * we[l - 1] / ml[l - 1] * HD[l - 1] + (z - HL[l - 1]) * we[l] / ml[l] * HD[l]) / FD[l - 1];
-  };
-  double z0 = HL[k - 1];
-  double w1 = we[k - 1] / ml[k - 1] * HD[k - 1];
-  double z1 = z0 + dt_ / 2 * w1;
-  double w2 = interp(locate(w1, z1), z1);
-  double z2 = z0 + dt_ / 2 * w2;
-  double w3 = interp(locate(w2, z2), z2);
-  double z3 = z0 + dt_ * w3;
-  double w4 = interp(locate(w3, z3), z3);
-  double deta = (w1 + 2 * w2 + 2 * w3 + w4) / 6 * dt_;
-  int ks, ke, s;
-  if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
-  deta = fabs(deta);
-  for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s) {
-    deta = deta - FD[l - 1];
-    if (deta < 0) return s * ((1 + deta / FD[l - 1]) + abs(l - ks));
-  }
-  return NAN;   // departure left the column: the reference keeps the previous value
-}
-
 // calc_grad_mf + calc_dphsdt + calc_we_lev + the mass batch's accum_we_lev
 // for one column (operators_mod.F90:939-1006, 1120-1143, 192-226).
 template <class R>
@@ -861,5 +820,64 @@ void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Wo
 
 INSTANTIATE(double)
 INSTANTIATE(float)
+
+}  // namespace gmc
+
+namespace gmc {
+namespace {
+
+// calc_div, order-2 branch (operators_mod.F90:354-412), on the filtered wind.
+template <class R>
+__global__ void k_div(DGrid g, Slot<R> n, R *div) {
+  __shared__ double red[32];
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  if (j == 1 || j == nlat) {
+    const int jv = j == 1 ? 1 : nhalf;
+    const double sgn = j == 1 ? 1.0 : -1.0;
+    double p = ring_sum(nlon, red, [&](int i) { return sgn * (double)n.v_f[ix3(nhalf, nlon, i, jv, k)]; });
+    p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) div[ix3(nlat, nlon, i, j, k)] = (R)p;
+    return;
+  }
+  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    R ue = n.u_f[ix3(nlat, nlon, i, j, k)], uw = n.u_f[ix3(nlat, nlon, wrap(i - 1, nlon), j, k)];
+    R vn = n.v_f[ix3(nhalf, nlon, i, j, k)], vs = n.v_f[ix3(nhalf, nlon, i, j - 1, k)];
+    div[ix3(nlat, nlon, i, j, k)] = ((ue * lel - uw * lel) + (vn * la0 - vs * la1)) / ac;
+  }
+}
+
+template <class R>
+__global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
+  const int k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  if ((int)blockIdx.x < nlat) {
+    const int j = blockIdx.x + 1;
+    if (j == 1 || j == nlat) return;
+    const R c = (R)g.div_c_lon[(size_t)(k - 1) * nlat + (j - 1)], de = (R)ROW(g.de_lon, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      size_t o = ix3(nlat, nlon, i, j, k);
+      n.u_lon[o] = n.u_lon[o] + c * (div[ix3(nlat, nlon, wrap(i + 1, nlon), j, k)] - div[o]) / de;
+    }
+    return;
+  }
+  const int j = blockIdx.x - nlat + 1;
+  const R c = (R)g.div_c_lat[(size_t)(k - 1) * nhalf + (j - 1)], de = (R)ROW(g.de_lat, j);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    size_t o = ix3(nhalf, nlon, i, j, k);
+    n.v_lat[o] = n.v_lat[o] + c * (div[ix3(nlat, nlon, i, j + 1, k)] - div[ix3(nlat, nlon, i, j, k)]) / de;
+  }
+}
+
+}  // namespace
+
+template <class R>
+void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div) {
+  k_div<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
+  k_div_damp<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
+}
+template void launch_div_damp<double>(const DGrid &, const Launch &, const Slot<double> &, double *);
+template void launch_div_damp<float>(const DGrid &, const Launch &, const Slot<float> &, float *);
 
 }  // namespace gmc

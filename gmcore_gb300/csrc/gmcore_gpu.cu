@@ -91,7 +91,17 @@ struct EngineBase {
   virtual void step(int nsteps) = 0;
   virtual void diagnose(int member, gmc_diag *out) = 0;
   virtual unsigned read_error() = 0;
+  virtual void set_tracer(int member, int l, const double *src) = 0;
+  virtual void get_tracer(int member, int l, double *dst) = 0;
   long time_step = 0;
+  // timing and profiling
+  double last_step_ms = 0;
+  long last_steps = 0, last_launches = 0, launches = 0;
+  bool prof = false;
+  struct Prof { std::string name; double ms = 0; long count = 0; };
+  std::vector<Prof> prof_table;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  std::vector<cudaEvent_t> event_pool;
 };
 
 template <class R>
@@ -112,6 +122,14 @@ struct Engine : EngineBase {
   double *pinned = nullptr;
   size_t pinned_n = 0;
   R *staging = nullptr;
+  // tracer batch (one per member) and its host-side cadence state
+  int ntr = 0;
+  std::vector<TracerBatch<R>> tb;     // [member]
+  std::vector<R *> q;                 // [(member * 2 + slot) * ntr + l]
+  int q_old = 0;
+  int nstep_adv = 1, uv_step = 0, mf_step = 0, we_step = 0;
+  double alert_last = 0, curr_time = 0;
+  bool alert_ring = false;
 
   size_t full3() const { return (size_t)grid.nlev * grid.nlat * grid.nlon; }
   size_t half3() const { return (size_t)grid.nlev * grid.nhalf * grid.nlon; }
@@ -186,6 +204,22 @@ struct Engine : EngineBase {
     carve(a, work[m], baroclinic);
     work[m].gzs = z;
     gzs[m] = z;
+    if (ntr > 0) {
+      TracerBatch<R> &b = tb[m];
+      b.u = a.template take<R>(full3());
+      b.v = a.template take<R>(half3());
+      b.mfx = a.template take<R>(full3());
+      b.mfy = a.template take<R>(half3());
+      b.we = a.template take<double>(lev3());
+      b.m_lev = a.template take<double>(lev3());
+      b.cflx = a.template take<R>(full3());
+      b.cfly = a.template take<R>(half3());
+      b.divx = a.template take<R>(full3());
+      b.divy = a.template take<R>(full3());
+      b.cflz = a.template take<R>(lev3());
+      b.old_phs_f = a.template take<double>(two_d());
+      for (int t = 0; t < 2 * ntr; ++t) q[(size_t)m * 2 * ntr + t] = a.template take<R>(full3());
+    }
   }
 
   explicit Engine(const gmc_config &cfg) {
@@ -193,6 +227,10 @@ struct Engine : EngineBase {
     if (!e.empty()) throw ApiError{GMC_EINVAL, e};
     nm = cfg.n_members;
     const bool bc = cfg.baroclinic != 0;
+    ntr = bc ? cfg.ntracer : 0;
+    tb.resize(nm);
+    q.assign((size_t)nm * 2 * std::max(ntr, 1), nullptr);
+    nstep_adv = std::max(1, (int)(cfg.dt_adv / cfg.dt_dyn));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     L.stream = stream;
     L.threads = grid.nlon >= 512 ? 256 : 128;
@@ -224,6 +262,10 @@ struct Engine : EngineBase {
 
   ~Engine() override {
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+    for (auto &p : prof_pending) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
+    if (ev_a) cudaEventDestroy(ev_a);
+    if (ev_b) cudaEventDestroy(ev_b);
     arena.release();
     tables.release();
     if (pinned) cudaFreeHost(pinned);
@@ -257,6 +299,7 @@ struct Engine : EngineBase {
     row(g.full_cos_lat, &dg.full_cos_lat); row(g.half_lat, &dg.half_lat);
     vec(g.hyai, &dg.hyai); vec(g.hybi, &dg.hybi); vec(g.half_lev, &dg.half_lev); vec(g.half_dlev, &dg.half_dlev);
     vec(g.full_dlev, &dg.full_dlev); vec(g.lon_damp_wgt_full, &dg.lon_damp_full);
+    vec(g.div_c_lon, &dg.div_c_lon); vec(g.div_c_lat, &dg.div_c_lat);
     // FP32 layer-mass coefficients
     std::vector<float> dA(g.nlev + 1, 0.f), dB(g.nlev + 1, 0.f);
     for (int k = 0; k < g.nlev && g.cfg.baroclinic; ++k) {
@@ -357,7 +400,6 @@ struct Engine : EngineBase {
       CK(cudaMemcpyAsync(pr, host, n * sizeof(R), cudaMemcpyHostToDevice, stream));
     }
     CK(cudaStreamSynchronize(stream));
-    prepared = false;
   }
 
   void get_field(int m, const std::string &name, double *dst) override {
@@ -377,14 +419,131 @@ struct Engine : EngineBase {
     }
   }
 
+  void set_tracer(int m, int l, const double *src) override {
+    if (l < 0 || l >= ntr) throw ApiError{GMC_EINVAL, "tracer index out of range"};
+    R *host = reinterpret_cast<R *>(pinned);
+    const size_t n = full3();
+    for (size_t t = 0; t < n; ++t) host[t] = (R)src[t];
+    // both time levels start from the initial mixing ratio
+    for (int sl = 0; sl < 2; ++sl)
+      CK(cudaMemcpyAsync(q[((size_t)m * 2 + sl) * ntr + l], host, n * sizeof(R), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  void get_tracer(int m, int l, double *dst) override {
+    if (l < 0 || l >= ntr) throw ApiError{GMC_EINVAL, "tracer index out of range"};
+    R *host = reinterpret_cast<R *>(pinned);
+    const size_t n = full3();
+    CK(cudaMemcpyAsync(host, q[((size_t)m * 2 + q_old) * ntr + l], n * sizeof(R), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (size_t t = 0; t < n; ++t) dst[t] = (double)host[t];
+  }
+
+  // adv_accum_wind for the static tracer batch (adv_mod.F90:420-455 with
+  // adv_batch_accum_uv_cell / _mf_cell / _we_lev, adv_batch_mod.F90:218-632):
+  // the first call of a cycle copies, the next nstep-1 add, the last averages
+  // over nstep+1 samples and only then refreshes the Courant numbers.  At the
+  // run prologue the mass fluxes and half-level masses are still zero.
+  void accum_wind(int m, const Slot<R> &s, bool prologue) {
+    TracerBatch<R> &b = tb[m];
+    const double dt_adv = grid.cfg.dt_adv;
+    auto cycle = [&](int &step, int &mode) {
+      if (step == 0) { mode = 0; step = step + 1; }
+      else if (step == nstep_adv) { mode = 2; step = 0; }
+      else { mode = 1; step = step + 1; }
+    };
+    const double div = nstep_adv + 1;
+    int mode;
+    cycle(uv_step, mode);
+    K("tracer_accum", 2, [&] {
+      launch_accum<R>(L, b.u, s.u_f, full3(), mode, div);
+      launch_accum<R>(L, b.v, s.v_f, half3(), mode, div);
+    });
+    if (uv_step == 0) K("tracer_batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, L, b.u, b.v, b.cflx, b.cfly, b.divx, b.divy, dt_adv); });
+    cycle(mf_step, mode);
+    K("tracer_accum", 2, [&] {
+      launch_accum<R>(L, b.mfx, prologue ? nullptr : s.mfx_lon, full3(), mode, div);
+      launch_accum<R>(L, b.mfy, prologue ? nullptr : s.mfy_lat, half3(), mode, div);
+    });
+    cycle(we_step, mode);
+    K("tracer_accum", 2, [&] {
+      launch_accum<double>(L, b.we, prologue ? nullptr : s.we_lev, lev3(), mode, div);
+      launch_half_level_mass(dg, L, prologue ? nullptr : s.phs_f, b.m_lev, mode, div);
+    });
+    if (we_step == 0) K("tracer_batch_cflz", 1, [&] { launch_batch_cflz<R>(dg, L, b.we, b.m_lev, b.cflz, dt_adv); });
+  }
+
+  // adv_run (adv_mod.F90:152-312) after the dynamics of a step.
+  void adv_run(int m, const Slot<R> &n, bool advect) {
+    TracerBatch<R> &b = tb[m];
+    Work<R> &w = work[m];
+    const double dt_adv = grid.cfg.dt_adv;
+    accum_wind(m, n, false);
+    if (advect) {
+      BatchView<R> bv{};
+      bv.u = b.u; bv.v = b.v; bv.mfx = b.mfx; bv.mfy = b.mfy;
+      bv.cflx = b.cflx; bv.cfly = b.cfly; bv.divx = b.divx; bv.divy = b.divy; bv.cflz = b.cflz;
+      for (int l = 0; l < ntr; ++l) {
+        R *qo = q[((size_t)m * 2 + q_old) * ntr + l], *qn = q[((size_t)m * 2 + (1 - q_old)) * ntr + l];
+        K("ffsl_hflx_tracer", 3, [&] { launch_ffsl_hflx<R>(dg, L, bv, qo, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt_adv); });
+        K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, L, qo, qn, w.ptf_lon, w.ptf_lat, b.old_phs_f, n.phs_f, dt_adv); });
+        K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, L, qn, b.cflz, b.we, n.phs_f, dt_adv); });
+        K("tracer_lon_damp", 1, [&] { launch_tracer_lon_damp<R>(dg, L, qn); });
+      }
+    }
+    // copy_old_m
+    CK(cudaMemcpyAsync(b.old_phs_f, n.phs_f, two_d() * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  }
+
+  cudaEvent_t take_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    return e;
+  }
+  int prof_index(const char *name) {
+    for (size_t t = 0; t < prof_table.size(); ++t)
+      if (prof_table[t].name == name) return (int)t;
+    prof_table.push_back(Prof{name, 0, 0});
+    return (int)prof_table.size() - 1;
+  }
+  // Launch group `name` of nk kernels; bracketed by events when profiling.
+  template <class F>
+  void K(const char *name, int nk, F &&f) {
+    launches += nk;
+    if (!prof) {
+      f();
+      return;
+    }
+    cudaEvent_t a = take_event(), b = take_event();
+    CK(cudaEventRecord(a, stream));
+    f();
+    CK(cudaEventRecord(b, stream));
+    prof_pending.push_back({prof_index(name), {a, b}});
+  }
+  void prof_collect() {
+    for (auto &p : prof_pending) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+      prof_table[p.first].ms += ms;
+      prof_table[p.first].count += 1;
+      event_pool.push_back(p.second.first);
+      event_pool.push_back(p.second.second);
+    }
+    prof_pending.clear();
+  }
+
   // operators_prepare forward list (operators_mod.F90:117-122)
   void forward_prepare(int m, const Slot<R> &s) {
     Work<R> &w = work[m];
-    launch_mass_flux<R>(dg, L, s);
-    launch_tangent_winds<R>(dg, L, s, w);
-    launch_kinetic_energy<R>(dg, L, s, w);
-    launch_pv<R>(dg, L, s, w);
-    launch_pv_edges<R>(dg, L, s, w);
+    K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
+    K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
+    K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
+    K("pv", 1, [&] { launch_pv<R>(dg, L, s, w); });
+    K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w); });
   }
 
   // space_operators forward pass (gmcore_mod.F90:467-528)
@@ -392,17 +551,17 @@ struct Engine : EngineBase {
     Work<R> &w = work[m];
     forward_prepare(m, s);
     if (grid.cfg.baroclinic) {
-      launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt);
-      launch_column_mass<R>(dg, L, s, w, dt);
+      K("batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt); });
+      K("column_mass", 1, [&] { launch_column_mass<R>(dg, L, s, w, dt); });
       BatchView<R> b{};
       b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
       b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
-      launch_ffsl_hflx<R>(dg, L, b, s.pt, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt);
-      launch_pt_tendency<R>(dg, L, s, w);
+      K("ffsl_hflx_pt", 3, [&] { launch_ffsl_hflx<R>(dg, L, b, s.pt, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt); });
+      K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, L, s, w); });
     } else {
-      launch_swm_dgz<R>(dg, L, s, w);
+      K("swm_dgz", 1, [&] { launch_swm_dgz<R>(dg, L, s, w); });
     }
-    launch_momentum_tend<R>(dg, L, s, w);
+    K("momentum_tend", 1, [&] { launch_momentum_tend<R>(dg, L, s, w); });
   }
 
   // step_forward_backward (time_schemes_mod.F90:102-118)
@@ -411,19 +570,31 @@ struct Engine : EngineBase {
     Work<R> &w = work[m];
     forward(m, S, dt);
     if (grid.cfg.baroclinic) {
-      launch_update_phs<R>(dg, L, O, N, w, dt);
-      launch_update_pt<R>(dg, L, O, N, w, dt);
-      launch_column_backward<R>(dg, L, N, w);
+      K("update_phs", 1, [&] { launch_update_phs<R>(dg, L, O, N, w, dt); });
+      K("update_pt", 1, [&] { launch_update_pt<R>(dg, L, O, N, w, dt); });
+      K("column_backward", 1, [&] { launch_column_backward<R>(dg, L, N, w); });
     } else {
-      launch_update_gz<R>(dg, L, O, N, w, dt);
+      K("update_gz", 1, [&] { launch_update_gz<R>(dg, L, O, N, w, dt); });
     }
-    launch_update_uv<R>(dg, L, O, N, w, dt);
+    K("update_uv", 1, [&] { launch_update_uv<R>(dg, L, O, N, w, dt); });
   }
 
   void prepare() override {
+    uv_step = mf_step = we_step = 0;
+    alert_last = -grid.cfg.dt_adv;
+    curr_time = 0;
+    alert_ring = false;
     for (int m = 0; m < nm; ++m) {
       const Slot<R> &s = slots[m * 3 + old_i];
       launch_filter_prologue<R>(dg, L, s);
+      if (ntr > 0) {
+        // the prologue's copy_old_m sees the layer mass before operators_prepare
+        CK(cudaMemsetAsync(tb[m].old_phs_f, 0, two_d() * sizeof(double), stream));
+        int save_uv = uv_step, save_mf = mf_step, save_we = we_step;
+        if (m > 0) { uv_step = save_uv; }
+        accum_wind(m, s, true);
+        if (m + 1 < nm) { uv_step = save_uv; mf_step = save_mf; we_step = save_we; }
+      }
       forward_prepare(m, s);
     }
     CK(cudaGetLastError());
@@ -432,11 +603,22 @@ struct Engine : EngineBase {
     time_step = 0;
   }
 
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;
   void step(int nsteps) override {
     if (!prepared) throw ApiError{GMC_ESTATE, "gmc_prepare must be called after setting the state"};
     const double dt = grid.cfg.dt_dyn;
+    if (!ev_a) {
+      CK(cudaEventCreate(&ev_a));
+      CK(cudaEventCreate(&ev_b));
+    }
+    const long launches0 = launches;
+    CK(cudaEventRecord(ev_a, stream));
     for (int it = 0; it < nsteps; ++it) {
       const int o = old_i, n = new_i, t3 = 3 - o - n;
+      // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
+      const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
+      if (ring) alert_ring = true;
+      const int su = uv_step, sm = mf_step, sw = we_step;
       for (int m = 0; m < nm; ++m) {
         switch (grid.cfg.time_scheme) {
           case GMC_TIME_EULER:
@@ -453,12 +635,28 @@ struct Engine : EngineBase {
             stage(m, o, t3, n, dt);
             break;
         }
+        const Slot<R> &N = slots[m * 3 + n];
+        if (grid.cfg.use_div_damp) K("div_damp", 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke); });
+        if (ntr > 0) {
+          uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
+          adv_run(m, N, ring && time_step > 0);
+        }
       }
+      if (ntr > 0 && ring && time_step > 0) q_old = 1 - q_old;
+      if (alert_ring) { alert_last = curr_time; alert_ring = false; }
+      curr_time += dt;
       std::swap(old_i, new_i);
       ++time_step;
     }
+    CK(cudaEventRecord(ev_b, stream));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ev_a, ev_b));
+    last_step_ms = ms;
+    last_steps = nsteps;
+    last_launches = launches - launches0;
+    if (prof) prof_collect();
   }
 
   void diagnose(int m, gmc_diag *out) override {
@@ -618,7 +816,6 @@ int gmc_create(const gmc_config *cfg, gmc_ctx **out) {
   int rc = guarded(ctx, [&]() {
     std::string e = validate_config(ctx->cfg);
     if (!e.empty()) throw ApiError{GMC_EINVAL, e};
-    if (ctx->cfg.ntracer > 0) throw ApiError{GMC_EINVAL, "tracer batches are not available in this build"};
     if (ctx->cfg.precision == GMC_PREC_FP64)
       ctx->eng.reset(new Engine<double>(ctx->cfg));
     else
@@ -660,15 +857,31 @@ int gmc_set_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view
 }
 
 int gmc_set_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v) {
-  (void)member; (void)tracer; (void)v;
   if (!ctx) return GMC_EINVAL;
-  return fail(ctx, GMC_EINVAL, "this context has no tracers");
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  if (tracer < 0 || tracer >= ctx->cfg.ntracer) return fail(ctx, GMC_EINVAL, "tracer index out of range");
+  return guarded(ctx, [&]() {
+    std::string err;
+    std::vector<double> buf;
+    if (!unpack_view(v, ctx->cfg.nlon, ctx->cfg.nlat, ctx->cfg.nlev, buf, err)) throw ApiError{GMC_EINVAL, err};
+    ctx->eng->set_tracer(member, tracer, buf.data());
+    return GMC_OK;
+  });
 }
 
 int gmc_get_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v) {
-  (void)member; (void)tracer; (void)v;
   if (!ctx) return GMC_EINVAL;
-  return fail(ctx, GMC_EINVAL, "this context has no tracers");
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  if (tracer < 0 || tracer >= ctx->cfg.ntracer) return fail(ctx, GMC_EINVAL, "tracer index out of range");
+  return guarded(ctx, [&]() {
+    std::string err;
+    std::vector<double> buf((size_t)ctx->cfg.nlon * ctx->cfg.nlat * ctx->cfg.nlev);
+    ctx->eng->get_tracer(member, tracer, buf.data());
+    if (!pack_view(v, ctx->cfg.nlon, ctx->cfg.nlat, ctx->cfg.nlev, buf, err)) throw ApiError{GMC_EINVAL, err};
+    return GMC_OK;
+  });
 }
 
 int gmc_prepare(gmc_ctx *ctx) {
@@ -719,6 +932,31 @@ int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out) {
 int gmc_time_step(const gmc_ctx *ctx, int64_t *out) {
   if (!ctx || !out || !ctx->eng) return GMC_EINVAL;
   *out = ctx->eng->time_step;
+  return GMC_OK;
+}
+
+int gmc_get_stats(const gmc_ctx *ctx, gmc_stats *out) {
+  if (!ctx || !out || !ctx->eng) return GMC_EINVAL;
+  out->step_ms = ctx->eng->last_step_ms;
+  out->steps = ctx->eng->last_steps;
+  out->kernel_launches = ctx->eng->last_launches;
+  return GMC_OK;
+}
+
+int gmc_set_profiling(gmc_ctx *ctx, int32_t on) {
+  if (!ctx || !ctx->eng) return GMC_EINVAL;
+  ctx->eng->prof = on != 0;
+  if (on) ctx->eng->prof_table.clear();
+  return GMC_OK;
+}
+
+int gmc_kernel_profile(const gmc_ctx *ctx, int32_t index, char *name, size_t name_len, double *total_ms,
+                       int64_t *launches) {
+  if (!ctx || !ctx->eng || index < 0 || (size_t)index >= ctx->eng->prof_table.size()) return GMC_EINVAL;
+  const EngineBase::Prof &p = ctx->eng->prof_table[index];
+  if (name && name_len) snprintf(name, name_len, "%s", p.name.c_str());
+  if (total_ms) *total_ms = p.ms;
+  if (launches) *launches = p.count;
   return GMC_OK;
 }
 

@@ -479,7 +479,11 @@ std::string Grid::build(const gmc_config &c) {
       }
     }
     auto shrink = [](int &n, double w) {
-      n = (int)(w * n);   // Fortran real-to-integer assignment truncates
+      // Fortran real-to-integer assignment truncates.  A non-finite factor
+      // (lat0 = 80 degrees makes exp_two_values divide by zero) leaves the
+      // row unfiltered instead of producing a garbage tap count.
+      double x = w * n;
+      n = std::isfinite(x) && x < 1e6 ? (int)x : 1;
       if (n % 2 == 0) n = n + 1;
     };
     for (int j = 2; j <= nlat - 1; ++j) {
@@ -551,13 +555,13 @@ std::string Grid::build(const gmc_config &c) {
     for (int j = 2; j <= nlat - 1; ++j) {
       double lat = std::fabs(full_lat_deg[j]);
       double w = std::exp((lat0 - lat) * (lat0 - lat) * std::log(1.0e-3) / ((lat0 - lat_cut) * (lat0 - lat_cut)));
-      lon_damp_wgt_full[j - 1] = w < 1.0e-6 ? 0.0 : w;
+      lon_damp_wgt_full[j - 1] = (w < 1.0e-6 || !std::isfinite(w)) ? 0.0 : w;
     }
     lat0 = -half_lat_deg[1];
     for (int j = 1; j <= nhalf; ++j) {
       double lat = std::fabs(half_lat_deg[j]);
       double w = std::exp((lat0 - lat) * (lat0 - lat) * std::log(1.0e-3) / ((lat0 - lat_cut) * (lat0 - lat_cut)));
-      lon_damp_wgt_half[j - 1] = w < 1.0e-6 ? 0.0 : w;
+      lon_damp_wgt_half[j - 1] = (w < 1.0e-6 || !std::isfinite(w)) ? 0.0 : w;
     }
   }
   return "";

@@ -69,6 +69,10 @@ template <class R> void launch_update_uv(const DGrid &g, const Launch &L, const 
 template <class R> void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s);
 template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out);
 
+// Divergence damping, order 2 (div_damp_run, div_damp_mod.F90:89-118);
+// div is a scratch cell field.
+template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div);
+
 // ---- advection (adv.cu) ---------------------------------------------------
 // Horizontal FFSL flux of q (ffsl_calc_tracer_hflx_cell): inner advective
 // operators, intermediate qx/qy, outer flux-form operators into (fx, fy).
@@ -76,5 +80,28 @@ template <class R> void launch_ffsl_hflx(const DGrid &g, const Launch &L, const 
 // Potential-temperature tendency: flux divergence of (ptf_lon, ptf_lat) with
 // pole rings plus the vertical FFSL flux with ghost levels (calc_grad_ptf).
 template <class R> void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w);
+
+// Tracer batch (adv_run, adv_mod.F90:152-312).
+template <class R>
+struct TracerBatch {
+  R *u, *v, *mfx, *mfy;            // accumulated winds and mass fluxes
+  double *we, *m_lev;              // accumulated vertical mass flux and half-level mass
+  R *cflx, *cfly, *divx, *divy, *cflz;
+  double *old_phs_f;               // surface pressure whose layer masses are old_m
+};
+// Accumulation of one field: mode 0 copy, 1 add, 2 average with divisor.
+template <class T> void launch_accum(const Launch &L, T *dst, const T *src, size_t n, int mode, double divisor);
+// Half-level mass of a slot (calc_m, operators_mod.F90:505-525) into a
+// level field, or zero it when src_phs_f is null.
+void launch_half_level_mass(const DGrid &g, const Launch &L, const double *phs_f, double *m_lev, int mode, double divisor);
+// Vertical Courant numbers of a batch (adv_batch_accum_we_lev RK4 part).
+template <class R> void launch_batch_cflz(const DGrid &g, const Launch &L, const double *we, const double *m_lev, R *cflz, double dt);
+// Horizontal tracer update with pole rings, division by the new mass and the
+// zonal negative fixer (adv_mod.F90:183-258).
+template <class R> void launch_tracer_horizontal(const DGrid &g, const Launch &L, const R *q_old, R *q_new, const R *fx, const R *fy, const double *old_phs_f, const double *phs_f, double dt_adv);
+// Vertical FFSL update with the vertical fixer (adv_mod.F90:259-297).
+template <class R> void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const double *we, const double *phs_f, double dt_adv);
+// Three passes of the order-2 zonal smoother (lon_damp_on_cell, adv_mod.F90:298-302).
+template <class R> void launch_tracer_lon_damp(const DGrid &g, const Launch &L, R *q);
 
 }  // namespace gmc

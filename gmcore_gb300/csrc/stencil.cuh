@@ -111,4 +111,45 @@ __device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, in
   return true;
 }
 
+// Vertical RK4 departure in eta and its Courant number
+// (adv_batch_accum_we_lev, adv_batch_mod.F90:525-628).  we and ml hold the
+// column's vertical mass flux and half-level mass, index [k-1].
+__device__ __forceinline__ double cflz_of(const DGrid &g, const double *we, const double *ml, int k, double dt_, bool &bad) {
+  const int nlev = g.nlev;
+  const double *HL = g.half_lev, *HD = g.half_dlev, *FD = g.full_dlev;   // [k-1]
+  auto locate = [&](double w, double z) {
+    int l;
+    if (w > 0) {
+      for (l = k; l <= nlev; ++l)
+        if (HL[l - 1] <= z && z <= HL[l]) break;
+      if (l == nlev + 1) { bad = true; l = nlev; }
+    } else {
+      for (l = k - 1; l >= 1; --l)
+        if (HL[l - 1] <= z && z <= HL[l]) break;
+      if (l == 0) { bad = true; l = 1; }
+    }
+    return l;
+  };
+  auto interp = [&](int l, double z) {
+    return ((HL[l] - z) * we[l - 1] / ml[l - 1] * HD[l - 1] + (z - HL[l - 1]) * we[l] / ml[l] * HD[l]) / FD[l - 1];
+  };
+  double z0 = HL[k - 1];
+  double w1 = we[k - 1] / ml[k - 1] * HD[k - 1];
+  double z1 = z0 + dt_ / 2 * w1;
+  double w2 = interp(locate(w1, z1), z1);
+  double z2 = z0 + dt_ / 2 * w2;
+  double w3 = interp(locate(w2, z2), z2);
+  double z3 = z0 + dt_ * w3;
+  double w4 = interp(locate(w3, z3), z3);
+  double deta = (w1 + 2 * w2 + 2 * w3 + w4) / 6 * dt_;
+  int ks, ke, s;
+  if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
+  deta = fabs(deta);
+  for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s) {
+    deta = deta - FD[l - 1];
+    if (deta < 0) return s * ((1 + deta / FD[l - 1]) + abs(l - ks));
+  }
+  return NAN;   // departure left the column: the reference keeps the previous value
+}
+
 }  // namespace gmc

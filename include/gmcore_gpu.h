@@ -129,7 +129,11 @@ int gmc_create(const gmc_config *cfg, gmc_ctx **out);
  * (process_mod.F90:208-213): max(namelist width, (big-filter taps - 1)/2). */
 int gmc_lon_halo_width(const gmc_ctx *ctx, int32_t *out);
 
-/* Set one prognostic field of one member, interior points only.
+/* Set one prognostic field of one member, interior points only.  Before
+ * gmc_prepare this defines the initial state; afterwards it overwrites the
+ * current state in place (e.g. a host that keeps its Fortran arrays and
+ * hands them to every step), keeping the filtered copies and the tracer
+ * batch of the previous step as the reference's state(old) would.
  * Names: "u_lon" (i=1..nlon half lon, j=1..nlat, k=1..nlev),
  *        "v_lat" (i=1..nlon, j=1..nlat-1, k=1..nlev),
  *        "pt"    (baroclinic) or "gz" (shallow water), full cells,
@@ -160,6 +164,24 @@ int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out);
 
 /* Number of steps taken since gmc_prepare. */
 int gmc_time_step(const gmc_ctx *ctx, int64_t *out);
+
+/* Timing of the last gmc_step call: device time between CUDA events
+ * recorded on the context's stream around the whole call, and the number
+ * of kernels it launched. */
+typedef struct gmc_stats {
+  double step_ms;           /* device time of the last gmc_step, all steps  */
+  int64_t steps;            /* steps in that call                            */
+  int64_t kernel_launches;  /* kernels launched by that call                 */
+} gmc_stats;
+int gmc_get_stats(const gmc_ctx *ctx, gmc_stats *out);
+
+/* Per-kernel device timing: when enabled, every kernel launch is bracketed
+ * by CUDA events on the context stream and its duration accumulated under
+ * the kernel's name.  gmc_kernel_profile returns entry `index` (GMC_EINVAL
+ * past the last one). */
+int gmc_set_profiling(gmc_ctx *ctx, int32_t on);
+int gmc_kernel_profile(const gmc_ctx *ctx, int32_t index, char *name, size_t name_len, double *total_ms,
+                       int64_t *launches);
 
 const char *gmc_last_error(const gmc_ctx *ctx);
 void gmc_destroy(gmc_ctx *ctx);

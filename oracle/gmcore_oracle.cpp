@@ -68,7 +68,10 @@ struct Error {
   int code = 0;
   std::string msg;
   void set(int c, const std::string &m) {
-    if (code == 0) { code = c; msg = m; }
+#pragma omp critical(orc_error)
+    {
+      if (code == 0) { code = c; msg = m; }
+    }
   }
 };
 
@@ -214,8 +217,9 @@ struct Model {
   void filter(const gmc::Filter &f, Arr &x, Arr *y, bool full_lat, int k0, int k1) {
     const int nlon = mesh.nlon;
     const int nrow = full_lat ? mesh.nlat : mesh.nhalf;
-    std::vector<double> tmp(x.n0);
-    for (int k = k0; k <= k1; ++k)
+#pragma omp parallel for schedule(dynamic)
+    for (int k = k0; k <= k1; ++k) {
+      std::vector<double> tmp(x.n0);
       for (int j = 1; j <= nrow; ++j) {
         int n = full_lat ? f.ngrid_full[j - 1] : f.ngrid_half[j - 1];
         if (n > 1) {
@@ -233,6 +237,7 @@ struct Model {
           for (int i = x.lb0; i <= x.ub0; ++i) (*y)(i, j, k) = x(i, j, k);
         }
       }
+    }
   }
 
   // ------------------------------------------------------------------------
@@ -310,6 +315,7 @@ struct Model {
 
   void calc_ph(State &s) {   // operators_mod.F90:136-168
     const int nlon = mesh.nlon, nlat = mesh.nlat, nlev = mesh.nlev;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev + 1; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -317,6 +323,7 @@ struct Model {
           s.ph_exn_lev(i, j, k) = std::pow(s.ph_lev(i, j, k), Rd_o_cpd);
         }
     fill_halo(s.ph_exn_lev, true, false, true, false, true);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) s.ph(i, j, k) = 0.5 * (s.ph_lev(i, j, k) + s.ph_lev(i, j, k + 1));
@@ -324,6 +331,7 @@ struct Model {
   }
 
   void calc_t(State &s) {   // operators_mod.F90:170-190, formula_mod.F90:24-31
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= mesh.nlev; ++k)
       for (int j = 1; j <= mesh.nlat; ++j)
         for (int i = 1; i <= mesh.nlon; ++i)
@@ -333,12 +341,14 @@ struct Model {
   void calc_m(State &s) {   // operators_mod.F90:471-543
     const int nlon = mesh.nlon, nlat = mesh.nlat, nlev = mesh.nlev, nhalf = mesh.nhalf;
     if (baroclinic) {
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k)
         for (int j = 1; j <= nlat; ++j)
           for (int i = 1; i <= nlon; ++i) {
             s.m(i, j, k) = s.ph_lev(i, j, k + 1) - s.ph_lev(i, j, k);
             if (s.m(i, j, k) <= 0) err.set(GMC_ENONMONO, "The pressure levels are not monotonic!");
           }
+      #pragma omp parallel for schedule(static)
       for (int k = 2; k <= nlev; ++k)
         for (int j = 1; j <= nlat; ++j)
           for (int i = 1; i <= nlon; ++i) s.m_lev(i, j, k) = s.ph(i, j, k) - s.ph(i, j, k - 1);
@@ -354,14 +364,17 @@ struct Model {
     }
     fill_halo(s.m, true);
     const gmc::Grid &g = G();
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) s.m_lon(i, j, k) = (s.m(i, j, k) + s.m(i + 1, j, k)) * 0.5;
     fill_halo(s.m_lon, true);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i) s.m_lat(i, j, k) = (s.m(i, j, k) + s.m(i, j + 1, k)) * 0.5;
     fill_halo(s.m_lat, false);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i)
@@ -388,6 +401,7 @@ struct Model {
       b.uv_step = b.uv_step + 1;
     }
     if (b.uv_step != 0) return;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       for (int j = 2; j <= nlat - 1; ++j) {
         double dx = g.de_lon[j];
@@ -444,6 +458,7 @@ struct Model {
           b.divy(i, j, k) = (b.v(i, j, k) * g.le_lat[j] - b.v(i, j - 1, k) * g.le_lat[j - 1]) / g.area_cell[j];
         }
     }
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       double p = ring([&](int i) { return b.v(i, 1, k); });
       p = p * g.le_lat[1] / nlon / g.area_cell[1];
@@ -491,6 +506,7 @@ struct Model {
       b.we_step = b.we_step + 1;
     }
     if (b.we_step != 0) return;
+    #pragma omp parallel for schedule(static)
     for (int k = 2; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -537,6 +553,7 @@ struct Model {
   void calc_we_lev(State &s, Tend &t, double dt) {   // operators_mod.F90:192-232
     const int nlon = mesh.nlon, nlat = mesh.nlat, nlev = mesh.nlev;
     const gmc::Grid &g = G();
+    #pragma omp parallel for schedule(static)
     for (int k = 2; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -551,11 +568,13 @@ struct Model {
       }
     fill_halo(s.we_lev, true);
     accum_we_lev(mass, s.we_lev, s.m_lev, dt);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev + 1; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i)
           s.we_lev_lon(i, j, k) = (g.area_lon_west[j] * s.we_lev(i, j, k) + g.area_lon_east[j] * s.we_lev(i + 1, j, k)) /
                                   g.area_lon[j];
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev + 1; ++k)
       for (int j = 1; j <= mesh.nhalf; ++j)
         for (int i = 1; i <= nlon; ++i)
@@ -568,6 +587,7 @@ struct Model {
     const gmc::Grid &g = G();
     Arr &u = s.u_f, &v = s.v_f, &ke = s.ke;
     auto sq = [](double x) { return x * x; };
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon + 1; ++i)
@@ -576,6 +596,7 @@ struct Model {
                         g.area_cell[j];
     if (cfg.ke_scheme == 2) {
       const double w = cfg.ke_cell_wgt;
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k)
         for (int j = 2; j <= nlat - 1; ++j)
           for (int i = 1; i <= nlon + 1; ++i) {
@@ -595,6 +616,7 @@ struct Model {
                           w * ke(i, j, k);
           }
     }
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       double p = ring([&](int i) { return v(i, 1, k) * v(i, 1, k); });
       p = p / nlon;
@@ -609,6 +631,7 @@ struct Model {
     const int nlon = mesh.nlon, nlat = mesh.nlat, nlev = mesh.nlev, nhalf = mesh.nhalf;
     const gmc::Grid &g = G();
     if (baroclinic) accum_uv_cell(mass, s.u_f, s.v_f, dt);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 0; i <= nlon; ++i) s.mfx_lon(i, j, k) = s.m_lon(i, j, k) * s.u_f(i, j, k);
@@ -616,6 +639,7 @@ struct Model {
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon + 1; ++i) s.mfy_lat(i, j, k) = s.m_lat(i, j, k) * s.v_f(i, j, k);
     if (baroclinic) accum_mf_cell(mass, s.mfx_lon, s.mfy_lat);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -624,6 +648,7 @@ struct Model {
           s.u_lat(i, j, k) = s.mfx_lat(i, j, k) / s.m_lat(i, j, k);
         }
     fill_halo(s.u_lat, false);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -638,12 +663,14 @@ struct Model {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
     Arr &u = s.u_f, &v = s.v_f, &vor = s.vor;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 0; i <= nlon; ++i)
           vor(i, j, k) = (u(i, j, k) * g.de_lon[j] - u(i, j + 1, k) * g.de_lon[j + 1] + v(i + 1, j, k) * g.de_lat[j] -
                           v(i, j, k) * g.de_lat[j]) / g.area_vtx[j];
     if (cfg.pv_pole_stokes) {
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k) {
         double p = ring([&](int i) { return -s.u_lat(i, 1, k) * g.le_lat[1]; });
         p = p / nlon / g.area_cell[1];
@@ -654,6 +681,7 @@ struct Model {
       }
     }
     (void)nlat;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i) s.pv(i, j, k) = (vor(i, j, k) + g.half_f[j]) / s.m_vtx(i, j, k);
@@ -674,10 +702,12 @@ struct Model {
     const double eps = std::numeric_limits<double>::epsilon();
     Arr &pv = s.pv;
     if (cfg.pv_scheme == GMC_PV_MIDPOINT) {
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k)
         for (int j = 1; j <= nhalf; ++j)
           for (int i = 1; i <= nlon; ++i) s.pv_lat(i, j, k) = 0.5 * (pv(i - 1, j, k) + pv(i, j, k));
       fill_halo(s.pv_lat, false, true, true, true, false);
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k)
         for (int j = 2; j <= nlat - 1; ++j)
           for (int i = 1; i <= nlon; ++i) s.pv_lon(i, j, k) = 0.5 * (pv(i, j, k) + pv(i, j - 1, k));
@@ -686,6 +716,7 @@ struct Model {
     }
     Arr &un = s.u_f, &vn = s.v_f, &ut = s.u_lat, &vt = s.v_lon;
     const double wgt = cfg.upwind_wgt_pv;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -712,6 +743,7 @@ struct Model {
 
   void calc_gz_lev(State &s) {   // operators_mod.F90:433-469
     const int nlon = mesh.nlon, nlat = mesh.nlat, nlev = mesh.nlev;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -721,6 +753,7 @@ struct Model {
           s.gz_lev(i, j, k) = gzs(i, j, 1) + dgz;
         }
     fill_halo(s.gz_lev, true);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) s.gz(i, j, k) = 0.5 * (s.gz_lev(i, j, k) + s.gz_lev(i, j, k + 1));
@@ -729,6 +762,7 @@ struct Model {
   void calc_coriolis(State &s, Tend &t) {   // operators_mod.F90:846-906
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -741,6 +775,7 @@ struct Model {
           else
             t.qhu(i, j, k) = s.mfx_lat(i, j, k) * s.pv_lat(i, j, k);
         }
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -757,6 +792,7 @@ struct Model {
 
   void calc_grad_ke(State &s, Tend &t) {   // operators_mod.F90:908-937
     const gmc::Grid &g = G();
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= mesh.nlev; ++k) {
       for (int j = 2; j <= mesh.nlat - 1; ++j)
         for (int i = 1; i <= mesh.nlon; ++i) t.dkedlon(i, j, k) = (s.ke(i + 1, j, k) - s.ke(i, j, k)) / g.de_lon[j];
@@ -770,6 +806,7 @@ struct Model {
   void flux_div(Arr &fx, Arr &fy, Arr &dx, Arr &dy) {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) dx(i, j, k) = (fx(i, j, k) - fx(i - 1, j, k)) * g.le_lon[j] / g.area_cell[j];
@@ -777,6 +814,7 @@ struct Model {
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i)
           dy(i, j, k) = (fy(i, j, k) * g.le_lat[j] - fy(i, j - 1, k) * g.le_lat[j - 1]) / g.area_cell[j];
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       double p = ring([&](int i) { return fy(i, 1, k); });
       p = p * g.le_lat[1] / nlon / g.area_cell[1];
@@ -789,8 +827,9 @@ struct Model {
 
   void calc_dphsdt(Tend &t) {   // operators_mod.F90:1120-1143
     std::fill(t.dphs.d.begin(), t.dphs.d.end(), 0.0);
-    for (int k = 1; k <= mesh.nlev; ++k)
-      for (int j = 1; j <= mesh.nlat; ++j)
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= mesh.nlat; ++j)
+      for (int k = 1; k <= mesh.nlev; ++k)
         for (int i = 1; i <= mesh.nlon; ++i)
           t.dphs(i, j, 1) = t.dphs(i, j, 1) - t.dmfdlon(i, j, k) - t.dmfdlat(i, j, k);
   }
@@ -798,6 +837,7 @@ struct Model {
   void calc_wedudlev_wedvdlev(State &s, Tend &t) {   // operators_mod.F90:1145-1216
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     Arr &u = s.u_f, &v = s.v_f;
+    #pragma omp parallel for schedule(static)
     for (int k = 2; k <= nlev - 1; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i)
@@ -808,6 +848,7 @@ struct Model {
         t.wedudlev(i, j, 1) = (s.we_lev_lon(i, j, 2) * (u(i, j, 2) - u(i, j, 1))) / s.m_lon(i, j, 1) / 2.0;
         t.wedudlev(i, j, nlev) = (s.we_lev_lon(i, j, nlev) * (u(i, j, nlev) - u(i, j, nlev - 1))) / s.m_lon(i, j, nlev) / 2.0;
       }
+    #pragma omp parallel for schedule(static)
     for (int k = 2; k <= nlev - 1; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i)
@@ -851,6 +892,7 @@ struct Model {
   void hflx_ppm_cell(Batch &b, Arr &u, Arr &v, Arr &mx, Arr &my, Arr &mfx, Arr &mfy) {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     Arr &mlx = b.qlx, &mly = b.qly, &dmx = b.dqx, &dmy = b.dqy, &m6x = b.q6x, &m6y = b.q6y;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -863,6 +905,7 @@ struct Model {
     fill_halo(mly, true, false, false, true, true);
     fill_halo(dmy, true, false, false, true, true);
     fill_halo(m6y, true, false, false, true, true);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -913,10 +956,12 @@ struct Model {
   void vflx_ppm_cell(Batch &b, Arr &w, Arr &m, Arr &mfz) {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nlat = mesh.nlat;
     Arr &mlz = b.qlx, &dmz = b.dqx, &m6z = b.q6x;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i)
           ppm(m(i, j, k - 2), m(i, j, k - 1), m(i, j, k), m(i, j, k + 1), m(i, j, k + 2), mlz(i, j, k), dmz(i, j, k), m6z(i, j, k));
+    #pragma omp parallel for schedule(static)
     for (int k = 2; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -953,6 +998,7 @@ struct Model {
     hflx_ppm_cell(b, b.u, b.v, q, q, qmfx, qmfy);
     fill_halo(qmfx, true, true, true, false, false);
     fill_halo(qmfy, false, false, false, true, true);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) {
@@ -961,6 +1007,7 @@ struct Model {
           qy(i, j, k) = q(i, j, k) - 0.5 * ((qmfy(i, j, k) * g.le_lat[j] - qmfy(i, j - 1, k) * g.le_lat[j - 1]) / g.area_cell[j] -
                                             b.divy(i, j, k) * q(i, j, k)) * dt_;
         }
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       double p = ring([&](int i) { return qmfy(i, 1, k); });
       p = p * g.le_lat[1] / nlon / g.area_cell[1];
@@ -994,6 +1041,7 @@ struct Model {
       for (int j = pt.lb1; j <= pt.ub1; ++j)
         for (int i = pt.lb0; i <= pt.ub0; ++i) pt(i, j, k) = 2 * pt(i, j, k - 1) - pt(i, j, k - 2);
     vflx_ppm_cell(mass, mass.we, pt, s.ptf_lev);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= mesh.nlat; ++j)
         for (int i = 1; i <= mesh.nlon; ++i) t.dptfdlev(i, j, k) = s.ptf_lev(i, j, k + 1) - s.ptf_lev(i, j, k);
@@ -1004,6 +1052,7 @@ struct Model {
     const gmc::Grid &g = G();
     if (hydrostatic) {   // pgf_lin97_run (pgf_lin97_mod.F90:20-105)
       Arr &pe = s.ph_exn_lev, &gz = s.gz_lev;
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k) {
         for (int j = 2; j <= nlat - 1; ++j)
           for (int i = 1; i <= nlon; ++i) {
@@ -1062,6 +1111,7 @@ struct Model {
     }
     calc_coriolis(star, t1);
     calc_grad_ke(star, t1);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i)
@@ -1087,6 +1137,7 @@ struct Model {
     t1.reset_flags();
     operators_prepare_bwd(nw);
     pgf_run(nw, t1);
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i) t1.du(i, j, k) = t2.du(i, j, k) - t1.pgf_lon(i, j, k);
@@ -1111,11 +1162,13 @@ struct Model {
         calc_m(n);
       }
       if (t.update_pt) {
+        #pragma omp parallel for schedule(static)
         for (int k = 1; k <= nlev; ++k)
           for (int j = 1; j <= nlat; ++j)
             for (int i = 1; i <= nlon; ++i) n.pt(i, j, k) = o.pt(i, j, k) * o.m(i, j, k) + dt * t.dpt(i, j, k);
         fill_halo(n.pt, true, true, true, false, false);
         filter(grid.small1, n.pt, nullptr, true, 1, nlev);
+        #pragma omp parallel for schedule(static)
         for (int k = 1; k <= nlev; ++k)
           for (int j = 1; j <= nlat; ++j)
             for (int i = 1; i <= nlon; ++i) n.pt(i, j, k) = n.pt(i, j, k) / n.m(i, j, k);
@@ -1131,6 +1184,7 @@ struct Model {
       fill_halo(n.gz, true);
     }
     if (t.update_u && t.update_v) {
+      #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k)
         for (int j = 2; j <= nlat - 1; ++j)
           for (int i = 1; i <= nlon; ++i) n.u_lon(i, j, k) = o.u_lon(i, j, k) + dt * t.du(i, j, k);
@@ -1174,11 +1228,13 @@ struct Model {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
     Arr &u = s.u_f, &v = s.v_f, &div = s.div;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i)
           div(i, j, k) = ((u(i, j, k) * g.le_lon[j] - u(i - 1, j, k) * g.le_lon[j]) +
                           (v(i, j, k) * g.le_lat[j] - v(i, j - 1, k) * g.le_lat[j - 1])) / g.area_cell[j];
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k) {
       double p = ring([&](int i) { return v(i, 1, k); });
       p = p * g.le_lat[1] / nlon / g.area_cell[1];
@@ -1196,11 +1252,13 @@ struct Model {
     const gmc::Grid &g = G();
     calc_div(s);
     Arr &div = s.div;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
         for (int i = 1; i <= nlon; ++i)
           s.u_lon(i, j, k) = s.u_lon(i, j, k) +
                              g.div_c_lon[(size_t)(k - 1) * nlat + (j - 1)] * (div(i + 1, j, k) - div(i, j, k)) / g.de_lon[j];
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon; ++i)
@@ -1527,6 +1585,7 @@ int orc_set_tracer(void *h, int l, const double *src) {
   for (int s = 0; s < 2; ++s) {
     orc::Arr &q = m->tracers.q[s][l];
     size_t o = 0;
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) q(i, j, k) = src[o++];
@@ -1541,6 +1600,7 @@ int orc_get_tracer(void *h, int l, double *dst) {
   const int nlon = m->mesh.nlon, nlat = m->mesh.nlat, nlev = m->mesh.nlev;
   orc::Arr &q = m->tracers.q[m->tracers.old_idx][l];
   size_t o = 0;
+  #pragma omp parallel for schedule(static)
   for (int k = 1; k <= nlev; ++k)
     for (int j = 1; j <= nlat; ++j)
       for (int i = 1; i <= nlon; ++i) dst[o++] = q(i, j, k);
