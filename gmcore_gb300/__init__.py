@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .abi import (Config, Diag, View, Stats, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
+from .abi import (Config, Diag, View, Stats, FfslFields, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
                   TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, LIMITER_NONE,
                   LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
                   VCOORD_WRF_L64, PREC_FP64, PREC_MIXED)
@@ -27,7 +27,7 @@ EXPORTED = (
     "gmc_config_default", "gmc_create", "gmc_lon_halo_width", "gmc_set_field", "gmc_set_tracer",
     "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
-    "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile",
+    "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx",
 )
 
 _lib = None
@@ -71,6 +71,7 @@ def load(build_if_missing=True):
     lib.gmc_filter_taps.argtypes = [P(Config), C.c_int32, C.c_int32, P(C.c_int32), C.c_size_t]
     lib.gmc_make_ic.argtypes = [P(Config), C.c_int32, C.c_uint64, C.c_double] + [P(C.c_double)] * 6
     lib.gmc_get_stats.argtypes = [C.c_void_p, P(Stats)]
+    lib.gmc_ffsl_hflx.argtypes = [C.c_void_p, P(FfslFields), C.c_double]
     lib.gmc_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
     _lib = lib
@@ -230,6 +231,12 @@ class Model:
         d = Diag()
         self._check(self.lib.gmc_diagnose(self.h, member, C.byref(d)))
         return d.as_dict()
+
+    def ffsl_hflx(self, fields, dt):
+        """Horizontal FFSL flux operator on device buffers.  `fields` maps the
+        gmc_ffsl_fields member names to device pointers (ints)."""
+        f = FfslFields(**fields)
+        self._check(self.lib.gmc_ffsl_hflx(self.h, C.byref(f), dt))
 
     def stats(self):
         """Device time (CUDA events on the context stream) and kernel count of

@@ -72,6 +72,10 @@ class Stats(C.Structure):
     _fields_ = [("step_ms", C.c_double), ("steps", C.c_int64), ("kernel_launches", C.c_int64)]
 
 
+class FfslFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("q", "u", "v", "mfx", "mfy", "cflx", "cfly", "divx", "divy", "qmfx", "qmfy")]
+
+
 class View(C.Structure):
     _fields_ = [("data", C.POINTER(C.c_double)), ("lb", C.c_int32 * 3), ("ub", C.c_int32 * 3)]
 

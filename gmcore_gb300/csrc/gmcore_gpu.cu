@@ -93,6 +93,7 @@ struct EngineBase {
   virtual unsigned read_error() = 0;
   virtual void set_tracer(int member, int l, const double *src) = 0;
   virtual void get_tracer(int member, int l, double *dst) = 0;
+  virtual void ffsl_hflx(const gmc_ffsl_fields &f, double dt) = 0;
   long time_step = 0;
   // timing and profiling
   double last_step_ms = 0;
@@ -436,6 +437,23 @@ struct Engine : EngineBase {
     CK(cudaMemcpyAsync(host, q[((size_t)m * 2 + q_old) * ntr + l], n * sizeof(R), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     for (size_t t = 0; t < n; ++t) dst[t] = (double)host[t];
+  }
+
+  // Operator entry point: one horizontal FFSL flux with pool-allocated scratch.
+  void ffsl_hflx(const gmc_ffsl_fields &f, double dt) override {
+    if (!f.q || !f.u || !f.v || !f.mfx || !f.mfy || !f.cflx || !f.cfly || !f.divx || !f.divy || !f.qmfx || !f.qmfy)
+      throw ApiError{GMC_EINVAL, "null field pointer"};
+    R *scr = nullptr;
+    const size_t n = full3();
+    CK(cudaMallocAsync((void **)&scr, 4 * n * sizeof(R) + 1024, stream));
+    BatchView<R> b{};
+    b.u = (const R *)f.u; b.v = (const R *)f.v; b.mfx = (const R *)f.mfx; b.mfy = (const R *)f.mfy;
+    b.cflx = (const R *)f.cflx; b.cfly = (const R *)f.cfly; b.divx = (const R *)f.divx; b.divy = (const R *)f.divy;
+    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr, scr + n, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(scr, stream);
+    if (e != cudaSuccess) throw CudaError(std::string("ffsl_hflx: ") + cudaGetErrorString(e));
+    CK(cudaStreamSynchronize(stream));
   }
 
   // adv_accum_wind for the static tracer batch (adv_mod.F90:420-455 with
@@ -933,6 +951,16 @@ int gmc_time_step(const gmc_ctx *ctx, int64_t *out) {
   if (!ctx || !out || !ctx->eng) return GMC_EINVAL;
   *out = ctx->eng->time_step;
   return GMC_OK;
+}
+
+int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!f) return fail(ctx, GMC_EINVAL, "null field set");
+  return guarded(ctx, [&]() {
+    ctx->eng->ffsl_hflx(*f, dt);
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
 }
 
 int gmc_get_stats(const gmc_ctx *ctx, gmc_stats *out) {

@@ -165,6 +165,25 @@ int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out);
 /* Number of steps taken since gmc_prepare. */
 int gmc_time_step(const gmc_ctx *ctx, int64_t *out);
 
+/* ---- operator entry points -----------------------------------------------
+ * Device pointers, interior layout [k][j][i] (i fastest), in the context's
+ * precision (double for GMC_PREC_FP64, float for GMC_PREC_MIXED).  Half-
+ * latitude fields have nlat-1 rows. */
+typedef struct gmc_ffsl_fields {
+  const void *q;                  /* advected field (cells)                       */
+  const void *u, *v;              /* advecting winds (lon edges, lat edges)       */
+  const void *mfx, *mfy;          /* mass fluxes of the outer operator            */
+  const void *cflx, *cfly;        /* Courant numbers (lon edges, lat edges)       */
+  const void *divx, *divy;        /* axis divergences (cells)                     */
+  void *qmfx, *qmfy;              /* out: fluxes on lon / lat edges               */
+} gmc_ffsl_fields;
+
+/* Horizontal FFSL flux of one field (inner advective operators, intermediate
+ * qx/qy, outer flux-form operators), the reference's adv_calc_tracer_hflx_cell
+ * plugin (adv_mod.F90:109, ffsl_calc_tracer_hflx_cell ffsl_mod.F90:318-413).
+ * Its four scratch fields are allocated from the device pool for the call. */
+int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
+
 /* Timing of the last gmc_step call: device time between CUDA events
  * recorded on the context's stream around the whole call, and the number
  * of kernels it launched. */

@@ -1626,6 +1626,41 @@ int orc_diagnose(void *h, double *out) {
   return GMC_OK;
 }
 
+// One horizontal FFSL flux (ffsl_calc_tracer_hflx_cell) of field q with the
+// given batch fields; inputs and outputs interior-only [k][j][i].
+int orc_ffsl_hflx(void *h, const double *q, const double *u, const double *v, const double *mfx, const double *mfy,
+                  const double *cflx, const double *cfly, const double *divx, const double *divy, double dt,
+                  double *qmfx, double *qmfy) {
+  orc::Model *m = (orc::Model *)h;
+  const int nlon = m->mesh.nlon, nlat = m->mesh.nlat, nhalf = m->mesh.nhalf, nlev = m->mesh.nlev;
+  orc::Fields F{&m->mesh};
+  orc::Batch b;
+  m->alloc_batch(b, dt, true, 0);
+  orc::Arr qa, fx, fy;
+  F.cell3(qa); F.lon3(fx); F.lat3(fy);
+  auto load = [&](orc::Arr &a, const double *src, int nrow, bool full) {
+    size_t o = 0;
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nrow; ++j)
+        for (int i = 1; i <= nlon; ++i) a(i, j, k) = src[o++];
+    m->fill_halo(a, full);
+  };
+  load(qa, q, nlat, true); load(b.u, u, nlat, true); load(b.v, v, nhalf, false);
+  load(b.mfx, mfx, nlat, true); load(b.mfy, mfy, nhalf, false);
+  load(b.cflx, cflx, nlat, true); load(b.cfly, cfly, nhalf, false);
+  load(b.divx, divx, nlat, true); load(b.divy, divy, nlat, true);
+  m->tracer_hflx_cell(b, qa, fx, fy, dt);
+  size_t o = 0;
+  for (int k = 1; k <= nlev; ++k)
+    for (int j = 1; j <= nlat; ++j)
+      for (int i = 1; i <= nlon; ++i) qmfx[o++] = fx(i, j, k);
+  o = 0;
+  for (int k = 1; k <= nlev; ++k)
+    for (int j = 1; j <= nhalf; ++j)
+      for (int i = 1; i <= nlon; ++i) qmfy[o++] = fy(i, j, k);
+  return m->err.code;
+}
+
 // Mesh/filter queries for the known-answer tests.
 int orc_metric(void *h, const char *name, double *out, int n) {
   orc::Model *m = (orc::Model *)h;

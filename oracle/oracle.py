@@ -43,6 +43,7 @@ def load(variant="parity"):
     lib.orc_diagnose.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.orc_metric.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int]
     lib.orc_filter_taps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
     _LIBS[variant] = lib
     return lib
 
@@ -145,3 +146,15 @@ class Oracle:
         out = np.zeros(n, dtype=np.int32)
         self.lib.orc_filter_taps(self.h, which, lat, out.ctypes.data_as(C.POINTER(C.c_int)))
         return out
+
+    def ffsl_hflx(self, q, u, v, mfx, mfy, cflx, cfly, divx, divy, dt):
+        """ffsl_calc_tracer_hflx_cell on interior arrays; returns (qmfx, qmfy)."""
+        c = self.cfg
+        full = (c.nlev, c.nlat, c.nlon)
+        half = (c.nlev, c.nlat - 1, c.nlon)
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (q, u, v, mfx, mfy, cflx, cfly, divx, divy)]
+        fx, fy = np.zeros(full), np.zeros(half)
+        rc = self.lib.orc_ffsl_hflx(self.h, *[_ptr(a) for a in arrs], dt, _ptr(fx), _ptr(fy))
+        if rc:
+            raise RuntimeError(f"oracle ffsl_hflx failed ({rc})")
+        return fx, fy
