@@ -27,7 +27,7 @@ EXPORTED = (
     "gmc_config_default", "gmc_create", "gmc_lon_halo_width", "gmc_set_field", "gmc_set_tracer",
     "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
-    "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx",
+    "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
 )
 
 _lib = None
@@ -72,6 +72,7 @@ def load(build_if_missing=True):
     lib.gmc_make_ic.argtypes = [P(Config), C.c_int32, C.c_uint64, C.c_double] + [P(C.c_double)] * 6
     lib.gmc_get_stats.argtypes = [C.c_void_p, P(Stats)]
     lib.gmc_ffsl_hflx.argtypes = [C.c_void_p, P(FfslFields), C.c_double]
+    lib.gmc_ffsl_hflx_noalloc.argtypes = [C.c_void_p, P(FfslFields), C.c_double]
     lib.gmc_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
     _lib = lib
@@ -237,6 +238,11 @@ class Model:
         gmc_ffsl_fields member names to device pointers (ints)."""
         f = FfslFields(**fields)
         self._check(self.lib.gmc_ffsl_hflx(self.h, C.byref(f), dt))
+
+    def ffsl_hflx_noalloc(self, fields, dt):
+        """gmc_ffsl_hflx with the library's fixed device scratch (no allocation)."""
+        f = FfslFields(**fields)
+        self._check(self.lib.gmc_ffsl_hflx_noalloc(self.h, C.byref(f), dt))
 
     def stats(self):
         """Device time (CUDA events on the context stream) and kernel count of

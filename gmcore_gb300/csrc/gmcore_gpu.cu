@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -94,7 +95,10 @@ struct EngineBase {
   virtual void set_tracer(int member, int l, const double *src) = 0;
   virtual void get_tracer(int member, int l, double *dst) = 0;
   virtual void ffsl_hflx(const gmc_ffsl_fields &f, double dt) = 0;
+  virtual size_t ffsl_scratch_bytes() const = 0;
+  virtual void ffsl_hflx_in(const gmc_ffsl_fields &f, double dt, void *scratch) = 0;
   long time_step = 0;
+  int device = 0;   // device current when the context was created
   // timing and profiling
   double last_step_ms = 0;
   long last_steps = 0, last_launches = 0, launches = 0;
@@ -232,6 +236,7 @@ struct Engine : EngineBase {
     tb.resize(nm);
     q.assign((size_t)nm * 2 * std::max(ntr, 1), nullptr);
     nstep_adv = std::max(1, (int)(cfg.dt_adv / cfg.dt_dyn));
+    CK(cudaGetDevice(&device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     L.stream = stream;
     L.threads = grid.nlon >= 512 ? 256 : 128;
@@ -453,6 +458,23 @@ struct Engine : EngineBase {
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(scr, stream);
     if (e != cudaSuccess) throw CudaError(std::string("ffsl_hflx: ") + cudaGetErrorString(e));
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  // Bytes of the four scratch fields of one horizontal FFSL flux.
+  size_t ffsl_scratch_bytes() const override { return 4 * full3() * sizeof(R); }
+
+  // The same flux with the scratch supplied by the caller (no allocation).
+  void ffsl_hflx_in(const gmc_ffsl_fields &f, double dt, void *scratch) override {
+    if (!f.q || !f.u || !f.v || !f.mfx || !f.mfy || !f.cflx || !f.cfly || !f.divx || !f.divy || !f.qmfx || !f.qmfy)
+      throw ApiError{GMC_EINVAL, "null field pointer"};
+    R *scr = static_cast<R *>(scratch);
+    const size_t n = full3();
+    BatchView<R> b{};
+    b.u = (const R *)f.u; b.v = (const R *)f.v; b.mfx = (const R *)f.mfx; b.mfy = (const R *)f.mfy;
+    b.cflx = (const R *)f.cflx; b.cfly = (const R *)f.cfly; b.divx = (const R *)f.divx; b.divy = (const R *)f.divy;
+    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr, scr + n, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
   }
 
@@ -799,6 +821,46 @@ void field_dims(const gmc_config &c, const std::string &name, int &nrow, int &nk
   if (name == "we_lev") nk = c.nlev + 1;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch for gmc_ffsl_hflx_noalloc: a fixed device array that every GPU
+// loading this library carries until the process exits.  Host code may not
+// use the symbol itself as a device address; the address is looked up once
+// per device with cudaGetSymbolAddress while that device is current.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;   // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on device `dev`.  The first call for a
+// device makes that device current for the lookup and restores the caller's
+// device afterwards.
+int noalloc_scratch_address(int dev, void **out, std::string &err) {
+  if (dev < 0 || dev >= kMaxDevices) { err = "device ordinal out of range"; return GMC_ECUDA; }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return GMC_ECUDA; }
+    if (cur != dev && (e = cudaSetDevice(dev)) != cudaSuccess) {
+      err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+      return GMC_ECUDA;
+    }
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (cur != dev) cudaSetDevice(cur);
+    if (e != cudaSuccess || !p) {
+      err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return GMC_ECUDA;
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return GMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -959,6 +1021,25 @@ int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt) {
   if (!f) return fail(ctx, GMC_EINVAL, "null field set");
   return guarded(ctx, [&]() {
     ctx->eng->ffsl_hflx(*f, dt);
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
+}
+
+int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!f) return fail(ctx, GMC_EINVAL, "null field set");
+  const size_t need = ctx->eng->ffsl_scratch_bytes();
+  if (need > kNoAllocScratchBytes)
+    return fail(ctx, GMC_EINVAL, "gmc_ffsl_hflx_noalloc: grid needs " + std::to_string(need) +
+                                     " scratch bytes, the fixed scratch holds " + std::to_string(kNoAllocScratchBytes) +
+                                     " (4 x nlon x nlat x nlev values); use gmc_ffsl_hflx");
+  return guarded(ctx, [&]() {
+    void *scr = nullptr;
+    std::string err;
+    int rc = noalloc_scratch_address(ctx->eng->device, &scr, err);
+    if (rc != GMC_OK) throw ApiError{rc, err};
+    ctx->eng->ffsl_hflx_in(*f, dt, scr);
     return error_word_status(ctx, ctx->eng->read_error());
   });
 }

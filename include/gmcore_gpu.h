@@ -184,6 +184,21 @@ typedef struct gmc_ffsl_fields {
  * Its four scratch fields are allocated from the device pool for the call. */
 int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
 
+/* gmc_ffsl_hflx without any device allocation.  No counterpart in the
+ * reference: it exists for callers that must not allocate at the moment of
+ * the call -- code running while a CUDA graph is being captured, a host that
+ * reserved all device memory for its own pool at start-up, or a real-time
+ * loop where a cudaMalloc would synchronise the device.  Its four scratch
+ * fields live in one fixed 32 MiB device array compiled into the library
+ * (every GPU that loads the library keeps it until the process exits), so it
+ * accepts grids with 4 x nlon x nlat x nlev x sizeof(value) <= 32 MiB and
+ * returns GMC_EINVAL beyond that.  The first call on a device looks up the
+ * array's device address (make that first call before any stream capture).
+ * All calls share the one array: nothing in it needs to start at zero, and
+ * calls whose kernels overlap on the GPU (two contexts on different streams
+ * at the same time) race on it.  Results equal gmc_ffsl_hflx's. */
+int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
+
 /* Timing of the last gmc_step call: device time between CUDA events
  * recorded on the context's stream around the whole call, and the number
  * of kernels it launched. */
