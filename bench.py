@@ -197,6 +197,7 @@ def run_ours(args):
     sdpd_rank = DT * args.steps / (dev_ms / 1000.0)
     value = sdpd_rank * WORLD
     launches_per_step = stats["kernel_launches"] / args.steps
+    ps_mixed = model.get_field("phs")   # after warmup + steps, compared with FP64 below
 
     # ---- end to end through the C ABI with host buffers ----
     host = {k: np.ascontiguousarray(v) for k, v in st.items()}
@@ -236,7 +237,6 @@ def run_ours(args):
     alg = algorithmic_bytes(top_name, cfg, 4)
     peak, peak_kind = measured_peaks()
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
-    ps_mixed = model.get_field("phs")
     model.close()
 
     # ---- FP64 form on the same initial state ----

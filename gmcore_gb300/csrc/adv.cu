@@ -263,15 +263,15 @@ __global__ void k_batch_cflz(DGrid g, const double *we_in, const double *ml_in, 
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
   if (i > nlon) return;
-  double we[66], ml[66];
+  R we[66], ml[66];
   for (int k = 1; k <= nlev + 1; ++k) {
     size_t o = ix3(nlat, nlon, i, j, k);
-    we[k - 1] = we_in[o];
-    ml[k - 1] = ml_in[o];
+    we[k - 1] = (R)we_in[o];
+    ml[k - 1] = (R)ml_in[o];
   }
   bool bad = false;
   for (int k = 2; k <= nlev; ++k) {
-    double c = cflz_of(g, we, ml, k, dt, bad);
+    R c = cflz_of<R>(g, we, ml, k, (R)dt, bad);
     if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = (R)c;
   }
   if (bad) atomicOr(g.err, ERR_CFLZ);

@@ -33,6 +33,7 @@ struct FilterDev {
   const int *off_full;     // weight offsets
   const int *off_half;
   const double *wgt;
+  const float *wgt_f;      // FP32 copy for rows accumulated in FP32
   int max_taps;
 };
 
@@ -54,6 +55,7 @@ struct DGrid {
   const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat;
   const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
+  const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables
   const double *lon_damp_full;                                     // [j-1]
   const double *div_c_lon, *div_c_lat;                             // [(k-1)*n + j-1]
   FilterDev big, small1, small2;

@@ -7,6 +7,8 @@
 // Reference routines are cited per kernel.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "kernels.hpp"
 #include "stencil.cuh"
 
@@ -230,6 +232,34 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       divy[o] = (R)p;
       divx[o] = (R)0;
     }
+  } else if constexpr (std::is_same<R, float>::value) {
+    // FP32 form of the x departure: positions in cells relative to face i,
+    // (radius half_lon(l) cos - x) / dx = (l - i) - a exactly in real arithmetic.
+    const float cdx = (float)(dt_ / ROW(g.de_lon, j));
+    const float lel = (float)ROW(g.le_lon, j), ac = (float)ROW(g.area_cell, j);
+    const float la0 = (float)ROW(g.le_lat, j), la1 = (float)ROW(g.le_lat, j - 1);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      auto Ul = [&](int l) {
+        int lw = ((l - 1) % nlon + nlon) % nlon + 1;
+        return u[ix3(nlat, nlon, lw, j, k)];
+      };
+      auto at = [&](float a) {   // wind at i + a
+        float fl = floorf(a);
+        int l = i + (int)fl;
+        float f = a - fl;
+        return (1.0f - f) * Ul(l) + f * Ul(l + 1);
+      };
+      const float u1 = Ul(i);
+      const float u2 = at(0.5f * cdx * u1);
+      const float u3 = at(0.5f * cdx * u2);
+      const float u4 = at(cdx * u3);
+      const float c = (u1 + 2.0f * u2 + 2.0f * u3 + u4) / 6.0f * cdx;
+      if (!(fabsf(c) <= (float)g.hx)) atomicOr(g.err, ERR_CFLX);
+      size_t o = ix3(nlat, nlon, i, j, k);
+      cflx[o] = c;
+      divx[o] = (u1 - Ul(i - 1)) * lel / ac;
+      divy[o] = (v[ix3(nhalf, nlon, i, j, k)] * la0 - v[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
+    }
   } else {
     const double dx = ROW(g.de_lon, j), cl = ROW(g.full_cos_lat, j);
     const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
@@ -258,6 +288,35 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       double vn = (double)v[ix3(nhalf, nlon, i, j, k)], vs = (double)v[ix3(nhalf, nlon, i, j - 1, k)];
       divy[o] = (R)((vn * la0 - vs * la1) / ac);
     }
+  }
+  if constexpr (std::is_same<R, float>::value) {
+    if (j <= nhalf) {
+      // FP32 form of the y departure: row offsets A(l) = radius (half_lat(l) - half_lat(j)) / dy.
+      // A departure more than one row away (|cfly| > 1, flagged below) keeps v1.
+      const double dy = ROW(g.de_lat, j);
+      const float cdy = (float)(dt_ / dy);
+      float A[4];   // l = j-1 .. j+2
+      for (int t = 0; t < 4; ++t) {
+        int l = j - 1 + t;
+        A[t] = (l >= 1 && l <= nhalf) ? (float)(radius * (ROW(g.half_lat, l) - ROW(g.half_lat, j)) / dy) : 0.f;
+      }
+      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+        auto Vl = [&](int l) { return v[ix3(nhalf, nlon, i, l, k)]; };
+        const float v1 = Vl(j);
+        auto at = [&](float b) {
+          int l = (int)floorf((float)j + b);
+          if (l < 1 || l > nhalf - 1 || l < j - 1 || l > j + 1) return v1;
+          return (A[l + 2 - j] - b) * Vl(l) + (b - A[l + 1 - j]) * Vl(l + 1);
+        };
+        const float v2 = at(0.5f * cdy * v1);
+        const float v3 = at(0.5f * cdy * v2);
+        const float v4 = at(cdy * v3);
+        const float c = (v1 + 2.0f * v2 + 2.0f * v3 + v4) / 6.0f * cdy;
+        if (!(fabsf(c) <= 1.0f)) atomicOr(g.err, ERR_CFLY);
+        cfly[ix3(nhalf, nlon, i, j, k)] = c;
+      }
+    }
+    return;
   }
   if (j <= nhalf) {
     const double dy = ROW(g.de_lat, j);
@@ -304,8 +363,9 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
     __syncthreads();
   }
   if (i > nlon) return;
+  typedef typename std::conditional<std::is_same<R, float>::value, float, double>::type T;
   double mfp[66];
-  double we[66], ml[66];
+  T we[66], ml[66];
   const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
   const int im = wrap(i - 1, nlon);
   double dphs = 0, mf = 0;
@@ -324,24 +384,29 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
   }
   const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
   w.dphs[c2] = dphs;
+  s.we_lev[ix3(nlat, nlon, i, j, 1)] = 0;
   we[0] = 0;
-  for (int k = 2; k <= nlev; ++k) we[k - 1] = -(g.hybi[k - 1] * dphs) - mfp[k - 2];
+  for (int k = 2; k <= nlev; ++k) {
+    double wv = -(g.hybi[k - 1] * dphs) - mfp[k - 2];
+    s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
+    we[k - 1] = (T)wv;
+  }
   we[nlev] = 0;
-  for (int k = 1; k <= nlev + 1; ++k) s.we_lev[ix3(nlat, nlon, i, j, k)] = we[k - 1];
+  s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
   // half-level mass from the hybrid pressures (calc_m, operators_mod.F90:505-525)
   const double phs = s.phs_f[c2];
   double plo = ph_lev(g, 1, phs), ph_prev = 0;
   for (int k = 1; k <= nlev; ++k) {
     double phi = ph_lev(g, k + 1, phs);
     double ph = 0.5 * (plo + phi);
-    ml[k - 1] = k == 1 ? ph - plo : ph - ph_prev;
+    ml[k - 1] = (T)(k == 1 ? ph - plo : ph - ph_prev);
     ph_prev = ph;
     plo = phi;
   }
-  ml[nlev] = plo - ph_prev;
+  ml[nlev] = (T)(plo - ph_prev);
   bool bad = false;
   for (int k = 2; k <= nlev; ++k) {
-    double c = cflz_of(g, we, ml, k, dt, bad);
+    T c = cflz_of<T>(g, we, ml, k, (T)dt, bad);
     size_t o = ix3(nlat, nlon, i, j, k);
     if (c == c) w.cflz[o] = (R)c;
   }
@@ -379,8 +444,8 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
       R du = qhv - dkedlon;
       if (g.baroclinic) {
         auto WEL = [&](int kk) {
-          double a = s.we_lev[ix3(nlat, nlon, i, j, kk)], b = s.we_lev[ix3(nlat, nlon, wrap(i + 1, nlon), j, kk)];
-          return (R)(((double)aw * a + (double)ae * b) / (double)al);
+          R a = (R)s.we_lev[ix3(nlat, nlon, i, j, kk)], b = (R)s.we_lev[ix3(nlat, nlon, wrap(i + 1, nlon), j, kk)];
+          return (aw * a + ae * b) / al;
         };
         auto Uk = [&](int kk) { return s.u_f[ix3(nlat, nlon, i, j, kk)]; };
         R m_lon = (M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * (R)0.5;
@@ -414,8 +479,8 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
       R dv = -qhu - dkedlat;
       if (g.baroclinic) {
         auto WEL = [&](int kk) {
-          double a = s.we_lev[ix3(nlat, nlon, i, j + 1, kk)], b = s.we_lev[ix3(nlat, nlon, i, j, kk)];
-          return (R)(((double)an * a + (double)as * b) / (double)al);
+          R a = (R)s.we_lev[ix3(nlat, nlon, i, j + 1, kk)], b = (R)s.we_lev[ix3(nlat, nlon, i, j, kk)];
+          return (an * a + as * b) / al;
         };
         auto Vk = [&](int kk) { return s.v_f[ix3(nhalf, nlon, i, j, kk)]; };
         R m_lat = (M.at(g, i, j, k) + M.at(g, i, j + 1, k)) * (R)0.5;
@@ -534,14 +599,34 @@ __global__ void k_column_backward(DGrid g, Slot<R> n, Work<R> w) {
   if (i > nlon) return;
   const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
   const double phs = n.phs_f[c2];
+  const double gzs = n.gzs[c2];
+  w.gz_lev[ix3(nlat, nlon, i, j, nlev + 1)] = gzs;
+  if constexpr (std::is_same<R, float>::value) {
+    // FP32 transcendentals, FP64 pressures and geopotential accumulation:
+    // ln(p(k+1)/p(k)) = log1p(dp/p) with dp, p from FP64 keeps ~1e-7 relative
+    // accuracy however thin the layer.
+    const float kap = (float)g.kappa;
+    double p_hi = ph_lev(g, nlev + 1, phs);
+    w.ph_exn_lev[ix3(nlat, nlon, i, j, nlev + 1)] = (double)powf((float)p_hi, kap);
+    double acc = 0;
+    for (int k = nlev; k >= 1; --k) {
+      double p_lo = ph_lev(g, k, phs);
+      w.ph_exn_lev[ix3(nlat, nlon, i, j, k)] = (double)powf((float)p_lo, kap);
+      double ph = 0.5 * (p_lo + p_hi);
+      float t = n.pt[ix3(nlat, nlon, i, j, k)] * powf((float)(ph / g.p0), kap);
+      float dlnp = log1pf((float)((p_hi - p_lo) / p_lo));
+      acc = (double)((float)g.Rd * t * dlnp) + acc;
+      w.gz_lev[ix3(nlat, nlon, i, j, k)] = gzs + acc;
+      p_hi = p_lo;
+    }
+    return;
+  }
   double pl[66];
   for (int k = 1; k <= nlev + 1; ++k) {
     pl[k - 1] = ph_lev(g, k, phs);
     w.ph_exn_lev[ix3(nlat, nlon, i, j, k)] = pow(pl[k - 1], g.kappa);
   }
   double acc = 0;
-  const double gzs = n.gzs[c2];
-  w.gz_lev[ix3(nlat, nlon, i, j, nlev + 1)] = gzs;
   for (int k = nlev; k >= 1; --k) {
     double ph = 0.5 * (pl[k - 1] + pl[k]);
     double t = (double)n.pt[ix3(nlat, nlon, i, j, k)] * pow(ph / g.p0, g.kappa);
@@ -601,10 +686,10 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
       size_t c = ix3(nlat, nlon, i + 1, j, k);
       row[i] = o.u_lon[c] + (R)dt * (w.du[c] - pgf_lon(g, n, w, i + 1, j, k));
     }
-    if (g.baroclinic) filter_row<R>(g.small2, true, j, nlon, row, ext);
+    if (g.baroclinic) filter_row<R, R>(g.small2, true, j, nlon, row, ext);
     __syncthreads();
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_lon[ix3(nlat, nlon, i + 1, j, k)] = row[i];
-    filter_row<R>(g.big, true, j, nlon, row, ext);
+    filter_row<R, R>(g.big, true, j, nlon, row, ext);
     __syncthreads();
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_f[ix3(nlat, nlon, i + 1, j, k)] = row[i];
     return;
@@ -615,7 +700,7 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
       size_t c = ix3(nhalf, nlon, i + 1, jj, k);
       dst[i] = o.v_lat[c] + (R)dt * (w.dv[c] - pgf_lat(g, n, w, i + 1, jj, k));
     }
-    if (g.baroclinic) filter_row<R>(g.small2, false, jj, nlon, dst, ext);
+    if (g.baroclinic) filter_row<R, R>(g.small2, false, jj, nlon, dst, ext);
     __syncthreads();
   };
   load_v(j, row);
@@ -626,7 +711,7 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
     __syncthreads();
   }
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_lat[ix3(nhalf, nlon, i + 1, j, k)] = row[i];
-  filter_row<R>(g.big, false, j, nlon, row, ext);
+  filter_row<R, R>(g.big, false, j, nlon, row, ext);
   __syncthreads();
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_f[ix3(nhalf, nlon, i + 1, j, k)] = row[i];
 }

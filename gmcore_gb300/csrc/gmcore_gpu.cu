@@ -313,8 +313,13 @@ struct Engine : EngineBase {
       dB[k] = (float)(g.hybi[k + 1] - g.hybi[k]);
     }
     size_t offA = push(dA.data(), dA.size() * 4), offB = push(dB.data(), dB.size() * 4);
+    std::vector<float> hlf(g.half_lev.begin(), g.half_lev.end()), hdf(g.half_dlev.begin(), g.half_dlev.end()),
+        fdf(g.full_dlev.begin(), g.full_dlev.end());
+    hlf.push_back(0.f); hdf.push_back(0.f); fdf.push_back(0.f);
+    size_t offHL = push(hlf.data(), hlf.size() * 4), offHD = push(hdf.data(), hdf.size() * 4),
+           offFD = push(fdf.data(), fdf.size() * 4);
     // filters
-    struct FFix { size_t nf, nh, of, oh, w; FilterDev *d; int maxt; };
+    struct FFix { size_t nf, nh, of, oh, w, wf; FilterDev *d; int maxt; };
     std::vector<FFix> ff;
     for (const Filter *f : {&g.big, &g.small1, &g.small2}) {
       std::vector<int> of(g.nlat), oh(g.nhalf);
@@ -328,6 +333,8 @@ struct Engine : EngineBase {
       x.of = push(of.data(), of.size() * 4);
       x.oh = push(oh.data(), oh.size() * 4);
       x.w = push(w.data(), w.size() * 8);
+      std::vector<float> wf(w.begin(), w.end());
+      x.wf = push(wf.data(), wf.size() * 4);
       x.d = f == &g.big ? &dg.big : f == &g.small1 ? &dg.small1 : &dg.small2;
       x.maxt = f->max_taps();
       ff.push_back(x);
@@ -337,12 +344,16 @@ struct Engine : EngineBase {
     for (const Fix &f : fixes) *f.dst = tables.base + f.off;
     dg.dmA = reinterpret_cast<const float *>(tables.base + offA);
     dg.dmB = reinterpret_cast<const float *>(tables.base + offB);
+    dg.half_lev_f = reinterpret_cast<const float *>(tables.base + offHL);
+    dg.half_dlev_f = reinterpret_cast<const float *>(tables.base + offHD);
+    dg.full_dlev_f = reinterpret_cast<const float *>(tables.base + offFD);
     for (const FFix &x : ff) {
       x.d->ntaps_full = reinterpret_cast<const int *>(tables.base + x.nf);
       x.d->ntaps_half = reinterpret_cast<const int *>(tables.base + x.nh);
       x.d->off_full = reinterpret_cast<const int *>(tables.base + x.of);
       x.d->off_half = reinterpret_cast<const int *>(tables.base + x.oh);
       x.d->wgt = reinterpret_cast<const double *>(tables.base + x.w);
+      x.d->wgt_f = reinterpret_cast<const float *>(tables.base + x.wf);
       x.d->max_taps = x.maxt;
     }
     const gmc_config &c = g.cfg;

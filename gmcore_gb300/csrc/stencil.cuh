@@ -2,6 +2,8 @@
 // PPM reconstruction, polar-filter row convolution.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace gmc {
@@ -87,14 +89,17 @@ __device__ __forceinline__ R ppm_tail(R sum, R fl, R df, R f6, R s1, R s2) {
 // Polar filter of one latitude row (filter_mod.F90:25-163): Gaussian
 // convolution with periodic wrap.  The row lives in shared memory; `ext`
 // receives the row extended by hn points on each side.  Returns false when
-// the row is not filtered (ngrid <= 1).  Accumulation is in FP64.
+// the row is not filtered (ngrid <= 1).  A is the accumulation type (FP64
+// unless the caller asks for the FP32 pipeline).
 // ---------------------------------------------------------------------------
-template <class R>
+template <class R, class A = double>
 __device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, int j, int nlon, R *row, R *ext) {
   const int n = full_lat ? f.ntaps_full[j - 1] : f.ntaps_half[j - 1];
   if (n <= 1) return false;
   const int hn = (n - 1) / 2;
-  const double *w = f.wgt + (full_lat ? f.off_full[j - 1] : f.off_half[j - 1]);
+  const int off = full_lat ? f.off_full[j - 1] : f.off_half[j - 1];
+  const A *w;
+  if constexpr (std::is_same<A, float>::value) w = f.wgt_f + off; else w = f.wgt + off;
   __syncthreads();
   for (int t = threadIdx.x; t < nlon + 2 * hn; t += blockDim.x) {
     int i = t - hn + 1;
@@ -103,8 +108,8 @@ __device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, in
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-    double s = 0;
-    for (int t = 0; t < n; ++t) s = s + w[t] * (double)ext[i + t];
+    A s = 0;
+    for (int t = 0; t < n; ++t) s = s + w[t] * (A)ext[i + t];
     row[i] = (R)s;
   }
   __syncthreads();
@@ -113,11 +118,25 @@ __device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, in
 
 // Vertical RK4 departure in eta and its Courant number
 // (adv_batch_accum_we_lev, adv_batch_mod.F90:525-628).  we and ml hold the
-// column's vertical mass flux and half-level mass, index [k-1].
-__device__ __forceinline__ double cflz_of(const DGrid &g, const double *we, const double *ml, int k, double dt_, bool &bad) {
+// column's vertical mass flux and half-level mass, index [k-1].  T = double
+// evaluates the reference's expressions in FP64; T = float runs the same
+// steps on the FP32 pipeline (eta is O(1), so FP32 resolves it to ~1e-7).
+template <class T>
+__device__ __forceinline__ const T *eta_table(const DGrid &g, int which);
+template <>
+__device__ __forceinline__ const double *eta_table<double>(const DGrid &g, int which) {
+  return which == 0 ? g.half_lev : which == 1 ? g.half_dlev : g.full_dlev;
+}
+template <>
+__device__ __forceinline__ const float *eta_table<float>(const DGrid &g, int which) {
+  return which == 0 ? g.half_lev_f : which == 1 ? g.half_dlev_f : g.full_dlev_f;
+}
+
+template <class T>
+__device__ __forceinline__ T cflz_of(const DGrid &g, const T *we, const T *ml, int k, T dt_, bool &bad) {
   const int nlev = g.nlev;
-  const double *HL = g.half_lev, *HD = g.half_dlev, *FD = g.full_dlev;   // [k-1]
-  auto locate = [&](double w, double z) {
+  const T *HL = eta_table<T>(g, 0), *HD = eta_table<T>(g, 1), *FD = eta_table<T>(g, 2);   // [k-1]
+  auto locate = [&](T w, T z) {
     int l;
     if (w > 0) {
       for (l = k; l <= nlev; ++l)
@@ -130,18 +149,18 @@ __device__ __forceinline__ double cflz_of(const DGrid &g, const double *we, cons
     }
     return l;
   };
-  auto interp = [&](int l, double z) {
+  auto interp = [&](int l, T z) {
     return ((HL[l] - z) * we[l - 1] / ml[l - 1] * HD[l - 1] + (z - HL[l - 1]) * we[l] / ml[l] * HD[l]) / FD[l - 1];
   };
-  double z0 = HL[k - 1];
-  double w1 = we[k - 1] / ml[k - 1] * HD[k - 1];
-  double z1 = z0 + dt_ / 2 * w1;
-  double w2 = interp(locate(w1, z1), z1);
-  double z2 = z0 + dt_ / 2 * w2;
-  double w3 = interp(locate(w2, z2), z2);
-  double z3 = z0 + dt_ * w3;
-  double w4 = interp(locate(w3, z3), z3);
-  double deta = (w1 + 2 * w2 + 2 * w3 + w4) / 6 * dt_;
+  T z0 = HL[k - 1];
+  T w1 = we[k - 1] / ml[k - 1] * HD[k - 1];
+  T z1 = z0 + dt_ / 2 * w1;
+  T w2 = interp(locate(w1, z1), z1);
+  T z2 = z0 + dt_ / 2 * w2;
+  T w3 = interp(locate(w2, z2), z2);
+  T z3 = z0 + dt_ * w3;
+  T w4 = interp(locate(w3, z3), z3);
+  T deta = (w1 + 2 * w2 + 2 * w3 + w4) / 6 * dt_;
   int ks, ke, s;
   if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
   deta = fabs(deta);
@@ -149,7 +168,7 @@ __device__ __forceinline__ double cflz_of(const DGrid &g, const double *we, cons
     deta = deta - FD[l - 1];
     if (deta < 0) return s * ((1 + deta / FD[l - 1]) + abs(l - ks));
   }
-  return NAN;   // departure left the column: the reference keeps the previous value
+  return (T)NAN;   // departure left the column: the reference keeps the previous value
 }
 
 }  // namespace gmc
