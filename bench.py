@@ -199,6 +199,16 @@ def run_ours(args):
     launches_per_step = stats["kernel_launches"] / args.steps
     ps_mixed = model.get_field("phs")   # after warmup + steps, compared with FP64 below
 
+    if args.device_only:
+        model.close()
+        if RANK == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "sim days/wall-day", "n_gpus": WORLD,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                              "device_only": True}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
     # ---- end to end through the C ABI with host buffers ----
     host = {k: np.ascontiguousarray(v) for k, v in st.items()}
     out = {k: np.empty_like(v) for k, v in host.items() if k != "q"}
@@ -359,6 +369,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--device-only", action="store_true",
+                    help="time only the device-resident mixed step (the case profiled under ncu)")
     args = ap.parse_args()
     if args.impl == "reference":
         if args.steps > 3:

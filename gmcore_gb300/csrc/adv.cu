@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.hpp"
 #include "stencil.cuh"
@@ -195,7 +196,7 @@ __global__ void k_pt_tendency(DGrid g, Slot<R> s, Work<R> w) {
     R f_bot = 0;
     if (k + 1 <= nlev) {
       const size_t ol = ix3(nlat, nlon, i, j, k + 1);
-      f_bot = vflx_at<R>(g, col, k + 1, w.cflz[ol], (R)s.we_lev[ol]);
+      f_bot = vflx_at<R>(g, col, k + 1, w.cflz[ol], s.we_lev[ol]);
     }
     R dlon, dlat;
     if (pole) {
@@ -228,15 +229,29 @@ __global__ void k_accum(T *dst, const T *src, size_t n, int mode, double divisor
 }
 
 // Half-level mass m_lev of calc_m (operators_mod.F90:505-525) folded into
-// the batch accumulator.
-__global__ void k_half_level_mass(DGrid g, const double *phs_f, double *m_lev, int mode, double divisor) {
+// the batch accumulator; sp.phs_f null zeroes the sample.  The FP32 form
+// takes (m(k-1) + m(k)) / 2 of the FP32 layer masses.
+template <class R>
+__global__ void k_half_level_mass(DGrid g, SurfP<R> sp, R *m_lev, int mode, double divisor) {
   const int j = blockIdx.y + 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
   if (i > nlon) return;
-  double ml[66];
-  if (phs_f) {
-    const double phs = phs_f[(size_t)(j - 1) * nlon + (i - 1)];
+  R ml[66];
+  const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
+  if (!sp.phs_f) {
+    for (int k = 0; k <= nlev; ++k) ml[k] = 0;
+  } else if constexpr (std::is_same<R, float>::value) {
+    const float psr = sp.at(c2);
+    float mprev = 0;
+    for (int k = 1; k <= nlev; ++k) {
+      float m = Mass<float>::layer(g, k, psr);
+      ml[k - 1] = 0.5f * (mprev + m);
+      mprev = m;
+    }
+    ml[nlev] = 0.5f * mprev;
+  } else {
+    const double phs = sp.phs_f[c2];
     double plo = ph_lev(g, 1, phs), ph_prev = 0;
     for (int k = 1; k <= nlev; ++k) {
       double phi = ph_lev(g, k + 1, phs);
@@ -246,19 +261,18 @@ __global__ void k_half_level_mass(DGrid g, const double *phs_f, double *m_lev, i
       plo = phi;
     }
     ml[nlev] = plo - ph_prev;
-  } else {
-    for (int k = 0; k <= nlev; ++k) ml[k] = 0;
   }
+  const R dv = (R)divisor;
   for (int k = 1; k <= nlev + 1; ++k) {
     size_t o = ix3(nlat, nlon, i, j, k);
     if (mode == 0) m_lev[o] = ml[k - 1];
     else if (mode == 1) m_lev[o] = m_lev[o] + ml[k - 1];
-    else m_lev[o] = (m_lev[o] + ml[k - 1]) / divisor;
+    else m_lev[o] = (m_lev[o] + ml[k - 1]) / dv;
   }
 }
 
 template <class R>
-__global__ void k_batch_cflz(DGrid g, const double *we_in, const double *ml_in, R *cflz, double dt) {
+__global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, double dt) {
   const int j = blockIdx.y + 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
@@ -266,13 +280,13 @@ __global__ void k_batch_cflz(DGrid g, const double *we_in, const double *ml_in, 
   R we[66], ml[66];
   for (int k = 1; k <= nlev + 1; ++k) {
     size_t o = ix3(nlat, nlon, i, j, k);
-    we[k - 1] = (R)we_in[o];
-    ml[k - 1] = (R)ml_in[o];
+    we[k - 1] = we_in[o];
+    ml[k - 1] = ml_in[o];
   }
   bool bad = false;
   for (int k = 2; k <= nlev; ++k) {
     R c = cflz_of<R>(g, we, ml, k, (R)dt, bad);
-    if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = (R)c;
+    if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = c;
   }
   if (bad) atomicOr(g.err, ERR_CFLZ);
 }
@@ -282,8 +296,8 @@ __global__ void k_batch_cflz(DGrid g, const double *we_in, const double *ml_in, 
 // it reads the longitude halo of q_new as the reference leaves it (the row's
 // values before this update, wrapped).
 template <class R>
-__global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *fx, const R *fy, const double *old_phs_f,
-                                    const double *phs_f, double dt_adv) {
+__global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *fx, const R *fy, SurfP<R> old_sp,
+                                    SurfP<R> sp, double dt_adv) {
   extern __shared__ double sh[];
   double *red = sh;
   R *row = reinterpret_cast<R *>(sh + 32);
@@ -308,8 +322,8 @@ __global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     const size_t o = ix3(nlat, nlon, i, j, k);
     const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
-    R om = Mass<R>::layer(g, k, old_phs_f[c2]);
-    R m = Mass<R>::layer(g, k, phs_f[c2]);
+    R om = Mass<R>::layer(g, k, old_sp.at(c2));
+    R m = Mass<R>::layer(g, k, sp.at(c2));
     R qn;
     if (!is_pole) {
       R a = (fx[o] - fx[ix3(nlat, nlon, wrap(i - 1, nlon), j, k)]) * lel;
@@ -326,8 +340,8 @@ __global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *
     neg |= qn < 0;
   }
   if (threadIdx.x == 0) {
-    mrow[0] = Mass<R>::layer(g, k, phs_f[(size_t)(j - 1) * nlon + (nlon - 1)]);
-    mrow[nlon + 1] = Mass<R>::layer(g, k, phs_f[(size_t)(j - 1) * nlon]);
+    mrow[0] = Mass<R>::layer(g, k, sp.at((size_t)(j - 1) * nlon + (nlon - 1)));
+    mrow[nlon + 1] = Mass<R>::layer(g, k, sp.at((size_t)(j - 1) * nlon));
   }
   if (__syncthreads_or(neg) && threadIdx.x == 0) {
     for (int i = 1; i <= nlon; ++i) {
@@ -355,7 +369,7 @@ __global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *
 // Vertical FFSL of the tracer column with copied ghost levels, then the
 // vertical negative fixer (adv_mod.F90:259-297).
 template <class R>
-__global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const double *we, const double *phs_f, double dt_adv) {
+__global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const R *we, SurfP<R> sp, double dt_adv) {
   const int j = blockIdx.y + 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
@@ -364,13 +378,13 @@ __global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const double *we
   for (int k = 1; k <= nlev; ++k) col[k + 1] = q[ix3(nlat, nlon, i, j, k)];
   col[1] = col[0] = col[2];
   col[nlev + 2] = col[nlev + 3] = col[nlev + 1];
-  const double phs = phs_f[(size_t)(j - 1) * nlon + (i - 1)];
-  for (int k = 1; k <= nlev; ++k) m[k - 1] = Mass<R>::layer(g, k, phs);
+  const auto ps = sp.at((size_t)(j - 1) * nlon + (i - 1));
+  for (int k = 1; k <= nlev; ++k) m[k - 1] = Mass<R>::layer(g, k, ps);
   mz[0] = 0;
   mz[nlev] = 0;
   for (int k = 2; k <= nlev; ++k) {
     size_t o = ix3(nlat, nlon, i, j, k);
-    mz[k - 1] = vflx_at<R>(g, col, k, cflz[o], (R)we[o]);
+    mz[k - 1] = vflx_at<R>(g, col, k, cflz[o], we[o]);
   }
   R *qc = col + 1;   // qc[k] = q(k)
   const R dta = (R)dt_adv;
@@ -458,29 +472,30 @@ void launch_accum(const Launch &L, T *dst, const T *src, size_t n, int mode, dou
 template void launch_accum<double>(const Launch &, double *, const double *, size_t, int, double);
 template void launch_accum<float>(const Launch &, float *, const float *, size_t, int, double);
 
-void launch_half_level_mass(const DGrid &g, const Launch &L, const double *phs_f, double *m_lev, int mode, double divisor) {
+template <class R>
+void launch_half_level_mass(const DGrid &g, const Launch &L, const SurfP<R> &sp, R *m_lev, int mode, double divisor) {
   const int bt = 64;
-  k_half_level_mass<<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, phs_f, m_lev, mode, divisor);
+  k_half_level_mass<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, sp, m_lev, mode, divisor);
 }
 
 template <class R>
-void launch_batch_cflz(const DGrid &g, const Launch &L, const double *we, const double *m_lev, R *cflz, double dt) {
+void launch_batch_cflz(const DGrid &g, const Launch &L, const R *we, const R *m_lev, R *cflz, double dt) {
   const int bt = 64;
   k_batch_cflz<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, we, m_lev, cflz, dt);
 }
 
 template <class R>
 void launch_tracer_horizontal(const DGrid &g, const Launch &L, const R *q_old, R *q_new, const R *fx, const R *fy,
-                              const double *old_phs_f, const double *phs_f, double dt_adv) {
+                              const SurfP<R> &old_sp, const SurfP<R> &sp, double dt_adv) {
   size_t smem = 32 * sizeof(double) + 2 * (g.nlon + 2) * sizeof(R) + 16;
-  k_tracer_horizontal<R><<<dim3(g.nlat, g.nlev), L.threads, smem, L.stream>>>(g, q_old, q_new, fx, fy, old_phs_f, phs_f, dt_adv);
+  k_tracer_horizontal<R><<<dim3(g.nlat, g.nlev), L.threads, smem, L.stream>>>(g, q_old, q_new, fx, fy, old_sp, sp, dt_adv);
 }
 
 template <class R>
-void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const double *we, const double *phs_f,
+void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const R *we, const SurfP<R> &sp,
                             double dt_adv) {
   const int bt = 64;
-  k_tracer_vertical<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, q, cflz, we, phs_f, dt_adv);
+  k_tracer_vertical<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, q, cflz, we, sp, dt_adv);
 }
 
 template <class R>
@@ -489,11 +504,12 @@ void launch_tracer_lon_damp(const DGrid &g, const Launch &L, R *q) {
 }
 
 #define INST_TRACER(R)                                                                                              \
-  template void launch_batch_cflz<R>(const DGrid &, const Launch &, const double *, const double *, R *, double); \
+  template void launch_half_level_mass<R>(const DGrid &, const Launch &, const SurfP<R> &, R *, int, double);      \
+  template void launch_batch_cflz<R>(const DGrid &, const Launch &, const R *, const R *, R *, double);           \
   template void launch_tracer_horizontal<R>(const DGrid &, const Launch &, const R *, R *, const R *, const R *,  \
-                                            const double *, const double *, double);                             \
-  template void launch_tracer_vertical<R>(const DGrid &, const Launch &, R *, const R *, const double *,           \
-                                          const double *, double);                                               \
+                                            const SurfP<R> &, const SurfP<R> &, double);                         \
+  template void launch_tracer_vertical<R>(const DGrid &, const Launch &, R *, const R *, const R *,                \
+                                          const SurfP<R> &, double);                                             \
   template void launch_tracer_lon_damp<R>(const DGrid &, const Launch &, R *);
 INST_TRACER(double)
 INST_TRACER(float)

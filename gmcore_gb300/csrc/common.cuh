@@ -56,6 +56,17 @@ struct DGrid {
   const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
   const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables
+  const float *hybi_f;                                             // FP32 copy of hybi [k-1]
+  // FP32 column sweep about a reference column with surface pressure ps_ref
+  // (pressures p_ref on half levels, ph_ref on full levels):
+  //   pr_c[k-1]    = hybi(k) / p_ref(k)              k = 1..nlev+1
+  //   pe_ref[k-1]  = p_ref(k)^kappa                  k = 1..nlev+1
+  //   dpe_ref[k-1] = p_ref(k+1)^kappa - p_ref(k)^kappa   k = 1..nlev
+  //   cf[k-1]      = (hybi(k) + hybi(k+1)) / 2 / ph_ref(k)
+  //   tf_ref[k-1]  = (ph_ref(k) / p0)^kappa
+  //   dlnp_ref[k-1] = ln(p_ref(k+1) / p_ref(k))
+  const float *pr_c, *pe_ref, *dpe_ref, *cf, *tf_ref, *dlnp_ref;
+  double ps_ref;
   const double *lon_damp_full;                                     // [j-1]
   const double *div_c_lon, *div_c_lat;                             // [(k-1)*n + j-1]
   FilterDev big, small1, small2;
@@ -63,6 +74,23 @@ struct DGrid {
 };
 
 #define ROW(t, j) ((t)[(j) + 1])
+
+// Surface pressure as the layer-mass formula of each form reads it: the FP64
+// form takes phs_f, the FP32 form psr = phs_f - ptop rounded once to FP32.
+template <class R>
+struct SurfP;
+template <>
+struct SurfP<double> {
+  const double *phs_f;
+  const float *psr;
+  __device__ __forceinline__ double at(size_t o) const { return phs_f[o]; }
+};
+template <>
+struct SurfP<float> {
+  const double *phs_f;
+  const float *psr;
+  __device__ __forceinline__ float at(size_t o) const { return psr[o]; }
+};
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); }
 

@@ -7,6 +7,7 @@
 // Reference routines are cited per kernel.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "kernels.hpp"
@@ -18,7 +19,7 @@ namespace {
 
 template <class R>
 __device__ __forceinline__ MassField<R> mass_of(const DGrid &g, const Slot<R> &s) {
-  return MassField<R>{s.phs_f, s.gz, s.gzs};
+  return MassField<R>{s.surf(), s.gz, s.gzs};
 }
 
 // ---------------------------------------------------------------------------
@@ -363,54 +364,98 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
     __syncthreads();
   }
   if (i > nlon) return;
-  typedef typename std::conditional<std::is_same<R, float>::value, float, double>::type T;
-  double mfp[66];
-  T we[66], ml[66];
-  const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
-  const int im = wrap(i - 1, nlon);
-  double dphs = 0, mf = 0;
-  for (int k = 1; k <= nlev; ++k) {
-    double dlon, dlat;
-    if (pole) {
-      dlon = 0;
-      dlat = ring[k - 1];
-    } else {
-      dlon = ((double)s.mfx_lon[ix3(nlat, nlon, i, j, k)] - (double)s.mfx_lon[ix3(nlat, nlon, im, j, k)]) * lel / ac;
-      dlat = ((double)s.mfy_lat[ix3(nhalf, nlon, i, j, k)] * la0 - (double)s.mfy_lat[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
-    }
-    dphs = dphs - dlon - dlat;
-    mf = mf + dlon + dlat;
-    mfp[k - 1] = mf;
-  }
   const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
-  w.dphs[c2] = dphs;
-  s.we_lev[ix3(nlat, nlon, i, j, 1)] = 0;
-  we[0] = 0;
-  for (int k = 2; k <= nlev; ++k) {
-    double wv = -(g.hybi[k - 1] * dphs) - mfp[k - 2];
-    s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
-    we[k - 1] = (T)wv;
+  const int im = wrap(i - 1, nlon);
+  if constexpr (std::is_same<R, float>::value) {
+    // FP32 form: divergences with per-row reciprocal factors, layer masses
+    // from psr, all on the FP32 pipeline.
+    const double ac = ROW(g.area_cell, j);
+    const float clon = (float)(ROW(g.le_lon, j) / ac), cn = (float)(ROW(g.le_lat, j) / ac),
+                cs = (float)(ROW(g.le_lat, j - 1) / ac);
+    float mfp[66], we[66], ml[66];
+    float mf = 0;
+    for (int k = 1; k <= nlev; ++k) {
+      float d;
+      if (pole) {
+        d = (float)ring[k - 1];
+      } else {
+        d = (s.mfx_lon[ix3(nlat, nlon, i, j, k)] - s.mfx_lon[ix3(nlat, nlon, im, j, k)]) * clon +
+            (s.mfy_lat[ix3(nhalf, nlon, i, j, k)] * cn - s.mfy_lat[ix3(nhalf, nlon, i, j - 1, k)] * cs);
+      }
+      mf = mf + d;
+      mfp[k - 1] = mf;
+    }
+    const float dphs = -mf;
+    w.dphs[c2] = (double)dphs;
+    s.we_lev[ix3(nlat, nlon, i, j, 1)] = 0;
+    we[0] = 0;
+    for (int k = 2; k <= nlev; ++k) {
+      float wv = -(g.hybi_f[k - 1] * dphs) - mfp[k - 2];
+      s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
+      we[k - 1] = wv;
+    }
+    we[nlev] = 0;
+    s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
+    // half-level mass: (m(k-1) + m(k)) / 2, half layers at the ends
+    const float psr = s.psr[c2];
+    float mprev = 0;
+    for (int k = 1; k <= nlev; ++k) {
+      float m = Mass<float>::layer(g, k, psr);
+      ml[k - 1] = 0.5f * (mprev + m);
+      mprev = m;
+    }
+    ml[nlev] = 0.5f * mprev;
+    bool bad = false;
+    for (int k = 2; k <= nlev; ++k) {
+      float c = cflz_of<float>(g, we, ml, k, (float)dt, bad);
+      if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
+    }
+    if (bad) atomicOr(g.err, ERR_CFLZ);
+  } else {
+    double mfp[66], we[66], ml[66];
+    const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
+    double dphs = 0, mf = 0;
+    for (int k = 1; k <= nlev; ++k) {
+      double dlon, dlat;
+      if (pole) {
+        dlon = 0;
+        dlat = ring[k - 1];
+      } else {
+        dlon = ((double)s.mfx_lon[ix3(nlat, nlon, i, j, k)] - (double)s.mfx_lon[ix3(nlat, nlon, im, j, k)]) * lel / ac;
+        dlat = ((double)s.mfy_lat[ix3(nhalf, nlon, i, j, k)] * la0 - (double)s.mfy_lat[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
+      }
+      dphs = dphs - dlon - dlat;
+      mf = mf + dlon + dlat;
+      mfp[k - 1] = mf;
+    }
+    w.dphs[c2] = dphs;
+    s.we_lev[ix3(nlat, nlon, i, j, 1)] = 0;
+    we[0] = 0;
+    for (int k = 2; k <= nlev; ++k) {
+      double wv = -(g.hybi[k - 1] * dphs) - mfp[k - 2];
+      s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
+      we[k - 1] = wv;
+    }
+    we[nlev] = 0;
+    s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
+    // half-level mass from the hybrid pressures (calc_m, operators_mod.F90:505-525)
+    const double phs = s.phs_f[c2];
+    double plo = ph_lev(g, 1, phs), ph_prev = 0;
+    for (int k = 1; k <= nlev; ++k) {
+      double phi = ph_lev(g, k + 1, phs);
+      double ph = 0.5 * (plo + phi);
+      ml[k - 1] = k == 1 ? ph - plo : ph - ph_prev;
+      ph_prev = ph;
+      plo = phi;
+    }
+    ml[nlev] = plo - ph_prev;
+    bool bad = false;
+    for (int k = 2; k <= nlev; ++k) {
+      double c = cflz_of<double>(g, we, ml, k, dt, bad);
+      if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = (R)c;
+    }
+    if (bad) atomicOr(g.err, ERR_CFLZ);
   }
-  we[nlev] = 0;
-  s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
-  // half-level mass from the hybrid pressures (calc_m, operators_mod.F90:505-525)
-  const double phs = s.phs_f[c2];
-  double plo = ph_lev(g, 1, phs), ph_prev = 0;
-  for (int k = 1; k <= nlev; ++k) {
-    double phi = ph_lev(g, k + 1, phs);
-    double ph = 0.5 * (plo + phi);
-    ml[k - 1] = (T)(k == 1 ? ph - plo : ph - ph_prev);
-    ph_prev = ph;
-    plo = phi;
-  }
-  ml[nlev] = (T)(plo - ph_prev);
-  bool bad = false;
-  for (int k = 2; k <= nlev; ++k) {
-    T c = cflz_of<T>(g, we, ml, k, (T)dt, bad);
-    size_t o = ix3(nlat, nlon, i, j, k);
-    if (c == c) w.cflz[o] = (R)c;
-  }
-  if (bad) atomicOr(g.err, ERR_CFLZ);
 }
 
 // Momentum tendencies of the forward pass (gmcore_mod.F90:478-490 / 507-518):
@@ -444,7 +489,7 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
       R du = qhv - dkedlon;
       if (g.baroclinic) {
         auto WEL = [&](int kk) {
-          R a = (R)s.we_lev[ix3(nlat, nlon, i, j, kk)], b = (R)s.we_lev[ix3(nlat, nlon, wrap(i + 1, nlon), j, kk)];
+          R a = s.we_lev[ix3(nlat, nlon, i, j, kk)], b = s.we_lev[ix3(nlat, nlon, wrap(i + 1, nlon), j, kk)];
           return (aw * a + ae * b) / al;
         };
         auto Uk = [&](int kk) { return s.u_f[ix3(nlat, nlon, i, j, kk)]; };
@@ -479,7 +524,7 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
       R dv = -qhu - dkedlat;
       if (g.baroclinic) {
         auto WEL = [&](int kk) {
-          R a = (R)s.we_lev[ix3(nlat, nlon, i, j + 1, kk)], b = (R)s.we_lev[ix3(nlat, nlon, i, j, kk)];
+          R a = s.we_lev[ix3(nlat, nlon, i, j + 1, kk)], b = s.we_lev[ix3(nlat, nlon, i, j, kk)];
           return (an * a + as * b) / al;
         };
         auto Vk = [&](int kk) { return s.v_f[ix3(nhalf, nlon, i, j, kk)]; };
@@ -544,7 +589,16 @@ __global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt
   }
   filter_row<double>(g.big, true, j, nlon, row, ext);
   __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.phs_f[(size_t)(j - 1) * nlon + i] = row[i];
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    n.phs_f[(size_t)(j - 1) * nlon + i] = row[i];
+    if (n.psr) n.psr[(size_t)(j - 1) * nlon + i] = (float)(row[i] - g.ptop);
+  }
+}
+
+// FP32 form: psr = phs_f - ptop
+__global__ void k_surface_rel(const double *phs_f, float *psr, size_t n, double ptop) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    psr[t] = (float)(phs_f[t] - ptop);
 }
 
 // pt = small1 filter(pt_old m_old + dt dpt) / m_new   (:153-173)
@@ -555,14 +609,14 @@ __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   R *row = reinterpret_cast<R *>(sh), *ext = row + nlon;
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     size_t c = ix3(nlat, nlon, i + 1, j, k);
-    R m_old = Mass<R>::layer(g, k, o.phs_f[(size_t)(j - 1) * nlon + i]);
+    R m_old = Mass<R>::layer(g, k, o.surf().at((size_t)(j - 1) * nlon + i));
     row[i] = o.pt[c] * m_old + (R)dt * w.dpt[c];
   }
-  filter_row<R>(g.small1, true, j, nlon, row, ext);
+  filter_row<R, R>(g.small1, true, j, nlon, row, ext);
   __syncthreads();
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     size_t c = ix3(nlat, nlon, i + 1, j, k);
-    R m_new = Mass<R>::layer(g, k, n.phs_f[(size_t)(j - 1) * nlon + i]);
+    R m_new = Mass<R>::layer(g, k, n.surf().at((size_t)(j - 1) * nlon + i));
     n.pt[c] = row[i] / m_new;
   }
 }
@@ -600,27 +654,39 @@ __global__ void k_column_backward(DGrid g, Slot<R> n, Work<R> w) {
   const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
   const double phs = n.phs_f[c2];
   const double gzs = n.gzs[c2];
-  w.gz_lev[ix3(nlat, nlon, i, j, nlev + 1)] = gzs;
   if constexpr (std::is_same<R, float>::value) {
-    // FP32 transcendentals, FP64 pressures and geopotential accumulation:
-    // ln(p(k+1)/p(k)) = log1p(dp/p) with dp, p from FP64 keeps ~1e-7 relative
-    // accuracy however thin the layer.
-    const float kap = (float)g.kappa;
-    double p_hi = ph_lev(g, nlev + 1, phs);
-    w.ph_exn_lev[ix3(nlat, nlon, i, j, nlev + 1)] = (double)powf((float)p_hi, kap);
-    double acc = 0;
+    // FP32 form about the reference column: p(k) = p_ref(k) (1 + r(k)) with
+    // r(k) = pr_c(k) (phs - ps_ref), so
+    //   p^kappa       = pe_ref(k) + pe_ref(k) expm1(kappa log1p(r))   (pea holds the second term)
+    //   ln(p(k+1)/p(k)) = dlnp_ref(k) + log1p(r(k+1)) - log1p(r(k))
+    //   (ph/p0)^kappa = tf_ref(k) exp(kappa log1p(rf)),  rf = cf(k) (phs - ps_ref).
+    // Every FP32 quantity is either small or relative, and the geopotential
+    // is summed upward as an unevaluated (hi, lo) FP32 pair, so differences
+    // between neighbours keep ~1e-7 relative accuracy without FP64 issue.
+    const float kap = (float)g.kappa, Rd = (float)g.Rd;
+    const float dps = (float)(phs - g.ps_ref);
+    float hi = (float)gzs;
+    float lo = (float)(gzs - (double)hi);
+    w.gzhl[ix3(nlat, nlon, i, j, nlev + 1)] = make_float2(hi, lo);
+    float L_hi = log1pf(g.pr_c[nlev] * dps);
+    w.pea[ix3(nlat, nlon, i, j, nlev + 1)] = g.pe_ref[nlev] * expm1f(kap * L_hi);
     for (int k = nlev; k >= 1; --k) {
-      double p_lo = ph_lev(g, k, phs);
-      w.ph_exn_lev[ix3(nlat, nlon, i, j, k)] = (double)powf((float)p_lo, kap);
-      double ph = 0.5 * (p_lo + p_hi);
-      float t = n.pt[ix3(nlat, nlon, i, j, k)] * powf((float)(ph / g.p0), kap);
-      float dlnp = log1pf((float)((p_hi - p_lo) / p_lo));
-      acc = (double)((float)g.Rd * t * dlnp) + acc;
-      w.gz_lev[ix3(nlat, nlon, i, j, k)] = gzs + acc;
-      p_hi = p_lo;
+      const float L_lo = log1pf(g.pr_c[k - 1] * dps);
+      w.pea[ix3(nlat, nlon, i, j, k)] = g.pe_ref[k - 1] * expm1f(kap * L_lo);
+      const float t = n.pt[ix3(nlat, nlon, i, j, k)] * (g.tf_ref[k - 1] * expf(kap * log1pf(g.cf[k - 1] * dps)));
+      const float x = Rd * t * (g.dlnp_ref[k - 1] + (L_hi - L_lo));
+      // (hi, lo) += x: two-sum, then renormalise
+      const float s1 = hi + x, bp = s1 - hi;
+      const float e = (hi - (s1 - bp)) + (x - bp);
+      lo = lo + e;
+      hi = s1 + lo;
+      lo = lo - (hi - s1);
+      w.gzhl[ix3(nlat, nlon, i, j, k)] = make_float2(hi, lo);
+      L_hi = L_lo;
     }
     return;
   }
+  w.gz_lev[ix3(nlat, nlon, i, j, nlev + 1)] = gzs;
   double pl[66];
   for (int k = 1; k <= nlev + 1; ++k) {
     pl[k - 1] = ph_lev(g, k, phs);
@@ -639,11 +705,26 @@ __global__ void k_column_backward(DGrid g, Slot<R> n, Work<R> w) {
 // to the poles; big filter into u_f, v_f   (time_schemes_mod.F90:198-238,
 // pgf_lin97_run pgf_lin97_mod.F90:59-105, pgf_swm_run pgf_swm_mod.F90:18-46,
 // backward pass gmcore_mod.F90:529-571).
+// Difference of two (hi, lo) FP32 pairs: the hi parts of neighbouring
+// geopotentials are within a factor two of each other, so their difference is
+// exact and the result carries the pair's full accuracy.
+__device__ __forceinline__ float hl_diff(float2 a, float2 b) { return (a.x - b.x) + (a.y - b.y); }
+
 template <class R>
-__device__ __forceinline__ R pgf_lon(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k) {
+__device__ __forceinline__ R pgf_lon(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k, R inv_d) {
   const int nlat = g.nlat, nlon = g.nlon;
   const int ip = wrap(i + 1, nlon);
   if (g.baroclinic) {
+    if constexpr (std::is_same<R, float>::value) {
+      const float *pa = w.pea;
+      const float2 *gz = w.gzhl;
+      const float dref = g.dpe_ref[k - 1];
+      float dph1 = dref + (pa[ix3(nlat, nlon, ip, j, k + 1)] - pa[ix3(nlat, nlon, i, j, k)]);
+      float dph2 = dref + (pa[ix3(nlat, nlon, i, j, k + 1)] - pa[ix3(nlat, nlon, ip, j, k)]);
+      float dgz1 = hl_diff(gz[ix3(nlat, nlon, i, j, k + 1)], gz[ix3(nlat, nlon, ip, j, k)]);
+      float dgz2 = hl_diff(gz[ix3(nlat, nlon, i, j, k)], gz[ix3(nlat, nlon, ip, j, k + 1)]);
+      return -(dph1 * dgz1 + dph2 * dgz2) * inv_d / (dph1 + dph2);
+    }
     const double *pe = w.ph_exn_lev, *gz = w.gz_lev;
     double dph1 = pe[ix3(nlat, nlon, ip, j, k + 1)] - pe[ix3(nlat, nlon, i, j, k)];
     double dph2 = pe[ix3(nlat, nlon, i, j, k + 1)] - pe[ix3(nlat, nlon, ip, j, k)];
@@ -654,9 +735,19 @@ __device__ __forceinline__ R pgf_lon(const DGrid &g, const Slot<R> &n, const Wor
   return (n.gz_f[ix3(nlat, nlon, ip, j, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / (R)ROW(g.de_lon, j);
 }
 template <class R>
-__device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k) {
+__device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k, R inv_d) {
   const int nlat = g.nlat, nlon = g.nlon;
   if (g.baroclinic) {
+    if constexpr (std::is_same<R, float>::value) {
+      const float *pa = w.pea;
+      const float2 *gz = w.gzhl;
+      const float dref = g.dpe_ref[k - 1];
+      float dph1 = dref + (pa[ix3(nlat, nlon, i, j + 1, k + 1)] - pa[ix3(nlat, nlon, i, j, k)]);
+      float dph2 = dref + (pa[ix3(nlat, nlon, i, j, k + 1)] - pa[ix3(nlat, nlon, i, j + 1, k)]);
+      float dgz1 = hl_diff(gz[ix3(nlat, nlon, i, j, k + 1)], gz[ix3(nlat, nlon, i, j + 1, k)]);
+      float dgz2 = hl_diff(gz[ix3(nlat, nlon, i, j, k)], gz[ix3(nlat, nlon, i, j + 1, k + 1)]);
+      return -(dph1 * dgz1 + dph2 * dgz2) * inv_d / (dph1 + dph2);
+    }
     const double *pe = w.ph_exn_lev, *gz = w.gz_lev;
     double dph1 = pe[ix3(nlat, nlon, i, j + 1, k + 1)] - pe[ix3(nlat, nlon, i, j, k)];
     double dph2 = pe[ix3(nlat, nlon, i, j, k + 1)] - pe[ix3(nlat, nlon, i, j + 1, k)];
@@ -682,9 +773,10 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
       }
       return;
     }
+    const R inv_d = (R)(1.0 / ROW(g.de_lon, j));
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
       size_t c = ix3(nlat, nlon, i + 1, j, k);
-      row[i] = o.u_lon[c] + (R)dt * (w.du[c] - pgf_lon(g, n, w, i + 1, j, k));
+      row[i] = o.u_lon[c] + (R)dt * (w.du[c] - pgf_lon(g, n, w, i + 1, j, k, inv_d));
     }
     if (g.baroclinic) filter_row<R, R>(g.small2, true, j, nlon, row, ext);
     __syncthreads();
@@ -696,9 +788,10 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   }
   const int j = blockIdx.x - nlat + 1;
   auto load_v = [&](int jj, R *dst) {
+    const R inv_d = (R)(1.0 / ROW(g.de_lat, jj));
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
       size_t c = ix3(nhalf, nlon, i + 1, jj, k);
-      dst[i] = o.v_lat[c] + (R)dt * (w.dv[c] - pgf_lat(g, n, w, i + 1, jj, k));
+      dst[i] = o.v_lat[c] + (R)dt * (w.dv[c] - pgf_lat(g, n, w, i + 1, jj, k, inv_d));
     }
     if (g.baroclinic) filter_row<R, R>(g.small2, false, jj, nlon, dst, ext);
     __syncthreads();
@@ -879,6 +972,12 @@ void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s) {
     k_filter_copy<R, R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, s.gz, s.gz_f, 0, 1, g.nlat);
 }
 template <class R>
+void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s) {
+  if (!s.psr || !s.phs_f) return;
+  const size_t n = (size_t)g.nlat * g.nlon;
+  k_surface_rel<<<(int)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, L.stream>>>(s.phs_f, s.psr, n, g.ptop);
+}
+template <class R>
 void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out) {
   (void)w;
   k_diag_partial<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, partial);
@@ -899,6 +998,7 @@ void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Wo
   template void launch_update_pt<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
   template void launch_update_gz<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
   template void launch_column_backward<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);       \
+  template void launch_surface_rel<R>(const DGrid &, const Launch &, const Slot<R> &);                             \
   template void launch_update_uv<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
   template void launch_filter_prologue<R>(const DGrid &, const Launch &, const Slot<R> &);                        \
   template void launch_diagnose<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &, double *, double *);

@@ -9,6 +9,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "gmcore_gpu.h"
@@ -136,6 +137,8 @@ struct Engine : EngineBase {
   double alert_last = 0, curr_time = 0;
   bool alert_ring = false;
 
+  static constexpr bool kFP32 = std::is_same<R, float>::value;
+
   size_t full3() const { return (size_t)grid.nlev * grid.nlat * grid.nlon; }
   size_t half3() const { return (size_t)grid.nlev * grid.nhalf * grid.nlon; }
   size_t lev3() const { return (size_t)(grid.nlev + 1) * grid.nlat * grid.nlon; }
@@ -156,13 +159,15 @@ struct Engine : EngineBase {
       s.pt = a.template take<R>(full3());
       s.phs = a.template take<double>(two_d());
       s.phs_f = a.template take<double>(two_d());
-      s.we_lev = a.template take<double>(lev3());
+      s.psr = kFP32 ? a.template take<float>(two_d()) : nullptr;
+      s.we_lev = a.template take<R>(lev3());
       s.gz = s.gz_f = nullptr;
     } else {
       s.gz = a.template take<R>(two_d());
       s.gz_f = a.template take<R>(two_d());
       s.pt = nullptr;
       s.phs = s.phs_f = nullptr;
+      s.psr = nullptr;
       s.we_lev = nullptr;
     }
   }
@@ -189,12 +194,16 @@ struct Engine : EngineBase {
       w.dphs = a.template take<double>(two_d());
       w.ph_exn_lev = a.template take<double>(lev3());
       w.gz_lev = a.template take<double>(lev3());
+      w.pea = kFP32 ? reinterpret_cast<float *>(w.ph_exn_lev) : nullptr;
+      w.gzhl = kFP32 ? reinterpret_cast<float2 *>(w.gz_lev) : nullptr;
       w.dgz = nullptr;
     } else {
       w.dgz = a.template take<R>(two_d());
       w.cflx = w.cfly = w.cflz = w.divx = w.divy = nullptr;
       w.qmfx = w.qmfy = w.qx = w.qy = w.ptf_lon = w.ptf_lat = w.dpt = nullptr;
       w.dphs = w.ph_exn_lev = w.gz_lev = nullptr;
+      w.pea = nullptr;
+      w.gzhl = nullptr;
     }
   }
 
@@ -215,14 +224,15 @@ struct Engine : EngineBase {
       b.v = a.template take<R>(half3());
       b.mfx = a.template take<R>(full3());
       b.mfy = a.template take<R>(half3());
-      b.we = a.template take<double>(lev3());
-      b.m_lev = a.template take<double>(lev3());
+      b.we = a.template take<R>(lev3());
+      b.m_lev = a.template take<R>(lev3());
       b.cflx = a.template take<R>(full3());
       b.cfly = a.template take<R>(half3());
       b.divx = a.template take<R>(full3());
       b.divy = a.template take<R>(full3());
       b.cflz = a.template take<R>(lev3());
       b.old_phs_f = a.template take<double>(two_d());
+      b.old_psr = kFP32 ? a.template take<float>(two_d()) : nullptr;
       for (int t = 0; t < 2 * ntr; ++t) q[(size_t)m * 2 * ntr + t] = a.template take<R>(full3());
     }
   }
@@ -318,6 +328,33 @@ struct Engine : EngineBase {
     hlf.push_back(0.f); hdf.push_back(0.f); fdf.push_back(0.f);
     size_t offHL = push(hlf.data(), hlf.size() * 4), offHD = push(hdf.data(), hdf.size() * 4),
            offFD = push(fdf.data(), fdf.size() * 4);
+    std::vector<float> hbf(g.hybi.begin(), g.hybi.end());
+    hbf.push_back(0.f);
+    size_t offHB = push(hbf.data(), hbf.size() * 4);
+    // FP32 column sweep about a reference column at ps_ref = p0
+    const int nl = g.nlev;
+    const double ps_ref = g.cfg.p0, kap = g.cfg.Rd / g.cfg.cpd;
+    std::vector<float> prc(nl + 2, 0.f), per(nl + 2, 0.f), dper(nl + 1, 0.f), cff(nl + 1, 0.f), tfr(nl + 1, 0.f),
+        dlr(nl + 1, 0.f);
+    if (g.cfg.baroclinic) {
+      std::vector<double> pr(nl + 1), pe(nl + 1);
+      for (int k = 0; k <= nl; ++k) {
+        pr[k] = g.hyai[k] * (g.cfg.hybrid_coord_p0 - g.local_ptop) + g.hybi[k] * (ps_ref - g.local_ptop) + g.local_ptop;
+        pe[k] = std::pow(pr[k], kap);
+        prc[k] = (float)(g.hybi[k] / pr[k]);
+        per[k] = (float)pe[k];
+      }
+      for (int k = 0; k < nl; ++k) {
+        const double ph = 0.5 * (pr[k] + pr[k + 1]);
+        dper[k] = (float)(pe[k + 1] - pe[k]);
+        cff[k] = (float)(0.5 * (g.hybi[k] + g.hybi[k + 1]) / ph);
+        tfr[k] = (float)std::pow(ph / g.cfg.p0, kap);
+        dlr[k] = (float)std::log(pr[k + 1] / pr[k]);
+      }
+    }
+    const size_t offPRC = push(prc.data(), prc.size() * 4), offPER = push(per.data(), per.size() * 4),
+                 offDPER = push(dper.data(), dper.size() * 4), offCF = push(cff.data(), cff.size() * 4),
+                 offTF = push(tfr.data(), tfr.size() * 4), offDL = push(dlr.data(), dlr.size() * 4);
     // filters
     struct FFix { size_t nf, nh, of, oh, w, wf; FilterDev *d; int maxt; };
     std::vector<FFix> ff;
@@ -347,6 +384,14 @@ struct Engine : EngineBase {
     dg.half_lev_f = reinterpret_cast<const float *>(tables.base + offHL);
     dg.half_dlev_f = reinterpret_cast<const float *>(tables.base + offHD);
     dg.full_dlev_f = reinterpret_cast<const float *>(tables.base + offFD);
+    dg.hybi_f = reinterpret_cast<const float *>(tables.base + offHB);
+    dg.pr_c = reinterpret_cast<const float *>(tables.base + offPRC);
+    dg.pe_ref = reinterpret_cast<const float *>(tables.base + offPER);
+    dg.dpe_ref = reinterpret_cast<const float *>(tables.base + offDPER);
+    dg.cf = reinterpret_cast<const float *>(tables.base + offCF);
+    dg.tf_ref = reinterpret_cast<const float *>(tables.base + offTF);
+    dg.dlnp_ref = reinterpret_cast<const float *>(tables.base + offDL);
+    dg.ps_ref = ps_ref;
     for (const FFix &x : ff) {
       x.d->ntaps_full = reinterpret_cast<const int *>(tables.base + x.nf);
       x.d->ntaps_half = reinterpret_cast<const int *>(tables.base + x.nh);
@@ -396,7 +441,7 @@ struct Engine : EngineBase {
     else if (name == "gz_f" && !bc) *pr = s.gz_f;
     else if (name == "phs" && bc) *pd = s.phs;
     else if (name == "phs_f" && bc) *pd = s.phs_f;
-    else if (name == "we_lev" && bc) *pd = s.we_lev;
+    else if (name == "we_lev" && bc) *pr = s.we_lev;
     else if (name == "gzs") *pd = gzs[m];
     if (!*pr && !*pd) throw ApiError{GMC_EINVAL, "unknown field '" + name + "' for this model"};
   }
@@ -517,8 +562,8 @@ struct Engine : EngineBase {
     });
     cycle(we_step, mode);
     K("tracer_accum", 2, [&] {
-      launch_accum<double>(L, b.we, prologue ? nullptr : s.we_lev, lev3(), mode, div);
-      launch_half_level_mass(dg, L, prologue ? nullptr : s.phs_f, b.m_lev, mode, div);
+      launch_accum<R>(L, b.we, prologue ? nullptr : s.we_lev, lev3(), mode, div);
+      launch_half_level_mass<R>(dg, L, prologue ? SurfP<R>{nullptr, nullptr} : s.surf(), b.m_lev, mode, div);
     });
     if (we_step == 0) K("tracer_batch_cflz", 1, [&] { launch_batch_cflz<R>(dg, L, b.we, b.m_lev, b.cflz, dt_adv); });
   }
@@ -536,13 +581,14 @@ struct Engine : EngineBase {
       for (int l = 0; l < ntr; ++l) {
         R *qo = q[((size_t)m * 2 + q_old) * ntr + l], *qn = q[((size_t)m * 2 + (1 - q_old)) * ntr + l];
         K("ffsl_hflx_tracer", 3, [&] { launch_ffsl_hflx<R>(dg, L, bv, qo, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt_adv); });
-        K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, L, qo, qn, w.ptf_lon, w.ptf_lat, b.old_phs_f, n.phs_f, dt_adv); });
-        K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, L, qn, b.cflz, b.we, n.phs_f, dt_adv); });
+        K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, L, qo, qn, w.ptf_lon, w.ptf_lat, b.old_surf(), n.surf(), dt_adv); });
+        K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, L, qn, b.cflz, b.we, n.surf(), dt_adv); });
         K("tracer_lon_damp", 1, [&] { launch_tracer_lon_damp<R>(dg, L, qn); });
       }
     }
     // copy_old_m
     CK(cudaMemcpyAsync(b.old_phs_f, n.phs_f, two_d() * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    if (b.old_psr) CK(cudaMemcpyAsync(b.old_psr, n.psr, two_d() * sizeof(float), cudaMemcpyDeviceToDevice, stream));
   }
 
   cudaEvent_t take_event() {
@@ -638,9 +684,11 @@ struct Engine : EngineBase {
     for (int m = 0; m < nm; ++m) {
       const Slot<R> &s = slots[m * 3 + old_i];
       launch_filter_prologue<R>(dg, L, s);
+      launch_surface_rel<R>(dg, L, s);
       if (ntr > 0) {
         // the prologue's copy_old_m sees the layer mass before operators_prepare
         CK(cudaMemsetAsync(tb[m].old_phs_f, 0, two_d() * sizeof(double), stream));
+        if (tb[m].old_psr) CK(cudaMemsetAsync(tb[m].old_psr, 0, two_d() * sizeof(float), stream));
         int save_uv = uv_step, save_mf = mf_step, save_we = we_step;
         if (m > 0) { uv_step = save_uv; }
         accum_wind(m, s, true);
@@ -664,6 +712,9 @@ struct Engine : EngineBase {
     }
     const long launches0 = launches;
     CK(cudaEventRecord(ev_a, stream));
+    // the FP32 surface pressure follows phs_f as set through the API
+    if (kFP32 && grid.cfg.baroclinic)
+      for (int m = 0; m < nm; ++m) K("surface_rel", 1, [&] { launch_surface_rel<R>(dg, L, slots[m * 3 + old_i]); });
     for (int it = 0; it < nsteps; ++it) {
       const int o = old_i, n = new_i, t3 = 3 - o - n;
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
@@ -712,6 +763,7 @@ struct Engine : EngineBase {
 
   void diagnose(int m, gmc_diag *out) override {
     const Slot<R> &s = slots[m * 3 + old_i];
+    launch_surface_rel<R>(dg, L, s);
     launch_diagnose<R>(dg, L, s, work[m], diag_partial, diag_out);
     double h[8];
     CK(cudaMemcpyAsync(h, diag_out, 7 * sizeof(double), cudaMemcpyDeviceToHost, stream));

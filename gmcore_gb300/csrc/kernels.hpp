@@ -17,10 +17,12 @@ struct Slot {
   R *pt;                             // baroclinic potential temperature
   R *gz, *gz_f;                      // shallow-water geopotential
   double *phs, *phs_f;               // surface pressure (baroclinic)
+  float *psr;                        // FP32 form: phs_f - ptop in FP32 (null in the FP64 form)
   R *mfx_lon, *mfy_lat;              // mass fluxes of the last forward pass on this slot
   R *pv, *pv_lon, *pv_lat;           // potential vorticity and its edge values
-  double *we_lev;                    // vertical mass flux on half levels
+  R *we_lev;                         // vertical mass flux on half levels
   const double *gzs;                 // surface geopotential (static, shared by the slots)
+  __host__ __device__ SurfP<R> surf() const { return SurfP<R>{phs_f, psr}; }
 };
 
 // Work arrays of one member that live only within a pass.
@@ -31,6 +33,10 @@ struct Work {
   R *qmfx, *qmfy, *qx, *qy, *ptf_lon, *ptf_lat;
   R *du, *dv, *dpt, *dgz;
   double *dphs, *ph_exn_lev, *gz_lev;
+  // FP32 form views of the same memory: Exner pressure minus the reference
+  // column's (pea) and geopotential as a (hi, lo) FP32 pair (gzhl).
+  float *pea;
+  float2 *gzhl;
   const double *gzs;
 };
 
@@ -67,6 +73,8 @@ template <class R> void launch_update_gz(const DGrid &g, const Launch &L, const 
 template <class R> void launch_column_backward(const DGrid &g, const Launch &L, const Slot<R> &n, const Work<R> &w);
 template <class R> void launch_update_uv(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt);
 template <class R> void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s);
+// FP32 form: psr = phs_f - ptop of a slot (no-op in the FP64 form).
+template <class R> void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s);
 template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out);
 
 // Divergence damping, order 2 (div_damp_run, div_damp_mod.F90:89-118);
@@ -85,22 +93,24 @@ template <class R> void launch_pt_tendency(const DGrid &g, const Launch &L, cons
 template <class R>
 struct TracerBatch {
   R *u, *v, *mfx, *mfy;            // accumulated winds and mass fluxes
-  double *we, *m_lev;              // accumulated vertical mass flux and half-level mass
+  R *we, *m_lev;                   // accumulated vertical mass flux and half-level mass
   R *cflx, *cfly, *divx, *divy, *cflz;
   double *old_phs_f;               // surface pressure whose layer masses are old_m
+  float *old_psr;                  // its FP32 form (null in the FP64 form)
+  __host__ __device__ SurfP<R> old_surf() const { return SurfP<R>{old_phs_f, old_psr}; }
 };
 // Accumulation of one field: mode 0 copy, 1 add, 2 average with divisor.
 template <class T> void launch_accum(const Launch &L, T *dst, const T *src, size_t n, int mode, double divisor);
 // Half-level mass of a slot (calc_m, operators_mod.F90:505-525) into a
 // level field, or zero it when src_phs_f is null.
-void launch_half_level_mass(const DGrid &g, const Launch &L, const double *phs_f, double *m_lev, int mode, double divisor);
+template <class R> void launch_half_level_mass(const DGrid &g, const Launch &L, const SurfP<R> &sp, R *m_lev, int mode, double divisor);
 // Vertical Courant numbers of a batch (adv_batch_accum_we_lev RK4 part).
-template <class R> void launch_batch_cflz(const DGrid &g, const Launch &L, const double *we, const double *m_lev, R *cflz, double dt);
+template <class R> void launch_batch_cflz(const DGrid &g, const Launch &L, const R *we, const R *m_lev, R *cflz, double dt);
 // Horizontal tracer update with pole rings, division by the new mass and the
 // zonal negative fixer (adv_mod.F90:183-258).
-template <class R> void launch_tracer_horizontal(const DGrid &g, const Launch &L, const R *q_old, R *q_new, const R *fx, const R *fy, const double *old_phs_f, const double *phs_f, double dt_adv);
+template <class R> void launch_tracer_horizontal(const DGrid &g, const Launch &L, const R *q_old, R *q_new, const R *fx, const R *fy, const SurfP<R> &old_sp, const SurfP<R> &sp, double dt_adv);
 // Vertical FFSL update with the vertical fixer (adv_mod.F90:259-297).
-template <class R> void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const double *we, const double *phs_f, double dt_adv);
+template <class R> void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const R *we, const SurfP<R> &sp, double dt_adv);
 // Three passes of the order-2 zonal smoother (lon_damp_on_cell, adv_mod.F90:298-302).
 template <class R> void launch_tracer_lon_damp(const DGrid &g, const Launch &L, R *q);
 

@@ -29,21 +29,23 @@ struct Mass<double> {
 };
 template <>
 struct Mass<float> {
-  static __device__ __forceinline__ float layer(const DGrid &g, int k, double phs) {
-    return fmaf(g.dmB[k - 1], (float)(phs - g.ptop), g.dmA[k - 1]);
+  // psr = phs - ptop in FP32
+  static __device__ __forceinline__ float layer(const DGrid &g, int k, float psr) {
+    return fmaf(g.dmB[k - 1], psr, g.dmA[k - 1]);
   }
 };
 
-// Cell mass at (i, j, k): baroclinic from phs_f, shallow water (gz - gzs)/g.
+// Cell mass at (i, j, k): baroclinic from the surface pressure, shallow water
+// (gz - gzs)/g.
 template <class R>
 struct MassField {
-  const double *phs_f;   // baroclinic
+  SurfP<R> sp;           // baroclinic
   const R *gz;           // shallow water
   const double *gzs;
   __device__ __forceinline__ R at(const DGrid &g, int i, int j, int k) const {
     i = wrap(i, g.nlon);
     size_t o = (size_t)(j - 1) * g.nlon + (i - 1);
-    if (g.baroclinic) return Mass<R>::layer(g, k, phs_f[o]);
+    if (g.baroclinic) return Mass<R>::layer(g, k, sp.at(o));
     return (R)(((double)gz[o] - gzs[o]) / g.g);
   }
 };
