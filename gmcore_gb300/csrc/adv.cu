@@ -23,47 +23,84 @@ namespace {
 // full-latitude rows without the poles, y fluxes on half-latitude rows.
 //   u, v  : advecting velocities (or mass fluxes for the outer operator)
 //   mx    : field reconstructed along x;  my : field reconstructed along y.
+// The block stages the x row with its periodic extension (hx + 3 cells each
+// side, the reach of the integer Courant part plus the PPM stencil) and the
+// six y rows j-2 .. j+3 (pole halo rows mapped as the reference's fill_halo
+// leaves them) in shared memory, so the face loop indexes shared memory only.
 template <class R>
 __global__ void k_hflx(DGrid g, const R *u, const R *v, const R *cflx, const R *cfly, const R *mx, const R *my,
                        R *fx, R *fy) {
+  extern __shared__ double sh_raw[];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
-  if (j != 1 && j != nlat) {
-    auto X = [&](int l) { return mx[ix3(nlat, nlon, wrap(l, nlon), j, k)]; };
+  const int E = g.hx + 3;
+  R *xrow = reinterpret_cast<R *>(sh_raw);   // [nlon + 2E], X(l) at xrow[l - 1 + E]
+  R *yrows = xrow + nlon + 2 * E;            // [6][nlon],  Y(jj) at yrows[(jj - j + 2) * nlon + i - 1]
+  const bool do_x = j != 1 && j != nlat, do_y = j <= nhalf;
+  if (do_x) {
+    const R *src = mx + ix3(nlat, nlon, 1, j, k);
+    if (E <= nlon) {
+      for (int t = threadIdx.x; t < nlon + 2 * E; t += blockDim.x) {
+        int l = t - E;   // 0-based column
+        l = l < 0 ? l + nlon : (l >= nlon ? l - nlon : l);
+        xrow[t] = src[l];
+      }
+    } else {   // coarse grids: the extension wraps more than once
+      for (int t = threadIdx.x; t < nlon + 2 * E; t += blockDim.x) xrow[t] = src[((t - E) % nlon + nlon) % nlon];
+    }
+  }
+  if (do_y) {
+    for (int r = 0; r < 6; ++r) {
+      // row jj as fill_halo leaves it: beyond a pole the mirrored row shifted by nlon/2
+      int jj = j - 2 + r, shift = 0;
+      if (jj < 1) { jj = 2 - jj; shift = g.half; }
+      else if (jj > nlat) { jj = 2 * nlat - jj; shift = g.half; }
+      const R *src = my + ix3(nlat, nlon, 1, jj, k);
+      R *dst = yrows + r * nlon;
+      for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+        int l = i + shift;
+        dst[i] = src[l >= nlon ? l - nlon : l];
+      }
+    }
+  }
+  __syncthreads();
+  if (do_x) {
+    const R hxr = (R)g.hx;
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       const size_t o = ix3(nlat, nlon, i, j, k);
       const R c = cflx[o];
       R flux;
-      if (!(fabs(c) <= (R)g.hx)) {   // |cflx| beyond the reach the reference allows: error, no flux
+      if (!(fabs(c) <= hxr)) {   // |cflx| beyond the reach the reference allows: error, no flux
         atomicOr(g.err, ERR_CFLX);
         fx[o] = 0;
         continue;
       }
       const int ci = (int)c;
       const R cf = c - (R)ci;
+      const R *X = xrow + (E - 1);   // X[l] = X(l)
       if (c > 0) {
         const int iu = i - ci;
         R sum = 0;
-        for (int l = i + 1 - ci; l <= i; ++l) sum = sum + X(l);
+        for (int l = i + 1 - ci; l <= i; ++l) sum = sum + X[l];
         R fl, df, f6;
-        ppm(lim, X(iu - 2), X(iu - 1), X(iu), X(iu + 1), X(iu + 2), fl, df, f6);
-        flux = u[o] * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1) / c;
+        ppm(lim, X[iu - 2], X[iu - 1], X[iu], X[iu + 1], X[iu + 2], fl, df, f6);
+        flux = fdiv(u[o] * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
       } else if (c < 0) {
         const int iu = i - ci + 1;
         R sum = 0;
-        for (int l = i + 1; l <= i - ci; ++l) sum = sum + X(l);
+        for (int l = i + 1; l <= i - ci; ++l) sum = sum + X[l];
         R fl, df, f6;
-        ppm(lim, X(iu - 2), X(iu - 1), X(iu), X(iu + 1), X(iu + 2), fl, df, f6);
-        flux = -u[o] * ppm_tail(sum, fl, df, f6, (R)0, -cf) / c;
+        ppm(lim, X[iu - 2], X[iu - 1], X[iu], X[iu + 1], X[iu + 2], fl, df, f6);
+        flux = fdiv(-u[o] * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
       } else {
         flux = 0;
       }
       fx[o] = flux;
     }
   }
-  if (j <= nhalf) {
+  if (do_y) {
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      auto Y = [&](int jj) { return rd_full(my, g, i, jj, k); };
+      auto YY = [&](int jj) { return yrows[(jj - j + 2) * nlon + (i - 1)]; };
       const size_t o = ix3(nhalf, nlon, i, j, k);
       const R c = cfly[o];
       R flux;
@@ -75,13 +112,13 @@ __global__ void k_hflx(DGrid g, const R *u, const R *v, const R *cflx, const R *
       if (c > 0) {
         const int ju = j;
         R fl, df, f6;
-        ppm(lim, Y(ju - 2), Y(ju - 1), Y(ju), Y(ju + 1), Y(ju + 2), fl, df, f6);
-        flux = v[o] * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1) / c;
+        ppm(lim, YY(ju - 2), YY(ju - 1), YY(ju), YY(ju + 1), YY(ju + 2), fl, df, f6);
+        flux = fdiv(v[o] * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
       } else if (c < 0) {
         const int ju = j + 1;
         R fl, df, f6;
-        ppm(lim, Y(ju - 2), Y(ju - 1), Y(ju), Y(ju + 1), Y(ju + 2), fl, df, f6);
-        flux = -v[o] * ppm_tail((R)0, fl, df, f6, (R)0, -c) / c;
+        ppm(lim, YY(ju - 2), YY(ju - 1), YY(ju), YY(ju + 1), YY(ju + 2), fl, df, f6);
+        flux = fdiv(-v[o] * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
       } else {
         flux = 0;
       }
@@ -114,7 +151,7 @@ __global__ void k_qxqy(DGrid g, const R *q, const R *qmfx, const R *qmfy, const 
     }
     return;
   }
-  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     const size_t o = ix3(nlat, nlon, i, j, k);
     const R qv = q[o];
@@ -188,7 +225,7 @@ __global__ void k_pt_tendency(DGrid g, Slot<R> s, Work<R> w) {
   col[0] = (R)2 * col[1] - col[2];                       // k = -1
   col[nlev + 2] = (R)2 * col[nlev + 1] - col[nlev];      // k = nlev+1
   col[nlev + 3] = (R)2 * col[nlev + 2] - col[nlev + 1];  // k = nlev+2
-  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   const int im = wrap(i - 1, nlon);
   R f_top = 0;   // ptf_lev(1) = 0
   for (int k = 1; k <= nlev; ++k) {
@@ -273,10 +310,26 @@ __global__ void k_half_level_mass(DGrid g, SurfP<R> sp, R *m_lev, int mode, doub
 
 template <class R>
 __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, double dt) {
+  extern __shared__ float colsh[];
   const int j = blockIdx.y + 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
   if (i > nlon) return;
+  if constexpr (std::is_same<R, float>::value) {
+    float *col = colsh + threadIdx.x;
+    const int st = blockDim.x;
+    for (int k = 1; k <= nlev + 1; ++k) {
+      size_t o = ix3(nlat, nlon, i, j, k);
+      col[(k - 1) * st] = we_in[o] / ml_in[o] * g.half_dlev_f[k - 1];
+    }
+    bool bad = false;
+    for (int k = 2; k <= nlev; ++k) {
+      float c = cflz_of_f(g, col, st, k, (float)dt, bad);
+      if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = c;
+    }
+    if (bad) atomicOr(g.err, ERR_CFLZ);
+    return;
+  }
   R we[66], ml[66];
   for (int k = 1; k <= nlev + 1; ++k) {
     size_t o = ix3(nlat, nlon, i, j, k);
@@ -316,7 +369,7 @@ __global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *
     double p = ring_sum(nlon, red, [&](int i) { return (double)fy[ix3(nhalf, nlon, i, jv, k)]; });
     pole = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j) * dt_adv;
   }
-  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   const R dta = (R)dt_adv;
   bool neg = false;
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
@@ -441,9 +494,11 @@ template <class R>
 void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy,
                       R *fx, R *fy, double dt) {
   dim3 grid(g.nlat, g.nlev);
-  k_hflx<R><<<grid, L.threads, 0, L.stream>>>(g, b.u, b.v, b.cflx, b.cfly, q, q, qmfx, qmfy);
+  const size_t smem = (size_t)(7 * g.nlon + 2 * (g.hx + 3)) * sizeof(R);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_hflx<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_hflx<R><<<grid, L.threads, smem, L.stream>>>(g, b.u, b.v, b.cflx, b.cfly, q, q, qmfx, qmfy);
   k_qxqy<R><<<grid, L.threads, 0, L.stream>>>(g, q, qmfx, qmfy, b.divx, b.divy, qx, qy, dt);
-  k_hflx<R><<<grid, L.threads, 0, L.stream>>>(g, b.mfx, b.mfy, b.cflx, b.cfly, qy, qx, fx, fy);
+  k_hflx<R><<<grid, L.threads, smem, L.stream>>>(g, b.mfx, b.mfy, b.cflx, b.cfly, qy, qx, fx, fy);
 }
 
 template <class R>
@@ -481,7 +536,8 @@ void launch_half_level_mass(const DGrid &g, const Launch &L, const SurfP<R> &sp,
 template <class R>
 void launch_batch_cflz(const DGrid &g, const Launch &L, const R *we, const R *m_lev, R *cflz, double dt) {
   const int bt = 64;
-  k_batch_cflz<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, we, m_lev, cflz, dt);
+  const size_t smem = std::is_same<R, float>::value ? (size_t)(g.nlev + 1) * bt * sizeof(float) : 0;
+  k_batch_cflz<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, we, m_lev, cflz, dt);
 }
 
 template <class R>

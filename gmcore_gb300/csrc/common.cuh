@@ -37,6 +37,16 @@ struct FilterDev {
   int max_taps;
 };
 
+// FP32 copies of the row tables (same indexing), read by the FP32 form so
+// that no FP64 arithmetic or conversion runs in its kernels.
+struct RowF {
+  const float *area_cell, *area_subcell1, *area_subcell2;
+  const float *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
+  const float *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
+  const float *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
+  const float *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat;
+};
+
 // Grid constants and 1-D metric tables (device pointers).  Row tables are
 // indexed [j + 1] for j = -1 .. n+2 (j = 0 and j = n+1 hold the reference's
 // halo values), level tables [k - 1].
@@ -53,10 +63,15 @@ struct DGrid {
   const double *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
   const double *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
   const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat;
+  RowF f;
+  // FP32 form of the y departure: offsets radius (half_lat(l) - half_lat(j)) / de_lat(j)
+  // for l = j-1 .. j+2 at [(j-1)*4 + l-j+1] (0 outside 1..nhalf)
+  const float *cfl_yoff;
   const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
   const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables
   const float *hybi_f;                                             // FP32 copy of hybi [k-1]
+  const float *full_dlev_rf;                                       // FP32 1 / full_dlev [k-1]
   // FP32 column sweep about a reference column with surface pressure ps_ref
   // (pressures p_ref on half levels, ph_ref on full levels):
   //   pr_c[k-1]    = hybi(k) / p_ref(k)              k = 1..nlev+1
@@ -74,6 +89,19 @@ struct DGrid {
 };
 
 #define ROW(t, j) ((t)[(j) + 1])
+
+// Row table `name` at row j in the arithmetic type R of the form.
+template <class R>
+struct RowSel;
+template <>
+struct RowSel<double> {
+  static __device__ __forceinline__ const double *pick(const double *d, const float *) { return d; }
+};
+template <>
+struct RowSel<float> {
+  static __device__ __forceinline__ const float *pick(const double *, const float *f) { return f; }
+};
+#define ROWR(R, name, j) (RowSel<R>::pick(g.name, g.f.name)[(j) + 1])
 
 // Surface pressure as the layer-mass formula of each form reads it: the FP64
 // form takes phs_f, the FP32 form psr = phs_f - ptop rounded once to FP32.

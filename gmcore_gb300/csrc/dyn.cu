@@ -55,7 +55,7 @@ __global__ void k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const MassField<R> M = mass_of(g, s);
   if (j <= g.nhalf) {
-    const R w1 = (R)ROW(g.htw1, j), w2 = (R)ROW(g.htw2, j);
+    const R w1 = ROWR(R, htw1, j), w2 = ROWR(R, htw2, j);
     for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
       const int im = wrap(i - 1, g.nlon);
       R mfx_lat = w1 * (s.mfx_lon[ix3(g.nlat, g.nlon, im, j, k)] + s.mfx_lon[ix3(g.nlat, g.nlon, i, j, k)]) +
@@ -67,7 +67,7 @@ __global__ void k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
   if (j == 1 || j == g.nlat) {
     for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) w.v_lon[ix3(g.nlat, g.nlon, i, j, k)] = (R)0;
   } else {
-    const R w1 = (R)ROW(g.ftw1, j), w2 = (R)ROW(g.ftw2, j);
+    const R w1 = ROWR(R, ftw1, j), w2 = ROWR(R, ftw2, j);
     for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
       const int ip = wrap(i + 1, g.nlon);
       R mfy_lon = w1 * (s.mfy_lat[ix3(g.nhalf, g.nlon, i, j - 1, k)] + s.mfy_lat[ix3(g.nhalf, g.nlon, ip, j - 1, k)]) +
@@ -99,25 +99,25 @@ __global__ void k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
   auto U = [&](int i, int jj) { return u[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
   auto V = [&](int i, int jj) { return v[ix3(nhalf, nlon, wrap(i, nlon), jj, k)]; };
   auto sq = [](R x) { return x * x; };
-  const R alw = (R)ROW(g.area_lon_west, j), ale = (R)ROW(g.area_lon_east, j);
-  const R aln = (R)ROW(g.area_lat_north, j - 1), als = (R)ROW(g.area_lat_south, j), ac = (R)ROW(g.area_cell, j);
+  const R alw = ROWR(R, area_lon_west, j), ale = ROWR(R, area_lon_east, j);
+  const R aln = ROWR(R, area_lat_north, j - 1), als = ROWR(R, area_lat_south, j), ac = ROWR(R, area_cell, j);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     R ke = (alw * sq(U(i - 1, j)) + ale * sq(U(i, j)) + aln * sq(V(i, j - 1)) + als * sq(V(i, j))) / ac;
     if (g.ke_scheme == 2) {
       const R cw = (R)g.ke_cell_wgt;
-      R k1 = ((R)ROW(g.area_lat_east, j) * sq(V(i - 1, j)) + (R)ROW(g.area_lat_west, j) * sq(V(i, j)) +
-              (R)ROW(g.area_lon_north, j) * sq(U(i - 1, j)) + (R)ROW(g.area_lon_south, j + 1) * sq(U(i - 1, j + 1))) /
-             (R)ROW(g.area_vtx, j);
-      R k2 = ((R)ROW(g.area_lat_east, j - 1) * sq(V(i - 1, j - 1)) + (R)ROW(g.area_lat_west, j - 1) * sq(V(i, j - 1)) +
-              (R)ROW(g.area_lon_north, j - 1) * sq(U(i - 1, j - 1)) + (R)ROW(g.area_lon_south, j) * sq(U(i - 1, j))) /
-             (R)ROW(g.area_vtx, j - 1);
-      R k3 = ((R)ROW(g.area_lat_east, j - 1) * sq(V(i, j - 1)) + (R)ROW(g.area_lat_west, j - 1) * sq(V(i + 1, j - 1)) +
-              (R)ROW(g.area_lon_north, j - 1) * sq(U(i, j - 1)) + (R)ROW(g.area_lon_south, j) * sq(U(i, j))) /
-             (R)ROW(g.area_vtx, j - 1);
-      R k4 = ((R)ROW(g.area_lat_east, j) * sq(V(i, j)) + (R)ROW(g.area_lat_west, j) * sq(V(i + 1, j)) +
-              (R)ROW(g.area_lon_north, j) * sq(U(i, j)) + (R)ROW(g.area_lon_south, j + 1) * sq(U(i, j + 1))) /
-             (R)ROW(g.area_vtx, j);
-      ke = ((R)1 - cw) * ((k1 + k4) * (R)ROW(g.area_subcell2, j) + (k2 + k3) * (R)ROW(g.area_subcell1, j)) / ac + cw * ke;
+      R k1 = (ROWR(R, area_lat_east, j) * sq(V(i - 1, j)) + ROWR(R, area_lat_west, j) * sq(V(i, j)) +
+              ROWR(R, area_lon_north, j) * sq(U(i - 1, j)) + ROWR(R, area_lon_south, j + 1) * sq(U(i - 1, j + 1))) /
+             ROWR(R, area_vtx, j);
+      R k2 = (ROWR(R, area_lat_east, j - 1) * sq(V(i - 1, j - 1)) + ROWR(R, area_lat_west, j - 1) * sq(V(i, j - 1)) +
+              ROWR(R, area_lon_north, j - 1) * sq(U(i - 1, j - 1)) + ROWR(R, area_lon_south, j) * sq(U(i - 1, j))) /
+             ROWR(R, area_vtx, j - 1);
+      R k3 = (ROWR(R, area_lat_east, j - 1) * sq(V(i, j - 1)) + ROWR(R, area_lat_west, j - 1) * sq(V(i + 1, j - 1)) +
+              ROWR(R, area_lon_north, j - 1) * sq(U(i, j - 1)) + ROWR(R, area_lon_south, j) * sq(U(i, j))) /
+             ROWR(R, area_vtx, j - 1);
+      R k4 = (ROWR(R, area_lat_east, j) * sq(V(i, j)) + ROWR(R, area_lat_west, j) * sq(V(i + 1, j)) +
+              ROWR(R, area_lon_north, j) * sq(U(i, j)) + ROWR(R, area_lon_south, j + 1) * sq(U(i, j + 1))) /
+             ROWR(R, area_vtx, j);
+      ke = ((R)1 - cw) * ((k1 + k4) * ROWR(R, area_subcell2, j) + (k2 + k3) * ROWR(R, area_subcell1, j)) / ac + cw * ke;
     }
     w.ke[ix3(nlat, nlon, i, j, k)] = ke;
   }
@@ -139,8 +139,8 @@ __global__ void k_pv(DGrid g, Slot<R> s, Work<R> w) {
     double p = ring_sum(nlon, red, [&](int i) { return sgn * (double)w.u_lat[ix3(nhalf, nlon, i, j, k)] * le; });
     pole_vor = p / nlon / ROW(g.area_cell, j == 1 ? 1 : nhalf + 1);
   }
-  const R dl0 = (R)ROW(g.de_lon, j), dl1 = (R)ROW(g.de_lon, j + 1), dt = (R)ROW(g.de_lat, j), av = (R)ROW(g.area_vtx, j);
-  const R as2 = (R)ROW(g.area_subcell2, j), as1 = (R)ROW(g.area_subcell1, j + 1), f = (R)ROW(g.half_f, j);
+  const R dl0 = ROWR(R, de_lon, j), dl1 = ROWR(R, de_lon, j + 1), dt = ROWR(R, de_lat, j), av = ROWR(R, area_vtx, j);
+  const R as2 = ROWR(R, area_subcell2, j), as1 = ROWR(R, area_subcell1, j + 1), f = ROWR(R, half_f, j);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     const int ip = wrap(i + 1, nlon);
     R vor;
@@ -236,9 +236,9 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
   } else if constexpr (std::is_same<R, float>::value) {
     // FP32 form of the x departure: positions in cells relative to face i,
     // (radius half_lon(l) cos - x) / dx = (l - i) - a exactly in real arithmetic.
-    const float cdx = (float)(dt_ / ROW(g.de_lon, j));
-    const float lel = (float)ROW(g.le_lon, j), ac = (float)ROW(g.area_cell, j);
-    const float la0 = (float)ROW(g.le_lat, j), la1 = (float)ROW(g.le_lat, j - 1);
+    const float cdx = (float)dt_ / ROWR(float, de_lon, j);
+    const float lel = ROWR(float, le_lon, j), ac = ROWR(float, area_cell, j);
+    const float la0 = ROWR(float, le_lat, j), la1 = ROWR(float, le_lat, j - 1);
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       auto Ul = [&](int l) {
         int lw = ((l - 1) % nlon + nlon) % nlon + 1;
@@ -294,13 +294,8 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
     if (j <= nhalf) {
       // FP32 form of the y departure: row offsets A(l) = radius (half_lat(l) - half_lat(j)) / dy.
       // A departure more than one row away (|cfly| > 1, flagged below) keeps v1.
-      const double dy = ROW(g.de_lat, j);
-      const float cdy = (float)(dt_ / dy);
-      float A[4];   // l = j-1 .. j+2
-      for (int t = 0; t < 4; ++t) {
-        int l = j - 1 + t;
-        A[t] = (l >= 1 && l <= nhalf) ? (float)(radius * (ROW(g.half_lat, l) - ROW(g.half_lat, j)) / dy) : 0.f;
-      }
+      const float cdy = (float)dt_ / ROWR(float, de_lat, j);
+      const float *A = g.cfl_yoff + (size_t)(j - 1) * 4;   // l = j-1 .. j+2
       for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
         auto Vl = [&](int l) { return v[ix3(nhalf, nlon, i, l, k)]; };
         const float v1 = Vl(j);
@@ -367,12 +362,13 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
   const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
   const int im = wrap(i - 1, nlon);
   if constexpr (std::is_same<R, float>::value) {
-    // FP32 form: divergences with per-row reciprocal factors, layer masses
-    // from psr, all on the FP32 pipeline.
-    const double ac = ROW(g.area_cell, j);
-    const float clon = (float)(ROW(g.le_lon, j) / ac), cn = (float)(ROW(g.le_lat, j) / ac),
-                cs = (float)(ROW(g.le_lat, j - 1) / ac);
-    float mfp[66], we[66], ml[66];
+    // FP32 form: divergences with per-row factors, layer masses from psr; the
+    // column's prefix sums and then wm = we / ml * half_dlev live in shared
+    // memory (one slot per level and thread).
+    float *col = reinterpret_cast<float *>(ring + nlev + 2) + threadIdx.x;
+    const int st = blockDim.x;
+    const float ac = ROWR(float, area_cell, j);
+    const float clon = ROWR(float, le_lon, j) / ac, cn = ROWR(float, le_lat, j) / ac, cs = ROWR(float, le_lat, j - 1) / ac;
     float mf = 0;
     for (int k = 1; k <= nlev; ++k) {
       float d;
@@ -383,31 +379,29 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
             (s.mfy_lat[ix3(nhalf, nlon, i, j, k)] * cn - s.mfy_lat[ix3(nhalf, nlon, i, j - 1, k)] * cs);
       }
       mf = mf + d;
-      mfp[k - 1] = mf;
+      col[(k - 1) * st] = mf;   // prefix sum through level k
     }
     const float dphs = -mf;
     w.dphs[c2] = (double)dphs;
-    s.we_lev[ix3(nlat, nlon, i, j, 1)] = 0;
-    we[0] = 0;
-    for (int k = 2; k <= nlev; ++k) {
-      float wv = -(g.hybi_f[k - 1] * dphs) - mfp[k - 2];
-      s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
-      we[k - 1] = wv;
-    }
-    we[nlev] = 0;
-    s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
-    // half-level mass: (m(k-1) + m(k)) / 2, half layers at the ends
     const float psr = s.psr[c2];
-    float mprev = 0;
-    for (int k = 1; k <= nlev; ++k) {
-      float m = Mass<float>::layer(g, k, psr);
-      ml[k - 1] = 0.5f * (mprev + m);
-      mprev = m;
+    s.we_lev[ix3(nlat, nlon, i, j, 1)] = 0;
+    float m_up = Mass<float>::layer(g, 1, psr);
+    float p_prev = col[0];
+    col[0] = 0;   // wm(1): we(1) = 0
+    for (int k = 2; k <= nlev; ++k) {
+      const float wv = -(g.hybi_f[k - 1] * dphs) - p_prev;
+      s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
+      const float m_lo = Mass<float>::layer(g, k, psr);
+      const float ml = 0.5f * (m_up + m_lo);   // half-level mass
+      p_prev = col[(k - 1) * st];
+      col[(k - 1) * st] = wv / ml * g.half_dlev_f[k - 1];
+      m_up = m_lo;
     }
-    ml[nlev] = 0.5f * mprev;
+    col[nlev * st] = 0;   // wm(nlev+1): we = 0
+    s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
     bool bad = false;
     for (int k = 2; k <= nlev; ++k) {
-      float c = cflz_of<float>(g, we, ml, k, (float)dt, bad);
+      float c = cflz_of_f(g, col, st, k, (float)dt, bad);
       if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
     if (bad) atomicOr(g.err, ERR_CFLZ);
@@ -472,8 +466,8 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
   auto PVLON = [&](int i, int jj) { return s.pv_lon[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
   auto PVLAT = [&](int i, int jj) { return s.pv_lat[ix3(nhalf, nlon, wrap(i, nlon), jj, k)]; };
   if (j != 1 && j != nlat) {
-    const R t1 = (R)ROW(g.ftw1, j), t2 = (R)ROW(g.ftw2, j), de = (R)ROW(g.de_lon, j);
-    const R aw = (R)ROW(g.area_lon_west, j), ae = (R)ROW(g.area_lon_east, j), al = (R)ROW(g.area_lon, j);
+    const R t1 = ROWR(R, ftw1, j), t2 = ROWR(R, ftw2, j), de = ROWR(R, de_lon, j);
+    const R aw = ROWR(R, area_lon_west, j), ae = ROWR(R, area_lon_east, j), al = ROWR(R, area_lon, j);
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       const size_t o = ix3(nlat, nlon, i, j, k);
       const R pl = s.pv_lon[o];
@@ -507,8 +501,8 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
     }
   }
   if (j <= nhalf) {
-    const R t1 = (R)ROW(g.htw1, j), t2 = (R)ROW(g.htw2, j), de = (R)ROW(g.de_lat, j);
-    const R an = (R)ROW(g.area_lat_north, j), as = (R)ROW(g.area_lat_south, j), al = (R)ROW(g.area_lat, j);
+    const R t1 = ROWR(R, htw1, j), t2 = ROWR(R, htw2, j), de = ROWR(R, de_lat, j);
+    const R an = ROWR(R, area_lat_north, j), as = ROWR(R, area_lat_south, j), al = ROWR(R, area_lat, j);
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       const size_t o = ix3(nhalf, nlon, i, j, k);
       const R pl = s.pv_lat[o];
@@ -558,7 +552,7 @@ __global__ void k_swm_dgz(DGrid g, Slot<R> s, Work<R> w) {
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) w.dgz[ix3(nlat, nlon, i, j, 1)] = (R)(-(0.0 + p) * g.g);
     return;
   }
-  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     R dlon = (s.mfx_lon[ix3(nlat, nlon, i, j, 1)] - s.mfx_lon[ix3(nlat, nlon, wrap(i - 1, nlon), j, 1)]) * lel / ac;
     R dlat = (s.mfy_lat[ix3(nhalf, nlon, i, j, 1)] * la0 - s.mfy_lat[ix3(nhalf, nlon, i, j - 1, 1)] * la1) / ac;
@@ -732,7 +726,7 @@ __device__ __forceinline__ R pgf_lon(const DGrid &g, const Slot<R> &n, const Wor
     double dgz2 = gz[ix3(nlat, nlon, i, j, k)] - gz[ix3(nlat, nlon, ip, j, k + 1)];
     return (R)(-(dph1 * dgz1 + dph2 * dgz2) / ROW(g.de_lon, j) / (dph1 + dph2));
   }
-  return (n.gz_f[ix3(nlat, nlon, ip, j, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / (R)ROW(g.de_lon, j);
+  return (n.gz_f[ix3(nlat, nlon, ip, j, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / ROWR(R, de_lon, j);
 }
 template <class R>
 __device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Work<R> &w, int i, int j, int k, R inv_d) {
@@ -755,7 +749,7 @@ __device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Wor
     double dgz2 = gz[ix3(nlat, nlon, i, j, k)] - gz[ix3(nlat, nlon, i, j + 1, k + 1)];
     return (R)(-(dph1 * dgz1 + dph2 * dgz2) / ROW(g.de_lat, j) / (dph1 + dph2));
   }
-  return (n.gz_f[ix3(nlat, nlon, i, j + 1, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / (R)ROW(g.de_lat, j);
+  return (n.gz_f[ix3(nlat, nlon, i, j + 1, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / ROWR(R, de_lat, j);
 }
 
 template <class R>
@@ -773,7 +767,7 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
       }
       return;
     }
-    const R inv_d = (R)(1.0 / ROW(g.de_lon, j));
+    const R inv_d = (R)1 / ROWR(R, de_lon, j);
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
       size_t c = ix3(nlat, nlon, i + 1, j, k);
       row[i] = o.u_lon[c] + (R)dt * (w.du[c] - pgf_lon(g, n, w, i + 1, j, k, inv_d));
@@ -788,7 +782,7 @@ __global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   }
   const int j = blockIdx.x - nlat + 1;
   auto load_v = [&](int jj, R *dst) {
-    const R inv_d = (R)(1.0 / ROW(g.de_lat, jj));
+    const R inv_d = (R)1 / ROWR(R, de_lat, jj);
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
       size_t c = ix3(nhalf, nlon, i + 1, jj, k);
       dst[i] = o.v_lat[c] + (R)dt * (w.dv[c] - pgf_lat(g, n, w, i + 1, jj, k, inv_d));
@@ -930,7 +924,7 @@ void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R
 template <class R>
 void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
   const int bt = 64;
-  size_t smem = (32 + g.nlev + 2) * sizeof(double);
+  size_t smem = (32 + g.nlev + 2) * sizeof(double) + (std::is_same<R, float>::value ? (size_t)(g.nlev + 1) * bt * sizeof(float) : 0);
   k_column_mass<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, s, w, dt);
 }
 template <class R>
@@ -1025,7 +1019,7 @@ __global__ void k_div(DGrid g, Slot<R> n, R *div) {
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) div[ix3(nlat, nlon, i, j, k)] = (R)p;
     return;
   }
-  const R lel = (R)ROW(g.le_lon, j), ac = (R)ROW(g.area_cell, j), la0 = (R)ROW(g.le_lat, j), la1 = (R)ROW(g.le_lat, j - 1);
+  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     R ue = n.u_f[ix3(nlat, nlon, i, j, k)], uw = n.u_f[ix3(nlat, nlon, wrap(i - 1, nlon), j, k)];
     R vn = n.v_f[ix3(nhalf, nlon, i, j, k)], vs = n.v_f[ix3(nhalf, nlon, i, j - 1, k)];
@@ -1040,7 +1034,7 @@ __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
   if ((int)blockIdx.x < nlat) {
     const int j = blockIdx.x + 1;
     if (j == 1 || j == nlat) return;
-    const R c = (R)g.div_c_lon[(size_t)(k - 1) * nlat + (j - 1)], de = (R)ROW(g.de_lon, j);
+    const R c = (R)g.div_c_lon[(size_t)(k - 1) * nlat + (j - 1)], de = ROWR(R, de_lon, j);
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       size_t o = ix3(nlat, nlon, i, j, k);
       n.u_lon[o] = n.u_lon[o] + c * (div[ix3(nlat, nlon, wrap(i + 1, nlon), j, k)] - div[o]) / de;
@@ -1048,7 +1042,7 @@ __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
     return;
   }
   const int j = blockIdx.x - nlat + 1;
-  const R c = (R)g.div_c_lat[(size_t)(k - 1) * nhalf + (j - 1)], de = (R)ROW(g.de_lat, j);
+  const R c = (R)g.div_c_lat[(size_t)(k - 1) * nhalf + (j - 1)], de = ROWR(R, de_lat, j);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     size_t o = ix3(nhalf, nlon, i, j, k);
     n.v_lat[o] = n.v_lat[o] + c * (div[ix3(nlat, nlon, i, j + 1, k)] - div[ix3(nlat, nlon, i, j, k)]) / de;

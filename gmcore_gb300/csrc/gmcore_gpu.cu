@@ -299,23 +299,39 @@ struct Engine : EngineBase {
     };
     struct Fix { size_t off; const void **dst; };
     std::vector<Fix> fixes;
-    auto row = [&](const RowTable &t, const double **dst) { fixes.push_back({push(t.v.data(), t.v.size() * 8), (const void **)dst}); };
+    auto row = [&](const RowTable &t, const double **dst, const float **dst_f) {
+      fixes.push_back({push(t.v.data(), t.v.size() * 8), (const void **)dst});
+      std::vector<float> tf(t.v.begin(), t.v.end());
+      fixes.push_back({push(tf.data(), tf.size() * 4), (const void **)dst_f});
+    };
     auto vec = [&](const std::vector<double> &t, const double **dst) {
       fixes.push_back({push(t.data(), t.size() * 8), (const void **)dst});
     };
-    row(g.area_cell, &dg.area_cell); row(g.area_subcell1, &dg.area_subcell1); row(g.area_subcell2, &dg.area_subcell2);
-    row(g.area_lon, &dg.area_lon); row(g.area_lon_west, &dg.area_lon_west); row(g.area_lon_east, &dg.area_lon_east);
-    row(g.area_lon_north, &dg.area_lon_north); row(g.area_lon_south, &dg.area_lon_south);
-    row(g.area_lat, &dg.area_lat); row(g.area_lat_west, &dg.area_lat_west); row(g.area_lat_east, &dg.area_lat_east);
-    row(g.area_lat_north, &dg.area_lat_north); row(g.area_lat_south, &dg.area_lat_south);
-    row(g.area_vtx, &dg.area_vtx); row(g.de_lon, &dg.de_lon); row(g.le_lon, &dg.le_lon); row(g.de_lat, &dg.de_lat);
-    row(g.le_lat, &dg.le_lat); row(g.full_f, &dg.full_f); row(g.half_f, &dg.half_f);
-    row(g.full_tangent_wgt1, &dg.ftw1); row(g.full_tangent_wgt2, &dg.ftw2);
-    row(g.half_tangent_wgt1, &dg.htw1); row(g.half_tangent_wgt2, &dg.htw2);
-    row(g.full_cos_lat, &dg.full_cos_lat); row(g.half_lat, &dg.half_lat);
+    row(g.area_cell, &dg.area_cell, &dg.f.area_cell); row(g.area_subcell1, &dg.area_subcell1, &dg.f.area_subcell1); row(g.area_subcell2, &dg.area_subcell2, &dg.f.area_subcell2);
+    row(g.area_lon, &dg.area_lon, &dg.f.area_lon); row(g.area_lon_west, &dg.area_lon_west, &dg.f.area_lon_west); row(g.area_lon_east, &dg.area_lon_east, &dg.f.area_lon_east);
+    row(g.area_lon_north, &dg.area_lon_north, &dg.f.area_lon_north); row(g.area_lon_south, &dg.area_lon_south, &dg.f.area_lon_south);
+    row(g.area_lat, &dg.area_lat, &dg.f.area_lat); row(g.area_lat_west, &dg.area_lat_west, &dg.f.area_lat_west); row(g.area_lat_east, &dg.area_lat_east, &dg.f.area_lat_east);
+    row(g.area_lat_north, &dg.area_lat_north, &dg.f.area_lat_north); row(g.area_lat_south, &dg.area_lat_south, &dg.f.area_lat_south);
+    row(g.area_vtx, &dg.area_vtx, &dg.f.area_vtx); row(g.de_lon, &dg.de_lon, &dg.f.de_lon); row(g.le_lon, &dg.le_lon, &dg.f.le_lon); row(g.de_lat, &dg.de_lat, &dg.f.de_lat);
+    row(g.le_lat, &dg.le_lat, &dg.f.le_lat); row(g.full_f, &dg.full_f, &dg.f.full_f); row(g.half_f, &dg.half_f, &dg.f.half_f);
+    row(g.full_tangent_wgt1, &dg.ftw1, &dg.f.ftw1); row(g.full_tangent_wgt2, &dg.ftw2, &dg.f.ftw2);
+    row(g.half_tangent_wgt1, &dg.htw1, &dg.f.htw1); row(g.half_tangent_wgt2, &dg.htw2, &dg.f.htw2);
+    row(g.full_cos_lat, &dg.full_cos_lat, &dg.f.full_cos_lat); row(g.half_lat, &dg.half_lat, &dg.f.half_lat);
     vec(g.hyai, &dg.hyai); vec(g.hybi, &dg.hybi); vec(g.half_lev, &dg.half_lev); vec(g.half_dlev, &dg.half_dlev);
     vec(g.full_dlev, &dg.full_dlev); vec(g.lon_damp_wgt_full, &dg.lon_damp_full);
     vec(g.div_c_lon, &dg.div_c_lon); vec(g.div_c_lat, &dg.div_c_lat);
+    {
+      std::vector<float> yo((size_t)g.nhalf * 4, 0.f);
+      for (int j = 1; j <= g.nhalf; ++j)
+        for (int t = 0; t < 4; ++t) {
+          int l = j - 1 + t;
+          if (l >= 1 && l <= g.nhalf)
+            yo[(size_t)(j - 1) * 4 + t] =
+                (float)(g.cfg.radius * (g.half_lat.v[l + 1] - g.half_lat.v[j + 1]) / g.de_lat.v[j + 1]);
+        }
+      yo.push_back(0.f);
+      fixes.push_back({push(yo.data(), yo.size() * 4), (const void **)&dg.cfl_yoff});
+    }
     // FP32 layer-mass coefficients
     std::vector<float> dA(g.nlev + 1, 0.f), dB(g.nlev + 1, 0.f);
     for (int k = 0; k < g.nlev && g.cfg.baroclinic; ++k) {
@@ -331,6 +347,10 @@ struct Engine : EngineBase {
     std::vector<float> hbf(g.hybi.begin(), g.hybi.end());
     hbf.push_back(0.f);
     size_t offHB = push(hbf.data(), hbf.size() * 4);
+    std::vector<float> rfd;
+    for (double d : g.full_dlev) rfd.push_back(d != 0 ? (float)(1.0 / d) : 0.f);
+    rfd.push_back(0.f);
+    size_t offRFD = push(rfd.data(), rfd.size() * 4);
     // FP32 column sweep about a reference column at ps_ref = p0
     const int nl = g.nlev;
     const double ps_ref = g.cfg.p0, kap = g.cfg.Rd / g.cfg.cpd;
@@ -385,6 +405,7 @@ struct Engine : EngineBase {
     dg.half_dlev_f = reinterpret_cast<const float *>(tables.base + offHD);
     dg.full_dlev_f = reinterpret_cast<const float *>(tables.base + offFD);
     dg.hybi_f = reinterpret_cast<const float *>(tables.base + offHB);
+    dg.full_dlev_rf = reinterpret_cast<const float *>(tables.base + offRFD);
     dg.pr_c = reinterpret_cast<const float *>(tables.base + offPRC);
     dg.pe_ref = reinterpret_cast<const float *>(tables.base + offPER);
     dg.dpe_ref = reinterpret_cast<const float *>(tables.base + offDPER);

@@ -63,13 +63,23 @@ __device__ __forceinline__ R slope(int limiter, R fm1, R f, R fp1) {
   return fsign(fmin(fmin(fabs(df), dmin), dmax), df);
 }
 
+// x / 6 and x / 3: exact divisions in the FP64 form, products with the
+// rounded reciprocal in the FP32 form.
+__device__ __forceinline__ double div6(double x) { return x / 6.0; }
+__device__ __forceinline__ float div6(float x) { return x * (1.0f / 6.0f); }
+__device__ __forceinline__ double div3(double x) { return x / 3.0; }
+__device__ __forceinline__ float div3(float x) { return x * (1.0f / 3.0f); }
+// a / b: IEEE division in the FP64 form, one reciprocal and product in FP32.
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float fdiv(float a, float b) { return a * __frcp_rn(b); }
+
 template <class R>
 __device__ __forceinline__ void ppm(int limiter, R fm2, R fm1, R f, R fp1, R fp2, R &fl, R &df, R &f6) {
   R dfl = slope(limiter, fm2, fm1, f);
   df = slope(limiter, fm1, f, fp1);
   R dfr = slope(limiter, f, fp1, fp2);
-  fl = (R)0.5 * (fm1 + f) + (dfl - df) / (R)6;
-  R fr = (R)0.5 * (fp1 + f) + (df - dfr) / (R)6;
+  fl = (R)0.5 * (fm1 + f) + div6(dfl - df);
+  R fr = (R)0.5 * (fp1 + f) + div6(df - dfr);
   fl = f - fsign(fmin(fabs(df), fabs(fl - f)), df);
   fr = f + fsign(fmin(fabs(df), fabs(fr - f)), df);
   f6 = (R)6 * f - (R)3 * (fl + fr);
@@ -84,7 +94,48 @@ __device__ __forceinline__ R ppm_tail(R sum, R fl, R df, R f6, R s1, R s2) {
   R ds1 = s2 - s1;
   R ds2 = s2 * s2 - s1 * s1;
   R ds3 = s2 * s2 * s2 - s1 * s1 * s1;
-  return sum + fl * ds1 + (R)0.5 * df * ds2 + f6 * (ds2 / (R)2 - ds3 / (R)3);
+  return sum + fl * ds1 + (R)0.5 * df * ds2 + f6 * (ds2 / (R)2 - div3(ds3));
+}
+
+// FP32 form of cflz_of over a column held as wm(l) = we(l) / ml(l) * half_dlev(l)
+// at wm[(l - 1) * stride] for l = 1 .. nlev+1: the per-level quotients are
+// formed once per column instead of once per RK4 interpolation.
+__device__ __forceinline__ float cflz_of_f(const DGrid &g, const float *wm, int stride, int k, float dt_, bool &bad) {
+  const int nlev = g.nlev;
+  const float *HL = g.half_lev_f, *RFD = g.full_dlev_rf;   // [k-1]
+  auto W = [&](int l) { return wm[(l - 1) * stride]; };   // l = 1 .. nlev+1
+  auto locate = [&](float w, float z) {
+    int l;
+    if (w > 0) {
+      for (l = k; l <= nlev; ++l)
+        if (HL[l - 1] <= z && z <= HL[l]) break;
+      if (l == nlev + 1) { bad = true; l = nlev; }
+    } else {
+      for (l = k - 1; l >= 1; --l)
+        if (HL[l - 1] <= z && z <= HL[l]) break;
+      if (l == 0) { bad = true; l = 1; }
+    }
+    return l;
+  };
+  auto interp = [&](int l, float z) { return ((HL[l] - z) * W(l) + (z - HL[l - 1]) * W(l + 1)) * RFD[l - 1]; };
+  const float z0 = HL[k - 1];
+  const float w1 = W(k);
+  const float z1 = z0 + 0.5f * dt_ * w1;
+  const float w2 = interp(locate(w1, z1), z1);
+  const float z2 = z0 + 0.5f * dt_ * w2;
+  const float w3 = interp(locate(w2, z2), z2);
+  const float z3 = z0 + dt_ * w3;
+  const float w4 = interp(locate(w3, z3), z3);
+  float deta = (w1 + 2.0f * w2 + 2.0f * w3 + w4) * (1.0f / 6.0f) * dt_;
+  int ks, ke, s;
+  if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
+  deta = fabsf(deta);
+  const float *FD = g.full_dlev_f;
+  for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s) {
+    deta = deta - FD[l - 1];
+    if (deta < 0) return s * ((1.0f + deta * RFD[l - 1]) + abs(l - ks));
+  }
+  return NAN;
 }
 
 // ---------------------------------------------------------------------------
