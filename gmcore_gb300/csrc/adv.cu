@@ -23,48 +23,51 @@ namespace {
 // full-latitude rows without the poles, y fluxes on half-latitude rows.
 //   u, v  : advecting velocities (or mass fluxes for the outer operator)
 //   mx    : field reconstructed along x;  my : field reconstructed along y.
-// The block stages the x row with its periodic extension (hx + 3 cells each
-// side, the reach of the integer Courant part plus the PPM stencil) and the
-// six y rows j-2 .. j+3 (pole halo rows mapped as the reference's fill_halo
-// leaves them) in shared memory, so the face loop indexes shared memory only.
+// blockIdx.z = 0: one full row per block.  The row is staged in shared
+// memory and the PPM slope, then the limited cell coefficients, are formed
+// once per cell; each face then reads its upwind cell.
+// blockIdx.z = 1: a strip of kHflxRows half rows per block.  Each thread
+// loads its column of the strip (plus the stencil's rows) into registers and
+// forms each slope once.  Pole halo rows are read as the reference's
+// fill_halo leaves them (mirrored row shifted by nlon/2).
+constexpr int kHflxRows = 8;
+
 template <class R>
-__global__ void k_hflx(DGrid g, const R *u, const R *v, const R *cflx, const R *cfly, const R *mx, const R *my,
-                       R *fx, R *fy) {
+__global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v, const R *__restrict__ cflx,
+                       const R *__restrict__ cfly, const R *__restrict__ mx, const R *__restrict__ my,
+                       R *__restrict__ fx, R *__restrict__ fy) {
   extern __shared__ double sh_raw[];
-  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
-  const int E = g.hx + 3;
-  R *xrow = reinterpret_cast<R *>(sh_raw);   // [nlon + 2E], X(l) at xrow[l - 1 + E]
-  R *yrows = xrow + nlon + 2 * E;            // [6][nlon],  Y(jj) at yrows[(jj - j + 2) * nlon + i - 1]
-  const bool do_x = j != 1 && j != nlat, do_y = j <= nhalf;
-  if (do_x) {
+  if (blockIdx.z == 0) {
+    const int j = blockIdx.x + 1;
+    if (j == 1 || j >= nlat) return;
+    R *xs = reinterpret_cast<R *>(sh_raw);   // row values        [nlon]
+    R *ss = xs + nlon;                       // slopes            [nlon]
+    R *cl = ss + nlon;                       // limited fl        [nlon]
+    R *cd = cl + nlon;                       // limited df        [nlon]
+    R *c6 = cd + nlon;                       // f6                [nlon]
+    auto W = [nlon](int l) { return l < 0 ? l + nlon : (l >= nlon ? l - nlon : l); };   // one wrap, 0-based
+    auto Wg = [nlon](int l) {   // any l (a Courant number may exceed nlon on coarse grids)
+      if (l >= 0 && l < nlon) return l;
+      l %= nlon;
+      return l < 0 ? l + nlon : l;
+    };
     const R *src = mx + ix3(nlat, nlon, 1, j, k);
-    if (E <= nlon) {
-      for (int t = threadIdx.x; t < nlon + 2 * E; t += blockDim.x) {
-        int l = t - E;   // 0-based column
-        l = l < 0 ? l + nlon : (l >= nlon ? l - nlon : l);
-        xrow[t] = src[l];
-      }
-    } else {   // coarse grids: the extension wraps more than once
-      for (int t = threadIdx.x; t < nlon + 2 * E; t += blockDim.x) xrow[t] = src[((t - E) % nlon + nlon) % nlon];
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[l] = src[l];
+    __syncthreads();
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) ss[l] = slope(lim, xs[W(l - 1)], xs[l], xs[W(l + 1)]);
+    __syncthreads();
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) {
+      const int lm = W(l - 1), lp = W(l + 1);
+      const R f = xs[l], s0 = ss[l];
+      R fl, df, f6;
+      ppm_cell(f, s0, ppm_edge(xs[lm], f, ss[lm], s0), ppm_edge(f, xs[lp], s0, ss[lp]), fl, df, f6);
+      cl[l] = fl;
+      cd[l] = df;
+      c6[l] = f6;
     }
-  }
-  if (do_y) {
-    for (int r = 0; r < 6; ++r) {
-      // row jj as fill_halo leaves it: beyond a pole the mirrored row shifted by nlon/2
-      int jj = j - 2 + r, shift = 0;
-      if (jj < 1) { jj = 2 - jj; shift = g.half; }
-      else if (jj > nlat) { jj = 2 * nlat - jj; shift = g.half; }
-      const R *src = my + ix3(nlat, nlon, 1, jj, k);
-      R *dst = yrows + r * nlon;
-      for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-        int l = i + shift;
-        dst[i] = src[l >= nlon ? l - nlon : l];
-      }
-    }
-  }
-  __syncthreads();
-  if (do_x) {
+    __syncthreads();
     const R hxr = (R)g.hx;
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       const size_t o = ix3(nlat, nlon, i, j, k);
@@ -77,47 +80,72 @@ __global__ void k_hflx(DGrid g, const R *u, const R *v, const R *cflx, const R *
       }
       const int ci = (int)c;
       const R cf = c - (R)ci;
-      const R *X = xrow + (E - 1);   // X[l] = X(l)
       if (c > 0) {
-        const int iu = i - ci;
+        const int iu = Wg(i - ci - 1);   // 0-based upwind cell
         R sum = 0;
-        for (int l = i + 1 - ci; l <= i; ++l) sum = sum + X[l];
-        R fl, df, f6;
-        ppm(lim, X[iu - 2], X[iu - 1], X[iu], X[iu + 1], X[iu + 2], fl, df, f6);
-        flux = fdiv(u[o] * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
+        for (int l = i + 1 - ci; l <= i; ++l) sum = sum + xs[Wg(l - 1)];
+        flux = fdiv(u[o] * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)1 - cf, (R)1), c);
       } else if (c < 0) {
-        const int iu = i - ci + 1;
+        const int iu = Wg(i - ci);       // 0-based upwind cell (i - ci + 1 in 1-based)
         R sum = 0;
-        for (int l = i + 1; l <= i - ci; ++l) sum = sum + X[l];
-        R fl, df, f6;
-        ppm(lim, X[iu - 2], X[iu - 1], X[iu], X[iu + 1], X[iu + 2], fl, df, f6);
-        flux = fdiv(-u[o] * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
+        for (int l = i + 1; l <= i - ci; ++l) sum = sum + xs[Wg(l - 1)];
+        flux = fdiv(-u[o] * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)0, -cf), c);
       } else {
         flux = 0;
       }
       fx[o] = flux;
     }
+    return;
   }
-  if (do_y) {
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      auto YY = [&](int jj) { return yrows[(jj - j + 2) * nlon + (i - 1)]; };
-      const size_t o = ix3(nhalf, nlon, i, j, k);
+  // ---- y faces on half rows j0 .. j0+kHflxRows-1
+  const int j0 = blockIdx.x * kHflxRows + 1;
+  if (j0 > nhalf) return;
+  constexpr int NV = kHflxRows + 5;   // rows j0-2 .. j0+kHflxRows+2
+  const R *rp[NV];
+  int rs[NV];
+#pragma unroll
+  for (int t = 0; t < NV; ++t) {
+    int jj = j0 - 2 + t, shift = 0;
+    if (jj < 1) { jj = 2 - jj; shift = g.half; }
+    else if (jj > nlat) { jj = 2 * nlat - jj; shift = g.half; }
+    if (jj > nlat) jj = nlat;   // rows past the strip's last face are never used
+    rp[t] = my + ix3(nlat, nlon, 1, jj, k);
+    rs[t] = shift;
+  }
+  const int nf = min(kHflxRows, nhalf - j0 + 1);
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    R y[NV], sl[NV];
+#pragma unroll
+    for (int t = 0; t < NV; ++t) {
+      if (t < nf + 5) {
+        int l = i + rs[t];
+        y[t] = rp[t][l >= nlon ? l - nlon : l];
+      } else {
+        y[t] = 0;
+      }
+    }
+    // sl[t] = slope at row j0-2+t, t = 1 .. nf+3
+#pragma unroll
+    for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
+#pragma unroll
+    for (int f = 0; f < kHflxRows; ++f) {
+      if (f >= nf) break;
+      const int j = j0 + f, t = f + 2;   // y[t] = Y(j)
+      const size_t o = ix3(nhalf, nlon, i + 1, j, k);
       const R c = cfly[o];
       R flux;
       if (!(fabs(c) <= (R)1)) {
         atomicOr(g.err, ERR_CFLY);
-        fy[o] = 0;
-        continue;
-      }
-      if (c > 0) {
-        const int ju = j;
+        flux = 0;
+      } else if (c > 0) {   // upwind cell j
         R fl, df, f6;
-        ppm(lim, YY(ju - 2), YY(ju - 1), YY(ju), YY(ju + 1), YY(ju + 2), fl, df, f6);
+        ppm_cell(y[t], sl[t], ppm_edge(y[t - 1], y[t], sl[t - 1], sl[t]), ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
+                 fl, df, f6);
         flux = fdiv(v[o] * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
-      } else if (c < 0) {
-        const int ju = j + 1;
+      } else if (c < 0) {   // upwind cell j + 1
         R fl, df, f6;
-        ppm(lim, YY(ju - 2), YY(ju - 1), YY(ju), YY(ju + 1), YY(ju + 2), fl, df, f6);
+        ppm_cell(y[t + 1], sl[t + 1], ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
+                 ppm_edge(y[t + 1], y[t + 2], sl[t + 1], sl[t + 2]), fl, df, f6);
         flux = fdiv(-v[o] * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
       } else {
         flux = 0;
@@ -199,6 +227,57 @@ __device__ __forceinline__ R vflx_at(const DGrid &g, const R *col, int k, R c, R
   return 0;
 }
 
+// vflx_at in cell-centric form for the interfaces k = 2, 3, ... of a column
+// in order.  The window holds C(k-2..k+2), the slopes s(k-2..k+1) and the
+// edge values e(k-1..k+1) (e(l) between levels l-1 and l), so each step forms
+// one slope and one edge.  For |c| < 1 the upwind cell is k-1 or k, always
+// inside 1..nlev; larger Courant numbers take the general vflx_at.  The
+// result equals vflx_at bit for bit.
+template <class R>
+struct VRoll {
+  const DGrid &g;
+  const R *col;   // col[l + 1] = C(l), l = -1 .. nlev+2
+  int k;
+  R c0, c1, c2, c3, c4;   // C(k-2) .. C(k+2)
+  R s0, s1, s2, s3;       // s(k-2) .. s(k+1)
+  R e0, e1, e2;           // e(k-1) .. e(k+1)
+  __device__ VRoll(const DGrid &g_, const R *col_) : g(g_), col(col_), k(2) {
+    const int lim = g.limiter;
+    c0 = col[1]; c1 = col[2]; c2 = col[3]; c3 = col[4]; c4 = col[5];
+    s0 = slope(lim, col[0], c0, c1);
+    s1 = slope(lim, c0, c1, c2);
+    s2 = slope(lim, c1, c2, c3);
+    s3 = slope(lim, c2, c3, c4);
+    e0 = ppm_edge(c0, c1, s0, s1);
+    e1 = ppm_edge(c1, c2, s1, s2);
+    e2 = ppm_edge(c2, c3, s2, s3);
+  }
+  // flux at the current interface k
+  __device__ __forceinline__ R flux(R c, R w) const {
+    if (!(fabs(c) < (R)1)) return vflx_at<R>(g, col, k, c, w);
+    R fl, df, f6;
+    if (c > 0) {
+      ppm_cell(c1, s1, e0, e1, fl, df, f6);
+      return fdiv(w * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
+    }
+    if (c < 0) {
+      ppm_cell(c2, s2, e1, e2, fl, df, f6);
+      return fdiv(-w * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
+    }
+    return 0;
+  }
+  // k -> k + 1 (requires k + 1 <= nlev)
+  __device__ __forceinline__ void advance() {
+    const R c5 = col[k + 4];   // C(k+3)
+    const R s4 = slope(g.limiter, c3, c4, c5);
+    const R e3 = ppm_edge(c3, c4, s3, s4);
+    c0 = c1; c1 = c2; c2 = c3; c3 = c4; c4 = c5;
+    s0 = s1; s1 = s2; s2 = s3; s3 = s4;
+    e0 = e1; e1 = e2; e2 = e3;
+    ++k;
+  }
+};
+
 // calc_grad_ptf tail (operators_mod.F90:1034-1098) with the tendency
 // assembly dpt = -(dptf/dlon + dptf/dlat + dptf/dlev) (gmcore_mod.F90:491-495).
 template <class R>
@@ -228,12 +307,14 @@ __global__ void k_pt_tendency(DGrid g, Slot<R> s, Work<R> w) {
   const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   const int im = wrap(i - 1, nlon);
   R f_top = 0;   // ptf_lev(1) = 0
+  VRoll<R> vr(g, col);
   for (int k = 1; k <= nlev; ++k) {
     const size_t o = ix3(nlat, nlon, i, j, k);
     R f_bot = 0;
     if (k + 1 <= nlev) {
       const size_t ol = ix3(nlat, nlon, i, j, k + 1);
-      f_bot = vflx_at<R>(g, col, k + 1, w.cflz[ol], s.we_lev[ol]);
+      if (k + 1 > 2) vr.advance();
+      f_bot = vr.flux(w.cflz[ol], s.we_lev[ol]);
     }
     R dlon, dlat;
     if (pole) {
@@ -435,9 +516,11 @@ __global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const R *we, Sur
   for (int k = 1; k <= nlev; ++k) m[k - 1] = Mass<R>::layer(g, k, ps);
   mz[0] = 0;
   mz[nlev] = 0;
+  VRoll<R> vr(g, col);
   for (int k = 2; k <= nlev; ++k) {
     size_t o = ix3(nlat, nlon, i, j, k);
-    mz[k - 1] = vflx_at<R>(g, col, k, cflz[o], we[o]);
+    if (k > 2) vr.advance();
+    mz[k - 1] = vr.flux(cflz[o], we[o]);
   }
   R *qc = col + 1;   // qc[k] = q(k)
   const R dta = (R)dt_adv;
@@ -494,11 +577,12 @@ template <class R>
 void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy,
                       R *fx, R *fy, double dt) {
   dim3 grid(g.nlat, g.nlev);
-  const size_t smem = (size_t)(7 * g.nlon + 2 * (g.hx + 3)) * sizeof(R);
+  dim3 hgrid(g.nlat, g.nlev, 2);   // z = 0: x rows, z = 1: y strips (first ceil(nhalf / kHflxRows) blocks)
+  const size_t smem = (size_t)5 * g.nlon * sizeof(R);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_hflx<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_hflx<R><<<grid, L.threads, smem, L.stream>>>(g, b.u, b.v, b.cflx, b.cfly, q, q, qmfx, qmfy);
+  k_hflx<R><<<hgrid, L.threads, smem, L.stream>>>(g, b.u, b.v, b.cflx, b.cfly, q, q, qmfx, qmfy);
   k_qxqy<R><<<grid, L.threads, 0, L.stream>>>(g, q, qmfx, qmfy, b.divx, b.divy, qx, qy, dt);
-  k_hflx<R><<<grid, L.threads, smem, L.stream>>>(g, b.mfx, b.mfy, b.cflx, b.cfly, qy, qx, fx, fy);
+  k_hflx<R><<<hgrid, L.threads, smem, L.stream>>>(g, b.mfx, b.mfy, b.cflx, b.cfly, qy, qx, fx, fy);
 }
 
 template <class R>

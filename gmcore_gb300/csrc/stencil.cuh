@@ -86,6 +86,23 @@ __device__ __forceinline__ void ppm(int limiter, R fm2, R fm1, R f, R fp1, R fp2
   df = fr - fl;
 }
 
+// Cell-centric form of ppm(): the unlimited edge value between cells (fm, f)
+// with slopes (sm, s) is shared by both cells, and the limited coefficients
+// of a cell follow from its value, slope and two edges.  ppm_cell(f, s,
+// ppm_edge(fm1, f, dfl, s), ppm_edge(f, fp1, s, dfr)) equals ppm() bit for bit
+// (the edge sum is commutative).
+template <class R>
+__device__ __forceinline__ R ppm_edge(R fm, R f, R sm, R s) {
+  return (R)0.5 * (fm + f) + div6(sm - s);
+}
+template <class R>
+__device__ __forceinline__ void ppm_cell(R f, R s, R el, R er, R &fl, R &df, R &f6) {
+  fl = f - fsign(fmin(fabs(s), fabs(el - f)), s);
+  const R fr = f + fsign(fmin(fabs(s), fabs(er - f)), s);
+  f6 = (R)6 * f - (R)3 * (fl + fr);
+  df = fr - fl;
+}
+
 // Whole-cell sum plus the integral of the parabola over the upwind fraction
 // [s1, s2] of the departure cell, the common tail of hflx_ppm_cell and
 // vflx_ppm_cell (ffsl_mod.F90:833-875, 917-935).
