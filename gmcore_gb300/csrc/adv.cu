@@ -53,6 +53,19 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
       l %= nlon;
       return l < 0 ? l + nlon : l;
     };
+    // face inputs of this thread's first faces are requested before the
+    // shared-memory phases so that their latency overlaps them
+    constexpr int kPre = 4;
+    R cpre[kPre], upre[kPre];
+#pragma unroll
+    for (int t = 0; t < kPre; ++t) {
+      const int i = 1 + threadIdx.x + t * blockDim.x;
+      if (i <= nlon) {
+        const size_t o = ix3(nlat, nlon, i, j, k);
+        cpre[t] = cflx[o];
+        upre[t] = u[o];
+      }
+    }
     const R *src = mx + ix3(nlat, nlon, 1, j, k);
     for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[l] = src[l];
     __syncthreads();
@@ -69,9 +82,18 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
     }
     __syncthreads();
     const R hxr = (R)g.hx;
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    int t = 0;
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
       const size_t o = ix3(nlat, nlon, i, j, k);
-      const R c = cflx[o];
+      R c, uo;
+      if (t < kPre) {
+#pragma unroll
+        for (int q = 0; q < kPre; ++q)
+          if (q == t) { c = cpre[q]; uo = upre[q]; }
+      } else {
+        c = cflx[o];
+        uo = u[o];
+      }
       R flux;
       if (!(fabs(c) <= hxr)) {   // |cflx| beyond the reach the reference allows: error, no flux
         atomicOr(g.err, ERR_CFLX);
@@ -84,12 +106,12 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
         const int iu = Wg(i - ci - 1);   // 0-based upwind cell
         R sum = 0;
         for (int l = i + 1 - ci; l <= i; ++l) sum = sum + xs[Wg(l - 1)];
-        flux = fdiv(u[o] * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)1 - cf, (R)1), c);
+        flux = fdiv(uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)1 - cf, (R)1), c);
       } else if (c < 0) {
         const int iu = Wg(i - ci);       // 0-based upwind cell (i - ci + 1 in 1-based)
         R sum = 0;
         for (int l = i + 1; l <= i - ci; ++l) sum = sum + xs[Wg(l - 1)];
-        flux = fdiv(-u[o] * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)0, -cf), c);
+        flux = fdiv(-uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)0, -cf), c);
       } else {
         flux = 0;
       }
@@ -124,6 +146,15 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
         y[t] = 0;
       }
     }
+    R cy[kHflxRows], vy[kHflxRows];
+#pragma unroll
+    for (int f = 0; f < kHflxRows; ++f) {
+      if (f < nf) {
+        const size_t o = ix3(nhalf, nlon, i + 1, j0 + f, k);
+        cy[f] = cfly[o];
+        vy[f] = v[o];
+      }
+    }
     // sl[t] = slope at row j0-2+t, t = 1 .. nf+3
 #pragma unroll
     for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
@@ -132,7 +163,7 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
       if (f >= nf) break;
       const int j = j0 + f, t = f + 2;   // y[t] = Y(j)
       const size_t o = ix3(nhalf, nlon, i + 1, j, k);
-      const R c = cfly[o];
+      const R c = cy[f];
       R flux;
       if (!(fabs(c) <= (R)1)) {
         atomicOr(g.err, ERR_CFLY);
@@ -141,12 +172,12 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
         R fl, df, f6;
         ppm_cell(y[t], sl[t], ppm_edge(y[t - 1], y[t], sl[t - 1], sl[t]), ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
                  fl, df, f6);
-        flux = fdiv(v[o] * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
+        flux = fdiv(vy[f] * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
       } else if (c < 0) {   // upwind cell j + 1
         R fl, df, f6;
         ppm_cell(y[t + 1], sl[t + 1], ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
                  ppm_edge(y[t + 1], y[t + 2], sl[t + 1], sl[t + 2]), fl, df, f6);
-        flux = fdiv(-v[o] * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
+        flux = fdiv(-vy[f] * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
       } else {
         flux = 0;
       }
@@ -330,6 +361,120 @@ __global__ void k_pt_tendency(DGrid g, Slot<R> s, Work<R> w) {
   }
 }
 
+
+// General vertical flux at interface k from a column in shared memory (any
+// Courant number): C(l) at C[(l + 1) * ld] for l = -1 .. nlev+2, limited cell
+// coefficients of cell l at FL/DF/F6[(l - 1) * ld] for l = 1 .. nlev.
+// Follows vflx_at term by term.
+template <class R>
+__device__ R vflx_tile(const DGrid &g, const R *C, const R *FL, const R *DF, const R *F6, int ld, int k, R c, R w) {
+  const int nlev = g.nlev;
+  if (!(fabs(c) <= (R)nlev)) {
+    atomicOr(g.err, ERR_CFLZ);
+    return 0;
+  }
+  auto Cv = [&](int kk) { return C[(min(max(kk, -1), nlev + 2) + 1) * ld]; };
+  const int ci = (int)c;
+  const R cf = c - (R)ci;
+  auto coef = [&](int ku, R &fl, R &df, R &f6) {
+    if (ku < 1 || ku > nlev) { fl = df = f6 = 0; return; }
+    fl = FL[(ku - 1) * ld]; df = DF[(ku - 1) * ld]; f6 = F6[(ku - 1) * ld];
+  };
+  R fl, df, f6;
+  if (c > 0) {
+    R sum = 0;
+    for (int l = k - ci; l <= k - 1; ++l) sum = sum + Cv(l);
+    coef(k - ci - 1, fl, df, f6);
+    return fdiv(w * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
+  }
+  if (c < 0) {
+    R sum = 0;
+    for (int l = k; l <= k - ci - 1; ++l) sum = sum + Cv(l);
+    coef(k - ci, fl, df, f6);
+    return fdiv(-w * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
+  }
+  return 0;
+}
+
+// FP32 form of k_pt_tendency over column tiles: the pt column with its
+// extrapolated ghost levels, slopes, limited cell coefficients and interface
+// fluxes are built in shared memory phase by phase, each phase parallel over
+// (column, level).
+__global__ void k_pt_tendency_f(DGrid g, Slot<float> s, Work<float> w) {
+  extern __shared__ double shd[];
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev, lim = g.limiter;
+  const int j = blockIdx.y + 1;
+  const int ti = threadIdx.x, kt = threadIdx.y, KT = blockDim.y;
+  const int i = blockIdx.x * kTileI + ti + 1;
+  const int ld = kTileI + 1;
+  const bool pole = j == 1 || j == nlat, valid = i <= nlon;
+  const int ic = valid ? i : nlon;
+  double *ring = shd;                                     // [nlev]
+  float *C = reinterpret_cast<float *>(shd + nlev) + ti;  // C(l) at [(l+1)*ld], l = -1 .. nlev+2
+  float *S = C + (nlev + 4) * ld;                         // s(l) at [l*ld],     l = 0 .. nlev+1
+  float *FL = S + (nlev + 2) * ld;                        // cell l at [(l-1)*ld]
+  float *DF = FL + nlev * ld;
+  float *F6 = DF + nlev * ld;
+  float *FZ = F6 + nlev * ld;                             // interface flux k at [(k-1)*ld], k = 1 .. nlev+1
+  if (pole) tile_pole_ring(g, j, ring, [&](int ii, int jv, int k) { return w.ptf_lat[ix3(nhalf, nlon, ii, jv, k)]; });
+  for (int k = 1 + kt; k <= nlev; k += KT) C[(k + 1) * ld] = s.pt[ix3(nlat, nlon, ic, j, k)];
+  __syncthreads();
+  if (kt == 0) {   // ghost levels by linear extrapolation
+    C[1 * ld] = 2.0f * C[2 * ld] - C[3 * ld];                         // C(0)
+    C[0] = 2.0f * C[1 * ld] - C[2 * ld];                              // C(-1)
+    C[(nlev + 2) * ld] = 2.0f * C[(nlev + 1) * ld] - C[nlev * ld];    // C(nlev+1)
+    C[(nlev + 3) * ld] = 2.0f * C[(nlev + 2) * ld] - C[(nlev + 1) * ld];   // C(nlev+2)
+  }
+  __syncthreads();
+  for (int l = kt; l <= nlev + 1; l += KT) S[l * ld] = slope(lim, C[l * ld], C[(l + 1) * ld], C[(l + 2) * ld]);
+  __syncthreads();
+  for (int l = 1 + kt; l <= nlev; l += KT) {
+    const float f = C[(l + 1) * ld], s0 = S[l * ld];
+    float fl, df, f6;
+    ppm_cell(f, s0, ppm_edge(C[l * ld], f, S[(l - 1) * ld], s0), ppm_edge(f, C[(l + 2) * ld], s0, S[(l + 1) * ld]), fl,
+             df, f6);
+    FL[(l - 1) * ld] = fl;
+    DF[(l - 1) * ld] = df;
+    F6[(l - 1) * ld] = f6;
+  }
+  __syncthreads();
+  for (int k = 1 + kt; k <= nlev + 1; k += KT) {
+    float fz = 0;
+    if (k != 1 && k != nlev + 1) {
+      const size_t ol = ix3(nlat, nlon, ic, j, k);
+      const float c = w.cflz[ol], wv = s.we_lev[ol];
+      if (fabsf(c) < 1.0f) {
+        if (c > 0) {
+          const int u = k - 2;   // cell k-1
+          fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
+        } else if (c < 0) {
+          const int u = k - 1;   // cell k
+          fz = fdiv(-wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 0.0f, -c), c);
+        }
+      } else if (valid) {
+        fz = vflx_tile<float>(g, C, FL, DF, F6, ld, k, c, wv);
+      }
+    }
+    FZ[(k - 1) * ld] = fz;
+  }
+  __syncthreads();
+  if (!valid) return;
+  const float ac = ROWR(float, area_cell, j);
+  const float clon = ROWR(float, le_lon, j), la0 = ROWR(float, le_lat, j), la1 = ROWR(float, le_lat, j - 1);
+  const int im = wrap(i - 1, nlon);
+  for (int k = 1 + kt; k <= nlev; k += KT) {
+    const size_t o = ix3(nlat, nlon, i, j, k);
+    float dlon, dlat;
+    if (pole) {
+      dlon = 0;
+      dlat = (float)ring[k - 1];
+    } else {
+      dlon = (w.ptf_lon[o] - w.ptf_lon[ix3(nlat, nlon, im, j, k)]) * clon / ac;
+      dlat = (w.ptf_lat[ix3(nhalf, nlon, i, j, k)] * la0 - w.ptf_lat[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
+    }
+    w.dpt[o] = -dlon - dlat - (FZ[k * ld] - FZ[(k - 1) * ld]);
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Tracer batch (adv_run, adv_mod.F90:152-312)
@@ -587,6 +732,11 @@ void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, co
 
 template <class R>
 void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  if constexpr (std::is_same<R, float>::value) {
+    const size_t smem = g.nlev * sizeof(double) + (size_t)(6 * g.nlev + 7) * (kTileI + 1) * sizeof(float);
+    k_pt_tendency_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w);
+    return;
+  }
   const int bt = 64;
   size_t smem = (32 + g.nlev + 2) * sizeof(double);
   k_pt_tendency<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, s, w);

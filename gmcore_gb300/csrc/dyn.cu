@@ -452,6 +452,77 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
   }
 }
 
+// FP32 form of k_column_mass over column tiles: layer divergences, their
+// prefix sums along the column (warp scans), we_lev, dphs and the vertical
+// Courant numbers, each phase parallel over (column, level).
+__global__ void k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, double dt) {
+  extern __shared__ double shd[];
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
+  const int j = blockIdx.y + 1;
+  const int ti = threadIdx.x, kt = threadIdx.y, KT = blockDim.y;
+  const int i = blockIdx.x * kTileI + ti + 1;
+  const int ld = kTileI + 1;
+  const bool pole = j == 1 || j == nlat, valid = i <= nlon;
+  double *ring = shd;                                    // [nlev]
+  float *P = reinterpret_cast<float *>(shd + nlev);      // [nlev][ld]   prefix sums
+  float *WM = P + nlev * ld;                             // [nlev+1][ld] we / ml * half_dlev
+  if (pole) tile_pole_ring(g, j, ring, [&](int ii, int jv, int k) { return s.mfy_lat[ix3(nhalf, nlon, ii, jv, k)]; });
+  __syncthreads();
+  const float ac = ROWR(float, area_cell, j);
+  const float clon = ROWR(float, le_lon, j) / ac, cn = ROWR(float, le_lat, j) / ac, cs = ROWR(float, le_lat, j - 1) / ac;
+  const int ic = valid ? i : nlon, im = wrap(ic - 1, nlon);
+  for (int k = 1 + kt; k <= nlev; k += KT) {
+    float d;
+    if (pole)
+      d = (float)ring[k - 1];
+    else
+      d = (s.mfx_lon[ix3(nlat, nlon, ic, j, k)] - s.mfx_lon[ix3(nlat, nlon, im, j, k)]) * clon +
+          (s.mfy_lat[ix3(nhalf, nlon, ic, j, k)] * cn - s.mfy_lat[ix3(nhalf, nlon, ic, j - 1, k)] * cs);
+    P[(k - 1) * ld + ti] = d;
+  }
+  __syncthreads();
+  {   // inclusive prefix sums along k, one warp per column at a time
+    const int lt = kt * kTileI + ti, lane = lt & 31, warp = lt >> 5, nw = (kTileI * KT) >> 5;
+    for (int c = warp; c < kTileI; c += nw) {
+      float carry = 0;
+      for (int base = 0; base < nlev; base += 32) {
+        const int k0 = base + lane;
+        float v = k0 < nlev ? P[k0 * ld + c] : 0.f;
+        for (int o = 1; o < 32; o <<= 1) {
+          float t = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += t;
+        }
+        v += carry;
+        if (k0 < nlev) P[k0 * ld + c] = v;
+        carry = __shfl_sync(0xffffffffu, v, 31);
+      }
+    }
+  }
+  __syncthreads();
+  const size_t c2 = (size_t)(j - 1) * nlon + (ic - 1);
+  const float dphs = -P[(nlev - 1) * ld + ti];
+  if (kt == 0 && valid) w.dphs[c2] = (double)dphs;
+  const float psr = s.psr[c2];
+  for (int k = 1 + kt; k <= nlev + 1; k += KT) {
+    float wv = 0, wm = 0;
+    if (k != 1 && k != nlev + 1) {
+      wv = -(g.hybi_f[k - 1] * dphs) - P[(k - 2) * ld + ti];
+      const float ml = 0.5f * (Mass<float>::layer(g, k - 1, psr) + Mass<float>::layer(g, k, psr));
+      wm = wv / ml * g.half_dlev_f[k - 1];
+    }
+    if (valid) s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
+    WM[(k - 1) * ld + ti] = wm;
+  }
+  __syncthreads();
+  if (!valid) return;
+  bool bad = false;
+  for (int k = 2 + kt; k <= nlev; k += KT) {
+    float c = cflz_of_f(g, WM + ti, ld, k, (float)dt, bad);
+    if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
+  }
+  if (bad) atomicOr(g.err, ERR_CFLZ);
+}
+
 // Momentum tendencies of the forward pass (gmcore_mod.F90:478-490 / 507-518):
 // du = qhv - dke/dlon - we du/dlev, dv = -qhu - dke/dlat - we dv/dlev with the
 // energy-conserving Coriolis term (calc_coriolis, operators_mod.F90:846-906),
@@ -923,8 +994,13 @@ void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R
 }
 template <class R>
 void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
+  if constexpr (std::is_same<R, float>::value) {
+    const size_t smem = g.nlev * sizeof(double) + (size_t)(2 * g.nlev + 1) * (kTileI + 1) * sizeof(float);
+    k_column_mass_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w, dt);
+    return;
+  }
   const int bt = 64;
-  size_t smem = (32 + g.nlev + 2) * sizeof(double) + (std::is_same<R, float>::value ? (size_t)(g.nlev + 1) * bt * sizeof(float) : 0);
+  size_t smem = (32 + g.nlev + 2) * sizeof(double);
   k_column_mass<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, s, w, dt);
 }
 template <class R>

@@ -114,6 +114,35 @@ __device__ __forceinline__ R ppm_tail(R sum, R fl, R df, R f6, R s1, R s2) {
   return sum + fl * ds1 + (R)0.5 * df * ds2 + f6 * (ds2 / (R)2 - div3(ds3));
 }
 
+// Sum over a warp of a double (all 32 lanes take part).
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Column tiles of the FP32 form: a block holds kTileI columns (threadIdx.x)
+// of one latitude row and spreads the levels over threadIdx.y, so every
+// level of every column is worked on in parallel; per-column vertical
+// quantities live in shared memory as [level][kTileI + 1] (padded against
+// bank conflicts).
+constexpr int kTileI = 32, kTileK = 8;
+
+// Pole ring sums of one level field by the warps of a column-tile block:
+// ring[k-1] = sgn * sum_i f(i, jv, k) * le_lat(jv) / nlon / area_cell(j).
+template <class F>
+__device__ __forceinline__ void tile_pole_ring(const DGrid &g, int j, double *ring, F f) {
+  const int lt = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = lt & 31, warp = lt >> 5, nw = (blockDim.x * blockDim.y) >> 5;
+  const int jv = j == 1 ? 1 : g.nhalf;
+  const double sgn = j == 1 ? 1.0 : -1.0;
+  for (int k = 1 + warp; k <= g.nlev; k += nw) {
+    double acc = 0;
+    for (int ii = 1 + lane; ii <= g.nlon; ii += 32) acc += (double)f(ii, jv, k);
+    acc = warp_sum(acc);
+    if (lane == 0) ring[k - 1] = sgn * acc * ROW(g.le_lat, jv) / g.nlon / ROW(g.area_cell, j);
+  }
+}
+
 // FP32 form of cflz_of over a column held as wm(l) = we(l) / ml(l) * half_dlev(l)
 // at wm[(l - 1) * stride] for l = 1 .. nlev+1: the per-level quotients are
 // formed once per column instead of once per RK4 interpolation.
