@@ -692,6 +692,106 @@ __global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const R *we, Sur
   for (int k = 1; k <= nlev; ++k) q[ix3(nlat, nlon, i, j, k)] = qc[k];
 }
 
+// FP32 form of k_tracer_vertical over column tiles: the column with copied
+// ghost levels, slopes, cell coefficients and interface fluxes in shared
+// memory, the update parallel over (column, level); the vertical fixer walks
+// a column in order and runs only in blocks that hold a negative value.
+__global__ void k_tracer_vertical_f(DGrid g, float *q, const float *cflz, const float *we, SurfP<float> sp,
+                                    double dt_adv) {
+  extern __shared__ float shf[];
+  const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev, lim = g.limiter;
+  const int j = blockIdx.y + 1;
+  const int ti = threadIdx.x, kt = threadIdx.y, KT = blockDim.y;
+  const int i = blockIdx.x * kTileI + ti + 1;
+  const int ld = kTileI + 1;
+  const bool valid = i <= nlon;
+  const int ic = valid ? i : nlon;
+  float *C = shf + ti;                  // C(l) at [(l+1)*ld], l = -1 .. nlev+2
+  float *S = C + (nlev + 4) * ld;       // s(l) at [l*ld], l = 0 .. nlev+1
+  float *FL = S + (nlev + 2) * ld;      // cell l at [(l-1)*ld]
+  float *DF = FL + nlev * ld;
+  float *F6 = DF + nlev * ld;
+  float *FZ = F6 + nlev * ld;           // interface k at [(k-1)*ld], k = 1 .. nlev+1
+  float *M = FZ + (nlev + 1) * ld;      // layer mass of level k at [(k-1)*ld]
+  const float psr = sp.at((size_t)(j - 1) * nlon + (ic - 1));
+  for (int k = 1 + kt; k <= nlev; k += KT) {
+    C[(k + 1) * ld] = q[ix3(nlat, nlon, ic, j, k)];
+    M[(k - 1) * ld] = Mass<float>::layer(g, k, psr);
+  }
+  __syncthreads();
+  if (kt == 0) {   // ghost levels copy the end levels
+    C[0] = C[1 * ld] = C[2 * ld];
+    C[(nlev + 2) * ld] = C[(nlev + 3) * ld] = C[(nlev + 1) * ld];
+  }
+  __syncthreads();
+  for (int l = kt; l <= nlev + 1; l += KT) S[l * ld] = slope(lim, C[l * ld], C[(l + 1) * ld], C[(l + 2) * ld]);
+  __syncthreads();
+  for (int l = 1 + kt; l <= nlev; l += KT) {
+    const float f = C[(l + 1) * ld], s0 = S[l * ld];
+    float fl, df, f6;
+    ppm_cell(f, s0, ppm_edge(C[l * ld], f, S[(l - 1) * ld], s0), ppm_edge(f, C[(l + 2) * ld], s0, S[(l + 1) * ld]), fl,
+             df, f6);
+    FL[(l - 1) * ld] = fl;
+    DF[(l - 1) * ld] = df;
+    F6[(l - 1) * ld] = f6;
+  }
+  __syncthreads();
+  for (int k = 1 + kt; k <= nlev + 1; k += KT) {
+    float fz = 0;
+    if (k != 1 && k != nlev + 1) {
+      const size_t ol = ix3(nlat, nlon, ic, j, k);
+      const float c = cflz[ol], wv = we[ol];
+      if (fabsf(c) < 1.0f) {
+        if (c > 0) {
+          const int u = k - 2;
+          fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
+        } else if (c < 0) {
+          const int u = k - 1;
+          fz = fdiv(-wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 0.0f, -c), c);
+        }
+      } else if (valid) {
+        fz = vflx_tile<float>(g, C, FL, DF, F6, ld, k, c, wv);
+      }
+    }
+    FZ[(k - 1) * ld] = fz;
+  }
+  __syncthreads();
+  const float dta = (float)dt_adv;
+  bool neg = false;
+  for (int k = 1 + kt; k <= nlev; k += KT) {
+    float qn = C[(k + 1) * ld] - ((FZ[k * ld] - FZ[(k - 1) * ld]) * dta) / M[(k - 1) * ld];
+    C[(k + 1) * ld] = qn;
+    neg |= valid && qn < 0;
+  }
+  if (__syncthreads_or(neg) && kt == 0 && valid) {
+    float *qc = C + ld;   // qc[k * ld] = q(k)
+    for (int k = 1; k <= nlev; ++k) {
+      float v = qc[k * ld];
+      if (v < 0) {
+        const float m0 = M[(k - 1) * ld];
+        const float qm0 = v * m0;
+        const float qm1 = k > 1 ? qc[(k - 1) * ld] * M[(k - 2) * ld] : 0.0f;
+        const float qm2 = k < nlev ? qc[(k + 1) * ld] * M[k * ld] : 0.0f;
+        const float qm0_half = 0.5f * qm0;
+        if (qm1 >= qm0_half && qm2 >= qm0_half) {
+          if (qm1 > 0) qc[(k - 1) * ld] = (qm1 - qm0_half) / M[(k - 2) * ld];
+          if (qm2 > 0) qc[(k + 1) * ld] = (qm2 - qm0_half) / M[k * ld];
+        } else if (qm1 > qm0) {
+          if (qm1 > 0) qc[(k - 1) * ld] = (qm1 - qm0) / M[(k - 2) * ld];
+        } else if (qm2 > qm0) {
+          if (qm2 > 0) qc[(k + 1) * ld] = (qm2 - qm0) / M[k * ld];
+        } else {
+          atomicOr(g.err, ERR_NEGTRACER);
+        }
+        qc[k * ld] = 0;
+      }
+    }
+  }
+  __syncthreads();
+  if (!valid) return;
+  for (int k = 1 + kt; k <= nlev; k += KT) q[ix3(nlat, nlon, i, j, k)] = C[(k + 1) * ld];
+}
+
 // Order-2 zonal smoother applied three times (lon_damp_1d, lon_damp_mod.F90:200-241).
 template <class R>
 __global__ void k_tracer_lon_damp(DGrid g, R *q) {
@@ -785,6 +885,12 @@ template <class R>
 void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz, const R *we, const SurfP<R> &sp,
                             double dt_adv) {
   const int bt = 64;
+  if constexpr (std::is_same<R, float>::value) {
+    const size_t smem = (size_t)(7 * g.nlev + 7) * (kTileI + 1) * sizeof(float);
+    k_tracer_vertical_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(
+        g, q, cflz, we, sp, dt_adv);
+    return;
+  }
   k_tracer_vertical<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, q, cflz, we, sp, dt_adv);
 }
 

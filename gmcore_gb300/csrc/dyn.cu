@@ -185,7 +185,7 @@ __global__ void k_pv_edges(DGrid g, Slot<R> s, Work<R> w) {
         val = (R)0.5 * (P(i, j) + P(i, j - 1));
       } else {
         R un = s.u_f[o], vt = w.v_lon[o];
-        R b = fabs(vt) / (sqrt(un * un + vt * vt) + eps);
+        R b = fdiv(fabs(vt), sqrt(un * un + vt * vt) + eps);
         R dir = fsign((R)1, vt);
         R up = g.upwind_order_pv == 3 ? upwind3(dir, wgt, P(i, j - 2), P(i, j - 1), P(i, j), P(i, j + 1))
                                       : upwind1(dir, wgt, P(i, j - 1), P(i, j));
@@ -202,7 +202,7 @@ __global__ void k_pv_edges(DGrid g, Slot<R> s, Work<R> w) {
         val = (R)0.5 * (P(i - 1, j) + P(i, j));
       } else {
         R ut = w.u_lat[o], vn = s.v_f[o];
-        R b = fabs(ut) / (sqrt(ut * ut + vn * vn) + eps);
+        R b = fdiv(fabs(ut), sqrt(ut * ut + vn * vn) + eps);
         R dir = fsign((R)1, ut);
         R up = g.upwind_order_pv == 3 ? upwind3(dir, wgt, P(i - 2, j), P(i - 1, j), P(i, j), P(i + 1, j))
                                       : upwind1(dir, wgt, P(i - 1, j), P(i, j));
@@ -236,13 +236,22 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
   } else if constexpr (std::is_same<R, float>::value) {
     // FP32 form of the x departure: positions in cells relative to face i,
     // (radius half_lon(l) cos - x) / dx = (l - i) - a exactly in real arithmetic.
+    // The row is staged in shared memory.
+    extern __shared__ float us[];
     const float cdx = (float)dt_ / ROWR(float, de_lon, j);
     const float lel = ROWR(float, le_lon, j), ac = ROWR(float, area_cell, j);
     const float la0 = ROWR(float, le_lat, j), la1 = ROWR(float, le_lat, j - 1);
+    const float *urow = u + ix3(nlat, nlon, 1, j, k);
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) us[l] = urow[l];
+    __syncthreads();
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      auto Ul = [&](int l) {
-        int lw = ((l - 1) % nlon + nlon) % nlon + 1;
-        return u[ix3(nlat, nlon, lw, j, k)];
+      auto Ul = [&](int l) {   // any l: a corrupted wind must not index out of the row
+        int lw = l - 1;
+        if (lw < 0 || lw >= nlon) {
+          lw %= nlon;
+          if (lw < 0) lw += nlon;
+        }
+        return us[lw];
       };
       auto at = [&](float a) {   // wind at i + a
         float fl = floorf(a);
@@ -646,6 +655,28 @@ __global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, nlon = g.nlon;
   double *row = sh, *ext = sh + nlon;
+  if constexpr (std::is_same<R, float>::value) {
+    // FP32 form: the filter runs on FP32 deviations from the row's first
+    // value; phs itself stays FP64.
+    float *dev = reinterpret_cast<float *>(sh + nlon), *fext = dev + nlon;
+    const size_t c0 = (size_t)(j - 1) * nlon;
+    const double ref = o.phs[c0] + dt * w.dphs[c0];
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const size_t c = c0 + i;
+      const double v = o.phs[c] + dt * w.dphs[c];
+      n.phs[c] = v;
+      row[i] = v;
+      dev[i] = (float)(v - ref);
+    }
+    const bool filtered = filter_row<float, float>(g.big, true, j, nlon, dev, fext);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const double f = filtered ? ref + (double)dev[i] : row[i];
+      n.phs_f[c0 + i] = f;
+      n.psr[c0 + i] = (float)(f - g.ptop);
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     size_t c = (size_t)(j - 1) * nlon + i;
     double v = o.phs[c] + dt * w.dphs[c];
@@ -990,7 +1021,8 @@ void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Wo
 }
 template <class R>
 void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt) {
-  k_batch_cfl<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, u, v, cflx, cfly, divx, divy, dt);
+  const size_t smem = std::is_same<R, float>::value ? g.nlon * sizeof(float) : 0;
+  k_batch_cfl<R><<<dim3(g.nlat, g.nlev), L.threads, smem, L.stream>>>(g, u, v, cflx, cfly, divx, divy, dt);
 }
 template <class R>
 void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
