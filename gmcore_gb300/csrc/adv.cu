@@ -23,83 +23,79 @@ namespace {
 // full-latitude rows without the poles, y fluxes on half-latitude rows.
 //   u, v  : advecting velocities (or mass fluxes for the outer operator)
 //   mx    : field reconstructed along x;  my : field reconstructed along y.
-// blockIdx.z = 0: one full row per block.  The row is staged in shared
-// memory and the PPM slope, then the limited cell coefficients, are formed
-// once per cell; each face then reads its upwind cell.
-// blockIdx.z = 1: a strip of kHflxRows half rows per block.  Each thread
-// loads its column of the strip (plus the stencil's rows) into registers and
-// forms each slope once.  Pole halo rows are read as the reference's
-// fill_halo leaves them (mirrored row shifted by nlon/2).
+// Along x a block takes one full row: the row is staged in shared memory and
+// the PPM slope, then the limited cell coefficients, are formed once per
+// cell; each face then reads its upwind cell.  Along y a block takes a strip
+// of kHflxRows half rows: each thread loads its column of the strip (plus
+// the stencil's rows) into registers and forms each slope once.  Pole halo
+// rows are read as the reference's fill_halo leaves them (mirrored row
+// shifted by nlon/2).
 constexpr int kHflxRows = 8;
 
-template <class R>
-__global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v, const R *__restrict__ cflx,
-                       const R *__restrict__ cfly, const R *__restrict__ mx, const R *__restrict__ my,
-                       R *__restrict__ fx, R *__restrict__ fy) {
-  extern __shared__ double sh_raw[];
-  const int k = blockIdx.y + 1;
-  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
-  if (blockIdx.z == 0) {
-    const int j = blockIdx.x + 1;
-    if (j == 1 || j >= nlat) return;
-    R *xs = reinterpret_cast<R *>(sh_raw);   // row values        [nlon]
-    R *ss = xs + nlon;                       // slopes            [nlon]
-    R *cl = ss + nlon;                       // limited fl        [nlon]
-    R *cd = cl + nlon;                       // limited df        [nlon]
-    R *c6 = cd + nlon;                       // f6                [nlon]
-    auto W = [nlon](int l) { return l < 0 ? l + nlon : (l >= nlon ? l - nlon : l); };   // one wrap, 0-based
-    auto Wg = [nlon](int l) {   // any l (a Courant number may exceed nlon on coarse grids)
-      if (l >= 0 && l < nlon) return l;
-      l %= nlon;
-      return l < 0 ? l + nlon : l;
-    };
-    // face inputs of this thread's first faces are requested before the
-    // shared-memory phases so that their latency overlaps them
-    constexpr int kPre = 4;
-    R cpre[kPre], upre[kPre];
+// x fluxes of full row j (2 .. nlat-1) at level k; out(i, o, flux) per face.
+// work: 5 * nlon values of shared memory.
+template <class R, class Out>
+__device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R *__restrict__ u,
+                                          const R *__restrict__ cflx, const R *__restrict__ mx, R *work, Out out) {
+  const int nlat = g.nlat, nlon = g.nlon, lim = g.limiter;
+  R *xs = work;          // row values        [nlon]
+  R *ss = xs + nlon;     // slopes            [nlon]
+  R *cl = ss + nlon;     // limited fl        [nlon]
+  R *cd = cl + nlon;     // limited df        [nlon]
+  R *c6 = cd + nlon;     // f6                [nlon]
+  auto W = [nlon](int l) { return l < 0 ? l + nlon : (l >= nlon ? l - nlon : l); };   // one wrap, 0-based
+  auto Wg = [nlon](int l) {   // any l (a Courant number may exceed nlon on coarse grids)
+    if (l >= 0 && l < nlon) return l;
+    l %= nlon;
+    return l < 0 ? l + nlon : l;
+  };
+  // face inputs of this thread's first faces are requested before the
+  // shared-memory phases so that their latency overlaps them
+  constexpr int kPre = 4;
+  R cpre[kPre], upre[kPre];
 #pragma unroll
-    for (int t = 0; t < kPre; ++t) {
-      const int i = 1 + threadIdx.x + t * blockDim.x;
-      if (i <= nlon) {
-        const size_t o = ix3(nlat, nlon, i, j, k);
-        cpre[t] = cflx[o];
-        upre[t] = u[o];
-      }
-    }
-    const R *src = mx + ix3(nlat, nlon, 1, j, k);
-    for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[l] = src[l];
-    __syncthreads();
-    for (int l = threadIdx.x; l < nlon; l += blockDim.x) ss[l] = slope(lim, xs[W(l - 1)], xs[l], xs[W(l + 1)]);
-    __syncthreads();
-    for (int l = threadIdx.x; l < nlon; l += blockDim.x) {
-      const int lm = W(l - 1), lp = W(l + 1);
-      const R f = xs[l], s0 = ss[l];
-      R fl, df, f6;
-      ppm_cell(f, s0, ppm_edge(xs[lm], f, ss[lm], s0), ppm_edge(f, xs[lp], s0, ss[lp]), fl, df, f6);
-      cl[l] = fl;
-      cd[l] = df;
-      c6[l] = f6;
-    }
-    __syncthreads();
-    const R hxr = (R)g.hx;
-    int t = 0;
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
+  for (int t = 0; t < kPre; ++t) {
+    const int i = 1 + threadIdx.x + t * blockDim.x;
+    if (i <= nlon) {
       const size_t o = ix3(nlat, nlon, i, j, k);
-      R c, uo;
-      if (t < kPre) {
+      cpre[t] = cflx[o];
+      upre[t] = u[o];
+    }
+  }
+  const R *src = mx + ix3(nlat, nlon, 1, j, k);
+  __syncthreads();   // work may still be read by a previous use
+  for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[l] = src[l];
+  __syncthreads();
+  for (int l = threadIdx.x; l < nlon; l += blockDim.x) ss[l] = slope(lim, xs[W(l - 1)], xs[l], xs[W(l + 1)]);
+  __syncthreads();
+  for (int l = threadIdx.x; l < nlon; l += blockDim.x) {
+    const int lm = W(l - 1), lp = W(l + 1);
+    const R f = xs[l], s0 = ss[l];
+    R fl, df, f6;
+    ppm_cell(f, s0, ppm_edge(xs[lm], f, ss[lm], s0), ppm_edge(f, xs[lp], s0, ss[lp]), fl, df, f6);
+    cl[l] = fl;
+    cd[l] = df;
+    c6[l] = f6;
+  }
+  __syncthreads();
+  const R hxr = (R)g.hx;
+  int t = 0;
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
+    const size_t o = ix3(nlat, nlon, i, j, k);
+    R c, uo;
+    if (t < kPre) {
 #pragma unroll
-        for (int q = 0; q < kPre; ++q)
-          if (q == t) { c = cpre[q]; uo = upre[q]; }
-      } else {
-        c = cflx[o];
-        uo = u[o];
-      }
-      R flux;
-      if (!(fabs(c) <= hxr)) {   // |cflx| beyond the reach the reference allows: error, no flux
-        atomicOr(g.err, ERR_CFLX);
-        fx[o] = 0;
-        continue;
-      }
+      for (int q = 0; q < kPre; ++q)
+        if (q == t) { c = cpre[q]; uo = upre[q]; }
+    } else {
+      c = cflx[o];
+      uo = u[o];
+    }
+    R flux;
+    if (!(fabs(c) <= hxr)) {   // |cflx| beyond the reach the reference allows: error, no flux
+      atomicOr(g.err, ERR_CFLX);
+      flux = 0;
+    } else {
       const int ci = (int)c;
       const R cf = c - (R)ci;
       if (c > 0) {
@@ -115,33 +111,73 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
       } else {
         flux = 0;
       }
-      fx[o] = flux;
     }
-    return;
+    out(i, o, flux);
   }
-  // ---- y faces on half rows j0 .. j0+kHflxRows-1
+}
+
+// Row pointer and column shift of row jj of a full-latitude field as the
+// reference's fill_halo leaves it beyond the poles.
+template <class R>
+__device__ __forceinline__ const R *halo_row(const DGrid &g, const R *f, int jj, int k, int &shift) {
+  shift = 0;
+  if (jj < 1) { jj = 2 - jj; shift = g.half; }
+  else if (jj > g.nlat) { jj = 2 * g.nlat - jj; shift = g.half; }
+  if (jj > g.nlat) jj = g.nlat;   // only rows the caller never reads
+  if (jj < 1) jj = 1;
+  return f + ix3(g.nlat, g.nlon, 1, jj, k);
+}
+
+// y flux through half row j with the column window y[t-1 .. t+2] = Y(j-1 .. j+2)
+// and slopes sl[t-1 .. t+2] at those rows.
+template <class R>
+__device__ __forceinline__ R hflx_yface(const DGrid &g, R c, R vv, const R *y, const R *sl, int t) {
+  if (!(fabs(c) <= (R)1)) {
+    atomicOr(g.err, ERR_CFLY);
+    return 0;
+  }
+  R fl, df, f6;
+  if (c > 0) {   // upwind cell j
+    ppm_cell(y[t], sl[t], ppm_edge(y[t - 1], y[t], sl[t - 1], sl[t]), ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]), fl, df,
+             f6);
+    return fdiv(vv * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
+  }
+  if (c < 0) {   // upwind cell j + 1
+    ppm_cell(y[t + 1], sl[t + 1], ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
+             ppm_edge(y[t + 1], y[t + 2], sl[t + 1], sl[t + 2]), fl, df, f6);
+    return fdiv(-vv * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
+  }
+  return 0;
+}
+
+// Outer pass: fluxes fx of qy along x with the zonal mass flux (one row per block).
+template <class R>
+__global__ void k_hflx_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ mx,
+                         R *__restrict__ fx) {
+  extern __shared__ double sh_raw[];
+  const int k = blockIdx.y + 1, j = blockIdx.x + 2;   // rows 2 .. nlat-1
+  hflx_xrow<R>(g, j, k, u, cflx, mx, reinterpret_cast<R *>(sh_raw), [&](int, size_t o, R f) { fx[o] = f; });
+}
+
+// Outer pass: fluxes fy of qx along y with the meridional mass flux (strips).
+template <class R>
+__global__ void k_hflx_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ my,
+                         R *__restrict__ fy) {
+  const int k = blockIdx.y + 1;
+  const int nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
   const int j0 = blockIdx.x * kHflxRows + 1;
   if (j0 > nhalf) return;
   constexpr int NV = kHflxRows + 5;   // rows j0-2 .. j0+kHflxRows+2
-  const R *rp[NV];
-  int rs[NV];
-#pragma unroll
-  for (int t = 0; t < NV; ++t) {
-    int jj = j0 - 2 + t, shift = 0;
-    if (jj < 1) { jj = 2 - jj; shift = g.half; }
-    else if (jj > nlat) { jj = 2 * nlat - jj; shift = g.half; }
-    if (jj > nlat) jj = nlat;   // rows past the strip's last face are never used
-    rp[t] = my + ix3(nlat, nlon, 1, jj, k);
-    rs[t] = shift;
-  }
   const int nf = min(kHflxRows, nhalf - j0 + 1);
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     R y[NV], sl[NV];
 #pragma unroll
     for (int t = 0; t < NV; ++t) {
       if (t < nf + 5) {
-        int l = i + rs[t];
-        y[t] = rp[t][l >= nlon ? l - nlon : l];
+        int sh;
+        const R *p = halo_row(g, my, j0 - 2 + t, k, sh);
+        int l = i + sh;
+        y[t] = p[l >= nlon ? l - nlon : l];
       } else {
         y[t] = 0;
       }
@@ -155,33 +191,126 @@ __global__ void k_hflx(DGrid g, const R *__restrict__ u, const R *__restrict__ v
         vy[f] = v[o];
       }
     }
-    // sl[t] = slope at row j0-2+t, t = 1 .. nf+3
 #pragma unroll
     for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
 #pragma unroll
     for (int f = 0; f < kHflxRows; ++f) {
       if (f >= nf) break;
-      const int j = j0 + f, t = f + 2;   // y[t] = Y(j)
-      const size_t o = ix3(nhalf, nlon, i + 1, j, k);
-      const R c = cy[f];
-      R flux;
-      if (!(fabs(c) <= (R)1)) {
-        atomicOr(g.err, ERR_CFLY);
-        flux = 0;
-      } else if (c > 0) {   // upwind cell j
-        R fl, df, f6;
-        ppm_cell(y[t], sl[t], ppm_edge(y[t - 1], y[t], sl[t - 1], sl[t]), ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
-                 fl, df, f6);
-        flux = fdiv(vy[f] * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
-      } else if (c < 0) {   // upwind cell j + 1
-        R fl, df, f6;
-        ppm_cell(y[t + 1], sl[t + 1], ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
-                 ppm_edge(y[t + 1], y[t + 2], sl[t + 1], sl[t + 2]), fl, df, f6);
-        flux = fdiv(-vy[f] * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
-      } else {
-        flux = 0;
+      fy[ix3(nhalf, nlon, i + 1, j0 + f, k)] = hflx_yface(g, cy[f], vy[f], y, sl, f + 2);
+    }
+  }
+}
+
+// Inner pass fused with the advective-form update (ffsl_mod.F90:353-406):
+// the advective fluxes of q stay on chip and the kernels write
+//   qx = q - dt/2 (dflux_x/dx - divx q),  qy = q - dt/2 (dflux_y/dy - divy q)
+// (pole rows: qx = q, qy from the ring mean of the polar half row's flux).
+// x: one full row per block.
+template <class R>
+__global__ void k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ q,
+                               const R *__restrict__ divx, R *__restrict__ qx, double dt) {
+  extern __shared__ double sh_raw[];
+  const int k = blockIdx.y + 1;
+  const int nlat = g.nlat, nlon = g.nlon;
+  const R hdt = (R)dt;
+  {
+    const int j = blockIdx.x + 1;
+    if (j == 1 || j == nlat) {
+      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+        const size_t o = ix3(nlat, nlon, i, j, k);
+        qx[o] = q[o];
       }
-      fy[o] = flux;
+      return;
+    }
+    R *work = reinterpret_cast<R *>(sh_raw);
+    R *frow = work + 5 * nlon;
+    hflx_xrow<R>(g, j, k, u, cflx, q, work, [&](int i, size_t, R f) { frow[i - 1] = f; });
+    __syncthreads();
+    const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j);
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      const size_t o = ix3(nlat, nlon, i, j, k);
+      const R qv = q[o];
+      const R fxe = frow[i - 1], fxw = frow[i == 1 ? nlon - 1 : i - 2];
+      qx[o] = qv - (R)0.5 * ((fxe - fxw) * lel / ac - divx[o] * qv) * hdt;
+    }
+  }
+}
+
+// y: strips whose faces start one half row below the strip, so that every
+// full row of the strip has both of its faces.
+template <class R>
+__global__ void __launch_bounds__(256, 4) k_ffsl_inner_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ q,
+                               const R *__restrict__ divy, R *__restrict__ qy, double dt) {
+  __shared__ double red[32];
+  const int k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
+  const R hdt = (R)dt;
+  const int j0 = blockIdx.x * kHflxRows + 1;
+  if (j0 > nhalf) return;
+  constexpr int NF = kHflxRows + 1;   // faces j0-1 .. j0+kHflxRows-1
+  constexpr int NV = kHflxRows + 6;   // rows j0-3 .. j0+kHflxRows+2
+  const int fl0 = j0 >= 2 ? 0 : 1;                       // first existing face
+  const int nfe = min(kHflxRows, nhalf - j0 + 1) + 1;    // faces up to nhalf
+  const bool has_s = j0 == 1, has_n = j0 <= nhalf && nhalf <= j0 + kHflxRows - 1;
+  double ring_s = 0, ring_n = 0;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    R y[NV], sl[NV];
+#pragma unroll
+    for (int t = 0; t < NV; ++t) {
+      if (t < nfe + 5) {
+        int sh;
+        const R *p = halo_row(g, q, j0 - 3 + t, k, sh);
+        int l = i + sh;
+        y[t] = p[l >= nlon ? l - nlon : l];
+      } else {
+        y[t] = 0;
+      }
+    }
+    R cy[NF], vy[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      if (f >= fl0 && f < nfe) {
+        const size_t o = ix3(nhalf, nlon, i + 1, j0 - 1 + f, k);
+        cy[f] = cfly[o];
+        vy[f] = v[o];
+      }
+    }
+#pragma unroll
+    for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
+    // faces in order; full row j0+f-1 is finished once face f (its north face) is known
+    R prev = 0;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      R cur = 0;
+      if (f >= fl0 && f < nfe) cur = hflx_yface(g, cy[f], vy[f], y, sl, f + 2);
+      const int jf = j0 - 1 + f;   // half row of face f
+      if (has_s && jf == 1) ring_s += (double)cur;
+      if (has_n && jf == nhalf) ring_n += (double)cur;
+      const int j = jf;            // full row whose north face is jf
+      if (f >= 1 && j >= 2 && j <= nlat - 1 && f < nfe) {
+        const size_t o = ix3(nlat, nlon, i + 1, j, k);
+        const R la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1), ac = ROWR(R, area_cell, j);
+        const R qv = y[f + 2];   // y[t] = Y(j0 - 3 + t)
+        qy[o] = qv - (R)0.5 * ((cur * la0 - prev * la1) / ac - divy[o] * qv) * hdt;
+      }
+      prev = cur;
+    }
+  }
+  // pole rows from the ring of their polar half row
+  for (int side = 0; side < 2; ++side) {
+    const bool has = side == 0 ? has_s : has_n;
+    if (!has) continue;
+    const int j = side == 0 ? 1 : nlat, jv = side == 0 ? 1 : nhalf;
+    double p = block_sum(side == 0 ? ring_s : ring_n, red);
+    p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
+    const R pole = (R)p;
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+      const size_t o = ix3(nlat, nlon, i, j, k);
+      const R qv = q[o];
+      if (j == 1)
+        qy[o] = qv - (R)0.5 * (pole - divy[o] * qv) * hdt;
+      else
+        qy[o] = qv + (R)0.5 * (pole - divy[o] * qv) * hdt;
     }
   }
 }
@@ -821,13 +950,16 @@ __global__ void k_tracer_lon_damp(DGrid g, R *q) {
 template <class R>
 void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy,
                       R *fx, R *fy, double dt) {
-  dim3 grid(g.nlat, g.nlev);
-  dim3 hgrid(g.nlat, g.nlev, 2);   // z = 0: x rows, z = 1: y strips (first ceil(nhalf / kHflxRows) blocks)
-  const size_t smem = (size_t)5 * g.nlon * sizeof(R);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_hflx<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_hflx<R><<<hgrid, L.threads, smem, L.stream>>>(g, b.u, b.v, b.cflx, b.cfly, q, q, qmfx, qmfy);
-  k_qxqy<R><<<grid, L.threads, 0, L.stream>>>(g, q, qmfx, qmfy, b.divx, b.divy, qx, qy, dt);
-  k_hflx<R><<<hgrid, L.threads, smem, L.stream>>>(g, b.mfx, b.mfy, b.cflx, b.cfly, qy, qx, fx, fy);
+  (void)qmfx;
+  (void)qmfy;
+  const dim3 rows(g.nlat, g.nlev), inner_rows(g.nlat - 2, g.nlev), strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
+  const size_t smem_o = (size_t)5 * g.nlon * sizeof(R), smem_i = (size_t)6 * g.nlon * sizeof(R);
+  if (smem_o > 48 * 1024) cudaFuncSetAttribute(k_hflx_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
+  if (smem_i > 48 * 1024) cudaFuncSetAttribute(k_ffsl_inner_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i);
+  k_ffsl_inner_x<R><<<rows, L.threads, smem_i, L.stream>>>(g, b.u, b.cflx, q, b.divx, qx, dt);
+  k_ffsl_inner_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
+  k_hflx_x<R><<<inner_rows, L.threads, smem_o, L.stream>>>(g, b.mfx, b.cflx, qy, fx);
+  k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
 }
 
 template <class R>
