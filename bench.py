@@ -130,16 +130,20 @@ class ClockSampler:
 
 # Algorithmic (compulsory) bytes of one launch of each kernel group, in units
 # of N s (N = nlon nlat nlev cells, s = bytes of a bulk value), N 8 (FP64
-# level fields) and H 8 (FP64 surface fields).  Each entry counts the bulk
-# fields a kernel must read and write once.
+# level fields) and H 8 (FP64 surface fields): the fields the group must read
+# and write once.  FFSL counts its operator inputs (q, u, v, mfx, mfy, cflx,
+# cfly, divx, divy) and outputs (fx, fy), not the qx/qy intermediates.
 KERNEL_BYTES = {
-    "mass_flux": (4, 0, 1), "tangent_winds": (4, 0, 1), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 1),
-    "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (3, 1, 2), "ffsl_hflx_pt": (22, 0, 0),
-    "pt_tendency": (5, 1, 0), "momentum_tend": (9, 1, 1), "update_phs": (0, 0, 4), "update_pt": (3, 0, 2),
-    "column_backward": (1, 2, 2), "update_uv": (8, 2, 0), "div_damp": (7, 0, 0), "tracer_accum": (2, 1, 1),
-    "tracer_batch_cfl": (6, 0, 0), "tracer_batch_cflz": (1, 2, 0), "ffsl_hflx_tracer": (22, 0, 0),
-    "tracer_horizontal": (4, 0, 2), "tracer_vertical": (3, 1, 1), "tracer_lon_damp": (0.3, 0, 0),
+    "mass_flux": (4, 0, 0.5), "tangent_winds": (4, 0, 0.5), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 0.5),
+    "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (4, 0, 1.5), "ffsl_hflx_pt": (11, 0, 0),
+    "pt_tendency": (6, 0, 0), "momentum_tend": (10, 0, 0.5), "update_phs": (0, 0, 4.5), "update_pt": (3, 0, 1),
+    "column_backward": (2, 1, 2), "update_uv": (9, 1, 0), "div_damp": (7, 0, 0), "tracer_accum": (4, 0, 0),
+    "tracer_batch_cfl": (6, 0, 0), "tracer_batch_cflz": (3, 0, 0), "ffsl_hflx_tracer": (11, 0, 0),
+    "tracer_horizontal": (4, 0, 1), "tracer_vertical": (4, 0, 0.5), "tracer_lon_damp": (0.3, 0, 0),
+    "surface_rel": (0, 0, 1.5),
 }
+# groups that launch more than one kernel (not a single kernel's roofline)
+MULTI_KERNEL = {"ffsl_hflx_pt", "ffsl_hflx_tracer", "tracer_accum", "div_damp"}
 
 
 def algorithmic_bytes(name, cfg, s):
@@ -147,6 +151,25 @@ def algorithmic_bytes(name, cfg, s):
     h = cfg.nlon * cfg.nlat
     a, b, c = KERNEL_BYTES.get(name, (0, 0, 0))
     return a * n * s + b * n * 8 + c * h * 8
+
+
+def step_compulsory_bytes(cfg, s, ntracer):
+    """Compulsory HBM bytes of one step when every intermediate stays on chip:
+    per stage the dynamics read/write 16 bulk fields (3 stages), tracers 2 per
+    tracer plus 10 shared batch fields, plus ~18 FP64 surface fields."""
+    n = cfg.nlon * cfg.nlat * cfg.nlev
+    h = cfg.nlon * cfg.nlat
+    return n * s * (48 + 2 * ntracer + 10) + 18 * h * 8
+
+
+def measured_traffic(name):
+    """DRAM bytes per launch of a kernel group from the committed ncu launch
+    list summary (profiles/kernel_traffic_c2_mixed.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "kernel_traffic_c2_mixed.json")) as f:
+            return json.load(f)["groups"].get(name)
+    except Exception:
+        return None
 
 
 def state_bytes(state):
@@ -197,7 +220,8 @@ def run_ours(args):
     sdpd_rank = DT * args.steps / (dev_ms / 1000.0)
     value = sdpd_rank * WORLD
     launches_per_step = stats["kernel_launches"] / args.steps
-    ps_mixed = model.get_field("phs")   # after warmup + steps, compared with FP64 below
+    # state after warmup + steps, compared with the FP64 form below
+    mixed_state = {name: model.get_field(name) for name in ("phs", "u_lon", "v_lat", "pt")}
 
     if args.device_only:
         model.close()
@@ -241,12 +265,16 @@ def run_ours(args):
     prof = model.kernel_profile()
     model.set_profiling(False)
     total = sum(ms for ms, _ in prof.values())
-    top = max(prof.items(), key=lambda kv: kv[1][0])
+    singles = {k: v for k, v in prof.items() if k not in MULTI_KERNEL}
+    top = max(singles.items(), key=lambda kv: kv[1][0])
     top_name, (top_ms, top_n) = top
     per_launch_ms = top_ms / top_n
     alg = algorithmic_bytes(top_name, cfg, 4)
     peak, peak_kind = measured_peaks()
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
+    traffic = measured_traffic(top_name)
+    b_step = step_compulsory_bytes(cfg, 4, NTRACER)
+    ncell = cfg.nlon * cfg.nlat * cfg.nlev
     model.close()
 
     # ---- FP64 form on the same initial state ----
@@ -258,9 +286,14 @@ def run_ours(args):
     m64.step(args.steps)
     barrier()
     ms64 = max_over_ranks(m64.stats()["step_ms"]) / args.steps
-    ps64 = m64.get_field("phs")
+    errors = {}
+    for name, a in mixed_state.items():
+        d = a - m64.get_field(name)
+        scale = 100.0 if name == "phs" else 1.0   # phs in hPa
+        errors[name] = {"rms": float(np.sqrt(np.mean(d * d)) / scale), "max": float(np.max(np.abs(d)) / scale),
+                        "unit": "hPa" if name == "phs" else ("K" if name == "pt" else "m/s")}
     m64.close()
-    ps_rms_hpa = float(np.sqrt(np.mean((ps_mixed - ps64) ** 2)) / 100.0)
+    ps_rms_hpa = errors["phs"]["rms"]
 
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
@@ -286,15 +319,20 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (state ~1.5 GB)"},
             "fp64": {"ms_per_step": ms64, "value": DT / (ms64 / 1000.0) * WORLD,
                      "mixed_speedup": ms64 / ms_per_step, "ps_rms_diff_hpa_after_steps": ps_rms_hpa,
-                     "steps_compared": args.warmup + args.steps},
+                     "steps_compared": args.warmup + args.steps, "mixed_minus_fp64": errors},
             "e2e": {"value": e2e_value, "unit": "sim days/wall-day", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
                     "path": "gmc_set_field/gmc_set_tracer + gmc_step(1) + gmc_get_field/gmc_get_tracer, host float64"},
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": alg, "avg_launch_ms": per_launch_ms,
-                         "share_of_step": top_ms / total if total else None},
+                         "share_of_step": top_ms / total if total else None,
+                         "traffic_source": "profiles/kernel_traffic_c2_mixed.json (ncu dram__bytes per launch)"},
+            "step_roofline": {"compulsory_bytes_per_step": b_step, "achieved_gbs": b_step / (ms_per_step / 1000.0) / 1e9,
+                              "frac": b_step / (ms_per_step / 1000.0) / 1e9 / peak,
+                              "note": "all intermediates on chip; 16 N s per stage, 2 N s per tracer, 10 N s batch"},
+            "cell_updates_per_s": ncell * args.steps / (dev_ms / 1000.0) * WORLD,
             "kernel_ms_per_step": {k: round(v[0] / 3.0, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clk,
         }

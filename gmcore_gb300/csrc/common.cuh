@@ -122,8 +122,10 @@ struct SurfP<float> {
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); }
 
+// Offset of (i, j, k) in a [k][j][i] field; 32-bit arithmetic (grids are
+// validated to (nlev+1) * nlat * nlon < 2^31).
 __device__ __forceinline__ size_t ix3(int nrow, int nlon, int i, int j, int k) {
-  return ((size_t)(k - 1) * nrow + (j - 1)) * nlon + (i - 1);
+  return (size_t)(((unsigned)(k - 1) * (unsigned)nrow + (unsigned)(j - 1)) * (unsigned)nlon + (unsigned)(i - 1));
 }
 
 // Read a full-latitude field at any (i, j) the reference's stencils touch.

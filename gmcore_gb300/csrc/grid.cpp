@@ -243,6 +243,8 @@ std::string validate_config(const gmc_config &c) {
   if (c.n_members < 1) return "n_members must be >= 1";
   if (c.use_div_damp && c.div_damp_order != 2) return "only div_damp_order = 2 is supported";
   if (c.lon_halo_width < 1) return "lon_halo_width must be >= 1";
+  // device kernels index one field with 32-bit arithmetic
+  if ((double)(c.nlev + 1) * c.nlat * c.nlon >= 2147483647.0) return "grid too large: (nlev+1)*nlat*nlon must be < 2^31";
   return "";
 }
 
