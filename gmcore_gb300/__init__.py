@@ -28,7 +28,10 @@ EXPORTED = (
     "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
+    "gmc_tlm_step", "gmc_adjoint",
 )
+# state fields of the tangent-linear and adjoint entry points, in ABI order
+TLAD_FIELDS = ("u_lon", "v_lat", "gz")
 
 _lib = None
 
@@ -74,6 +77,8 @@ def load(build_if_missing=True):
     lib.gmc_ffsl_hflx.argtypes = [C.c_void_p, P(FfslFields), C.c_double]
     lib.gmc_ffsl_hflx_noalloc.argtypes = [C.c_void_p, P(FfslFields), C.c_double]
     lib.gmc_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    lib.gmc_tlm_step.argtypes = [C.c_void_p, C.c_int32, P(View), P(View)]
+    lib.gmc_adjoint.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View), P(View)]
     lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
     _lib = lib
     return lib
@@ -204,6 +209,34 @@ class Model:
         out = np.zeros(field_shape(self.cfg, name))
         self._check(self.lib.gmc_get_field(self.h, member, name.encode(), C.byref(view_of(out))))
         return out
+
+    def _views3(self, fields, fill=None):
+        arrs = []
+        for name in TLAD_FIELDS:
+            if fill is None:
+                a = np.ascontiguousarray(fields[name], dtype=np.float64).reshape(field_shape(self.cfg, name))
+            else:
+                a = np.zeros(field_shape(self.cfg, name))
+            arrs.append(a)
+        views = (View * 3)(*[view_of(a) for a in arrs])
+        return arrs, views
+
+    def tlm_step(self, nsteps, dx0):
+        """Tangent-linear model over nsteps from the prepared state:
+        {u_lon, v_lat, gz} perturbation at step 0 -> perturbation at nsteps.
+        The model itself advances nsteps."""
+        keep_in, vin = self._views3(dx0)
+        out, vout = self._views3(None, fill=True)
+        self._check(self.lib.gmc_tlm_step(self.h, nsteps, vin, vout))
+        return dict(zip(TLAD_FIELDS, out))
+
+    def adjoint(self, nsteps, lam_n, ckpt_every=8):
+        """Adjoint over nsteps from the prepared state: gradient of J with
+        respect to {u_lon, v_lat, gz} at step nsteps -> at step 0."""
+        keep_in, vin = self._views3(lam_n)
+        out, vout = self._views3(None, fill=True)
+        self._check(self.lib.gmc_adjoint(self.h, nsteps, ckpt_every, vin, vout))
+        return dict(zip(TLAD_FIELDS, out))
 
     def set_tracer(self, l, q, member=0):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.cfg.nlev, self.cfg.nlat, self.cfg.nlon)

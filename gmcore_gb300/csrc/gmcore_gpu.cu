@@ -98,6 +98,10 @@ struct EngineBase {
   virtual void ffsl_hflx(const gmc_ffsl_fields &f, double dt) = 0;
   virtual size_t ffsl_scratch_bytes() const = 0;
   virtual void ffsl_hflx_in(const gmc_ffsl_fields &f, double dt, void *scratch) = 0;
+  // tangent-linear and adjoint of nsteps steps from the prepared state; the
+  // three fields are u_lon, v_lat, gz (host, dense interior arrays)
+  virtual void tlm(int nsteps, const double *const dx0[3], double *const dxn[3]) = 0;
+  virtual void adjoint(int nsteps, int ckpt, const double *const lam_n[3], double *const lam_0[3]) = 0;
   long time_step = 0;
   int device = 0;   // device current when the context was created
   // timing and profiling
@@ -284,6 +288,7 @@ struct Engine : EngineBase {
     if (ev_b) cudaEventDestroy(ev_b);
     arena.release();
     tables.release();
+    if (tl) tl->arena.release();
     if (pinned) cudaFreeHost(pinned);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -655,8 +660,8 @@ struct Engine : EngineBase {
   }
 
   // operators_prepare forward list (operators_mod.F90:117-122)
-  void forward_prepare(int m, const Slot<R> &s) {
-    Work<R> &w = work[m];
+  void forward_prepare(int m, const Slot<R> &s) { forward_prepare_w(work[m], s); }
+  void forward_prepare_w(Work<R> &w, const Slot<R> &s) {
     K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
     K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
     K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
@@ -665,9 +670,9 @@ struct Engine : EngineBase {
   }
 
   // space_operators forward pass (gmcore_mod.F90:467-528)
-  void forward(int m, const Slot<R> &s, double dt) {
-    Work<R> &w = work[m];
-    forward_prepare(m, s);
+  void forward(int m, const Slot<R> &s, double dt) { forward_w(work[m], s, dt); }
+  void forward_w(Work<R> &w, const Slot<R> &s, double dt) {
+    forward_prepare_w(w, s);
     if (grid.cfg.baroclinic) {
       K("batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt); });
       K("column_mass", 1, [&] { launch_column_mass<R>(dg, L, s, w, dt); });
@@ -684,9 +689,10 @@ struct Engine : EngineBase {
 
   // step_forward_backward (time_schemes_mod.F90:102-118)
   void stage(int m, int o, int s, int n, double dt) {
-    const Slot<R> &O = slots[m * 3 + o], &S = slots[m * 3 + s], &N = slots[m * 3 + n];
-    Work<R> &w = work[m];
-    forward(m, S, dt);
+    stage_io(slots[m * 3 + o], slots[m * 3 + s], slots[m * 3 + n], work[m], dt);
+  }
+  void stage_io(const Slot<R> &O, const Slot<R> &S, const Slot<R> &N, Work<R> &w, double dt) {
+    forward_w(w, S, dt);
     if (grid.cfg.baroclinic) {
       K("update_phs", 1, [&] { launch_update_phs<R>(dg, L, O, N, w, dt); });
       K("update_pt", 1, [&] { launch_update_pt<R>(dg, L, O, N, w, dt); });
@@ -721,6 +727,240 @@ struct Engine : EngineBase {
     CK(cudaStreamSynchronize(stream));
     prepared = true;
     time_step = 0;
+  }
+
+  // -------------------------------------------------------------------------
+  // Tangent-linear and adjoint of the shallow-water step (FP64).
+  //
+  // States X[0..nst] hold the step's start state and the stage outputs
+  // (stage st: old X[0], star X[S(st)], new X[st+1]); D[] and A[] are their
+  // tangents and adjoints.  The adjoint re-runs the step's stages from its
+  // start state, then walks the stages backwards: adjoint of the updates
+  // (consumes A[new], adds to A[0]), adjoint of the forward pass at the star
+  // state (adds to A[star]).  Step start states come from checkpoints every
+  // `ckpt` steps and a forward recomputation inside each segment.
+  // -------------------------------------------------------------------------
+  struct Tlad {
+    Arena arena;
+    Slot<double> X[4], D[4], A[4], DS, AS;   // DS/AS: tangent/adjoint work slots (mfx, mfy, pv*)
+    Work<double> WF, DW, AW;
+    double *su = nullptr, *sv = nullptr;
+    bool ready = false;
+  };
+  std::unique_ptr<Tlad> tl;
+
+  int tlad_stages() const { return grid.cfg.time_scheme == GMC_TIME_EULER ? 1 : 3; }
+  double tlad_dt(int st) const {
+    const double dt = grid.cfg.dt_dyn;
+    if (grid.cfg.time_scheme == GMC_TIME_EULER) return dt;
+    if (grid.cfg.time_scheme == GMC_TIME_PC2) return st == 2 ? dt : dt / 2.0;
+    return st == 0 ? dt / 3.0 : (st == 1 ? dt / 2.0 : dt);
+  }
+  static int tlad_star(int st) { return st; }   // star of stage st is X[st] (X[0] for the first)
+
+  void tlad_check() {
+    if (!std::is_same<R, double>::value || grid.cfg.baroclinic)
+      throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: available for the FP64 shallow-water model"};
+    if (nm != 1) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: one member"};
+    if (grid.cfg.use_div_damp) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: divergence damping not differentiated"};
+    if (!grid.cfg.pv_pole_stokes) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: needs pv_pole_stokes"};
+    if (!prepared || time_step != 0) throw ApiError{GMC_ESTATE, "tangent-linear/adjoint start from the prepared state (gmc_prepare)"};
+  }
+
+  size_t state_bytes() const { return (3 * full3() + 2 * half3() + 0) * sizeof(double) + 8 * 256; }
+  // copy the prognostic fields (u, v, gz and their filtered copies)
+  void copy_state(const Slot<R> &d, const Slot<R> &s) {
+    CK(cudaMemcpyAsync(d.u_lon, s.u_lon, full3() * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+    CK(cudaMemcpyAsync(d.u_f, s.u_f, full3() * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+    CK(cudaMemcpyAsync(d.v_lat, s.v_lat, half3() * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+    CK(cudaMemcpyAsync(d.v_f, s.v_f, half3() * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+    CK(cudaMemcpyAsync(d.gz, s.gz, two_d() * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+    CK(cudaMemcpyAsync(d.gz_f, s.gz_f, two_d() * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+  }
+  void zero_state(const Slot<R> &d) {
+    CK(cudaMemsetAsync(d.u_lon, 0, full3() * sizeof(R), stream));
+    CK(cudaMemsetAsync(d.u_f, 0, full3() * sizeof(R), stream));
+    CK(cudaMemsetAsync(d.v_lat, 0, half3() * sizeof(R), stream));
+    CK(cudaMemsetAsync(d.v_f, 0, half3() * sizeof(R), stream));
+    CK(cudaMemsetAsync(d.gz, 0, two_d() * sizeof(R), stream));
+    CK(cudaMemsetAsync(d.gz_f, 0, two_d() * sizeof(R), stream));
+  }
+  // a flat copy of the six prognostic fields, for checkpoints
+  void flat_save(R *dst, const Slot<R> &s) {
+    R *q = dst;
+    for (auto f : {std::make_pair(s.u_lon, full3()), std::make_pair(s.u_f, full3()), std::make_pair(s.v_lat, half3()),
+                   std::make_pair(s.v_f, half3()), std::make_pair(s.gz, two_d()), std::make_pair(s.gz_f, two_d())}) {
+      CK(cudaMemcpyAsync(q, f.first, f.second * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+      q += f.second;
+    }
+  }
+  void flat_load(const Slot<R> &d, const R *src) {
+    const R *q = src;
+    for (auto f : {std::make_pair(d.u_lon, full3()), std::make_pair(d.u_f, full3()), std::make_pair(d.v_lat, half3()),
+                   std::make_pair(d.v_f, half3()), std::make_pair(d.gz, two_d()), std::make_pair(d.gz_f, two_d())}) {
+      CK(cudaMemcpyAsync(f.first, q, f.second * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+      q += f.second;
+    }
+  }
+  size_t flat_count() const { return 2 * full3() + 2 * half3() + 2 * two_d(); }
+
+  void tlad_alloc() {
+    if (tl && tl->ready) return;
+    tl.reset(new Tlad());
+    auto carve_all = [&](auto &a) {
+      for (int t = 0; t < 4; ++t) {
+        carve(a, tl->X[t], false);
+        carve(a, tl->D[t], false);
+        carve(a, tl->A[t], false);
+      }
+      carve(a, tl->DS, false);
+      carve(a, tl->AS, false);
+      carve(a, tl->WF, false);
+      carve(a, tl->DW, false);
+      carve(a, tl->AW, false);
+      tl->su = a.template take<double>(full3());
+      tl->sv = a.template take<double>(half3());
+    };
+    Counter cnt;
+    carve_all(cnt);
+    tl->arena.reserve(cnt.used + 4096);
+    carve_all(tl->arena);
+    for (int t = 0; t < 4; ++t) tl->X[t].gzs = tl->D[t].gzs = tl->A[t].gzs = gzs[0];
+    tl->DS.gzs = tl->AS.gzs = gzs[0];
+    tl->WF.gzs = tl->DW.gzs = tl->AW.gzs = gzs[0];
+    tl->ready = true;
+  }
+
+  // tangent slot of the star state with the tangent work arrays
+  Slot<R> with_work(const Slot<R> &st, const Slot<R> &wk) {
+    Slot<R> c = st;
+    c.mfx_lon = wk.mfx_lon; c.mfy_lat = wk.mfy_lat; c.pv = wk.pv; c.pv_lon = wk.pv_lon; c.pv_lat = wk.pv_lat;
+    return c;
+  }
+
+  void tlad_step_forward() {
+    const int nst = tlad_stages();
+    for (int st = 0; st < nst; ++st) stage_io(tl->X[0], tl->X[tlad_star(st)], tl->X[st + 1], tl->WF, tlad_dt(st));
+    std::swap(tl->X[0], tl->X[nst]);
+  }
+
+  void upload3(const Slot<R> &d, const double *const h[3]) {
+    CK(cudaMemcpyAsync(d.u_lon, h[0], full3() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.v_lat, h[1], half3() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.gz, h[2], two_d() * sizeof(double), cudaMemcpyHostToDevice, stream));
+  }
+  void download3(double *const h[3], const Slot<R> &s) {
+    CK(cudaMemcpyAsync(h[0], s.u_lon, full3() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h[1], s.v_lat, half3() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h[2], s.gz, two_d() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  void tlm(int nsteps, const double *const dx0[3], double *const dxn[3]) override {
+    if constexpr (std::is_same<R, double>::value) {
+      tlad_check();
+      tlad_alloc();
+      Tlad &T = *tl;
+      const int nst = tlad_stages();
+      copy_state(T.X[0], slots[old_i]);
+      for (int t = 0; t < 4; ++t) zero_state(T.D[t]);
+      upload3(T.D[0], dx0);
+      launch_filter_prologue<R>(dg, L, T.D[0]);   // the prologue filters are linear
+      for (int it = 0; it < nsteps; ++it) {
+        for (int st = 0; st < nst; ++st) {
+          const double dt = tlad_dt(st);
+          const Slot<R> &S = T.X[tlad_star(st)];
+          forward_w(T.WF, S, dt);
+          const Slot<R> Tc = with_work(T.D[tlad_star(st)], T.DS);
+          tl_forward_prepare(dg, L, S, T.WF, Tc, T.DW);
+          launch_swm_dgz<R>(dg, L, Tc, T.DW);   // linear in the mass fluxes
+          tl_momentum(dg, L, S, Tc, T.DW);
+          launch_update_gz<R>(dg, L, T.X[0], T.X[st + 1], T.WF, dt);
+          launch_update_uv<R>(dg, L, T.X[0], T.X[st + 1], T.WF, dt);
+          launch_update_gz<R>(dg, L, T.D[0], T.D[st + 1], T.DW, dt);   // linear updates
+          launch_update_uv<R>(dg, L, T.D[0], T.D[st + 1], T.DW, dt);
+        }
+        std::swap(T.X[0], T.X[nst]);
+        std::swap(T.D[0], T.D[nst]);
+      }
+      CK(cudaGetLastError());
+      copy_state(slots[old_i], T.X[0]);
+      time_step += nsteps;
+      download3(dxn, T.D[0]);
+    } else {
+      (void)nsteps; (void)dx0; (void)dxn;
+      throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: available for the FP64 shallow-water model"};
+    }
+  }
+
+  void adjoint(int nsteps, int ckpt, const double *const lam_n[3], double *const lam_0[3]) override {
+    if constexpr (std::is_same<R, double>::value) {
+      tlad_check();
+      if (ckpt < 1) throw ApiError{GMC_EINVAL, "ckpt_every must be >= 1"};
+      tlad_alloc();
+      Tlad &T = *tl;
+      const int nst = tlad_stages();
+      const int k = std::min(ckpt, std::max(nsteps, 1));
+      const int nseg = (nsteps + k - 1) / k;
+      const size_t fc = flat_count();
+      Arena store;
+      struct Release {
+        Arena &a;
+        ~Release() { a.release(); }
+      } release_store{store};
+      store.reserve(((size_t)nseg + (size_t)k) * (fc * sizeof(R) + 256) + 4096);
+      std::vector<R *> cp(nseg), sb(k);
+      for (int c = 0; c < nseg; ++c) cp[c] = store.template take<R>(fc);
+      for (int c = 0; c < k; ++c) sb[c] = store.template take<R>(fc);
+      // forward sweep with checkpoints
+      copy_state(T.X[0], slots[old_i]);
+      for (int it = 0; it < nsteps; ++it) {
+        if (it % k == 0) flat_save(cp[it / k], T.X[0]);
+        tlad_step_forward();
+      }
+      copy_state(slots[old_i], T.X[0]);   // the model ends at step nsteps
+      // adjoint of the final state
+      for (int t = 0; t < 4; ++t) zero_state(T.A[t]);
+      upload3(T.A[nst], lam_n);
+      for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int s0 = seg * k, s1 = std::min(nsteps, s0 + k);
+        flat_load(T.X[0], cp[seg]);
+        for (int it = s0; it < s1; ++it) {
+          flat_save(sb[it - s0], T.X[0]);
+          if (it + 1 < s1) tlad_step_forward();
+        }
+        for (int it = s1 - 1; it >= s0; --it) {
+          flat_load(T.X[0], sb[it - s0]);
+          for (int st = 0; st + 1 < nst; ++st) stage_io(T.X[0], T.X[tlad_star(st)], T.X[st + 1], T.WF, tlad_dt(st));
+          for (int st = nst - 1; st >= 0; --st) {
+            const double dt = tlad_dt(st);
+            const Slot<R> &S = T.X[tlad_star(st)];
+            forward_w(T.WF, S, dt);   // linearisation point of this stage
+            ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.su, T.sv, dt);
+            CK(cudaMemsetAsync(T.AS.mfx_lon, 0, full3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AS.mfy_lat, 0, half3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AS.pv, 0, half3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AS.pv_lon, 0, full3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AS.pv_lat, 0, half3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AW.u_lat, 0, half3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AW.v_lon, 0, full3() * sizeof(R), stream));
+            CK(cudaMemsetAsync(T.AW.ke, 0, full3() * sizeof(R), stream));
+            ad_forward(dg, L, S, T.WF, with_work(T.A[tlad_star(st)], T.AS), T.AW);
+          }
+          // A[0] is the adjoint of the step's start state: it seeds the step before
+          std::swap(T.A[0], T.A[nst]);
+          for (int t = 0; t < nst; ++t) zero_state(T.A[t]);
+        }
+      }
+      ad_prologue(dg, L, T.A[nst]);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(stream));
+      time_step += nsteps;
+      download3(lam_0, T.A[nst]);
+    } else {
+      (void)nsteps; (void)ckpt; (void)lam_n; (void)lam_0;
+      throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: available for the FP64 shallow-water model"};
+    }
   }
 
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
@@ -1124,6 +1364,69 @@ int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt) {
     int rc = noalloc_scratch_address(ctx->eng->device, &scr, err);
     if (rc != GMC_OK) throw ApiError{rc, err};
     ctx->eng->ffsl_hflx_in(*f, dt, scr);
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
+}
+
+namespace {
+const char *const kTladFields[3] = {"u_lon", "v_lat", "gz"};
+}
+
+int gmc_tlm_step(gmc_ctx *ctx, int32_t nsteps, const gmc_view dx0[3], const gmc_view dxn[3]) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!dx0 || !dxn) return fail(ctx, GMC_EINVAL, "null view array");
+  if (nsteps < 0) return fail(ctx, GMC_EINVAL, "nsteps < 0");
+  return guarded(ctx, [&]() {
+    std::vector<double> in[3], out[3];
+    const double *pin[3];
+    double *pout[3];
+    for (int f = 0; f < 3; ++f) {
+      int nrow, nk;
+      std::string err;
+      field_dims(ctx->cfg, kTladFields[f], nrow, nk);
+      if (!unpack_view(&dx0[f], ctx->cfg.nlon, nrow, nk, in[f], err)) throw ApiError{GMC_EINVAL, err};
+      out[f].assign((size_t)ctx->cfg.nlon * nrow * nk, 0.0);
+      pin[f] = in[f].data();
+      pout[f] = out[f].data();
+    }
+    ctx->eng->tlm(nsteps, pin, pout);
+    for (int f = 0; f < 3; ++f) {
+      int nrow, nk;
+      std::string err;
+      field_dims(ctx->cfg, kTladFields[f], nrow, nk);
+      if (!pack_view(&dxn[f], ctx->cfg.nlon, nrow, nk, out[f], err)) throw ApiError{GMC_EINVAL, err};
+    }
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
+}
+
+int gmc_adjoint(gmc_ctx *ctx, int32_t nsteps, int32_t ckpt_every, const gmc_view lambda_n[3], const gmc_view lambda_0[3]) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!lambda_n || !lambda_0) return fail(ctx, GMC_EINVAL, "null view array");
+  if (nsteps < 0) return fail(ctx, GMC_EINVAL, "nsteps < 0");
+  if (ckpt_every < 1) return fail(ctx, GMC_EINVAL, "ckpt_every must be >= 1");
+  return guarded(ctx, [&]() {
+    std::vector<double> in[3], out[3];
+    const double *pin[3];
+    double *pout[3];
+    for (int f = 0; f < 3; ++f) {
+      int nrow, nk;
+      std::string err;
+      field_dims(ctx->cfg, kTladFields[f], nrow, nk);
+      if (!unpack_view(&lambda_n[f], ctx->cfg.nlon, nrow, nk, in[f], err)) throw ApiError{GMC_EINVAL, err};
+      out[f].assign((size_t)ctx->cfg.nlon * nrow * nk, 0.0);
+      pin[f] = in[f].data();
+      pout[f] = out[f].data();
+    }
+    ctx->eng->adjoint(nsteps, ckpt_every, pin, pout);
+    for (int f = 0; f < 3; ++f) {
+      int nrow, nk;
+      std::string err;
+      field_dims(ctx->cfg, kTladFields[f], nrow, nk);
+      if (!pack_view(&lambda_0[f], ctx->cfg.nlon, nrow, nk, out[f], err)) throw ApiError{GMC_EINVAL, err};
+    }
     return error_word_status(ctx, ctx->eng->read_error());
   });
 }

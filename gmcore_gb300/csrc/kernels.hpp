@@ -114,4 +114,23 @@ template <class R> void launch_tracer_vertical(const DGrid &g, const Launch &L, 
 // Three passes of the order-2 zonal smoother (lon_damp_on_cell, adv_mod.F90:298-302).
 template <class R> void launch_tracer_lon_damp(const DGrid &g, const Launch &L, R *q);
 
+// ---- tangent-linear and adjoint of the shallow-water step (tlad.cu, FP64) ----
+// TL of forward_prepare at the star state s (values w from forward_prepare):
+// tangents of mfx, mfy, pv, pv_lon, pv_lat into t, of u_lat, v_lon, ke into tw.
+void tl_forward_prepare(const DGrid &g, const Launch &L, const Slot<double> &s, const Work<double> &w,
+                        const Slot<double> &t, const Work<double> &tw);
+// TL of the shallow-water momentum tendencies into tw.du, tw.dv.
+void tl_momentum(const DGrid &g, const Launch &L, const Slot<double> &s, const Slot<double> &t, const Work<double> &tw);
+// AD of the updates of a stage: consumes the adjoint of the new slot an,
+// adds to the old slot ao and sets aw.du, aw.dv, aw.dgz; su, sv: row scratch.
+void ad_update(const DGrid &g, const Launch &L, const Slot<double> &ao, const Slot<double> &an, const Work<double> &aw,
+               double *su, double *sv, double dt);
+// AD of the forward pass at the star state s: from aw.du, aw.dv, aw.dgz into
+// the star adjoint a (u_f, v_f, gz; work adjoints mfx, mfy, pv, pv_lon, pv_lat
+// in a must start at zero, as must aw.u_lat, aw.v_lon, aw.ke).
+void ad_forward(const DGrid &g, const Launch &L, const Slot<double> &s, const Work<double> &w, const Slot<double> &a,
+                const Work<double> &aw);
+// AD of the run-prologue filters: u += big^T u_f, v += big^T v_f, gz += big^T gz_f.
+void ad_prologue(const DGrid &g, const Launch &L, const Slot<double> &a);
+
 }  // namespace gmc

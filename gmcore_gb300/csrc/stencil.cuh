@@ -50,6 +50,18 @@ struct MassField {
   }
 };
 
+// Upwind interpolation of order 3 and 1 (upwind_mod.F90:27-39) along the
+// direction dir = sign of the advecting wind, weighted by wgt.
+template <class R>
+__device__ __forceinline__ R upwind3(R dir, R wgt, R f1, R f2, R f3, R f4) {
+  const R c31 = (R)(7.0 / 12.0), c32 = (R)(-1.0 / 12.0), c33 = (R)(1.0 / 12.0);
+  return c31 * (f3 + f2) + c32 * (f4 + f1) + c33 * (f4 - f1 - (R)3 * (f3 - f2)) * wgt * dir;
+}
+template <class R>
+__device__ __forceinline__ R upwind1(R dir, R wgt, R f1, R f2) {
+  return (R)0.5 * (f2 + f1) + (R)(-0.5) * (f2 - f1) * wgt * dir;
+}
+
 // ---------------------------------------------------------------------------
 // PPM sub-grid reconstruction with slope limiter (ffsl_mod.F90:1147-1205).
 // ---------------------------------------------------------------------------

@@ -199,6 +199,24 @@ int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
  * at the same time) race on it.  Results equal gmc_ffsl_hflx's. */
 int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
 
+/* Tangent-linear and adjoint of nsteps model steps (the benchmark spec's
+ * differentiation path; the reference, a forward-only model, has no
+ * counterpart: its closest interface is time_integrate,
+ * gmcore_mod.F90:577-591, whose derivative these are).  Both start from the
+ * prepared state (call right after gmc_prepare) and leave the model at step
+ * nsteps, like gmc_step(nsteps).  The three views are, in order, u_lon,
+ * v_lat and gz (interior bounds as for gmc_set_field).  Available for the
+ * FP64 shallow-water model with one member, pv_pole_stokes on and no
+ * divergence damping (GMC_EINVAL otherwise).
+ *   gmc_tlm_step: dx_n = M'(x_0) dx_0, with the run prologue's filters
+ *                 applied to dx_0.
+ *   gmc_adjoint:  lambda_0 = M'(x_0)^T lambda_n; the step start states are
+ *                 recomputed from checkpoints stored every ckpt_every steps.
+ * For J(x_n), lambda_n = dJ/dx_n gives lambda_0 = dJ/dx_0. */
+int gmc_tlm_step(gmc_ctx *ctx, int32_t nsteps, const gmc_view dx0[3], const gmc_view dxn[3]);
+int gmc_adjoint(gmc_ctx *ctx, int32_t nsteps, int32_t ckpt_every, const gmc_view lambda_n[3],
+                const gmc_view lambda_0[3]);
+
 /* Timing of the last gmc_step call: device time between CUDA events
  * recorded on the context's stream around the whole call, and the number
  * of kernels it launched. */
