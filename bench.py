@@ -295,6 +295,8 @@ def run_ours(args):
     m64.close()
     ps_rms_hpa = errors["phs"]["rms"]
 
+    adj = adjoint_cost() if RANK == 0 else None
+
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sample_steps=1)
@@ -336,11 +338,47 @@ def run_ours(args):
             "kernel_ms_per_step": {k: round(v[0] / 3.0, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clk,
         }
+        if adj is not None:
+            line["adjoint"] = adj
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def adjoint_cost():
+    """Cost of the adjoint relative to the forward model on the shallow-water
+    adjoint case (1 degree 360x180, predict-correct, dt = 60 s, 96 steps,
+    checkpoint every 8 steps, FP64): wall time of gmc_adjoint (which runs the
+    checkpointed forward sweep itself) over wall time of gmc_step(96)."""
+    import gmcore_gb300 as g
+    from gmcore_gb300 import abi
+    cfg = abi.default_config(nlon=360, nlat=180, nlev=1, baroclinic=0, dt_dyn=60.0, time_scheme=abi.TIME_PC2)
+    st = g.make_ic(cfg, 1, SEED, 0.0)
+    nsteps, ckpt = 96, 8
+    lam = {"u_lon": np.zeros((1, cfg.nlat, cfg.nlon)), "v_lat": np.zeros((1, cfg.nlat - 1, cfg.nlon)),
+           "gz": np.ones((cfg.nlat, cfg.nlon))}
+
+    def timed(kind):
+        m = g.Model(cfg)
+        m.set_state(st)
+        m.prepare()
+        t0 = time.perf_counter()
+        if kind == "fwd":
+            m.step(nsteps)
+        else:
+            m.adjoint(nsteps, lam, ckpt_every=ckpt)
+        t = time.perf_counter() - t0
+        m.close()
+        return t
+
+    timed("fwd"), timed("adj")   # warm-up (allocation, module load)
+    fwd = min(timed("fwd") for _ in range(3))
+    adj = min(timed("adj") for _ in range(3))
+    return {"config": "shallow water 1deg 360x180, pc2, dt=60 s, 96 steps, checkpoint every 8, fp64",
+            "forward_ms": fwd * 1e3, "adjoint_ms": adj * 1e3, "adjoint_over_forward": adj / fwd,
+            "note": "wall time per call; the adjoint includes its checkpointed forward sweep"}
 
 
 def cpu_baseline(args, sample_steps=1, warm=0):

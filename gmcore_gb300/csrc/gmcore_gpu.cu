@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -288,7 +289,10 @@ struct Engine : EngineBase {
     if (ev_b) cudaEventDestroy(ev_b);
     arena.release();
     tables.release();
-    if (tl) tl->arena.release();
+    if (tl) {
+      tl->arena.release();
+      tl->zarena.release();
+    }
     if (pinned) cudaFreeHost(pinned);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -741,7 +745,7 @@ struct Engine : EngineBase {
   // `ckpt` steps and a forward recomputation inside each segment.
   // -------------------------------------------------------------------------
   struct Tlad {
-    Arena arena;
+    Arena arena, zarena;                      // zarena: the adjoint work arrays, zeroed per stage
     Slot<double> X[4], D[4], A[4], DS, AS;   // DS/AS: tangent/adjoint work slots (mfx, mfy, pv*)
     Work<double> WF, DW, AW;
     double *su = nullptr, *sv = nullptr;
@@ -814,17 +818,22 @@ struct Engine : EngineBase {
         carve(a, tl->A[t], false);
       }
       carve(a, tl->DS, false);
-      carve(a, tl->AS, false);
       carve(a, tl->WF, false);
       carve(a, tl->DW, false);
-      carve(a, tl->AW, false);
       tl->su = a.template take<double>(full3());
       tl->sv = a.template take<double>(half3());
     };
-    Counter cnt;
+    auto carve_zero = [&](auto &a) {
+      carve(a, tl->AS, false);
+      carve(a, tl->AW, false);
+    };
+    Counter cnt, zcnt;
     carve_all(cnt);
+    carve_zero(zcnt);
     tl->arena.reserve(cnt.used + 4096);
+    tl->zarena.reserve(zcnt.used + 4096);
     carve_all(tl->arena);
+    carve_zero(tl->zarena);
     for (int t = 0; t < 4; ++t) tl->X[t].gzs = tl->D[t].gzs = tl->A[t].gzs = gzs[0];
     tl->DS.gzs = tl->AS.gzs = gzs[0];
     tl->WF.gzs = tl->DW.gzs = tl->AW.gzs = gzs[0];
@@ -903,15 +912,33 @@ struct Engine : EngineBase {
       const int k = std::min(ckpt, std::max(nsteps, 1));
       const int nseg = (nsteps + k - 1) / k;
       const size_t fc = flat_count();
+      // checkpoints, and one segment's trajectory: for every step of the
+      // segment the stage outputs (with the diagnostics forward_prepare left
+      // in them when they served as star state) and the forward work of each
+      // stage, so the reverse sweep recomputes nothing
+      std::vector<R *> cp(nseg);
+      std::vector<std::array<Slot<R>, 4>> xs(k);
+      std::vector<std::array<Work<R>, 3>> ws(k);
+      auto carve_store = [&](auto &a) {
+        for (int c = 0; c < nseg; ++c) cp[c] = a.template take<R>(fc);
+        for (int t = 0; t < k; ++t) {
+          for (int q = 0; q <= nst; ++q) carve(a, xs[t][q], false);
+          for (int q = 0; q < nst; ++q) carve(a, ws[t][q], false);
+        }
+      };
+      Counter cnt;
+      carve_store(cnt);
       Arena store;
       struct Release {
         Arena &a;
         ~Release() { a.release(); }
       } release_store{store};
-      store.reserve(((size_t)nseg + (size_t)k) * (fc * sizeof(R) + 256) + 4096);
-      std::vector<R *> cp(nseg), sb(k);
-      for (int c = 0; c < nseg; ++c) cp[c] = store.template take<R>(fc);
-      for (int c = 0; c < k; ++c) sb[c] = store.template take<R>(fc);
+      store.reserve(cnt.used + 4096);
+      carve_store(store);
+      for (int t = 0; t < k; ++t) {
+        for (int q = 0; q <= nst; ++q) xs[t][q].gzs = gzs[0];
+        for (int q = 0; q < nst; ++q) ws[t][q].gzs = gzs[0];
+      }
       // forward sweep with checkpoints
       copy_state(T.X[0], slots[old_i]);
       for (int it = 0; it < nsteps; ++it) {
@@ -920,36 +947,31 @@ struct Engine : EngineBase {
       }
       copy_state(slots[old_i], T.X[0]);   // the model ends at step nsteps
       // adjoint of the final state
-      for (int t = 0; t < 4; ++t) zero_state(T.A[t]);
+      for (int t = 0; t <= nst; ++t) zero_state(T.A[t]);
       upload3(T.A[nst], lam_n);
       for (int seg = nseg - 1; seg >= 0; --seg) {
         const int s0 = seg * k, s1 = std::min(nsteps, s0 + k);
-        flat_load(T.X[0], cp[seg]);
-        for (int it = s0; it < s1; ++it) {
-          flat_save(sb[it - s0], T.X[0]);
-          if (it + 1 < s1) tlad_step_forward();
+        // recompute the segment: xs[t][0] is step s0+t's start state
+        flat_load(xs[0][0], cp[seg]);
+        for (int t = 0; t < s1 - s0; ++t) {
+          std::array<Slot<R>, 4> &X = xs[t];
+          if (t > 0) X[0] = xs[t - 1][nst];   // the previous step's output (never a star there)
+          const int last = t + 1 < s1 - s0 ? nst : nst - 1;   // the segment's last step needs no final stage
+          for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[t][st], tlad_dt(st));
+          if (last < nst) forward_w(ws[t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
         }
-        for (int it = s1 - 1; it >= s0; --it) {
-          flat_load(T.X[0], sb[it - s0]);
-          for (int st = 0; st + 1 < nst; ++st) stage_io(T.X[0], T.X[tlad_star(st)], T.X[st + 1], T.WF, tlad_dt(st));
+        for (int t = s1 - s0 - 1; t >= 0; --t) {
+          std::array<Slot<R>, 4> &X = xs[t];
           for (int st = nst - 1; st >= 0; --st) {
             const double dt = tlad_dt(st);
-            const Slot<R> &S = T.X[tlad_star(st)];
-            forward_w(T.WF, S, dt);   // linearisation point of this stage
             ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.su, T.sv, dt);
-            CK(cudaMemsetAsync(T.AS.mfx_lon, 0, full3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AS.mfy_lat, 0, half3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AS.pv, 0, half3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AS.pv_lon, 0, full3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AS.pv_lat, 0, half3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AW.u_lat, 0, half3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AW.v_lon, 0, full3() * sizeof(R), stream));
-            CK(cudaMemsetAsync(T.AW.ke, 0, full3() * sizeof(R), stream));
-            ad_forward(dg, L, S, T.WF, with_work(T.A[tlad_star(st)], T.AS), T.AW);
+            // adjoint work arrays start at zero (AW's du, dv, dgz are set by ad_update after this)
+            CK(cudaMemsetAsync(T.AS.u_lon, 0, (char *)T.AW.du - (char *)T.AS.u_lon, stream));
+            ad_forward(dg, L, X[tlad_star(st)], ws[t][st], with_work(T.A[tlad_star(st)], T.AS), T.AW);
           }
-          // A[0] is the adjoint of the step's start state: it seeds the step before
+          // A[0] is the adjoint of the step's start state: it seeds the step
+          // before; every A[st+1] was consumed (zeroed) by its stage's ad_update
           std::swap(T.A[0], T.A[nst]);
-          for (int t = 0; t < nst; ++t) zero_state(T.A[t]);
         }
       }
       ad_prologue(dg, L, T.A[nst]);

@@ -186,9 +186,8 @@ __global__ void k_tl_ke(DGrid g, Slot<double> s, Slot<double> t, Work<double> tw
                                       aln * s.v_f[vs] * t.v_f[vs] + als * s.v_f[vn] * t.v_f[vn]) / ac;
   }
 }
-__global__ void k_ad_ke(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw) {
+__device__ __forceinline__ void ad_ke_body(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw, int j) {
   __shared__ double red[32];
-  const int j = blockIdx.x + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   if (j == 1 || j == nlat) {
     const int jv = j == 1 ? 1 : nhalf;
@@ -243,9 +242,8 @@ __global__ void k_tl_pv(DGrid g, Slot<double> s, Slot<double> t, Work<double> tw
     t.pv[o] = (dvor - s.pv[o] * dm_vtx) / m_vtx;
   }
 }
-__global__ void k_ad_pv(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw) {
+__device__ __forceinline__ void ad_pv_body(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw, int j) {
   __shared__ double red[32];
-  const int j = blockIdx.x + 1;
   const int nhalf = g.nhalf, nlon = g.nlon;
   const double ig = 1.0 / g.g;
   const bool pole = g.pv_pole_stokes && (j == 1 || j == nhalf);
@@ -488,8 +486,7 @@ __global__ void k_tl_momentum(DGrid g, Slot<double> s, Slot<double> t, Work<doub
     tw.dv[o] = -dq - (tw.ke[off_full(g, i, j + 1)] - tw.ke[off_full(g, i, j)]) / de;
   }
 }
-__global__ void k_ad_momentum(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw) {
-  const int j = blockIdx.x + 1;
+__device__ __forceinline__ void ad_momentum_body(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw, int j) {
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   if (j != 1 && j != nlat) {
     const double t1 = ROW(g.ftw1, j), t2 = ROW(g.ftw2, j), de = ROW(g.de_lon, j);
@@ -560,9 +557,8 @@ __global__ void k_ad_momentum(DGrid g, Slot<double> s, Slot<double> a, Work<doub
 // ---------------------------------------------------------------------------
 // adjoint of the shallow-water dgz = -(dmf/dlon + dmf/dlat) g with pole rings
 // ---------------------------------------------------------------------------
-__global__ void k_ad_dgz(DGrid g, Slot<double> a, Work<double> aw) {
+__device__ __forceinline__ void ad_dgz_body(DGrid g, Slot<double> a, Work<double> aw, int j) {
   __shared__ double red[32];
-  const int j = blockIdx.x + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   if (j == 1 || j == nlat) {
     const int jv = j == 1 ? 1 : nhalf;
@@ -725,6 +721,18 @@ __global__ void k_ad_prologue(DGrid g, Slot<double> a) {
   }
 }
 
+// fused launches of the adjoint forward pass (one block per full row)
+__global__ void k_ad_dgz_momentum(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw) {
+  const int j = blockIdx.x + 1;
+  ad_dgz_body(g, a, aw, j);
+  ad_momentum_body(g, s, a, aw, j);
+}
+__global__ void k_ad_pv_ke(DGrid g, Slot<double> s, Slot<double> a, Work<double> aw) {
+  const int j = blockIdx.x + 1;
+  if (j <= g.nhalf) ad_pv_body(g, s, a, aw, j);
+  ad_ke_body(g, s, a, aw, j);
+}
+
 inline size_t row_smem(const DGrid &g, int rows) {
   int hmax = (g.big.max_taps - 1) / 2;
   return (size_t)(rows * g.nlon + g.nlon + 2 * hmax + 8) * sizeof(double);
@@ -751,11 +759,9 @@ void ad_update(const DGrid &g, const Launch &L, const Slot<double> &ao, const Sl
 }
 void ad_forward(const DGrid &g, const Launch &L, const Slot<double> &s, const Work<double> &w, const Slot<double> &a,
                 const Work<double> &aw) {
-  k_ad_dgz<<<g.nlat, L.threads, 0, L.stream>>>(g, a, aw);
-  k_ad_momentum<<<g.nlat, L.threads, 0, L.stream>>>(g, s, a, aw);
+  k_ad_dgz_momentum<<<g.nlat, L.threads, 0, L.stream>>>(g, s, a, aw);
   k_ad_pv_edges<<<g.nlat, L.threads, 0, L.stream>>>(g, s, w, a, aw);
-  k_ad_pv<<<g.nhalf, L.threads, 0, L.stream>>>(g, s, a, aw);
-  k_ad_ke<<<g.nlat, L.threads, 0, L.stream>>>(g, s, a, aw);
+  k_ad_pv_ke<<<g.nlat, L.threads, 0, L.stream>>>(g, s, a, aw);
   k_ad_tangent<<<g.nlat, L.threads, 0, L.stream>>>(g, s, w, a, aw);
   k_ad_mass_flux<<<g.nlat, L.threads, 0, L.stream>>>(g, s, a);
 }
