@@ -28,7 +28,7 @@ EXPORTED = (
     "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
-    "gmc_tlm_step", "gmc_adjoint",
+    "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -78,6 +78,7 @@ def load(build_if_missing=True):
     lib.gmc_ffsl_hflx_noalloc.argtypes = [C.c_void_p, P(FfslFields), C.c_double]
     lib.gmc_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.gmc_tlm_step.argtypes = [C.c_void_p, C.c_int32, P(View), P(View)]
+    lib.gmc_set_graphs.argtypes = [C.c_void_p, C.c_int32]
     lib.gmc_adjoint.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View), P(View)]
     lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
     _lib = lib
@@ -220,6 +221,10 @@ class Model:
             arrs.append(a)
         views = (View * 3)(*[view_of(a) for a in arrs])
         return arrs, views
+
+    def set_graphs(self, on):
+        """Replay captured CUDA graphs in step() (default) or launch directly."""
+        self._check(self.lib.gmc_set_graphs(self.h, 1 if on else 0))
 
     def tlm_step(self, nsteps, dx0):
         """Tangent-linear model over nsteps from the prepared state:

@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <tuple>
+#include <map>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -103,6 +105,7 @@ struct EngineBase {
   // three fields are u_lon, v_lat, gz (host, dense interior arrays)
   virtual void tlm(int nsteps, const double *const dx0[3], double *const dxn[3]) = 0;
   virtual void adjoint(int nsteps, int ckpt, const double *const lam_n[3], double *const lam_0[3]) = 0;
+  virtual void set_graphs(bool on) = 0;
   long time_step = 0;
   int device = 0;   // device current when the context was created
   // timing and profiling
@@ -273,6 +276,7 @@ struct Engine : EngineBase {
     arena.reserve(cnt.used + 4096);
     for (int m = 0; m < nm; ++m) carve_member(arena, m, bc);
     diag_partial = arena.take<double>(8 * nblk);
+    member_streams();
     diag_out = arena.take<double>(64);
     err = arena.take<unsigned>(64);
     staging = arena.take<R>(std::max(lev3(), full3()));
@@ -287,11 +291,17 @@ struct Engine : EngineBase {
     for (auto &p : prof_pending) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
     if (ev_a) cudaEventDestroy(ev_a);
     if (ev_b) cudaEventDestroy(ev_b);
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (cudaStream_t st : mstreams) cudaStreamDestroy(st);
+    for (cudaEvent_t e : mevents) cudaEventDestroy(e);
+    if (fork_ev) cudaEventDestroy(fork_ev);
     arena.release();
     tables.release();
     if (tl) {
+      tl->drop_graphs();
       tl->arena.release();
       tl->zarena.release();
+      tl->store.release();
     }
     if (pinned) cudaFreeHost(pinned);
     if (stream) cudaStreamDestroy(stream);
@@ -617,8 +627,10 @@ struct Engine : EngineBase {
       }
     }
     // copy_old_m
-    CK(cudaMemcpyAsync(b.old_phs_f, n.phs_f, two_d() * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-    if (b.old_psr) CK(cudaMemcpyAsync(b.old_psr, n.psr, two_d() * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+    if (!dry) {
+      CK(cudaMemcpyAsync(b.old_phs_f, n.phs_f, two_d() * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+      if (b.old_psr) CK(cudaMemcpyAsync(b.old_psr, n.psr, two_d() * sizeof(float), cudaMemcpyDeviceToDevice, L.stream));
+    }
   }
 
   cudaEvent_t take_event() {
@@ -641,6 +653,7 @@ struct Engine : EngineBase {
   template <class F>
   void K(const char *name, int nk, F &&f) {
     launches += nk;
+    if (dry) return;   // a captured graph replays these launches
     if (!prof) {
       f();
       return;
@@ -750,6 +763,19 @@ struct Engine : EngineBase {
     Work<double> WF, DW, AW;
     double *su = nullptr, *sv = nullptr;
     bool ready = false;
+    // checkpoint and segment storage of the adjoint, kept for repeated calls
+    // with the same (segments, interval)
+    Arena store;
+    int store_nseg = -1, store_k = -1;
+    std::vector<double *> cp;
+    std::vector<std::array<Slot<double>, 4>> xs;
+    std::vector<std::array<Work<double>, 3>> ws;
+    // captured launch sequences keyed by the buffers they touch
+    std::map<std::vector<intptr_t>, cudaGraphExec_t> graphs;
+    void drop_graphs() {
+      for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+      graphs.clear();
+    }
   };
   std::unique_ptr<Tlad> tl;
 
@@ -902,6 +928,37 @@ struct Engine : EngineBase {
     }
   }
 
+  // Launch the work f enqueues on the context stream as a CUDA graph captured
+  // on first use under `key` (graphs off or profiling: launch directly).
+  template <class F>
+  void replay(const std::vector<intptr_t> &key, F &&f) {
+    if (!graphs_on || prof) {
+      f();
+      return;
+    }
+    auto &gm = tl->graphs;
+    auto gi = gm.find(key);
+    if (gi == gm.end()) {
+      cudaGraph_t gr = nullptr;
+      CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        f();
+      } catch (...) {
+        cudaStreamEndCapture(stream, &gr);
+        if (gr) cudaGraphDestroy(gr);
+        throw;
+      }
+      CK(cudaStreamEndCapture(stream, &gr));
+      cudaGraphExec_t ex = nullptr;
+      cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
+      cudaGraphDestroy(gr);
+      if (e != cudaSuccess) throw CudaError(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      gi = gm.emplace(key, ex).first;
+    }
+    CK(cudaGraphLaunch(gi->second, stream));
+  }
+  static intptr_t ip(const void *p) { return reinterpret_cast<intptr_t>(p); }
+
   void adjoint(int nsteps, int ckpt, const double *const lam_n[3], double *const lam_0[3]) override {
     if constexpr (std::is_same<R, double>::value) {
       tlad_check();
@@ -916,34 +973,41 @@ struct Engine : EngineBase {
       // segment the stage outputs (with the diagnostics forward_prepare left
       // in them when they served as star state) and the forward work of each
       // stage, so the reverse sweep recomputes nothing
-      std::vector<R *> cp(nseg);
-      std::vector<std::array<Slot<R>, 4>> xs(k);
-      std::vector<std::array<Work<R>, 3>> ws(k);
-      auto carve_store = [&](auto &a) {
-        for (int c = 0; c < nseg; ++c) cp[c] = a.template take<R>(fc);
+      if (T.store_nseg != nseg || T.store_k != k) {
+        T.drop_graphs();
+        T.store.release();
+        T.cp.assign(nseg, nullptr);
+        T.xs.assign(k, {});
+        T.ws.assign(k, {});
+        auto carve_store = [&](auto &a) {
+          for (int c = 0; c < nseg; ++c) T.cp[c] = a.template take<R>(fc);
+          for (int t = 0; t < k; ++t) {
+            for (int q = 0; q <= nst; ++q) carve(a, T.xs[t][q], false);
+            for (int q = 0; q < nst; ++q) carve(a, T.ws[t][q], false);
+          }
+        };
+        Counter cnt;
+        carve_store(cnt);
+        T.store.reserve(cnt.used + 4096);
+        carve_store(T.store);
         for (int t = 0; t < k; ++t) {
-          for (int q = 0; q <= nst; ++q) carve(a, xs[t][q], false);
-          for (int q = 0; q < nst; ++q) carve(a, ws[t][q], false);
+          for (int q = 0; q <= nst; ++q) T.xs[t][q].gzs = gzs[0];
+          for (int q = 0; q < nst; ++q) T.ws[t][q].gzs = gzs[0];
+          if (t > 0) T.xs[t][0] = T.xs[t - 1][nst];   // a step starts from the previous step's output
         }
-      };
-      Counter cnt;
-      carve_store(cnt);
-      Arena store;
-      struct Release {
-        Arena &a;
-        ~Release() { a.release(); }
-      } release_store{store};
-      store.reserve(cnt.used + 4096);
-      carve_store(store);
-      for (int t = 0; t < k; ++t) {
-        for (int q = 0; q <= nst; ++q) xs[t][q].gzs = gzs[0];
-        for (int q = 0; q < nst; ++q) ws[t][q].gzs = gzs[0];
+        T.store_nseg = nseg;
+        T.store_k = k;
       }
+      auto &xs = T.xs;
+      auto &ws = T.ws;
       // forward sweep with checkpoints
       copy_state(T.X[0], slots[old_i]);
       for (int it = 0; it < nsteps; ++it) {
-        if (it % k == 0) flat_save(cp[it / k], T.X[0]);
-        tlad_step_forward();
+        if (it % k == 0) flat_save(T.cp[it / k], T.X[0]);
+        replay({1, ip(T.X[0].u_lon), ip(T.X[1].u_lon), ip(T.X[2].u_lon), ip(T.X[3].u_lon)}, [&] {
+          for (int st = 0; st < nst; ++st) stage_io(T.X[0], T.X[tlad_star(st)], T.X[st + 1], T.WF, tlad_dt(st));
+        });
+        std::swap(T.X[0], T.X[nst]);
       }
       copy_state(slots[old_i], T.X[0]);   // the model ends at step nsteps
       // adjoint of the final state
@@ -952,23 +1016,26 @@ struct Engine : EngineBase {
       for (int seg = nseg - 1; seg >= 0; --seg) {
         const int s0 = seg * k, s1 = std::min(nsteps, s0 + k);
         // recompute the segment: xs[t][0] is step s0+t's start state
-        flat_load(xs[0][0], cp[seg]);
+        flat_load(xs[0][0], T.cp[seg]);
         for (int t = 0; t < s1 - s0; ++t) {
-          std::array<Slot<R>, 4> &X = xs[t];
-          if (t > 0) X[0] = xs[t - 1][nst];   // the previous step's output (never a star there)
           const int last = t + 1 < s1 - s0 ? nst : nst - 1;   // the segment's last step needs no final stage
-          for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[t][st], tlad_dt(st));
-          if (last < nst) forward_w(ws[t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
+          replay({2, t, last}, [&] {
+            std::array<Slot<R>, 4> &X = xs[t];
+            for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[t][st], tlad_dt(st));
+            if (last < nst) forward_w(ws[t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
+          });
         }
         for (int t = s1 - s0 - 1; t >= 0; --t) {
-          std::array<Slot<R>, 4> &X = xs[t];
-          for (int st = nst - 1; st >= 0; --st) {
-            const double dt = tlad_dt(st);
-            ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.su, T.sv, dt);
-            // adjoint work arrays start at zero (AW's du, dv, dgz are set by ad_update after this)
-            CK(cudaMemsetAsync(T.AS.u_lon, 0, (char *)T.AW.du - (char *)T.AS.u_lon, stream));
-            ad_forward(dg, L, X[tlad_star(st)], ws[t][st], with_work(T.A[tlad_star(st)], T.AS), T.AW);
-          }
+          replay({3, t, ip(T.A[0].u_lon), ip(T.A[nst].u_lon)}, [&] {
+            std::array<Slot<R>, 4> &X = xs[t];
+            for (int st = nst - 1; st >= 0; --st) {
+              const double dt = tlad_dt(st);
+              ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.su, T.sv, dt);
+              // adjoint work arrays start at zero (AW's du, dv, dgz were just set by ad_update)
+              CK(cudaMemsetAsync(T.AS.u_lon, 0, (char *)T.AW.du - (char *)T.AS.u_lon, stream));
+              ad_forward(dg, L, X[tlad_star(st)], ws[t][st], with_work(T.A[tlad_star(st)], T.AS), T.AW);
+            }
+          });
           // A[0] is the adjoint of the step's start state: it seeds the step
           // before; every A[st+1] was consumed (zeroed) by its stage's ad_update
           std::swap(T.A[0], T.A[nst]);
@@ -985,6 +1052,83 @@ struct Engine : EngineBase {
     }
   }
 
+  // ---- CUDA graphs of one step and member streams ------------------------
+  // A step's launches (kernels, arguments, pointers) are fixed by the slot
+  // roles, the tracer cadence counters, whether tracers advect and the tracer
+  // time level; each such state is captured once into a graph and replayed.
+  // While a graph is replayed the host logic of the step still runs (dry
+  // mode: launches skipped, counters advanced).
+  struct GraphKey {
+    int o, n, su, sm, sw, adv, qo;
+    bool operator<(const GraphKey &b) const {
+      return std::tie(o, n, su, sm, sw, adv, qo) < std::tie(b.o, b.n, b.su, b.sm, b.sw, b.adv, b.qo);
+    }
+  };
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  bool dry = false;
+  bool graphs_on = true;
+  void set_graphs(bool on) override { graphs_on = on; }
+  // ensemble members run on their own streams (forked from and joined to the
+  // context stream) so that small grids fill the GPU
+  std::vector<cudaStream_t> mstreams;
+  std::vector<cudaEvent_t> mevents;
+  cudaEvent_t fork_ev = nullptr;
+
+  void member_streams() {
+    if (nm <= 1 || !mstreams.empty()) return;
+    const int ns = std::min(nm, 8);
+    mstreams.resize(ns);
+    mevents.resize(ns);
+    for (int t = 0; t < ns; ++t) {
+      CK(cudaStreamCreateWithFlags(&mstreams[t], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&mevents[t], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+  }
+
+  // the launches of one step (all members)
+  void step_body(int o, int n, bool ring) {
+    const double dt = grid.cfg.dt_dyn;
+    const int t3 = 3 - o - n;
+    const int su = uv_step, sm = mf_step, sw = we_step;
+    const bool fork = nm > 1 && !prof;
+    if (fork && !dry) {
+      CK(cudaEventRecord(fork_ev, stream));
+      for (cudaStream_t st : mstreams) CK(cudaStreamWaitEvent(st, fork_ev, 0));
+    }
+    for (int m = 0; m < nm; ++m) {
+      if (fork) L.stream = mstreams[m % mstreams.size()];
+      switch (grid.cfg.time_scheme) {
+        case GMC_TIME_EULER:
+          stage(m, o, o, n, dt);
+          break;
+        case GMC_TIME_PC2:
+          stage(m, o, o, n, dt / 2.0);
+          stage(m, o, n, t3, dt / 2.0);
+          stage(m, o, t3, n, dt);
+          break;
+        default:
+          stage(m, o, o, n, dt / 3.0);
+          stage(m, o, n, t3, dt / 2.0);
+          stage(m, o, t3, n, dt);
+          break;
+      }
+      const Slot<R> &N = slots[m * 3 + n];
+      if (grid.cfg.use_div_damp) K("div_damp", 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke); });
+      if (ntr > 0) {
+        uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
+        adv_run(m, N, ring && time_step > 0);
+      }
+    }
+    L.stream = stream;
+    if (fork && !dry) {
+      for (size_t t = 0; t < mstreams.size(); ++t) {
+        CK(cudaEventRecord(mevents[t], mstreams[t]));
+        CK(cudaStreamWaitEvent(stream, mevents[t], 0));
+      }
+    }
+  }
+
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
   void step(int nsteps) override {
     if (!prepared) throw ApiError{GMC_ESTATE, "gmc_prepare must be called after setting the state"};
@@ -998,34 +1142,44 @@ struct Engine : EngineBase {
     // the FP32 surface pressure follows phs_f as set through the API
     if (kFP32 && grid.cfg.baroclinic)
       for (int m = 0; m < nm; ++m) K("surface_rel", 1, [&] { launch_surface_rel<R>(dg, L, slots[m * 3 + old_i]); });
+    const bool use_graphs = graphs_on && !prof;
     for (int it = 0; it < nsteps; ++it) {
-      const int o = old_i, n = new_i, t3 = 3 - o - n;
+      const int o = old_i, n = new_i;
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
       const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
       if (ring) alert_ring = true;
-      const int su = uv_step, sm = mf_step, sw = we_step;
-      for (int m = 0; m < nm; ++m) {
-        switch (grid.cfg.time_scheme) {
-          case GMC_TIME_EULER:
-            stage(m, o, o, n, dt);
-            break;
-          case GMC_TIME_PC2:
-            stage(m, o, o, n, dt / 2.0);
-            stage(m, o, n, t3, dt / 2.0);
-            stage(m, o, t3, n, dt);
-            break;
-          default:
-            stage(m, o, o, n, dt / 3.0);
-            stage(m, o, n, t3, dt / 2.0);
-            stage(m, o, t3, n, dt);
-            break;
+      if (use_graphs) {
+        const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old};
+        auto gi = graphs.find(key);
+        if (gi == graphs.end()) {
+          cudaGraph_t gr = nullptr;
+          CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+          try {
+            step_body(o, n, ring);
+          } catch (...) {
+            cudaStreamEndCapture(stream, &gr);
+            if (gr) cudaGraphDestroy(gr);
+            throw;
+          }
+          CK(cudaStreamEndCapture(stream, &gr));
+          cudaGraphExec_t ex = nullptr;
+          cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
+          cudaGraphDestroy(gr);
+          if (e != cudaSuccess) throw CudaError(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+          gi = graphs.emplace(key, ex).first;
+        } else {
+          dry = true;
+          try {
+            step_body(o, n, ring);
+          } catch (...) {
+            dry = false;
+            throw;
+          }
+          dry = false;
         }
-        const Slot<R> &N = slots[m * 3 + n];
-        if (grid.cfg.use_div_damp) K("div_damp", 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke); });
-        if (ntr > 0) {
-          uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
-          adv_run(m, N, ring && time_step > 0);
-        }
+        CK(cudaGraphLaunch(gi->second, stream));
+      } else {
+        step_body(o, n, ring);
       }
       if (ntr > 0 && ring && time_step > 0) q_old = 1 - q_old;
       if (alert_ring) { alert_last = curr_time; alert_ring = false; }
@@ -1451,6 +1605,12 @@ int gmc_adjoint(gmc_ctx *ctx, int32_t nsteps, int32_t ckpt_every, const gmc_view
     }
     return error_word_status(ctx, ctx->eng->read_error());
   });
+}
+
+int gmc_set_graphs(gmc_ctx *ctx, int32_t on) {
+  if (!ctx || !ctx->eng) return GMC_EINVAL;
+  ctx->eng->set_graphs(on != 0);
+  return GMC_OK;
 }
 
 int gmc_get_stats(const gmc_ctx *ctx, gmc_stats *out) {

@@ -217,6 +217,13 @@ int gmc_tlm_step(gmc_ctx *ctx, int32_t nsteps, const gmc_view dx0[3], const gmc_
 int gmc_adjoint(gmc_ctx *ctx, int32_t nsteps, int32_t ckpt_every, const gmc_view lambda_n[3],
                 const gmc_view lambda_0[3]);
 
+/* CUDA graphs for gmc_step (on by default): each distinct launch sequence
+ * of a step (slot roles, tracer cadence) is captured once and replayed.
+ * Results are identical either way; profiling (gmc_set_profiling) launches
+ * kernels directly.  No counterpart in the reference (a host-side launch
+ * mechanism). */
+int gmc_set_graphs(gmc_ctx *ctx, int32_t on);
+
 /* Timing of the last gmc_step call: device time between CUDA events
  * recorded on the context's stream around the whole call, and the number
  * of kernels it launched. */
