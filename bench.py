@@ -296,6 +296,7 @@ def run_ours(args):
     ps_rms_hpa = errors["phs"]["rms"]
 
     adj = adjoint_cost() if RANK == 0 else None
+    ens = ensemble_throughput() if RANK == 0 else None
 
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
@@ -340,6 +341,8 @@ def run_ours(args):
         }
         if adj is not None:
             line["adjoint"] = adj
+        if ens is not None:
+            line["ensemble"] = ens
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -385,6 +388,33 @@ def adjoint_cost():
     return {"config": "shallow water 1deg 360x180, pc2, dt=60 s, 96 steps, checkpoint every 8, fp64",
             "forward_ms": fwd * 1e3, "adjoint_ms": adj * 1e3, "adjoint_over_forward": adj / fwd,
             "note": "wall time per call on a re-prepared context; the adjoint includes its checkpointed forward sweep"}
+
+
+def ensemble_throughput(steps=10, warmup=3):
+    """Batched ensembles (mixed FP32/FP64, test_l26, wrfrk3): 48 members at
+    2 degrees (180x90x26, dt = 600 s) and 16 members at 1 degree (360x180x26,
+    dt = 300 s), members differing by seeded 0.1 K temperature noise, each
+    ensemble one context (members on forked streams, steps replayed as CUDA
+    graphs).  Device time per step of the whole ensemble and member
+    simulated days per wall-day."""
+    import gmcore_gb300 as g
+    from gmcore_gb300 import abi
+    out = []
+    for nlon, nlat, members, dt in ((180, 90, 48, 600.0), (360, 180, 16, 300.0)):
+        kw = dict(nlon=nlon, nlat=nlat, nlev=26, baroclinic=1, dt_dyn=dt, vert_coord_template=abi.VCOORD_TEST_L26,
+                  time_scheme=abi.TIME_WRFRK3, max_wave_speed=400.0, precision=abi.PREC_MIXED)
+        base = abi.default_config(**kw)
+        m = g.Model(abi.default_config(n_members=members, **kw))
+        for mem in range(members):
+            m.set_state(g.make_ic(base, 2, SEED + mem, 0.1), member=mem)
+        m.prepare()
+        m.step(warmup)
+        m.step(steps)
+        ms = m.stats()["step_ms"] / steps
+        m.close()
+        out.append({"grid": f"{nlon}x{nlat}x26", "members": members, "dt": dt, "steps": steps,
+                    "ms_per_step": ms, "member_sdpd": members * dt / (ms / 1000.0)})
+    return out
 
 
 def cpu_baseline(args, sample_steps=1, warm=0):
@@ -444,6 +474,53 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c5(args):
+    """The high-resolution case (0.25 degrees 1440x720, 64 levels wrf_l64,
+    8 FFSL tracers, dt = 60 s): mixed form device-timed over --steps steps,
+    the FP64 form over 3 steps, and their differences after those 3 steps."""
+    import gmcore_gb300 as g
+    from gmcore_gb300 import abi
+
+    def cfg_of(prec):
+        return abi.default_config(nlon=1440, nlat=720, nlev=64, baroclinic=1, dt_dyn=60.0,
+                                  vert_coord_template=abi.VCOORD_WRF_L64, time_scheme=abi.TIME_WRFRK3,
+                                  max_wave_speed=400.0, ntracer=8, precision=prec)
+    st = g.make_ic(cfg_of(abi.PREC_MIXED), 2, SEED, 1.0)
+    res = {}
+    for prec, steps in ((abi.PREC_MIXED, args.steps), (abi.PREC_FP64, 3)):
+        m = g.Model(cfg_of(prec))
+        m.set_state(st)
+        m.prepare()
+        m.step(3 if prec == abi.PREC_MIXED else 0)
+        m.step(steps)
+        ms = m.stats()["step_ms"] / steps
+        if prec == abi.PREC_MIXED:   # state after 3 steps for the comparison
+            m2 = g.Model(cfg_of(prec))
+            m2.set_state(st)
+            m2.prepare()
+            m2.step(3)
+            state = {f: m2.get_field(f) for f in ("phs", "u_lon", "pt")}
+            m2.close()
+        else:
+            state = {f: m.get_field(f) for f in ("phs", "u_lon", "pt")}
+        m.close()
+        res[prec] = (ms, state)
+    ms_m, s_m = res[abi.PREC_MIXED]
+    ms_d, s_d = res[abi.PREC_FP64]
+    n = 1440 * 720 * 64
+    line = {"metric": "sim days/wall-day at 0.25°L64, 8 tracers: mixed vs FP64 GPU", "value": 60.0 / (ms_m / 1000.0),
+            "unit": "sim days/wall-day", "n_gpus": 1, "steps": args.steps, "ms_per_step": ms_m, "higher_is_better": True,
+            "dtype": "f32 bulk + f64 (rings, surface pressure, integrals)", "data": "synthetic (seeded)",
+            "config": {"workload": "hydrostatic baroclinic 0.25deg 1440x720 L64 (wrf_l64), 8 FFSL tracers, dt=60 s",
+                       "time_scheme": "wrfrk3", "max_wave_speed": 400.0},
+            "fp64": {"ms_per_step": ms_d, "mixed_speedup": ms_d / ms_m,
+                     "mixed_minus_fp64_after_3_steps": {f: float(np.sqrt(np.mean((s_m[f] - s_d[f]) ** 2))) for f in s_m}},
+            "cell_updates_per_s": n / (ms_m / 1000.0),
+            "step_roofline": {"compulsory_bytes_per_step": n * 4 * (48 + 2 * 8 + 10) + 18 * 1440 * 720 * 8}}
+    line["step_roofline"]["frac"] = line["step_roofline"]["compulsory_bytes_per_step"] / (ms_m / 1000.0) / 1e9 / measured_peaks()[0]
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,7 +530,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident mixed step (the case profiled under ncu)")
+    ap.add_argument("--workload", choices=("c2", "c5"), default="c2",
+                    help="c2: 0.5deg L32 4 tracers (headline); c5: 0.25deg L64 8 tracers")
     args = ap.parse_args()
+    if args.workload == "c5":
+        run_c5(args)
+        return
     if args.impl == "reference":
         if args.steps > 3:
             log("reference arm: each step of the CPU restatement takes seconds; timing", args.steps, "steps")

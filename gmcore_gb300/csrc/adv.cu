@@ -966,6 +966,7 @@ template <class R>
 void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
   if constexpr (std::is_same<R, float>::value) {
     const size_t smem = g.nlev * sizeof(double) + (size_t)(6 * g.nlev + 7) * (kTileI + 1) * sizeof(float);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_pt_tendency_f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pt_tendency_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w);
     return;
   }
@@ -1019,6 +1020,7 @@ void launch_tracer_vertical(const DGrid &g, const Launch &L, R *q, const R *cflz
   const int bt = 64;
   if constexpr (std::is_same<R, float>::value) {
     const size_t smem = (size_t)(7 * g.nlev + 7) * (kTileI + 1) * sizeof(float);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_tracer_vertical_f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_tracer_vertical_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(
         g, q, cflz, we, sp, dt_adv);
     return;

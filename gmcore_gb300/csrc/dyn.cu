@@ -904,7 +904,9 @@ __global__ void k_filter_copy(DGrid g, const T *src, T *dst, int which, int full
   const FilterDev &f = which == 0 ? g.big : which == 1 ? g.small1 : g.small2;
   T *row = reinterpret_cast<T *>(sh), *ext = row + nlon;
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) row[i] = src[ix3(nrow, nlon, i + 1, j, k)];
-  filter_row<T>(f, full_lat != 0, j, nlon, row, ext);
+  // FP32 rows of the FP32 form accumulate in FP32 like the step's own filters
+  filter_row<T, typename std::conditional<std::is_same<T, float>::value, float, double>::type>(f, full_lat != 0, j, nlon,
+                                                                                               row, ext);
   __syncthreads();
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) dst[ix3(nrow, nlon, i + 1, j, k)] = row[i];
 }
@@ -1019,6 +1021,7 @@ template <class R>
 void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
   if constexpr (std::is_same<R, float>::value) {
     const size_t smem = g.nlev * sizeof(double) + (size_t)(2 * g.nlev + 1) * (kTileI + 1) * sizeof(float);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_column_mass_f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_column_mass_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w, dt);
     return;
   }
@@ -1036,14 +1039,17 @@ void launch_swm_dgz(const DGrid &g, const Launch &L, const Slot<R> &s, const Wor
 }
 template <class R>
 void launch_update_phs(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  allow_smem(k_update_phs<R>, filter_smem(g, 1, sizeof(double)));
   k_update_phs<R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 1, sizeof(double)), L.stream>>>(g, o, n, w, dt);
 }
 template <class R>
 void launch_update_pt(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  allow_smem(k_update_pt<R>, filter_smem(g, 1, sizeof(R)));
   k_update_pt<R><<<dim3(g.nlat, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, o, n, w, dt);
 }
 template <class R>
 void launch_update_gz(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  allow_smem(k_update_gz<R>, filter_smem(g, 2, sizeof(R)));
   k_update_gz<R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt);
 }
 template <class R>
@@ -1053,10 +1059,13 @@ void launch_column_backward(const DGrid &g, const Launch &L, const Slot<R> &n, c
 }
 template <class R>
 void launch_update_uv(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
+  allow_smem(k_update_uv<R>, filter_smem(g, 2, sizeof(R)));
   k_update_uv<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt);
 }
 template <class R>
 void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s) {
+  allow_smem(k_filter_copy<R, R>, filter_smem(g, 1, sizeof(R)));
+  allow_smem(k_filter_copy<R, double>, filter_smem(g, 1, sizeof(double)));
   k_filter_copy<R, R><<<dim3(g.nlat, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, s.u_lon, s.u_f, 0, 1, g.nlat);
   k_filter_copy<R, R><<<dim3(g.nhalf, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, s.v_lat, s.v_f, 0, 0, g.nhalf);
   if (g.baroclinic)

@@ -761,7 +761,6 @@ struct Engine : EngineBase {
     Arena arena, zarena;                      // zarena: the adjoint work arrays, zeroed per stage
     Slot<double> X[4], D[4], A[4], DS, AS;   // DS/AS: tangent/adjoint work slots (mfx, mfy, pv*)
     Work<double> WF, DW, AW;
-    double *su = nullptr, *sv = nullptr;
     bool ready = false;
     // checkpoint and segment storage of the adjoint, kept for repeated calls
     // with the same (segments, interval)
@@ -846,8 +845,6 @@ struct Engine : EngineBase {
       carve(a, tl->DS, false);
       carve(a, tl->WF, false);
       carve(a, tl->DW, false);
-      tl->su = a.template take<double>(full3());
-      tl->sv = a.template take<double>(half3());
     };
     auto carve_zero = [&](auto &a) {
       carve(a, tl->AS, false);
@@ -1000,39 +997,45 @@ struct Engine : EngineBase {
       }
       auto &xs = T.xs;
       auto &ws = T.ws;
-      // forward sweep with checkpoints
+      // segment step t: stages of step s0+t into the segment storage (the
+      // final stage's update only when its output is needed)
+      auto seg_step = [&](int t, int last) {
+        replay({2, t, last}, [&] {
+          std::array<Slot<R>, 4> &X = xs[t];
+          for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[t][st], tlad_dt(st));
+          if (last < nst) forward_w(ws[t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
+        });
+      };
+      // forward sweep with checkpoints; the last segment runs straight into
+      // the segment storage, so the reverse sweep starts without recomputing it
+      const int slast = (nseg - 1) * k;
       copy_state(T.X[0], slots[old_i]);
-      for (int it = 0; it < nsteps; ++it) {
+      for (int it = 0; it < slast; ++it) {
         if (it % k == 0) flat_save(T.cp[it / k], T.X[0]);
         replay({1, ip(T.X[0].u_lon), ip(T.X[1].u_lon), ip(T.X[2].u_lon), ip(T.X[3].u_lon)}, [&] {
           for (int st = 0; st < nst; ++st) stage_io(T.X[0], T.X[tlad_star(st)], T.X[st + 1], T.WF, tlad_dt(st));
         });
         std::swap(T.X[0], T.X[nst]);
       }
-      copy_state(slots[old_i], T.X[0]);   // the model ends at step nsteps
+      copy_state(xs[0][0], T.X[0]);
+      for (int it = slast; it < nsteps; ++it) seg_step(it - slast, nst);
+      copy_state(slots[old_i], xs[nsteps - 1 - slast][nst]);   // the model ends at step nsteps
       // adjoint of the final state
       for (int t = 0; t <= nst; ++t) zero_state(T.A[t]);
       upload3(T.A[nst], lam_n);
       for (int seg = nseg - 1; seg >= 0; --seg) {
         const int s0 = seg * k, s1 = std::min(nsteps, s0 + k);
-        // recompute the segment: xs[t][0] is step s0+t's start state
-        flat_load(xs[0][0], T.cp[seg]);
-        for (int t = 0; t < s1 - s0; ++t) {
-          const int last = t + 1 < s1 - s0 ? nst : nst - 1;   // the segment's last step needs no final stage
-          replay({2, t, last}, [&] {
-            std::array<Slot<R>, 4> &X = xs[t];
-            for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[t][st], tlad_dt(st));
-            if (last < nst) forward_w(ws[t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
-          });
+        if (seg < nseg - 1) {   // recompute the segment: xs[t][0] is step s0+t's start state
+          flat_load(xs[0][0], T.cp[seg]);
+          for (int t = 0; t < s1 - s0; ++t) seg_step(t, t + 1 < s1 - s0 ? nst : nst - 1);
         }
         for (int t = s1 - s0 - 1; t >= 0; --t) {
           replay({3, t, ip(T.A[0].u_lon), ip(T.A[nst].u_lon)}, [&] {
             std::array<Slot<R>, 4> &X = xs[t];
             for (int st = nst - 1; st >= 0; --st) {
               const double dt = tlad_dt(st);
-              ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.su, T.sv, dt);
-              // adjoint work arrays start at zero (AW's du, dv, dgz were just set by ad_update)
-              CK(cudaMemsetAsync(T.AS.u_lon, 0, (char *)T.AW.du - (char *)T.AS.u_lon, stream));
+              // clears the adjoint work (AS, AW up to AW.du) for the forward-pass adjoint
+              ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.AS.u_lon, (size_t)(T.AW.du - T.AS.u_lon), dt);
               ad_forward(dg, L, X[tlad_star(st)], ws[t][st], with_work(T.A[tlad_star(st)], T.AS), T.AW);
             }
           });

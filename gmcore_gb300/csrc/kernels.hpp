@@ -51,6 +51,13 @@ struct BatchView {
   const R *m_lev;
 };
 
+// Opt a kernel in to more than 48 KB of dynamic shared memory when a launch
+// needs it (wide rows, tall columns).
+template <class Kern>
+inline void allow_smem(Kern k, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 struct Launch {
   cudaStream_t stream;
   int threads;   // block size for row kernels
@@ -121,10 +128,11 @@ void tl_forward_prepare(const DGrid &g, const Launch &L, const Slot<double> &s, 
                         const Slot<double> &t, const Work<double> &tw);
 // TL of the shallow-water momentum tendencies into tw.du, tw.dv.
 void tl_momentum(const DGrid &g, const Launch &L, const Slot<double> &s, const Slot<double> &t, const Work<double> &tw);
-// AD of the updates of a stage: consumes the adjoint of the new slot an,
-// adds to the old slot ao and sets aw.du, aw.dv, aw.dgz; su, sv: row scratch.
+// AD of the updates of a stage: consumes (and clears) the adjoint of the new
+// slot an, adds to the old slot ao, sets aw.du, aw.dv, aw.dgz, and clears
+// the nzero values at zero (the adjoint work the forward pass accumulates into).
 void ad_update(const DGrid &g, const Launch &L, const Slot<double> &ao, const Slot<double> &an, const Work<double> &aw,
-               double *su, double *sv, double dt);
+               double *zero, size_t nzero, double dt);
 // AD of the forward pass at the star state s: from aw.du, aw.dv, aw.dgz into
 // the star adjoint a (u_f, v_f, gz; work adjoints mfx, mfy, pv, pv_lon, pv_lat
 // in a must start at zero, as must aw.u_lat, aw.v_lon, aw.ke).

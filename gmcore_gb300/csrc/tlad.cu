@@ -603,12 +603,25 @@ __device__ bool filter_row_t(const FilterDev &f, bool full_lat, int j, int nlon,
   return true;
 }
 
-// update_gz adjoint: t = gz_o + dt dgz; gz_f = big(t); gz = small1(t)
-__global__ void k_ad_update_gz(DGrid g, Slot<double> ao, Slot<double> an, Work<double> aw, double dt) {
+// update_gz adjoint: t = gz_o + dt dgz; gz_f = big(t); gz = small1(t).
+// Also clears the new slot's u/v adjoints (consumed by k_ad_uv) and the
+// adjoint work range [zero, zero + nzero) the forward-pass adjoint
+// accumulates into.
+__global__ void k_ad_update_gz(DGrid g, Slot<double> ao, Slot<double> an, Work<double> aw, double dt, double *zero,
+                               size_t nzero) {
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, nlon = g.nlon;
   double *r1 = sh, *r2 = sh + nlon, *ext = r2 + nlon;
   const size_t c0 = (size_t)(j - 1) * nlon;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nzero; t += (size_t)gridDim.x * blockDim.x) zero[t] = 0;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    an.u_lon[c0 + i] = 0;
+    an.u_f[c0 + i] = 0;
+    if (j <= g.nhalf) {
+      an.v_lat[c0 + i] = 0;
+      an.v_f[c0 + i] = 0;
+    }
+  }
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     r1[i] = an.gz_f[c0 + i];
     r2[i] = an.gz[c0 + i];
@@ -625,56 +638,38 @@ __global__ void k_ad_update_gz(DGrid g, Slot<double> ao, Slot<double> an, Work<d
   }
 }
 
-// update_uv adjoint, phase 1: adjoint of the unfiltered rows
-//   u rows (non-pole): su = u_n_bar + big^T(u_f_n_bar)
-//   v rows:            sv = v_n_bar + big^T(v_f_n_bar)   (before the pole blend)
-__global__ void k_ad_uv_rows(DGrid g, Slot<double> an, double *su, double *sv) {
+// update_uv adjoint.  Forward rows: t = old + dt (tend - pgf) with
+// pgf = d gz_f / d edge; u = t, u_f = big(u) (pole rows of u untouched);
+// v(1) = 0.4 t(1) + 0.6 t(2), v(nhalf) = 0.4 t(nhalf) + 0.6 t(nhalf-1), other
+// rows v = t; v_f = big(v).  A block takes one u row or one v row; the v rows
+// next to the pole rows also form the pole rows' adjoint (their blend
+// partner).  The new slot's u/v adjoints are read here and cleared later by
+// k_ad_update_gz.
+__device__ void ad_v_post(const DGrid &g, const Slot<double> &an, int j, double *row, double *ext) {
+  // row <- adjoint of the blended v row j: v_n_bar + big^T(v_f_n_bar)
+  const size_t c0 = (size_t)(j - 1) * g.nlon;
+  __syncthreads();
+  for (int i = threadIdx.x; i < g.nlon; i += blockDim.x) row[i] = an.v_f[c0 + i];
+  filter_row_t(g.big, false, j, g.nlon, row, ext);
+  __syncthreads();
+  for (int i = threadIdx.x; i < g.nlon; i += blockDim.x) row[i] += an.v_lat[c0 + i];
+  __syncthreads();
+}
+__global__ void k_ad_uv(DGrid g, Slot<double> ao, Slot<double> an, Work<double> aw, double dt) {
   extern __shared__ double sh[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
-  double *row = sh, *ext = sh + nlon;
+  double *row = sh, *row2 = sh + nlon, *ext = row2 + nlon;
   if ((int)blockIdx.x < nlat) {
     const int j = blockIdx.x + 1;
+    if (j == 1 || j == nlat) return;   // pole rows of u are not updated: their adjoint ends here
     const size_t c0 = (size_t)(j - 1) * nlon;
-    if (j == 1 || j == nlat) {   // pole rows of u are not updated: their adjoint ends here
-      for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-        su[c0 + i] = 0;
-        an.u_lon[c0 + i] = 0;
-        an.u_f[c0 + i] = 0;
-      }
-      return;
-    }
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) row[i] = an.u_f[c0 + i];
     filter_row_t(g.big, true, j, nlon, row, ext);
     __syncthreads();
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-      su[c0 + i] = an.u_lon[c0 + i] + row[i];
-      an.u_lon[c0 + i] = 0;
-      an.u_f[c0 + i] = 0;
-    }
-    return;
-  }
-  const int j = blockIdx.x - nlat + 1;
-  const size_t c0 = (size_t)(j - 1) * nlon;
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) row[i] = an.v_f[c0 + i];
-  filter_row_t(g.big, false, j, nlon, row, ext);
-  __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-    sv[c0 + i] = an.v_lat[c0 + i] + row[i];
-    an.v_lat[c0 + i] = 0;
-    an.v_f[c0 + i] = 0;
-  }
-}
-// phase 2: t = old + dt (tend - pgf); v pole blend v(1) = 0.4 t(1) + 0.6 t(2)
-__global__ void k_ad_uv_apply(DGrid g, Slot<double> ao, Slot<double> an, Work<double> aw, const double *su,
-                              const double *sv, double dt) {
-  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
-  if ((int)blockIdx.x < nlat) {
-    const int j = blockIdx.x + 1;
-    if (j == 1 || j == nlat) return;
     const double de = ROW(g.de_lon, j);
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       const size_t o = off_full(g, i, j);
-      const double tb = su[o];
+      const double tb = row[i - 1] + an.u_lon[o];
       ao.u_lon[o] += tb;
       aw.du[o] = dt * tb;
       const double pb = -dt * tb / de;   // pgf = (gz_f(i+1) - gz_f(i)) / de
@@ -684,15 +679,15 @@ __global__ void k_ad_uv_apply(DGrid g, Slot<double> ao, Slot<double> an, Work<do
     return;
   }
   const int j = blockIdx.x - nlat + 1;
-  const double de = ROW(g.de_lat, j);
   const double wgt = 0.6;
+  ad_v_post(g, an, j, row, ext);
+  const bool with_s = j == 2, with_n = j == nhalf - 1;   // partner of a pole row
+  if (with_s || with_n) ad_v_post(g, an, with_s ? 1 : nhalf, row2, ext);
+  const double de = ROW(g.de_lat, j);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     const size_t o = off_hlat(g, i, j);
-    double tb;
-    if (j == 1 || j == nhalf) tb = (1.0 - wgt) * sv[o];
-    else tb = sv[o];
-    if (j == 2) tb += wgt * sv[off_hlat(g, i, 1)];
-    if (j == nhalf - 1) tb += wgt * sv[off_hlat(g, i, nhalf)];
+    double tb = (j == 1 || j == nhalf) ? (1.0 - wgt) * row[i - 1] : row[i - 1];
+    if (with_s || with_n) tb += wgt * row2[i - 1];
     ao.v_lat[o] += tb;
     aw.dv[o] = dt * tb;
     const double pb = -dt * tb / de;   // pgf = (gz_f(i, j+1) - gz_f(i, j)) / de
@@ -752,10 +747,11 @@ void tl_momentum(const DGrid &g, const Launch &L, const Slot<double> &s, const S
   k_tl_momentum<<<g.nlat, L.threads, 0, L.stream>>>(g, s, t, tw);
 }
 void ad_update(const DGrid &g, const Launch &L, const Slot<double> &ao, const Slot<double> &an, const Work<double> &aw,
-               double *su, double *sv, double dt) {
-  k_ad_uv_rows<<<g.nlat + g.nhalf, L.threads, row_smem(g, 1), L.stream>>>(g, an, su, sv);
-  k_ad_uv_apply<<<g.nlat + g.nhalf, L.threads, 0, L.stream>>>(g, ao, an, aw, su, sv, dt);
-  k_ad_update_gz<<<g.nlat, L.threads, row_smem(g, 2), L.stream>>>(g, ao, an, aw, dt);
+               double *zero, size_t nzero, double dt) {
+  allow_smem(k_ad_uv, row_smem(g, 2));
+  allow_smem(k_ad_update_gz, row_smem(g, 2));
+  k_ad_uv<<<g.nlat + g.nhalf, L.threads, row_smem(g, 2), L.stream>>>(g, ao, an, aw, dt);
+  k_ad_update_gz<<<g.nlat, L.threads, row_smem(g, 2), L.stream>>>(g, ao, an, aw, dt, zero, nzero);
 }
 void ad_forward(const DGrid &g, const Launch &L, const Slot<double> &s, const Work<double> &w, const Slot<double> &a,
                 const Work<double> &aw) {
@@ -766,6 +762,7 @@ void ad_forward(const DGrid &g, const Launch &L, const Slot<double> &s, const Wo
   k_ad_mass_flux<<<g.nlat, L.threads, 0, L.stream>>>(g, s, a);
 }
 void ad_prologue(const DGrid &g, const Launch &L, const Slot<double> &a) {
+  allow_smem(k_ad_prologue, row_smem(g, 1));
   k_ad_prologue<<<dim3(g.nlat, 3), L.threads, row_smem(g, 1), L.stream>>>(g, a);
 }
 
