@@ -16,7 +16,8 @@ import os
 import numpy as np
 
 from .abi import (Config, Diag, View, Stats, FfslFields, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
-                  TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, LIMITER_NONE,
+                  TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, PV_TVD, TVD_NONE, TVD_VAN_LEER,
+                  TVD_MC, FLUX_PPM, FLUX_VAN_LEER, LIMITER_NONE,
                   LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
                   VCOORD_WRF_L64, PREC_FP64, PREC_MIXED)
 

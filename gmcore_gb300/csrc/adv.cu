@@ -68,16 +68,19 @@ __device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R 
   __syncthreads();
   for (int l = threadIdx.x; l < nlon; l += blockDim.x) ss[l] = slope(lim, xs[W(l - 1)], xs[l], xs[W(l + 1)]);
   __syncthreads();
-  for (int l = threadIdx.x; l < nlon; l += blockDim.x) {
-    const int lm = W(l - 1), lp = W(l + 1);
-    const R f = xs[l], s0 = ss[l];
-    R fl, df, f6;
-    ppm_cell(f, s0, ppm_edge(xs[lm], f, ss[lm], s0), ppm_edge(f, xs[lp], s0, ss[lp]), fl, df, f6);
-    cl[l] = fl;
-    cd[l] = df;
-    c6[l] = f6;
+  const bool vl = g.flux_type == GMC_FLUX_VAN_LEER;
+  if (!vl) {
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) {
+      const int lm = W(l - 1), lp = W(l + 1);
+      const R f = xs[l], s0 = ss[l];
+      R fl, df, f6;
+      ppm_cell(f, s0, ppm_edge(xs[lm], f, ss[lm], s0), ppm_edge(f, xs[lp], s0, ss[lp]), fl, df, f6);
+      cl[l] = fl;
+      cd[l] = df;
+      c6[l] = f6;
+    }
+    __syncthreads();
   }
-  __syncthreads();
   const R hxr = (R)g.hx;
   int t = 0;
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
@@ -102,12 +105,18 @@ __device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R 
         const int iu = Wg(i - ci - 1);   // 0-based upwind cell
         R sum = 0;
         for (int l = i + 1 - ci; l <= i; ++l) sum = sum + xs[Wg(l - 1)];
-        flux = fdiv(uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)1 - cf, (R)1), c);
+        if (vl)   // hflx_van_leer_cell (ffsl_mod.F90:585-590)
+          flux = fdiv(uo * (cf * (xs[iu] + ss[iu] * (R)0.5 * ((R)1 - cf)) + sum), c);
+        else
+          flux = fdiv(uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)1 - cf, (R)1), c);
       } else if (c < 0) {
         const int iu = Wg(i - ci);       // 0-based upwind cell (i - ci + 1 in 1-based)
         R sum = 0;
         for (int l = i + 1; l <= i - ci; ++l) sum = sum + xs[Wg(l - 1)];
-        flux = fdiv(-uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)0, -cf), c);
+        if (vl)   // (ffsl_mod.F90:591-594)
+          flux = fdiv(uo * (cf * (xs[iu] - ss[iu] * (R)0.5 * ((R)1 + cf)) - sum), c);
+        else
+          flux = fdiv(-uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)0, -cf), c);
       } else {
         flux = 0;
       }
@@ -135,6 +144,10 @@ __device__ __forceinline__ R hflx_yface(const DGrid &g, R c, R vv, const R *y, c
   if (!(fabs(c) <= (R)1)) {
     atomicOr(g.err, ERR_CFLY);
     return 0;
+  }
+  if (g.flux_type == GMC_FLUX_VAN_LEER) {   // hflx_van_leer_cell (ffsl_mod.F90:603-610)
+    const R yu = c > 0 ? y[t] : y[t + 1], su = c > 0 ? sl[t] : sl[t + 1];   // upwind cell j (c > 0) or j + 1
+    return vv * (yu + su * (R)0.5 * (fsign((R)1, c) - c));
   }
   R fl, df, f6;
   if (c > 0) {   // upwind cell j
@@ -368,6 +381,23 @@ __device__ __forceinline__ R vflx_at(const DGrid &g, const R *col, int k, R c, R
     if (ku < 1 || ku > nlev) { fl = df = f6 = 0; return; }
     ppm(lim, C(ku - 2), C(ku - 1), C(ku), C(ku + 1), C(ku + 2), fl, df, f6);
   };
+  if (g.flux_type == GMC_FLUX_VAN_LEER) {   // vflx_van_leer_cell (ffsl_mod.F90:637-653)
+    if (c > 0) {
+      const int ku = k - ci - 1;
+      R sum = 0;
+      for (int l = k - ci; l <= k - 1; ++l) sum = sum + C(l);
+      const R dm = slope(lim, C(ku - 1), C(ku), C(ku + 1));
+      return fdiv(w * (cf * (C(ku) + dm * (R)0.5 * ((R)1 - cf)) + sum), c);
+    }
+    if (c < 0) {
+      const int ku = k - ci;
+      R sum = 0;
+      for (int l = k; l <= k - ci - 1; ++l) sum = sum + C(l);
+      const R dm = slope(lim, C(ku - 1), C(ku), C(ku + 1));
+      return fdiv(w * (cf * (C(ku) - dm * (R)0.5 * ((R)1 + cf)) - sum), c);
+    }
+    return 0;
+  }
   if (c > 0) {
     const int ku = k - ci - 1;
     R sum = 0;
@@ -415,6 +445,11 @@ struct VRoll {
   // flux at the current interface k
   __device__ __forceinline__ R flux(R c, R w) const {
     if (!(fabs(c) < (R)1)) return vflx_at<R>(g, col, k, c, w);
+    if (g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 (c > 0) or k, slope s(k-1) or s(k)
+      if (c > 0) return fdiv(w * (c * (c1 + s1 * (R)0.5 * ((R)1 - c))), c);
+      if (c < 0) return fdiv(w * (c * (c2 - s2 * (R)0.5 * ((R)1 + c))), c);
+      return 0;
+    }
     R fl, df, f6;
     if (c > 0) {
       ppm_cell(c1, s1, e0, e1, fl, df, f6);
@@ -505,6 +540,24 @@ __device__ R vflx_tile(const DGrid &g, const R *C, const R *FL, const R *DF, con
   auto Cv = [&](int kk) { return C[(min(max(kk, -1), nlev + 2) + 1) * ld]; };
   const int ci = (int)c;
   const R cf = c - (R)ci;
+  if (g.flux_type == GMC_FLUX_VAN_LEER) {   // vflx_van_leer_cell (ffsl_mod.F90:637-653)
+    const int lim = g.limiter;
+    if (c > 0) {
+      const int ku = k - ci - 1;
+      R sum = 0;
+      for (int l = k - ci; l <= k - 1; ++l) sum = sum + Cv(l);
+      const R dm = slope(lim, Cv(ku - 1), Cv(ku), Cv(ku + 1));
+      return fdiv(w * (cf * (Cv(ku) + dm * (R)0.5 * ((R)1 - cf)) + sum), c);
+    }
+    if (c < 0) {
+      const int ku = k - ci;
+      R sum = 0;
+      for (int l = k; l <= k - ci - 1; ++l) sum = sum + Cv(l);
+      const R dm = slope(lim, Cv(ku - 1), Cv(ku), Cv(ku + 1));
+      return fdiv(w * (cf * (Cv(ku) - dm * (R)0.5 * ((R)1 + cf)) - sum), c);
+    }
+    return 0;
+  }
   auto coef = [&](int ku, R &fl, R &df, R &f6) {
     if (ku < 1 || ku > nlev) { fl = df = f6 = 0; return; }
     fl = FL[(ku - 1) * ld]; df = DF[(ku - 1) * ld]; f6 = F6[(ku - 1) * ld];
@@ -572,7 +625,10 @@ __global__ void k_pt_tendency_f(DGrid g, Slot<float> s, Work<float> w) {
     if (k != 1 && k != nlev + 1) {
       const size_t ol = ix3(nlat, nlon, ic, j, k);
       const float c = w.cflz[ol], wv = s.we_lev[ol];
-      if (fabsf(c) < 1.0f) {
+      if (fabsf(c) < 1.0f && g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 or k
+        if (c > 0) fz = fdiv(wv * (c * (C[k * ld] + S[(k - 1) * ld] * 0.5f * (1.0f - c))), c);
+        else if (c < 0) fz = fdiv(wv * (c * (C[(k + 1) * ld] - S[k * ld] * 0.5f * (1.0f + c))), c);
+      } else if (fabsf(c) < 1.0f) {
         if (c > 0) {
           const int u = k - 2;   // cell k-1
           fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
@@ -870,7 +926,10 @@ __global__ void k_tracer_vertical_f(DGrid g, float *q, const float *cflz, const 
     if (k != 1 && k != nlev + 1) {
       const size_t ol = ix3(nlat, nlon, ic, j, k);
       const float c = cflz[ol], wv = we[ol];
-      if (fabsf(c) < 1.0f) {
+      if (fabsf(c) < 1.0f && g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 or k
+        if (c > 0) fz = fdiv(wv * (c * (C[k * ld] + S[(k - 1) * ld] * 0.5f * (1.0f - c))), c);
+        else if (c < 0) fz = fdiv(wv * (c * (C[(k + 1) * ld] - S[k * ld] * 0.5f * (1.0f + c))), c);
+      } else if (fabsf(c) < 1.0f) {
         if (c > 0) {
           const int u = k - 2;
           fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);

@@ -44,7 +44,7 @@ struct RowF {
   const float *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
   const float *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
   const float *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
-  const float *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat;
+  const float *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat, *half_cos_lat;
 };
 
 // Grid constants and 1-D metric tables (device pointers).  Row tables are
@@ -62,8 +62,11 @@ struct DGrid {
   const double *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
   const double *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
   const double *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
-  const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat;
+  const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat, *half_cos_lat;
   RowF f;
+  int flux_type;        // GMC_FLUX_*
+  int tvd_limiter;      // GMC_TVD_* (pv_scheme = tvd)
+  int div_damp_order;   // 2 or 4
   // FP32 form of the y departure: offsets radius (half_lat(l) - half_lat(j)) / de_lat(j)
   // for l = j-1 .. j+2 at [(j-1)*4 + l-j+1] (0 outside 1..nhalf)
   const float *cfl_yoff;

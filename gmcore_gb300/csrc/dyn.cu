@@ -158,13 +158,34 @@ __global__ void k_pv(DGrid g, Slot<R> s, Work<R> w) {
 
 // interp_pv_midpoint / interp_pv_upwind (operators_mod.F90:705-795).
 template <class R>
-__global__ void k_pv_edges(DGrid g, Slot<R> s, Work<R> w) {
+__global__ void k_pv_edges(DGrid g, Slot<R> s, Work<R> w, double dt) {
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const R eps = (R)2.220446049250313e-16;
   const R wgt = (R)g.upwind_wgt_pv;
   const R *pv = s.pv;
   auto P = [&](int i, int jj) { return rd_half(pv, g, i, jj, k); };
+  if (g.pv_scheme == GMC_PV_TVD) {   // interp_pv_tvd (operators_mod.F90:797-832)
+    if (j != 1 && j != nlat) {
+      const R le = ROWR(R, le_lon, j);
+      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+        const size_t o = ix3(nlat, nlon, i, j, k);
+        const R cfl = w.v_lon[o] * (R)dt / le;
+        s.pv_lon[o] = tvd_interp<R>(g.tvd_limiter, cfl, P(i, j - 2), P(i, j - 1), P(i, j), P(i, j + 1));
+      }
+    } else {
+      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) s.pv_lon[ix3(nlat, nlon, i, j, k)] = (R)0;
+    }
+    if (j <= nhalf) {
+      const R le = ROWR(R, le_lat, j);
+      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+        const size_t o = ix3(nhalf, nlon, i, j, k);
+        const R cfl = w.u_lat[o] * (R)dt / le;
+        s.pv_lat[o] = tvd_interp<R>(g.tvd_limiter, cfl, P(i - 2, j), P(i - 1, j), P(i, j), P(i + 1, j));
+      }
+    }
+    return;
+  }
   if (j == 1 || j == nlat) {
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) s.pv_lon[ix3(nlat, nlon, i, j, k)] = (R)0;
   } else {
@@ -1009,8 +1030,8 @@ void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> 
   k_pv<R><<<dim3(g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
 }
 template <class R>
-void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  k_pv_edges<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
+  k_pv_edges<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w, dt);
 }
 template <class R>
 void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt) {
@@ -1091,7 +1112,7 @@ void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Wo
   template void launch_tangent_winds<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);         \
   template void launch_kinetic_energy<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);        \
   template void launch_pv<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);                    \
-  template void launch_pv_edges<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);              \
+  template void launch_pv_edges<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &, double);      \
   template void launch_batch_cfl<R>(const DGrid &, const Launch &, const R *, const R *, R *, R *, R *, R *, double); \
   template void launch_column_mass<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &, double);   \
   template void launch_momentum_tend<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);         \
@@ -1135,8 +1156,30 @@ __global__ void k_div(DGrid g, Slot<R> n, R *div) {
   }
 }
 
+// div2 = Laplacian of div on non-pole rows (operators_mod.F90:412-425); pole
+// rows stay zero as the reference's zero-initialised array leaves them.
+template <class R>
+__global__ void k_div2(DGrid g, const R *div, R *div2) {
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nlon = g.nlon;
+  if (j == 1 || j == nlat) {
+    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) div2[ix3(nlat, nlon, i, j, k)] = (R)0;
+    return;
+  }
+  const R dl = ROWR(R, de_lon, j), c0 = ROWR(R, half_cos_lat, j), c1 = ROWR(R, half_cos_lat, j - 1);
+  const R d0 = ROWR(R, de_lat, j), d1 = ROWR(R, de_lat, j - 1), le = ROWR(R, le_lon, j), cf = ROWR(R, full_cos_lat, j);
+  auto D = [&](int i, int jj) { return div[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    const R d = D(i, j);
+    div2[ix3(nlat, nlon, i, j, k)] =
+        (D(i + 1, j) - (R)2 * d + D(i - 1, j)) / (dl * dl) + ((D(i, j + 1) - d) * c0 / d0 - (d - D(i, j - 1)) * c1 / d1) / le / cf;
+  }
+}
+
+// order 2: u += c (div(i+1) - div(i)) / de; order 4: u -= c (div2(i+1) - div2(i)) / de
 template <class R>
 __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
+  const R sgn = g.div_damp_order == 4 ? (R)-1 : (R)1;
   const int k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   if ((int)blockIdx.x < nlat) {
@@ -1145,7 +1188,7 @@ __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
     const R c = (R)g.div_c_lon[(size_t)(k - 1) * nlat + (j - 1)], de = ROWR(R, de_lon, j);
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       size_t o = ix3(nlat, nlon, i, j, k);
-      n.u_lon[o] = n.u_lon[o] + c * (div[ix3(nlat, nlon, wrap(i + 1, nlon), j, k)] - div[o]) / de;
+      n.u_lon[o] = n.u_lon[o] + sgn * (c * (div[ix3(nlat, nlon, wrap(i + 1, nlon), j, k)] - div[o]) / de);
     }
     return;
   }
@@ -1153,18 +1196,23 @@ __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
   const R c = (R)g.div_c_lat[(size_t)(k - 1) * nhalf + (j - 1)], de = ROWR(R, de_lat, j);
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     size_t o = ix3(nhalf, nlon, i, j, k);
-    n.v_lat[o] = n.v_lat[o] + c * (div[ix3(nlat, nlon, i, j + 1, k)] - div[ix3(nlat, nlon, i, j, k)]) / de;
+    n.v_lat[o] = n.v_lat[o] + sgn * (c * (div[ix3(nlat, nlon, i, j + 1, k)] - div[ix3(nlat, nlon, i, j, k)]) / de);
   }
 }
 
 }  // namespace
 
 template <class R>
-void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div) {
+void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, R *div2) {
   k_div<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
-  k_div_damp<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
+  if (g.div_damp_order == 4) {
+    k_div2<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, div, div2);
+    k_div_damp<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, n, div2);
+  } else {
+    k_div_damp<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
+  }
 }
-template void launch_div_damp<double>(const DGrid &, const Launch &, const Slot<double> &, double *);
-template void launch_div_damp<float>(const DGrid &, const Launch &, const Slot<float> &, float *);
+template void launch_div_damp<double>(const DGrid &, const Launch &, const Slot<double> &, double *, double *);
+template void launch_div_damp<float>(const DGrid &, const Launch &, const Slot<float> &, float *, float *);
 
 }  // namespace gmc

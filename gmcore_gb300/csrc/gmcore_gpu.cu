@@ -335,7 +335,7 @@ struct Engine : EngineBase {
     row(g.le_lat, &dg.le_lat, &dg.f.le_lat); row(g.full_f, &dg.full_f, &dg.f.full_f); row(g.half_f, &dg.half_f, &dg.f.half_f);
     row(g.full_tangent_wgt1, &dg.ftw1, &dg.f.ftw1); row(g.full_tangent_wgt2, &dg.ftw2, &dg.f.ftw2);
     row(g.half_tangent_wgt1, &dg.htw1, &dg.f.htw1); row(g.half_tangent_wgt2, &dg.htw2, &dg.f.htw2);
-    row(g.full_cos_lat, &dg.full_cos_lat, &dg.f.full_cos_lat); row(g.half_lat, &dg.half_lat, &dg.f.half_lat);
+    row(g.full_cos_lat, &dg.full_cos_lat, &dg.f.full_cos_lat); row(g.half_cos_lat, &dg.half_cos_lat, &dg.f.half_cos_lat); row(g.half_lat, &dg.half_lat, &dg.f.half_lat);
     vec(g.hyai, &dg.hyai); vec(g.hybi, &dg.hybi); vec(g.half_lev, &dg.half_lev); vec(g.half_dlev, &dg.half_dlev);
     vec(g.full_dlev, &dg.full_dlev); vec(g.lon_damp_wgt_full, &dg.lon_damp_full);
     vec(g.div_c_lon, &dg.div_c_lon); vec(g.div_c_lat, &dg.div_c_lat);
@@ -450,6 +450,7 @@ struct Engine : EngineBase {
     dg.ke_scheme = c.ke_scheme; dg.ke_cell_wgt = c.ke_cell_wgt;
     dg.pv_scheme = c.pv_scheme; dg.upwind_order_pv = c.upwind_order_pv; dg.pv_pole_stokes = c.pv_pole_stokes;
     dg.coriolis_scheme = c.coriolis_scheme; dg.limiter = c.limiter_type; dg.upwind_wgt_pv = c.upwind_wgt_pv;
+    dg.flux_type = c.ffsl_flux_type; dg.tvd_limiter = c.tvd_limiter_type; dg.div_damp_order = c.div_damp_order;
   }
 
   FieldInfo info(const std::string &name) const {
@@ -677,19 +678,19 @@ struct Engine : EngineBase {
   }
 
   // operators_prepare forward list (operators_mod.F90:117-122)
-  void forward_prepare(int m, const Slot<R> &s) { forward_prepare_w(work[m], s); }
-  void forward_prepare_w(Work<R> &w, const Slot<R> &s) {
+  void forward_prepare(int m, const Slot<R> &s, double dt) { forward_prepare_w(work[m], s, dt); }
+  void forward_prepare_w(Work<R> &w, const Slot<R> &s, double dt) {
     K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
     K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
     K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
     K("pv", 1, [&] { launch_pv<R>(dg, L, s, w); });
-    K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w); });
+    K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w, dt); });
   }
 
   // space_operators forward pass (gmcore_mod.F90:467-528)
   void forward(int m, const Slot<R> &s, double dt) { forward_w(work[m], s, dt); }
   void forward_w(Work<R> &w, const Slot<R> &s, double dt) {
-    forward_prepare_w(w, s);
+    forward_prepare_w(w, s, dt);
     if (grid.cfg.baroclinic) {
       K("batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt); });
       K("column_mass", 1, [&] { launch_column_mass<R>(dg, L, s, w, dt); });
@@ -738,7 +739,7 @@ struct Engine : EngineBase {
         accum_wind(m, s, true);
         if (m + 1 < nm) { uv_step = save_uv; mf_step = save_mf; we_step = save_we; }
       }
-      forward_prepare(m, s);
+      forward_prepare(m, s, grid.cfg.dt_dyn);   // operators_prepare(blocks, old, dt_dyn)
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
@@ -793,6 +794,7 @@ struct Engine : EngineBase {
     if (nm != 1) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: one member"};
     if (grid.cfg.use_div_damp) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: divergence damping not differentiated"};
     if (!grid.cfg.pv_pole_stokes) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: needs pv_pole_stokes"};
+    if (grid.cfg.pv_scheme == GMC_PV_TVD) throw ApiError{GMC_EINVAL, "tangent-linear/adjoint: pv_scheme tvd not differentiated"};
     if (!prepared || time_step != 0) throw ApiError{GMC_ESTATE, "tangent-linear/adjoint start from the prepared state (gmc_prepare)"};
   }
 
@@ -1117,7 +1119,8 @@ struct Engine : EngineBase {
           break;
       }
       const Slot<R> &N = slots[m * 3 + n];
-      if (grid.cfg.use_div_damp) K("div_damp", 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke); });
+      if (grid.cfg.use_div_damp)
+        K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke, work[m].du); });
       if (ntr > 0) {
         uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
         adv_run(m, N, ring && time_step > 0);
@@ -1389,6 +1392,8 @@ void gmc_config_default(gmc_config *c) {
   c->n_members = 1;
   const double pi = std::atan(1.0) * 4.0;
   c->radius = 6.37122e6; c->omega = 2 * pi / 86400.0; c->g = 9.80616; c->Rd = 287.04; c->cpd = 1004.0; c->p0 = 1.0e5;
+  c->tvd_limiter_type = GMC_TVD_VAN_LEER;
+  c->div_damp_coef4 = 0.01;
 }
 
 int gmc_create(const gmc_config *cfg, gmc_ctx **out) {

@@ -230,18 +230,21 @@ std::string validate_config(const gmc_config &c) {
   }
   if (c.time_scheme < GMC_TIME_EULER || c.time_scheme > GMC_TIME_WRFRK3) return "bad time_scheme";
   if (c.ke_scheme != 1 && c.ke_scheme != 2) return "ke_scheme must be 1 or 2";
-  if (c.pv_scheme != GMC_PV_MIDPOINT && c.pv_scheme != GMC_PV_UPWIND) return "pv_scheme must be midpoint or upwind";
+  if (c.pv_scheme != GMC_PV_MIDPOINT && c.pv_scheme != GMC_PV_UPWIND && c.pv_scheme != GMC_PV_TVD)
+    return "pv_scheme must be midpoint, upwind or tvd";
+  if (c.pv_scheme == GMC_PV_TVD && (c.tvd_limiter_type < GMC_TVD_NONE || c.tvd_limiter_type > GMC_TVD_MC))
+    return "bad tvd_limiter_type";
   if (c.pv_scheme == GMC_PV_UPWIND && c.upwind_order_pv != 1 && c.upwind_order_pv != 3)
     return "upwind_order_pv must be 1 or 3";
   if (c.coriolis_scheme != 1 && c.coriolis_scheme != 2) return "coriolis_scheme must be 1 or 2";
-  if (c.ffsl_flux_type != GMC_FLUX_PPM) return "only ffsl_flux_type = ppm is supported";
+  if (c.ffsl_flux_type != GMC_FLUX_PPM && c.ffsl_flux_type != GMC_FLUX_VAN_LEER) return "ffsl_flux_type must be ppm or van_leer";
   if (c.limiter_type < GMC_LIMITER_NONE || c.limiter_type > GMC_LIMITER_PD) return "bad limiter_type";
   if (!(c.dt_dyn > 0)) return "dt_dyn must be > 0";
   if (c.ntracer < 0 || c.ntracer > 64) return "ntracer must be in 0..64";
   if (c.ntracer > 0 && !c.baroclinic) return "tracers need the baroclinic model";
   if (c.precision != GMC_PREC_FP64 && c.precision != GMC_PREC_MIXED) return "bad precision";
   if (c.n_members < 1) return "n_members must be >= 1";
-  if (c.use_div_damp && c.div_damp_order != 2) return "only div_damp_order = 2 is supported";
+  if (c.use_div_damp && c.div_damp_order != 2 && c.div_damp_order != 4) return "div_damp_order must be 2 or 4";
   if (c.lon_halo_width < 1) return "lon_halo_width must be >= 1";
   // device kernels index one field with 32-bit arithmetic
   if ((double)(c.nlev + 1) * c.nlat * c.nlon >= 2147483647.0) return "grid too large: (nlev+1)*nlat*nlon must be < 2^31";
@@ -528,10 +531,17 @@ std::string Grid::build(const gmc_config &c) {
   for (int j = 1; j <= nhalf; ++j) max_hw = std::max(max_hw, (big.ngrid_half[j - 1] - 1) / 2);
   lon_halo_width = std::max(max_hw, c.lon_halo_width);
 
-  // divergence damping, order 2 (div_damp_mod.F90:41-64)
+  // divergence damping coefficients (div_damp_mod.F90:41-76)
   div_c_lon.assign((size_t)nlev * nlat, 0.0);
   div_c_lat.assign((size_t)nlev * nhalf, 0.0);
-  if (c.use_div_damp) {
+  if (c.use_div_damp && c.div_damp_order == 4) {
+    for (int k = 1; k <= nlev; ++k) {
+      for (int j = 2; j <= nlat - 1; ++j)
+        div_c_lon[(size_t)(k - 1) * nlat + (j - 1)] = c.div_damp_coef4 * (le_lon[j] * le_lon[j]) * (de_lon[j] * de_lon[j]);
+      for (int j = 1; j <= nhalf; ++j)
+        div_c_lat[(size_t)(k - 1) * nhalf + (j - 1)] = c.div_damp_coef4 * (le_lat[j] * le_lat[j]) * (de_lat[j] * de_lat[j]);
+    }
+  } else if (c.use_div_damp) {
     for (int k = 1; k <= nlev; ++k) {
       double amp = 1.0;
       if (c.baroclinic) {

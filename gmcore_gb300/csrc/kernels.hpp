@@ -68,7 +68,7 @@ template <class R> void launch_mass_flux(const DGrid &g, const Launch &L, const 
 template <class R> void launch_tangent_winds(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w);
 template <class R> void launch_kinetic_energy(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w);
 template <class R> void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w);
-template <class R> void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w);
+template <class R> void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt);
 // CFL numbers and axis divergences of a batch (adv_batch_accum_uv_cell).
 template <class R> void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt);
 template <class R> void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt);
@@ -84,9 +84,9 @@ template <class R> void launch_filter_prologue(const DGrid &g, const Launch &L, 
 template <class R> void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s);
 template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out);
 
-// Divergence damping, order 2 (div_damp_run, div_damp_mod.F90:89-118);
-// div is a scratch cell field.
-template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div);
+// Divergence damping of order 2 or 4 (div_damp_run, div_damp_mod.F90:89-139);
+// div and div2 are scratch cell fields.
+template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, R *div2);
 
 // ---- advection (adv.cu) ---------------------------------------------------
 // Horizontal FFSL flux of q (ffsl_calc_tracer_hflx_cell): inner advective

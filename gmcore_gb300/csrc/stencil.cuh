@@ -50,6 +50,19 @@ struct MassField {
   }
 };
 
+// TVD interpolation with flux limiter (tvd_mod.F90:44-84); eps is the
+// default-kind literal 1.0e-6 of the reference widened to double.
+template <class R>
+__device__ __forceinline__ R tvd_interp(int limiter, R cfl, R fm1, R f, R fp1, R fp2) {
+  const R eps = (R)(double)1.0e-6f;
+  const R r = cfl > 0 ? (f - fm1 + eps) / (fp1 - f + eps) : (fp2 - fp1 + eps) / (fp1 - f + eps);
+  R C;
+  if (limiter == GMC_TVD_NONE) C = 1;
+  else if (limiter == GMC_TVD_MC) C = fmax((R)0, fmin(fmin((R)2 * r, (R)0.5 * (1 + r)), (R)2));
+  else C = (r + fabs(r)) / (1 + fabs(r));
+  return (R)0.5 * (fp1 + f - ((1 - C) * fsign((R)1, cfl) + cfl * C) * (fp1 - f));
+}
+
 // Upwind interpolation of order 3 and 1 (upwind_mod.F90:27-39) along the
 // direction dir = sign of the advecting wind, weighted by wgt.
 template <class R>

@@ -56,8 +56,14 @@ extern "C" {
 
 #define GMC_PV_MIDPOINT   0  /* pv_scheme = 'midpoint' */
 #define GMC_PV_UPWIND     1  /* pv_scheme = 'upwind'   */
+#define GMC_PV_TVD        2  /* pv_scheme = 'tvd'      */
 
-#define GMC_FLUX_PPM      0  /* ffsl_flux_type = 'ppm' */
+#define GMC_TVD_NONE      0  /* tvd_limiter_type = 'none'     */
+#define GMC_TVD_VAN_LEER  1  /* tvd_limiter_type = 'van_leer' */
+#define GMC_TVD_MC        2  /* tvd_limiter_type = 'mc'       */
+
+#define GMC_FLUX_PPM      0  /* ffsl_flux_type = 'ppm'      */
+#define GMC_FLUX_VAN_LEER 1  /* ffsl_flux_type = 'van_leer' */
 
 #define GMC_LIMITER_NONE  0  /* limiter_type = 'none'  */
 #define GMC_LIMITER_MONO  1  /* limiter_type = 'mono'  */
@@ -89,7 +95,7 @@ typedef struct gmc_config {
   int32_t ffsl_flux_type;          /* GMC_FLUX_*                                 */
   int32_t limiter_type;            /* GMC_LIMITER_*                              */
   int32_t use_div_damp;            /* divergence damping after each step         */
-  int32_t div_damp_order;          /* 2 (4 is not supported)                     */
+  int32_t div_damp_order;          /* 2 or 4                                     */
   double  div_damp_coef2;          /* namelist div_damp_coef2                    */
   int32_t vert_coord_template;     /* GMC_VCOORD_*                               */
   double  ptop;                    /* Pa (namelist ptop)                         */
@@ -101,6 +107,8 @@ typedef struct gmc_config {
   int32_t precision;               /* GMC_PREC_*                                 */
   int32_t n_members;               /* ensemble members sharing this grid         */
   double  radius, omega, g, Rd, cpd, p0;   /* const_mod.F90:51-85 ('earth')     */
+  int32_t tvd_limiter_type;        /* GMC_TVD_* (pv_scheme = tvd)                */
+  double  div_damp_coef4;          /* namelist div_damp_coef4 (order 4)          */
 } gmc_config;
 
 /* Diagnostics of gmcore_mod.F90:213-341 (FP64, compensated sums). */

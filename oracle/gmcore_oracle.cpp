@@ -113,7 +113,7 @@ struct Fields {
 struct State {
   Arr u_lon, v_lon, u_f, u_lat, v_lat, v_f, we_lev, we_lev_lon, we_lev_lat, gz, gz_lev, m, m_vtx, m_lon,
       m_lat, m_lev, mfx_lon, mfy_lon, mfy_lat, mfx_lat, pv, pv_lon, pv_lat, ke, pt, ptf_lon, ptf_lat,
-      ptf_lev, t, ph, ph_lev, ph_exn_lev, phs, phs_f, vor, gz_f, div;
+      ptf_lev, t, ph, ph_lev, ph_exn_lev, phs, phs_f, vor, gz_f, div, div2;
 };
 
 struct Tend {
@@ -251,6 +251,7 @@ struct Model {
     F.vtx3(s.pv); F.lon3(s.pv_lon); F.lat3(s.pv_lat); F.cell3(s.ke); F.cell3(s.pt);
     F.lon3(s.ptf_lon); F.lat3(s.ptf_lat); F.lev3(s.ptf_lev); F.cell3(s.t); F.cell3(s.ph);
     F.lev3(s.ph_lev); F.lev3(s.ph_exn_lev); F.cell2(s.phs); F.cell2(s.phs_f); F.vtx3(s.vor); F.cell3(s.div);
+    F.cell3(s.div2);   // zero at allocation, pole rows never written (allocator_mod.F90:198)
     if (!baroclinic) F.cell3(s.gz_f);
   }
   void alloc_tend(Tend &t) {
@@ -697,10 +698,47 @@ struct Model {
     return c31 * (f3 + f2) + c32 * (f4 + f1) + c33 * (f4 - f1 - 3 * (f3 - f2)) * wgt * dir;
   }
 
-  void interp_pv(State &s) {   // operators_mod.F90:705-795
+  // tvd (tvd_mod.F90:44-60) with the flux limiters of :62-84; eps is the
+  // default-kind literal 1.0e-6 widened to double.
+  double tvd(double cfl, double fm1, double f, double fp1, double fp2) const {
+    const double eps = (double)1.0e-6f;
+    double r;
+    if (cfl > 0)
+      r = (f - fm1 + eps) / (fp1 - f + eps);
+    else
+      r = (fp2 - fp1 + eps) / (fp1 - f + eps);
+    double C;
+    switch (cfg.tvd_limiter_type) {
+      case GMC_TVD_NONE: C = 1; break;
+      case GMC_TVD_MC: C = std::fmax(0.0, std::fmin(std::fmin(2.0 * r, 0.5 * (1 + r)), 2.0)); break;
+      default: C = (r + std::fabs(r)) / (1 + std::fabs(r)); break;
+    }
+    return 0.5 * (fp1 + f - ((1 - C) * fsign(1.0, cfl) + cfl * C) * (fp1 - f));
+  }
+
+  void interp_pv(State &s, double dt) {   // operators_mod.F90:705-832
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const double eps = std::numeric_limits<double>::epsilon();
     Arr &pv = s.pv;
+    if (cfg.pv_scheme == GMC_PV_TVD) {   // interp_pv_tvd :797-832
+      const gmc::Grid &g = G();
+      #pragma omp parallel for schedule(static)
+      for (int k = 1; k <= nlev; ++k) {
+        for (int j = 2; j <= nlat - 1; ++j)
+          for (int i = 1; i <= nlon; ++i) {
+            double cfl = s.v_lon(i, j, k) * dt / g.le_lon[j];
+            s.pv_lon(i, j, k) = tvd(cfl, pv(i, j - 2, k), pv(i, j - 1, k), pv(i, j, k), pv(i, j + 1, k));
+          }
+        for (int j = 1; j <= nhalf; ++j)
+          for (int i = 1; i <= nlon; ++i) {
+            double cfl = s.u_lat(i, j, k) * dt / g.le_lat[j];
+            s.pv_lat(i, j, k) = tvd(cfl, pv(i - 2, j, k), pv(i - 1, j, k), pv(i, j, k), pv(i + 1, j, k));
+          }
+      }
+      fill_halo(s.pv_lon, true, true, true, false, true);
+      fill_halo(s.pv_lat, false, true, true, true, false);
+      return;
+    }
     if (cfg.pv_scheme == GMC_PV_MIDPOINT) {
       #pragma omp parallel for schedule(static)
       for (int k = 1; k <= nlev; ++k)
@@ -990,12 +1028,86 @@ struct Model {
         }
   }
 
+  // hflx_van_leer_cell (ffsl_mod.F90:556-616)
+  void hflx_van_leer_cell(Batch &b, Arr &u, Arr &v, Arr &mx, Arr &my, Arr &mfx, Arr &mfy) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
+    #pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nlev; ++k) {
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          double c = b.cflx(i, j, k);
+          int ci = (int)c;
+          double cf = c - ci;
+          if (c > 0) {
+            int iu = i - ci;
+            double dm = slope(mx(iu - 1, j, k), mx(iu, j, k), mx(iu + 1, j, k));
+            double sum = 0;
+            for (int l = i + 1 - ci; l <= i; ++l) sum = sum + mx(l, j, k);
+            mfx(i, j, k) = u(i, j, k) * (cf * (mx(iu, j, k) + dm * 0.5 * (1 - cf)) + sum) / c;
+          } else if (c < 0) {
+            int iu = i - ci + 1;
+            double dm = slope(mx(iu - 1, j, k), mx(iu, j, k), mx(iu + 1, j, k));
+            double sum = 0;
+            for (int l = i + 1; l <= i - ci; ++l) sum = sum + mx(l, j, k);
+            mfx(i, j, k) = u(i, j, k) * (cf * (mx(iu, j, k) - dm * 0.5 * (1 + cf)) - sum) / c;
+          } else {
+            mfx(i, j, k) = 0;
+          }
+        }
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          double cf = b.cfly(i, j, k);
+          int ju = cf > 0 ? j : j + 1;
+          double dm = slope(my(i, ju - 1, k), my(i, ju, k), my(i, ju + 1, k));
+          mfy(i, j, k) = v(i, j, k) * (my(i, ju, k) + dm * 0.5 * (fsign(1.0, cf) - cf));
+        }
+    }
+  }
+
+  // vflx_van_leer_cell (ffsl_mod.F90:618-658)
+  void vflx_van_leer_cell(Batch &b, Arr &w, Arr &m, Arr &mfz) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nlat = mesh.nlat;
+    #pragma omp parallel for schedule(static)
+    for (int k = 2; k <= nlev; ++k)
+      for (int j = 1; j <= nlat; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          double c = b.cflz(i, j, k);
+          int ci = (int)c;
+          double cf = c - ci;
+          if (c > 0) {
+            int ku = k - ci - 1;
+            double dm = slope(m(i, j, ku - 1), m(i, j, ku), m(i, j, ku + 1));
+            double sum = 0;
+            for (int l = k - ci; l <= k - 1; ++l) sum = sum + m(i, j, l);
+            mfz(i, j, k) = w(i, j, k) * (cf * (m(i, j, ku) + dm * 0.5 * (1 - cf)) + sum) / c;
+          } else if (c < 0) {
+            int ku = k - ci;
+            double dm = slope(m(i, j, ku - 1), m(i, j, ku), m(i, j, ku + 1));
+            double sum = 0;
+            for (int l = k; l <= k - ci - 1; ++l) sum = sum + m(i, j, l);
+            mfz(i, j, k) = w(i, j, k) * (cf * (m(i, j, ku) - dm * 0.5 * (1 + cf)) - sum) / c;
+          } else {
+            mfz(i, j, k) = 0;
+          }
+        }
+  }
+
+  // the hflx_cell / vflx_cell procedure pointers (ffsl_mod.F90:114-142)
+  void hflx_cell(Batch &b, Arr &u, Arr &v, Arr &mx, Arr &my, Arr &mfx, Arr &mfy) {
+    if (cfg.ffsl_flux_type == GMC_FLUX_VAN_LEER) hflx_van_leer_cell(b, u, v, mx, my, mfx, mfy);
+    else hflx_ppm_cell(b, u, v, mx, my, mfx, mfy);
+  }
+  void vflx_cell(Batch &b, Arr &w, Arr &m, Arr &mfz) {
+    if (cfg.ffsl_flux_type == GMC_FLUX_VAN_LEER) vflx_van_leer_cell(b, w, m, mfz);
+    else vflx_ppm_cell(b, w, m, mfz);
+  }
+
   // ffsl_calc_tracer_hflx_cell (ffsl_mod.F90:318-413)
   void tracer_hflx_cell(Batch &b, Arr &q, Arr &qmfx, Arr &qmfy, double dt_) {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
     Arr &qx = b.qx, &qy = b.qy;
-    hflx_ppm_cell(b, b.u, b.v, q, q, qmfx, qmfy);
+    hflx_cell(b, b.u, b.v, q, q, qmfx, qmfy);
     fill_halo(qmfx, true, true, true, false, false);
     fill_halo(qmfy, false, false, false, true, true);
     #pragma omp parallel for schedule(static)
@@ -1024,7 +1136,7 @@ struct Model {
     }
     fill_halo(qx, true, false, false, true, true);
     fill_halo(qy, true, true, true, false, false);
-    hflx_ppm_cell(b, b.mfx, b.mfy, qy, qx, qmfx, qmfy);
+    hflx_cell(b, b.mfx, b.mfy, qy, qx, qmfx, qmfy);
   }
 
   void calc_grad_ptf(State &s, Tend &t, double dt) {   // operators_mod.F90:1008-1118
@@ -1040,7 +1152,7 @@ struct Model {
     for (int k = nlev + 1; k <= nlev + 2; ++k)
       for (int j = pt.lb1; j <= pt.ub1; ++j)
         for (int i = pt.lb0; i <= pt.ub0; ++i) pt(i, j, k) = 2 * pt(i, j, k - 1) - pt(i, j, k - 2);
-    vflx_ppm_cell(mass, mass.we, pt, s.ptf_lev);
+    vflx_cell(mass, mass.we, pt, s.ptf_lev);
     #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 1; j <= mesh.nlat; ++j)
@@ -1087,7 +1199,7 @@ struct Model {
     calc_mf(s, dt);
     calc_ke(s);
     calc_pv(s);
-    interp_pv(s);
+    interp_pv(s, dt);
   }
   void operators_prepare_bwd(State &s) {
     if (hydrostatic) {
@@ -1243,14 +1355,46 @@ struct Model {
       p = p * g.le_lat[nhalf] / nlon / g.area_cell[nlat];
       for (int i = 1; i <= nlon; ++i) div(i, nlat, k) = p;
     }
-    fill_halo(div, true, false, true, false, true);
+    if (cfg.div_damp_order != 4) {
+      fill_halo(div, true, false, true, false, true);
+      return;
+    }
+    fill_halo(div, true);
+    Arr &div2 = s.div2;   // operators_mod.F90:412-425
+    #pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i)
+          div2(i, j, k) = (div(i + 1, j, k) - 2 * div(i, j, k) + div(i - 1, j, k)) / (g.de_lon[j] * g.de_lon[j]) +
+                          ((div(i, j + 1, k) - div(i, j, k)) * g.half_cos_lat[j] / g.de_lat[j] -
+                           (div(i, j, k) - div(i, j - 1, k)) * g.half_cos_lat[j - 1] / g.de_lat[j - 1]) /
+                              g.le_lon[j] / g.full_cos_lat[j];
+    fill_halo(div2, true, false, true, false, true);
   }
 
-  // div_damp_run, order 2 (div_damp_mod.F90:89-118)
+  // div_damp_run (div_damp_mod.F90:89-139)
   void div_damp_run(State &s) {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
     calc_div(s);
+    if (cfg.div_damp_order == 4) {
+      Arr &div2 = s.div2;
+      #pragma omp parallel for schedule(static)
+      for (int k = 1; k <= nlev; ++k)
+        for (int j = 2; j <= nlat - 1; ++j)
+          for (int i = 1; i <= nlon; ++i)
+            s.u_lon(i, j, k) = s.u_lon(i, j, k) -
+                               g.div_c_lon[(size_t)(k - 1) * nlat + (j - 1)] * (div2(i + 1, j, k) - div2(i, j, k)) / g.de_lon[j];
+      #pragma omp parallel for schedule(static)
+      for (int k = 1; k <= nlev; ++k)
+        for (int j = 1; j <= nhalf; ++j)
+          for (int i = 1; i <= nlon; ++i)
+            s.v_lat(i, j, k) = s.v_lat(i, j, k) -
+                               g.div_c_lat[(size_t)(k - 1) * nhalf + (j - 1)] * (div2(i, j + 1, k) - div2(i, j, k)) / g.de_lat[j];
+      fill_halo(s.u_lon, true);
+      fill_halo(s.v_lat, false);
+      return;
+    }
     Arr &div = s.div;
     #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
@@ -1354,7 +1498,7 @@ struct Model {
         for (int k = nlev + 1; k <= qn.ub2; ++k)
           for (int j = qn.lb1; j <= qn.ub1; ++j)
             for (int i = qn.lb0; i <= qn.ub0; ++i) qn(i, j, k) = qn(i, j, nlev);
-        vflx_ppm_cell(b, b.we, qn, b.qmf_lev);
+        vflx_cell(b, b.we, qn, b.qmf_lev);
         for (int k = 1; k <= nlev; ++k)
           for (int j = 1; j <= nlat; ++j)
             for (int i = 1; i <= nlon; ++i)
@@ -1422,7 +1566,7 @@ struct Model {
     calc_mf(s, cfg.dt_dyn);
     calc_ke(s);
     calc_pv(s);
-    interp_pv(s);
+    interp_pv(s, cfg.dt_dyn);
     if (hydrostatic) calc_gz_lev(s);
   }
 

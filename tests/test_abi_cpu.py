@@ -38,8 +38,8 @@ def test_config_default_matches_python_mirror():
 
 def test_invalid_configs_are_rejected_before_any_device_work():
     bad = [dict(nlon=7), dict(nlat=3), dict(nlev=2, baroclinic=0), dict(baroclinic=1, nlev=30, vert_coord_template=32),
-           dict(time_scheme=9), dict(pv_scheme=7), dict(ntracer=2), dict(use_div_damp=1, div_damp_order=4),
-           dict(dt_dyn=0.0)]
+           dict(time_scheme=9), dict(pv_scheme=7), dict(ntracer=2), dict(use_div_damp=1, div_damp_order=3),
+           dict(dt_dyn=0.0), dict(pv_scheme=abi.PV_TVD, tvd_limiter_type=5), dict(ffsl_flux_type=4)]
     for kw in bad:
         cfg = abi.default_config(**kw)
         with pytest.raises(g.GmcError) as e:
