@@ -1570,6 +1570,40 @@ struct Model {
     if (hydrostatic) calc_gz_lev(s);
   }
 
+  // debug_check_space_operators (debug_mod.F90:113-220): inner products of
+  // the forward-pass tendencies of state(old) that the C-grid scheme keeps
+  // near zero.  out = {ip_cf, |cf|, ip_ke, |ke|, ip_mf, |mf|, ip_ptf, |ptf|},
+  // each divided by 4 pi radius^2 (the |.| entries sum absolute terms, for scale).
+  void space_identities(double out[8]) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
+    const gmc::Grid &g = G();
+    State &s = state[old_i];
+    Tend &t = tend[0];
+    space_operators_fwd(s, t, cfg.dt_dyn);
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    auto add = [&](int q, double x) { v[q] += x; v[q + 1] += std::fabs(x); };
+    for (int k = 1; k <= nlev; ++k) {
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          add(0, t.qhv(i, j, k) * s.mfx_lon(i, j, k) * g.area_lon[j]);
+          add(2, t.dkedlon(i, j, k) * s.mfx_lon(i, j, k) * g.area_lon[j] * 2);
+        }
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          add(0, -t.qhu(i, j, k) * s.mfy_lat(i, j, k) * g.area_lat[j]);
+          add(2, t.dkedlat(i, j, k) * s.mfy_lat(i, j, k) * g.area_lat[j] * 2);
+        }
+      for (int j = 1; j <= nlat; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          add(2, (t.dmfdlon(i, j, k) + t.dmfdlat(i, j, k)) * s.ke(i, j, k) * g.area_cell[j]);
+          add(4, (t.dmfdlon(i, j, k) + t.dmfdlat(i, j, k)) * g.area_cell[j]);
+          if (hydrostatic) add(6, (t.dptfdlon(i, j, k) + t.dptfdlat(i, j, k) + t.dptfdlev(i, j, k)) * g.area_cell[j]);
+        }
+    }
+    const double pi = std::atan(1.0) * 4.0, a = 4 * pi * cfg.radius * cfg.radius;
+    for (int q = 0; q < 8; ++q) out[q] = v[q] / a;
+  }
+
   void time_integrate() {
     const double dt = cfg.dt_dyn;
     const int o = old_i, n = new_i, t3 = 3 - o - n;
@@ -1763,6 +1797,11 @@ int orc_step(void *h, int nsteps, char *errbuf, int errlen) {
   for (int n = 0; n < nsteps && m->err.code == 0; ++n) m->time_integrate();
   if (m->err.code && errbuf) snprintf(errbuf, errlen, "%s", m->err.msg.c_str());
   return m->err.code;
+}
+
+int orc_space_identities(void *h, double *out) {
+  ((orc::Model *)h)->space_identities(out);
+  return 0;
 }
 
 int orc_diagnose(void *h, double *out) {

@@ -41,6 +41,7 @@ def load(variant="parity"):
     lib.orc_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     lib.orc_step.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
     lib.orc_diagnose.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.orc_space_identities.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.orc_metric.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int]
     lib.orc_filter_taps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
@@ -134,6 +135,13 @@ class Oracle:
         out = np.zeros(8)
         self.lib.orc_diagnose(self.h, _ptr(out))
         return dict(zip(("tm", "te", "te_ke", "te_ie", "te_pe", "tav", "tpe", "tpt"), out))
+
+    def space_identities(self):
+        """Inner products of debug_check_space_operators at state(old)
+        (call after prepare): {name: (sum, sum of |terms|)} per 4 pi r^2."""
+        out = np.zeros(8)
+        self.lib.orc_space_identities(self.h, _ptr(out))
+        return {"coriolis": (out[0], out[1]), "ke": (out[2], out[3]), "mass": (out[4], out[5]), "ptf": (out[6], out[7])}
 
     def metric(self, name, n):
         out = np.zeros(n)

@@ -142,3 +142,39 @@ def test_seeded_initial_state_is_deterministic():
     assert not np.array_equal(a["pt"], c["pt"])
     # golden checksum of the generator (SplitMix64 + Box-Muller)
     assert abs(float(a["pt"].sum()) - float(b["pt"].sum())) == 0.0
+
+
+@pytest.mark.parametrize("baroclinic", [False, True])
+def test_space_operator_energy_identities(baroclinic):
+    """debug_check_space_operators (debug_mod.F90:113-220): with the
+    energy-conserving Coriolis scheme the Coriolis force does no work, the KE
+    gradient's work cancels the KE flux divergence, mass and (baroclinic) pt
+    flux divergences integrate to zero -- each to round-off relative to the sum
+    of the magnitudes of its terms.  The non-conserving coriolis_scheme 2 must
+    not satisfy the first identity."""
+    from oracle import Oracle
+    from helpers import baroclinic_config, initial_state, load_state, swm_config
+    if baroclinic:
+        cfg, steps = baroclinic_config(), 3
+    else:
+        cfg, steps = swm_config(), 0
+    o = Oracle(cfg)
+    load_state(o, initial_state(cfg))
+    o.prepare()
+    o.step(steps)
+    r = o.space_identities()
+    names = ("coriolis", "ke", "mass") + (("ptf",) if baroclinic else ())
+    for name in names:
+        val, scale = r[name]
+        assert scale > 0, name
+        assert abs(val) <= 1e-13 * scale, (name, val, scale)
+    o.close()
+    if baroclinic:
+        cfg2 = baroclinic_config(coriolis_scheme=2)
+        o = Oracle(cfg2)
+        load_state(o, initial_state(cfg2))
+        o.prepare()
+        o.step(steps)
+        val, scale = o.space_identities()["coriolis"]
+        assert abs(val) > 1e-8 * scale
+        o.close()
