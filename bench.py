@@ -235,8 +235,8 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with host buffers ----
     host = {k: np.ascontiguousarray(v) for k, v in st.items()}
-    out = {k: np.empty_like(v) for k, v in host.items() if k != "q"}
-    qout = np.empty_like(host["q"])
+    out = {k: np.zeros_like(v) for k, v in host.items() if k != "q"}   # touched: no page faults when timed
+    qout = np.zeros_like(host["q"])
     e2e_steps = max(2, min(args.steps, 10))
     barrier()
     t0 = time.perf_counter()
@@ -247,13 +247,13 @@ def run_ours(args):
             model.set_tracer(l, host["q"][l])
         model.step(1)
         for name in ("u_lon", "v_lat", "pt", "phs"):
-            out[name][...] = model.get_field(name)
+            model.get_field(name, out=out[name])
         for l in range(NTRACER):
-            qout[l] = model.get_tracer(l)
-        host["u_lon"], host["v_lat"], host["pt"], host["phs"] = out["u_lon"], out["v_lat"], out["pt"], out["phs"]
-        host["q"] = qout
-        out = {k: np.empty_like(v) for k, v in out.items()}
-        qout = np.empty_like(qout)
+            model.get_tracer(l, out=qout[l])
+        # the step's result is the next step's input
+        for name in ("u_lon", "v_lat", "pt", "phs"):
+            host[name], out[name] = out[name], host[name]
+        host["q"], qout = qout, host["q"]
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     h2d = sum(host[k].nbytes for k in ("u_lon", "v_lat", "pt", "phs", "q"))

@@ -207,8 +207,13 @@ class Model:
         a = np.ascontiguousarray(a, dtype=np.float64).reshape(field_shape(self.cfg, name))
         self._check(self.lib.gmc_set_field(self.h, member, name.encode(), C.byref(view_of(a))))
 
-    def get_field(self, name, member=0):
-        out = np.zeros(field_shape(self.cfg, name))
+    def get_field(self, name, member=0, out=None):
+        """Field of the current state; written into `out` (a C-contiguous
+        float64 array of the field's shape) when given."""
+        if out is None:
+            out = np.empty(field_shape(self.cfg, name))
+        elif out.shape != field_shape(self.cfg, name):
+            raise ValueError(f"out has shape {out.shape}, field {name} {field_shape(self.cfg, name)}")
         self._check(self.lib.gmc_get_field(self.h, member, name.encode(), C.byref(view_of(out))))
         return out
 
@@ -248,8 +253,12 @@ class Model:
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.cfg.nlev, self.cfg.nlat, self.cfg.nlon)
         self._check(self.lib.gmc_set_tracer(self.h, member, l, C.byref(view_of(q))))
 
-    def get_tracer(self, l, member=0):
-        out = np.zeros((self.cfg.nlev, self.cfg.nlat, self.cfg.nlon))
+    def get_tracer(self, l, member=0, out=None):
+        shape = (self.cfg.nlev, self.cfg.nlat, self.cfg.nlon)
+        if out is None:
+            out = np.empty(shape)
+        elif out.shape != shape:
+            raise ValueError(f"out has shape {out.shape}, tracer {shape}")
         self._check(self.lib.gmc_get_tracer(self.h, member, l, C.byref(view_of(out))))
         return out
 

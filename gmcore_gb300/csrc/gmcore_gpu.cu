@@ -7,11 +7,14 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <condition_variable>
 #include <memory>
 #include <tuple>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -88,16 +91,114 @@ struct FieldInfo {
 // ---------------------------------------------------------------------------
 // Engine: one precision instantiation of the step.
 // ---------------------------------------------------------------------------
+// Host-side parallel loop over [0, n) in contiguous chunks (the row gathers,
+// scatters and FP64<->FP32 conversions of field transfers), on a persistent
+// pool of worker threads shared by all contexts; the calling thread works too.
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool pool;
+    return pool;
+  }
+  template <class F>
+  void run(size_t n, F &&f) {
+    const unsigned nt = (unsigned)std::min<size_t>(workers_.size() + 1, std::max<size_t>(1, n / 16));
+    if (nt <= 1) {
+      f((size_t)0, n);
+      return;
+    }
+    std::unique_lock<std::mutex> call(call_mu_);   // one parallel loop at a time
+    const size_t chunk = (n + nt - 1) / nt;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = [&f, n, chunk](unsigned t) {
+        const size_t a = t * chunk, b = std::min(n, a + chunk);
+        if (a < b) f(a, b);
+      };
+      ntasks_ = nt;
+      next_ = 0;
+      remaining_ = nt;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return remaining_ == 0; });
+    job_ = nullptr;
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto &w : workers_) w.join();
+  }
+
+ private:
+  HostPool() {
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (unsigned t = 1; t < hw; ++t)
+      workers_.emplace_back([this] {
+        uint64_t seen = 0;
+        for (;;) {
+          {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+          }
+          work();
+        }
+      });
+  }
+  void work() {
+    for (;;) {
+      unsigned t;
+      std::function<void(unsigned)> job;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (next_ >= ntasks_ || !job_) return;
+        t = next_++;
+        job = job_;
+      }
+      job(t);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--remaining_ == 0) done_cv_.notify_all();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex mu_, call_mu_;
+  std::condition_variable cv_, done_cv_;
+  std::function<void(unsigned)> job_;
+  unsigned ntasks_ = 0, next_ = 0, remaining_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+template <class F>
+void host_par_for(size_t n, F &&f) {
+  HostPool::get().run(n, f);
+}
+
+// Row r (k-major over nk levels of nrow rows) of the interior of a view.
+inline double *view_row(const gmc_view &v, int nrow, size_t r) {
+  const long n0 = v.ub[0] - v.lb[0] + 1, n1 = v.ub[1] - v.lb[1] + 1;
+  const int k = (int)(r / nrow) + 1, j = (int)(r % nrow) + 1;
+  return v.data + (size_t)(1 - v.lb[0]) + (size_t)n0 * ((size_t)(j - v.lb[1]) + (size_t)n1 * (size_t)(k - v.lb[2]));
+}
+
 struct EngineBase {
   virtual ~EngineBase() {}
-  virtual void set_field(int member, const std::string &name, const double *src) = 0;
-  virtual void get_field(int member, const std::string &name, double *dst) = 0;
+  // host fields cross as gmc_view (interior rows gathered/scattered in place)
+  virtual void set_field(int member, const std::string &name, const gmc_view &src) = 0;
+  virtual void get_field(int member, const std::string &name, const gmc_view &dst) = 0;
   virtual void prepare() = 0;
   virtual void step(int nsteps) = 0;
   virtual void diagnose(int member, gmc_diag *out) = 0;
   virtual unsigned read_error() = 0;
-  virtual void set_tracer(int member, int l, const double *src) = 0;
-  virtual void get_tracer(int member, int l, double *dst) = 0;
+  virtual void set_tracer(int member, int l, const gmc_view &src) = 0;
+  virtual void get_tracer(int member, int l, const gmc_view &dst) = 0;
   virtual void ffsl_hflx(const gmc_ffsl_fields &f, double dt) = 0;
   virtual size_t ffsl_scratch_bytes() const = 0;
   virtual void ffsl_hflx_in(const gmc_ffsl_fields &f, double dt, void *scratch) = 0;
@@ -294,6 +395,7 @@ struct Engine : EngineBase {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     for (cudaStream_t st : mstreams) cudaStreamDestroy(st);
     for (cudaEvent_t e : mevents) cudaEventDestroy(e);
+    for (cudaEvent_t e : xfer_ev) cudaEventDestroy(e);
     if (fork_ev) cudaEventDestroy(fork_ev);
     arena.release();
     tables.release();
@@ -489,56 +591,93 @@ struct Engine : EngineBase {
 
   size_t count(const FieldInfo &f) const { return (size_t)f.nk * f.nrow * grid.nlon; }
 
-  void set_field(int m, const std::string &name, const double *src) override {
-    FieldInfo f = info(name);
-    R *pr;
-    double *pd;
-    locate(slots[m * 3 + old_i], m, name, &pr, &pd);
-    const size_t n = count(f);
-    if (pd) {
-      CK(cudaMemcpyAsync(pd, src, n * sizeof(double), cudaMemcpyHostToDevice, stream));
-    } else {
-      R *host = reinterpret_cast<R *>(pinned);
-      for (size_t t = 0; t < n; ++t) host[t] = (R)src[t];
-      CK(cudaMemcpyAsync(pr, host, n * sizeof(R), cudaMemcpyHostToDevice, stream));
+  // Host <-> device transfers of a field given as a view.  The rows are moved
+  // in chunks: while one chunk's DMA runs the host pool converts the next
+  // (gather and FP64 -> T on upload, T -> FP64 and scatter on download).
+  static constexpr int kXferChunks = 8;
+  std::vector<cudaEvent_t> xfer_ev;
+  void xfer_events() {
+    if (!xfer_ev.empty()) return;
+    xfer_ev.resize(kXferChunks);
+    for (auto &e : xfer_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  template <class T>
+  void upload_view(const gmc_view &v, int nrow, int nk, T *dev, T *const *also = nullptr, int nalso = 0) {
+    const int nlon = grid.nlon;
+    const size_t rows = (size_t)nrow * nk, per = (rows + kXferChunks - 1) / kXferChunks;
+    T *host = reinterpret_cast<T *>(pinned);
+    for (size_t a = 0; a < rows; a += per) {
+      const size_t b = std::min(rows, a + per);
+      host_par_for(b - a, [&](size_t x, size_t y) {
+        for (size_t r = a + x; r < a + y; ++r) {
+          const double *src = view_row(v, nrow, r);
+          T *d = host + r * nlon;
+          for (int i = 0; i < nlon; ++i) d[i] = (T)src[i];
+        }
+      });
+      CK(cudaMemcpyAsync(dev + a * nlon, host + a * nlon, (b - a) * nlon * sizeof(T), cudaMemcpyHostToDevice, stream));
     }
+    for (int t = 0; t < nalso; ++t)   // further device copies of the same field
+      CK(cudaMemcpyAsync(also[t], dev, rows * nlon * sizeof(T), cudaMemcpyDeviceToDevice, stream));
     CK(cudaStreamSynchronize(stream));
   }
+  template <class T>
+  void download_view(const T *dev, int nrow, int nk, const gmc_view &v) {
+    xfer_events();
+    const int nlon = grid.nlon;
+    const size_t rows = (size_t)nrow * nk, per = (rows + kXferChunks - 1) / kXferChunks;
+    T *host = reinterpret_cast<T *>(pinned);
+    int c = 0;
+    for (size_t a = 0; a < rows; a += per, ++c) {
+      const size_t b = std::min(rows, a + per);
+      CK(cudaMemcpyAsync(host + a * nlon, dev + a * nlon, (b - a) * nlon * sizeof(T), cudaMemcpyDeviceToHost, stream));
+      CK(cudaEventRecord(xfer_ev[c], stream));
+    }
+    c = 0;
+    for (size_t a = 0; a < rows; a += per, ++c) {
+      const size_t b = std::min(rows, a + per);
+      CK(cudaEventSynchronize(xfer_ev[c]));
+      host_par_for(b - a, [&](size_t x, size_t y) {
+        for (size_t r = a + x; r < a + y; ++r) {
+          double *dst = view_row(v, nrow, r);
+          const T *src = host + r * nlon;
+          for (int i = 0; i < nlon; ++i) dst[i] = (double)src[i];
+        }
+      });
+    }
+  }
 
-  void get_field(int m, const std::string &name, double *dst) override {
+  void set_field(int m, const std::string &name, const gmc_view &src) override {
     FieldInfo f = info(name);
     R *pr;
     double *pd;
     locate(slots[m * 3 + old_i], m, name, &pr, &pd);
-    const size_t n = count(f);
-    if (pd) {
-      CK(cudaMemcpyAsync(dst, pd, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
-      CK(cudaStreamSynchronize(stream));
-    } else {
-      R *host = reinterpret_cast<R *>(pinned);
-      CK(cudaMemcpyAsync(host, pr, n * sizeof(R), cudaMemcpyDeviceToHost, stream));
-      CK(cudaStreamSynchronize(stream));
-      for (size_t t = 0; t < n; ++t) dst[t] = (double)host[t];
-    }
+    if (pd)
+      upload_view<double>(src, f.nrow, f.nk, pd);
+    else
+      upload_view<R>(src, f.nrow, f.nk, pr);
   }
 
-  void set_tracer(int m, int l, const double *src) override {
+  void get_field(int m, const std::string &name, const gmc_view &dst) override {
+    FieldInfo f = info(name);
+    R *pr;
+    double *pd;
+    locate(slots[m * 3 + old_i], m, name, &pr, &pd);
+    if (pd)
+      download_view<double>(pd, f.nrow, f.nk, dst);
+    else
+      download_view<R>(pr, f.nrow, f.nk, dst);
+  }
+
+  void set_tracer(int m, int l, const gmc_view &src) override {
     if (l < 0 || l >= ntr) throw ApiError{GMC_EINVAL, "tracer index out of range"};
-    R *host = reinterpret_cast<R *>(pinned);
-    const size_t n = full3();
-    for (size_t t = 0; t < n; ++t) host[t] = (R)src[t];
     // both time levels start from the initial mixing ratio
-    for (int sl = 0; sl < 2; ++sl)
-      CK(cudaMemcpyAsync(q[((size_t)m * 2 + sl) * ntr + l], host, n * sizeof(R), cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
+    R *second = q[((size_t)m * 2 + 1) * ntr + l];
+    upload_view<R>(src, grid.nlat, grid.nlev, q[((size_t)m * 2 + 0) * ntr + l], &second, 1);
   }
-  void get_tracer(int m, int l, double *dst) override {
+  void get_tracer(int m, int l, const gmc_view &dst) override {
     if (l < 0 || l >= ntr) throw ApiError{GMC_EINVAL, "tracer index out of range"};
-    R *host = reinterpret_cast<R *>(pinned);
-    const size_t n = full3();
-    CK(cudaMemcpyAsync(host, q[((size_t)m * 2 + q_old) * ntr + l], n * sizeof(R), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    for (size_t t = 0; t < n; ++t) dst[t] = (double)host[t];
+    download_view<R>(q[((size_t)m * 2 + q_old) * ntr + l], grid.nlat, grid.nlev, dst);
   }
 
   // Operator entry point: one horizontal FFSL flux with pool-allocated scratch.
@@ -1280,6 +1419,19 @@ gmc_config normalised(const gmc_config &c) {
 }
 
 // Copy the interior of a Fortran-bounded view into a packed [k][j][i] array.
+// The view must have non-empty bounds covering the interior 1..nlon x 1..nrow x 1..nk.
+bool check_view(const gmc_view *v, int nlon, int nrow, int nk, std::string &err) {
+  if (!v || !v->data) { err = "null view"; return false; }
+  for (int d = 0; d < 3; ++d)
+    if (v->ub[d] < v->lb[d]) { err = "view bounds are empty"; return false; }
+  if (v->lb[0] > 1 || v->ub[0] < nlon || v->lb[1] > 1 || v->ub[1] < nrow || v->lb[2] > 1 || v->ub[2] < nk) {
+    err = "view does not cover the interior (" + std::to_string(nlon) + "x" + std::to_string(nrow) + "x" +
+          std::to_string(nk) + ")";
+    return false;
+  }
+  return true;
+}
+
 bool unpack_view(const gmc_view *v, int nlon, int nrow, int nk, std::vector<double> &out, std::string &err) {
   if (!v || !v->data) { err = "null view"; return false; }
   for (int d = 0; d < 3; ++d)
@@ -1437,9 +1589,8 @@ int gmc_set_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view
     int nrow, nk;
     std::string n(name), err;
     field_dims(ctx->cfg, n, nrow, nk);
-    std::vector<double> buf;
-    if (!unpack_view(v, ctx->cfg.nlon, nrow, nk, buf, err)) throw ApiError{GMC_EINVAL, err};
-    ctx->eng->set_field(member, n, buf.data());
+    if (!check_view(v, ctx->cfg.nlon, nrow, nk, err)) throw ApiError{GMC_EINVAL, err};
+    ctx->eng->set_field(member, n, *v);
     return GMC_OK;
   });
 }
@@ -1451,9 +1602,8 @@ int gmc_set_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view 
   if (tracer < 0 || tracer >= ctx->cfg.ntracer) return fail(ctx, GMC_EINVAL, "tracer index out of range");
   return guarded(ctx, [&]() {
     std::string err;
-    std::vector<double> buf;
-    if (!unpack_view(v, ctx->cfg.nlon, ctx->cfg.nlat, ctx->cfg.nlev, buf, err)) throw ApiError{GMC_EINVAL, err};
-    ctx->eng->set_tracer(member, tracer, buf.data());
+    if (!check_view(v, ctx->cfg.nlon, ctx->cfg.nlat, ctx->cfg.nlev, err)) throw ApiError{GMC_EINVAL, err};
+    ctx->eng->set_tracer(member, tracer, *v);
     return GMC_OK;
   });
 }
@@ -1465,9 +1615,8 @@ int gmc_get_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view 
   if (tracer < 0 || tracer >= ctx->cfg.ntracer) return fail(ctx, GMC_EINVAL, "tracer index out of range");
   return guarded(ctx, [&]() {
     std::string err;
-    std::vector<double> buf((size_t)ctx->cfg.nlon * ctx->cfg.nlat * ctx->cfg.nlev);
-    ctx->eng->get_tracer(member, tracer, buf.data());
-    if (!pack_view(v, ctx->cfg.nlon, ctx->cfg.nlat, ctx->cfg.nlev, buf, err)) throw ApiError{GMC_EINVAL, err};
+    if (!check_view(v, ctx->cfg.nlon, ctx->cfg.nlat, ctx->cfg.nlev, err)) throw ApiError{GMC_EINVAL, err};
+    ctx->eng->get_tracer(member, tracer, *v);
     return GMC_OK;
   });
 }
@@ -1500,9 +1649,8 @@ int gmc_get_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view
     int nrow, nk;
     std::string n(name), err;
     field_dims(ctx->cfg, n, nrow, nk);
-    std::vector<double> buf((size_t)ctx->cfg.nlon * nrow * nk);
-    ctx->eng->get_field(member, n, buf.data());
-    if (!pack_view(v, ctx->cfg.nlon, nrow, nk, buf, err)) throw ApiError{GMC_EINVAL, err};
+    if (!check_view(v, ctx->cfg.nlon, nrow, nk, err)) throw ApiError{GMC_EINVAL, err};
+    ctx->eng->get_field(member, n, *v);
     return GMC_OK;
   });
 }
