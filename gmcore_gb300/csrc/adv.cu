@@ -23,35 +23,30 @@ namespace {
 // full-latitude rows without the poles, y fluxes on half-latitude rows.
 //   u, v  : advecting velocities (or mass fluxes for the outer operator)
 //   mx    : field reconstructed along x;  my : field reconstructed along y.
-// Along x a block takes one full row: the row is staged in shared memory and
-// the PPM slope, then the limited cell coefficients, are formed once per
-// cell; each face then reads its upwind cell.  Along y a block takes a strip
-// of kHflxRows half rows: each thread loads its column of the strip (plus
-// the stencil's rows) into registers and forms each slope once.  Pole halo
-// rows are read as the reference's fill_halo leaves them (mirrored row
+// Along x a block takes one full row: the row is staged in shared memory
+// (one barrier) and each face forms the PPM slope and limited coefficients
+// of its upwind cell from the five cells around it.  Along y a block takes a
+// strip of kHflxRows half rows: each thread loads its column of the strip
+// (plus the stencil's rows) into registers and forms each slope once.  Pole
+// halo rows are read as the reference's fill_halo leaves them (mirrored row
 // shifted by nlon/2).
-constexpr int kHflxRows = 8;
+constexpr int kHflxRows = 4;
 
 // x fluxes of full row j (2 .. nlat-1) at level k; out(i, o, flux) per face.
-// work: 5 * nlon values of shared memory.
+// xs: nlon values of shared memory.
 template <class R, class Out>
 __device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R *__restrict__ u,
-                                          const R *__restrict__ cflx, const R *__restrict__ mx, R *work, Out out) {
+                                          const R *__restrict__ cflx, const R *__restrict__ mx, R *xs, Out out) {
   const int nlat = g.nlat, nlon = g.nlon, lim = g.limiter;
-  R *xs = work;          // row values        [nlon]
-  R *ss = xs + nlon;     // slopes            [nlon]
-  R *cl = ss + nlon;     // limited fl        [nlon]
-  R *cd = cl + nlon;     // limited df        [nlon]
-  R *c6 = cd + nlon;     // f6                [nlon]
   auto W = [nlon](int l) { return l < 0 ? l + nlon : (l >= nlon ? l - nlon : l); };   // one wrap, 0-based
   auto Wg = [nlon](int l) {   // any l (a Courant number may exceed nlon on coarse grids)
     if (l >= 0 && l < nlon) return l;
     l %= nlon;
     return l < 0 ? l + nlon : l;
   };
-  // face inputs of this thread's first faces are requested before the
-  // shared-memory phases so that their latency overlaps them
-  constexpr int kPre = 4;
+  // face inputs of this thread's first faces are requested before the row is
+  // staged so that their latency overlaps it
+  constexpr int kPre = 3;
   R cpre[kPre], upre[kPre];
 #pragma unroll
   for (int t = 0; t < kPre; ++t) {
@@ -63,24 +58,17 @@ __device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R 
     }
   }
   const R *src = mx + ix3(nlat, nlon, 1, j, k);
-  __syncthreads();   // work may still be read by a previous use
+  __syncthreads();   // xs may still be read by a previous use
   for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[l] = src[l];
   __syncthreads();
-  for (int l = threadIdx.x; l < nlon; l += blockDim.x) ss[l] = slope(lim, xs[W(l - 1)], xs[l], xs[W(l + 1)]);
-  __syncthreads();
   const bool vl = g.flux_type == GMC_FLUX_VAN_LEER;
-  if (!vl) {
-    for (int l = threadIdx.x; l < nlon; l += blockDim.x) {
-      const int lm = W(l - 1), lp = W(l + 1);
-      const R f = xs[l], s0 = ss[l];
-      R fl, df, f6;
-      ppm_cell(f, s0, ppm_edge(xs[lm], f, ss[lm], s0), ppm_edge(f, xs[lp], s0, ss[lp]), fl, df, f6);
-      cl[l] = fl;
-      cd[l] = df;
-      c6[l] = f6;
-    }
-    __syncthreads();
-  }
+  // PPM coefficients of cell l (0-based) from cells l-2 .. l+2; the same
+  // operations as ppm() on the slopes of cells l-1, l, l+1
+  auto coef = [&](int l, R &fl, R &df, R &f6) {
+    const R a = xs[W(l - 2)], b = xs[W(l - 1)], c = xs[l], d = xs[W(l + 1)], e = xs[W(l + 2)];
+    const R sm = slope(lim, a, b, c), s0 = slope(lim, b, c, d), sp = slope(lim, c, d, e);
+    ppm_cell(c, s0, ppm_edge(b, c, sm, s0), ppm_edge(c, d, s0, sp), fl, df, f6);
+  };
   const R hxr = (R)g.hx;
   int t = 0;
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
@@ -105,18 +93,26 @@ __device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R 
         const int iu = Wg(i - ci - 1);   // 0-based upwind cell
         R sum = 0;
         for (int l = i + 1 - ci; l <= i; ++l) sum = sum + xs[Wg(l - 1)];
-        if (vl)   // hflx_van_leer_cell (ffsl_mod.F90:585-590)
-          flux = fdiv(uo * (cf * (xs[iu] + ss[iu] * (R)0.5 * ((R)1 - cf)) + sum), c);
-        else
-          flux = fdiv(uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)1 - cf, (R)1), c);
+        if (vl) {   // hflx_van_leer_cell (ffsl_mod.F90:585-590)
+          const R su = slope(lim, xs[W(iu - 1)], xs[iu], xs[W(iu + 1)]);
+          flux = fdiv(uo * (cf * (xs[iu] + su * (R)0.5 * ((R)1 - cf)) + sum), c);
+        } else {
+          R fl, df, f6;
+          coef(iu, fl, df, f6);
+          flux = fdiv(uo * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
+        }
       } else if (c < 0) {
         const int iu = Wg(i - ci);       // 0-based upwind cell (i - ci + 1 in 1-based)
         R sum = 0;
         for (int l = i + 1; l <= i - ci; ++l) sum = sum + xs[Wg(l - 1)];
-        if (vl)   // (ffsl_mod.F90:591-594)
-          flux = fdiv(uo * (cf * (xs[iu] - ss[iu] * (R)0.5 * ((R)1 + cf)) - sum), c);
-        else
-          flux = fdiv(-uo * ppm_tail(sum, cl[iu], cd[iu], c6[iu], (R)0, -cf), c);
+        if (vl) {   // (ffsl_mod.F90:591-594)
+          const R su = slope(lim, xs[W(iu - 1)], xs[iu], xs[W(iu + 1)]);
+          flux = fdiv(uo * (cf * (xs[iu] - su * (R)0.5 * ((R)1 + cf)) - sum), c);
+        } else {
+          R fl, df, f6;
+          coef(iu, fl, df, f6);
+          flux = fdiv(-uo * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
+        }
       } else {
         flux = 0;
       }
@@ -165,7 +161,7 @@ __device__ __forceinline__ R hflx_yface(const DGrid &g, R c, R vv, const R *y, c
 
 // Outer pass: fluxes fx of qy along x with the zonal mass flux (one row per block).
 template <class R>
-__global__ void k_hflx_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ mx,
+__global__ void GMC_BOUNDS(R, 8) k_hflx_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ mx,
                          R *__restrict__ fx) {
   extern __shared__ double sh_raw[];
   const int k = blockIdx.y + 1, j = blockIdx.x + 2;   // rows 2 .. nlat-1
@@ -174,7 +170,7 @@ __global__ void k_hflx_x(DGrid g, const R *__restrict__ u, const R *__restrict__
 
 // Outer pass: fluxes fy of qx along y with the meridional mass flux (strips).
 template <class R>
-__global__ void k_hflx_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ my,
+__global__ void GMC_BOUNDS(R, 6) k_hflx_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ my,
                          R *__restrict__ fy) {
   const int k = blockIdx.y + 1;
   const int nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
@@ -220,7 +216,7 @@ __global__ void k_hflx_y(DGrid g, const R *__restrict__ v, const R *__restrict__
 // (pole rows: qx = q, qy from the ring mean of the polar half row's flux).
 // x: one full row per block.
 template <class R>
-__global__ void k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ q,
+__global__ void GMC_BOUNDS(R, 8) k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ q,
                                const R *__restrict__ divx, R *__restrict__ qx, double dt) {
   extern __shared__ double sh_raw[];
   const int k = blockIdx.y + 1;
@@ -236,7 +232,7 @@ __global__ void k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__rest
       return;
     }
     R *work = reinterpret_cast<R *>(sh_raw);
-    R *frow = work + 5 * nlon;
+    R *frow = work + nlon;
     hflx_xrow<R>(g, j, k, u, cflx, q, work, [&](int i, size_t, R f) { frow[i - 1] = f; });
     __syncthreads();
     const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j);
@@ -244,7 +240,7 @@ __global__ void k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__rest
       const size_t o = ix3(nlat, nlon, i, j, k);
       const R qv = q[o];
       const R fxe = frow[i - 1], fxw = frow[i == 1 ? nlon - 1 : i - 2];
-      qx[o] = qv - (R)0.5 * ((fxe - fxw) * lel / ac - divx[o] * qv) * hdt;
+      qx[o] = qv - (R)0.5 * (fdiv((fxe - fxw) * lel, ac) - divx[o] * qv) * hdt;
     }
   }
 }
@@ -252,7 +248,7 @@ __global__ void k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__rest
 // y: strips whose faces start one half row below the strip, so that every
 // full row of the strip has both of its faces.
 template <class R>
-__global__ void __launch_bounds__(256, 4) k_ffsl_inner_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ q,
+__global__ void GMC_BOUNDS(R, 5) k_ffsl_inner_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ q,
                                const R *__restrict__ divy, R *__restrict__ qy, double dt) {
   __shared__ double red[32];
   const int k = blockIdx.y + 1;
@@ -291,14 +287,14 @@ __global__ void __launch_bounds__(256, 4) k_ffsl_inner_y(DGrid g, const R *__res
 #pragma unroll
     for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
     // faces in order; full row j0+f-1 is finished once face f (its north face) is known
-    R prev = 0;
+    R prev = 0, face_s = 0, face_n = 0;
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       R cur = 0;
       if (f >= fl0 && f < nfe) cur = hflx_yface(g, cy[f], vy[f], y, sl, f + 2);
       const int jf = j0 - 1 + f;   // half row of face f
-      if (has_s && jf == 1) ring_s += (double)cur;
-      if (has_n && jf == nhalf) ring_n += (double)cur;
+      if (jf == 1) face_s = cur;
+      if (jf == nhalf) face_n = cur;
       const int j = jf;            // full row whose north face is jf
       if (f >= 1 && j >= 2 && j <= nlat - 1 && f < nfe) {
         const size_t o = ix3(nlat, nlon, i + 1, j, k);
@@ -308,6 +304,10 @@ __global__ void __launch_bounds__(256, 4) k_ffsl_inner_y(DGrid g, const R *__res
       }
       prev = cur;
     }
+    // the polar faces' fluxes join the ring sums in FP64 only in the strips
+    // that hold them (one conversion per column there, none elsewhere)
+    if (has_s) ring_s += (double)face_s;
+    if (has_n) ring_n += (double)face_n;
   }
   // pole rows from the ring of their polar half row
   for (int side = 0; side < 2; ++side) {
@@ -325,41 +325,6 @@ __global__ void __launch_bounds__(256, 4) k_ffsl_inner_y(DGrid g, const R *__res
       else
         qy[o] = qv + (R)0.5 * (pole - divy[o] * qv) * hdt;
     }
-  }
-}
-
-// Intermediate advective-form values qx, qy (ffsl_mod.F90:353-406).
-template <class R>
-__global__ void k_qxqy(DGrid g, const R *q, const R *qmfx, const R *qmfy, const R *divx, const R *divy, R *qx, R *qy,
-                       double dt) {
-  __shared__ double red[32];
-  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
-  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
-  const R hdt = (R)dt;
-  if (j == 1 || j == nlat) {
-    const int jv = j == 1 ? 1 : nhalf;
-    double p = ring_sum(nlon, red, [&](int i) { return (double)qmfy[ix3(nhalf, nlon, i, jv, k)]; });
-    p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
-    const R pole = (R)p;
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      const size_t o = ix3(nlat, nlon, i, j, k);
-      const R qv = q[o];
-      qx[o] = qv;
-      if (j == 1)
-        qy[o] = qv - (R)0.5 * (pole - divy[o] * qv) * hdt;
-      else
-        qy[o] = qv + (R)0.5 * (pole - divy[o] * qv) * hdt;
-    }
-    return;
-  }
-  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
-  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-    const size_t o = ix3(nlat, nlon, i, j, k);
-    const R qv = q[o];
-    R fxe = qmfx[o], fxw = qmfx[ix3(nlat, nlon, wrap(i - 1, nlon), j, k)];
-    qx[o] = qv - (R)0.5 * ((fxe - fxw) * lel / ac - divx[o] * qv) * hdt;
-    R fyn = qmfy[ix3(nhalf, nlon, i, j, k)], fys = qmfy[ix3(nhalf, nlon, i, j - 1, k)];
-    qy[o] = qv - (R)0.5 * ((fyn * la0 - fys * la1) / ac - divy[o] * qv) * hdt;
   }
 }
 
@@ -582,7 +547,7 @@ __device__ R vflx_tile(const DGrid &g, const R *C, const R *FL, const R *DF, con
 // extrapolated ghost levels, slopes, limited cell coefficients and interface
 // fluxes are built in shared memory phase by phase, each phase parallel over
 // (column, level).
-__global__ void k_pt_tendency_f(DGrid g, Slot<float> s, Work<float> w) {
+__global__ void GMC_BOUNDS_F(8) k_pt_tendency_f(DGrid g, Slot<float> s, Work<float> w) {
   extern __shared__ double shd[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev, lim = g.limiter;
   const int j = blockIdx.y + 1;
@@ -731,11 +696,12 @@ __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, d
     const int st = blockDim.x;
     for (int k = 1; k <= nlev + 1; ++k) {
       size_t o = ix3(nlat, nlon, i, j, k);
-      col[(k - 1) * st] = we_in[o] / ml_in[o] * g.half_dlev_f[k - 1];
+      col[(k - 1) * st] = fdiv(we_in[o], ml_in[o]) * g.half_dlev_f[k - 1];
     }
     bool bad = false;
+    const float dtf = (float)dt;
     for (int k = 2; k <= nlev; ++k) {
-      float c = cflz_of_f(g, col, st, k, (float)dt, bad);
+      float c = cflz_of_f(g, col, st, k, dtf, bad);
       if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
     if (bad) atomicOr(g.err, ERR_CFLZ);
@@ -760,7 +726,7 @@ __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, d
 // it reads the longitude halo of q_new as the reference leaves it (the row's
 // values before this update, wrapped).
 template <class R>
-__global__ void k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *fx, const R *fy, SurfP<R> old_sp,
+__global__ void GMC_BOUNDS(R, 8) k_tracer_horizontal(DGrid g, const R *q_old, R *q_new, const R *fx, const R *fy, SurfP<R> old_sp,
                                     SurfP<R> sp, double dt_adv) {
   extern __shared__ double sh[];
   double *red = sh;
@@ -881,7 +847,7 @@ __global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const R *we, Sur
 // ghost levels, slopes, cell coefficients and interface fluxes in shared
 // memory, the update parallel over (column, level); the vertical fixer walks
 // a column in order and runs only in blocks that hold a negative value.
-__global__ void k_tracer_vertical_f(DGrid g, float *q, const float *cflz, const float *we, SurfP<float> sp,
+__global__ void GMC_BOUNDS_F(6) k_tracer_vertical_f(DGrid g, float *q, const float *cflz, const float *we, SurfP<float> sp,
                                     double dt_adv) {
   extern __shared__ float shf[];
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev, lim = g.limiter;
@@ -1012,7 +978,7 @@ void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, co
   (void)qmfx;
   (void)qmfy;
   const dim3 rows(g.nlat, g.nlev), inner_rows(g.nlat - 2, g.nlev), strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
-  const size_t smem_o = (size_t)5 * g.nlon * sizeof(R), smem_i = (size_t)6 * g.nlon * sizeof(R);
+  const size_t smem_o = (size_t)g.nlon * sizeof(R), smem_i = (size_t)2 * g.nlon * sizeof(R);
   if (smem_o > 48 * 1024) cudaFuncSetAttribute(k_hflx_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
   if (smem_i > 48 * 1024) cudaFuncSetAttribute(k_ffsl_inner_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i);
   k_ffsl_inner_x<R><<<rows, L.threads, smem_i, L.stream>>>(g, b.u, b.cflx, q, b.divx, qx, dt);

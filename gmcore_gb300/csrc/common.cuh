@@ -123,6 +123,15 @@ struct SurfP<float> {
   __device__ __forceinline__ float at(size_t o) const { return psr[o]; }
 };
 
+// Launch bounds of the row and column kernels (blocks of at most 256
+// threads). Their FP32 forms are bound by memory latency: each is capped at
+// the register count that keeps NB blocks resident per SM without spilling
+// (8 blocks = 2048 threads at 32 registers, 6 at 40, 4 at 64), which measured
+// faster than forms with fewer resident warps and more loads in flight per
+// thread. The FP64 forms are capped at 128 registers.
+#define GMC_BOUNDS(R, NB) __launch_bounds__(256, sizeof(R) == 4 ? NB : 2)
+#define GMC_BOUNDS_F(NB) __launch_bounds__(256, NB)
+
 __device__ __forceinline__ int wrap(int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); }
 
 // Offset of (i, j, k) in a [k][j][i] field; 32-bit arithmetic (grids are

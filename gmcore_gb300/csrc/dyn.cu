@@ -28,52 +28,59 @@ __device__ __forceinline__ MassField<R> mass_of(const DGrid &g, const Slot<R> &s
 // (interp_mod.F90:233-275).  Pole rows of mfx_lon stay zero.
 // ---------------------------------------------------------------------------
 template <class R>
-__global__ void k_mass_flux(DGrid g, Slot<R> s) {
+__device__ __forceinline__ LevMass<R> lev_mass(const DGrid &g, const Slot<R> &s, int k) {
+  return LevMass<R>(g, s.surf(), s.gz, s.gzs, k);
+}
+
+template <class R>
+__global__ void GMC_BOUNDS(R, 8) k_mass_flux(DGrid g, Slot<R> s) {
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
-  const MassField<R> M = mass_of(g, s);
-  if (j == 1 || j == g.nlat) {
-    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) s.mfx_lon[ix3(g.nlat, g.nlon, i, j, k)] = (R)0;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const LevMass<R> M = lev_mass(g, s, k);
+  const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k), ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+  const unsigned mo = (unsigned)(j - 1) * nlon;   // cell row j of the 2D mass field
+  if (j == 1 || j == nlat) {
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) s.mfx_lon[fo + i0] = (R)0;
   } else {
-    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
-      R m_lon = (M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * (R)0.5;
-      size_t o = ix3(g.nlat, g.nlon, i, j, k);
-      s.mfx_lon[o] = m_lon * s.u_f[o];
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+      const int ip = i0 + 1 == nlon ? 0 : i0 + 1;
+      s.mfx_lon[fo + i0] = (M.at(mo + i0) + M.at(mo + ip)) * (R)0.5 * s.u_f[fo + i0];
     }
   }
-  if (j <= g.nhalf) {
-    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
-      R m_lat = (M.at(g, i, j, k) + M.at(g, i, j + 1, k)) * (R)0.5;
-      size_t o = ix3(g.nhalf, g.nlon, i, j, k);
-      s.mfy_lat[o] = m_lat * s.v_f[o];
-    }
+  if (j <= nhalf) {
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x)
+      s.mfy_lat[ho + i0] = (M.at(mo + i0) + M.at(mo + nlon + i0)) * (R)0.5 * s.v_f[ho + i0];
   }
 }
 
 // Tangential mass fluxes and winds (operators_mod.F90:585-605).
 template <class R>
-__global__ void k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
+__global__ void GMC_BOUNDS(R, 8) k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
-  const MassField<R> M = mass_of(g, s);
-  if (j <= g.nhalf) {
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const LevMass<R> M = lev_mass(g, s, k);
+  const unsigned mo = (unsigned)(j - 1) * nlon;
+  if (j <= nhalf) {
     const R w1 = ROWR(R, htw1, j), w2 = ROWR(R, htw2, j);
-    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
-      const int im = wrap(i - 1, g.nlon);
-      R mfx_lat = w1 * (s.mfx_lon[ix3(g.nlat, g.nlon, im, j, k)] + s.mfx_lon[ix3(g.nlat, g.nlon, i, j, k)]) +
-                  w2 * (s.mfx_lon[ix3(g.nlat, g.nlon, im, j + 1, k)] + s.mfx_lon[ix3(g.nlat, g.nlon, i, j + 1, k)]);
-      R m_lat = (M.at(g, i, j, k) + M.at(g, i, j + 1, k)) * (R)0.5;
-      w.u_lat[ix3(g.nhalf, g.nlon, i, j, k)] = mfx_lat / m_lat;
+    const unsigned fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon, ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+      const int im = i0 == 0 ? nlon - 1 : i0 - 1;
+      R mfx_lat = w1 * (s.mfx_lon[fs + im] + s.mfx_lon[fs + i0]) + w2 * (s.mfx_lon[fn + im] + s.mfx_lon[fn + i0]);
+      R m_lat = (M.at(mo + i0) + M.at(mo + nlon + i0)) * (R)0.5;
+      w.u_lat[ho + i0] = fdiv(mfx_lat, m_lat);
     }
   }
-  if (j == 1 || j == g.nlat) {
-    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) w.v_lon[ix3(g.nlat, g.nlon, i, j, k)] = (R)0;
+  const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k);
+  if (j == 1 || j == nlat) {
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) w.v_lon[fo + i0] = (R)0;
   } else {
     const R w1 = ROWR(R, ftw1, j), w2 = ROWR(R, ftw2, j);
-    for (int i = 1 + threadIdx.x; i <= g.nlon; i += blockDim.x) {
-      const int ip = wrap(i + 1, g.nlon);
-      R mfy_lon = w1 * (s.mfy_lat[ix3(g.nhalf, g.nlon, i, j - 1, k)] + s.mfy_lat[ix3(g.nhalf, g.nlon, ip, j - 1, k)]) +
-                  w2 * (s.mfy_lat[ix3(g.nhalf, g.nlon, i, j, k)] + s.mfy_lat[ix3(g.nhalf, g.nlon, ip, j, k)]);
-      R m_lon = (M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * (R)0.5;
-      w.v_lon[ix3(g.nlat, g.nlon, i, j, k)] = mfy_lon / m_lon;
+    const unsigned hn = (unsigned)ix3(nhalf, nlon, 1, j, k), hs = hn - nlon;
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+      const int ip = i0 + 1 == nlon ? 0 : i0 + 1;
+      R mfy_lon = w1 * (s.mfy_lat[hs + i0] + s.mfy_lat[hs + ip]) + w2 * (s.mfy_lat[hn + i0] + s.mfy_lat[hn + ip]);
+      R m_lon = (M.at(mo + i0) + M.at(mo + ip)) * (R)0.5;
+      w.v_lon[fo + i0] = fdiv(mfy_lon, m_lon);
     }
   }
 }
@@ -81,7 +88,7 @@ __global__ void k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
 // calc_ke (operators_mod.F90:234-352): cell KE, optionally blended with the
 // four vertex KEs (ke_scheme 2); pole cells take the ring mean of v^2.
 template <class R>
-__global__ void k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
+__global__ void GMC_BOUNDS(R, 6) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const R *u = s.u_f, *v = s.v_f;
@@ -96,41 +103,42 @@ __global__ void k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) w.ke[ix3(nlat, nlon, i, j, k)] = (R)p;
     return;
   }
-  auto U = [&](int i, int jj) { return u[ix3(nlat, nlon, wrap(i, nlon), jj, k)]; };
-  auto V = [&](int i, int jj) { return v[ix3(nhalf, nlon, wrap(i, nlon), jj, k)]; };
   auto sq = [](R x) { return x * x; };
   const R alw = ROWR(R, area_lon_west, j), ale = ROWR(R, area_lon_east, j);
   const R aln = ROWR(R, area_lat_north, j - 1), als = ROWR(R, area_lat_south, j), ac = ROWR(R, area_cell, j);
-  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-    R ke = (alw * sq(U(i - 1, j)) + ale * sq(U(i, j)) + aln * sq(V(i, j - 1)) + als * sq(V(i, j))) / ac;
-    if (g.ke_scheme == 2) {
-      const R cw = (R)g.ke_cell_wgt;
-      R k1 = (ROWR(R, area_lat_east, j) * sq(V(i - 1, j)) + ROWR(R, area_lat_west, j) * sq(V(i, j)) +
-              ROWR(R, area_lon_north, j) * sq(U(i - 1, j)) + ROWR(R, area_lon_south, j + 1) * sq(U(i - 1, j + 1))) /
-             ROWR(R, area_vtx, j);
-      R k2 = (ROWR(R, area_lat_east, j - 1) * sq(V(i - 1, j - 1)) + ROWR(R, area_lat_west, j - 1) * sq(V(i, j - 1)) +
-              ROWR(R, area_lon_north, j - 1) * sq(U(i - 1, j - 1)) + ROWR(R, area_lon_south, j) * sq(U(i - 1, j))) /
-             ROWR(R, area_vtx, j - 1);
-      R k3 = (ROWR(R, area_lat_east, j - 1) * sq(V(i, j - 1)) + ROWR(R, area_lat_west, j - 1) * sq(V(i + 1, j - 1)) +
-              ROWR(R, area_lon_north, j - 1) * sq(U(i, j - 1)) + ROWR(R, area_lon_south, j) * sq(U(i, j))) /
-             ROWR(R, area_vtx, j - 1);
-      R k4 = (ROWR(R, area_lat_east, j) * sq(V(i, j)) + ROWR(R, area_lat_west, j) * sq(V(i + 1, j)) +
-              ROWR(R, area_lon_north, j) * sq(U(i, j)) + ROWR(R, area_lon_south, j + 1) * sq(U(i, j + 1))) /
-             ROWR(R, area_vtx, j);
-      ke = ((R)1 - cw) * ((k1 + k4) * ROWR(R, area_subcell2, j) + (k2 + k3) * ROWR(R, area_subcell1, j)) / ac + cw * ke;
+  // row offsets at level k: u on full rows j-1, j, j+1; v on half rows j-1, j
+  const unsigned uc = (unsigned)ix3(nlat, nlon, 1, j, k), us = uc - nlon, un = uc + nlon;
+  const unsigned vc = (unsigned)ix3(nhalf, nlon, 1, j, k), vs = vc - nlon;
+  const bool vtx = g.ke_scheme == 2;
+  const R cw = (R)g.ke_cell_wgt;
+  const R ate = ROWR(R, area_lat_east, j), atw = ROWR(R, area_lat_west, j), ate1 = ROWR(R, area_lat_east, j - 1),
+          atw1 = ROWR(R, area_lat_west, j - 1);
+  const R aon = ROWR(R, area_lon_north, j), aon1 = ROWR(R, area_lon_north, j - 1), aos = ROWR(R, area_lon_south, j),
+          aosn = ROWR(R, area_lon_south, j + 1);
+  const R av = ROWR(R, area_vtx, j), av1 = ROWR(R, area_vtx, j - 1), as2 = ROWR(R, area_subcell2, j),
+          as1 = ROWR(R, area_subcell1, j);
+  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+    const int im = i0 == 0 ? nlon - 1 : i0 - 1, ip = i0 + 1 == nlon ? 0 : i0 + 1;
+    const R uw = u[uc + im], ue = u[uc + i0], vsc = v[vs + i0], vnc = v[vc + i0];
+    R ke = fdiv(alw * sq(uw) + ale * sq(ue) + aln * sq(vsc) + als * sq(vnc), ac);
+    if (vtx) {
+      const R k1 = fdiv(ate * sq(v[vc + im]) + atw * sq(vnc) + aon * sq(uw) + aosn * sq(u[un + im]), av);
+      const R k2 = fdiv(ate1 * sq(v[vs + im]) + atw1 * sq(vsc) + aon1 * sq(u[us + im]) + aos * sq(uw), av1);
+      const R k3 = fdiv(ate1 * sq(vsc) + atw1 * sq(v[vs + ip]) + aon1 * sq(u[us + i0]) + aos * sq(ue), av1);
+      const R k4 = fdiv(ate * sq(vnc) + atw * sq(v[vc + ip]) + aon * sq(ue) + aosn * sq(u[un + i0]), av);
+      ke = fdiv(((R)1 - cw) * ((k1 + k4) * as2 + (k2 + k3) * as1), ac) + cw * ke;
     }
-    w.ke[ix3(nlat, nlon, i, j, k)] = ke;
+    w.ke[uc + i0] = ke;
   }
 }
 
 // calc_vor + calc_pv (operators_mod.F90:612-703) with the vertex mass of
 // interp_cell_to_vtx (interp_mod.F90:438-463).
 template <class R>
-__global__ void k_pv(DGrid g, Slot<R> s, Work<R> w) {
+__global__ void GMC_BOUNDS(R, 6) k_pv(DGrid g, Slot<R> s, Work<R> w) {
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
-  const MassField<R> M = mass_of(g, s);
   const bool pole = g.pv_pole_stokes && (j == 1 || j == nhalf);
   double pole_vor = 0;
   if (pole) {
@@ -141,86 +149,98 @@ __global__ void k_pv(DGrid g, Slot<R> s, Work<R> w) {
   }
   const R dl0 = ROWR(R, de_lon, j), dl1 = ROWR(R, de_lon, j + 1), dt = ROWR(R, de_lat, j), av = ROWR(R, area_vtx, j);
   const R as2 = ROWR(R, area_subcell2, j), as1 = ROWR(R, area_subcell1, j + 1), f = ROWR(R, half_f, j);
-  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-    const int ip = wrap(i + 1, nlon);
+  const LevMass<R> LM = lev_mass(g, s, k);
+  const unsigned us = (unsigned)ix3(nlat, nlon, 1, j, k), un = us + nlon, ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+  const unsigned ms = (unsigned)(j - 1) * nlon, mn = ms + nlon;
+  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+    const int ip = i0 + 1 == nlon ? 0 : i0 + 1;
     R vor;
     if (pole) {
       vor = (R)pole_vor;
     } else {
-      vor = (s.u_f[ix3(nlat, nlon, i, j, k)] * dl0 - s.u_f[ix3(nlat, nlon, i, j + 1, k)] * dl1 +
-             s.v_f[ix3(nhalf, nlon, ip, j, k)] * dt - s.v_f[ix3(nhalf, nlon, i, j, k)] * dt) / av;
+      vor = fdiv(s.u_f[us + i0] * dl0 - s.u_f[un + i0] * dl1 + s.v_f[ho + ip] * dt - s.v_f[ho + i0] * dt, av);
     }
-    R m_vtx = ((M.at(g, i, j, k) + M.at(g, i + 1, j, k)) * as2 + (M.at(g, i, j + 1, k) + M.at(g, i + 1, j + 1, k)) * as1) / av;
-    s.pv[ix3(nhalf, nlon, i, j, k)] = (vor + f) / m_vtx;
+    R m_vtx = fdiv((LM.at(ms + i0) + LM.at(ms + ip)) * as2 + (LM.at(mn + i0) + LM.at(mn + ip)) * as1, av);
+    s.pv[ho + i0] = fdiv(vor + f, m_vtx);
   }
 }
 
 
-// interp_pv_midpoint / interp_pv_upwind (operators_mod.F90:705-795).
+// interp_pv_midpoint / interp_pv_upwind (operators_mod.F90:705-795).  The
+// half rows of pv a block reads are resolved once per block (row offset and
+// the longitude shift of the rows mirrored beyond the poles, as rd_half reads
+// them), so the per-point work is the interpolation itself.
+struct PvRow {
+  unsigned off;   // offset of the half row at the block's level
+  int sh;         // longitude shift (nlon/2 beyond the poles, else 0)
+};
+__device__ __forceinline__ PvRow pv_row(const DGrid &g, int jj, int k) {
+  int sh = 0;
+  if (jj < 1) { jj = 1 - jj; sh = g.half; }
+  else if (jj > g.nhalf) { jj = 2 * g.nhalf + 1 - jj; sh = g.half; }
+  return {(unsigned)ix3(g.nhalf, g.nlon, 1, jj, k), sh};
+}
+
 template <class R>
-__global__ void k_pv_edges(DGrid g, Slot<R> s, Work<R> w, double dt) {
+__global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, double dt) {
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const R eps = (R)2.220446049250313e-16;
   const R wgt = (R)g.upwind_wgt_pv;
-  const R *pv = s.pv;
-  auto P = [&](int i, int jj) { return rd_half(pv, g, i, jj, k); };
-  if (g.pv_scheme == GMC_PV_TVD) {   // interp_pv_tvd (operators_mod.F90:797-832)
-    if (j != 1 && j != nlat) {
-      const R le = ROWR(R, le_lon, j);
-      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-        const size_t o = ix3(nlat, nlon, i, j, k);
-        const R cfl = w.v_lon[o] * (R)dt / le;
-        s.pv_lon[o] = tvd_interp<R>(g.tvd_limiter, cfl, P(i, j - 2), P(i, j - 1), P(i, j), P(i, j + 1));
-      }
-    } else {
-      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) s.pv_lon[ix3(nlat, nlon, i, j, k)] = (R)0;
-    }
-    if (j <= nhalf) {
-      const R le = ROWR(R, le_lat, j);
-      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-        const size_t o = ix3(nhalf, nlon, i, j, k);
-        const R cfl = w.u_lat[o] * (R)dt / le;
-        s.pv_lat[o] = tvd_interp<R>(g.tvd_limiter, cfl, P(i - 2, j), P(i - 1, j), P(i, j), P(i + 1, j));
-      }
-    }
-    return;
-  }
+  const R *__restrict__ pv = s.pv;
+  const bool tvd = g.pv_scheme == GMC_PV_TVD, mid_only = g.pv_scheme == GMC_PV_MIDPOINT, up3 = g.upwind_order_pv == 3;
+  // pv at 0-based longitude l (l + shift in [-nlon, 2 nlon)) of a resolved row
+  auto P = [&](const PvRow &r, int l) {
+    l += r.sh;
+    l = l < 0 ? l + nlon : (l >= nlon ? l - nlon : l);
+    return pv[r.off + l];
+  };
+  // pv_lon on full row j: pv of half rows j-2 .. j+1 at the same longitude
   if (j == 1 || j == nlat) {
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) s.pv_lon[ix3(nlat, nlon, i, j, k)] = (R)0;
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) s.pv_lon[ix3(nlat, nlon, i0 + 1, j, k)] = (R)0;
   } else {
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      size_t o = ix3(nlat, nlon, i, j, k);
-      R mid = P(i, j - 1) + P(i, j);
+    const PvRow r0 = pv_row(g, j - 2, k), r1 = pv_row(g, j - 1, k), r2 = pv_row(g, j, k), r3 = pv_row(g, j + 1, k);
+    const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k);
+    const R le = ROWR(R, le_lon, j);
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
       R val;
-      if (g.pv_scheme == GMC_PV_MIDPOINT) {
-        val = (R)0.5 * (P(i, j) + P(i, j - 1));
+      if (tvd) {   // interp_pv_tvd (operators_mod.F90:797-832)
+        const R cfl = w.v_lon[fo + i0] * (R)dt / le;
+        val = tvd_interp<R>(g.tvd_limiter, cfl, P(r0, i0), P(r1, i0), P(r2, i0), P(r3, i0));
+      } else if (mid_only) {
+        val = (R)0.5 * (P(r2, i0) + P(r1, i0));
       } else {
-        R un = s.u_f[o], vt = w.v_lon[o];
-        R b = fdiv(fabs(vt), sqrt(un * un + vt * vt) + eps);
-        R dir = fsign((R)1, vt);
-        R up = g.upwind_order_pv == 3 ? upwind3(dir, wgt, P(i, j - 2), P(i, j - 1), P(i, j), P(i, j + 1))
-                                      : upwind1(dir, wgt, P(i, j - 1), P(i, j));
-        val = b * up + ((R)1 - b) * (R)0.5 * mid;
+        const R pm = P(r1, i0), pc = P(r2, i0);
+        const R un = s.u_f[fo + i0], vt = w.v_lon[fo + i0];
+        const R bb = fdiv(fabs(vt), sqrt(un * un + vt * vt) + eps);
+        const R dir = fsign((R)1, vt);
+        const R up = up3 ? upwind3(dir, wgt, P(r0, i0), pm, pc, P(r3, i0)) : upwind1(dir, wgt, pm, pc);
+        val = bb * up + ((R)1 - bb) * (R)0.5 * (pm + pc);
       }
-      s.pv_lon[o] = val;
+      s.pv_lon[fo + i0] = val;
     }
   }
+  // pv_lat on half row j: pv of the same row at longitudes i-2 .. i+1
   if (j <= nhalf) {
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      size_t o = ix3(nhalf, nlon, i, j, k);
+    const PvRow r = pv_row(g, j, k);
+    const unsigned ho = r.off;
+    const R le = ROWR(R, le_lat, j);
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
       R val;
-      if (g.pv_scheme == GMC_PV_MIDPOINT) {
-        val = (R)0.5 * (P(i - 1, j) + P(i, j));
+      const R pm = P(r, i0 - 1), pc = pv[ho + i0];
+      if (tvd) {
+        const R cfl = w.u_lat[ho + i0] * (R)dt / le;
+        val = tvd_interp<R>(g.tvd_limiter, cfl, P(r, i0 - 2), pm, pc, P(r, i0 + 1));
+      } else if (mid_only) {
+        val = (R)0.5 * (pm + pc);
       } else {
-        R ut = w.u_lat[o], vn = s.v_f[o];
-        R b = fdiv(fabs(ut), sqrt(ut * ut + vn * vn) + eps);
-        R dir = fsign((R)1, ut);
-        R up = g.upwind_order_pv == 3 ? upwind3(dir, wgt, P(i - 2, j), P(i - 1, j), P(i, j), P(i + 1, j))
-                                      : upwind1(dir, wgt, P(i - 1, j), P(i, j));
-        val = b * up + ((R)1 - b) * (R)0.5 * (P(i - 1, j) + P(i, j));
+        const R ut = w.u_lat[ho + i0], vn = s.v_f[ho + i0];
+        const R bb = fdiv(fabs(ut), sqrt(ut * ut + vn * vn) + eps);
+        const R dir = fsign((R)1, ut);
+        const R up = up3 ? upwind3(dir, wgt, P(r, i0 - 2), pm, pc, P(r, i0 + 1)) : upwind1(dir, wgt, pm, pc);
+        val = bb * up + ((R)1 - bb) * (R)0.5 * (pm + pc);
       }
-      s.pv_lat[o] = val;
+      s.pv_lat[ho + i0] = val;
     }
   }
 }
@@ -253,6 +273,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
     const float cdx = (float)dt_ / ROWR(float, de_lon, j);
     const float lel = ROWR(float, le_lon, j), ac = ROWR(float, area_cell, j);
     const float la0 = ROWR(float, le_lat, j), la1 = ROWR(float, le_lat, j - 1);
+    const float hx = (float)g.hx;
     const float *urow = u + ix3(nlat, nlon, 1, j, k);
     for (int l = threadIdx.x; l < nlon; l += blockDim.x) us[l] = urow[l];
     __syncthreads();
@@ -275,12 +296,12 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       const float u2 = at(0.5f * cdx * u1);
       const float u3 = at(0.5f * cdx * u2);
       const float u4 = at(cdx * u3);
-      const float c = (u1 + 2.0f * u2 + 2.0f * u3 + u4) / 6.0f * cdx;
-      if (!(fabsf(c) <= (float)g.hx)) atomicOr(g.err, ERR_CFLX);
+      const float c = div6(u1 + 2.0f * u2 + 2.0f * u3 + u4) * cdx;
+      if (!(fabsf(c) <= hx)) atomicOr(g.err, ERR_CFLX);
       size_t o = ix3(nlat, nlon, i, j, k);
       cflx[o] = c;
-      divx[o] = (u1 - Ul(i - 1)) * lel / ac;
-      divy[o] = (v[ix3(nhalf, nlon, i, j, k)] * la0 - v[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
+      divx[o] = fdiv((u1 - Ul(i - 1)) * lel, ac);
+      divy[o] = fdiv(v[ix3(nhalf, nlon, i, j, k)] * la0 - v[ix3(nhalf, nlon, i, j - 1, k)] * la1, ac);
     }
   } else {
     const double dx = ROW(g.de_lon, j), cl = ROW(g.full_cos_lat, j);
@@ -328,7 +349,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
         const float v2 = at(0.5f * cdy * v1);
         const float v3 = at(0.5f * cdy * v2);
         const float v4 = at(cdy * v3);
-        const float c = (v1 + 2.0f * v2 + 2.0f * v3 + v4) / 6.0f * cdy;
+        const float c = div6(v1 + 2.0f * v2 + 2.0f * v3 + v4) * cdy;
         if (!(fabsf(c) <= 1.0f)) atomicOr(g.err, ERR_CFLY);
         cfly[ix3(nhalf, nlon, i, j, k)] = c;
       }
@@ -415,14 +436,15 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
       const float m_lo = Mass<float>::layer(g, k, psr);
       const float ml = 0.5f * (m_up + m_lo);   // half-level mass
       p_prev = col[(k - 1) * st];
-      col[(k - 1) * st] = wv / ml * g.half_dlev_f[k - 1];
+      col[(k - 1) * st] = fdiv(wv, ml) * g.half_dlev_f[k - 1];
       m_up = m_lo;
     }
     col[nlev * st] = 0;   // wm(nlev+1): we = 0
     s.we_lev[ix3(nlat, nlon, i, j, nlev + 1)] = 0;
     bool bad = false;
+    const float dtf = (float)dt;
     for (int k = 2; k <= nlev; ++k) {
-      float c = cflz_of_f(g, col, st, k, (float)dt, bad);
+      float c = cflz_of_f(g, col, st, k, dtf, bad);
       if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
     if (bad) atomicOr(g.err, ERR_CFLZ);
@@ -476,7 +498,7 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
 // FP32 form of k_column_mass over column tiles: layer divergences, their
 // prefix sums along the column (warp scans), we_lev, dphs and the vertical
 // Courant numbers, each phase parallel over (column, level).
-__global__ void k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, double dt) {
+__global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, double dt) {
   extern __shared__ double shd[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
   const int j = blockIdx.y + 1;
@@ -529,7 +551,7 @@ __global__ void k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, double dt
     if (k != 1 && k != nlev + 1) {
       wv = -(g.hybi_f[k - 1] * dphs) - P[(k - 2) * ld + ti];
       const float ml = 0.5f * (Mass<float>::layer(g, k - 1, psr) + Mass<float>::layer(g, k, psr));
-      wm = wv / ml * g.half_dlev_f[k - 1];
+      wm = fdiv(wv, ml) * g.half_dlev_f[k - 1];
     }
     if (valid) s.we_lev[ix3(nlat, nlon, i, j, k)] = wv;
     WM[(k - 1) * ld + ti] = wm;
@@ -537,8 +559,9 @@ __global__ void k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, double dt
   __syncthreads();
   if (!valid) return;
   bool bad = false;
+  const float dtf = (float)dt;
   for (int k = 2 + kt; k <= nlev; k += KT) {
-    float c = cflz_of_f(g, WM + ti, ld, k, (float)dt, bad);
+    float c = cflz_of_f(g, WM + ti, ld, k, dtf, bad);
     if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
   }
   if (bad) atomicOr(g.err, ERR_CFLZ);
@@ -625,6 +648,70 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
         dv = dv - wd;
       }
       w.dv[o] = dv;
+    }
+  }
+}
+
+// FP32 form of k_momentum_tend (baroclinic): the same terms with the arrays
+// passed as non-aliasing kernel arguments addressed by 32-bit row offsets (the
+// base pointers stay in the parameter bank, so the kernel fits in 32
+// registers) and the divisions taken as reciprocal products (fdiv).
+__global__ void GMC_BOUNDS_F(8) k_momentum_f(DGrid g, const float *__restrict__ mfx, const float *__restrict__ mfy,
+                                             const float *__restrict__ pvlon, const float *__restrict__ pvlat,
+                                             const float *__restrict__ ke, const float *__restrict__ we,
+                                             const float *__restrict__ uf, const float *__restrict__ vf,
+                                             const float *__restrict__ psr, float *__restrict__ du,
+                                             float *__restrict__ dv) {
+  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
+  const bool cor1 = g.coriolis_scheme == 1;
+  const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
+  const unsigned lf = (unsigned)nlat * nlon, lh = (unsigned)nhalf * nlon;   // level strides
+  if (j != 1 && j != nlat) {
+    const float t1 = ROWR(float, ftw1, j), t2 = ROWR(float, ftw2, j), de = ROWR(float, de_lon, j);
+    const float aw = ROWR(float, area_lon_west, j), ae = ROWR(float, area_lon_east, j), al = ROWR(float, area_lon, j);
+    const unsigned hs = (unsigned)ix3(nhalf, nlon, 1, j - 1, k), hn = hs + nlon;   // half rows j-1, j
+    const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k), po = (unsigned)(j - 1) * nlon;
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+      const int ip = i0 + 1 == nlon ? 0 : i0 + 1;
+      const float pl = pvlon[fo + i0];
+      float qhv;
+      if (cor1)
+        qhv = (t1 * (mfy[hs + i0] * (pl + pvlat[hs + i0]) + mfy[hs + ip] * (pl + pvlat[hs + ip])) +
+               t2 * (mfy[hn + i0] * (pl + pvlat[hn + i0]) + mfy[hn + ip] * (pl + pvlat[hn + ip]))) * 0.5f;
+      else
+        qhv = (t1 * (mfy[hs + i0] + mfy[hs + ip]) + t2 * (mfy[hn + i0] + mfy[hn + ip])) * pl;
+      const float d = qhv - fdiv(ke[fo + ip] - ke[fo + i0], de);
+      const float m_lon = (fmaf(dB, psr[po + i0], dA) + fmaf(dB, psr[po + ip], dA)) * 0.5f;
+      const float u0 = uf[fo + i0];
+      float wd = 0;
+      if (k < nlev) wd = fdiv(aw * we[fo + lf + i0] + ae * we[fo + lf + ip], al) * (uf[fo + lf + i0] - u0);
+      if (k > 1) wd += fdiv(aw * we[fo + i0] + ae * we[fo + ip], al) * (u0 - uf[fo - lf + i0]);
+      du[fo + i0] = d - fdiv(wd, m_lon) * 0.5f;
+    }
+  }
+  if (j > nhalf) return;
+  {
+    const float t1 = ROWR(float, htw1, j), t2 = ROWR(float, htw2, j), de = ROWR(float, de_lat, j);
+    const float an = ROWR(float, area_lat_north, j), as = ROWR(float, area_lat_south, j), al = ROWR(float, area_lat, j);
+    const unsigned fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon;   // full rows j, j+1
+    const unsigned ho = (unsigned)ix3(nhalf, nlon, 1, j, k), ps = (unsigned)(j - 1) * nlon, pn = ps + nlon;
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+      const int im = i0 == 0 ? nlon - 1 : i0 - 1;
+      const float pl = pvlat[ho + i0];
+      float qhu;
+      if (cor1)
+        qhu = (t1 * (mfx[fs + im] * (pl + pvlon[fs + im]) + mfx[fs + i0] * (pl + pvlon[fs + i0])) +
+               t2 * (mfx[fn + im] * (pl + pvlon[fn + im]) + mfx[fn + i0] * (pl + pvlon[fn + i0]))) * 0.5f;
+      else
+        qhu = (t1 * (mfx[fs + im] + mfx[fs + i0]) + t2 * (mfx[fn + im] + mfx[fn + i0])) * pl;
+      const float d = -qhu - fdiv(ke[fn + i0] - ke[fs + i0], de);
+      const float m_lat = (fmaf(dB, psr[ps + i0], dA) + fmaf(dB, psr[pn + i0], dA)) * 0.5f;
+      const float v0 = vf[ho + i0];
+      float wd = 0;
+      if (k < nlev) wd = fdiv(an * we[fn + lf + i0] + as * we[fs + lf + i0], al) * (vf[ho + lh + i0] - v0);
+      if (k > 1) wd += fdiv(an * we[fn + i0] + as * we[fs + i0], al) * (v0 - vf[ho - lh + i0]);
+      dv[ho + i0] = d - fdiv(wd, m_lat) * 0.5f;
     }
   }
 }
@@ -831,7 +918,7 @@ __device__ __forceinline__ R pgf_lon(const DGrid &g, const Slot<R> &n, const Wor
       float dph2 = dref + (pa[ix3(nlat, nlon, i, j, k + 1)] - pa[ix3(nlat, nlon, ip, j, k)]);
       float dgz1 = hl_diff(gz[ix3(nlat, nlon, i, j, k + 1)], gz[ix3(nlat, nlon, ip, j, k)]);
       float dgz2 = hl_diff(gz[ix3(nlat, nlon, i, j, k)], gz[ix3(nlat, nlon, ip, j, k + 1)]);
-      return -(dph1 * dgz1 + dph2 * dgz2) * inv_d / (dph1 + dph2);
+      return fdiv(-(dph1 * dgz1 + dph2 * dgz2) * inv_d, dph1 + dph2);
     }
     const double *pe = w.ph_exn_lev, *gz = w.gz_lev;
     double dph1 = pe[ix3(nlat, nlon, ip, j, k + 1)] - pe[ix3(nlat, nlon, i, j, k)];
@@ -854,7 +941,7 @@ __device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Wor
       float dph2 = dref + (pa[ix3(nlat, nlon, i, j, k + 1)] - pa[ix3(nlat, nlon, i, j + 1, k)]);
       float dgz1 = hl_diff(gz[ix3(nlat, nlon, i, j, k + 1)], gz[ix3(nlat, nlon, i, j + 1, k)]);
       float dgz2 = hl_diff(gz[ix3(nlat, nlon, i, j, k)], gz[ix3(nlat, nlon, i, j + 1, k + 1)]);
-      return -(dph1 * dgz1 + dph2 * dgz2) * inv_d / (dph1 + dph2);
+      return fdiv(-(dph1 * dgz1 + dph2 * dgz2) * inv_d, dph1 + dph2);
     }
     const double *pe = w.ph_exn_lev, *gz = w.gz_lev;
     double dph1 = pe[ix3(nlat, nlon, i, j + 1, k + 1)] - pe[ix3(nlat, nlon, i, j, k)];
@@ -866,55 +953,109 @@ __device__ __forceinline__ R pgf_lat(const DGrid &g, const Slot<R> &n, const Wor
   return (n.gz_f[ix3(nlat, nlon, i, j + 1, 1)] - n.gz_f[ix3(nlat, nlon, i, j, 1)]) / ROWR(R, de_lat, j);
 }
 
+// FP32 Lin97 pressure-gradient force at the edge between cells p (west or
+// south) and q (east or north), offsets at level k; level k+1 is lf further.
+// The same operations as the FP32 branch of pgf_lon / pgf_lat.
+__device__ __forceinline__ float pgf_pq(const float *__restrict__ pa, const float2 *__restrict__ gz, unsigned p, unsigned q,
+                                        unsigned lf, float dref, float inv_d) {
+  const float dph1 = dref + (pa[q + lf] - pa[p]);
+  const float dph2 = dref + (pa[p + lf] - pa[q]);
+  const float dgz1 = hl_diff(gz[p + lf], gz[q]);
+  const float dgz2 = hl_diff(gz[p], gz[q + lf]);
+  return fdiv(-(dph1 * dgz1 + dph2 * dgz2) * inv_d, dph1 + dph2);
+}
+
+__device__ __forceinline__ bool filter_on(const FilterDev &f, bool full_lat, int j) {
+  return (full_lat ? f.ntaps_full[j - 1] : f.ntaps_half[j - 1]) > 1;
+}
+
+// Each row is staged in shared memory (also where no filter touches it: the
+// stores then do not order the next points' loads behind them).
 template <class R>
-__global__ void k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+__global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
   extern __shared__ double sh[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const int k = blockIdx.y + 1;
+  const bool bc = g.baroclinic;
+  const unsigned lf = (unsigned)nlat * nlon;   // level stride of the half-level pea / gzhl
+  float dref = 0;
+  if constexpr (std::is_same<R, float>::value) dref = bc ? g.dpe_ref[k - 1] : 0.0f;
   R *row = reinterpret_cast<R *>(sh), *nb = row + nlon, *ext = nb + nlon;
   if ((int)blockIdx.x < nlat) {
     const int j = blockIdx.x + 1;
+    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
     if (j == 1 || j == nlat) {   // pole rows are not updated; the big filter copies them
-      for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-        size_t c = ix3(nlat, nlon, i + 1, j, k);
-        n.u_f[c] = n.u_lon[c];
-      }
+      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_f[c0 + i0] = n.u_lon[c0 + i0];
       return;
     }
     const R inv_d = (R)1 / ROWR(R, de_lon, j);
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-      size_t c = ix3(nlat, nlon, i + 1, j, k);
-      row[i] = o.u_lon[c] + (R)dt * (w.du[c] - pgf_lon(g, n, w, i + 1, j, k, inv_d));
-    }
-    if (g.baroclinic) filter_row<R, R>(g.small2, true, j, nlon, row, ext);
+    auto val = [&](int i0) {
+      R p;
+      if constexpr (std::is_same<R, float>::value) {
+        if (bc) p = pgf_pq(w.pea, w.gzhl, c0 + i0, c0 + (i0 + 1 == nlon ? 0 : i0 + 1), lf, dref, inv_d);
+        else p = pgf_lon(g, n, w, i0 + 1, j, k, inv_d);
+      } else {
+        p = pgf_lon(g, n, w, i0 + 1, j, k, inv_d);
+      }
+      return o.u_lon[c0 + i0] + (R)dt * (w.du[c0 + i0] - p);
+    };
+    const bool small = bc && filter_on(g.small2, true, j), big = filter_on(g.big, true, j);
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[i0] = val(i0);
+    if (small) filter_row<R, R>(g.small2, true, j, nlon, row, ext);
     __syncthreads();
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_lon[ix3(nlat, nlon, i + 1, j, k)] = row[i];
+    if (!big) {
+      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+        const R v = row[i0];
+        n.u_lon[c0 + i0] = v;
+        n.u_f[c0 + i0] = v;
+      }
+      return;
+    }
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_lon[c0 + i0] = row[i0];
     filter_row<R, R>(g.big, true, j, nlon, row, ext);
     __syncthreads();
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_f[ix3(nlat, nlon, i + 1, j, k)] = row[i];
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_f[c0 + i0] = row[i0];
     return;
   }
   const int j = blockIdx.x - nlat + 1;
+  auto vval = [&](int jj, R inv_d, int i0) {
+    const unsigned cv = (unsigned)ix3(nhalf, nlon, 1, jj, k);
+    R p;
+    if constexpr (std::is_same<R, float>::value) {
+      const unsigned ps = (unsigned)ix3(nlat, nlon, 1, jj, k);
+      if (bc) p = pgf_pq(w.pea, w.gzhl, ps + i0, ps + nlon + i0, lf, dref, inv_d);
+      else p = pgf_lat(g, n, w, i0 + 1, jj, k, inv_d);
+    } else {
+      p = pgf_lat(g, n, w, i0 + 1, jj, k, inv_d);
+    }
+    return o.v_lat[cv + i0] + (R)dt * (w.dv[cv + i0] - p);
+  };
+  const unsigned cj = (unsigned)ix3(nhalf, nlon, 1, j, k);
   auto load_v = [&](int jj, R *dst) {
     const R inv_d = (R)1 / ROWR(R, de_lat, jj);
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-      size_t c = ix3(nhalf, nlon, i + 1, jj, k);
-      dst[i] = o.v_lat[c] + (R)dt * (w.dv[c] - pgf_lat(g, n, w, i + 1, jj, k, inv_d));
-    }
-    if (g.baroclinic) filter_row<R, R>(g.small2, false, jj, nlon, dst, ext);
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) dst[i0] = vval(jj, inv_d, i0);
+    if (bc) filter_row<R, R>(g.small2, false, jj, nlon, dst, ext);
     __syncthreads();
   };
   load_v(j, row);
   if (j == 1 || j == nhalf) {
     load_v(j == 1 ? 2 : nhalf - 1, nb);
     const R wgt = (R)0.6;
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) row[i] = ((R)1 - wgt) * row[i] + wgt * nb[i];
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[i0] = ((R)1 - wgt) * row[i0] + wgt * nb[i0];
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_lat[ix3(nhalf, nlon, i + 1, j, k)] = row[i];
+  if (!filter_on(g.big, false, j)) {
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+      const R v = row[i0];
+      n.v_lat[cj + i0] = v;
+      n.v_f[cj + i0] = v;
+    }
+    return;
+  }
+  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.v_lat[cj + i0] = row[i0];
   filter_row<R, R>(g.big, false, j, nlon, row, ext);
   __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_f[ix3(nhalf, nlon, i + 1, j, k)] = row[i];
+  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.v_f[cj + i0] = row[i0];
 }
 
 // Run-prologue filters (gmcore_mod.F90:112-122): u_f, v_f, phs_f | gz_f.
@@ -1052,6 +1193,13 @@ void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const
 }
 template <class R>
 void launch_momentum_tend(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.baroclinic) {
+      k_momentum_f<<<dim3(g.nlat, g.nlev), 256, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
+                                                              s.u_f, s.v_f, s.psr, w.du, w.dv);
+      return;
+    }
+  }
   k_momentum_tend<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
 }
 template <class R>

@@ -50,6 +50,33 @@ struct MassField {
   }
 };
 
+// Cell mass on level k with the level's constants held by the block; at(o)
+// takes the 0-based offset o = (j-1) nlon + (i-1) of the cell in a 2D field
+// and gives MassField::at bit for bit.
+template <class R>
+struct LevMass {
+  const DGrid &g;
+  SurfP<R> sp;
+  const R *gz;
+  const double *gzs;
+  int k;
+  float a = 0, b = 0;   // FP32 form: dmA_k, dmB_k
+  __device__ __forceinline__ LevMass(const DGrid &g_, SurfP<R> sp_, const R *gz_, const double *gzs_, int k_)
+      : g(g_), sp(sp_), gz(gz_), gzs(gzs_), k(k_) {
+    if constexpr (std::is_same<R, float>::value) {
+      a = g.dmA[k - 1];
+      b = g.dmB[k - 1];
+    }
+  }
+  __device__ __forceinline__ R at(unsigned o) const {
+    if (g.baroclinic) {
+      if constexpr (std::is_same<R, float>::value) return fmaf(b, sp.psr[o], a);
+      else return Mass<double>::layer(g, k, sp.phs_f[o]);
+    }
+    return (R)(((double)gz[o] - gzs[o]) / g.g);
+  }
+};
+
 // TVD interpolation with flux limiter (tvd_mod.F90:44-84); eps is the
 // default-kind literal 1.0e-6 of the reference widened to double.
 template <class R>
@@ -200,11 +227,13 @@ __device__ __forceinline__ float cflz_of_f(const DGrid &g, const float *wm, int 
   float deta = (w1 + 2.0f * w2 + 2.0f * w3 + w4) * (1.0f / 6.0f) * dt_;
   int ks, ke, s;
   if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
+  const float sf = deta < 0 ? -1.0f : 1.0f;
   deta = fabsf(deta);
   const float *FD = g.full_dlev_f;
-  for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s) {
+  float whole = 0;   // |l - ks| counted in FP32 (no integer conversions)
+  for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s, whole += 1.0f) {
     deta = deta - FD[l - 1];
-    if (deta < 0) return s * ((1.0f + deta * RFD[l - 1]) + abs(l - ks));
+    if (deta < 0) return sf * ((1.0f + deta * RFD[l - 1]) + whole);
   }
   return NAN;
 }
