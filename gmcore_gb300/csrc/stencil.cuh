@@ -260,7 +260,26 @@ __device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, in
     ext[t] = row[i - 1];
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+  // three consecutive outputs per thread over a rolling window of ext: one
+  // ext and one weight load per tap for three sums (each sum in tap order,
+  // as the one-output loop below forms it)
+  const int nfull = nlon - nlon % 3;
+  for (int b = 3 * threadIdx.x; b < nfull; b += 3 * blockDim.x) {
+    A s0 = 0, s1 = 0, s2 = 0;
+    A e0 = (A)ext[b], e1 = (A)ext[b + 1];
+    for (int t = 0; t < n; ++t) {
+      const A wt = w[t], e2 = (A)ext[b + t + 2];
+      s0 = s0 + wt * e0;
+      s1 = s1 + wt * e1;
+      s2 = s2 + wt * e2;
+      e0 = e1;
+      e1 = e2;
+    }
+    row[b] = (R)s0;
+    row[b + 1] = (R)s1;
+    row[b + 2] = (R)s2;
+  }
+  for (int i = nfull + threadIdx.x; i < nlon; i += blockDim.x) {
     A s = 0;
     for (int t = 0; t < n; ++t) s = s + w[t] * (A)ext[i + t];
     row[i] = (R)s;
