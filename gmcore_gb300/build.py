@@ -38,18 +38,25 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+# FP32 arithmetic of the mixed form: subnormals flushed, division and square
+# root to the hardware approximations (within 2 ulp).  FP64 arithmetic, and so
+# the FP64 form, is unaffected by these flags.
+FP32_FLAGS = ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
+
+
 def build(verbose=False, force=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(BUILD_DIR, exist_ok=True)
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-    headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "gmcore_gpu.h")]
+    headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "gmcore_gpu.h"),
+                                                           os.path.abspath(__file__)]
     cmds, objs = [], []
     for src in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD_DIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmds.append([nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+            cmds.append([nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", *FP32_FLAGS,
                          "-Xcompiler", "-fPIC", *inc, "-c", s, "-o", o])
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)

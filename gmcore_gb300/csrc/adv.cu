@@ -773,22 +773,35 @@ __global__ void GMC_BOUNDS(R, 8) k_tracer_horizontal(DGrid g, const R *q_old, R 
     mrow[0] = Mass<R>::layer(g, k, sp.at((size_t)(j - 1) * nlon + (nlon - 1)));
     mrow[nlon + 1] = Mass<R>::layer(g, k, sp.at((size_t)(j - 1) * nlon));
   }
-  if (__syncthreads_or(neg) && threadIdx.x == 0) {
-    for (int i = 1; i <= nlon; ++i) {
-      if (row[i] < 0) {
-        R qm0 = row[i] * mrow[i], qm1 = row[i - 1] * mrow[i - 1], qm2 = row[i + 1] * mrow[i + 1];
-        R qm0_half = (R)0.5 * qm0;
-        if (qm1 >= qm0_half && qm2 >= qm0_half) {
-          row[i - 1] = (qm1 - qm0_half) / mrow[i - 1];
-          row[i + 1] = (qm2 - qm0_half) / mrow[i + 1];
-        } else if (qm1 > qm0) {
-          row[i - 1] = (qm1 - qm0) / mrow[i - 1];
-        } else if (qm2 > qm0) {
-          row[i + 1] = (qm2 - qm0) / mrow[i + 1];
-        } else {
-          atomicOr(g.err, ERR_NEGTRACER);
+  // The fixer visits i = 1 .. nlon in order.  One warp walks the row 32
+  // cells at a time: a ballot finds the negative cells, lane 0 fixes the
+  // lowest one, and the cells after it are tested again (a fix changes its
+  // right neighbour), which visits the negatives in the same order with the
+  // same values as the sequential walk.
+  if (__syncthreads_or(neg) && threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    for (int base = 1; base <= nlon; base += 32) {
+      const int i = base + lane;
+      unsigned mask = __ballot_sync(0xffffffffu, i <= nlon && row[i] < 0);
+      while (mask) {
+        const int p = base + __ffs(mask) - 1;
+        if (lane == 0) {
+          R qm0 = row[p] * mrow[p], qm1 = row[p - 1] * mrow[p - 1], qm2 = row[p + 1] * mrow[p + 1];
+          R qm0_half = (R)0.5 * qm0;
+          if (qm1 >= qm0_half && qm2 >= qm0_half) {
+            row[p - 1] = (qm1 - qm0_half) / mrow[p - 1];
+            row[p + 1] = (qm2 - qm0_half) / mrow[p + 1];
+          } else if (qm1 > qm0) {
+            row[p - 1] = (qm1 - qm0) / mrow[p - 1];
+          } else if (qm2 > qm0) {
+            row[p + 1] = (qm2 - qm0) / mrow[p + 1];
+          } else {
+            atomicOr(g.err, ERR_NEGTRACER);
+          }
+          row[p] = 0;
         }
-        row[i] = 0;
+        __syncwarp();
+        mask = __ballot_sync(0xffffffffu, i <= nlon && i > p && row[i] < 0);
       }
     }
   }

@@ -121,9 +121,10 @@ __device__ __forceinline__ double div6(double x) { return x / 6.0; }
 __device__ __forceinline__ float div6(float x) { return x * (1.0f / 6.0f); }
 __device__ __forceinline__ double div3(double x) { return x / 3.0; }
 __device__ __forceinline__ float div3(float x) { return x * (1.0f / 3.0f); }
-// a / b: IEEE division in the FP64 form, one reciprocal and product in FP32.
+// a / b: IEEE division in the FP64 form, the approximate division (MUFU
+// reciprocal and product, within 2 ulp) in FP32.
 __device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
-__device__ __forceinline__ float fdiv(float a, float b) { return a * __frcp_rn(b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
 template <class R>
 __device__ __forceinline__ void ppm(int limiter, R fm2, R fm1, R f, R fp1, R fp2, R &fl, R &df, R &f6) {
