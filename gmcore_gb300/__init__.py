@@ -29,7 +29,7 @@ EXPORTED = (
     "gmc_prepare", "gmc_step", "gmc_get_field", "gmc_get_tracer", "gmc_diagnose", "gmc_time_step",
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
-    "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs",
+    "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs", "gmc_host_register", "gmc_host_unregister",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -82,8 +82,39 @@ def load(build_if_missing=True):
     lib.gmc_set_graphs.argtypes = [C.c_void_p, C.c_int32]
     lib.gmc_adjoint.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View), P(View)]
     lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
+    lib.gmc_host_register.argtypes = [C.c_void_p, C.c_size_t]
+    lib.gmc_host_unregister.argtypes = [C.c_void_p]
     _lib = lib
     return lib
+
+
+def page_aligned(shape):
+    """Zeroed float64 array whose memory starts on a host page and shares no
+    page with other arrays (so that it can be registered on its own)."""
+    import mmap
+    page = mmap.PAGESIZE
+    n = int(np.prod(shape))
+    per = page // 8
+    buf = np.zeros(n + 2 * per)
+    off = (-buf.ctypes.data % page) // 8
+    return buf[off:off + n].reshape(shape)
+
+
+def host_register(a):
+    """Page-lock and map the memory of a C-contiguous array (gmc_host_register):
+    transfers of fields and tracers to and from it then gather, scatter and
+    convert on the GPU.  Call host_unregister(a) before the array is freed."""
+    if not a.flags.c_contiguous:
+        raise ValueError("host_register needs a C-contiguous array")
+    rc = load().gmc_host_register(C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes))
+    if rc != 0:
+        raise GmcError(rc, "gmc_host_register refused the range")
+
+
+def host_unregister(a):
+    rc = load().gmc_host_unregister(C.c_void_p(a.ctypes.data))
+    if rc != 0:
+        raise GmcError(rc, "gmc_host_unregister: range not registered")
 
 
 def _dptr(a):

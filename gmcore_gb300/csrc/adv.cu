@@ -251,6 +251,8 @@ template <class R>
 __global__ void GMC_BOUNDS(R, 5) k_ffsl_inner_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ q,
                                const R *__restrict__ divy, R *__restrict__ qy, double dt) {
   __shared__ double red[32];
+  extern __shared__ double sh_faces[];
+  R *face_sh = reinterpret_cast<R *>(sh_faces);   // polar face fluxes [2][nlon] (strips with a pole)
   const int k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
   const R hdt = (R)dt;
@@ -261,7 +263,6 @@ __global__ void GMC_BOUNDS(R, 5) k_ffsl_inner_y(DGrid g, const R *__restrict__ v
   const int fl0 = j0 >= 2 ? 0 : 1;                       // first existing face
   const int nfe = min(kHflxRows, nhalf - j0 + 1) + 1;    // faces up to nhalf
   const bool has_s = j0 == 1, has_n = j0 <= nhalf && nhalf <= j0 + kHflxRows - 1;
-  double ring_s = 0, ring_n = 0;
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     R y[NV], sl[NV];
 #pragma unroll
@@ -304,17 +305,20 @@ __global__ void GMC_BOUNDS(R, 5) k_ffsl_inner_y(DGrid g, const R *__restrict__ v
       }
       prev = cur;
     }
-    // the polar faces' fluxes join the ring sums in FP64 only in the strips
-    // that hold them (one conversion per column there, none elsewhere)
-    if (has_s) ring_s += (double)face_s;
-    if (has_n) ring_n += (double)face_n;
+    // the polar faces' fluxes wait in shared memory for the FP64 ring sums
+    // below, so the column loop holds no FP64 arithmetic
+    if (has_s) face_sh[i] = face_s;
+    if (has_n) face_sh[nlon + i] = face_n;
   }
   // pole rows from the ring of their polar half row
   for (int side = 0; side < 2; ++side) {
     const bool has = side == 0 ? has_s : has_n;
     if (!has) continue;
     const int j = side == 0 ? 1 : nlat, jv = side == 0 ? 1 : nhalf;
-    double p = block_sum(side == 0 ? ring_s : ring_n, red);
+    __syncthreads();
+    double ring = 0;   // each thread its columns in order, then the fixed-order block sum
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) ring += (double)face_sh[side * nlon + i];
+    double p = block_sum(ring, red);
     p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
     const R pole = (R)p;
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
@@ -556,7 +560,7 @@ __global__ void GMC_BOUNDS_F(8) k_pt_tendency_f(DGrid g, Slot<float> s, Work<flo
   const int ld = kTileI + 1;
   const bool pole = j == 1 || j == nlat, valid = i <= nlon;
   const int ic = valid ? i : nlon;
-  double *ring = shd;                                     // [nlev]
+  float *ring = reinterpret_cast<float *>(shd);           // [nlev] (FP64 sums rounded once)
   float *C = reinterpret_cast<float *>(shd + nlev) + ti;  // C(l) at [(l+1)*ld], l = -1 .. nlev+2
   float *S = C + (nlev + 4) * ld;                         // s(l) at [l*ld],     l = 0 .. nlev+1
   float *FL = S + (nlev + 2) * ld;                        // cell l at [(l-1)*ld]
@@ -617,7 +621,7 @@ __global__ void GMC_BOUNDS_F(8) k_pt_tendency_f(DGrid g, Slot<float> s, Work<flo
     float dlon, dlat;
     if (pole) {
       dlon = 0;
-      dlat = (float)ring[k - 1];
+      dlat = ring[k - 1];
     } else {
       dlon = (w.ptf_lon[o] - w.ptf_lon[ix3(nlat, nlon, im, j, k)]) * clon / ac;
       dlat = (w.ptf_lat[ix3(nhalf, nlon, i, j, k)] * la0 - w.ptf_lat[ix3(nhalf, nlon, i, j - 1, k)] * la1) / ac;
@@ -995,7 +999,7 @@ void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, co
   if (smem_o > 48 * 1024) cudaFuncSetAttribute(k_hflx_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
   if (smem_i > 48 * 1024) cudaFuncSetAttribute(k_ffsl_inner_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i);
   k_ffsl_inner_x<R><<<rows, L.threads, smem_i, L.stream>>>(g, b.u, b.cflx, q, b.divx, qx, dt);
-  k_ffsl_inner_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
+  k_ffsl_inner_y<R><<<strips, L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
   k_hflx_x<R><<<inner_rows, L.threads, smem_o, L.stream>>>(g, b.mfx, b.cflx, qy, fx);
   k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
 }

@@ -506,7 +506,7 @@ __global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<flo
   const int i = blockIdx.x * kTileI + ti + 1;
   const int ld = kTileI + 1;
   const bool pole = j == 1 || j == nlat, valid = i <= nlon;
-  double *ring = shd;                                    // [nlev]
+  float *ring = reinterpret_cast<float *>(shd);          // [nlev] (FP64 sums rounded once)
   float *P = reinterpret_cast<float *>(shd + nlev);      // [nlev][ld]   prefix sums
   float *WM = P + nlev * ld;                             // [nlev+1][ld] we / ml * half_dlev
   if (pole) tile_pole_ring(g, j, ring, [&](int ii, int jv, int k) { return s.mfy_lat[ix3(nhalf, nlon, ii, jv, k)]; });
@@ -517,7 +517,7 @@ __global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<flo
   for (int k = 1 + kt; k <= nlev; k += KT) {
     float d;
     if (pole)
-      d = (float)ring[k - 1];
+      d = ring[k - 1];
     else
       d = (s.mfx_lon[ix3(nlat, nlon, ic, j, k)] - s.mfx_lon[ix3(nlat, nlon, im, j, k)]) * clon +
           (s.mfy_lat[ix3(nhalf, nlon, ic, j, k)] * cn - s.mfy_lat[ix3(nhalf, nlon, ic, j - 1, k)] * cs);

@@ -182,6 +182,53 @@ void host_par_for(size_t n, F &&f) {
 }
 
 // Row r (k-major over nk levels of nrow rows) of the interior of a view.
+// Host ranges the caller registered with gmc_host_register (page-locked and
+// mapped): transfers of views inside one of them run as device kernels that
+// read or write the rows over the host link and convert on the GPU.
+struct HostRange {
+  uintptr_t base;
+  size_t bytes;
+  char *dev;   // device address of base
+};
+std::mutex g_host_mu;
+std::vector<HostRange> g_host_ranges;
+
+// Device address of [p, p + bytes) when one registered range holds all of it.
+char *mapped_range(const void *p, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  const uintptr_t a = (uintptr_t)p;
+  for (const HostRange &r : g_host_ranges)
+    if (a >= r.base && bytes <= r.bytes && a - r.base <= r.bytes - bytes) return r.dev + (a - r.base);
+  return nullptr;
+}
+
+// Interior row r (0-based, level-major) of a view relative to its row 0,
+// in elements (view_row's arithmetic on the device).
+struct ViewDims {
+  long n0, n1;   // allocated extents of the view's first two dimensions
+  int nrow, nlon;
+};
+__device__ __forceinline__ long view_rel(const ViewDims &d, size_t r) {
+  const long j = (long)(r % d.nrow) + 1, k = (long)(r / d.nrow) + 1;
+  return d.n0 * ((j - 1) + d.n1 * (k - 1));
+}
+template <class T>
+__global__ void k_view_gather(const double *__restrict__ row0, ViewDims d, size_t rows, T *__restrict__ dst) {
+  for (size_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const double *src = row0 + view_rel(d, r);
+    T *o = dst + r * d.nlon;
+    for (int i = threadIdx.x; i < d.nlon; i += blockDim.x) o[i] = (T)src[i];
+  }
+}
+template <class T>
+__global__ void k_view_scatter(const T *__restrict__ src, ViewDims d, size_t rows, double *__restrict__ row0) {
+  for (size_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    double *o = row0 + view_rel(d, r);
+    const T *s = src + r * d.nlon;
+    for (int i = threadIdx.x; i < d.nlon; i += blockDim.x) o[i] = (double)s[i];
+  }
+}
+
 inline double *view_row(const gmc_view &v, int nrow, size_t r) {
   const long n0 = v.ub[0] - v.lb[0] + 1, n1 = v.ub[1] - v.lb[1] + 1;
   const int k = (int)(r / nrow) + 1, j = (int)(r % nrow) + 1;
@@ -601,10 +648,30 @@ struct Engine : EngineBase {
     xfer_ev.resize(kXferChunks);
     for (auto &e : xfer_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
+  // Device address of the view's first interior row when the caller has
+  // registered the whole span of its interior rows (nullptr otherwise).
+  double *mapped_view(const gmc_view &v, int nrow, int nk, ViewDims &d) const {
+    const size_t rows = (size_t)nrow * nk;
+    const double *first = view_row(v, nrow, 0), *last = view_row(v, nrow, rows - 1) + grid.nlon;
+    char *dev = mapped_range(first, (size_t)(last - first) * sizeof(double));
+    d = {v.ub[0] - v.lb[0] + 1, v.ub[1] - v.lb[1] + 1, nrow, grid.nlon};
+    return reinterpret_cast<double *>(dev);
+  }
+  static int xfer_blocks(size_t rows) { return (int)std::min<size_t>(rows, 152 * 8); }
+
   template <class T>
   void upload_view(const gmc_view &v, int nrow, int nk, T *dev, T *const *also = nullptr, int nalso = 0) {
     const int nlon = grid.nlon;
     const size_t rows = (size_t)nrow * nk, per = (rows + kXferChunks - 1) / kXferChunks;
+    ViewDims vd;
+    if (const double *row0 = mapped_view(v, nrow, nk, vd)) {   // registered: gather and convert on the GPU
+      k_view_gather<T><<<xfer_blocks(rows), 256, 0, stream>>>(row0, vd, rows, dev);
+      CK(cudaGetLastError());
+      for (int t = 0; t < nalso; ++t)
+        CK(cudaMemcpyAsync(also[t], dev, rows * nlon * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+      CK(cudaStreamSynchronize(stream));
+      return;
+    }
     T *host = reinterpret_cast<T *>(pinned);
     for (size_t a = 0; a < rows; a += per) {
       const size_t b = std::min(rows, a + per);
@@ -626,6 +693,13 @@ struct Engine : EngineBase {
     xfer_events();
     const int nlon = grid.nlon;
     const size_t rows = (size_t)nrow * nk, per = (rows + kXferChunks - 1) / kXferChunks;
+    ViewDims vd;
+    if (double *row0 = mapped_view(v, nrow, nk, vd)) {   // registered: convert and scatter on the GPU
+      k_view_scatter<T><<<xfer_blocks(rows), 256, 0, stream>>>(dev, vd, rows, row0);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(stream));
+      return;
+    }
     T *host = reinterpret_cast<T *>(pinned);
     int c = 0;
     for (size_t a = 0; a < rows; a += per, ++c) {
@@ -1766,6 +1840,46 @@ int gmc_adjoint(gmc_ctx *ctx, int32_t nsteps, int32_t ckpt_every, const gmc_view
 int gmc_set_graphs(gmc_ctx *ctx, int32_t on) {
   if (!ctx || !ctx->eng) return GMC_EINVAL;
   ctx->eng->set_graphs(on != 0);
+  return GMC_OK;
+}
+
+int gmc_host_register(void *ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return GMC_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    const uintptr_t a = (uintptr_t)ptr;
+    for (const HostRange &r : g_host_ranges)
+      if (a < r.base + r.bytes && r.base < a + bytes) return GMC_EINVAL;   // overlaps a registered range
+  }
+  if (cudaHostRegister(ptr, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable) != cudaSuccess) {
+    cudaGetLastError();
+    return GMC_ECUDA;
+  }
+  void *dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, ptr, 0) != cudaSuccess || !dev) {
+    cudaGetLastError();
+    cudaHostUnregister(ptr);
+    cudaGetLastError();
+    return GMC_ECUDA;
+  }
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  g_host_ranges.push_back({(uintptr_t)ptr, bytes, static_cast<char *>(dev)});
+  return GMC_OK;
+}
+
+int gmc_host_unregister(void *ptr) {
+  if (!ptr) return GMC_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = std::find_if(g_host_ranges.begin(), g_host_ranges.end(),
+                           [&](const HostRange &r) { return r.base == (uintptr_t)ptr; });
+    if (it == g_host_ranges.end()) return GMC_EINVAL;
+    g_host_ranges.erase(it);
+  }
+  if (cudaHostUnregister(ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return GMC_ECUDA;
+  }
   return GMC_OK;
 }
 

@@ -183,7 +183,7 @@ constexpr int kTileI = 32, kTileK = 8;
 // Pole ring sums of one level field by the warps of a column-tile block:
 // ring[k-1] = sgn * sum_i f(i, jv, k) * le_lat(jv) / nlon / area_cell(j).
 template <class F>
-__device__ __forceinline__ void tile_pole_ring(const DGrid &g, int j, double *ring, F f) {
+__device__ __forceinline__ void tile_pole_ring(const DGrid &g, int j, float *ring, F f) {
   const int lt = threadIdx.y * blockDim.x + threadIdx.x;
   const int lane = lt & 31, warp = lt >> 5, nw = (blockDim.x * blockDim.y) >> 5;
   const int jv = j == 1 ? 1 : g.nhalf;
@@ -192,7 +192,7 @@ __device__ __forceinline__ void tile_pole_ring(const DGrid &g, int j, double *ri
     double acc = 0;
     for (int ii = 1 + lane; ii <= g.nlon; ii += 32) acc += (double)f(ii, jv, k);
     acc = warp_sum(acc);
-    if (lane == 0) ring[k - 1] = sgn * acc * ROW(g.le_lat, jv) / g.nlon / ROW(g.area_cell, j);
+    if (lane == 0) ring[k - 1] = (float)(sgn * acc * ROW(g.le_lat, jv) / g.nlon / ROW(g.area_cell, j));
   }
 }
 

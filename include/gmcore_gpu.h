@@ -21,7 +21,8 @@
  *    lower/upper bounds per dimension, column-major (i fastest), so a
  *    Fortran array with halos can be passed as c_loc(a) with lbound/ubound.
  *    Only interior points are read or written; halos are left untouched.
- *  - The caller owns host memory; the library never keeps host pointers.
+ *  - The caller owns host memory; the library keeps no host pointer except
+ *    the ranges the caller registers with gmc_host_register.
  *    The library owns device memory; model state stays resident in HBM
  *    between calls.
  *  - One host thread per context at a time.  All calls are synchronous.
@@ -231,6 +232,19 @@ int gmc_adjoint(gmc_ctx *ctx, int32_t nsteps, int32_t ckpt_every, const gmc_view
  * kernels directly.  No counterpart in the reference (a host-side launch
  * mechanism). */
 int gmc_set_graphs(gmc_ctx *ctx, int32_t on);
+
+/* Page-lock and map a caller-owned host range (cudaHostRegister, mapped).
+ * gmc_set_field / gmc_get_field / gmc_set_tracer / gmc_get_tracer of a view
+ * whose interior rows lie inside one registered range skip the host-side
+ * staging: a device kernel gathers or scatters the rows over the host link
+ * and converts FP64 <-> the form's type on the GPU (same values as the staged
+ * path).  The library keeps the range until gmc_host_unregister(ptr) with the
+ * same ptr; the caller keeps the memory alive until then.  Ranges may not
+ * overlap.  No reference counterpart: a transfer option of the same calls.
+ * Returns GMC_EINVAL (null, empty or overlapping range; unknown ptr) or
+ * GMC_ECUDA (registration refused). */
+int gmc_host_register(void *ptr, size_t bytes);
+int gmc_host_unregister(void *ptr);
 
 /* Timing of the last gmc_step call: device time between CUDA events
  * recorded on the context's stream around the whole call, and the number
