@@ -287,6 +287,23 @@ struct Engine : EngineBase {
   // tracer batch (one per member) and its host-side cadence state
   int ntr = 0;
   std::vector<TracerBatch<R>> tb;     // [member]
+  // one member with several tracers: each tracer's advection runs on its own
+  // stream (forked from and joined to the context stream) with its own FFSL
+  // scratch, so that the tracers' kernels overlap
+  struct TracerScratch {
+    R *qx, *qy, *fx, *fy;
+  };
+  std::vector<TracerScratch> tsc;     // [tracer]
+  std::vector<cudaStream_t> tstreams;
+  std::vector<cudaEvent_t> tevents;
+  cudaEvent_t tfork_ev = nullptr;
+  bool tracer_streams() const { return nm == 1 && ntr > 1; }
+  // one baroclinic member: the forward pass runs its batch-CFL / column-mass /
+  // potential-temperature FFSL chain on a side stream, overlapping the
+  // tangent-wind / KE / PV / momentum chain of the context stream
+  cudaStream_t dside = nullptr;
+  cudaEvent_t dfork_ev = nullptr, dmf_ev = nullptr, dcm_ev = nullptr, dpt_ev = nullptr;
+  bool dyn_split() const { return nm == 1 && grid.cfg.baroclinic && !prof; }
   std::vector<R *> q;                 // [(member * 2 + slot) * ntr + l]
   int q_old = 0;
   int nstep_adv = 1, uv_step = 0, mf_step = 0, we_step = 0;
@@ -390,6 +407,15 @@ struct Engine : EngineBase {
       b.old_phs_f = a.template take<double>(two_d());
       b.old_psr = kFP32 ? a.template take<float>(two_d()) : nullptr;
       for (int t = 0; t < 2 * ntr; ++t) q[(size_t)m * 2 * ntr + t] = a.template take<R>(full3());
+      if (tracer_streams()) {
+        tsc.resize(ntr);
+        for (TracerScratch &t : tsc) {
+          t.qx = a.template take<R>(full3());
+          t.qy = a.template take<R>(full3());
+          t.fx = a.template take<R>(full3());
+          t.fy = a.template take<R>(half3());
+        }
+      }
     }
   }
 
@@ -425,6 +451,19 @@ struct Engine : EngineBase {
     for (int m = 0; m < nm; ++m) carve_member(arena, m, bc);
     diag_partial = arena.take<double>(8 * nblk);
     member_streams();
+    if (nm == 1 && bc) {
+      CK(cudaStreamCreateWithFlags(&dside, cudaStreamNonBlocking));
+      for (cudaEvent_t *e : {&dfork_ev, &dmf_ev, &dcm_ev, &dpt_ev}) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    if (tracer_streams()) {
+      tstreams.resize(ntr);
+      tevents.resize(ntr);
+      for (int t = 0; t < ntr; ++t) {
+        CK(cudaStreamCreateWithFlags(&tstreams[t], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&tevents[t], cudaEventDisableTiming));
+      }
+      CK(cudaEventCreateWithFlags(&tfork_ev, cudaEventDisableTiming));
+    }
     diag_out = arena.take<double>(64);
     err = arena.take<unsigned>(64);
     staging = arena.take<R>(std::max(lev3(), full3()));
@@ -444,6 +483,12 @@ struct Engine : EngineBase {
     for (cudaEvent_t e : mevents) cudaEventDestroy(e);
     for (cudaEvent_t e : xfer_ev) cudaEventDestroy(e);
     if (fork_ev) cudaEventDestroy(fork_ev);
+    for (cudaStream_t st : tstreams) cudaStreamDestroy(st);
+    for (cudaEvent_t e : tevents) cudaEventDestroy(e);
+    if (tfork_ev) cudaEventDestroy(tfork_ev);
+    if (dside) cudaStreamDestroy(dside);
+    for (cudaEvent_t e : {dfork_ev, dmf_ev, dcm_ev, dpt_ev})
+      if (e) cudaEventDestroy(e);
     arena.release();
     tables.release();
     if (tl) {
@@ -832,12 +877,31 @@ struct Engine : EngineBase {
       BatchView<R> bv{};
       bv.u = b.u; bv.v = b.v; bv.mfx = b.mfx; bv.mfy = b.mfy;
       bv.cflx = b.cflx; bv.cfly = b.cfly; bv.divx = b.divx; bv.divy = b.divy; bv.cflz = b.cflz;
+      // tracers on their own streams unless profiling (whose events time
+      // the context stream)
+      const bool tfork = tracer_streams() && !prof;
+      if (tfork && !dry) {
+        CK(cudaEventRecord(tfork_ev, L.stream));
+        for (cudaStream_t st : tstreams) CK(cudaStreamWaitEvent(st, tfork_ev, 0));
+      }
       for (int l = 0; l < ntr; ++l) {
         R *qo = q[((size_t)m * 2 + q_old) * ntr + l], *qn = q[((size_t)m * 2 + (1 - q_old)) * ntr + l];
-        K("ffsl_hflx_tracer", 3, [&] { launch_ffsl_hflx<R>(dg, L, bv, qo, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt_adv); });
-        K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, L, qo, qn, w.ptf_lon, w.ptf_lat, b.old_surf(), n.surf(), dt_adv); });
-        K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, L, qn, b.cflz, b.we, n.surf(), dt_adv); });
-        K("tracer_lon_damp", 1, [&] { launch_tracer_lon_damp<R>(dg, L, qn); });
+        Launch Lt = L;
+        R *qx = w.qx, *qy = w.qy, *fx = w.ptf_lon, *fy = w.ptf_lat;
+        if (tfork) {
+          Lt.stream = tstreams[l];
+          qx = tsc[l].qx; qy = tsc[l].qy; fx = tsc[l].fx; fy = tsc[l].fy;
+        }
+        K("ffsl_hflx_tracer", 3, [&] { launch_ffsl_hflx<R>(dg, Lt, bv, qo, w.qmfx, w.qmfy, qx, qy, fx, fy, dt_adv); });
+        K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, Lt, qo, qn, fx, fy, b.old_surf(), n.surf(), dt_adv); });
+        K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, Lt, qn, b.cflz, b.we, n.surf(), dt_adv); });
+        K("tracer_lon_damp", 1, [&] { launch_tracer_lon_damp<R>(dg, Lt, qn); });
+      }
+      if (tfork && !dry) {
+        for (int t = 0; t < ntr; ++t) {
+          CK(cudaEventRecord(tevents[t], tstreams[t]));
+          CK(cudaStreamWaitEvent(L.stream, tevents[t], 0));
+        }
       }
     }
     // copy_old_m
@@ -903,6 +967,10 @@ struct Engine : EngineBase {
   // space_operators forward pass (gmcore_mod.F90:467-528)
   void forward(int m, const Slot<R> &s, double dt) { forward_w(work[m], s, dt); }
   void forward_w(Work<R> &w, const Slot<R> &s, double dt) {
+    if (dyn_split()) {
+      forward_split(w, s, dt);
+      return;
+    }
     forward_prepare_w(w, s, dt);
     if (grid.cfg.baroclinic) {
       K("batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt); });
@@ -916,6 +984,40 @@ struct Engine : EngineBase {
       K("swm_dgz", 1, [&] { launch_swm_dgz<R>(dg, L, s, w); });
     }
     K("momentum_tend", 1, [&] { launch_momentum_tend<R>(dg, L, s, w); });
+  }
+
+  // The same launches as forward_w on two streams.  Side: batch_cfl, then
+  // (after mass_flux) column_mass, ffsl_hflx_pt, pt_tendency.  Context:
+  // mass_flux, tangent_winds, kinetic_energy, pv, pv_edges, then (after
+  // column_mass) momentum_tend; the context stream joins the side stream
+  // before the backward pass.  The two chains write disjoint work fields.
+  void forward_split(Work<R> &w, const Slot<R> &s, double dt) {
+    Launch Ls = L;
+    Ls.stream = dside;
+    auto edge = [&](cudaEvent_t e, cudaStream_t from, cudaStream_t to) {
+      if (dry) return;   // a captured graph holds the dependency
+      CK(cudaEventRecord(e, from));
+      CK(cudaStreamWaitEvent(to, e, 0));
+    };
+    edge(dfork_ev, L.stream, dside);
+    K("batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, Ls, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt); });
+    K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
+    edge(dmf_ev, L.stream, dside);
+    K("column_mass", 1, [&] { launch_column_mass<R>(dg, Ls, s, w, dt); });
+    if (!dry) CK(cudaEventRecord(dcm_ev, dside));
+    BatchView<R> b{};
+    b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
+    b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
+    K("ffsl_hflx_pt", 3, [&] { launch_ffsl_hflx<R>(dg, Ls, b, s.pt, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt); });
+    K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, Ls, s, w); });
+    if (!dry) CK(cudaEventRecord(dpt_ev, dside));
+    K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
+    K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
+    K("pv", 1, [&] { launch_pv<R>(dg, L, s, w); });
+    K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w, dt); });
+    if (!dry) CK(cudaStreamWaitEvent(L.stream, dcm_ev, 0));
+    K("momentum_tend", 1, [&] { launch_momentum_tend<R>(dg, L, s, w); });
+    if (!dry) CK(cudaStreamWaitEvent(L.stream, dpt_ev, 0));
   }
 
   // step_forward_backward (time_schemes_mod.F90:102-118)
