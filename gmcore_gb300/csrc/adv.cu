@@ -705,7 +705,7 @@ __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, d
     bool bad = false;
     const float dtf = (float)dt;
     for (int k = 2; k <= nlev; ++k) {
-      float c = cflz_of_f(g, col, st, k, dtf, bad);
+      float c = cflz_of_f(g.half_lev_f, g.full_dlev_f, g.full_dlev_rf, nlev, col, st, k, dtf, bad);
       if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
     if (bad) atomicOr(g.err, ERR_CFLZ);

@@ -444,7 +444,7 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
     bool bad = false;
     const float dtf = (float)dt;
     for (int k = 2; k <= nlev; ++k) {
-      float c = cflz_of_f(g, col, st, k, dtf, bad);
+      float c = cflz_of_f(g.half_lev_f, g.full_dlev_f, g.full_dlev_rf, nlev, col, st, k, dtf, bad);
       if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
     if (bad) atomicOr(g.err, ERR_CFLZ);
@@ -509,6 +509,14 @@ __global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<flo
   float *ring = reinterpret_cast<float *>(shd);          // [nlev] (FP64 sums rounded once)
   float *P = reinterpret_cast<float *>(shd + nlev);      // [nlev][ld]   prefix sums
   float *WM = P + nlev * ld;                             // [nlev+1][ld] we / ml * half_dlev
+  float *HL = WM + (nlev + 1) * ld, *FD = HL + nlev + 1, *RFD = FD + nlev;   // level tables
+  for (int t = kt * kTileI + ti; t <= nlev; t += kTileI * KT) {
+    HL[t] = g.half_lev_f[t];
+    if (t < nlev) {
+      FD[t] = g.full_dlev_f[t];
+      RFD[t] = g.full_dlev_rf[t];
+    }
+  }
   if (pole) tile_pole_ring(g, j, ring, [&](int ii, int jv, int k) { return s.mfy_lat[ix3(nhalf, nlon, ii, jv, k)]; });
   __syncthreads();
   const float ac = ROWR(float, area_cell, j);
@@ -561,7 +569,7 @@ __global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<flo
   bool bad = false;
   const float dtf = (float)dt;
   for (int k = 2 + kt; k <= nlev; k += KT) {
-    float c = cflz_of_f(g, WM + ti, ld, k, dtf, bad);
+    float c = cflz_of_f(HL, FD, RFD, nlev, WM + ti, ld, k, dtf, bad);
     if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
   }
   if (bad) atomicOr(g.err, ERR_CFLZ);
@@ -802,18 +810,14 @@ __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1, nlon = g.nlon, nlat = g.nlat;
   R *row = reinterpret_cast<R *>(sh), *ext = row + nlon;
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-    size_t c = ix3(nlat, nlon, i + 1, j, k);
-    R m_old = Mass<R>::layer(g, k, o.surf().at((size_t)(j - 1) * nlon + i));
-    row[i] = o.pt[c] * m_old + (R)dt * w.dpt[c];
-  }
+  const R dtr = (R)dt;
+  const SurfP<R> so = o.surf(), sn = n.surf();
+  const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k), m0 = (unsigned)(j - 1) * nlon;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x)
+    row[i] = o.pt[c0 + i] * Mass<R>::layer(g, k, so.at(m0 + i)) + dtr * w.dpt[c0 + i];
   filter_row<R, R>(g.small1, true, j, nlon, row, ext);
   __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-    size_t c = ix3(nlat, nlon, i + 1, j, k);
-    R m_new = Mass<R>::layer(g, k, n.surf().at((size_t)(j - 1) * nlon + i));
-    n.pt[c] = row[i] / m_new;
-  }
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.pt[c0 + i] = row[i] / Mass<R>::layer(g, k, sn.at(m0 + i));
 }
 
 // Shallow water: gz = gz_old + dt dgz; gz_f = big(gz); gz = small1(gz) (:178-192)
@@ -822,9 +826,10 @@ __global__ void k_update_gz(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, nlon = g.nlon;
   R *row = reinterpret_cast<R *>(sh), *row2 = row + nlon, *ext = row2 + nlon;
+  const R dtr = (R)dt;
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     size_t c = (size_t)(j - 1) * nlon + i;
-    R v = o.gz[c] + (R)dt * w.dgz[c];
+    R v = o.gz[c] + dtr * w.dgz[c];
     row[i] = v;
     row2[i] = v;
   }
@@ -977,6 +982,7 @@ __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const int k = blockIdx.y + 1;
   const bool bc = g.baroclinic;
+  const R dtr = (R)dt;
   const unsigned lf = (unsigned)nlat * nlon;   // level stride of the half-level pea / gzhl
   float dref = 0;
   if constexpr (std::is_same<R, float>::value) dref = bc ? g.dpe_ref[k - 1] : 0.0f;
@@ -997,7 +1003,7 @@ __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work
       } else {
         p = pgf_lon(g, n, w, i0 + 1, j, k, inv_d);
       }
-      return o.u_lon[c0 + i0] + (R)dt * (w.du[c0 + i0] - p);
+      return o.u_lon[c0 + i0] + dtr * (w.du[c0 + i0] - p);
     };
     const bool small = bc && filter_on(g.small2, true, j), big = filter_on(g.big, true, j);
     for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[i0] = val(i0);
@@ -1028,7 +1034,7 @@ __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work
     } else {
       p = pgf_lat(g, n, w, i0 + 1, jj, k, inv_d);
     }
-    return o.v_lat[cv + i0] + (R)dt * (w.dv[cv + i0] - p);
+    return o.v_lat[cv + i0] + dtr * (w.dv[cv + i0] - p);
   };
   const unsigned cj = (unsigned)ix3(nhalf, nlon, 1, j, k);
   auto load_v = [&](int jj, R *dst) {
@@ -1182,7 +1188,8 @@ void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R
 template <class R>
 void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
   if constexpr (std::is_same<R, float>::value) {
-    const size_t smem = g.nlev * sizeof(double) + (size_t)(2 * g.nlev + 1) * (kTileI + 1) * sizeof(float);
+    const size_t smem = g.nlev * sizeof(double) + (size_t)(2 * g.nlev + 1) * (kTileI + 1) * sizeof(float) +
+                        (size_t)(3 * g.nlev + 1) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_column_mass_f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_column_mass_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w, dt);
     return;

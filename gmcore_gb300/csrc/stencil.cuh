@@ -199,9 +199,10 @@ __device__ __forceinline__ void tile_pole_ring(const DGrid &g, int j, float *rin
 // FP32 form of cflz_of over a column held as wm(l) = we(l) / ml(l) * half_dlev(l)
 // at wm[(l - 1) * stride] for l = 1 .. nlev+1: the per-level quotients are
 // formed once per column instead of once per RK4 interpolation.
-__device__ __forceinline__ float cflz_of_f(const DGrid &g, const float *wm, int stride, int k, float dt_, bool &bad) {
-  const int nlev = g.nlev;
-  const float *HL = g.half_lev_f, *RFD = g.full_dlev_rf;   // [k-1]
+// HL, FD, RFD: half_lev, full_dlev and 1 / full_dlev in FP32 (index [k-1]),
+// from the grid tables or a shared-memory copy of them.
+__device__ __forceinline__ float cflz_of_f(const float *HL, const float *FD, const float *RFD, int nlev, const float *wm,
+                                           int stride, int k, float dt_, bool &bad) {
   auto W = [&](int l) { return wm[(l - 1) * stride]; };   // l = 1 .. nlev+1
   auto locate = [&](float w, float z) {
     int l;
@@ -230,7 +231,6 @@ __device__ __forceinline__ float cflz_of_f(const DGrid &g, const float *wm, int 
   if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
   const float sf = deta < 0 ? -1.0f : 1.0f;
   deta = fabsf(deta);
-  const float *FD = g.full_dlev_f;
   float whole = 0;   // |l - ks| counted in FP32 (no integer conversions)
   for (int l = ks; s > 0 ? l <= ke : l >= ke; l += s, whole += 1.0f) {
     deta = deta - FD[l - 1];
