@@ -670,12 +670,15 @@ __global__ void GMC_BOUNDS_F(8) k_momentum_f(DGrid g, const float *__restrict__ 
                                              const float *__restrict__ uf, const float *__restrict__ vf,
                                              const float *__restrict__ psr, float *__restrict__ du,
                                              float *__restrict__ dv) {
-  const int j = blockIdx.x + 1, k = blockIdx.y + 1;
+  const int k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
   const bool cor1 = g.coriolis_scheme == 1;
   const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
   const unsigned lf = (unsigned)nlat * nlon, lh = (unsigned)nhalf * nlon;   // level strides
-  if (j != 1 && j != nlat) {
+  // blocks 0 .. nlat-3: du on full rows 2 .. nlat-1; then dv on half rows 1 .. nhalf
+  const bool urow = (int)blockIdx.x < nlat - 2;
+  const int j = urow ? blockIdx.x + 2 : blockIdx.x - (nlat - 2) + 1;
+  if (urow) {
     const float t1 = ROWR(float, ftw1, j), t2 = ROWR(float, ftw2, j), de = ROWR(float, de_lon, j);
     const float aw = ROWR(float, area_lon_west, j), ae = ROWR(float, area_lon_east, j), al = ROWR(float, area_lon, j);
     const unsigned hs = (unsigned)ix3(nhalf, nlon, 1, j - 1, k), hn = hs + nlon;   // half rows j-1, j
@@ -697,8 +700,8 @@ __global__ void GMC_BOUNDS_F(8) k_momentum_f(DGrid g, const float *__restrict__ 
       if (k > 1) wd += fdiv(aw * we[fo + i0] + ae * we[fo + ip], al) * (u0 - uf[fo - lf + i0]);
       du[fo + i0] = d - fdiv(wd, m_lon) * 0.5f;
     }
+    return;
   }
-  if (j > nhalf) return;
   {
     const float t1 = ROWR(float, htw1, j), t2 = ROWR(float, htw2, j), de = ROWR(float, de_lat, j);
     const float an = ROWR(float, area_lat_north, j), as = ROWR(float, area_lat_south, j), al = ROWR(float, area_lat, j);
@@ -1202,7 +1205,7 @@ template <class R>
 void launch_momentum_tend(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
   if constexpr (std::is_same<R, float>::value) {
     if (g.baroclinic) {
-      k_momentum_f<<<dim3(g.nlat, g.nlev), 256, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
+      k_momentum_f<<<dim3(g.nlat - 2 + g.nhalf, g.nlev), 256, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
                                                               s.u_f, s.v_f, s.psr, w.du, w.dv);
       return;
     }
