@@ -978,30 +978,54 @@ __device__ __forceinline__ bool filter_on(const FilterDev &f, bool full_lat, int
 }
 
 // Each row is staged in shared memory (also where no filter touches it: the
-// stores then do not order the next points' loads behind them).
+// stores then do not order the next points' loads behind them).  A block takes
+// one row at kUvLevels(R) consecutive levels, so that the filters load each
+// weight once for all of them and each thread has more independent loads.
+template <class R>
+constexpr int kUvLevels = std::is_same<R, float>::value ? 2 : 1;
+
 template <class R>
 __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  constexpr int KB = kUvLevels<R>;
   extern __shared__ double sh[];
-  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
-  const int k = blockIdx.y + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
+  const int k0 = blockIdx.y * KB + 1;
   const bool bc = g.baroclinic;
   const R dtr = (R)dt;
   const unsigned lf = (unsigned)nlat * nlon;   // level stride of the half-level pea / gzhl
-  float dref = 0;
-  if constexpr (std::is_same<R, float>::value) dref = bc ? g.dpe_ref[k - 1] : 0.0f;
-  R *row = reinterpret_cast<R *>(sh), *nb = row + nlon, *ext = nb + nlon;
+  const int es = nlon + 2 * ((g.big.max_taps - 1) / 2) + 8;   // ext row stride
+  R *row = reinterpret_cast<R *>(sh), *nb = row + KB * nlon, *ext = nb + KB * nlon;
+  float dref[KB];
+#pragma unroll
+  for (int kk = 0; kk < KB; ++kk) {
+    dref[kk] = 0;
+    if constexpr (std::is_same<R, float>::value) dref[kk] = bc && k0 + kk <= nlev ? g.dpe_ref[k0 + kk - 1] : 0.0f;
+  }
+  // the group's filter: all KB levels together, or one by one for a partial
+  // last group
+  const int nk = min(KB, nlev - k0 + 1);
+  auto filt = [&](const FilterDev &f, bool full, int jj, R *rows) {
+    if (nk == KB) return filter_rows<KB, R, R>(f, full, jj, nlon, rows, nlon, ext, es);
+    bool any = false;
+    for (int kk = 0; kk < nk; ++kk) any = filter_row<R, R>(f, full, jj, nlon, rows + kk * nlon, ext) || any;
+    return any;
+  };
   if ((int)blockIdx.x < nlat) {
     const int j = blockIdx.x + 1;
-    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
     if (j == 1 || j == nlat) {   // pole rows are not updated; the big filter copies them
-      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_f[c0 + i0] = n.u_lon[c0 + i0];
+      for (int kk = 0; kk < nk; ++kk) {
+        const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k0 + kk);
+        for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_f[c0 + i0] = n.u_lon[c0 + i0];
+      }
       return;
     }
     const R inv_d = (R)1 / ROWR(R, de_lon, j);
-    auto val = [&](int i0) {
+    auto val = [&](int kk, int i0) {
+      const int k = k0 + kk;
+      const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
       R p;
       if constexpr (std::is_same<R, float>::value) {
-        if (bc) p = pgf_pq(w.pea, w.gzhl, c0 + i0, c0 + (i0 + 1 == nlon ? 0 : i0 + 1), lf, dref, inv_d);
+        if (bc) p = pgf_pq(w.pea, w.gzhl, c0 + i0, c0 + (i0 + 1 == nlon ? 0 : i0 + 1), lf, dref[kk], inv_d);
         else p = pgf_lon(g, n, w, i0 + 1, j, k, inv_d);
       } else {
         p = pgf_lon(g, n, w, i0 + 1, j, k, inv_d);
@@ -1009,62 +1033,71 @@ __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work
       return o.u_lon[c0 + i0] + dtr * (w.du[c0 + i0] - p);
     };
     const bool small = bc && filter_on(g.small2, true, j), big = filter_on(g.big, true, j);
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[i0] = val(i0);
-    if (small) filter_row<R, R>(g.small2, true, j, nlon, row, ext);
+    for (int kk = 0; kk < nk; ++kk)
+      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[kk * nlon + i0] = val(kk, i0);
+    if (small) filt(g.small2, true, j, row);
     __syncthreads();
-    if (!big) {
+    for (int kk = 0; kk < nk; ++kk) {
+      const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k0 + kk);
       for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
-        const R v = row[i0];
+        const R v = row[kk * nlon + i0];
         n.u_lon[c0 + i0] = v;
-        n.u_f[c0 + i0] = v;
+        if (!big) n.u_f[c0 + i0] = v;
       }
-      return;
     }
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_lon[c0 + i0] = row[i0];
-    filter_row<R, R>(g.big, true, j, nlon, row, ext);
+    if (!big) return;
+    filt(g.big, true, j, row);
     __syncthreads();
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_f[c0 + i0] = row[i0];
+    for (int kk = 0; kk < nk; ++kk) {
+      const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k0 + kk);
+      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.u_f[c0 + i0] = row[kk * nlon + i0];
+    }
     return;
   }
   const int j = blockIdx.x - nlat + 1;
-  auto vval = [&](int jj, R inv_d, int i0) {
+  auto vval = [&](int kk, int jj, R inv_d, int i0) {
+    const int k = k0 + kk;
     const unsigned cv = (unsigned)ix3(nhalf, nlon, 1, jj, k);
     R p;
     if constexpr (std::is_same<R, float>::value) {
       const unsigned ps = (unsigned)ix3(nlat, nlon, 1, jj, k);
-      if (bc) p = pgf_pq(w.pea, w.gzhl, ps + i0, ps + nlon + i0, lf, dref, inv_d);
+      if (bc) p = pgf_pq(w.pea, w.gzhl, ps + i0, ps + nlon + i0, lf, dref[kk], inv_d);
       else p = pgf_lat(g, n, w, i0 + 1, jj, k, inv_d);
     } else {
       p = pgf_lat(g, n, w, i0 + 1, jj, k, inv_d);
     }
     return o.v_lat[cv + i0] + dtr * (w.dv[cv + i0] - p);
   };
-  const unsigned cj = (unsigned)ix3(nhalf, nlon, 1, j, k);
   auto load_v = [&](int jj, R *dst) {
     const R inv_d = (R)1 / ROWR(R, de_lat, jj);
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) dst[i0] = vval(jj, inv_d, i0);
-    if (bc) filter_row<R, R>(g.small2, false, jj, nlon, dst, ext);
+    for (int kk = 0; kk < nk; ++kk)
+      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) dst[kk * nlon + i0] = vval(kk, jj, inv_d, i0);
+    if (bc) filt(g.small2, false, jj, dst);
     __syncthreads();
   };
   load_v(j, row);
   if (j == 1 || j == nhalf) {
     load_v(j == 1 ? 2 : nhalf - 1, nb);
     const R wgt = (R)0.6;
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[i0] = ((R)1 - wgt) * row[i0] + wgt * nb[i0];
+    for (int t = threadIdx.x; t < nk * nlon; t += blockDim.x) row[t] = ((R)1 - wgt) * row[t] + wgt * nb[t];
     __syncthreads();
   }
-  if (!filter_on(g.big, false, j)) {
+  const bool big = filter_on(g.big, false, j);
+  for (int kk = 0; kk < nk; ++kk) {
+    const unsigned cj = (unsigned)ix3(nhalf, nlon, 1, j, k0 + kk);
     for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
-      const R v = row[i0];
+      const R v = row[kk * nlon + i0];
       n.v_lat[cj + i0] = v;
-      n.v_f[cj + i0] = v;
+      if (!big) n.v_f[cj + i0] = v;
     }
-    return;
   }
-  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.v_lat[cj + i0] = row[i0];
-  filter_row<R, R>(g.big, false, j, nlon, row, ext);
+  if (!big) return;
+  filt(g.big, false, j, row);
   __syncthreads();
-  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.v_f[cj + i0] = row[i0];
+  for (int kk = 0; kk < nk; ++kk) {
+    const unsigned cj = (unsigned)ix3(nhalf, nlon, 1, j, k0 + kk);
+    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) n.v_f[cj + i0] = row[kk * nlon + i0];
+  }
 }
 
 // Run-prologue filters (gmcore_mod.F90:112-122): u_f, v_f, phs_f | gz_f.
@@ -1238,8 +1271,11 @@ void launch_column_backward(const DGrid &g, const Launch &L, const Slot<R> &n, c
 }
 template <class R>
 void launch_update_uv(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
-  allow_smem(k_update_uv<R>, filter_smem(g, 2, sizeof(R)));
-  k_update_uv<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt);
+  constexpr int KB = kUvLevels<R>;
+  const int hmax = (g.big.max_taps - 1) / 2;
+  const size_t smem = (size_t)KB * (2 * g.nlon + g.nlon + 2 * hmax + 8) * sizeof(R);
+  allow_smem(k_update_uv<R>, smem);
+  k_update_uv<R><<<dim3(g.nlat + g.nhalf, (g.nlev + KB - 1) / KB), L.threads, smem, L.stream>>>(g, o, n, w, dt);
 }
 template <class R>
 void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s) {

@@ -246,8 +246,12 @@ __device__ __forceinline__ float cflz_of_f(const float *HL, const float *FD, con
 // the row is not filtered (ngrid <= 1).  A is the accumulation type (FP64
 // unless the caller asks for the FP32 pipeline).
 // ---------------------------------------------------------------------------
-template <class R, class A = double>
-__device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, int j, int nlon, R *row, R *ext) {
+// KB rows of the same latitude (KB levels of one row) filtered together: the
+// weights are loaded once per tap for all of them.  row[kk * rs + i],
+// ext[kk * es + t]; every row equals filter_row of that row alone.
+template <int KB, class R, class A = double>
+__device__ __forceinline__ bool filter_rows(const FilterDev &f, bool full_lat, int j, int nlon, R *row, int rs, R *ext,
+                                            int es) {
   const int n = full_lat ? f.ntaps_full[j - 1] : f.ntaps_half[j - 1];
   if (n <= 1) return false;
   const int hn = (n - 1) / 2;
@@ -255,38 +259,56 @@ __device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, in
   const A *w;
   if constexpr (std::is_same<A, float>::value) w = f.wgt_f + off; else w = f.wgt + off;
   __syncthreads();
-  for (int t = threadIdx.x; t < nlon + 2 * hn; t += blockDim.x) {
-    int i = t - hn + 1;
-    i = i < 1 ? i + nlon : (i > nlon ? i - nlon : i);
-    ext[t] = row[i - 1];
-  }
+  for (int kk = 0; kk < KB; ++kk)
+    for (int t = threadIdx.x; t < nlon + 2 * hn; t += blockDim.x) {
+      int i = t - hn + 1;
+      i = i < 1 ? i + nlon : (i > nlon ? i - nlon : i);
+      ext[kk * es + t] = row[kk * rs + i - 1];
+    }
   __syncthreads();
   // three consecutive outputs per thread over a rolling window of ext: one
-  // ext and one weight load per tap for three sums (each sum in tap order,
-  // as the one-output loop below forms it)
+  // ext load per row and one weight load per tap for 3 KB sums (each sum in
+  // tap order, as the one-output loop below forms it)
   const int nfull = nlon - nlon % 3;
   for (int b = 3 * threadIdx.x; b < nfull; b += 3 * blockDim.x) {
-    A s0 = 0, s1 = 0, s2 = 0;
-    A e0 = (A)ext[b], e1 = (A)ext[b + 1];
-    for (int t = 0; t < n; ++t) {
-      const A wt = w[t], e2 = (A)ext[b + t + 2];
-      s0 = s0 + wt * e0;
-      s1 = s1 + wt * e1;
-      s2 = s2 + wt * e2;
-      e0 = e1;
-      e1 = e2;
+    A s0[KB], s1[KB], s2[KB], e0[KB], e1[KB];
+#pragma unroll
+    for (int kk = 0; kk < KB; ++kk) {
+      s0[kk] = s1[kk] = s2[kk] = 0;
+      e0[kk] = (A)ext[kk * es + b];
+      e1[kk] = (A)ext[kk * es + b + 1];
     }
-    row[b] = (R)s0;
-    row[b + 1] = (R)s1;
-    row[b + 2] = (R)s2;
+    for (int t = 0; t < n; ++t) {
+      const A wt = w[t];
+#pragma unroll
+      for (int kk = 0; kk < KB; ++kk) {
+        const A e2 = (A)ext[kk * es + b + t + 2];
+        s0[kk] = s0[kk] + wt * e0[kk];
+        s1[kk] = s1[kk] + wt * e1[kk];
+        s2[kk] = s2[kk] + wt * e2;
+        e0[kk] = e1[kk];
+        e1[kk] = e2;
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < KB; ++kk) {
+      row[kk * rs + b] = (R)s0[kk];
+      row[kk * rs + b + 1] = (R)s1[kk];
+      row[kk * rs + b + 2] = (R)s2[kk];
+    }
   }
-  for (int i = nfull + threadIdx.x; i < nlon; i += blockDim.x) {
-    A s = 0;
-    for (int t = 0; t < n; ++t) s = s + w[t] * (A)ext[i + t];
-    row[i] = (R)s;
-  }
+  for (int i = nfull + threadIdx.x; i < nlon; i += blockDim.x)
+    for (int kk = 0; kk < KB; ++kk) {
+      A s = 0;
+      for (int t = 0; t < n; ++t) s = s + w[t] * (A)ext[kk * es + i + t];
+      row[kk * rs + i] = (R)s;
+    }
   __syncthreads();
   return true;
+}
+template <class R, class A = double>
+__device__ __forceinline__ bool filter_row(const FilterDev &f, bool full_lat, int j, int nlon, R *row, R *ext) {
+  return filter_rows<1, R, A>(f, full_lat, j, nlon, row, 0, ext, 0);
 }
 
 // Vertical RK4 departure in eta and its Courant number
