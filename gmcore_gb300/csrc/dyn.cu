@@ -807,20 +807,39 @@ __global__ void k_surface_rel(const double *phs_f, float *psr, size_t n, double 
     psr[t] = (float)(phs_f[t] - ptop);
 }
 
-// pt = small1 filter(pt_old m_old + dt dpt) / m_new   (:153-173)
+// pt = small1 filter(pt_old m_old + dt dpt) / m_new   (:153-173); a block
+// takes one row at kPtLevels(R) consecutive levels (shared filter weights).
+template <class R>
+constexpr int kPtLevels = std::is_same<R, float>::value ? 2 : 1;
+
 template <class R>
 __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  constexpr int KB = kPtLevels<R>;
   extern __shared__ double sh[];
-  const int j = blockIdx.x + 1, k = blockIdx.y + 1, nlon = g.nlon, nlat = g.nlat;
-  R *row = reinterpret_cast<R *>(sh), *ext = row + nlon;
+  const int j = blockIdx.x + 1, k0 = blockIdx.y * KB + 1, nlon = g.nlon, nlat = g.nlat, nlev = g.nlev;
+  const int nk = min(KB, nlev - k0 + 1);
+  const int es = nlon + 2 * ((g.big.max_taps - 1) / 2) + 8;
+  R *row = reinterpret_cast<R *>(sh), *ext = row + KB * nlon;
   const R dtr = (R)dt;
   const SurfP<R> so = o.surf(), sn = n.surf();
-  const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k), m0 = (unsigned)(j - 1) * nlon;
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x)
-    row[i] = o.pt[c0 + i] * Mass<R>::layer(g, k, so.at(m0 + i)) + dtr * w.dpt[c0 + i];
-  filter_row<R, R>(g.small1, true, j, nlon, row, ext);
+  const unsigned m0 = (unsigned)(j - 1) * nlon;
+  for (int kk = 0; kk < nk; ++kk) {
+    const int k = k0 + kk;
+    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x)
+      row[kk * nlon + i] = o.pt[c0 + i] * Mass<R>::layer(g, k, so.at(m0 + i)) + dtr * w.dpt[c0 + i];
+  }
+  if (nk == KB) {
+    filter_rows<KB, R, R>(g.small1, true, j, nlon, row, nlon, ext, es);
+  } else {
+    for (int kk = 0; kk < nk; ++kk) filter_row<R, R>(g.small1, true, j, nlon, row + kk * nlon, ext);
+  }
   __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.pt[c0 + i] = row[i] / Mass<R>::layer(g, k, sn.at(m0 + i));
+  for (int kk = 0; kk < nk; ++kk) {
+    const int k = k0 + kk;
+    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.pt[c0 + i] = row[kk * nlon + i] / Mass<R>::layer(g, k, sn.at(m0 + i));
+  }
 }
 
 // Shallow water: gz = gz_old + dt dgz; gz_f = big(gz); gz = small1(gz) (:178-192)
@@ -1256,8 +1275,11 @@ void launch_update_phs(const DGrid &g, const Launch &L, const Slot<R> &o, const 
 }
 template <class R>
 void launch_update_pt(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
-  allow_smem(k_update_pt<R>, filter_smem(g, 1, sizeof(R)));
-  k_update_pt<R><<<dim3(g.nlat, g.nlev), L.threads, filter_smem(g, 1, sizeof(R)), L.stream>>>(g, o, n, w, dt);
+  constexpr int KB = kPtLevels<R>;
+  const int hmax = (g.big.max_taps - 1) / 2;
+  const size_t smem = (size_t)KB * (g.nlon + g.nlon + 2 * hmax + 8) * sizeof(R);
+  allow_smem(k_update_pt<R>, smem);
+  k_update_pt<R><<<dim3(g.nlat, (g.nlev + KB - 1) / KB), L.threads, smem, L.stream>>>(g, o, n, w, dt);
 }
 template <class R>
 void launch_update_gz(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
