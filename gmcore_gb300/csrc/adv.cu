@@ -645,6 +645,41 @@ __global__ void k_accum(T *dst, const T *src, size_t n, int mode, double divisor
   }
 }
 
+// Several accumulations in one launch (blockIdx.y = entry): the batch's
+// winds, mass fluxes and vertical mass flux after a step.  Same arithmetic per
+// element as k_accum; four elements per thread where the entry's length and
+// addresses allow 16-byte vectors.
+template <class T>
+__global__ void k_accum_multi(AccumSet<T> set) {
+  const AccumEntry<T> &e = set.e[blockIdx.y];
+  const T dv = (T)e.divisor;
+  auto one = [&](T d, T s) {
+    if (e.mode == 0) return s;
+    if (e.mode == 1) return d + s;
+    return (T)((d + s) / dv);
+  };
+  const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if constexpr (std::is_same<T, float>::value) {
+    if (e.n % 4 == 0 && ((uintptr_t)e.dst % 16) == 0 && (!e.src || ((uintptr_t)e.src % 16) == 0)) {
+      float4 *d4 = reinterpret_cast<float4 *>(e.dst);
+      const float4 *s4 = reinterpret_cast<const float4 *>(e.src);
+      for (size_t t = t0; t < e.n / 4; t += stride) {
+        const float4 s = s4 ? s4[t] : make_float4(0, 0, 0, 0);
+        float4 d = e.mode == 0 ? s : d4[t];
+        if (e.mode != 0) {
+          d.x = one(d.x, s.x); d.y = one(d.y, s.y); d.z = one(d.z, s.z); d.w = one(d.w, s.w);
+        }
+        d4[t] = d;
+      }
+      return;
+    }
+  }
+  for (size_t t = t0; t < e.n; t += stride) {
+    const T s = e.src ? e.src[t] : (T)0;
+    e.dst[t] = e.mode == 0 ? s : one(e.dst[t], s);
+  }
+}
+
 // Half-level mass m_lev of calc_m (operators_mod.F90:505-525) folded into
 // the batch accumulator; sp.phs_f null zeroes the sample.  The FP32 form
 // takes (m(k-1) + m(k)) / 2 of the FP32 layer masses.
@@ -1035,6 +1070,17 @@ void launch_accum(const Launch &L, T *dst, const T *src, size_t n, int mode, dou
 }
 template void launch_accum<double>(const Launch &, double *, const double *, size_t, int, double);
 template void launch_accum<float>(const Launch &, float *, const float *, size_t, int, double);
+
+template <class T>
+void launch_accum_multi(const Launch &L, const AccumSet<T> &set) {
+  if (set.count <= 0) return;
+  size_t nmax = 0;
+  for (int t = 0; t < set.count; ++t) nmax = std::max(nmax, set.e[t].n);
+  const int blocks = (int)std::min<size_t>((nmax / 4 + 255) / 256 + 1, 152 * 4);
+  k_accum_multi<T><<<dim3(blocks, set.count), 256, 0, L.stream>>>(set);
+}
+template void launch_accum_multi<double>(const Launch &, const AccumSet<double> &);
+template void launch_accum_multi<float>(const Launch &, const AccumSet<float> &);
 
 template <class R>
 void launch_half_level_mass(const DGrid &g, const Launch &L, const SurfP<R> &sp, R *m_lev, int mode, double divisor) {

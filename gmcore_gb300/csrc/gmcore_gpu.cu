@@ -847,23 +847,22 @@ struct Engine : EngineBase {
       else { mode = 1; step = step + 1; }
     };
     const double div = nstep_adv + 1;
-    int mode;
-    cycle(uv_step, mode);
+    int mode_uv, mode_mf, mode_we;
+    cycle(uv_step, mode_uv);
+    cycle(mf_step, mode_mf);
+    cycle(we_step, mode_we);
+    AccumSet<R> set{};
+    set.e[0] = {b.u, s.u_f, full3(), mode_uv, div};
+    set.e[1] = {b.v, s.v_f, half3(), mode_uv, div};
+    set.e[2] = {b.mfx, prologue ? nullptr : s.mfx_lon, full3(), mode_mf, div};
+    set.e[3] = {b.mfy, prologue ? nullptr : s.mfy_lat, half3(), mode_mf, div};
+    set.e[4] = {b.we, prologue ? nullptr : s.we_lev, lev3(), mode_we, div};
+    set.count = 5;
     K("tracer_accum", 2, [&] {
-      launch_accum<R>(L, b.u, s.u_f, full3(), mode, div);
-      launch_accum<R>(L, b.v, s.v_f, half3(), mode, div);
+      launch_accum_multi<R>(L, set);
+      launch_half_level_mass<R>(dg, L, prologue ? SurfP<R>{nullptr, nullptr} : s.surf(), b.m_lev, mode_we, div);
     });
     if (uv_step == 0) K("tracer_batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, L, b.u, b.v, b.cflx, b.cfly, b.divx, b.divy, dt_adv); });
-    cycle(mf_step, mode);
-    K("tracer_accum", 2, [&] {
-      launch_accum<R>(L, b.mfx, prologue ? nullptr : s.mfx_lon, full3(), mode, div);
-      launch_accum<R>(L, b.mfy, prologue ? nullptr : s.mfy_lat, half3(), mode, div);
-    });
-    cycle(we_step, mode);
-    K("tracer_accum", 2, [&] {
-      launch_accum<R>(L, b.we, prologue ? nullptr : s.we_lev, lev3(), mode, div);
-      launch_half_level_mass<R>(dg, L, prologue ? SurfP<R>{nullptr, nullptr} : s.surf(), b.m_lev, mode, div);
-    });
     if (we_step == 0) K("tracer_batch_cflz", 1, [&] { launch_batch_cflz<R>(dg, L, b.we, b.m_lev, b.cflz, dt_adv); });
   }
 

@@ -108,6 +108,21 @@ struct TracerBatch {
 };
 // Accumulation of one field: mode 0 copy, 1 add, 2 average with divisor.
 template <class T> void launch_accum(const Launch &L, T *dst, const T *src, size_t n, int mode, double divisor);
+// accumulation entries of one launch (copy / add / average, as launch_accum)
+template <class T>
+struct AccumEntry {
+  T *dst;
+  const T *src;   // null: a zero sample
+  size_t n;
+  int mode;
+  double divisor;
+};
+template <class T>
+struct AccumSet {
+  AccumEntry<T> e[6];
+  int count;
+};
+template <class T> void launch_accum_multi(const Launch &L, const AccumSet<T> &set);
 // Half-level mass of a slot (calc_m, operators_mod.F90:505-525) into a
 // level field, or zero it when src_phs_f is null.
 template <class R> void launch_half_level_mass(const DGrid &g, const Launch &L, const SurfP<R> &sp, R *m_lev, int mode, double divisor);
