@@ -32,11 +32,14 @@ namespace {
 // shifted by nlon/2).
 constexpr int kHflxRows = 4;
 
-// x fluxes of full row j (2 .. nlat-1) at level k; out(i, o, flux) per face.
-// xs: nlon values of shared memory.
-template <class R, class Out>
-__device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R *__restrict__ u,
-                                          const R *__restrict__ cflx, const R *__restrict__ mx, R *xs, Out out) {
+// x fluxes of full row j (2 .. nlat-1) at level k of NF fields that share the
+// Courant numbers cflx: field f is fld[f] advected by the multiplier mul[f]
+// (a velocity or a mass flux); out(i, o, flux[NF]) per face.  xs: NF * nlon
+// values of shared memory.  The upwind cell, the whole-cell count and the
+// fractional Courant number are formed once per face for all fields.
+template <int NF, class R, class Out>
+__device__ __forceinline__ void hflx_xrows(const DGrid &g, int j, int k, const R *const (&mul)[NF],
+                                           const R *__restrict__ cflx, const R *const (&fld)[NF], R *xs, Out out) {
   const int nlat = g.nlat, nlon = g.nlon, lim = g.limiter;
   auto W = [nlon](int l) { return l < 0 ? l + nlon : (l >= nlon ? l - nlon : l); };   // one wrap, 0-based
   auto Wg = [nlon](int l) {   // any l (a Courant number may exceed nlon on coarse grids)
@@ -44,77 +47,95 @@ __device__ __forceinline__ void hflx_xrow(const DGrid &g, int j, int k, const R 
     l %= nlon;
     return l < 0 ? l + nlon : l;
   };
-  // face inputs of this thread's first faces are requested before the row is
-  // staged so that their latency overlaps it
+  // face inputs of this thread's first faces are requested before the rows
+  // are staged so that their latency overlaps it
   constexpr int kPre = 3;
-  R cpre[kPre], upre[kPre];
+  R cpre[kPre], mpre[NF][kPre];
 #pragma unroll
   for (int t = 0; t < kPre; ++t) {
     const int i = 1 + threadIdx.x + t * blockDim.x;
     if (i <= nlon) {
       const size_t o = ix3(nlat, nlon, i, j, k);
       cpre[t] = cflx[o];
-      upre[t] = u[o];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) mpre[f][t] = mul[f][o];
     }
   }
-  const R *src = mx + ix3(nlat, nlon, 1, j, k);
+  const size_t ro = ix3(nlat, nlon, 1, j, k);
   __syncthreads();   // xs may still be read by a previous use
-  for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[l] = src[l];
+#pragma unroll
+  for (int f = 0; f < NF; ++f)
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[f * nlon + l] = fld[f][ro + l];
   __syncthreads();
   const bool vl = g.flux_type == GMC_FLUX_VAN_LEER;
-  // PPM coefficients of cell l (0-based) from cells l-2 .. l+2; the same
-  // operations as ppm() on the slopes of cells l-1, l, l+1
-  auto coef = [&](int l, R &fl, R &df, R &f6) {
-    const R a = xs[W(l - 2)], b = xs[W(l - 1)], c = xs[l], d = xs[W(l + 1)], e = xs[W(l + 2)];
+  // PPM coefficients of cell l (0-based) of row x from cells l-2 .. l+2; the
+  // same operations as ppm() on the slopes of cells l-1, l, l+1
+  auto coef = [&](const R *x, int l, R &fl, R &df, R &f6) {
+    const R a = x[W(l - 2)], b = x[W(l - 1)], c = x[l], d = x[W(l + 1)], e = x[W(l + 2)];
     const R sm = slope(lim, a, b, c), s0 = slope(lim, b, c, d), sp = slope(lim, c, d, e);
     ppm_cell(c, s0, ppm_edge(b, c, sm, s0), ppm_edge(c, d, s0, sp), fl, df, f6);
   };
   const R hxr = (R)g.hx;
   int t = 0;
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
-    const size_t o = ix3(nlat, nlon, i, j, k);
-    R c, uo;
+    const size_t o = ro + (i - 1);
+    R c, mo[NF];
     if (t < kPre) {
 #pragma unroll
       for (int q = 0; q < kPre; ++q)
-        if (q == t) { c = cpre[q]; uo = upre[q]; }
+        if (q == t) {
+          c = cpre[q];
+#pragma unroll
+          for (int f = 0; f < NF; ++f) mo[f] = mpre[f][q];
+        }
     } else {
       c = cflx[o];
-      uo = u[o];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) mo[f] = mul[f][o];
     }
-    R flux;
+    R flux[NF];
     if (!(fabs(c) <= hxr)) {   // |cflx| beyond the reach the reference allows: error, no flux
       atomicOr(g.err, ERR_CFLX);
-      flux = 0;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) flux[f] = 0;
     } else {
       const int ci = (int)c;
       const R cf = c - (R)ci;
       if (c > 0) {
         const int iu = Wg(i - ci - 1);   // 0-based upwind cell
-        R sum = 0;
-        for (int l = i + 1 - ci; l <= i; ++l) sum = sum + xs[Wg(l - 1)];
-        if (vl) {   // hflx_van_leer_cell (ffsl_mod.F90:585-590)
-          const R su = slope(lim, xs[W(iu - 1)], xs[iu], xs[W(iu + 1)]);
-          flux = fdiv(uo * (cf * (xs[iu] + su * (R)0.5 * ((R)1 - cf)) + sum), c);
-        } else {
-          R fl, df, f6;
-          coef(iu, fl, df, f6);
-          flux = fdiv(uo * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const R *x = xs + f * nlon;
+          R sum = 0;
+          for (int l = i + 1 - ci; l <= i; ++l) sum = sum + x[Wg(l - 1)];
+          if (vl) {   // hflx_van_leer_cell (ffsl_mod.F90:585-590)
+            const R su = slope(lim, x[W(iu - 1)], x[iu], x[W(iu + 1)]);
+            flux[f] = fdiv(mo[f] * (cf * (x[iu] + su * (R)0.5 * ((R)1 - cf)) + sum), c);
+          } else {
+            R fl, df, f6;
+            coef(x, iu, fl, df, f6);
+            flux[f] = fdiv(mo[f] * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
+          }
         }
       } else if (c < 0) {
         const int iu = Wg(i - ci);       // 0-based upwind cell (i - ci + 1 in 1-based)
-        R sum = 0;
-        for (int l = i + 1; l <= i - ci; ++l) sum = sum + xs[Wg(l - 1)];
-        if (vl) {   // (ffsl_mod.F90:591-594)
-          const R su = slope(lim, xs[W(iu - 1)], xs[iu], xs[W(iu + 1)]);
-          flux = fdiv(uo * (cf * (xs[iu] - su * (R)0.5 * ((R)1 + cf)) - sum), c);
-        } else {
-          R fl, df, f6;
-          coef(iu, fl, df, f6);
-          flux = fdiv(-uo * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const R *x = xs + f * nlon;
+          R sum = 0;
+          for (int l = i + 1; l <= i - ci; ++l) sum = sum + x[Wg(l - 1)];
+          if (vl) {   // (ffsl_mod.F90:591-594)
+            const R su = slope(lim, x[W(iu - 1)], x[iu], x[W(iu + 1)]);
+            flux[f] = fdiv(mo[f] * (cf * (x[iu] - su * (R)0.5 * ((R)1 + cf)) - sum), c);
+          } else {
+            R fl, df, f6;
+            coef(x, iu, fl, df, f6);
+            flux[f] = fdiv(-mo[f] * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
+          }
         }
       } else {
-        flux = 0;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) flux[f] = 0;
       }
     }
     out(i, o, flux);
@@ -157,15 +178,6 @@ __device__ __forceinline__ R hflx_yface(const DGrid &g, R c, R vv, const R *y, c
     return fdiv(-vv * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
   }
   return 0;
-}
-
-// Outer pass: fluxes fx of qy along x with the zonal mass flux (one row per block).
-template <class R>
-__global__ void GMC_BOUNDS(R, 8) k_hflx_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ mx,
-                         R *__restrict__ fx) {
-  extern __shared__ double sh_raw[];
-  const int k = blockIdx.y + 1, j = blockIdx.x + 2;   // rows 2 .. nlat-1
-  hflx_xrow<R>(g, j, k, u, cflx, mx, reinterpret_cast<R *>(sh_raw), [&](int, size_t o, R f) { fx[o] = f; });
 }
 
 // Outer pass: fluxes fy of qx along y with the meridional mass flux (strips).
@@ -214,34 +226,40 @@ __global__ void GMC_BOUNDS(R, 6) k_hflx_y(DGrid g, const R *__restrict__ v, cons
 // the advective fluxes of q stay on chip and the kernels write
 //   qx = q - dt/2 (dflux_x/dx - divx q),  qy = q - dt/2 (dflux_y/dy - divy q)
 // (pole rows: qx = q, qy from the ring mean of the polar half row's flux).
-// x: one full row per block.
+// x: one full row per block, together with the outer x pass (fluxes fx of qy
+// with the zonal mass flux), which shares the Courant numbers; qy comes from
+// the y inner pass launched before.
 template <class R>
-__global__ void GMC_BOUNDS(R, 8) k_ffsl_inner_x(DGrid g, const R *__restrict__ u, const R *__restrict__ cflx, const R *__restrict__ q,
-                               const R *__restrict__ divx, R *__restrict__ qx, double dt) {
+__global__ void GMC_BOUNDS(R, 6) k_ffsl_x2(DGrid g, const R *__restrict__ u, const R *__restrict__ mfx,
+                                           const R *__restrict__ cflx, const R *__restrict__ q,
+                                           const R *__restrict__ qy, const R *__restrict__ divx, R *__restrict__ qx,
+                                           R *__restrict__ fx, double dt) {
   extern __shared__ double sh_raw[];
-  const int k = blockIdx.y + 1;
+  const int k = blockIdx.y + 1, j = blockIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon;
   const R hdt = (R)dt;
-  {
-    const int j = blockIdx.x + 1;
-    if (j == 1 || j == nlat) {
-      for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-        const size_t o = ix3(nlat, nlon, i, j, k);
-        qx[o] = q[o];
-      }
-      return;
-    }
-    R *work = reinterpret_cast<R *>(sh_raw);
-    R *frow = work + nlon;
-    hflx_xrow<R>(g, j, k, u, cflx, q, work, [&](int i, size_t, R f) { frow[i - 1] = f; });
-    __syncthreads();
-    const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j);
+  if (j == 1 || j == nlat) {   // no x flux on the pole rows (fx left as it is)
     for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
       const size_t o = ix3(nlat, nlon, i, j, k);
-      const R qv = q[o];
-      const R fxe = frow[i - 1], fxw = frow[i == 1 ? nlon - 1 : i - 2];
-      qx[o] = qv - (R)0.5 * (fdiv((fxe - fxw) * lel, ac) - divx[o] * qv) * hdt;
+      qx[o] = q[o];
     }
+    return;
+  }
+  R *xs = reinterpret_cast<R *>(sh_raw);   // [2][nlon]: q, qy
+  R *frow = xs + 2 * nlon;
+  const R *mul[2] = {u, mfx};
+  const R *fld[2] = {q, qy};
+  hflx_xrows<2, R>(g, j, k, mul, cflx, fld, xs, [&](int i, size_t o, const R (&f)[2]) {
+    frow[i - 1] = f[0];
+    fx[o] = f[1];
+  });
+  __syncthreads();
+  const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j);
+  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+    const size_t o = ix3(nlat, nlon, i, j, k);
+    const R qv = xs[i - 1];
+    const R fxe = frow[i - 1], fxw = frow[i == 1 ? nlon - 1 : i - 2];
+    qx[o] = qv - (R)0.5 * (fdiv((fxe - fxw) * lel, ac) - divx[o] * qv) * hdt;
   }
 }
 
@@ -1029,13 +1047,12 @@ void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, co
                       R *fx, R *fy, double dt) {
   (void)qmfx;
   (void)qmfy;
-  const dim3 rows(g.nlat, g.nlev), inner_rows(g.nlat - 2, g.nlev), strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
-  const size_t smem_o = (size_t)g.nlon * sizeof(R), smem_i = (size_t)2 * g.nlon * sizeof(R);
-  if (smem_o > 48 * 1024) cudaFuncSetAttribute(k_hflx_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
-  if (smem_i > 48 * 1024) cudaFuncSetAttribute(k_ffsl_inner_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i);
-  k_ffsl_inner_x<R><<<rows, L.threads, smem_i, L.stream>>>(g, b.u, b.cflx, q, b.divx, qx, dt);
+  const dim3 rows(g.nlat, g.nlev), strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
+  const size_t smem_x = (size_t)3 * g.nlon * sizeof(R);
+  if (smem_x > 48 * 1024) cudaFuncSetAttribute(k_ffsl_x2<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x);
+  // y inner pass (qy), then both x passes (qx and fx), then the y outer pass on qx
   k_ffsl_inner_y<R><<<strips, L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
-  k_hflx_x<R><<<inner_rows, L.threads, smem_o, L.stream>>>(g, b.mfx, b.cflx, qy, fx);
+  k_ffsl_x2<R><<<rows, L.threads, smem_x, L.stream>>>(g, b.u, b.mfx, b.cflx, q, qy, b.divx, qx, fx, dt);
   k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
 }
 
