@@ -131,19 +131,21 @@ class ClockSampler:
 # Algorithmic (compulsory) bytes of one launch of each kernel group, in units
 # of N s (N = nlon nlat nlev cells, s = bytes of a bulk value), N 8 (FP64
 # level fields) and H 8 (FP64 surface fields): the fields the group must read
-# and write once.  FFSL counts its operator inputs (q, u, v, mfx, mfy, cflx,
-# cfly, divx, divy) and outputs (fx, fy), not the qx/qy intermediates.
+# and write once.  The FFSL kernels count their own inputs and outputs
+# (ffsl_inner_y: q, v, cfly, divy -> qy; ffsl_x2: q, qy, u, mfx, cflx, divx ->
+# qx, fx; ffsl_hflx_y: qx, mfy, cfly -> fy).
 KERNEL_BYTES = {
     "mass_flux": (4, 0, 0.5), "tangent_winds": (4, 0, 0.5), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 0.5),
-    "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (4, 0, 1.5), "ffsl_hflx_pt": (11, 0, 0),
+    "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (4, 0, 1.5),
+    "ffsl_x2": (8, 0, 0), "ffsl_inner_y": (5, 0, 0), "ffsl_hflx_y": (4, 0, 0),
     "pt_tendency": (6, 0, 0), "momentum_tend": (10, 0, 0.5), "update_phs": (0, 0, 4.5), "update_pt": (3, 0, 1),
     "column_backward": (2, 1, 2), "update_uv": (9, 1, 0), "div_damp": (7, 0, 0), "tracer_accum": (4, 0, 0),
-    "tracer_batch_cfl": (6, 0, 0), "tracer_batch_cflz": (3, 0, 0), "ffsl_hflx_tracer": (11, 0, 0),
+    "tracer_batch_cfl": (6, 0, 0), "tracer_batch_cflz": (3, 0, 0),
     "tracer_horizontal": (4, 0, 1), "tracer_vertical": (4, 0, 0.5), "tracer_lon_damp": (0.3, 0, 0),
     "surface_rel": (0, 0, 1.5),
 }
 # groups that launch more than one kernel (not a single kernel's roofline)
-MULTI_KERNEL = {"ffsl_hflx_pt", "ffsl_hflx_tracer", "tracer_accum", "div_damp"}
+MULTI_KERNEL = {"tracer_accum", "div_damp"}
 
 
 def algorithmic_bytes(name, cfg, s):

@@ -1057,6 +1057,24 @@ void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, co
 }
 
 template <class R>
+void launch_ffsl_inner_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qy, double dt) {
+  const dim3 strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
+  k_ffsl_inner_y<R><<<strips, L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
+}
+template <class R>
+void launch_ffsl_x2(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, const R *qy, R *qx, R *fx,
+                    double dt) {
+  const size_t smem_x = (size_t)3 * g.nlon * sizeof(R);
+  if (smem_x > 48 * 1024) cudaFuncSetAttribute(k_ffsl_x2<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x);
+  k_ffsl_x2<R><<<dim3(g.nlat, g.nlev), L.threads, smem_x, L.stream>>>(g, b.u, b.mfx, b.cflx, q, qy, b.divx, qx, fx, dt);
+}
+template <class R>
+void launch_hflx_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *qx, R *fy) {
+  const dim3 strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
+  k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
+}
+
+template <class R>
 void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
   if constexpr (std::is_same<R, float>::value) {
     const size_t smem = g.nlev * sizeof(double) + (size_t)(6 * g.nlev + 7) * (kTileI + 1) * sizeof(float);
@@ -1073,6 +1091,13 @@ template void launch_ffsl_hflx<double>(const DGrid &, const Launch &, const Batc
                                        double *, double *, double *, double *, double *, double);
 template void launch_ffsl_hflx<float>(const DGrid &, const Launch &, const BatchView<float> &, const float *, float *,
                                       float *, float *, float *, float *, float *, double);
+#define INST_FFSL_PARTS(R)                                                                                           \
+  template void launch_ffsl_inner_y<R>(const DGrid &, const Launch &, const BatchView<R> &, const R *, R *, double);  \
+  template void launch_ffsl_x2<R>(const DGrid &, const Launch &, const BatchView<R> &, const R *, const R *, R *, R *, \
+                                  double);                                                                            \
+  template void launch_hflx_y<R>(const DGrid &, const Launch &, const BatchView<R> &, const R *, R *);
+INST_FFSL_PARTS(double)
+INST_FFSL_PARTS(float)
 template void launch_pt_tendency<double>(const DGrid &, const Launch &, const Slot<double> &, const Work<double> &);
 template void launch_pt_tendency<float>(const DGrid &, const Launch &, const Slot<float> &, const Work<float> &);
 

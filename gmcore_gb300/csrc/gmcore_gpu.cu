@@ -891,7 +891,7 @@ struct Engine : EngineBase {
           Lt.stream = tstreams[l];
           qx = tsc[l].qx; qy = tsc[l].qy; fx = tsc[l].fx; fy = tsc[l].fy;
         }
-        K("ffsl_hflx_tracer", 3, [&] { launch_ffsl_hflx<R>(dg, Lt, bv, qo, w.qmfx, w.qmfy, qx, qy, fx, fy, dt_adv); });
+        ffsl3(Lt, bv, qo, qx, qy, fx, fy, dt_adv);
         K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, Lt, qo, qn, fx, fy, b.old_surf(), n.surf(), dt_adv); });
         K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, Lt, qn, b.cflz, b.we, n.surf(), dt_adv); });
         K("tracer_lon_damp", 1, [&] { launch_tracer_lon_damp<R>(dg, Lt, qn); });
@@ -953,6 +953,14 @@ struct Engine : EngineBase {
     prof_pending.clear();
   }
 
+  // horizontal FFSL fluxes fx, fy of q (the launches of launch_ffsl_hflx,
+  // profiled per kernel): y inner pass, both x passes, y outer pass
+  void ffsl3(const Launch &La, const BatchView<R> &b, const R *qf, R *qx, R *qy, R *fx, R *fy, double dt) {
+    K("ffsl_inner_y", 1, [&] { launch_ffsl_inner_y<R>(dg, La, b, qf, qy, dt); });
+    K("ffsl_x2", 1, [&] { launch_ffsl_x2<R>(dg, La, b, qf, qy, qx, fx, dt); });
+    K("ffsl_hflx_y", 1, [&] { launch_hflx_y<R>(dg, La, b, qx, fy); });
+  }
+
   // operators_prepare forward list (operators_mod.F90:117-122)
   void forward_prepare(int m, const Slot<R> &s, double dt) { forward_prepare_w(work[m], s, dt); }
   void forward_prepare_w(Work<R> &w, const Slot<R> &s, double dt) {
@@ -977,7 +985,7 @@ struct Engine : EngineBase {
       BatchView<R> b{};
       b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
       b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
-      K("ffsl_hflx_pt", 3, [&] { launch_ffsl_hflx<R>(dg, L, b, s.pt, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt); });
+      ffsl3(L, b, s.pt, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt);
       K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, L, s, w); });
     } else {
       K("swm_dgz", 1, [&] { launch_swm_dgz<R>(dg, L, s, w); });
@@ -1007,7 +1015,7 @@ struct Engine : EngineBase {
     BatchView<R> b{};
     b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
     b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
-    K("ffsl_hflx_pt", 3, [&] { launch_ffsl_hflx<R>(dg, Ls, b, s.pt, w.qmfx, w.qmfy, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt); });
+    ffsl3(Ls, b, s.pt, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt);
     K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, Ls, s, w); });
     if (!dry) CK(cudaEventRecord(dpt_ev, dside));
     K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });

@@ -92,6 +92,10 @@ template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const S
 // Horizontal FFSL flux of q (ffsl_calc_tracer_hflx_cell): inner advective
 // operators, intermediate qx/qy, outer flux-form operators into (fx, fy).
 template <class R> void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy, R *fx, R *fy, double dt);
+// the three FFSL kernels of launch_ffsl_hflx separately (profiled as three groups)
+template <class R> void launch_ffsl_inner_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qy, double dt);
+template <class R> void launch_ffsl_x2(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, const R *qy, R *qx, R *fx, double dt);
+template <class R> void launch_hflx_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *qx, R *fy);
 // Potential-temperature tendency: flux divergence of (ptf_lon, ptf_lat) with
 // pole rings plus the vertical FFSL flux with ghost levels (calc_grad_ptf).
 template <class R> void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w);
