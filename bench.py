@@ -135,7 +135,7 @@ class ClockSampler:
 # (ffsl_inner_y: q, v, cfly, divy -> qy; ffsl_x2: q, qy, u, mfx, cflx, divx ->
 # qx, fx; ffsl_hflx_y: qx, mfy, cfly -> fy).
 KERNEL_BYTES = {
-    "mass_flux": (4, 0, 0.5), "tangent_winds": (4, 0, 0.5), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 0.5),
+    "mass_flux": (4, 0, 0.5), "tangent_winds": (4, 0, 0.5), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 0.5)
     "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (4, 0, 1.5),
     "ffsl_x2": (8, 0, 0), "ffsl_inner_y": (5, 0, 0), "ffsl_hflx_y": (4, 0, 0),
     "pt_tendency": (6, 0, 0), "momentum_tend": (10, 0, 0.5), "update_phs": (0, 0, 4.5), "update_pt": (3, 0, 1),
@@ -300,6 +300,16 @@ def run_ours(args):
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
     traffic = measured_traffic(top_name)
     b_step = step_compulsory_bytes(cfg, 4, NTRACER)
+    # DRAM bytes of a step from the ncu traffic per launch of each group (the
+    # profiled run covers 3 steps): the redundancy over the compulsory bytes and
+    # the kernel-time-weighted DRAM throughput of the step's kernels
+    ncu_bytes = 0.0
+    covered_ms = 0.0
+    for name, (ms, cnt) in prof.items():
+        tb = measured_traffic(name)
+        if tb is not None:
+            ncu_bytes += tb * cnt / 3.0
+            covered_ms += ms / 3.0
     ncell = cfg.nlon * cfg.nlat * cfg.nlev
     model.close()
 
@@ -364,7 +374,11 @@ def run_ours(args):
                          "traffic_source": "profiles/kernel_traffic_c2_mixed.json (ncu dram__bytes per launch)"},
             "step_roofline": {"compulsory_bytes_per_step": b_step, "achieved_gbs": b_step / (ms_per_step / 1000.0) / 1e9,
                               "frac": b_step / (ms_per_step / 1000.0) / 1e9 / peak,
-                              "note": "all intermediates on chip; 16 N s per stage, 2 N s per tracer, 10 N s batch"},
+                              "note": "all intermediates on chip; 16 N s per stage, 2 N s per tracer, 10 N s batch",
+                              "ncu_dram_bytes_per_step": ncu_bytes,
+                              "redundancy": ncu_bytes / b_step,
+                              "kernel_time_weighted_dram_frac": (ncu_bytes / (covered_ms / 1000.0) / 1e9 / peak
+                                                                 if covered_ms else None)},
             "cell_updates_per_s": ncell * args.steps / (dev_ms / 1000.0) * WORLD,
             "kernel_ms_per_step": {k: round(v[0] / 3.0, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clk,
