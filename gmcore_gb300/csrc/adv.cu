@@ -1043,20 +1043,6 @@ __global__ void k_tracer_lon_damp(DGrid g, R *q) {
 }  // namespace
 
 template <class R>
-void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy,
-                      R *fx, R *fy, double dt) {
-  (void)qmfx;
-  (void)qmfy;
-  const dim3 rows(g.nlat, g.nlev), strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
-  const size_t smem_x = (size_t)3 * g.nlon * sizeof(R);
-  if (smem_x > 48 * 1024) cudaFuncSetAttribute(k_ffsl_x2<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x);
-  // y inner pass (qy), then both x passes (qx and fx), then the y outer pass on qx
-  k_ffsl_inner_y<R><<<strips, L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
-  k_ffsl_x2<R><<<rows, L.threads, smem_x, L.stream>>>(g, b.u, b.mfx, b.cflx, q, qy, b.divx, qx, fx, dt);
-  k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
-}
-
-template <class R>
 void launch_ffsl_inner_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qy, double dt) {
   const dim3 strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
   k_ffsl_inner_y<R><<<strips, L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
@@ -1072,6 +1058,19 @@ template <class R>
 void launch_hflx_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *qx, R *fy) {
   const dim3 strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
   k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
+}
+
+// One horizontal FFSL flux evaluation (fx, fy of q; qx, qy scratch; the
+// first two scratch fields of the operator entry points are not used): the y
+// inner pass (qy), then both x passes (qx and fx), then the y outer pass on qx.
+template <class R>
+void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy,
+                      R *fx, R *fy, double dt) {
+  (void)qmfx;
+  (void)qmfy;
+  launch_ffsl_inner_y<R>(g, L, b, q, qy, dt);
+  launch_ffsl_x2<R>(g, L, b, q, qy, qx, fx, dt);
+  launch_hflx_y<R>(g, L, b, qx, fy);
 }
 
 template <class R>
