@@ -135,7 +135,7 @@ class ClockSampler:
 # (ffsl_inner_y: q, v, cfly, divy -> qy; ffsl_x2: q, qy, u, mfx, cflx, divx ->
 # qx, fx; ffsl_hflx_y: qx, mfy, cfly -> fy).
 KERNEL_BYTES = {
-    "mass_flux": (4, 0, 0.5), "tangent_winds": (4, 0, 0.5), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 0.5)
+    "mass_flux": (4, 0, 0.5), "tangent_winds": (4, 0, 0.5), "kinetic_energy": (3, 0, 0), "pv": (3, 0, 0.5),
     "pv_edges": (7, 0, 0), "batch_cfl": (6, 0, 0), "column_mass": (4, 0, 1.5),
     "ffsl_x2": (8, 0, 0), "ffsl_inner_y": (5, 0, 0), "ffsl_hflx_y": (4, 0, 0),
     "pt_tendency": (6, 0, 0), "momentum_tend": (10, 0, 0.5), "update_phs": (0, 0, 4.5), "update_pt": (3, 0, 1),
