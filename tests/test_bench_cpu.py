@@ -21,3 +21,28 @@ def test_bench_byte_table_names_profiled_groups():
     spec.loader.exec_module(mod)
     for name in ("ffsl_x2", "ffsl_inner_y", "ffsl_hflx_y", "update_uv", "momentum_tend"):
         assert name in mod.KERNEL_BYTES, name
+
+
+def test_page_aligned_arrays_own_their_pages():
+    import mmap
+
+    import numpy as np
+
+    import gmcore_gb300 as g
+    a, b = g.page_aligned((3, 5, 7)), g.page_aligned((11,))
+    for x in (a, b):
+        assert x.ctypes.data % mmap.PAGESIZE == 0
+        assert x.dtype == np.float64 and not x.any()
+    # the page after the end of one array is not the start of the other's
+    end_a = a.ctypes.data + a.nbytes
+    assert not (b.ctypes.data <= end_a < b.ctypes.data + b.nbytes)
+
+
+def test_host_register_checks_its_argument_before_cuda():
+    import numpy as np
+    import pytest
+
+    import gmcore_gb300 as g
+    a = np.zeros((4, 6))[:, ::2]   # not contiguous
+    with pytest.raises(ValueError):
+        g.host_register(a)
