@@ -178,3 +178,29 @@ def test_space_operator_energy_identities(baroclinic):
         val, scale = o.space_identities()["coriolis"]
         assert abs(val) > 1e-8 * scale
         o.close()
+
+
+@pytest.mark.parametrize("pv_scheme", ["midpoint", "upwind1", "tvd"])
+def test_coriolis_does_no_work_for_any_pv_interpolation(pv_scheme):
+    """The energy-conserving Coriolis term (calc_coriolis scheme 1,
+    operators_mod.F90:846-906) does no work whatever values the edge PV takes,
+    so the identity of debug_check_space_operators holds for every
+    interp_pv option (midpoint, first-order upwind, TVD with the van Leer
+    limiter) and for the van Leer FFSL flux."""
+    from oracle import Oracle
+    from gmcore_gb300 import abi
+    from helpers import baroclinic_config, initial_state, load_state
+    kw = {"midpoint": dict(pv_scheme=abi.PV_MIDPOINT), "upwind1": dict(pv_scheme=abi.PV_UPWIND, upwind_order_pv=1),
+          "tvd": dict(pv_scheme=abi.PV_TVD, tvd_limiter_type=abi.TVD_VAN_LEER,
+                      ffsl_flux_type=abi.FLUX_VAN_LEER)}[pv_scheme]
+    cfg = baroclinic_config(**kw)
+    o = Oracle(cfg)
+    load_state(o, initial_state(cfg))
+    o.prepare()
+    o.step(2)
+    r = o.space_identities()
+    for name in ("coriolis", "ke", "mass", "ptf"):
+        val, scale = r[name]
+        assert scale > 0, name
+        assert abs(val) <= 1e-13 * scale, (pv_scheme, name, val, scale)
+    o.close()
