@@ -1844,9 +1844,20 @@ int orc_ffsl_hflx(void *h, const double *q, const double *u, const double *v, co
   return m->err.code;
 }
 
-// Mesh/filter queries for the known-answer tests.
+// Mesh/filter queries for the known-answer tests.  Besides the per-row
+// tables, the vertical coordinate's eta levels (full_lev = hyam + hybm,
+// half_lev = hyai + hybi, hybrid_coord_mod.F90:129-132) so that a test can
+// build the reference's analytic states on them.
 int orc_metric(void *h, const char *name, double *out, int n) {
   orc::Model *m = (orc::Model *)h;
+  const std::vector<double> *lev = !std::strcmp(name, "full_lev")   ? &m->grid.full_lev
+                                   : !std::strcmp(name, "half_lev") ? &m->grid.half_lev
+                                                                    : nullptr;
+  if (lev) {
+    if (n != (int)lev->size()) return GMC_EINVAL;
+    for (int k = 0; k < n; ++k) out[k] = (*lev)[k];
+    return GMC_OK;
+  }
   const gmc::RowTable *t = m->grid.metric(name);
   if (!t) return GMC_EINVAL;
   for (int j = 1; j <= n; ++j) out[j - 1] = (*t)[j];
