@@ -1,20 +1,28 @@
-"""Known-answer check of the oracle's flux-form semi-Lagrangian transport
+"""Known-answer checks of the oracle's flux-form semi-Lagrangian transport
 (ffsl_calc_tracer_hflx_cell, src/dynamics/adv/ffsl_mod.F90) with the
-reference's own advection test: solid-body rotation of a cosine bell over the
-poles for one revolution (src/tests/adv/solid_rotation_test_mod.F90).
+reference's own advection tests, one 12-day period each, m = 1 and
+mfx = u, mfy = v, u set on non-pole rows only:
 
-Parameters follow that test: period 12 days, bell height h0 = 1000 and radius
-R0 = a/3 centred at (3 pi/2, 0) (solid_rotation_test_mod.F90:16-20, 43-58),
-rotation axis tilted by alpha = 90 degrees, u set on non-pole rows only,
-m = 1, mfx = u, mfy = v (solid_rotation_test_mod.F90:83-101), and a background
-tracer q0 = 1 beside the bell (solid_rotation_test_mod.F90:38, 48).  With
-m = 1 the tracer update is the flux divergence of the FFSL face fluxes, with
-the pole cells closed by the ring sums of the meridional fluxes.  The norms
-are those of the reference's error tool (normalised L2 against the initial
-field).  The checks: the bell's total is conserved to round-off, the
-monotone limiter keeps it non-negative, the background stays 1 up to the
-discrete divergence of the analytic wind, and the error falls by more than
-second-order-like rates from 5 to 2.5 degrees."""
+* solid-body rotation of a cosine bell over the poles
+  (src/tests/adv/solid_rotation_test_mod.F90): bell height h0 = 1000 and
+  radius R0 = a/3 centred at (3 pi/2, 0), rotation axis tilted by
+  alpha = 90 degrees (solid_rotation_test_mod.F90:16-20, 43-58, 83-101), and
+  the background tracer q0 = 1 (:38, 48);
+* the reversing deformational flow of case 2 (src/tests/adv/deform_test_mod.F90):
+  hills centred at (5 pi/6, 0) and (7 pi/6, 0) (:42-45), the Gaussian hills
+  0.95 exp(-5 |x - x_i|^2) (:113-125) and the cosine hills of radius a/2 on a
+  0.1 background (:74-88), winds
+  u = k sin^2(lon) sin(2 lat) cos(pi t / T), v = k sin(2 lon) cos(lat) cos(pi t / T),
+  k = 10 a / T (:169-207), taken at mid-step.  The flow returns every tracer
+  to its initial position at t = T, so the initial field is the exact answer.
+
+With m = 1 the tracer update is the flux divergence of the FFSL face fluxes,
+with the pole cells closed by the ring sums of the meridional fluxes.  The
+norms are those of the reference's error tool (normalised against the
+initial field).  The checks: totals conserved to round-off, no new extrema
+beyond round-off and the small undershoots of the split 2-D scheme, the
+background kept to the analytic wind's discrete divergence, and the error
+falling as the grid is refined."""
 import math
 
 import numpy as np
@@ -27,45 +35,52 @@ PERIOD = 12 * 86400.0
 H0 = 1000.0
 
 
-def solid_rotation(nlon, nlat, dt, alpha=math.pi / 2):
-    """One revolution; returns (bell, background, bell0, cell area)."""
-    cfg = abi.default_config(nlon=nlon, nlat=nlat, nlev=1, baroclinic=0, dt_dyn=dt, dt_adv=dt,
-                             limiter_type=abi.LIMITER_MONO)
-    o = Oracle(cfg)
-    try:
-        a = cfg.radius
-        dlon = 2 * math.pi / nlon
-        full_lat, half_lat = o.metric("full_lat", nlat), o.metric("half_lat", nlat - 1)
-        de_lon, le_lon = o.metric("de_lon", nlat), o.metric("le_lon", nlat)
-        de_lat, le_lat = o.metric("de_lat", nlat - 1), o.metric("le_lat", nlat - 1)
-        area = o.metric("area_cell", nlat)
-        full_lon = np.arange(nlon) * dlon
-        half_lon = full_lon + 0.5 * dlon
-        u0 = 2 * math.pi * a / PERIOD
-        lon_u, lat_u = np.meshgrid(half_lon, full_lat)
-        lon_v, _ = np.meshgrid(full_lon, half_lat)
-        u = u0 * (np.cos(lat_u) * math.cos(alpha) + np.sin(lat_u) * np.cos(lon_u) * math.sin(alpha))
+class Transport:
+    """One tracer-transport harness on a lat-lon grid of the oracle."""
+
+    def __init__(self, nlon, nlat, dt):
+        cfg = abi.default_config(nlon=nlon, nlat=nlat, nlev=1, baroclinic=0, dt_dyn=dt, dt_adv=dt,
+                                 limiter_type=abi.LIMITER_MONO)
+        self.o = Oracle(cfg)
+        self.cfg, self.dt, self.nlon, self.nlat = cfg, dt, nlon, nlat
+        m = self.o.metric
+        self.full_lat, self.half_lat = m("full_lat", nlat), m("half_lat", nlat - 1)
+        self.de_lon, self.le_lon = m("de_lon", nlat), m("le_lon", nlat)
+        self.de_lat, self.le_lat = m("de_lat", nlat - 1), m("le_lat", nlat - 1)
+        self.area = m("area_cell", nlat)
+        dl = 2 * math.pi / nlon
+        self.full_lon = np.arange(nlon) * dl
+        self.half_lon = self.full_lon + 0.5 * dl
+        self.weight = np.broadcast_to(self.area[:, None], (nlat, nlon))
+
+    def batch(self, u, v):
+        """Courant numbers and axis divergences of the winds (u on lon edges,
+        v on lat edges), the pole rows of u zero."""
+        nlat, nlon, dt = self.nlat, self.nlon, self.dt
+        u = u.copy()
         u[0], u[-1] = 0.0, 0.0
-        v = -u0 * np.sin(lon_v) * math.sin(alpha)
         cflx = np.zeros_like(u)
-        cflx[1:-1] = u[1:-1] * dt / de_lon[1:-1, None]
-        cfly = v * dt / de_lat[:, None]
+        cflx[1:-1] = u[1:-1] * dt / self.de_lon[1:-1, None]
+        cfly = v * dt / self.de_lat[:, None]
+        area, le_lon, le_lat = self.area, self.le_lon, self.le_lat
         divx = np.zeros((nlat, nlon))
         divy = np.zeros((nlat, nlon))
         divx[1:-1] = (u[1:-1] - np.roll(u[1:-1], 1, axis=1)) * le_lon[1:-1, None] / area[1:-1, None]
         divy[1:-1] = (v[1:] * le_lat[1:, None] - v[:-1] * le_lat[:-1, None]) / area[1:-1, None]
         divy[0] = v[0].sum() * le_lat[0] / nlon / area[0]
         divy[-1] = -v[-1].sum() * le_lat[-1] / nlon / area[-1]
+        return [x[None] for x in (u, v, u, v, cflx, cfly, divx, divy)]
 
-        lon_c, lat_c = np.meshgrid(full_lon, full_lat)
-        cosr = np.sin(lat_c) * math.sin(0.0) + np.cos(lat_c) * math.cos(0.0) * np.cos(lon_c - 1.5 * math.pi)
-        r = a * np.arccos(np.clip(cosr, -1.0, 1.0))
-        R0 = a / 3
-        bell0 = np.where(r < R0, H0 / 2 * (1 + np.cos(math.pi * r / R0)), 0.0)
-        q = np.stack([bell0, np.ones_like(bell0)])
-        wind = [x[None] for x in (u, v, u, v, cflx, cfly, divx, divy)]
-        for _ in range(int(round(PERIOD / dt))):
-            fx, fy = zip(*(o.ffsl_hflx(q[l:l + 1], *wind, dt) for l in range(2)))
+    def run(self, q, winds_at, steady=False):
+        """Advance the tracers q[l] over one period; winds_at(t) gives (u, v)
+        at time t (called once when the winds are steady)."""
+        dt, nlon = self.dt, self.nlon
+        le_lon, le_lat, area = self.le_lon, self.le_lat, self.area
+        wind = None
+        for s in range(int(round(PERIOD / dt))):
+            if wind is None or not steady:
+                wind = self.batch(*winds_at((s + 0.5) * dt))
+            fx, fy = zip(*(self.o.ffsl_hflx(q[l:l + 1], *wind, dt) for l in range(len(q))))
             fx, fy = np.concatenate(fx), np.concatenate(fy)
             dx = (fx[:, 1:-1] - np.roll(fx[:, 1:-1], 1, axis=2)) * le_lon[None, 1:-1, None]
             dy = fy[:, 1:] * le_lat[None, 1:, None] - fy[:, :-1] * le_lat[None, :-1, None]
@@ -74,33 +89,105 @@ def solid_rotation(nlon, nlat, dt, alpha=math.pi / 2):
             qn[:, 0] -= (fy[:, 0].sum(axis=1) * le_lat[0] / nlon / area[0] * dt)[:, None]
             qn[:, -1] += (fy[:, -1].sum(axis=1) * le_lat[-1] / nlon / area[-1] * dt)[:, None]
             q = qn
-    finally:
-        o.close()
-    return q[0], q[1], bell0, np.broadcast_to(area[:, None], bell0.shape)
+        self.o.close()
+        return q
+
+    def l2(self, q, q0):
+        d = q - q0
+        return math.sqrt(np.sum(d * d * self.weight) / np.sum(q0 * q0 * self.weight))
+
+    def mass_change(self, q, q0):
+        return abs(np.sum((q - q0) * self.weight)) / np.sum(q0 * self.weight)
 
 
-def l2_error(q, q0, w):
-    d = q - q0
-    return math.sqrt(np.sum(d * d * w) / np.sum(q0 * q0 * w))
+def distance(lon0, lat0, lon, lat):
+    """Great-circle angle between (lon0, lat0) and the points (lon, lat)."""
+    c = math.sin(lat0) * np.sin(lat) + math.cos(lat0) * np.cos(lat) * np.cos(lon - lon0)
+    return np.arccos(np.clip(c, -1.0, 1.0))
+
+
+def solid_rotation(nlon, nlat, dt, alpha=math.pi / 2):
+    tr = Transport(nlon, nlat, dt)
+    u0 = 2 * math.pi * tr.cfg.radius / PERIOD
+    lon_u, lat_u = np.meshgrid(tr.half_lon, tr.full_lat)
+    lon_v, _ = np.meshgrid(tr.full_lon, tr.half_lat)
+    u = u0 * (np.cos(lat_u) * math.cos(alpha) + np.sin(lat_u) * np.cos(lon_u) * math.sin(alpha))
+    v = -u0 * np.sin(lon_v) * math.sin(alpha)
+    lon_c, lat_c = np.meshgrid(tr.full_lon, tr.full_lat)
+    r = distance(1.5 * math.pi, 0.0, lon_c, lat_c)
+    R0 = 1.0 / 3.0
+    bell0 = np.where(r < R0, H0 / 2 * (1 + np.cos(math.pi * r / R0)), 0.0)
+    q0 = np.stack([bell0, np.ones_like(bell0)])
+    q = tr.run(q0, lambda t: (u, v), steady=True)
+    return tr, q, q0
+
+
+def deformational_flow(nlon, nlat, dt):
+    tr = Transport(nlon, nlat, dt)
+    k = 10 * tr.cfg.radius / PERIOD
+    u_shape = np.sin(tr.half_lon)[None] ** 2 * np.sin(2 * tr.full_lat)[:, None]
+    v_shape = np.sin(2 * tr.full_lon)[None] * np.cos(tr.half_lat)[:, None]
+
+    def winds(t):
+        c = k * math.cos(math.pi * t / PERIOD)
+        return c * u_shape, c * v_shape
+
+    lon, lat = np.meshgrid(tr.full_lon, tr.full_lat)
+    centres = ((5 * math.pi / 6, 0.0), (7 * math.pi / 6, 0.0))
+    x = np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)])
+    gauss = np.zeros_like(lon)
+    for lo, la in centres:
+        xc = np.array([math.cos(la) * math.cos(lo), math.cos(la) * math.sin(lo), math.sin(la)])[:, None, None]
+        gauss += 0.95 * np.exp(-5 * ((x - xc) ** 2).sum(0))
+    r1, r2 = (distance(lo, la, lon, lat) for lo, la in centres)
+    hill = lambda r: 0.1 + 0.9 * 0.5 * (1 + np.cos(math.pi * r / 0.5))
+    cosine = np.where(r1 < 0.5, hill(r1), np.where(r2 < 0.5, hill(r2), 0.1))
+    q0 = np.stack([gauss, cosine])
+    q = tr.run(q0, winds)
+    return tr, q, q0
 
 
 @pytest.fixture(scope="module")
-def runs():
+def rotation_runs():
     return {res: solid_rotation(*args) for res, args in ((5.0, (72, 37, 3600.0)), (2.5, (144, 73, 1800.0)))}
 
 
+@pytest.fixture(scope="module")
+def deform_runs():
+    return {res: deformational_flow(*args) for res, args in ((5.0, (72, 37, 3600.0)), (3.75, (96, 49, 2400.0)))}
+
+
 @pytest.mark.parametrize("res", [5.0, 2.5])
-def test_solid_rotation_conserves_and_stays_monotone(runs, res):
-    bell, background, bell0, w = runs[res]
-    m0, m1 = np.sum(bell0 * w), np.sum(bell * w)
-    assert abs(m1 - m0) / m0 < 1e-12
+def test_solid_rotation_conserves_and_stays_monotone(rotation_runs, res):
+    tr, q, q0 = rotation_runs[res]
+    bell, background = q
+    assert tr.mass_change(bell, q0[0]) < 1e-12
     assert bell.min() > -1e-10 * H0
     assert bell.max() <= H0 * (1 + 1e-12)
     assert np.abs(background - 1).max() < 1e-3
 
 
-def test_solid_rotation_error_converges(runs):
-    e5 = l2_error(*[runs[5.0][i] for i in (0, 2, 3)])
-    e25 = l2_error(*[runs[2.5][i] for i in (0, 2, 3)])
-    assert e25 < 0.1
-    assert e25 < 0.35 * e5
+def test_solid_rotation_error_converges(rotation_runs):
+    e = {res: tr.l2(q[0], q0[0]) for res, (tr, q, q0) in rotation_runs.items()}
+    # measured: 0.327 at 5 degrees, 0.077 at 2.5 degrees
+    assert e[2.5] < 0.1
+    assert e[2.5] < 0.35 * e[5.0]
+
+
+@pytest.mark.parametrize("res", [5.0, 3.75])
+def test_deformational_flow_conserves_and_stays_bounded(deform_runs, res):
+    tr, q, q0 = deform_runs[res]
+    gauss, cosine = q
+    assert tr.mass_change(gauss, q0[0]) < 1e-13
+    assert tr.mass_change(cosine, q0[1]) < 1e-13
+    assert gauss.min() >= 0.0 and gauss.max() <= q0[0].max()
+    # cosine hills on a 0.1 background: undershoots of the split 2-D
+    # scheme stay below 1e-4 (measured 6e-6 at 5 degrees)
+    assert cosine.min() > 0.1 - 1e-4 and cosine.max() <= 1.0
+
+
+def test_deformational_flow_error_converges(deform_runs):
+    e = {res: tr.l2(q[0], q0[0]) for res, (tr, q, q0) in deform_runs.items()}
+    # Gaussian hills, measured: 0.246 at 5 degrees, 0.164 at 3.75 degrees
+    assert e[3.75] < 0.2
+    assert e[3.75] < 0.8 * e[5.0]
