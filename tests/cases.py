@@ -7,6 +7,7 @@ import numpy as np
 
 from oracle import Oracle
 
+from gmcore_gb300 import abi
 from helpers import initial_state, load_state
 
 
@@ -103,3 +104,130 @@ def swm_state(cfg, ic):
     u, v, gz, gzs = ic(o, cfg)
     o.close()
     return {"u_lon": u[None], "v_lat": v[None], "gz": gz[None], "gzs": gzs}
+
+
+# Tracer transport with prescribed winds (the reference's advection tests,
+# src/tests/adv/): one period T = 12 days, m = 1, mfx = u, mfy = v, u set on
+# non-pole rows only; the update is the flux divergence of the FFSL face
+# fluxes with the pole cells closed by ring sums of the meridional fluxes.
+PERIOD = 12 * 86400.0
+H0 = 1000.0
+
+
+def transport_config(nlon, nlat, dt):
+    return abi.default_config(nlon=nlon, nlat=nlat, nlev=1, baroclinic=0, dt_dyn=dt, dt_adv=dt,
+                              limiter_type=abi.LIMITER_MONO)
+
+
+class Transport:
+    """One tracer-transport harness on a lat-lon grid of the oracle."""
+
+    def __init__(self, nlon, nlat, dt):
+        cfg = transport_config(nlon, nlat, dt)
+        self.o = Oracle(cfg)
+        self.cfg, self.dt, self.nlon, self.nlat = cfg, dt, nlon, nlat
+        m = self.o.metric
+        self.full_lat, self.half_lat = m("full_lat", nlat), m("half_lat", nlat - 1)
+        self.de_lon, self.le_lon = m("de_lon", nlat), m("le_lon", nlat)
+        self.de_lat, self.le_lat = m("de_lat", nlat - 1), m("le_lat", nlat - 1)
+        self.area = m("area_cell", nlat)
+        dl = 2 * math.pi / nlon
+        self.full_lon = np.arange(nlon) * dl
+        self.half_lon = self.full_lon + 0.5 * dl
+        self.weight = np.broadcast_to(self.area[:, None], (nlat, nlon))
+
+    def batch(self, u, v):
+        """Courant numbers and axis divergences of the winds (u on lon edges,
+        v on lat edges), the pole rows of u zero."""
+        nlat, nlon, dt = self.nlat, self.nlon, self.dt
+        u = u.copy()
+        u[0], u[-1] = 0.0, 0.0
+        cflx = np.zeros_like(u)
+        cflx[1:-1] = u[1:-1] * dt / self.de_lon[1:-1, None]
+        cfly = v * dt / self.de_lat[:, None]
+        area, le_lon, le_lat = self.area, self.le_lon, self.le_lat
+        divx = np.zeros((nlat, nlon))
+        divy = np.zeros((nlat, nlon))
+        divx[1:-1] = (u[1:-1] - np.roll(u[1:-1], 1, axis=1)) * le_lon[1:-1, None] / area[1:-1, None]
+        divy[1:-1] = (v[1:] * le_lat[1:, None] - v[:-1] * le_lat[:-1, None]) / area[1:-1, None]
+        divy[0] = v[0].sum() * le_lat[0] / nlon / area[0]
+        divy[-1] = -v[-1].sum() * le_lat[-1] / nlon / area[-1]
+        return [x[None] for x in (u, v, u, v, cflx, cfly, divx, divy)]
+
+    def run(self, q, winds_at, steady=False, flux=None):
+        """Advance the tracers q[l] over one period; winds_at(t) gives (u, v)
+        at time t (called once when the winds are steady).  flux(q, wind, dt)
+        returns the face fluxes (fx, fy) of one tracer; the oracle's
+        ffsl_calc_tracer_hflx_cell by default."""
+        flux = flux or (lambda q1, wind, dt_: self.o.ffsl_hflx(q1, *wind, dt_))
+        dt, nlon = self.dt, self.nlon
+        le_lon, le_lat, area = self.le_lon, self.le_lat, self.area
+        wind = None
+        for s in range(int(round(PERIOD / dt))):
+            if wind is None or not steady:
+                wind = self.batch(*winds_at((s + 0.5) * dt))
+            fx, fy = zip(*(flux(q[l:l + 1], wind, dt) for l in range(len(q))))
+            fx, fy = np.concatenate(fx), np.concatenate(fy)
+            dx = (fx[:, 1:-1] - np.roll(fx[:, 1:-1], 1, axis=2)) * le_lon[None, 1:-1, None]
+            dy = fy[:, 1:] * le_lat[None, 1:, None] - fy[:, :-1] * le_lat[None, :-1, None]
+            qn = q.copy()
+            qn[:, 1:-1] -= (dx + dy) / area[None, 1:-1, None] * dt
+            qn[:, 0] -= (fy[:, 0].sum(axis=1) * le_lat[0] / nlon / area[0] * dt)[:, None]
+            qn[:, -1] += (fy[:, -1].sum(axis=1) * le_lat[-1] / nlon / area[-1] * dt)[:, None]
+            q = qn
+        self.o.close()
+        return q
+
+    def l2(self, q, q0):
+        d = q - q0
+        return math.sqrt(np.sum(d * d * self.weight) / np.sum(q0 * q0 * self.weight))
+
+    def mass_change(self, q, q0):
+        return abs(np.sum((q - q0) * self.weight)) / np.sum(q0 * self.weight)
+
+
+def distance(lon0, lat0, lon, lat):
+    """Great-circle angle between (lon0, lat0) and the points (lon, lat)."""
+    c = math.sin(lat0) * np.sin(lat) + math.cos(lat0) * np.cos(lat) * np.cos(lon - lon0)
+    return np.arccos(np.clip(c, -1.0, 1.0))
+
+
+def solid_rotation(nlon, nlat, dt, alpha=math.pi / 2, flux=None):
+    tr = Transport(nlon, nlat, dt)
+    u0 = 2 * math.pi * tr.cfg.radius / PERIOD
+    lon_u, lat_u = np.meshgrid(tr.half_lon, tr.full_lat)
+    lon_v, _ = np.meshgrid(tr.full_lon, tr.half_lat)
+    u = u0 * (np.cos(lat_u) * math.cos(alpha) + np.sin(lat_u) * np.cos(lon_u) * math.sin(alpha))
+    v = -u0 * np.sin(lon_v) * math.sin(alpha)
+    lon_c, lat_c = np.meshgrid(tr.full_lon, tr.full_lat)
+    r = distance(1.5 * math.pi, 0.0, lon_c, lat_c)
+    R0 = 1.0 / 3.0
+    bell0 = np.where(r < R0, H0 / 2 * (1 + np.cos(math.pi * r / R0)), 0.0)
+    q0 = np.stack([bell0, np.ones_like(bell0)])
+    q = tr.run(q0, lambda t: (u, v), steady=True, flux=flux)
+    return tr, q, q0
+
+
+def deformational_flow(nlon, nlat, dt, flux=None):
+    tr = Transport(nlon, nlat, dt)
+    k = 10 * tr.cfg.radius / PERIOD
+    u_shape = np.sin(tr.half_lon)[None] ** 2 * np.sin(2 * tr.full_lat)[:, None]
+    v_shape = np.sin(2 * tr.full_lon)[None] * np.cos(tr.half_lat)[:, None]
+
+    def winds(t):
+        c = k * math.cos(math.pi * t / PERIOD)
+        return c * u_shape, c * v_shape
+
+    lon, lat = np.meshgrid(tr.full_lon, tr.full_lat)
+    centres = ((5 * math.pi / 6, 0.0), (7 * math.pi / 6, 0.0))
+    x = np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)])
+    gauss = np.zeros_like(lon)
+    for lo, la in centres:
+        xc = np.array([math.cos(la) * math.cos(lo), math.cos(la) * math.sin(lo), math.sin(la)])[:, None, None]
+        gauss += 0.95 * np.exp(-5 * ((x - xc) ** 2).sum(0))
+    r1, r2 = (distance(lo, la, lon, lat) for lo, la in centres)
+    hill = lambda r: 0.1 + 0.9 * 0.5 * (1 + np.cos(math.pi * r / 0.5))
+    cosine = np.where(r1 < 0.5, hill(r1), np.where(r2 < 0.5, hill(r2), 0.1))
+    q0 = np.stack([gauss, cosine])
+    q = tr.run(q0, winds, flux=flux)
+    return tr, q, q0

@@ -2,7 +2,11 @@
 states: the Rossby-Haurwitz wave and the zonal flow over a mountain in
 shallow water (src/tests/swm/rossby_haurwitz_wave_test_mod.F90,
 mountain_zonal_flow_test_mod.F90) and the perturbed baroclinic wave on the
-26-level test coordinate (src/tests/baroclinic_wave_test_mod.F90).
+26-level test coordinate (src/tests/baroclinic_wave_test_mod.F90); and the
+FFSL operator entry point (gmc_ffsl_hflx) driving the reference's advection
+tests for a whole 12-day period (src/tests/adv/solid_rotation_test_mod.F90,
+deform_test_mod.F90 case 2) against the same transport driven by the
+oracle's fluxes.
 
 Tolerances as for the seeded states: max-norm error <= 1e-12 after one step
 and <= 1e-9 after a few hours.  Winds are measured against the wind scale
@@ -15,7 +19,8 @@ import pytest
 from gmcore_gb300 import Model
 from oracle import Oracle
 
-from cases import baroclinic_wave_state, mountain_zonal_flow, rossby_haurwitz, swm_state
+from cases import (baroclinic_wave_state, deformational_flow, mountain_zonal_flow, rossby_haurwitz,
+                   solid_rotation, swm_state, transport_config)
 from helpers import baroclinic_config, load_state, swm_config
 
 pytestmark = pytest.mark.gpu
@@ -62,3 +67,38 @@ def test_swm_case_matches_oracle(ic):
 def test_baroclinic_wave_matches_oracle():
     cfg = baroclinic_config(nlon=72, nlat=37, nlev=26, dt=600.0)
     check_pair(cfg, baroclinic_wave_state(cfg, perturb=True), ("u_lon", "v_lat", "pt", "phs"), 12)
+
+
+def device_flux(model):
+    """flux(q, wind, dt) through gmc_ffsl_hflx on device buffers."""
+    import torch
+
+    def flux(q1, wind, dt):
+        names = ("q", "u", "v", "mfx", "mfy", "cflx", "cfly", "divx", "divy")
+        dev = {k: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+               for k, a in zip(names, (q1, *wind))}
+        qmfx = torch.zeros_like(dev["q"])
+        qmfy = torch.zeros_like(dev["v"])
+        torch.cuda.synchronize()
+        ptrs = {k: t.data_ptr() for k, t in dev.items()}
+        ptrs.update(qmfx=qmfx.data_ptr(), qmfy=qmfy.data_ptr())
+        model.ffsl_hflx(ptrs, dt)
+        return qmfx.cpu().numpy(), qmfy.cpu().numpy()
+    return flux
+
+
+@pytest.mark.parametrize("case", [solid_rotation, deformational_flow], ids=["solid_rotation", "deformational_flow"])
+def test_ffsl_transport_period_matches_oracle(case):
+    pytest.importorskip("torch")
+    nlon, nlat, dt = 72, 37, 3600.0
+    model = Model(transport_config(nlon, nlat, dt))
+    try:
+        tr, qg, q0 = case(nlon, nlat, dt, flux=device_flux(model))
+    finally:
+        model.close()
+    _, qo, _ = case(nlon, nlat, dt)
+    err = [float(np.abs(qg[l] - qo[l]).max() / np.abs(qo[l]).max()) for l in range(len(qo))]
+    mass = [tr.mass_change(qg[l], q0[l]) for l in range(len(qo))]
+    print(case.__name__, "max-norm vs oracle after one period", err, "mass", mass)
+    assert max(err) <= 1e-9, err
+    assert max(mass) < 1e-12, mass
