@@ -178,32 +178,58 @@ def state_bytes(state):
     return sum(a.nbytes for a in state.values())
 
 
+class Ranks:
+    """Coordination of the replicas (one process per GPU, each advancing its
+    own copy of the workload; no collective on the data path): a barrier
+    around the timed region and the maximum of a time over ranks.  With one
+    process both are no-ops."""
+
+    def __init__(self, backend="nccl"):
+        self.dist = None
+        self.device = "cuda" if backend == "nccl" else "cpu"
+        if WORLD > 1:
+            import torch
+            import torch.distributed as dist
+            if backend == "nccl":
+                torch.cuda.set_device(0)
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def replica_throughput(max_ms, steps, world):
+    """(ms per step, whole-job simulated days per wall-day) of `world`
+    replicas that each advanced `steps` steps of DT seconds, the slowest in
+    max_ms milliseconds."""
+    return max_ms / steps, DT * steps / (max_ms / 1000.0) * world
+
+
 def run_ours(args):
     import gmcore_gb300 as g
     from gmcore_gb300 import abi
 
-    dist = None
-    if WORLD > 1:
-        import torch
-        import torch.distributed as dist
-        torch.cuda.set_device(0)
-        dist.init_process_group("nccl")
+    ranks = Ranks("nccl")
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     cfg = workload_config(abi.PREC_MIXED)
     cfg64 = workload_config(abi.PREC_FP64)
     st = g.make_ic(cfg, 2, SEED, 1.0)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     # ---- device-resident timing of the mixed form ----
     model = g.Model(cfg)
@@ -218,9 +244,7 @@ def run_ours(args):
     clk = clocks.stop()
     stats = model.stats()
     dev_ms = max_over_ranks(stats["step_ms"])
-    ms_per_step = dev_ms / args.steps
-    sdpd_rank = DT * args.steps / (dev_ms / 1000.0)
-    value = sdpd_rank * WORLD
+    ms_per_step, value = replica_throughput(dev_ms, args.steps, WORLD)
     launches_per_step = stats["kernel_launches"] / args.steps
     # state after warmup + steps, compared with the FP64 form below
     mixed_state = {name: model.get_field(name) for name in ("phs", "u_lon", "v_lat", "pt")}
@@ -231,8 +255,7 @@ def run_ours(args):
             print(json.dumps({"metric": METRIC, "value": value, "unit": "sim days/wall-day", "n_gpus": WORLD,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
                               "device_only": True}), flush=True)
-        if dist is not None:
-            dist.destroy_process_group()
+        ranks.close()
         return
 
     # ---- end to end through the C ABI with host buffers ----
@@ -390,8 +413,7 @@ def run_ours(args):
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    ranks.close()
 
 
 def adjoint_cost():
