@@ -1845,14 +1845,18 @@ int orc_ffsl_hflx(void *h, const double *q, const double *u, const double *v, co
 }
 
 // Mesh/filter queries for the known-answer tests.  Besides the per-row
-// tables, the vertical coordinate's eta levels (full_lev = hyam + hybm,
-// half_lev = hyai + hybi, hybrid_coord_mod.F90:129-132) so that a test can
-// build the reference's analytic states on them.
+// tables, the vertical coordinate: the hybrid coefficients hyai, hybi (the
+// template's tables) and hyam, hybm, and the eta levels full_lev = hyam + hybm,
+// half_lev = hyai + hybi (hybrid_coord_mod.F90:121-132).
 int orc_metric(void *h, const char *name, double *out, int n) {
   orc::Model *m = (orc::Model *)h;
-  const std::vector<double> *lev = !std::strcmp(name, "full_lev")   ? &m->grid.full_lev
-                                   : !std::strcmp(name, "half_lev") ? &m->grid.half_lev
-                                                                    : nullptr;
+  const gmc::Grid &g = m->grid;
+  struct V { const char *name; const std::vector<double> *v; };
+  const V vecs[] = {{"full_lev", &g.full_lev}, {"half_lev", &g.half_lev}, {"hyai", &g.hyai},
+                    {"hybi", &g.hybi},         {"hyam", &g.hyam},         {"hybm", &g.hybm}};
+  const std::vector<double> *lev = nullptr;
+  for (const V &e : vecs)
+    if (!std::strcmp(name, e.name)) lev = e.v;
   if (lev) {
     if (n != (int)lev->size()) return GMC_EINVAL;
     for (int k = 0; k < n; ++k) out[k] = (*lev)[k];
@@ -1861,6 +1865,18 @@ int orc_metric(void *h, const char *name, double *out, int n) {
   const gmc::RowTable *t = m->grid.metric(name);
   if (!t) return GMC_EINVAL;
   for (int j = 1; j <= n; ++j) out[j - 1] = (*t)[j];
+  return GMC_OK;
+}
+
+// Normalised weights of one polar-filter row (which: 0 big, 1 small1,
+// 2 small2; lat: 0 full, 1 half latitudes; j 1-based); n must equal the
+// row's tap count.
+int orc_filter_weights(void *h, int which, int lat, int j, double *out, int n) {
+  orc::Model *m = (orc::Model *)h;
+  const gmc::Filter &f = which == 0 ? m->grid.big : which == 1 ? m->grid.small1 : m->grid.small2;
+  const std::vector<std::vector<double>> &w = lat ? f.wgt_half : f.wgt_full;
+  if (j < 1 || j > (int)w.size() || n != (int)w[j - 1].size()) return GMC_EINVAL;
+  for (int t = 0; t < n; ++t) out[t] = w[j - 1][t];
   return GMC_OK;
 }
 

@@ -44,6 +44,7 @@ def load(variant="parity"):
     lib.orc_space_identities.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.orc_metric.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int]
     lib.orc_filter_taps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    lib.orc_filter_weights.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
     _LIBS[variant] = lib
     return lib
@@ -153,6 +154,15 @@ class Oracle:
         n = self.cfg.nlat - 1 if lat else self.cfg.nlat
         out = np.zeros(n, dtype=np.int32)
         self.lib.orc_filter_taps(self.h, which, lat, out.ctypes.data_as(C.POINTER(C.c_int)))
+        return out
+
+    def filter_weights(self, which, lat, j):
+        """Weights of polar-filter row j (1-based) of filter `which`
+        (0 big, 1 small1, 2 small2) on full (lat=0) or half (lat=1) rows."""
+        n = int(self.filter_taps(which, lat)[j - 1])
+        out = np.zeros(n)
+        if self.lib.orc_filter_weights(self.h, which, lat, j, _ptr(out), n):
+            raise IndexError((which, lat, j))
         return out
 
     def ffsl_hflx(self, q, u, v, mfx, mfy, cflx, cfly, divx, divy, dt):
