@@ -1,0 +1,209 @@
+"""The 1-D mesh metrics of the latitude-longitude C-grid against a separate
+restatement of mesh_init_global (mesh_mod.F90:134-447, default options:
+uniform latitudes, classic tangent weights):
+
+* latitudes built by accumulating dlat from the south pole, snapped to 0
+  within 1e-12 and mirrored for equatorial symmetry (:186-234), their sines
+  and cosines with exact poles (:236-264);
+* cell, sub-cell and vertex areas of the zonal strips (:266-283, 328);
+* the areas of the triangles around each edge (:284-370).  The reference
+  sums spherical angles in binary128 (calc_area, sphere_geometry_mod.F90:
+  305-326); here each spherical excess is computed in 40-digit arithmetic by
+  a different formula (Van Oosterom and Strackee's tan(E/2)) on the same
+  vertices (x, y from double-precision sines and cosines multiplied in
+  extended precision, z a double product, as cartesian_transform_1_r16
+  forms them, :110-123).  Two properties of the reference's arithmetic are
+  kept because they show at 1e-12: calc_area subtracts (n - 2) pi with the
+  double-precision pi, so every triangle area carries R^2 (pi - pi_double);
+  and the lune of a latitude arc (calc_area_with_last_small_arc, :328-390)
+  is the polar sector minus the polar triangle, with the sector's longitude
+  span from the vertices' recovered longitudes (atan2 of their coordinates)
+  and its latitude sine z / R;
+* edge lengths and distances (:372-391), classic tangent weights
+  (:417-426) and Coriolis parameters (:436-441).
+
+Closed forms must agree to 4 ulps, the triangle areas and what depends on
+them to 1e-14 (measured: all 30 tables bit for bit at 5, 1 and 0.5
+degrees)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import Oracle
+
+from helpers import swm_config
+
+mpmath = pytest.importorskip("mpmath")
+mp = mpmath.mp
+
+PI = math.atan(1.0) * 4.0
+PI2, PI05 = PI * 2, PI * 0.5
+DEG = 180.0 / PI
+
+
+def latitudes(nlat):
+    nhalf = nlat - 1
+    dlat = (PI05 - (-PI05)) / nhalf
+    full = np.zeros(nlat)
+    half = np.zeros(nhalf)
+    full[0] = -PI05
+    for j in range(1, nlat - 1):
+        full[j] = full[j - 1] + dlat
+        if abs(full[j]) < 1e-12:
+            full[j] = 0.0
+    full[-1] = PI05
+    for j in range(nhalf):
+        half[j] = full[j] + 0.5 * dlat
+        if abs(half[j]) < 1e-12:
+            half[j] = 0.0
+    for a in (full, half):
+        n = len(a)
+        for j in range(n):
+            if a[j] > 0:
+                a[j] = -a[n - 1 - j]
+    return full, half
+
+
+def point(R, lon, lat):
+    c = mpmath.mpf(math.cos(lat))
+    return [mpmath.mpf(R) * c * mpmath.mpf(math.cos(lon)), mpmath.mpf(R) * c * mpmath.mpf(math.sin(lon)),
+            mpmath.mpf(R * math.sin(lat))]
+
+
+def unit(v):
+    n = mpmath.sqrt(sum(x * x for x in v))
+    return [x / n for x in v]
+
+
+def great_triangle(R, a, b, c):
+    """calc_area of the great-circle triangle abc: R^2 (E + pi - pi_double),
+    the spherical excess E by Van Oosterom and Strackee."""
+    a, b, c = unit(a), unit(b), unit(c)
+    dot = lambda p, q: sum(x * y for x, y in zip(p, q))
+    cross = [b[1] * c[2] - b[2] * c[1], b[2] * c[0] - b[0] * c[2], b[0] * c[1] - b[1] * c[0]]
+    num = abs(dot(a, cross))
+    den = 1 + dot(a, b) + dot(b, c) + dot(c, a)
+    excess = 2 * mpmath.atan2(num, den)
+    return mpmath.mpf(R * R) * (excess + mpmath.pi - mpmath.mpf(PI))
+
+
+def lon_lat(R, p):
+    lon = mpmath.atan2(p[1], p[0])
+    if lon < 0:
+        lon += mpmath.mpf(PI2)
+    return lon, mpmath.asin(p[2] / mpmath.mpf(R))
+
+
+def triangle_with_latitude_arc(R, p0, p1, p2):
+    """Area bounded by great arcs p0-p1, p0-p2 and the latitude arc p1-p2."""
+    tri = great_triangle(R, p0, p1, p2)
+    (_, lat0), (lon1, lat1), (lon2, _) = lon_lat(R, p0), lon_lat(R, p1), lon_lat(R, p2)
+    if lat1 == 0:
+        return tri
+    dlon = lon2 - lon1 if lat0 > lat1 else lon1 - lon2
+    if dlon < 0:
+        dlon += mpmath.mpf(PI2)
+    s1 = p1[2] / mpmath.mpf(R)
+    poleward = lat0 * lat1 >= 0 and abs(lat0) > abs(lat1)
+    q1, q2 = (p1, p2) if poleward else (p2, p1)
+    pole = [0, 0, mpmath.mpf(R) if lat1 > 0 else -mpmath.mpf(R)]
+    sector = mpmath.mpf(R * R) * dlon * ((1 - s1) if lat1 > 0 else (s1 + 1))
+    lune = sector - great_triangle(R, pole, q1, q2)
+    if lune < 0 and -lune > 1e-10:
+        lune = 0
+    return tri + lune if poleward else tri - lune
+
+
+def restated(cfg):
+    nlon, nlat = cfg.nlon, cfg.nlat
+    nhalf = nlat - 1
+    R, om = cfg.radius, cfg.omega
+    mp.dps = 40
+    dlon = (PI2 - 0.0) / nlon
+    flon = [i * dlon for i in range(3)]
+    hlon = [x + 0.5 * dlon for x in flon]
+    full, half = latitudes(nlat)
+    fc, fs = np.cos(full), np.sin(full)
+    hc, hs = np.cos(half), np.sin(half)
+    fc[0], fs[0], fc[-1], fs[-1] = 0.0, -1.0, 0.0, 1.0
+    M = {n: np.zeros(nlat) for n in ("area_cell", "area_subcell1", "area_subcell2", "area_lon_west", "area_lon_east",
+                                     "area_lon", "area_lon_north", "area_lon_south", "de_lon", "le_lon",
+                                     "full_tangent_wgt1", "full_tangent_wgt2", "full_f")}
+    M.update({n: np.zeros(nhalf) for n in ("area_vtx", "area_lat_west", "area_lat_east", "area_lat_north",
+                                          "area_lat_south", "area_lat", "le_lat", "de_lat", "half_tangent_wgt1",
+                                          "half_tangent_wgt2", "half_f")})
+    for j in range(nlat):
+        if j == 0:
+            M["area_cell"][j] = R ** 2 * dlon * (hs[j] + 1.0)
+            M["area_subcell2"][j] = R ** 2 * 0.5 * dlon * (hs[j] + 1.0)
+        elif j == nlat - 1:
+            M["area_cell"][j] = R ** 2 * dlon * (1.0 - hs[j - 1])
+            M["area_subcell1"][j] = R ** 2 * 0.5 * dlon * (1.0 - hs[j - 1])
+        else:
+            M["area_cell"][j] = R ** 2 * dlon * (hs[j] - hs[j - 1])
+            M["area_subcell1"][j] = R ** 2 * 0.5 * dlon * (fs[j] - hs[j - 1])
+            M["area_subcell2"][j] = R ** 2 * 0.5 * dlon * (hs[j] - fs[j])
+            w = great_triangle(R, point(R, flon[0], full[j]), point(R, hlon[0], half[j - 1]),
+                               point(R, hlon[0], half[j]))
+            M["area_lon_west"][j] = M["area_lon_east"][j] = float(w)
+            M["area_lon"][j] = M["area_lon_west"][j] + M["area_lon_east"][j]
+            M["area_lon_north"][j] = float(triangle_with_latitude_arc(
+                R, point(R, hlon[0], half[j]), point(R, flon[0], full[j]), point(R, flon[1], full[j])))
+            M["area_lon_south"][j] = float(triangle_with_latitude_arc(
+                R, point(R, hlon[0], half[j - 1]), point(R, flon[1], full[j]), point(R, flon[0], full[j])))
+    for j in range(nhalf):
+        M["area_vtx"][j] = R ** 2 * dlon * (fs[j + 1] - fs[j])
+        w = great_triangle(R, point(R, hlon[0], half[j]), point(R, flon[1], full[j]), point(R, flon[1], full[j + 1]))
+        M["area_lat_west"][j] = M["area_lat_east"][j] = float(w)
+        M["area_lat_north"][j] = float(triangle_with_latitude_arc(
+            R, point(R, flon[1], full[j + 1]), point(R, hlon[0], half[j]), point(R, hlon[1], half[j])))
+        M["area_lat_south"][j] = float(triangle_with_latitude_arc(
+            R, point(R, flon[1], full[j]), point(R, hlon[1], half[j]), point(R, hlon[0], half[j])))
+        if j == 0:
+            M["area_lat_south"][j] = M["area_cell"][j]
+        elif j + 1 == nlat - 1:
+            M["area_lat_north"][j] = M["area_cell"][j + 1]
+        M["area_lat"][j] = M["area_lat_north"][j] + M["area_lat_south"][j]
+    for j in range(1, nlat - 1):
+        M["de_lon"][j] = R * fc[j] * dlon
+        M["le_lon"][j] = 2.0 * M["area_lon"][j] / M["de_lon"][j]
+    for j in range(nhalf):
+        M["le_lat"][j] = R * hc[j] * dlon
+        M["de_lat"][j] = 2.0 * M["area_lat"][j] / M["le_lat"][j]
+    # rows the scheme does not set keep the allocation fill, huge(1.0_r8)
+    # (const_mod.F90:18, mesh_mod.F90:656)
+    M["full_tangent_wgt1"][[0, -1]] = M["full_tangent_wgt2"][[0, -1]] = np.finfo(float).max
+    for j in range(1, nlat - 1):
+        M["full_tangent_wgt1"][j] = M["le_lat"][j - 1] / M["de_lon"][j] * 0.25
+        M["full_tangent_wgt2"][j] = M["le_lat"][j] / M["de_lon"][j] * 0.25
+    for j in range(nhalf):
+        M["half_tangent_wgt1"][j] = M["le_lon"][j] / M["de_lat"][j] * 0.25
+        M["half_tangent_wgt2"][j] = M["le_lon"][j + 1] / M["de_lat"][j] * 0.25
+    M["full_f"] = 2.0 * om * fs
+    M["half_f"] = 2.0 * om * hs
+    M.update(full_lat=full, half_lat=half, full_cos_lat=fc, full_sin_lat=fs, half_cos_lat=hc, half_sin_lat=hs)
+    return M
+
+
+CLOSED = {"full_lat", "half_lat", "full_cos_lat", "full_sin_lat", "half_cos_lat", "half_sin_lat", "area_cell",
+          "area_subcell1", "area_subcell2", "area_vtx", "de_lon", "le_lat", "full_f", "half_f"}
+
+
+@pytest.mark.parametrize("nlon,nlat", [(72, 37), (360, 180), (720, 360)])
+def test_mesh_metrics_match_restatement(nlon, nlat):
+    cfg = swm_config(nlon=nlon, nlat=nlat, dt=60.0)
+    want = restated(cfg)
+    o = Oracle(cfg)
+    try:
+        for name, w in sorted(want.items()):
+            got = o.metric(name, len(w))
+            fill = w == np.finfo(float).max
+            assert np.array_equal(got[fill], w[fill]), name
+            got, w = got[~fill], w[~fill]
+            scale = np.abs(w).max()
+            err = float(np.abs(got - w).max() / scale)
+            tol = 4 * np.finfo(float).eps if name in CLOSED else 1e-14
+            assert err <= tol, (name, err)
+    finally:
+        o.close()
