@@ -1847,13 +1847,23 @@ int orc_ffsl_hflx(void *h, const double *q, const double *u, const double *v, co
 // Mesh/filter queries for the known-answer tests.  Besides the per-row
 // tables, the vertical coordinate: the hybrid coefficients hyai, hybi (the
 // template's tables) and hyam, hybm, and the eta levels full_lev = hyam + hybm,
-// half_lev = hyai + hybi (hybrid_coord_mod.F90:121-132).
+// half_lev = hyai + hybi (hybrid_coord_mod.F90:121-132); the divergence-damping
+// coefficients c_lon, c_lat by level (div_damp_mod.F90:27-80, [k][j]); the
+// zonal smoother's weights (lon_damp_mod.F90:43-68).
 int orc_metric(void *h, const char *name, double *out, int n) {
   orc::Model *m = (orc::Model *)h;
   const gmc::Grid &g = m->grid;
   struct V { const char *name; const std::vector<double> *v; };
-  const V vecs[] = {{"full_lev", &g.full_lev}, {"half_lev", &g.half_lev}, {"hyai", &g.hyai},
-                    {"hybi", &g.hybi},         {"hyam", &g.hyam},         {"hybm", &g.hybm}};
+  const V vecs[] = {{"full_lev", &g.full_lev},
+                    {"half_lev", &g.half_lev},
+                    {"hyai", &g.hyai},
+                    {"hybi", &g.hybi},
+                    {"hyam", &g.hyam},
+                    {"hybm", &g.hybm},
+                    {"div_c_lon", &g.div_c_lon},
+                    {"div_c_lat", &g.div_c_lat},
+                    {"lon_damp_wgt_full", &g.lon_damp_wgt_full},
+                    {"lon_damp_wgt_half", &g.lon_damp_wgt_half}};
   const std::vector<double> *lev = nullptr;
   for (const V &e : vecs)
     if (!std::strcmp(name, e.name)) lev = e.v;

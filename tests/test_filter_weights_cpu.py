@@ -14,7 +14,7 @@ independent restatement of filter_types_mod.F90:31-147 and exp_two_values
             x = i - (n+1)/2, normalised by their sum.
 
 Tap counts must agree exactly, weights to a few ulps (both sides evaluate
-exp and tanh through the C library)."""
+exp and tanh through the C library; measured: bit for bit)."""
 import math
 
 import numpy as np
@@ -29,7 +29,8 @@ BIG, SMALL1, SMALL2 = 0, 1, 2
 
 def gaussian(width, n, b):
     s = b * width / 2.0
-    w = [math.exp(-float((i - (n + 1) // 2) ** 2) / (2 * s ** 2)) / (s * math.sqrt(2 * math.pi))
+    # Fortran s**2 is s*s (Python's float ** goes through pow)
+    w = [math.exp(-float((i - (n + 1) // 2) ** 2) / (2 * (s * s))) / (s * math.sqrt(2 * math.pi))
          for i in range(1, n + 1)]
     total = 0.0
     for x in w:
@@ -38,7 +39,8 @@ def gaussian(width, n, b):
 
 
 def exp_two_values(v1, v2, x0, x1, x):
-    w = math.exp((x - x0) ** 2 * math.log(1.0e-3) / (x1 - x0) ** 2)
+    d, c = x - x0, x1 - x0
+    w = math.exp(d * d * math.log(1.0e-3) / (c * c))
     return w * v1 + (1 - w) * v2
 
 

@@ -43,26 +43,30 @@ DEG = 180.0 / PI
 
 
 def latitudes(nlat):
+    """(full, half, full_deg, half_deg) latitudes."""
     nhalf = nlat - 1
     dlat = (PI05 - (-PI05)) / nhalf
-    full = np.zeros(nlat)
-    half = np.zeros(nhalf)
-    full[0] = -PI05
+    full, half = np.zeros(nlat), np.zeros(nhalf)
+    full_deg, half_deg = np.zeros(nlat), np.zeros(nhalf)
+    full[0], full_deg[0] = -PI05, -PI05 * DEG
     for j in range(1, nlat - 1):
         full[j] = full[j - 1] + dlat
         if abs(full[j]) < 1e-12:
             full[j] = 0.0
-    full[-1] = PI05
+        full_deg[j] = full[j] * DEG
+    full[-1], full_deg[-1] = PI05, PI05 * DEG
     for j in range(nhalf):
         half[j] = full[j] + 0.5 * dlat
         if abs(half[j]) < 1e-12:
             half[j] = 0.0
-    for a in (full, half):
+        half_deg[j] = half[j] * DEG
+    for a, d in ((full, full_deg), (half, half_deg)):
         n = len(a)
         for j in range(n):
             if a[j] > 0:
                 a[j] = -a[n - 1 - j]
-    return full, half
+                d[j] = -d[n - 1 - j]
+    return full, half, full_deg, half_deg
 
 
 def point(R, lon, lat):
@@ -123,7 +127,7 @@ def restated(cfg):
     dlon = (PI2 - 0.0) / nlon
     flon = [i * dlon for i in range(3)]
     hlon = [x + 0.5 * dlon for x in flon]
-    full, half = latitudes(nlat)
+    full, half, full_deg, half_deg = latitudes(nlat)
     fc, fs = np.cos(full), np.sin(full)
     hc, hs = np.cos(half), np.sin(half)
     fc[0], fs[0], fc[-1], fs[-1] = 0.0, -1.0, 0.0, 1.0
@@ -135,15 +139,15 @@ def restated(cfg):
                                           "half_tangent_wgt2", "half_f")})
     for j in range(nlat):
         if j == 0:
-            M["area_cell"][j] = R ** 2 * dlon * (hs[j] + 1.0)
-            M["area_subcell2"][j] = R ** 2 * 0.5 * dlon * (hs[j] + 1.0)
+            M["area_cell"][j] = R * R * dlon * (hs[j] + 1.0)
+            M["area_subcell2"][j] = R * R * 0.5 * dlon * (hs[j] + 1.0)
         elif j == nlat - 1:
-            M["area_cell"][j] = R ** 2 * dlon * (1.0 - hs[j - 1])
-            M["area_subcell1"][j] = R ** 2 * 0.5 * dlon * (1.0 - hs[j - 1])
+            M["area_cell"][j] = R * R * dlon * (1.0 - hs[j - 1])
+            M["area_subcell1"][j] = R * R * 0.5 * dlon * (1.0 - hs[j - 1])
         else:
-            M["area_cell"][j] = R ** 2 * dlon * (hs[j] - hs[j - 1])
-            M["area_subcell1"][j] = R ** 2 * 0.5 * dlon * (fs[j] - hs[j - 1])
-            M["area_subcell2"][j] = R ** 2 * 0.5 * dlon * (hs[j] - fs[j])
+            M["area_cell"][j] = R * R * dlon * (hs[j] - hs[j - 1])
+            M["area_subcell1"][j] = R * R * 0.5 * dlon * (fs[j] - hs[j - 1])
+            M["area_subcell2"][j] = R * R * 0.5 * dlon * (hs[j] - fs[j])
             w = great_triangle(R, point(R, flon[0], full[j]), point(R, hlon[0], half[j - 1]),
                                point(R, hlon[0], half[j]))
             M["area_lon_west"][j] = M["area_lon_east"][j] = float(w)
@@ -153,7 +157,7 @@ def restated(cfg):
             M["area_lon_south"][j] = float(triangle_with_latitude_arc(
                 R, point(R, hlon[0], half[j - 1]), point(R, flon[1], full[j]), point(R, flon[0], full[j])))
     for j in range(nhalf):
-        M["area_vtx"][j] = R ** 2 * dlon * (fs[j + 1] - fs[j])
+        M["area_vtx"][j] = R * R * dlon * (fs[j + 1] - fs[j])
         w = great_triangle(R, point(R, hlon[0], half[j]), point(R, flon[1], full[j]), point(R, flon[1], full[j + 1]))
         M["area_lat_west"][j] = M["area_lat_east"][j] = float(w)
         M["area_lat_north"][j] = float(triangle_with_latitude_arc(
@@ -182,11 +186,12 @@ def restated(cfg):
         M["half_tangent_wgt2"][j] = M["le_lon"][j + 1] / M["de_lat"][j] * 0.25
     M["full_f"] = 2.0 * om * fs
     M["half_f"] = 2.0 * om * hs
-    M.update(full_lat=full, half_lat=half, full_cos_lat=fc, full_sin_lat=fs, half_cos_lat=hc, half_sin_lat=hs)
+    M.update(full_lat=full, half_lat=half, full_cos_lat=fc, full_sin_lat=fs, half_cos_lat=hc, half_sin_lat=hs,
+             full_lat_deg=full_deg, half_lat_deg=half_deg)
     return M
 
 
-CLOSED = {"full_lat", "half_lat", "full_cos_lat", "full_sin_lat", "half_cos_lat", "half_sin_lat", "area_cell",
+CLOSED = {"full_lat", "half_lat", "full_lat_deg", "half_lat_deg", "full_cos_lat", "full_sin_lat", "half_cos_lat", "half_sin_lat", "area_cell",
           "area_subcell1", "area_subcell2", "area_vtx", "de_lon", "le_lat", "full_f", "half_f"}
 
 
@@ -207,3 +212,93 @@ def test_mesh_metrics_match_restatement(nlon, nlat):
             assert err <= tol, (name, err)
     finally:
         o.close()
+
+
+# Coefficient tables derived from the mesh.
+
+def lon_damp_weights(deg_rows, lat0, interior):
+    """lon_damp_init (lon_damp_mod.F90:43-68): exp((lat0 - |lat|)^2 ln(1e-3)
+    / (lat0 - 80)^2), zero below 1e-6."""
+    w = np.zeros(len(deg_rows))
+    for j in interior:
+        d, c = lat0 - abs(deg_rows[j]), lat0 - 80.0
+        x = math.exp(d * d * math.log(1.0e-3) / (c * c))   # Fortran x**2 is x*x
+        w[j] = 0.0 if x < 1.0e-6 else x
+    return w
+
+
+def test_zonal_smoother_weights_match_restatement():
+    cfg = swm_config(nlon=720, nlat=360, dt=180.0)
+    full, half, full_deg, half_deg = latitudes(cfg.nlat)
+    o = Oracle(cfg)
+    try:
+        got_f = o.metric("lon_damp_wgt_full", cfg.nlat)
+        got_h = o.metric("lon_damp_wgt_half", cfg.nlat - 1)
+    finally:
+        o.close()
+    want_f = lon_damp_weights(full_deg, -full_deg[1], range(1, cfg.nlat - 1))
+    want_h = lon_damp_weights(half_deg, -half_deg[0], range(cfg.nlat - 1))
+    assert np.count_nonzero(want_f) > 0 and np.count_nonzero(want_h) > 0
+    assert np.array_equal(got_f, want_f) and np.array_equal(got_h, want_h)
+
+
+def div_damp_tables(cfg, o, M):
+    """div_damp_init (div_damp_mod.F90:27-80) with the reference's pressures:
+    vert_coord_calc_ph(k, p0) = hyam (p0_hybrid - ptop_local) + hybm (p0 -
+    ptop_local) + ptop_local (hybrid_coord_mod.F90:146-152), where test_l26
+    keeps ptop_local = 0 and resets the namelist ptop to p0_hybrid hyai(1)
+    (hybrid_coord_test_mod.F90:145) and the wrf templates set ptop_local =
+    ptop (hybrid_coord_mod.F90:78-90)."""
+    nlat, nhalf, nlev = cfg.nlat, cfg.nlat - 1, cfg.nlev
+    c_lon, c_lat = np.zeros((nlev, nlat)), np.zeros((nlev, nhalf))
+    amp = np.ones(nlev)
+    if cfg.baroclinic:
+        hyai, hyam, hybm = o.metric("hyai", nlev + 1), o.metric("hyam", nlev), o.metric("hybm", nlev)
+        test_l26 = cfg.vert_coord_template == 26
+        local_ptop = 0.0 if test_l26 else cfg.ptop
+        ptop = cfg.hybrid_coord_p0 * hyai[0] if test_l26 else cfg.ptop
+        for k in range(nlev):
+            ph = hyam[k] * (cfg.hybrid_coord_p0 - local_ptop) + hybm[k] * (cfg.p0 - local_ptop) + local_ptop
+            amp[k] = max(1.0, 8 * (1 + math.tanh(math.log(ptop / ph))))
+    for k in range(nlev):
+        for j in range(1, nlat - 1):
+            le, de = M["le_lon"][j], M["de_lon"][j]
+            if cfg.div_damp_order == 4:
+                c_lon[k, j] = cfg.div_damp_coef4 * (le * le) * (de * de)
+            elif cfg.baroclinic:
+                c_lon[k, j] = cfg.div_damp_coef2 * amp[k] * le * de
+            else:
+                c_lon[k, j] = cfg.div_damp_coef2 * le * de
+        for j in range(nhalf):
+            le, de = M["le_lat"][j], M["de_lat"][j]
+            if cfg.div_damp_order == 4:
+                c_lat[k, j] = cfg.div_damp_coef4 * (le * le) * (de * de)
+            elif cfg.baroclinic:
+                c_lat[k, j] = cfg.div_damp_coef2 * amp[k] * le * de
+            else:
+                c_lat[k, j] = cfg.div_damp_coef2 * le * de
+    return c_lon, c_lat, amp
+
+
+@pytest.mark.parametrize("case", ["swm_order2", "test_l26_order2", "wrf_l32_order2", "test_l26_order4"])
+def test_divergence_damping_coefficients_match_restatement(case):
+    from helpers import baroclinic_config
+    kw = dict(use_div_damp=1, div_damp_order=4 if case.endswith("4") else 2, div_damp_coef2=1.0 / 128,
+              div_damp_coef4=0.01)
+    if case == "swm_order2":
+        cfg = swm_config(nlon=72, nlat=37, dt=600.0, **kw)
+    else:
+        cfg = baroclinic_config(nlon=72, nlat=37, nlev=32 if "l32" in case else 26, dt=600.0, **kw)
+    M = restated(cfg)
+    o = Oracle(cfg)
+    try:
+        want_lon, want_lat, amp = div_damp_tables(cfg, o, M)
+        got_lon = o.metric("div_c_lon", cfg.nlev * cfg.nlat).reshape(cfg.nlev, cfg.nlat)
+        got_lat = o.metric("div_c_lat", cfg.nlev * (cfg.nlat - 1)).reshape(cfg.nlev, cfg.nlat - 1)
+    finally:
+        o.close()
+    if case.endswith("order2") and case != "swm_order2":
+        assert amp.max() > 1.0   # the upper levels are amplified
+    for got, want in ((got_lon, want_lon), (got_lat, want_lat)):
+        err = np.abs(got - want).max() / np.abs(want).max()
+        assert err <= 4 * np.finfo(float).eps, (case, err)
