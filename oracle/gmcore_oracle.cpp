@@ -1762,11 +1762,12 @@ int orc_set_tracer(void *h, int l, const double *src) {
   // leaves the second level uninitialised, adv_mod.F90:390).
   for (int s = 0; s < 2; ++s) {
     orc::Arr &q = m->tracers.q[s][l];
-    size_t o = 0;
     #pragma omp parallel for schedule(static)
-    for (int k = 1; k <= nlev; ++k)
+    for (int k = 1; k <= nlev; ++k) {
+      size_t o = (size_t)(k - 1) * nlat * nlon;   // each level from its own offset
       for (int j = 1; j <= nlat; ++j)
         for (int i = 1; i <= nlon; ++i) q(i, j, k) = src[o++];
+    }
     m->fill_halo(q, true);
   }
   return GMC_OK;
@@ -1777,11 +1778,12 @@ int orc_get_tracer(void *h, int l, double *dst) {
   if (!m->has_tracers || l < 0 || l >= m->cfg.ntracer) return GMC_EINVAL;
   const int nlon = m->mesh.nlon, nlat = m->mesh.nlat, nlev = m->mesh.nlev;
   orc::Arr &q = m->tracers.q[m->tracers.old_idx][l];
-  size_t o = 0;
   #pragma omp parallel for schedule(static)
-  for (int k = 1; k <= nlev; ++k)
+  for (int k = 1; k <= nlev; ++k) {
+    size_t o = (size_t)(k - 1) * nlat * nlon;
     for (int j = 1; j <= nlat; ++j)
       for (int i = 1; i <= nlon; ++i) dst[o++] = q(i, j, k);
+  }
   return GMC_OK;
 }
 

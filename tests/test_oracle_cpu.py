@@ -213,3 +213,25 @@ def test_coriolis_does_no_work_for_any_pv_interpolation(pv_scheme):
         assert scale > 0, name
         assert abs(val) <= 1e-13 * scale, (pv_scheme, name, val, scale)
     o.close()
+
+
+def test_openmp_build_matches_parity_build_with_tracers():
+    """The OpenMP build of the oracle (the CPU baseline and the reference arm
+    of the benchmark) copies tracers in and out level by level in parallel
+    and must reproduce the parity build bit for bit, tracers included."""
+    import os
+    os.environ.setdefault("OMP_NUM_THREADS", "4")
+    cfg = baroclinic_config(ntracer=2)
+    st = initial_state(cfg)
+    out = {}
+    for variant in ("parity", "omp"):
+        o = Oracle(cfg, variant=variant)
+        load_state(o, st)
+        for l in range(2):
+            assert np.array_equal(o.get_tracer(l), st["q"][l]), (variant, l)
+        o.prepare()
+        o.step(4)
+        out[variant] = [o.get_field(f) for f in ("u_lon", "v_lat", "pt", "phs")] + [o.get_tracer(l) for l in range(2)]
+        o.close()
+    for a, b in zip(out["parity"], out["omp"]):
+        assert np.array_equal(a, b)
