@@ -1806,6 +1806,51 @@ int orc_space_identities(void *h, double *out) {
   return 0;
 }
 
+// One pass of the space operators on state(old), for the known-answer tests:
+// pass 0 the forward pass (space_operators_fwd) into tend[0]; pass 1 the
+// backward pass's prepare (calc_ph, calc_t, calc_gz_lev, calc_m) and the
+// pressure-gradient force into tend[1].
+int orc_run_pass(void *h, int pass) {
+  orc::Model *m = (orc::Model *)h;
+  orc::State &s = m->state[m->old_i];
+  if (pass == 0) {
+    m->space_operators_fwd(s, m->tend[0], m->cfg.dt_dyn);
+  } else if (pass == 1) {
+    m->operators_prepare_bwd(s);
+    m->pgf_run(s, m->tend[1]);
+  } else {
+    return GMC_EINVAL;
+  }
+  return m->err.code;
+}
+
+// A tendency of tend[pass] by name, interior-only [k][j][i] (dphs: [j][i]).
+int orc_get_tend(void *h, int pass, const char *name, double *dst) {
+  orc::Model *m = (orc::Model *)h;
+  if (pass < 0 || pass > 1) return GMC_EINVAL;
+  orc::Tend &t = m->tend[pass];
+  const int nlat = m->mesh.nlat, nhalf = m->mesh.nhalf, nlev = m->mesh.nlev;
+  struct T { const char *name; orc::Arr *a; int nrow, nk; };
+  const T tab[] = {{"du", &t.du, nlat, nlev},           {"dv", &t.dv, nhalf, nlev},
+                   {"dgz", &t.dgz, nlat, nlev},         {"dpt", &t.dpt, nlat, nlev},
+                   {"dphs", &t.dphs, nlat, 1},          {"qhu", &t.qhu, nhalf, nlev},
+                   {"qhv", &t.qhv, nlat, nlev},         {"dkedlon", &t.dkedlon, nlat, nlev},
+                   {"dkedlat", &t.dkedlat, nhalf, nlev}, {"dmfdlon", &t.dmfdlon, nlat, nlev},
+                   {"dmfdlat", &t.dmfdlat, nlat, nlev}, {"dptfdlon", &t.dptfdlon, nlat, nlev},
+                   {"dptfdlat", &t.dptfdlat, nlat, nlev}, {"dptfdlev", &t.dptfdlev, nlat, nlev},
+                   {"pgf_lon", &t.pgf_lon, nlat, nlev}, {"pgf_lat", &t.pgf_lat, nhalf, nlev},
+                   {"wedudlev", &t.wedudlev, nlat, nlev}, {"wedvdlev", &t.wedvdlev, nhalf, nlev}};
+  for (const T &e : tab) {
+    if (std::strcmp(name, e.name)) continue;
+    size_t o = 0;
+    for (int k = 1; k <= e.nk; ++k)
+      for (int j = 1; j <= e.nrow; ++j)
+        for (int i = 1; i <= m->mesh.nlon; ++i) dst[o++] = (*e.a)(i, j, k);
+    return GMC_OK;
+  }
+  return GMC_EINVAL;
+}
+
 int orc_diagnose(void *h, double *out) {
   ((orc::Model *)h)->diagnose(out);
   return GMC_OK;

@@ -45,6 +45,8 @@ def load(variant="parity"):
     lib.orc_metric.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int]
     lib.orc_filter_taps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]
     lib.orc_filter_weights.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int]
+    lib.orc_run_pass.argtypes = [C.c_void_p, C.c_int]
+    lib.orc_get_tend.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_double)]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
     _LIBS[variant] = lib
     return lib
@@ -154,6 +156,25 @@ class Oracle:
         n = self.cfg.nlat - 1 if lat else self.cfg.nlat
         out = np.zeros(n, dtype=np.int32)
         self.lib.orc_filter_taps(self.h, which, lat, out.ctypes.data_as(C.POINTER(C.c_int)))
+        return out
+
+    def run_pass(self, which):
+        """One space-operator pass on state(old): 0 forward, 1 backward
+        (prepare and pressure-gradient force)."""
+        rc = self.lib.orc_run_pass(self.h, which)
+        if rc:
+            raise RuntimeError(f"oracle pass {which} failed ({rc})")
+
+    TEND_HALF = {"dv", "qhu", "dkedlat", "pgf_lat", "wedvdlev"}
+
+    def get_tend(self, which, name):
+        """A tendency of the last run_pass(which), [k][j][i] ([j][i] for dphs)."""
+        c = self.cfg
+        nrow = c.nlat - 1 if name in self.TEND_HALF else c.nlat
+        shape = (nrow, c.nlon) if name == "dphs" else (c.nlev, nrow, c.nlon)
+        out = np.zeros(shape)
+        if self.lib.orc_get_tend(self.h, which, name.encode(), _ptr(out)):
+            raise KeyError(name)
         return out
 
     def filter_weights(self, which, lat, j):

@@ -45,12 +45,15 @@ def ring(x):
 
 def prepared(cfg, seed=7):
     """The oracle after the run prologue on a seeded state, with a smooth
-    meridional wind added (the seeded jets have v = 0)."""
+    meridional wind added and the winds sheared in the vertical (the seeded
+    jets have v = 0, no shear and no zonal variation)."""
     st = initial_state(cfg, seed)
-    v = st["v_lat"]
+    shear = (1.0 + 0.03 * np.arange(cfg.nlev))[:, None, None]
     lon = np.arange(cfg.nlon) * 2 * np.pi / cfg.nlon
+    st["u_lon"] = st["u_lon"] * shear * (1.0 + 0.2 * np.sin(2 * lon))[None, None, :]
+    v = st["v_lat"]
     lat = np.linspace(-np.pi / 2, np.pi / 2, cfg.nlat + 1)[1:-1]
-    st["v_lat"] = v + 8.0 * np.cos(lat)[None, :, None] * np.sin(3 * lon + 0.5)[None, None, :] * np.ones((v.shape[0], 1, 1))
+    st["v_lat"] = v + 8.0 * np.cos(lat)[None, :, None] * np.sin(3 * lon + 0.5)[None, None, :] * shear
     o = Oracle(cfg)
     load_state(o, st)
     o.prepare()
@@ -223,5 +226,121 @@ def test_horizontal_operators_match_restatement(case):
             assert got.shape == want.shape, name
             assert np.abs(want).max() > 0, name
             assert close(got, want), (case, name)
+    finally:
+        o.close()
+
+
+# ---------------------------------------------------------------------------
+# tendencies of the forward pass (space_operators, gmcore_mod.F90:467-528)
+# and the pressure-gradient force of the backward pass
+# ---------------------------------------------------------------------------
+def forward_tendencies(cfg, o):
+    """calc_coriolis scheme 1 (:846-906), calc_grad_ke (:908-937),
+    calc_grad_mf (:939-1006), calc_dphsdt (:1120-1143), calc_we_lev
+    (:192-232, area-weighted edge means interp_mod.F90:308-436) and
+    calc_wedudlev_wedvdlev (SB81, :1145-1216), from the pass's own
+    diagnostics."""
+    nlat, nhalf, nlon, nlev = cfg.nlat, cfg.nlat - 1, cfg.nlon, cfg.nlev
+    M = {n: o.metric(n, nlat) for n in ("de_lon", "le_lon", "area_cell", "area_lon", "area_lon_west",
+                                         "area_lon_east", "full_tangent_wgt1", "full_tangent_wgt2")}
+    M.update({n: o.metric(n, nhalf) for n in ("de_lat", "le_lat", "area_lat", "area_lat_north", "area_lat_south",
+                                             "half_tangent_wgt1", "half_tangent_wgt2")})
+    col = lambda n: M[n][None, :, None]
+    F = {n: o.get_field(n) for n in ("mfx_lon", "mfy_lat", "pv_lon", "pv_lat", "ke", "u_f", "v_f", "m")}
+    mfx, mfy, pvx, pvy, ke = F["mfx_lon"], F["mfy_lat"], F["pv_lon"], F["pv_lat"], F["ke"]
+    I = slice(1, nlat - 1)
+    out = {}
+    out["qhu"] = (col("half_tangent_wgt1") * (prev(mfx[:, :-1]) * (pvy + prev(pvx[:, :-1])) +
+                                               mfx[:, :-1] * (pvy + pvx[:, :-1])) +
+                  col("half_tangent_wgt2") * (prev(mfx[:, 1:]) * (pvy + prev(pvx[:, 1:])) +
+                                               mfx[:, 1:] * (pvy + pvx[:, 1:]))) * 0.5, None
+    pc = pvx[:, I]
+    out["qhv"] = (col("full_tangent_wgt1")[:, I] * (mfy[:, :-1] * (pc + pvy[:, :-1]) +
+                                                     nxt(mfy[:, :-1]) * (pc + nxt(pvy[:, :-1]))) +
+                  col("full_tangent_wgt2")[:, I] * (mfy[:, 1:] * (pc + pvy[:, 1:]) +
+                                                     nxt(mfy[:, 1:]) * (pc + nxt(pvy[:, 1:])))) * 0.5, I
+    out["dkedlon"] = (nxt(ke[:, I]) - ke[:, I]) / col("de_lon")[:, I], I
+    out["dkedlat"] = (ke[:, 1:] - ke[:, :-1]) / col("de_lat"), None
+    out["dmfdlon"] = (mfx[:, I] - prev(mfx[:, I])) * col("le_lon")[:, I] / col("area_cell")[:, I], I
+    dmfdlat = np.zeros((nlev, nlat, nlon))
+    dmfdlat[:, I] = (mfy[:, 1:] * col("le_lat")[:, 1:] - mfy[:, :-1] * col("le_lat")[:, :-1]) / col("area_cell")[:, I]
+    dmfdlat[:, 0] = (ring(mfy[:, 0]) * M["le_lat"][0] / nlon / M["area_cell"][0])[:, None]
+    dmfdlat[:, -1] = (ring(-mfy[:, -1]) * M["le_lat"][-1] / nlon / M["area_cell"][-1])[:, None]
+    out["dmfdlat"] = dmfdlat, None
+    if not cfg.baroclinic:
+        return out
+    dmfdlon = o.get_tend(0, "dmfdlon")          # pole rows as the pass leaves them
+    dmfdlon[:, I] = out["dmfdlon"][0]
+    dphs = np.zeros((nlat, nlon))
+    for k in range(nlev):
+        dphs = dphs - dmfdlon[k] - dmfdlat[k]
+    out["dphs"] = dphs, None
+    hybi = o.metric("hybi", nlev + 1)
+    we = np.zeros((nlev + 1, nlat, nlon))
+    mf = np.zeros((nlat, nlon))
+    for k in range(1, nlev):
+        mf = mf + dmfdlon[k - 1] + dmfdlat[k - 1]
+        we[k] = -(hybi[k] * dphs) - mf
+    out["we_lev"] = we, None
+    we_lon = (col("area_lon_west")[:, I] * we[:, I] + col("area_lon_east")[:, I] * nxt(we[:, I])) / col("area_lon")[:, I]
+    we_lat = (col("area_lat_north") * we[:, 1:] + col("area_lat_south") * we[:, :-1]) / col("area_lat")
+    m = F["m"]
+    m_lon, m_lat = ((m + nxt(m)) * 0.5)[:, I], (m[:, :-1] + m[:, 1:]) * 0.5
+
+    def sb81(w, x, mm):
+        r = np.zeros_like(x)
+        r[1:-1] = (w[2:-1] * (x[2:] - x[1:-1]) + w[1:-2] * (x[1:-1] - x[:-2])) / mm[1:-1] / 2.0
+        r[0] = (w[1] * (x[1] - x[0])) / mm[0] / 2.0
+        r[-1] = (w[-2] * (x[-1] - x[-2])) / mm[-1] / 2.0
+        return r
+    out["wedudlev"] = sb81(we_lon, F["u_f"][:, I], m_lon), I
+    out["wedvdlev"] = sb81(we_lat, F["v_f"], m_lat), None
+    out["du"] = out["qhv"][0] - out["dkedlon"][0] - out["wedudlev"][0], I
+    out["dv"] = -out["qhu"][0] - out["dkedlat"][0] - out["wedvdlev"][0], None
+    return out
+
+
+def pressure_gradient(cfg, o):
+    """pgf_lin97_run, hydrostatic (pgf_lin97_mod.F90:20-105), or pgf_swm_run
+    (pgf_swm_mod.F90:18-46)."""
+    nlat, nhalf = cfg.nlat, cfg.nlat - 1
+    de_lon, de_lat = o.metric("de_lon", nlat)[None, :, None], o.metric("de_lat", nhalf)[None, :, None]
+    I = slice(1, nlat - 1)
+    if not cfg.baroclinic:
+        gz = o.get_field("gz_f")
+        return {"pgf_lon": ((nxt(gz[:, I]) - gz[:, I]) / de_lon[:, I], I),
+                "pgf_lat": ((gz[:, 1:] - gz[:, :-1]) / de_lat, None)}
+    E, Z = o.get_field("ph_exn_lev"), o.get_field("gz_lev")
+
+    def lin97(e0, e1, z0, z1, de):
+        """Corners: 0 this side, 1 the other; [:-1] level k, [1:] level k+1."""
+        dph1 = e1[1:] - e0[:-1]
+        dph2 = e0[1:] - e1[:-1]
+        dgz1 = z0[1:] - z1[:-1]
+        dgz2 = z0[:-1] - z1[1:]
+        return -(dph1 * dgz1 + dph2 * dgz2) / de / (dph1 + dph2)
+    return {"pgf_lon": (lin97(E[:, I], nxt(E[:, I]), Z[:, I], nxt(Z[:, I]), de_lon[:, I]), I),
+            "pgf_lat": (lin97(E[:, :-1], E[:, 1:], Z[:, :-1], Z[:, 1:], de_lat), None)}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_tendencies_match_restatement(case):
+    cfg = CASES[case]()
+    o = prepared(cfg)
+    try:
+        o.run_pass(0)
+        for name, (want, rows) in forward_tendencies(cfg, o).items():
+            got = o.get_field(name) if name == "we_lev" else o.get_tend(0, name)
+            if rows is not None:
+                got = got[:, rows]
+            assert got.shape == want.shape, name
+            assert np.abs(want).max() > 0, name
+            assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
+        o.run_pass(1)
+        for name, (want, rows) in pressure_gradient(cfg, o).items():
+            got = o.get_tend(1, name)
+            if rows is not None:
+                got = got[:, rows]
+            assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
