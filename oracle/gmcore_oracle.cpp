@@ -1851,6 +1851,27 @@ int orc_get_tend(void *h, int pass, const char *name, double *dst) {
   return GMC_EINVAL;
 }
 
+// A field of the dynamic mass batch (adv_batch_mass) as the last pass left it,
+// interior-only [k][j][i]: the winds u, v it holds, the Courant numbers cflx,
+// cfly and the axis divergences divx, divy (adv_batch_mod.F90:218-377).
+int orc_get_batch(void *h, const char *name, double *dst) {
+  orc::Model *m = (orc::Model *)h;
+  orc::Batch &b = m->mass;
+  const int nlat = m->mesh.nlat, nhalf = m->mesh.nhalf, nlev = m->mesh.nlev;
+  struct T { const char *name; orc::Arr *a; int nrow; };
+  const T tab[] = {{"u", &b.u, nlat},       {"v", &b.v, nhalf},       {"cflx", &b.cflx, nlat},
+                   {"cfly", &b.cfly, nhalf}, {"divx", &b.divx, nlat}, {"divy", &b.divy, nlat}};
+  for (const T &e : tab) {
+    if (std::strcmp(name, e.name)) continue;
+    size_t o = 0;
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= e.nrow; ++j)
+        for (int i = 1; i <= m->mesh.nlon; ++i) dst[o++] = (*e.a)(i, j, k);
+    return GMC_OK;
+  }
+  return GMC_EINVAL;
+}
+
 int orc_diagnose(void *h, double *out) {
   ((orc::Model *)h)->diagnose(out);
   return GMC_OK;

@@ -47,6 +47,7 @@ def load(variant="parity"):
     lib.orc_filter_weights.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int]
     lib.orc_run_pass.argtypes = [C.c_void_p, C.c_int]
     lib.orc_get_tend.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_double)]
+    lib.orc_get_batch.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
     _LIBS[variant] = lib
     return lib
@@ -174,6 +175,15 @@ class Oracle:
         shape = (nrow, c.nlon) if name == "dphs" else (c.nlev, nrow, c.nlon)
         out = np.zeros(shape)
         if self.lib.orc_get_tend(self.h, which, name.encode(), _ptr(out)):
+            raise KeyError(name)
+        return out
+
+    def get_batch(self, name):
+        """A field of the dynamic mass batch (u, v, cflx, cfly, divx, divy)."""
+        c = self.cfg
+        nrow = c.nlat - 1 if name in ("v", "cfly") else c.nlat
+        out = np.zeros((c.nlev, nrow, c.nlon))
+        if self.lib.orc_get_batch(self.h, name.encode(), _ptr(out)):
             raise KeyError(name)
         return out
 

@@ -43,7 +43,7 @@ def ring(x):
     return np.cumsum(x, axis=-1)[..., -1]
 
 
-def prepared(cfg, seed=7):
+def prepared(cfg, seed=7, u_wave=0.0):
     """The oracle after the run prologue on a seeded state, with a smooth
     meridional wind added and the winds sheared in the vertical (the seeded
     jets have v = 0, no shear and no zonal variation)."""
@@ -51,6 +51,9 @@ def prepared(cfg, seed=7):
     shear = (1.0 + 0.03 * np.arange(cfg.nlev))[:, None, None]
     lon = np.arange(cfg.nlon) * 2 * np.pi / cfg.nlon
     st["u_lon"] = st["u_lon"] * shear * (1.0 + 0.2 * np.sin(2 * lon))[None, None, :]
+    # optional wavenumber-2 zonal wind of both signs that keeps its strength
+    # up to the poles (Courant numbers beyond one cell where rows are short)
+    st["u_lon"] = st["u_lon"] + u_wave * np.sin(2 * (lon + np.pi / cfg.nlon))[None, None, :]
     v = st["v_lat"]
     lat = np.linspace(-np.pi / 2, np.pi / 2, cfg.nlat + 1)[1:-1]
     st["v_lat"] = v + 8.0 * np.cos(lat)[None, :, None] * np.sin(3 * lon + 0.5)[None, None, :] * shear
@@ -341,6 +344,93 @@ def test_tendencies_match_restatement(case):
             got = o.get_tend(1, name)
             if rows is not None:
                 got = got[:, rows]
+            assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
+    finally:
+        o.close()
+
+
+# ---------------------------------------------------------------------------
+# the dynamic mass batch: Courant numbers from RK4 departure points and the
+# axis divergences (adv_batch_accum_uv_cell, adv_batch_mod.F90:218-377)
+# ---------------------------------------------------------------------------
+def batch_courant(cfg, o, dt):
+    nlat, nhalf, nlon, nlev = cfg.nlat, cfg.nlat - 1, cfg.nlon, cfg.nlev
+    R = cfg.radius
+    dlon = (2 * math.pi - 0.0) / nlon
+    half_lon = lambda l: (0.0 + (l - 1) * dlon) + 0.5 * dlon          # any index, halo included
+    u, v = o.get_batch("u"), o.get_batch("v")
+    fcos, hlat = o.metric("full_cos_lat", nlat), o.metric("half_lat", nhalf)
+    de_lon, de_lat = o.metric("de_lon", nlat), o.metric("de_lat", nhalf)
+    le_lon, le_lat, area = o.metric("le_lon", nlat), o.metric("le_lat", nhalf), o.metric("area_cell", nlat)
+    I = slice(1, nlat - 1)
+    # x: rows 2..nlat-1, faces i = 1..nlon; u at any face index by the wrap
+    ii = np.arange(1, nlon + 1)[None, None, :].astype(float)
+    cos = fcos[None, I, None]
+    dx = de_lon[None, I, None]
+    uI = u[:, I]
+    uat = lambda l: np.take_along_axis(uI, (l - 1) % nlon, axis=-1)
+    x0 = R * half_lon(ii) * cos
+
+    def ux(x):
+        l = np.floor(ii + (x - x0) / dx).astype(np.int64)
+        return ((R * half_lon(l + 1) * cos - x) * uat(l) + (x - R * half_lon(l) * cos) * uat(l + 1)) / dx
+    u1 = uI
+    x1 = x0 + dt / 2 * u1
+    u2 = ux(x1)
+    x2 = x0 + dt / 2 * u2
+    u3 = ux(x2)
+    x3 = x0 + dt * u3
+    u4 = ux(x3)
+    cflx = (u1 + 2 * u2 + 2 * u3 + u4) / 6 * dt / dx
+    # y: half rows 1..nhalf; outside 1..nhalf-1 the first stage's wind
+    jj = np.arange(1, nhalf + 1)[None, :, None].astype(float)
+    dy = de_lat[None, :, None]
+    y0 = R * hlat[None, :, None]
+    hl = lambda l: hlat[np.clip(l, 1, nhalf) - 1]
+
+    def vy(y, v1):
+        l = np.floor(jj + (y - y0) / dy).astype(np.int64) * np.ones_like(v1, dtype=np.int64)
+        inside = (l >= 1) & (l <= nhalf - 1)
+        lc = np.clip(l, 1, nhalf - 1)
+        va = np.take_along_axis(v, lc - 1, axis=1)
+        vb = np.take_along_axis(v, lc, axis=1)
+        interp = ((R * hl(lc + 1) - y) * va + (y - R * hl(lc)) * vb) / dy
+        return np.where(inside, interp, v1)
+    v1 = v
+    y1 = y0 + dt / 2 * v1
+    v2 = vy(y1, v1)
+    y2 = y0 + dt / 2 * v2
+    v3 = vy(y2, v1)
+    y3 = y0 + dt * v3
+    v4 = vy(y3, v1)
+    cfly = (v1 + 2 * v2 + 2 * v3 + v4) / 6 * dt / dy
+    divx = (uI - prev(uI)) * le_lon[None, I, None] / area[None, I, None]
+    divy = np.zeros((nlev, nlat, nlon))
+    divy[:, I] = (v[:, 1:] * le_lat[None, 1:, None] - v[:, :-1] * le_lat[None, :-1, None]) / area[None, I, None]
+    divy[:, 0] = (ring(v[:, 0]) * le_lat[0] / nlon / area[0])[:, None]
+    divy[:, -1] = (ring(-v[:, -1]) * le_lat[-1] / nlon / area[-1])[:, None]
+    return {"cflx": (cflx, I), "cfly": (cfly, None), "divx": (divx, I), "divy": (divy, None)}
+
+
+@pytest.mark.parametrize("case", ["baroclinic_5deg_l26", "baroclinic_4deg_wrf_l32", "long_step"])
+def test_batch_courant_numbers_match_restatement(case):
+    if case == "long_step":   # departure points several cells away, winds of both signs
+        cfg = baroclinic_config(dt=1200.0)
+        o = prepared(cfg, u_wave=60.0)
+    else:
+        cfg = CASES[case]()
+        o = prepared(cfg)
+    try:
+        o.run_pass(0)
+        if case == "long_step":
+            assert np.abs(o.get_batch("cflx")).max() > 1.0 and o.get_batch("u").min() < 0.0
+        assert np.array_equal(o.get_batch("u")[:, 1:-1], o.get_field("u_f")[:, 1:-1])   # the dynamic batch copies
+        for name, (want, rows) in batch_courant(cfg, o, cfg.dt_dyn).items():
+            got = o.get_batch(name)
+            if rows is not None:
+                got = got[:, rows]
+            assert got.shape == want.shape, name
+            assert np.abs(want).max() > 0, name
             assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
