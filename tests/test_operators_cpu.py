@@ -434,3 +434,43 @@ def test_batch_courant_numbers_match_restatement(case):
             assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
+
+
+# ---------------------------------------------------------------------------
+# the polar filters applied by the run prologue (gmcore_mod.F90:109-122):
+# u_f, v_f and phs_f / gz_f are the big filter of u_lon, v_lat, phs / gz
+# (filter_on_lon_edge / _lat_edge / _cell, filter_mod.F90:25-163)
+# ---------------------------------------------------------------------------
+def filter_rows(o, x, lat):
+    """tmp(i) = sum(wgt(:n,j) * x(i-hn:i+hn,j)), summed over the taps in
+    order, on rows with more than one tap; other rows copied."""
+    y = x.copy()
+    taps = o.filter_taps(0, lat)
+    for j in range(x.shape[-2]):
+        n = int(taps[j])
+        if n <= 1:
+            continue
+        w, hn = o.filter_weights(0, lat, j + 1), (n - 1) // 2
+        row = x[..., j, :]
+        acc = np.zeros_like(row)
+        for t in range(n):
+            acc = acc + w[t] * np.roll(row, hn - t, axis=-1)     # x(i - hn + t)
+        y[..., j, :] = acc
+    return y
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_prologue_filters_match_restatement(case):
+    cfg = CASES[case]()
+    o = prepared(cfg)
+    try:
+        pairs = [("u_lon", "u_f", 0), ("v_lat", "v_f", 1)]
+        pairs.append(("phs", "phs_f", 0) if cfg.baroclinic else ("gz", "gz_f", 0))
+        for src, dst, lat in pairs:
+            x = o.get_field(src)
+            want = filter_rows(o, x, lat)
+            got = o.get_field(dst)
+            assert not np.array_equal(want, x), dst          # some rows are filtered
+            assert close(got, want), (case, dst, float(np.abs(got - want).max() / np.abs(want).max()))
+    finally:
+        o.close()
