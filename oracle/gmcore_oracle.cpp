@@ -1853,18 +1853,23 @@ int orc_get_tend(void *h, int pass, const char *name, double *dst) {
 
 // A field of the dynamic mass batch (adv_batch_mass) as the last pass left it,
 // interior-only [k][j][i]: the winds u, v it holds, the Courant numbers cflx,
-// cfly and the axis divergences divx, divy (adv_batch_mod.F90:218-377).
+// cfly and the axis divergences divx, divy (adv_batch_mod.F90:218-377); on
+// half levels the vertical mass flux we, the half-level mass m_lev and the
+// vertical Courant number cflz (:493-632).
 int orc_get_batch(void *h, const char *name, double *dst) {
   orc::Model *m = (orc::Model *)h;
   orc::Batch &b = m->mass;
   const int nlat = m->mesh.nlat, nhalf = m->mesh.nhalf, nlev = m->mesh.nlev;
-  struct T { const char *name; orc::Arr *a; int nrow; };
-  const T tab[] = {{"u", &b.u, nlat},       {"v", &b.v, nhalf},       {"cflx", &b.cflx, nlat},
-                   {"cfly", &b.cfly, nhalf}, {"divx", &b.divx, nlat}, {"divy", &b.divy, nlat}};
+  struct T { const char *name; orc::Arr *a; int nrow, nk; };
+  const T tab[] = {{"u", &b.u, nlat, nlev},          {"v", &b.v, nhalf, nlev},
+                   {"cflx", &b.cflx, nlat, nlev},    {"cfly", &b.cfly, nhalf, nlev},
+                   {"divx", &b.divx, nlat, nlev},    {"divy", &b.divy, nlat, nlev},
+                   {"we", &b.we, nlat, nlev + 1},    {"m_lev", &b.m_lev, nlat, nlev + 1},
+                   {"cflz", &b.cflz, nlat, nlev + 1}};
   for (const T &e : tab) {
     if (std::strcmp(name, e.name)) continue;
     size_t o = 0;
-    for (int k = 1; k <= nlev; ++k)
+    for (int k = 1; k <= e.nk; ++k)
       for (int j = 1; j <= e.nrow; ++j)
         for (int i = 1; i <= m->mesh.nlon; ++i) dst[o++] = (*e.a)(i, j, k);
     return GMC_OK;

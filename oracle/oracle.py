@@ -179,10 +179,12 @@ class Oracle:
         return out
 
     def get_batch(self, name):
-        """A field of the dynamic mass batch (u, v, cflx, cfly, divx, divy)."""
+        """A field of the dynamic mass batch (u, v, cflx, cfly, divx, divy;
+        on half levels we, m_lev, cflz)."""
         c = self.cfg
         nrow = c.nlat - 1 if name in ("v", "cfly") else c.nlat
-        out = np.zeros((c.nlev, nrow, c.nlon))
+        nk = c.nlev + 1 if name in ("we", "m_lev", "cflz") else c.nlev
+        out = np.zeros((nk, nrow, c.nlon))
         if self.lib.orc_get_batch(self.h, name.encode(), _ptr(out)):
             raise KeyError(name)
         return out

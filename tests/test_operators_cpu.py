@@ -474,3 +474,83 @@ def test_prologue_filters_match_restatement(case):
             assert close(got, want), (case, dst, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
+
+
+# ---------------------------------------------------------------------------
+# the vertical Courant number of the mass batch: RK4 in eta with a level
+# search, then the Lagrangian walk over whole layers (adv_batch_accum_we_lev,
+# adv_batch_mod.F90:493-632; level spacings vert_coord_mod.F90:84-101)
+# ---------------------------------------------------------------------------
+def vertical_courant(cfg, o, dt):
+    nlev = cfg.nlev
+    hl, fl = [0.0] + list(o.metric("half_lev", nlev + 1)), [0.0] + list(o.metric("full_lev", nlev))   # 1-based
+    full_dlev = [0.0] + [hl[k + 1] - hl[k] for k in range(1, nlev + 1)]
+    half_dlev = [0.0] * (nlev + 2)
+    for k in range(2, nlev + 1):
+        half_dlev[k] = fl[k] - fl[k - 1]
+    half_dlev[1] = fl[1] - hl[1]
+    half_dlev[nlev + 1] = hl[nlev + 1] - fl[nlev]
+    we, mlev = o.get_batch("we"), o.get_batch("m_lev")
+    cflz = o.get_batch("cflz").copy()          # the boundary levels as the batch keeps them
+    _, nlat, nlon = we.shape
+
+    def find(k, z, w):
+        if w > 0:
+            for l in range(k, nlev + 1):
+                if hl[l] <= z <= hl[l + 1]:
+                    return l
+        else:
+            for l in range(k - 1, 0, -1):
+                if hl[l] <= z <= hl[l + 1]:
+                    return l
+        raise AssertionError("cflz exceeds range")
+
+    for j in range(nlat):
+        for i in range(nlon):
+            W = [0.0] + [float(x) for x in we[:, j, i]]
+            Ml = [0.0] + [float(x) for x in mlev[:, j, i]]
+            for k in range(2, nlev + 1):
+                z0 = hl[k]
+                w1 = W[k] / Ml[k] * half_dlev[k]
+                z1 = z0 + dt / 2 * w1
+                l = find(k, z1, w1)
+                w2 = ((hl[l + 1] - z1) * W[l] / Ml[l] * half_dlev[l] +
+                      (z1 - hl[l]) * W[l + 1] / Ml[l + 1] * half_dlev[l + 1]) / full_dlev[l]
+                z2 = z0 + dt / 2 * w2
+                l = find(k, z2, w2)
+                w3 = ((hl[l + 1] - z2) * W[l] / Ml[l] * half_dlev[l] +
+                      (z2 - hl[l]) * W[l + 1] / Ml[l + 1] * half_dlev[l + 1]) / full_dlev[l]
+                z3 = z0 + dt * w3
+                l = find(k, z3, w3)
+                w4 = ((hl[l + 1] - z3) * W[l] / Ml[l] * half_dlev[l] +
+                      (z3 - hl[l]) * W[l + 1] / Ml[l + 1] * half_dlev[l + 1]) / full_dlev[l]
+                deta = (w1 + 2 * w2 + 2 * w3 + w4) / 6 * dt
+                ks, ke, s = (k - 1, 1, -1) if deta < 0 else (k, nlev, 1)
+                deta = abs(deta)
+                for l in range(ks, ke + s, s):
+                    deta = deta - full_dlev[l]
+                    if deta < 0:
+                        cflz[k - 1, j, i] = s * ((1 + deta / full_dlev[l]) + abs(l - ks))
+                        break
+    return cflz
+
+
+@pytest.mark.parametrize("case", ["baroclinic_5deg_l26", "long_step"])
+def test_vertical_courant_numbers_match_restatement(case):
+    if case == "long_step":
+        cfg = baroclinic_config(dt=1200.0)
+        o = prepared(cfg, u_wave=60.0)
+    else:
+        cfg = CASES[case]()
+        o = prepared(cfg)
+    try:
+        o.run_pass(0)
+        assert np.array_equal(o.get_batch("we"), o.get_field("we_lev"))      # the dynamic batch copies
+        want = vertical_courant(cfg, o, cfg.dt_dyn)
+        got = o.get_batch("cflz")
+        assert np.abs(want[1:-1]).max() > 0
+        if case == "long_step":
+            assert np.abs(got).max() > 1.0      # departure beyond the adjacent layer
+        assert close(got, want), (case, float(np.abs(got - want).max() / np.abs(want).max()))
+    finally:
+        o.close()
