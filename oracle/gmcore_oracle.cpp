@@ -1855,7 +1855,8 @@ int orc_get_tend(void *h, int pass, const char *name, double *dst) {
 // interior-only [k][j][i]: the winds u, v it holds, the Courant numbers cflx,
 // cfly and the axis divergences divx, divy (adv_batch_mod.F90:218-377); on
 // half levels the vertical mass flux we, the half-level mass m_lev and the
-// vertical Courant number cflz (:493-632).
+// vertical Courant number cflz (:493-632); the FFSL intermediates qx, qy of
+// the last horizontal flux (ffsl_mod.F90:353-406).
 int orc_get_batch(void *h, const char *name, double *dst) {
   orc::Model *m = (orc::Model *)h;
   orc::Batch &b = m->mass;
@@ -1865,7 +1866,8 @@ int orc_get_batch(void *h, const char *name, double *dst) {
                    {"cflx", &b.cflx, nlat, nlev},    {"cfly", &b.cfly, nhalf, nlev},
                    {"divx", &b.divx, nlat, nlev},    {"divy", &b.divy, nlat, nlev},
                    {"we", &b.we, nlat, nlev + 1},    {"m_lev", &b.m_lev, nlat, nlev + 1},
-                   {"cflz", &b.cflz, nlat, nlev + 1}};
+                   {"cflz", &b.cflz, nlat, nlev + 1}, {"qx", &b.qx, nlat, nlev},
+                   {"qy", &b.qy, nlat, nlev}};
   for (const T &e : tab) {
     if (std::strcmp(name, e.name)) continue;
     size_t o = 0;

@@ -631,3 +631,102 @@ def test_vertical_flux_divergence_matches_restatement(case):
         assert close(got, want), (case, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
+
+
+# ---------------------------------------------------------------------------
+# the horizontal FFSL flux of pt and its divergence (calc_grad_ptf,
+# operators_mod.F90:1008-1083; ffsl_calc_tracer_hflx_cell, ffsl_mod.F90:
+# 318-413; hflx_ppm_cell, :778-881): inner advective fluxes of q, the
+# intermediates qx, qy with the divergence corrections and the polar rings,
+# then the outer fluxes of qy along x and qx along y with the mass fluxes
+# ---------------------------------------------------------------------------
+def lat_halo(x):
+    """Two full rows beyond each pole, rotated by nlon/2 (fill_halo)."""
+    h = x.shape[-1] // 2
+    r = lambda j: np.roll(x[:, j:j + 1], h, axis=-1)
+    return np.concatenate([r(2), r(1), x, r(-2), r(-3)], axis=1)
+
+
+def hflx_ppm(u, v, mx, my, cflx, cfly):
+    nlat = mx.shape[1]
+    nlon = mx.shape[-1]
+    cx = ppm_cells(np.roll(mx, 2, -1), np.roll(mx, 1, -1), mx, np.roll(mx, -1, -1), np.roll(mx, -2, -1))
+    Y = lat_halo(my)
+    cy = ppm_cells(Y[:, 0:nlat], Y[:, 1:nlat + 1], Y[:, 2:nlat + 2], Y[:, 3:nlat + 3], Y[:, 4:nlat + 4])
+    # whole cells S first, then the parabola's terms, left to right as written
+    integral = lambda S, fl, dq, q6, s1, s2: (S + fl * (s2 - s1) + 0.5 * dq * (s2 * s2 - s1 * s1) +
+                                              q6 * ((s2 * s2 - s1 * s1) / 2.0 - (s2 * s2 * s2 - s1 * s1 * s1) / 3.0))
+    # along x, rows 2 .. nlat-1, faces i = 1 .. nlon (Fortran indices)
+    I = slice(1, nlat - 1)
+    c = cflx[:, I]
+    ci = np.trunc(c).astype(np.int64)
+    cf = c - ci
+    pos = c > 0
+    fi = np.arange(1, nlon + 1)[None, None, :]
+    cell = lambda a, m: np.take_along_axis(a[:, I], (m - 1) % nlon, axis=-1)
+    iu = np.where(pos, fi - ci, fi - ci + 1)
+    first = np.where(pos, fi + 1 - ci, fi + 1)
+    S = np.zeros_like(c)
+    for t in range(int(np.abs(ci).max())):
+        take = t < np.abs(ci)
+        S = np.where(take, S + cell(mx, np.where(take, first + t, 1)), S)
+    s1, s2 = np.where(pos, 1 - cf, 0.0), np.where(pos, 1.0, -cf)
+    body = integral(S, cell(cx[0], iu), cell(cx[1], iu), cell(cx[2], iu), s1, s2)
+    fx = np.zeros_like(mx)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fx[:, I] = np.where(c == 0, 0.0, np.where(pos, u[:, I] * body / c, -u[:, I] * body / c))
+    # along y, half rows j = 1 .. nhalf: upwind cell j (c > 0) or j + 1
+    c = cfly
+    pos = c > 0
+    up = lambda a: np.where(pos, a[:, :-1], a[:, 1:])
+    s1, s2 = np.where(pos, 1 - c, 0.0), np.where(pos, 1.0, -c)
+    body = integral(0.0, up(cy[0]), up(cy[1]), up(cy[2]), s1, s2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fy = np.where(c == 0, 0.0, np.where(pos, v * body / c, -v * body / c))
+    return fx, fy
+
+
+def horizontal_ffsl(cfg, o, dt):
+    nlat, nlon = cfg.nlat, cfg.nlon
+    le_lon, le_lat, area = (o.metric("le_lon", nlat)[None, :, None], o.metric("le_lat", nlat - 1)[None, :, None],
+                            o.metric("area_cell", nlat)[None, :, None])
+    B = {n: o.get_batch(n) for n in ("u", "v", "cflx", "cfly", "divx", "divy")}
+    q = o.get_field("pt")
+    mfx, mfy = o.get_field("mfx_lon"), o.get_field("mfy_lat")
+    I = slice(1, nlat - 1)
+    fx, fy = hflx_ppm(B["u"], B["v"], q, q, B["cflx"], B["cfly"])
+    qx, qy = q.copy(), q.copy()
+    qx[:, I] = q[:, I] - 0.5 * ((fx[:, I] - prev(fx[:, I])) * le_lon[:, I] / area[:, I] - B["divx"][:, I] * q[:, I]) * dt
+    qy[:, I] = q[:, I] - 0.5 * ((fy[:, 1:] * le_lat[:, 1:] - fy[:, :-1] * le_lat[:, :-1]) / area[:, I] -
+                                B["divy"][:, I] * q[:, I]) * dt
+    ps = (ring(fy[:, 0]) * le_lat[0, 0, 0] / nlon / area[0, 0, 0])[:, None]
+    pn = (ring(fy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0])[:, None]
+    qy[:, 0] = q[:, 0] - 0.5 * (ps - B["divy"][:, 0] * q[:, 0]) * dt
+    qy[:, -1] = q[:, -1] + 0.5 * (pn - B["divy"][:, -1] * q[:, -1]) * dt
+    gx, gy = hflx_ppm(mfx, mfy, qy, qx, B["cflx"], B["cfly"])
+    dlon = (gx[:, I] - prev(gx[:, I])) * le_lon[:, I] / area[:, I]
+    dlat = np.zeros_like(q)
+    dlat[:, I] = (gy[:, 1:] * le_lat[:, 1:] - gy[:, :-1] * le_lat[:, :-1]) / area[:, I]
+    dlat[:, 0] = (ring(gy[:, 0]) * le_lat[0, 0, 0] / nlon / area[0, 0, 0])[:, None]
+    dlat[:, -1] = (ring(-gy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0])[:, None]
+    return {"dptfdlon": (dlon, I), "dptfdlat": (dlat, None)}
+
+
+@pytest.mark.parametrize("case", ["baroclinic_5deg_l26", "baroclinic_4deg_wrf_l32", "long_step"])
+def test_horizontal_ffsl_matches_restatement(case):
+    if case == "long_step":   # whole-cell departures (|cflx| > 1) near the poles
+        cfg = baroclinic_config(dt=1200.0)
+        o = prepared(cfg, u_wave=60.0)
+    else:
+        cfg = CASES[case]()
+        o = prepared(cfg)
+    try:
+        o.run_pass(0)
+        for name, (want, rows) in horizontal_ffsl(cfg, o, cfg.dt_dyn).items():
+            got = o.get_tend(0, name)
+            if rows is not None:
+                got = got[:, rows]
+            assert np.abs(want).max() > 0, name
+            assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
+    finally:
+        o.close()
