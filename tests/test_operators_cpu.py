@@ -441,16 +441,17 @@ def test_batch_courant_numbers_match_restatement(case):
 # u_f, v_f and phs_f / gz_f are the big filter of u_lon, v_lat, phs / gz
 # (filter_on_lon_edge / _lat_edge / _cell, filter_mod.F90:25-163)
 # ---------------------------------------------------------------------------
-def filter_rows(o, x, lat):
+def filter_rows(o, x, lat, which=0):
     """tmp(i) = sum(wgt(:n,j) * x(i-hn:i+hn,j)), summed over the taps in
-    order, on rows with more than one tap; other rows copied."""
+    order, on rows with more than one tap; other rows copied.  which: 0 big,
+    1 small1, 2 small2."""
     y = x.copy()
-    taps = o.filter_taps(0, lat)
+    taps = o.filter_taps(which, lat)
     for j in range(x.shape[-2]):
         n = int(taps[j])
         if n <= 1:
             continue
-        w, hn = o.filter_weights(0, lat, j + 1), (n - 1) // 2
+        w, hn = o.filter_weights(which, lat, j + 1), (n - 1) // 2
         row = x[..., j, :]
         acc = np.zeros_like(row)
         for t in range(n):
@@ -727,6 +728,61 @@ def test_horizontal_ffsl_matches_restatement(case):
             if rows is not None:
                 got = got[:, rows]
             assert np.abs(want).max() > 0, name
+            assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
+    finally:
+        o.close()
+
+
+# ---------------------------------------------------------------------------
+# update_state (time_schemes_mod.F90:120-242) over one Euler step (one
+# forward-backward pair, step_forward_backward :102-118): phs and its big
+# filter, pt through the layer mass with the small1 filter, u and v with the
+# small2 filter, the v blend next to the poles (weight 0.6) and the big filter
+# to u_f, v_f; the pass tendencies are the oracle's own (pinned above)
+# ---------------------------------------------------------------------------
+def euler_update(cfg, o, old, dt):
+    nlat, nlev = cfg.nlat, cfg.nlev
+    I = slice(1, nlat - 1)
+    dphs, dpt = o.get_tend(0, "dphs"), o.get_tend(0, "dpt")
+    du, dv = o.get_tend(1, "du"), o.get_tend(1, "dv")
+    new = {}
+    phs = old["phs"] + dt * dphs
+    new["phs"] = phs
+    new["phs_f"] = filter_rows(o, phs[None], 0)[0]
+    hyai, hybi = o.metric("hyai", nlev + 1), o.metric("hybi", nlev + 1)
+    lp = 0.0 if cfg.vert_coord_template == 26 else cfg.ptop
+    ph_lev = np.array([hyai[k] * (cfg.hybrid_coord_p0 - lp) + hybi[k] * (new["phs_f"] - lp) + lp
+                       for k in range(nlev + 1)])
+    m_new = ph_lev[1:] - ph_lev[:-1]
+    new["pt"] = filter_rows(o, old["pt"] * old["m"] + dt * dpt, 0, which=1) / m_new
+    u = o.get_field("u_lon").copy()                  # pole rows: never updated
+    u[:, I] = old["u_lon"][:, I] + dt * du[:, I]
+    v = old["v_lat"] + dt * dv
+    u = filter_rows(o, u, 0, which=2)
+    v = filter_rows(o, v, 1, which=2)
+    wgt = 0.6
+    v[:, 0] = (1 - wgt) * v[:, 0] + wgt * v[:, 1]
+    v[:, -1] = (1 - wgt) * v[:, -1] + wgt * v[:, -2]
+    new["u_lon"], new["v_lat"] = u, v
+    new["u_f"], new["v_f"] = filter_rows(o, u, 0), filter_rows(o, v, 1)
+    return new
+
+
+@pytest.mark.parametrize("case", ["baroclinic_5deg_l26", "baroclinic_4deg_wrf_l32"])
+def test_update_state_matches_restatement(case):
+    from gmcore_gb300 import abi
+    # dt = 600 s: long enough that the small filters act on the polar rows
+    kw = dict(nlon=90, nlat=46, nlev=32, dt=600.0) if "wrf" in case else dict(dt=600.0)
+    cfg = baroclinic_config(time_scheme=abi.TIME_EULER, **kw)
+    o = prepared(cfg)
+    try:
+        for which, lat in ((1, 0), (2, 0), (2, 1)):
+            assert (o.filter_taps(which, lat) > 1).any()
+        old = {f: o.get_field(f) for f in ("u_lon", "v_lat", "pt", "phs", "m")}
+        o.step(1)
+        for name, want in euler_update(cfg, o, old, cfg.dt_dyn).items():
+            got = o.get_field(name)
+            assert got.shape == want.shape, name
             assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
