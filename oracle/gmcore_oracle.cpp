@@ -1436,6 +1436,59 @@ struct Model {
     fill_halo(f, true);
   }
 
+  // Negative fixer along longitude (adv_mod.F90:236-258): sequential in i,
+  // borrowing from i-1 and i+1, which at the row ends are the longitude halo.
+  void zonal_fixer(Arr &qn, const Arr &m) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nlat = mesh.nlat;
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nlat; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          if (qn(i, j, k) < 0) {
+            double qm0 = qn(i, j, k) * m(i, j, k);
+            double qm1 = qn(i - 1, j, k) * m(i - 1, j, k);
+            double qm2 = qn(i + 1, j, k) * m(i + 1, j, k);
+            double qm0_half = 0.5 * qm0;
+            if (qm1 >= qm0_half && qm2 >= qm0_half) {
+              qn(i - 1, j, k) = (qm1 - qm0_half) / m(i - 1, j, k);
+              qn(i + 1, j, k) = (qm2 - qm0_half) / m(i + 1, j, k);
+            } else if (qm1 > qm0) {
+              qn(i - 1, j, k) = (qm1 - qm0) / m(i - 1, j, k);
+            } else if (qm2 > qm0) {
+              qn(i + 1, j, k) = (qm2 - qm0) / m(i + 1, j, k);
+            } else {
+              err.set(GMC_ENEGTRACER, "Negative tracer!");
+            }
+            qn(i, j, k) = 0;
+          }
+        }
+  }
+
+  // Negative fixer along the column (adv_mod.F90:275-297).
+  void vertical_fixer(Arr &qn, const Arr &m) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nlat = mesh.nlat;
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nlat; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          if (qn(i, j, k) < 0) {
+            double qm0 = qn(i, j, k) * m(i, j, k);
+            double qm1 = k > 1 ? qn(i, j, k - 1) * m(i, j, k - 1) : 0.0;
+            double qm2 = k < nlev ? qn(i, j, k + 1) * m(i, j, k + 1) : 0.0;
+            double qm0_half = 0.5 * qm0;
+            if (qm1 >= qm0_half && qm2 >= qm0_half) {
+              if (qm1 > 0) qn(i, j, k - 1) = (qm1 - qm0_half) / m(i, j, k - 1);
+              if (qm2 > 0) qn(i, j, k + 1) = (qm2 - qm0_half) / m(i, j, k + 1);
+            } else if (qm1 > qm0) {
+              if (qm1 > 0) qn(i, j, k - 1) = (qm1 - qm0) / m(i, j, k - 1);
+            } else if (qm2 > qm0) {
+              if (qm2 > 0) qn(i, j, k + 1) = (qm2 - qm0) / m(i, j, k + 1);
+            } else {
+              err.set(GMC_ENEGTRACER, "Negative tracer!");
+            }
+            qn(i, j, k) = 0;
+          }
+        }
+  }
+
   void adv_run(State &s) {
     const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
     const gmc::Grid &g = G();
@@ -1470,28 +1523,7 @@ struct Model {
         for (int k = 1; k <= nlev; ++k)
           for (int j = 1; j <= nlat; ++j)
             for (int i = 1; i <= nlon; ++i) qn(i, j, k) = qn(i, j, k) / s.m(i, j, k);
-        // horizontal negative fixer (sequential in i, reads the longitude halo)
-        for (int k = 1; k <= nlev; ++k)
-          for (int j = 1; j <= nlat; ++j)
-            for (int i = 1; i <= nlon; ++i) {
-              if (qn(i, j, k) < 0) {
-                double qm0 = qn(i, j, k) * s.m(i, j, k);
-                double qm1 = qn(i - 1, j, k) * s.m(i - 1, j, k);
-                double qm2 = qn(i + 1, j, k) * s.m(i + 1, j, k);
-                double qm0_half = 0.5 * qm0;
-                if (qm1 >= qm0_half && qm2 >= qm0_half) {
-                  qn(i - 1, j, k) = (qm1 - qm0_half) / s.m(i - 1, j, k);
-                  qn(i + 1, j, k) = (qm2 - qm0_half) / s.m(i + 1, j, k);
-                } else if (qm1 > qm0) {
-                  qn(i - 1, j, k) = (qm1 - qm0) / s.m(i - 1, j, k);
-                } else if (qm2 > qm0) {
-                  qn(i + 1, j, k) = (qm2 - qm0) / s.m(i + 1, j, k);
-                } else {
-                  err.set(GMC_ENEGTRACER, "Negative tracer!");
-                }
-                qn(i, j, k) = 0;
-              }
-            }
+        zonal_fixer(qn, s.m);
         for (int k = qn.lb2; k <= 0; ++k)
           for (int j = qn.lb1; j <= qn.ub1; ++j)
             for (int i = qn.lb0; i <= qn.ub0; ++i) qn(i, j, k) = qn(i, j, 1);
@@ -1503,28 +1535,7 @@ struct Model {
           for (int j = 1; j <= nlat; ++j)
             for (int i = 1; i <= nlon; ++i)
               qn(i, j, k) = qn(i, j, k) - ((b.qmf_lev(i, j, k + 1) - b.qmf_lev(i, j, k)) * dt_adv) / s.m(i, j, k);
-        // vertical negative fixer
-        for (int k = 1; k <= nlev; ++k)
-          for (int j = 1; j <= nlat; ++j)
-            for (int i = 1; i <= nlon; ++i) {
-              if (qn(i, j, k) < 0) {
-                double qm0 = qn(i, j, k) * s.m(i, j, k);
-                double qm1 = k > 1 ? qn(i, j, k - 1) * s.m(i, j, k - 1) : 0.0;
-                double qm2 = k < nlev ? qn(i, j, k + 1) * s.m(i, j, k + 1) : 0.0;
-                double qm0_half = 0.5 * qm0;
-                if (qm1 >= qm0_half && qm2 >= qm0_half) {
-                  if (qm1 > 0) qn(i, j, k - 1) = (qm1 - qm0_half) / s.m(i, j, k - 1);
-                  if (qm2 > 0) qn(i, j, k + 1) = (qm2 - qm0_half) / s.m(i, j, k + 1);
-                } else if (qm1 > qm0) {
-                  if (qm1 > 0) qn(i, j, k - 1) = (qm1 - qm0) / s.m(i, j, k - 1);
-                } else if (qm2 > qm0) {
-                  if (qm2 > 0) qn(i, j, k + 1) = (qm2 - qm0) / s.m(i, j, k + 1);
-                } else {
-                  err.set(GMC_ENEGTRACER, "Negative tracer!");
-                }
-                qn(i, j, k) = 0;
-              }
-            }
+        vertical_fixer(qn, s.m);
         fill_halo(qn, true, true, true, false, false);
         for (int it = 0; it < 3; ++it) lon_damp_on_cell(qn);
         fill_halo(qn, true);
@@ -1877,6 +1888,45 @@ int orc_get_batch(void *h, const char *name, double *dst) {
     return GMC_OK;
   }
   return GMC_EINVAL;
+}
+
+// One piece of the tracer step applied to a given cell field, for the
+// known-answer tests: which 0 the zonal negative fixer, 1 the vertical
+// negative fixer (with layer masses m), 2 three passes of the order-2 zonal
+// smoother.  q (in/out) and m interior-only [k][j][i]; their halos are filled
+// from the interior before the call, and what a fixer writes into a halo
+// cell is dropped, as the reference's next fill_halo drops it.
+int orc_tracer_piece(void *h, int which, double *q, const double *mass) {
+  orc::Model *m = (orc::Model *)h;
+  const int nlon = m->mesh.nlon, nlat = m->mesh.nlat, nlev = m->mesh.nlev;
+  orc::Fields F{&m->mesh};
+  orc::Arr qa, ma;
+  F.cell3(qa);
+  F.cell3(ma);
+  size_t o = 0;
+  for (int k = 1; k <= nlev; ++k)
+    for (int j = 1; j <= nlat; ++j)
+      for (int i = 1; i <= nlon; ++i, ++o) {
+        qa(i, j, k) = q[o];
+        ma(i, j, k) = mass[o];
+      }
+  m->fill_halo(qa, true);
+  m->fill_halo(ma, true);
+  m->err = {};
+  if (which == 0) {
+    m->zonal_fixer(qa, ma);
+  } else if (which == 1) {
+    m->vertical_fixer(qa, ma);
+  } else if (which == 2) {
+    for (int it = 0; it < 3; ++it) m->lon_damp_on_cell(qa);
+  } else {
+    return GMC_EINVAL;
+  }
+  o = 0;
+  for (int k = 1; k <= nlev; ++k)
+    for (int j = 1; j <= nlat; ++j)
+      for (int i = 1; i <= nlon; ++i) q[o++] = qa(i, j, k);
+  return m->err.code;
 }
 
 int orc_diagnose(void *h, double *out) {

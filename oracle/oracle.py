@@ -48,6 +48,7 @@ def load(variant="parity"):
     lib.orc_run_pass.argtypes = [C.c_void_p, C.c_int]
     lib.orc_get_tend.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_double)]
     lib.orc_get_batch.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+    lib.orc_tracer_piece.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
     _LIBS[variant] = lib
     return lib
@@ -188,6 +189,15 @@ class Oracle:
         if self.lib.orc_get_batch(self.h, name.encode(), _ptr(out)):
             raise KeyError(name)
         return out
+
+    def tracer_piece(self, which, q, m):
+        """One tracer-step piece on cell field q with layer masses m: 0 the
+        zonal negative fixer, 1 the vertical one, 2 three passes of the
+        zonal smoother.  Returns (q after, status)."""
+        qa = np.ascontiguousarray(q, dtype=np.float64).copy()
+        ma = np.ascontiguousarray(m, dtype=np.float64)
+        rc = self.lib.orc_tracer_piece(self.h, which, _ptr(qa), _ptr(ma))
+        return qa, rc
 
     def filter_weights(self, which, lat, j):
         """Weights of polar-filter row j (1-based) of filter `which`
