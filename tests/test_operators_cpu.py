@@ -786,3 +786,57 @@ def test_update_state_matches_restatement(case):
             assert close(got, want), (case, name, float(np.abs(got - want).max() / np.abs(want).max()))
     finally:
         o.close()
+
+
+# ---------------------------------------------------------------------------
+# diagnose (gmcore_mod.F90:213-341): the global integrals, each a sequential
+# sum in the reference's loop order
+# ---------------------------------------------------------------------------
+def seq(*blocks):
+    """Sum of the blocks' elements one after another, in row-major order."""
+    return float(np.cumsum(np.concatenate([np.ravel(b) for b in blocks]))[-1])
+
+
+def diagnostics(cfg, o):
+    nlat, nhalf = cfg.nlat, cfg.nlat - 1
+    I = slice(1, nlat - 1)
+    ac = o.metric("area_cell", nlat)[None, :, None]
+    alon, alat = o.metric("area_lon", nlat)[None, :, None], o.metric("area_lat", nhalf)[None, :, None]
+    avtx = o.metric("area_vtx", nhalf)[None, :, None]
+    F = {n: o.get_field(n) for n in ("u_lon", "v_lat", "mfx_lon", "mfy_lat", "m", "pv", "pv_lon", "pv_lat", "gzs")}
+    m = F["m"]
+    m_lon, m_lat = ((m + nxt(m)) * 0.5)[:, I], (m[:, :-1] + m[:, 1:]) * 0.5
+    nlev = m.shape[0]
+    tm = seq(m * ac)
+    ke_lon = F["mfx_lon"][:, I] * 0.5 * F["u_lon"][:, I] * alon[:, I] * 2
+    ke_lat = F["mfy_lat"] * 0.5 * F["v_lat"] * alat * 2
+    te_ke = seq(*[b for k in range(nlev) for b in (ke_lon[k], ke_lat[k])])
+    if cfg.baroclinic:
+        te_ie = seq(m * cfg.cpd * o.get_field("t") * ac)
+        te_pe = seq(F["gzs"] * o.get_field("phs") * ac[0])
+        tpt = seq(m * o.get_field("pt") * ac)
+    else:
+        te_ie, tpt = 0.0, 0.0
+        m1 = m[0]
+        te_pe = seq((m1 * m1 * cfg.g * 0.5 + m1 * F["gzs"]) * ac[0])
+    tav = seq(F["pv"] * avtx)
+    pe_lon = m_lon * (F["pv_lon"][:, I] * F["pv_lon"][:, I]) * 0.5 * alon[:, I]
+    pe_lat = m_lat * (F["pv_lat"] * F["pv_lat"]) * 0.5 * alat
+    tpe = seq(*[b for k in range(nlev) for b in (pe_lon[k], pe_lat[k])])
+    return {"tm": tm, "te": te_ke + te_ie + te_pe, "te_ke": te_ke, "te_ie": te_ie, "te_pe": te_pe,
+            "tav": tav, "tpe": tpe, "tpt": tpt}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_diagnostics_match_restatement(case):
+    cfg = CASES[case]()
+    o = prepared(cfg)
+    try:
+        got = o.diagnose()
+        want = diagnostics(cfg, o)
+        for name, w in want.items():
+            if w == 0.0:
+                continue
+            assert abs(got[name] - w) <= 4 * np.finfo(float).eps * abs(w), (case, name, got[name], w)
+    finally:
+        o.close()
