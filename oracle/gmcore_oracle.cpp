@@ -1820,7 +1820,8 @@ int orc_space_identities(void *h, double *out) {
 // One pass of the space operators on state(old), for the known-answer tests:
 // pass 0 the forward pass (space_operators_fwd) into tend[0]; pass 1 the
 // backward pass's prepare (calc_ph, calc_t, calc_gz_lev, calc_m) and the
-// pressure-gradient force into tend[1].
+// pressure-gradient force into tend[1]; pass 2 the divergence damping of
+// u_lon, v_lat (div_damp_run, div_damp_mod.F90:89-139).
 int orc_run_pass(void *h, int pass) {
   orc::Model *m = (orc::Model *)h;
   orc::State &s = m->state[m->old_i];
@@ -1829,6 +1830,8 @@ int orc_run_pass(void *h, int pass) {
   } else if (pass == 1) {
     m->operators_prepare_bwd(s);
     m->pgf_run(s, m->tend[1]);
+  } else if (pass == 2) {
+    m->div_damp_run(s);
   } else {
     return GMC_EINVAL;
   }

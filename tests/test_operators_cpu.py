@@ -840,3 +840,55 @@ def test_diagnostics_match_restatement(case):
             assert abs(got[name] - w) <= 4 * np.finfo(float).eps * abs(w), (case, name, got[name], w)
     finally:
         o.close()
+
+
+# ---------------------------------------------------------------------------
+# divergence damping (div_damp_run, div_damp_mod.F90:89-139; calc_div with
+# the order-4 Laplacian of divergence, operators_mod.F90:354-431)
+# ---------------------------------------------------------------------------
+def divergence_damping(cfg, o):
+    nlat, nhalf, nlon, nlev = cfg.nlat, cfg.nlat - 1, cfg.nlon, cfg.nlev
+    I = slice(1, nlat - 1)
+    row = lambda n, rows: o.metric(n, rows)[None, :, None]
+    le_lon, de_lon, ac = row("le_lon", nlat), row("de_lon", nlat), row("area_cell", nlat)
+    le_lat, de_lat = row("le_lat", nhalf), row("de_lat", nhalf)
+    fcos, hcos = row("full_cos_lat", nlat), row("half_cos_lat", nhalf)
+    u, v = o.get_field("u_f"), o.get_field("v_f")
+    div = np.zeros((nlev, nlat, nlon))
+    div[:, I] = ((u[:, I] * le_lon[:, I] - prev(u[:, I]) * le_lon[:, I]) +
+                 (v[:, 1:] * le_lat[:, 1:] - v[:, :-1] * le_lat[:, :-1])) / ac[:, I]
+    div[:, 0] = (ring(v[:, 0]) * le_lat[0, 0, 0] / nlon / ac[0, 0, 0])[:, None]
+    div[:, -1] = (ring(-v[:, -1]) * le_lat[0, -1, 0] / nlon / ac[0, -1, 0])[:, None]
+    c_lon = o.metric("div_c_lon", nlev * nlat).reshape(nlev, nlat)[:, :, None]
+    c_lat = o.metric("div_c_lat", nlev * nhalf).reshape(nlev, nhalf)[:, :, None]
+    u_lon, v_lat = o.get_field("u_lon"), o.get_field("v_lat")
+    if cfg.div_damp_order == 4:
+        d = np.zeros_like(div)          # pole rows are never set
+        dc = div[:, I]
+        d[:, I] = ((nxt(dc) - 2 * dc + prev(dc)) / (de_lon[:, I] * de_lon[:, I]) +
+                   ((div[:, 2:] - dc) * hcos[:, 1:] / de_lat[:, 1:] -
+                    (dc - div[:, :-2]) * hcos[:, :-1] / de_lat[:, :-1]) / le_lon[:, I] / fcos[:, I])
+        u_lon[:, I] = u_lon[:, I] - c_lon[:, I] * (nxt(d[:, I]) - d[:, I]) / de_lon[:, I]
+        v_lat = v_lat - c_lat * (d[:, 1:] - d[:, :-1]) / de_lat
+    else:
+        u_lon[:, I] = u_lon[:, I] + c_lon[:, I] * (nxt(div[:, I]) - div[:, I]) / de_lon[:, I]
+        v_lat = v_lat + c_lat * (div[:, 1:] - div[:, :-1]) / de_lat
+    return {"u_lon": u_lon, "v_lat": v_lat}
+
+
+@pytest.mark.parametrize("case", ["swm_order2", "baroclinic_order2", "baroclinic_order4", "swm_order4"])
+def test_divergence_damping_matches_restatement(case):
+    order = 4 if case.endswith("4") else 2
+    kw = dict(use_div_damp=1, div_damp_order=order, div_damp_coef2=1.0 / 128, div_damp_coef4=0.01)
+    cfg = swm_config(**kw) if case.startswith("swm") else baroclinic_config(**kw)
+    o = prepared(cfg)
+    try:
+        before = {f: o.get_field(f) for f in ("u_lon", "v_lat")}
+        want = divergence_damping(cfg, o)
+        o.run_pass(2)
+        for name, w in want.items():
+            got = o.get_field(name)
+            assert not np.array_equal(w, before[name]), name
+            assert close(got, w), (case, name, float(np.abs(got - w).max() / np.abs(w).max()))
+    finally:
+        o.close()
