@@ -116,3 +116,33 @@ def test_baroclinic_wave_first_day(perturb):
         # planetary-scale amplitude
         F = np.abs(np.fft.rfft(ps - ps.mean(axis=1, keepdims=True), axis=1)).max(axis=0)
         assert F[3 * len(F) // 4:].max() < 0.01 * F[1:6].max()
+
+
+def test_time_schemes_converge_to_one_solution():
+    """euler, pc2 and wrfrk3 (time_schemes_mod.F90:244-288) advance the
+    Rossby-Haurwitz wave for one hour with the polar filter off (its width
+    depends on dt).  Each converges at first order in dt: every stage updates
+    the winds with the pressure gradient of the mass the stage has just
+    updated (step_forward_backward, :102-118), and that end-of-stage
+    evaluation costs an order for all three.  All three converge to the same
+    solution, which catches a stage that advances the wrong span of time."""
+    from gmcore_gb300 import abi
+    from cases import swm_state
+    T = 3600.0
+    run = {}
+    for scheme in (abi.TIME_EULER, abi.TIME_PC2, abi.TIME_WRFRK3):
+        for dt in (60.0, 30.0, 15.0):
+            cfg = swm_config(dt=dt, time_scheme=scheme, max_wave_speed=0.0)
+            o = Oracle(cfg)
+            load_state(o, swm_state(cfg, rossby_haurwitz))
+            o.prepare()
+            o.step(int(round(T / dt)))
+            run[scheme, dt] = np.concatenate([o.get_field(f).ravel() for f in ("u_lon", "v_lat")])
+            o.close()
+    diff = lambda a, b: float(np.abs(run[a] - run[b]).max())
+    for scheme in (abi.TIME_EULER, abi.TIME_PC2, abi.TIME_WRFRK3):
+        d60, d30 = diff((scheme, 60.0), (scheme, 30.0)), diff((scheme, 30.0), (scheme, 15.0))
+        assert 1.8 < d60 / d30 < 2.2, (scheme, d60, d30)
+    for scheme in (abi.TIME_PC2, abi.TIME_WRFRK3):
+        e60, e30 = diff((scheme, 60.0), (abi.TIME_EULER, 60.0)), diff((scheme, 30.0), (abi.TIME_EULER, 30.0))
+        assert 1.8 < e60 / e30 < 2.2, (scheme, e60, e30)
