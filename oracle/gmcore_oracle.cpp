@@ -1871,17 +1871,16 @@ int orc_get_tend(void *h, int pass, const char *name, double *dst) {
 // half levels the vertical mass flux we, the half-level mass m_lev and the
 // vertical Courant number cflz (:493-632); the FFSL intermediates qx, qy of
 // the last horizontal flux (ffsl_mod.F90:353-406).
-int orc_get_batch(void *h, const char *name, double *dst) {
-  orc::Model *m = (orc::Model *)h;
-  orc::Batch &b = m->mass;
+static int get_batch_field(orc::Model *m, orc::Batch &b, const char *name, double *dst) {
   const int nlat = m->mesh.nlat, nhalf = m->mesh.nhalf, nlev = m->mesh.nlev;
   struct T { const char *name; orc::Arr *a; int nrow, nk; };
   const T tab[] = {{"u", &b.u, nlat, nlev},          {"v", &b.v, nhalf, nlev},
+                   {"mfx", &b.mfx, nlat, nlev},      {"mfy", &b.mfy, nhalf, nlev},
                    {"cflx", &b.cflx, nlat, nlev},    {"cfly", &b.cfly, nhalf, nlev},
                    {"divx", &b.divx, nlat, nlev},    {"divy", &b.divy, nlat, nlev},
                    {"we", &b.we, nlat, nlev + 1},    {"m_lev", &b.m_lev, nlat, nlev + 1},
                    {"cflz", &b.cflz, nlat, nlev + 1}, {"qx", &b.qx, nlat, nlev},
-                   {"qy", &b.qy, nlat, nlev}};
+                   {"qy", &b.qy, nlat, nlev},        {"old_m", &b.old_m, nlat, nlev}};
   for (const T &e : tab) {
     if (std::strcmp(name, e.name)) continue;
     size_t o = 0;
@@ -1891,6 +1890,34 @@ int orc_get_batch(void *h, const char *name, double *dst) {
     return GMC_OK;
   }
   return GMC_EINVAL;
+}
+
+int orc_get_batch(void *h, const char *name, double *dst) {
+  orc::Model *m = (orc::Model *)h;
+  return get_batch_field(m, m->mass, name, dst);
+}
+
+// The same fields of the static tracer batch (adv_mod.F90:152-312), with its
+// previous layer mass old_m.
+int orc_get_tracer_batch(void *h, const char *name, double *dst) {
+  orc::Model *m = (orc::Model *)h;
+  if (!m->has_tracers) return GMC_EINVAL;
+  return get_batch_field(m, m->tracers, name, dst);
+}
+
+// Tracer l of time level lev (0 the batch's old level, 1 its new level) with
+// two longitude-halo columns on each side as the level holds them now,
+// [k][j][nlon + 4] from i = -1.
+int orc_get_tracer_level(void *h, int l, int lev, double *dst) {
+  orc::Model *m = (orc::Model *)h;
+  if (!m->has_tracers || l < 0 || l >= m->cfg.ntracer || lev < 0 || lev > 1) return GMC_EINVAL;
+  orc::Batch &b = m->tracers;
+  orc::Arr &q = b.q[lev == 0 ? b.old_idx : b.new_idx][l];
+  size_t o = 0;
+  for (int k = 1; k <= m->mesh.nlev; ++k)
+    for (int j = 1; j <= m->mesh.nlat; ++j)
+      for (int i = -1; i <= m->mesh.nlon + 2; ++i) dst[o++] = q(i, j, k);
+  return GMC_OK;
 }
 
 // One piece of the tracer step applied to a given cell field, for the

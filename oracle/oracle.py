@@ -48,6 +48,8 @@ def load(variant="parity"):
     lib.orc_run_pass.argtypes = [C.c_void_p, C.c_int]
     lib.orc_get_tend.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_double)]
     lib.orc_get_batch.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+    lib.orc_get_tracer_batch.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+    lib.orc_get_tracer_level.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.orc_tracer_piece.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
     _LIBS[variant] = lib
@@ -179,15 +181,31 @@ class Oracle:
             raise KeyError(name)
         return out
 
-    def get_batch(self, name):
-        """A field of the dynamic mass batch (u, v, cflx, cfly, divx, divy;
-        on half levels we, m_lev, cflz)."""
+    def _batch(self, fn, name):
         c = self.cfg
-        nrow = c.nlat - 1 if name in ("v", "cfly") else c.nlat
+        nrow = c.nlat - 1 if name in ("v", "cfly", "mfy") else c.nlat
         nk = c.nlev + 1 if name in ("we", "m_lev", "cflz") else c.nlev
         out = np.zeros((nk, nrow, c.nlon))
-        if self.lib.orc_get_batch(self.h, name.encode(), _ptr(out)):
+        if fn(self.h, name.encode(), _ptr(out)):
             raise KeyError(name)
+        return out
+
+    def get_batch(self, name):
+        """A field of the dynamic mass batch (u, v, mfx, mfy, cflx, cfly, divx,
+        divy, qx, qy, old_m; on half levels we, m_lev, cflz)."""
+        return self._batch(self.lib.orc_get_batch, name)
+
+    def get_tracer_batch(self, name):
+        """The same fields of the static tracer batch."""
+        return self._batch(self.lib.orc_get_tracer_batch, name)
+
+    def get_tracer_level(self, l, lev):
+        """Tracer l of the batch's old (lev 0) or new (lev 1) time level with
+        two longitude-halo columns each side, [k][j][nlon + 4] from i = -1."""
+        c = self.cfg
+        out = np.zeros((c.nlev, c.nlat, c.nlon + 4))
+        if self.lib.orc_get_tracer_level(self.h, l, lev, _ptr(out)):
+            raise KeyError((l, lev))
         return out
 
     def tracer_piece(self, which, q, m):

@@ -589,10 +589,17 @@ def vertical_flux_divergence(cfg, o):
     g[0] = 2 * g[1] - g[2]
     g[nlev + 2] = 2 * g[nlev + 1] - g[nlev]
     g[nlev + 3] = 2 * g[nlev + 2] - g[nlev + 1]
+    flux = vertical_flux(g, o.get_batch("we"), o.get_batch("cflz"))
+    return flux[1:] - flux[:-1]
+
+
+def vertical_flux(g, we, cflz):
+    """vflx_ppm_cell: fluxes on the half levels of the field g given with two
+    ghost levels each side (level k at index k + 1)."""
+    nlev = g.shape[0] - 4
     fl, dq, q6 = ppm_cells(g[0:nlev], g[1:nlev + 1], g[2:nlev + 2], g[3:nlev + 3], g[4:nlev + 4])
     cell = lambda a, k: np.take_along_axis(a, (k - 1)[None], axis=0)[0]     # cell k (1-based), per column
     lev = lambda k: np.take_along_axis(g, (k + 1)[None], axis=0)[0]
-    we, cflz = o.get_batch("we"), o.get_batch("cflz")
     flux = np.zeros_like(we)
     for k in range(2, nlev + 1):
         c = cflz[k - 1]
@@ -613,7 +620,7 @@ def vertical_flux_divergence(cfg, o):
         body = total + cell(fl, kc) * ds1 + 0.5 * cell(dq, kc) * ds2 + cell(q6, kc) * (ds2 / 2.0 - ds3 / 3.0)
         with np.errstate(divide="ignore", invalid="ignore"):     # c = 0 takes the zero branch
             flux[k - 1] = np.where(c == 0, 0.0, np.where(pos, w * body / c, -w * body / c))
-    return flux[1:] - flux[:-1]
+    return flux
 
 
 @pytest.mark.parametrize("case", ["baroclinic_5deg_l26", "baroclinic_4deg_wrf_l32", "long_step"])
@@ -687,13 +694,12 @@ def hflx_ppm(u, v, mx, my, cflx, cfly):
     return fx, fy
 
 
-def horizontal_ffsl(cfg, o, dt):
+def ffsl_fluxes(cfg, o, q, B, mfx, mfy, dt):
+    """ffsl_calc_tracer_hflx_cell: the outer fluxes (qmfx, qmfy) of q with
+    batch B (u, v, cflx, cfly, divx, divy) and mass fluxes mfx, mfy."""
     nlat, nlon = cfg.nlat, cfg.nlon
     le_lon, le_lat, area = (o.metric("le_lon", nlat)[None, :, None], o.metric("le_lat", nlat - 1)[None, :, None],
                             o.metric("area_cell", nlat)[None, :, None])
-    B = {n: o.get_batch(n) for n in ("u", "v", "cflx", "cfly", "divx", "divy")}
-    q = o.get_field("pt")
-    mfx, mfy = o.get_field("mfx_lon"), o.get_field("mfy_lat")
     I = slice(1, nlat - 1)
     fx, fy = hflx_ppm(B["u"], B["v"], q, q, B["cflx"], B["cfly"])
     qx, qy = q.copy(), q.copy()
@@ -704,9 +710,18 @@ def horizontal_ffsl(cfg, o, dt):
     pn = (ring(fy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0])[:, None]
     qy[:, 0] = q[:, 0] - 0.5 * (ps - B["divy"][:, 0] * q[:, 0]) * dt
     qy[:, -1] = q[:, -1] + 0.5 * (pn - B["divy"][:, -1] * q[:, -1]) * dt
-    gx, gy = hflx_ppm(mfx, mfy, qy, qx, B["cflx"], B["cfly"])
+    return hflx_ppm(mfx, mfy, qy, qx, B["cflx"], B["cfly"])
+
+
+def horizontal_ffsl(cfg, o, dt):
+    nlat, nlon = cfg.nlat, cfg.nlon
+    le_lon, le_lat, area = (o.metric("le_lon", nlat)[None, :, None], o.metric("le_lat", nlat - 1)[None, :, None],
+                            o.metric("area_cell", nlat)[None, :, None])
+    B = {n: o.get_batch(n) for n in ("u", "v", "cflx", "cfly", "divx", "divy")}
+    I = slice(1, nlat - 1)
+    gx, gy = ffsl_fluxes(cfg, o, o.get_field("pt"), B, o.get_field("mfx_lon"), o.get_field("mfy_lat"), dt)
     dlon = (gx[:, I] - prev(gx[:, I])) * le_lon[:, I] / area[:, I]
-    dlat = np.zeros_like(q)
+    dlat = np.zeros((cfg.nlev, nlat, nlon))
     dlat[:, I] = (gy[:, 1:] * le_lat[:, 1:] - gy[:, :-1] * le_lat[:, :-1]) / area[:, I]
     dlat[:, 0] = (ring(gy[:, 0]) * le_lat[0, 0, 0] / nlon / area[0, 0, 0])[:, None]
     dlat[:, -1] = (ring(-gy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0])[:, None]

@@ -28,10 +28,14 @@ from helpers import baroclinic_config
 ZONAL, VERTICAL, SMOOTH = 0, 1, 2
 
 
-def zonal_fixer(q, m, hits):
+def zonal_fixer(q, m, hits, halo=None):
+    """halo: the (i = 0, i = nlon + 1) columns of q as last filled, if not
+    the wrap of q itself."""
     nlon = q.shape[-1]
     wrap = lambda a: np.concatenate([a[..., -1:], a, a[..., :1]], axis=-1)   # halo cells 0 and nlon+1
     P, M = wrap(q), wrap(m)
+    if halo is not None:
+        P[..., 0], P[..., -1] = halo
     for i in range(1, nlon + 1):
         neg = P[..., i] < 0
         qm0 = P[..., i] * M[..., i]
@@ -162,3 +166,71 @@ def test_zonal_smoother_matches_restatement(oracle_5deg):
     want = zonal_smoother(q, wgt)
     assert not np.array_equal(want, q)
     assert np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------------------
+# one whole tracer step of adv_run (adv_mod.F90:152-312) from the static
+# batch's fields: FFSL fluxes of q(old), the flux-form update from old_m with
+# the polar rings, division by the new layer mass, the zonal fixer reading the
+# longitude halo of q(new) as it was last filled, copied ghost levels, the
+# vertical FFSL update, the vertical fixer and three smoother passes
+# ---------------------------------------------------------------------------
+def tracer_step(cfg, o, q_old, old_m, halo, m, B, dt):
+    from test_operators_cpu import ffsl_fluxes, ring, prev, vertical_flux
+    nlat, nlon, nlev = cfg.nlat, cfg.nlon, cfg.nlev
+    row = lambda n, rows: o.metric(n, rows)[None, :, None]
+    le_lon, le_lat, area = row("le_lon", nlat), row("le_lat", nlat - 1), row("area_cell", nlat)
+    I = slice(1, nlat - 1)
+    gx, gy = ffsl_fluxes(cfg, o, q_old, B, B["mfx"], B["mfy"], dt)
+    qn = np.zeros_like(q_old)
+    qn[:, I] = old_m[:, I] * q_old[:, I] - ((gx[:, I] - prev(gx[:, I])) * le_lon[:, I] +
+                                             (gy[:, 1:] * le_lat[:, 1:] - gy[:, :-1] * le_lat[:, :-1])) / area[:, I] * dt
+    ps = ring(gy[:, 0]) * le_lat[0, 0, 0] / nlon / area[0, 0, 0] * dt
+    pn = ring(gy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0] * dt
+    qn[:, 0] = old_m[:, 0] * q_old[:, 0] - ps[:, None]
+    qn[:, -1] = old_m[:, -1] * q_old[:, -1] + pn[:, None]
+    qn = qn / m
+    hits = dict(both=0, left=0, right=0, ends=0)
+    qn = zonal_fixer(qn, m, hits, halo)
+    g = np.concatenate([qn[:1], qn[:1], qn, qn[-1:], qn[-1:]])     # copied ghost levels
+    flux = vertical_flux(g, B["we"], B["cflz"])
+    qn = qn - ((flux[1:] - flux[:-1]) * dt) / m
+    qn = vertical_fixer(qn, m, hits)
+    return zonal_smoother(qn, o.metric("lon_damp_wgt_full", nlat)), hits
+
+
+def test_tracer_steps_match_restatement():
+    """Two advected steps (the first step does not advect); the second tracer
+    starts with scattered negative cells so that both fixers act inside a
+    step, and by the third step the new level's halo is stale."""
+    cfg = baroclinic_config(ntracer=2)
+    from helpers import initial_state, load_state
+    o = Oracle(cfg)
+    try:
+        st = initial_state(cfg)
+        rng = np.random.default_rng(11)
+        q1 = st["q"][1] + 0.5
+        q1[rng.random(q1.shape) < 0.01] = -0.05
+        st["q"][1] = q1
+        load_state(o, st)
+        o.prepare()
+        o.step(1)                                   # no advection at the first step
+        dt = cfg.dt_adv if cfg.dt_adv > 0 else cfg.dt_dyn
+        fixed = 0
+        for _ in range(2):
+            old_m = o.get_tracer_batch("old_m")
+            before = [(o.get_tracer_level(l, 0)[..., 2:-2], o.get_tracer_level(l, 1)) for l in range(2)]
+            o.step(1)
+            B = {n: o.get_tracer_batch(n) for n in ("u", "v", "mfx", "mfy", "cflx", "cfly", "divx", "divy", "we", "cflz")}
+            m = o.get_field("m")
+            for l, (q_old, q_new_prev) in enumerate(before):
+                halo = (q_new_prev[..., 1], q_new_prev[..., -2])          # i = 0 and i = nlon + 1
+                want, hits = tracer_step(cfg, o, q_old, old_m, halo, m, B, dt)
+                fixed += hits["both"] + hits["left"] + hits["right"]
+                got = o.get_tracer(l)
+                assert not np.array_equal(got, q_old), l
+                err = float(np.abs(got - want).max() / np.abs(want).max())
+                assert err <= 8 * np.finfo(float).eps, (l, err)
+        assert fixed > 0
+    finally:
+        o.close()
