@@ -353,12 +353,14 @@ def test_tendencies_match_restatement(case):
 # the dynamic mass batch: Courant numbers from RK4 departure points and the
 # axis divergences (adv_batch_accum_uv_cell, adv_batch_mod.F90:218-377)
 # ---------------------------------------------------------------------------
-def batch_courant(cfg, o, dt):
+def batch_courant(cfg, o, dt, get=None):
+    """get(name): the batch field reader (the mass batch by default)."""
+    get = get or o.get_batch
     nlat, nhalf, nlon, nlev = cfg.nlat, cfg.nlat - 1, cfg.nlon, cfg.nlev
     R = cfg.radius
     dlon = (2 * math.pi - 0.0) / nlon
     half_lon = lambda l: (0.0 + (l - 1) * dlon) + 0.5 * dlon          # any index, halo included
-    u, v = o.get_batch("u"), o.get_batch("v")
+    u, v = get("u"), get("v")
     fcos, hlat = o.metric("full_cos_lat", nlat), o.metric("half_lat", nhalf)
     de_lon, de_lat = o.metric("de_lon", nlat), o.metric("de_lat", nhalf)
     le_lon, le_lat, area = o.metric("le_lon", nlat), o.metric("le_lat", nhalf), o.metric("area_cell", nlat)
@@ -482,7 +484,9 @@ def test_prologue_filters_match_restatement(case):
 # search, then the Lagrangian walk over whole layers (adv_batch_accum_we_lev,
 # adv_batch_mod.F90:493-632; level spacings vert_coord_mod.F90:84-101)
 # ---------------------------------------------------------------------------
-def vertical_courant(cfg, o, dt):
+def vertical_courant(cfg, o, dt, get=None):
+    """get(name): the batch field reader (the mass batch by default)."""
+    get = get or o.get_batch
     nlev = cfg.nlev
     hl, fl = [0.0] + list(o.metric("half_lev", nlev + 1)), [0.0] + list(o.metric("full_lev", nlev))   # 1-based
     full_dlev = [0.0] + [hl[k + 1] - hl[k] for k in range(1, nlev + 1)]
@@ -491,8 +495,8 @@ def vertical_courant(cfg, o, dt):
         half_dlev[k] = fl[k] - fl[k - 1]
     half_dlev[1] = fl[1] - hl[1]
     half_dlev[nlev + 1] = hl[nlev + 1] - fl[nlev]
-    we, mlev = o.get_batch("we"), o.get_batch("m_lev")
-    cflz = o.get_batch("cflz").copy()          # the boundary levels as the batch keeps them
+    we, mlev = get("we"), get("m_lev")
+    cflz = get("cflz").copy()                  # the boundary levels as the batch keeps them
     _, nlat, nlon = we.shape
 
     def find(k, z, w):

@@ -234,3 +234,45 @@ def test_tracer_steps_match_restatement():
         assert fixed > 0
     finally:
         o.close()
+
+
+def test_static_batch_cadence():
+    """The static tracer batch with dt_adv = dt_dyn (nstep = 1,
+    adv_batch_mod.F90:239-252, 389-401, 512-525): the run prologue copies the
+    winds, mass fluxes, vertical mass flux and half-level mass in; each step's
+    call then alternately averages the held values with the new state's
+    ((held + new) / 2, refreshing the Courant numbers from the averages) and
+    copies the new state's in (keeping the previous Courant numbers)."""
+    from helpers import initial_state, load_state
+    from test_operators_cpu import batch_courant, vertical_courant
+    cfg = baroclinic_config(ntracer=1)
+    dt = cfg.dt_adv if cfg.dt_adv > 0 else cfg.dt_dyn
+    o = Oracle(cfg)
+    pairs = (("u", "u_f"), ("v", "v_f"), ("mfx", "mfx_lon"), ("mfy", "mfy_lat"), ("we", "we_lev"),
+             ("m_lev", "m_lev"))
+    try:
+        load_state(o, initial_state(cfg))
+        o.prepare()
+        for b, f in pairs[:2]:
+            assert np.array_equal(o.get_tracer_batch(b), o.get_field(f)), b      # prologue copy
+        for step in range(1, 5):
+            held = {b: o.get_tracer_batch(b) for b in ("u", "v", "mfx", "mfy", "we", "m_lev", "cflx", "cfly", "cflz")}
+            o.step(1)
+            now = {b: o.get_tracer_batch(b) for b in held}
+            average = step % 2 == 1
+            for b, f in pairs:
+                new = o.get_field(f)
+                want = (held[b] + new) / 2 if average else new
+                assert np.array_equal(now[b], want), (step, b)
+            if average:
+                for name, (w, rows) in batch_courant(cfg, o, dt, get=o.get_tracer_batch).items():
+                    if name in ("cflx", "cfly"):
+                        got = now[name][:, rows] if rows is not None else now[name]
+                        assert np.array_equal(got, w), (step, name)
+                assert np.array_equal(now["cflz"], vertical_courant(cfg, o, dt, get=o.get_tracer_batch)), step
+                assert not np.array_equal(now["cflx"], held["cflx"]), step
+            else:
+                for name in ("cflx", "cfly", "cflz"):
+                    assert np.array_equal(now[name], held[name]), (step, name)
+    finally:
+        o.close()
