@@ -911,3 +911,68 @@ def test_divergence_damping_matches_restatement(case):
             assert close(got, w), (case, name, float(np.abs(got - w).max() / np.abs(w).max()))
     finally:
         o.close()
+
+
+# ---------------------------------------------------------------------------
+# the other PV edge interpolations: midpoint (interp_pv_midpoint,
+# operators_mod.F90:705-736), first-order upwind (:738-770; upwind1,
+# upwind_mod.F90:14-25) and TVD with its three limiters (interp_pv_tvd,
+# :797-832; tvd, flux limiters, tvd_mod.F90:83-102; eps the default-kind
+# literal 1.0e-6, rounded to float32 and widened)
+# ---------------------------------------------------------------------------
+TVD_EPS = float(np.float32(1.0e-6))
+
+
+def tvd(cfl, fm1, f, fp1, fp2, limiter):
+    r = np.where(cfl > 0, (f - fm1 + TVD_EPS) / (fp1 - f + TVD_EPS), (fp2 - fp1 + TVD_EPS) / (fp1 - f + TVD_EPS))
+    if limiter == 0:
+        C = np.ones_like(r)
+    elif limiter == 1:
+        C = (r + np.abs(r)) / (1 + np.abs(r))
+    else:
+        C = np.maximum(0.0, np.minimum(np.minimum(2.0 * r, 0.5 * (1 + r)), 2.0))
+    return 0.5 * (fp1 + f - ((1 - C) * np.copysign(1.0, cfl) + cfl * C) * (fp1 - f))
+
+
+def pv_edges_variant(cfg, o, scheme):
+    from gmcore_gb300 import abi
+    nlat, nlon = cfg.nlat, cfg.nlon
+    I = slice(1, nlat - 1)
+    pv, u, v = o.get_field("pv"), o.get_field("u_f"), o.get_field("v_f")
+    ut, vt = o.get_field("u_lat"), o.get_field("v_lon")[:, I]
+    P = np.concatenate([np.roll(pv[:, :1], nlon // 2, axis=-1), pv, np.roll(pv[:, -1:], nlon // 2, axis=-1)], axis=1)
+    jf = np.arange(1, nlat - 1)
+    fy = [P[:, jf - 1], P[:, jf], P[:, jf + 1], P[:, jf + 2]]          # pv(j-2) .. pv(j+1) along a column
+    fx = [np.roll(pv, 2, axis=-1), prev(pv), pv, nxt(pv)]             # pv(i-2) .. pv(i+1) along a row
+    if scheme == "midpoint":
+        return 0.5 * (fy[2] + fy[1]), 0.5 * (fx[1] + fx[2])
+    if scheme == "upwind1":
+        w = cfg.upwind_wgt_pv
+        up1 = lambda f1, f2, sgn: 0.5 * (f2 + f1) + -0.5 * (f2 - f1) * w * sgn
+        b_lon = np.abs(vt) / (np.sqrt(u[:, I] * u[:, I] + vt * vt) + EPS)
+        b_lat = np.abs(ut) / (np.sqrt(ut * ut + v * v) + EPS)
+        return (b_lon * up1(fy[1], fy[2], np.copysign(1.0, vt)) + (1 - b_lon) * 0.5 * (fy[1] + fy[2]),
+                b_lat * up1(fx[1], fx[2], np.copysign(1.0, ut)) + (1 - b_lat) * 0.5 * (fx[1] + fx[2]))
+    dt = cfg.dt_dyn
+    lim = cfg.tvd_limiter_type
+    cfl_lon = vt * dt / o.metric("le_lon", nlat)[None, I, None]
+    cfl_lat = ut * dt / o.metric("le_lat", nlat - 1)[None, :, None]
+    return tvd(cfl_lon, *fy, lim), tvd(cfl_lat, *fx, lim)
+
+
+@pytest.mark.parametrize("scheme", ["midpoint", "upwind1", "tvd_none", "tvd_van_leer", "tvd_mc"])
+def test_pv_edge_variants_match_restatement(scheme):
+    from gmcore_gb300 import abi
+    kw = {"midpoint": dict(pv_scheme=abi.PV_MIDPOINT), "upwind1": dict(pv_scheme=abi.PV_UPWIND, upwind_order_pv=1),
+          "tvd_none": dict(pv_scheme=abi.PV_TVD, tvd_limiter_type=abi.TVD_NONE),
+          "tvd_van_leer": dict(pv_scheme=abi.PV_TVD, tvd_limiter_type=abi.TVD_VAN_LEER),
+          "tvd_mc": dict(pv_scheme=abi.PV_TVD, tvd_limiter_type=abi.TVD_MC)}[scheme]
+    cfg = baroclinic_config(**kw)
+    o = prepared(cfg)
+    try:
+        want_lon, want_lat = pv_edges_variant(cfg, o, scheme.split("_")[0] if scheme.startswith("tvd") else scheme)
+        got_lon, got_lat = o.get_field("pv_lon")[:, 1:-1], o.get_field("pv_lat")
+        assert close(got_lon, want_lon), (scheme, float(np.abs(got_lon - want_lon).max()))
+        assert close(got_lat, want_lat), (scheme, float(np.abs(got_lat - want_lat).max()))
+    finally:
+        o.close()
