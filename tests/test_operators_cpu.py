@@ -698,14 +698,15 @@ def hflx_ppm(u, v, mx, my, cflx, cfly):
     return fx, fy
 
 
-def ffsl_fluxes(cfg, o, q, B, mfx, mfy, dt):
+def ffsl_fluxes(cfg, o, q, B, mfx, mfy, dt, hflx=None):
     """ffsl_calc_tracer_hflx_cell: the outer fluxes (qmfx, qmfy) of q with
     batch B (u, v, cflx, cfly, divx, divy) and mass fluxes mfx, mfy."""
     nlat, nlon = cfg.nlat, cfg.nlon
     le_lon, le_lat, area = (o.metric("le_lon", nlat)[None, :, None], o.metric("le_lat", nlat - 1)[None, :, None],
                             o.metric("area_cell", nlat)[None, :, None])
     I = slice(1, nlat - 1)
-    fx, fy = hflx_ppm(B["u"], B["v"], q, q, B["cflx"], B["cfly"])
+    hflx = hflx or hflx_ppm
+    fx, fy = hflx(B["u"], B["v"], q, q, B["cflx"], B["cfly"])
     qx, qy = q.copy(), q.copy()
     qx[:, I] = q[:, I] - 0.5 * ((fx[:, I] - prev(fx[:, I])) * le_lon[:, I] / area[:, I] - B["divx"][:, I] * q[:, I]) * dt
     qy[:, I] = q[:, I] - 0.5 * ((fy[:, 1:] * le_lat[:, 1:] - fy[:, :-1] * le_lat[:, :-1]) / area[:, I] -
@@ -714,7 +715,7 @@ def ffsl_fluxes(cfg, o, q, B, mfx, mfy, dt):
     pn = (ring(fy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0])[:, None]
     qy[:, 0] = q[:, 0] - 0.5 * (ps - B["divy"][:, 0] * q[:, 0]) * dt
     qy[:, -1] = q[:, -1] + 0.5 * (pn - B["divy"][:, -1] * q[:, -1]) * dt
-    return hflx_ppm(mfx, mfy, qy, qx, B["cflx"], B["cfly"])
+    return hflx(mfx, mfy, qy, qx, B["cflx"], B["cfly"])
 
 
 def horizontal_ffsl(cfg, o, dt):
@@ -974,5 +975,101 @@ def test_pv_edge_variants_match_restatement(scheme):
         got_lon, got_lat = o.get_field("pv_lon")[:, 1:-1], o.get_field("pv_lat")
         assert close(got_lon, want_lon), (scheme, float(np.abs(got_lon - want_lon).max()))
         assert close(got_lat, want_lat), (scheme, float(np.abs(got_lat - want_lat).max()))
+    finally:
+        o.close()
+
+
+# ---------------------------------------------------------------------------
+# ffsl_flux_type = 'van_leer': the limited linear profile in place of the
+# parabola (hflx_van_leer_cell, vflx_van_leer_cell, ffsl_mod.F90:556-658)
+# ---------------------------------------------------------------------------
+def hflx_van_leer(u, v, mx, my, cflx, cfly):
+    nlat, nlon = mx.shape[1], mx.shape[-1]
+    I = slice(1, nlat - 1)
+    c = cflx[:, I]
+    ci = np.trunc(c).astype(np.int64)
+    cf = c - ci
+    pos = c > 0
+    fi = np.arange(1, nlon + 1)[None, None, :]
+    cell = lambda m: np.take_along_axis(mx[:, I], (m - 1) % nlon, axis=-1)
+    iu = np.where(pos, fi - ci, fi - ci + 1)
+    first = np.where(pos, fi + 1 - ci, fi + 1)
+    S = np.zeros_like(c)
+    for t in range(int(np.abs(ci).max())):
+        take = t < np.abs(ci)
+        S = np.where(take, S + cell(np.where(take, first + t, 1)), S)
+    dm = slope_mono(cell(iu - 1), cell(iu), cell(iu + 1))
+    fx = np.zeros_like(mx)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fx[:, I] = np.where(c == 0, 0.0, np.where(
+            pos, u[:, I] * (cf * (cell(iu) + dm * 0.5 * (1 - cf)) + S) / c,
+            u[:, I] * (cf * (cell(iu) - dm * 0.5 * (1 + cf)) - S) / c))
+    Y = lat_halo(my)                                    # full row r at index r + 1 (r = -1 .. nlat + 2)
+    c = cfly
+    pos = c > 0
+    ju = np.where(pos, np.arange(1, nlat)[None, :, None], np.arange(2, nlat + 1)[None, :, None]) * np.ones_like(c, dtype=np.int64)
+    row = lambda r: np.take_along_axis(Y, r + 1, axis=1)
+    dm = slope_mono(row(ju - 1), row(ju), row(ju + 1))
+    fy = v * (row(ju) + dm * 0.5 * (np.copysign(1.0, c) - c))
+    return fx, fy
+
+
+def vertical_flux_van_leer(g, we, cflz):
+    nlev = g.shape[0] - 4
+    lev = lambda k: np.take_along_axis(g, (k + 1)[None], axis=0)[0]
+    flux = np.zeros_like(we)
+    for k in range(2, nlev + 1):
+        c, w = cflz[k - 1], we[k - 1]
+        ci = np.trunc(c).astype(np.int64)
+        cf = c - ci
+        pos = c > 0
+        ku = np.where(pos, k - ci - 1, k - ci)
+        first = np.where(pos, k - ci, k)
+        S = np.zeros_like(c)
+        for t in range(int(np.abs(ci).max())):
+            take = t < np.abs(ci)
+            S = np.where(take, S + lev(np.where(take, first + t, k)), S)
+        dm = slope_mono(lev(ku - 1), lev(ku), lev(ku + 1))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            flux[k - 1] = np.where(c == 0, 0.0, np.where(pos, w * (cf * (lev(ku) + dm * 0.5 * (1 - cf)) + S) / c,
+                                                         w * (cf * (lev(ku) - dm * 0.5 * (1 + cf)) - S) / c))
+    return flux
+
+
+@pytest.mark.parametrize("case", ["van_leer", "van_leer_long_step"])
+def test_van_leer_flux_divergences_match_restatement(case):
+    from gmcore_gb300 import abi
+    long = case.endswith("long_step")
+    cfg = baroclinic_config(ffsl_flux_type=abi.FLUX_VAN_LEER, **(dict(dt=1200.0) if long else {}))
+    o = prepared(cfg, u_wave=60.0 if long else 0.0)
+    try:
+        o.run_pass(0)
+        nlat, nlon, nlev = cfg.nlat, cfg.nlon, cfg.nlev
+        le_lon, le_lat, area = (o.metric("le_lon", nlat)[None, :, None], o.metric("le_lat", nlat - 1)[None, :, None],
+                                o.metric("area_cell", nlat)[None, :, None])
+        I = slice(1, nlat - 1)
+        B = {n: o.get_batch(n) for n in ("u", "v", "cflx", "cfly", "divx", "divy")}
+        gx, gy = ffsl_fluxes(cfg, o, o.get_field("pt"), B, o.get_field("mfx_lon"), o.get_field("mfy_lat"),
+                             cfg.dt_dyn, hflx=hflx_van_leer)
+        want = {"dptfdlon": (gx[:, I] - prev(gx[:, I])) * le_lon[:, I] / area[:, I]}
+        dlat = np.zeros((nlev, nlat, nlon))
+        dlat[:, I] = (gy[:, 1:] * le_lat[:, 1:] - gy[:, :-1] * le_lat[:, :-1]) / area[:, I]
+        dlat[:, 0] = (ring(gy[:, 0]) * le_lat[0, 0, 0] / nlon / area[0, 0, 0])[:, None]
+        dlat[:, -1] = (ring(-gy[:, -1]) * le_lat[0, -1, 0] / nlon / area[0, -1, 0])[:, None]
+        want["dptfdlat"] = dlat
+        pt = o.get_field("pt")
+        g = np.zeros((nlev + 4,) + pt.shape[1:])
+        g[2:nlev + 2] = pt
+        g[1] = 2 * g[2] - g[3]
+        g[0] = 2 * g[1] - g[2]
+        g[nlev + 2] = 2 * g[nlev + 1] - g[nlev]
+        g[nlev + 3] = 2 * g[nlev + 2] - g[nlev + 1]
+        flux = vertical_flux_van_leer(g, o.get_batch("we"), o.get_batch("cflz"))
+        want["dptfdlev"] = flux[1:] - flux[:-1]
+        for name, w in want.items():
+            got = o.get_tend(0, name)
+            if name == "dptfdlon":
+                got = got[:, I]
+            assert close(got, w), (case, name, float(np.abs(got - w).max() / np.abs(w).max()))
     finally:
         o.close()
