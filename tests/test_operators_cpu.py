@@ -211,6 +211,7 @@ def horizontal(cfg, o):
 
 CASES = {
     "swm_5deg": lambda: swm_config(),
+    "swm_5deg_coriolis2": lambda: swm_config(coriolis_scheme=2),
     "swm_1deg": lambda: swm_config(nlon=360, nlat=180, dt=60.0),
     "baroclinic_5deg_l26": lambda: baroclinic_config(),
     "baroclinic_4deg_wrf_l32": lambda: baroclinic_config(nlon=90, nlat=46, nlev=32, dt=600.0),
@@ -270,7 +271,19 @@ def forward_tendencies(cfg, o):
     dmfdlat[:, 0] = (ring(mfy[:, 0]) * M["le_lat"][0] / nlon / M["area_cell"][0])[:, None]
     dmfdlat[:, -1] = (ring(-mfy[:, -1]) * M["le_lat"][-1] / nlon / M["area_cell"][-1])[:, None]
     out["dmfdlat"] = dmfdlat, None
-    if not cfg.baroclinic:
+    if cfg.coriolis_scheme == 2:      # qhu = mfx_lat pv_lat, qhv = mfy_lon pv_lon (:879, 899)
+        mfx_lat = (col("half_tangent_wgt1") * (prev(mfx[:, :-1]) + mfx[:, :-1]) +
+                   col("half_tangent_wgt2") * (prev(mfx[:, 1:]) + mfx[:, 1:]))
+        mfy_lon = (col("full_tangent_wgt1")[:, I] * (mfy[:, :-1] + nxt(mfy[:, :-1])) +
+                   col("full_tangent_wgt2")[:, I] * (mfy[:, 1:] + nxt(mfy[:, 1:])))
+        out["qhu"] = mfx_lat * pvy, None
+        out["qhv"] = mfy_lon * pvx[:, I], I
+    if not cfg.baroclinic:            # shallow water (gmcore_mod.F90:503-518)
+        out["du"] = out["qhv"][0] - out["dkedlon"][0], I
+        out["dv"] = -out["qhu"][0] - out["dkedlat"][0], None
+        dmfdlon = o.get_tend(0, "dmfdlon")
+        dmfdlon[:, I] = out["dmfdlon"][0]
+        out["dgz"] = -(dmfdlon + dmfdlat) * cfg.g, None
         return out
     dmfdlon = o.get_tend(0, "dmfdlon")          # pole rows as the pass leaves them
     dmfdlon[:, I] = out["dmfdlon"][0]
