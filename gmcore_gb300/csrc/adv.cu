@@ -1064,10 +1064,8 @@ void launch_hflx_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const
 // first two scratch fields of the operator entry points are not used): the y
 // inner pass (qy), then both x passes (qx and fx), then the y outer pass on qx.
 template <class R>
-void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy,
-                      R *fx, R *fy, double dt) {
-  (void)qmfx;
-  (void)qmfy;
+void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qx, R *qy, R *fx, R *fy,
+                      double dt) {
   launch_ffsl_inner_y<R>(g, L, b, q, qy, dt);
   launch_ffsl_x2<R>(g, L, b, q, qy, qx, fx, dt);
   launch_hflx_y<R>(g, L, b, qx, fy);
@@ -1087,9 +1085,9 @@ void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const
 }
 
 template void launch_ffsl_hflx<double>(const DGrid &, const Launch &, const BatchView<double> &, const double *, double *,
-                                       double *, double *, double *, double *, double *, double);
+                                       double *, double *, double *, double);
 template void launch_ffsl_hflx<float>(const DGrid &, const Launch &, const BatchView<float> &, const float *, float *,
-                                      float *, float *, float *, float *, float *, double);
+                                      float *, float *, float *, double);
 #define INST_FFSL_PARTS(R)                                                                                           \
   template void launch_ffsl_inner_y<R>(const DGrid &, const Launch &, const BatchView<R> &, const R *, R *, double);  \
   template void launch_ffsl_x2<R>(const DGrid &, const Launch &, const BatchView<R> &, const R *, const R *, R *, R *, \

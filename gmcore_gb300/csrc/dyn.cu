@@ -1317,8 +1317,7 @@ void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s) {
   k_surface_rel<<<(int)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, L.stream>>>(s.phs_f, s.psr, n, g.ptop);
 }
 template <class R>
-void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out) {
-  (void)w;
+void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, double *partial, double *out) {
   k_diag_partial<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, partial);
   k_diag_final<<<1, 256, 0, L.stream>>>(partial, g.nlat * g.nlev, out);
 }
@@ -1340,7 +1339,7 @@ void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Wo
   template void launch_surface_rel<R>(const DGrid &, const Launch &, const Slot<R> &);                             \
   template void launch_update_uv<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
   template void launch_filter_prologue<R>(const DGrid &, const Launch &, const Slot<R> &);                        \
-  template void launch_diagnose<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &, double *, double *);
+  template void launch_diagnose<R>(const DGrid &, const Launch &, const Slot<R> &, double *, double *);
 
 INSTANTIATE(double)
 INSTANTIATE(float)

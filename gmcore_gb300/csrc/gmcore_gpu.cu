@@ -809,14 +809,16 @@ struct Engine : EngineBase {
     BatchView<R> b{};
     b.u = (const R *)f.u; b.v = (const R *)f.v; b.mfx = (const R *)f.mfx; b.mfy = (const R *)f.mfy;
     b.cflx = (const R *)f.cflx; b.cfly = (const R *)f.cfly; b.divx = (const R *)f.divx; b.divy = (const R *)f.divy;
-    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr, scr + n, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
+    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(scr, stream);
     if (e != cudaSuccess) throw CudaError(std::string("ffsl_hflx: ") + cudaGetErrorString(e));
     CK(cudaStreamSynchronize(stream));
   }
 
-  // Bytes of the four scratch fields of one horizontal FFSL flux.
+  // Bytes of the scratch of one horizontal FFSL flux: four fields, the size the
+  // no-allocation entry point documents; the flux keeps its intermediates qx,
+  // qy in the last two.
   size_t ffsl_scratch_bytes() const override { return 4 * full3() * sizeof(R); }
 
   // The same flux with the scratch supplied by the caller (no allocation).
@@ -828,7 +830,7 @@ struct Engine : EngineBase {
     BatchView<R> b{};
     b.u = (const R *)f.u; b.v = (const R *)f.v; b.mfx = (const R *)f.mfx; b.mfy = (const R *)f.mfy;
     b.cflx = (const R *)f.cflx; b.cfly = (const R *)f.cfly; b.divx = (const R *)f.divx; b.divy = (const R *)f.divy;
-    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr, scr + n, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
+    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
   }
@@ -1529,7 +1531,7 @@ struct Engine : EngineBase {
   void diagnose(int m, gmc_diag *out) override {
     const Slot<R> &s = slots[m * 3 + old_i];
     launch_surface_rel<R>(dg, L, s);
-    launch_diagnose<R>(dg, L, s, work[m], diag_partial, diag_out);
+    launch_diagnose<R>(dg, L, s, diag_partial, diag_out);
     double h[8];
     CK(cudaMemcpyAsync(h, diag_out, 7 * sizeof(double), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));

@@ -82,7 +82,7 @@ template <class R> void launch_update_uv(const DGrid &g, const Launch &L, const 
 template <class R> void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s);
 // FP32 form: psr = phs_f - ptop of a slot (no-op in the FP64 form).
 template <class R> void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s);
-template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double *partial, double *out);
+template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, double *partial, double *out);
 
 // Divergence damping of order 2 or 4 (div_damp_run, div_damp_mod.F90:89-139);
 // div and div2 are scratch cell fields.
@@ -91,7 +91,7 @@ template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const S
 // ---- advection (adv.cu) ---------------------------------------------------
 // Horizontal FFSL flux of q (ffsl_calc_tracer_hflx_cell): inner advective
 // operators, intermediate qx/qy, outer flux-form operators into (fx, fy).
-template <class R> void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qmfx, R *qmfy, R *qx, R *qy, R *fx, R *fy, double dt);
+template <class R> void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qx, R *qy, R *fx, R *fy, double dt);
 // the three FFSL kernels of launch_ffsl_hflx separately (profiled as three groups)
 template <class R> void launch_ffsl_inner_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qy, double dt);
 template <class R> void launch_ffsl_x2(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, const R *qy, R *qx, R *fx, double dt);
