@@ -302,3 +302,25 @@ def test_divergence_damping_coefficients_match_restatement(case):
     for got, want in ((got_lon, want_lon), (got_lat, want_lat)):
         err = np.abs(got - want).max() / np.abs(want).max()
         assert err <= 4 * np.finfo(float).eps, (case, err)
+
+
+@pytest.mark.parametrize("nlon,nlat", [(72, 37), (360, 180)])
+def test_library_host_tables_match_restatement(nlon, nlat):
+    """The library's own host entry points (gmc_mesh_metric, gmc_filter_taps,
+    which build the grid from the library's normalised configuration) give
+    the restated tables and the oracle's tap counts."""
+    import gmcore_gb300 as g
+    cfg = swm_config(nlon=nlon, nlat=nlat, dt=60.0)
+    want = restated(cfg)
+    for name, w in sorted(want.items()):
+        got = g.mesh_metric(cfg, name)
+        fill = w == np.finfo(float).max
+        assert np.array_equal(got[fill], w[fill]), name
+        assert np.array_equal(got[~fill], w[~fill]), name
+    o = Oracle(cfg)
+    try:
+        for which in (0, 1, 2):
+            for lat in (0, 1):
+                assert np.array_equal(g.filter_taps(cfg, which, lat), o.filter_taps(which, lat)), (which, lat)
+    finally:
+        o.close()
