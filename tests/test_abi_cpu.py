@@ -53,3 +53,17 @@ def test_null_arguments():
     assert lib.gmc_step(None, 1) == abi.GMC_EINVAL
     assert lib.gmc_prepare(None) == abi.GMC_EINVAL
     assert lib.gmc_last_error(None) == b"null context"
+
+
+def test_no_gpu_means_an_error_not_a_fallback():
+    """Without a usable CUDA device a context cannot be created: gmc_create
+    returns GMC_ECUDA with the CUDA runtime's message and no CPU path runs."""
+    from conftest import gpu_available
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    from helpers import baroclinic_config, swm_config
+    for cfg in (swm_config(), baroclinic_config()):
+        with pytest.raises(g.GmcError) as e:
+            g.Model(cfg)
+        assert e.value.code == abi.GMC_ECUDA
+        assert "cuda" in str(e.value).lower()
