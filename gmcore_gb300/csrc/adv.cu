@@ -94,8 +94,8 @@ __device__ __forceinline__ void hflx_xrows(const DGrid &g, int j, int k, const R
       for (int f = 0; f < NF; ++f) mo[f] = mul[f][o];
     }
     R flux[NF];
-    if (!(fabs(c) <= hxr)) {   // |cflx| beyond the reach the reference allows: error, no flux
-      atomicOr(g.err, ERR_CFLX);
+    if (fabs(c) > hxr) {   // |cflx| beyond the reach the reference allows: error, no flux (NaN: no flux below)
+      raise_err(g, ERR_CFLX);
 #pragma unroll
       for (int f = 0; f < NF; ++f) flux[f] = 0;
     } else {
@@ -158,8 +158,8 @@ __device__ __forceinline__ const R *halo_row(const DGrid &g, const R *f, int jj,
 // and slopes sl[t-1 .. t+2] at those rows.
 template <class R>
 __device__ __forceinline__ R hflx_yface(const DGrid &g, R c, R vv, const R *y, const R *sl, int t) {
-  if (!(fabs(c) <= (R)1)) {
-    atomicOr(g.err, ERR_CFLY);
+  if (fabs(c) > (R)1) {   // a NaN Courant number falls through to a zero flux
+    raise_err(g, ERR_CFLY);
     return 0;
   }
   if (g.flux_type == GMC_FLUX_VAN_LEER) {   // hflx_van_leer_cell (ffsl_mod.F90:603-610)
@@ -359,7 +359,7 @@ __device__ __forceinline__ R vflx_at(const DGrid &g, const R *col, int k, R c, R
   const int nlev = g.nlev, lim = g.limiter;
   auto C = [&](int kk) { return col[min(max(kk, -1), nlev + 2) + 1]; };
   if (!(fabs(c) <= (R)nlev)) {
-    atomicOr(g.err, ERR_CFLZ);
+    raise_err(g, ERR_CFLZ);
     return 0;
   }
   const int ci = (int)c;
@@ -521,7 +521,7 @@ template <class R>
 __device__ R vflx_tile(const DGrid &g, const R *C, const R *FL, const R *DF, const R *F6, int ld, int k, R c, R w) {
   const int nlev = g.nlev;
   if (!(fabs(c) <= (R)nlev)) {
-    atomicOr(g.err, ERR_CFLZ);
+    raise_err(g, ERR_CFLZ);
     return 0;
   }
   auto Cv = [&](int kk) { return C[(min(max(kk, -1), nlev + 2) + 1) * ld]; };
@@ -761,7 +761,7 @@ __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, d
       float c = cflz_of_f(g.half_lev_f, g.full_dlev_f, g.full_dlev_rf, nlev, col, st, k, dtf, bad);
       if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
-    if (bad) atomicOr(g.err, ERR_CFLZ);
+    if (bad) raise_err(g, ERR_CFLZ);
     return;
   }
   R we[66], ml[66];
@@ -775,7 +775,7 @@ __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, d
     R c = cflz_of<R>(g, we, ml, k, (R)dt, bad);
     if (c == c) cflz[ix3(nlat, nlon, i, j, k)] = c;
   }
-  if (bad) atomicOr(g.err, ERR_CFLZ);
+  if (bad) raise_err(g, ERR_CFLZ);
 }
 
 // q_new = (old_m q_old - dt div(qmf)) / m, then the zonal negative fixer,
@@ -853,7 +853,7 @@ __global__ void GMC_BOUNDS(R, 8) k_tracer_horizontal(DGrid g, const R *q_old, R 
           } else if (qm2 > qm0) {
             row[p + 1] = (qm2 - qm0) / mrow[p + 1];
           } else {
-            atomicOr(g.err, ERR_NEGTRACER);
+            raise_err(g, ERR_NEGTRACER);
           }
           row[p] = 0;
         }
@@ -905,7 +905,7 @@ __global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const R *we, Sur
       } else if (qm2 > qm0) {
         if (qm2 > 0) qc[k + 1] = (qm2 - qm0) / m[k];
       } else {
-        atomicOr(g.err, ERR_NEGTRACER);
+        raise_err(g, ERR_NEGTRACER);
       }
       qc[k] = 0;
     }
@@ -1005,7 +1005,7 @@ __global__ void GMC_BOUNDS_F(6) k_tracer_vertical_f(DGrid g, float *q, const flo
         } else if (qm2 > qm0) {
           if (qm2 > 0) qc[(k + 1) * ld] = (qm2 - qm0) / M[k * ld];
         } else {
-          atomicOr(g.err, ERR_NEGTRACER);
+          raise_err(g, ERR_NEGTRACER);
         }
         qc[k * ld] = 0;
       }
@@ -1060,8 +1060,7 @@ void launch_hflx_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const
   k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
 }
 
-// One horizontal FFSL flux evaluation (fx, fy of q; qx, qy scratch; the
-// first two scratch fields of the operator entry points are not used): the y
+// One horizontal FFSL flux evaluation (fx, fy of q; qx, qy scratch): the y
 // inner pass (qy), then both x passes (qx and fx), then the y outer pass on qx.
 template <class R>
 void launch_ffsl_hflx(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qx, R *qy, R *fx, R *fy,

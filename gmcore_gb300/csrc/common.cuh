@@ -72,6 +72,7 @@ struct DGrid {
   const float *cfl_yoff;
   const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
+  int f_layer_mass;                                                // 1: the form's layer mass is dmA + dmB psr (FP32)
   const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables
   const float *hybi_f;                                             // FP32 copy of hybi [k-1]
   const float *full_dlev_rf;                                       // FP32 1 / full_dlev [k-1]
@@ -88,8 +89,16 @@ struct DGrid {
   const double *lon_damp_full;                                     // [j-1]
   const double *div_c_lon, *div_c_lat;                             // [(k-1)*n + j-1]
   FilterDev big, small1, small2;
-  unsigned *err;                                                   // device error word
+  unsigned *err;                                                   // device error words [2] (raise_err)
 };
+
+// Raise an error from a kernel: err[0] collects every bit raised, err[1]
+// keeps the first one (kernels run in the step's launch order, so that is the
+// error the reference, which stops at its first log_error, would report).
+__device__ __forceinline__ void raise_err(const DGrid &g, unsigned bit) {
+  atomicOr(g.err, bit);
+  atomicCAS(g.err + 1, 0u, bit);
+}
 
 #define ROW(t, j) ((t)[(j) + 1])
 

@@ -297,7 +297,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       const float u3 = at(0.5f * cdx * u2);
       const float u4 = at(cdx * u3);
       const float c = div6(u1 + 2.0f * u2 + 2.0f * u3 + u4) * cdx;
-      if (!(fabsf(c) <= hx)) atomicOr(g.err, ERR_CFLX);
+      if (fabsf(c) > hx) raise_err(g, ERR_CFLX);   // NaN passes, as abs(cflx) > width does
       size_t o = ix3(nlat, nlon, i, j, k);
       cflx[o] = c;
       divx[o] = fdiv((u1 - Ul(i - 1)) * lel, ac);
@@ -323,7 +323,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       l = (int)floor(i + (x3 - x0) / dx);
       double u4 = ((radius * half_lon(l + 1) * cl - x3) * Ul(l) + (x3 - radius * half_lon(l) * cl) * Ul(l + 1)) / dx;
       double c = (u1 + 2 * u2 + 2 * u3 + u4) / 6 * dt_ / dx;
-      if (!(fabs(c) <= (double)g.hx)) atomicOr(g.err, ERR_CFLX);
+      if (fabs(c) > (double)g.hx) raise_err(g, ERR_CFLX);
       size_t o = ix3(nlat, nlon, i, j, k);
       cflx[o] = (R)c;
       double uw = Ul(i - 1);
@@ -350,7 +350,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
         const float v3 = at(0.5f * cdy * v2);
         const float v4 = at(cdy * v3);
         const float c = div6(v1 + 2.0f * v2 + 2.0f * v3 + v4) * cdy;
-        if (!(fabsf(c) <= 1.0f)) atomicOr(g.err, ERR_CFLY);
+        if (fabsf(c) > 1.0f) raise_err(g, ERR_CFLY);
         cfly[ix3(nhalf, nlon, i, j, k)] = c;
       }
     }
@@ -375,7 +375,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       l = (int)floor(j + (y3 - y0) / dy);
       double v4 = (l < 1 || l > nhalf - 1) ? v1 : interp(l, y3);
       double c = (v1 + 2 * v2 + 2 * v3 + v4) / 6 * dt_ / dy;
-      if (!(fabs(c) <= 1.0)) atomicOr(g.err, ERR_CFLY);
+      if (fabs(c) > 1.0) raise_err(g, ERR_CFLY);
       cfly[ix3(nhalf, nlon, i, j, k)] = (R)c;
     }
   }
@@ -447,7 +447,7 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
       float c = cflz_of_f(g.half_lev_f, g.full_dlev_f, g.full_dlev_rf, nlev, col, st, k, dtf, bad);
       if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
     }
-    if (bad) atomicOr(g.err, ERR_CFLZ);
+    if (bad) raise_err(g, ERR_CFLZ);
   } else {
     double mfp[66], we[66], ml[66];
     const double lel = ROW(g.le_lon, j), ac = ROW(g.area_cell, j), la0 = ROW(g.le_lat, j), la1 = ROW(g.le_lat, j - 1);
@@ -491,7 +491,7 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
       double c = cflz_of<double>(g, we, ml, k, dt, bad);
       if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = (R)c;
     }
-    if (bad) atomicOr(g.err, ERR_CFLZ);
+    if (bad) raise_err(g, ERR_CFLZ);
   }
 }
 
@@ -572,7 +572,7 @@ __global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<flo
     float c = cflz_of_f(HL, FD, RFD, nlev, WM + ti, ld, k, dtf, bad);
     if (c == c) w.cflz[ix3(nlat, nlon, i, j, k)] = c;
   }
-  if (bad) atomicOr(g.err, ERR_CFLZ);
+  if (bad) raise_err(g, ERR_CFLZ);
 }
 
 // Momentum tendencies of the forward pass (gmcore_mod.F90:478-490 / 507-518):
@@ -759,6 +759,25 @@ __device__ __forceinline__ T *smem_rows(double *base, int nlon, int which) {
   return reinterpret_cast<T *>(base) + (size_t)which * nlon;
 }
 
+// Error checks of one column's new surface pressure phs (unfiltered) and its
+// filtered value phs_f: ERR_NAN when either is not finite, ERR_NONMONO when
+// a layer mass from phs_f is not positive (calc_m, operators_mod.F90:489-500).
+// The FP32 form checks its own layer masses dA_k + dB_k psr (psr = phs_f - ptop
+// in FP32); the FP64 form the hybrid-formula difference ph_lev(k+1) - ph_lev(k).
+__device__ __forceinline__ void check_column(const DGrid &g, double phs, double phs_f, float psr) {
+  if (!isfinite(phs) || !isfinite(phs_f)) {
+    raise_err(g, ERR_NAN);
+    return;
+  }
+  bool bad = false;
+  if (g.f_layer_mass) {
+    for (int k = 1; k <= g.nlev; ++k) bad |= !(fmaf(g.dmB[k - 1], psr, g.dmA[k - 1]) > 0.0f);
+  } else {
+    for (int k = 1; k <= g.nlev; ++k) bad |= !(Mass<double>::layer(g, k, phs_f) > 0.0);
+  }
+  if (bad) raise_err(g, ERR_NONMONO);
+}
+
 // phs = phs_old + dt dphs; phs_f = big filter(phs)   (:134-143)
 template <class R>
 __global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
@@ -782,8 +801,10 @@ __global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt
     __syncthreads();
     for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
       const double f = filtered ? ref + (double)dev[i] : row[i];
+      const float psr = (float)(f - g.ptop);
       n.phs_f[c0 + i] = f;
-      n.psr[c0 + i] = (float)(f - g.ptop);
+      n.psr[c0 + i] = psr;
+      check_column(g, row[i], f, psr);
     }
     return;
   }
@@ -798,7 +819,18 @@ __global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
     n.phs_f[(size_t)(j - 1) * nlon + i] = row[i];
     if (n.psr) n.psr[(size_t)(j - 1) * nlon + i] = (float)(row[i] - g.ptop);
+    check_column(g, n.phs[(size_t)(j - 1) * nlon + i], row[i], 0.0f);
   }
+}
+
+// Column checks of a new surface pressure: a non-finite value, and the
+// layer masses of calc_m (operators_mod.F90:489-500, m = ph_lev(k+1) -
+// ph_lev(k) <= 0 stops the reference with 'The pressure levels are not
+// monotonic!') from the filtered surface pressure phs_f, as each form forms
+// them (FP64 hybrid formula; FP32 dA_k + dB_k psr).
+__global__ void k_check_columns(DGrid g, const double *__restrict__ phs_f, const float *__restrict__ psr, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    check_column(g, phs_f[t], phs_f[t], psr ? psr[t] : 0.0f);
 }
 
 // FP32 form: psr = phs_f - ptop
@@ -838,7 +870,11 @@ __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   for (int kk = 0; kk < nk; ++kk) {
     const int k = k0 + kk;
     const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.pt[c0 + i] = row[kk * nlon + i] / Mass<R>::layer(g, k, sn.at(m0 + i));
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const R v = row[kk * nlon + i] / Mass<R>::layer(g, k, sn.at(m0 + i));
+      n.pt[c0 + i] = v;
+      if (!isfinite(v)) raise_err(g, ERR_NAN);
+    }
   }
 }
 
@@ -860,7 +896,10 @@ __global__ void k_update_gz(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.gz_f[(size_t)(j - 1) * nlon + i] = row2[i];
   filter_row<R>(g.small1, true, j, nlon, row, ext);
   __syncthreads();
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.gz[(size_t)(j - 1) * nlon + i] = row[i];
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    n.gz[(size_t)(j - 1) * nlon + i] = row[i];
+    if (!isfinite(row[i])) raise_err(g, ERR_NAN);
+  }
 }
 
 // Backward-pass column sweep (operators_prepare_2 backward,
@@ -1061,6 +1100,7 @@ __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work
       for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
         const R v = row[kk * nlon + i0];
         n.u_lon[c0 + i0] = v;
+        if (!isfinite(v)) raise_err(g, ERR_NAN);
         if (!big) n.u_f[c0 + i0] = v;
       }
     }
@@ -1107,6 +1147,7 @@ __global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work
     for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
       const R v = row[kk * nlon + i0];
       n.v_lat[cj + i0] = v;
+      if (!isfinite(v)) raise_err(g, ERR_NAN);
       if (!big) n.v_f[cj + i0] = v;
     }
   }
@@ -1317,6 +1358,12 @@ void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s) {
   k_surface_rel<<<(int)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, L.stream>>>(s.phs_f, s.psr, n, g.ptop);
 }
 template <class R>
+void launch_check_columns(const DGrid &g, const Launch &L, const Slot<R> &s) {
+  if (!s.phs_f) return;
+  const size_t n = (size_t)g.nlat * g.nlon;
+  k_check_columns<<<(int)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, L.stream>>>(g, s.phs_f, s.psr, n);
+}
+template <class R>
 void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, double *partial, double *out) {
   k_diag_partial<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, partial);
   k_diag_final<<<1, 256, 0, L.stream>>>(partial, g.nlat * g.nlev, out);
@@ -1337,6 +1384,7 @@ void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, double *
   template void launch_update_gz<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
   template void launch_column_backward<R>(const DGrid &, const Launch &, const Slot<R> &, const Work<R> &);       \
   template void launch_surface_rel<R>(const DGrid &, const Launch &, const Slot<R> &);                             \
+  template void launch_check_columns<R>(const DGrid &, const Launch &, const Slot<R> &);                           \
   template void launch_update_uv<R>(const DGrid &, const Launch &, const Slot<R> &, const Slot<R> &, const Work<R> &, double);  \
   template void launch_filter_prologue<R>(const DGrid &, const Launch &, const Slot<R> &);                        \
   template void launch_diagnose<R>(const DGrid &, const Launch &, const Slot<R> &, double *, double *);

@@ -50,6 +50,7 @@ struct Arena {
     cudaError_t e = cudaMalloc(&base, bytes);
     if (e != cudaSuccess) {
       base = nullptr;
+      cudaGetLastError();   // a failed allocation must not surface as a later call's error
       throw ApiError{GMC_ENOMEM, std::string("device allocation of ") + std::to_string(bytes) + " bytes failed: " +
                                      cudaGetErrorString(e)};
     }
@@ -420,6 +421,14 @@ struct Engine : EngineBase {
   }
 
   explicit Engine(const gmc_config &cfg) {
+    try {
+      construct(cfg);
+    } catch (...) {
+      release_all();   // a constructor that throws runs no destructor
+      throw;
+    }
+  }
+  void construct(const gmc_config &cfg) {
     std::string e = grid.build(cfg);
     if (!e.empty()) throw ApiError{GMC_EINVAL, e};
     nm = cfg.n_members;
@@ -472,7 +481,8 @@ struct Engine : EngineBase {
     CK(cudaMallocHost(&pinned, pinned_n * sizeof(double)));
   }
 
-  ~Engine() override {
+  ~Engine() override { release_all(); }
+  void release_all() {
     if (stream) cudaStreamSynchronize(stream);
     for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
     for (auto &p : prof_pending) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
@@ -498,7 +508,9 @@ struct Engine : EngineBase {
       tl->store.release();
     }
     if (pinned) cudaFreeHost(pinned);
+    pinned = nullptr;
     if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
   }
 
   void upload_tables() {
@@ -626,6 +638,7 @@ struct Engine : EngineBase {
     dg.tf_ref = reinterpret_cast<const float *>(tables.base + offTF);
     dg.dlnp_ref = reinterpret_cast<const float *>(tables.base + offDL);
     dg.ps_ref = ps_ref;
+    dg.f_layer_mass = kFP32 ? 1 : 0;
     for (const FFix &x : ff) {
       x.d->ntaps_full = reinterpret_cast<const int *>(tables.base + x.nf);
       x.d->ntaps_half = reinterpret_cast<const int *>(tables.base + x.nh);
@@ -805,21 +818,20 @@ struct Engine : EngineBase {
       throw ApiError{GMC_EINVAL, "null field pointer"};
     R *scr = nullptr;
     const size_t n = full3();
-    CK(cudaMallocAsync((void **)&scr, 4 * n * sizeof(R) + 1024, stream));
+    CK(cudaMallocAsync((void **)&scr, ffsl_scratch_bytes(), stream));
     BatchView<R> b{};
     b.u = (const R *)f.u; b.v = (const R *)f.v; b.mfx = (const R *)f.mfx; b.mfy = (const R *)f.mfy;
     b.cflx = (const R *)f.cflx; b.cfly = (const R *)f.cfly; b.divx = (const R *)f.divx; b.divy = (const R *)f.divy;
-    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
+    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr, scr + n, (R *)f.qmfx, (R *)f.qmfy, dt);
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(scr, stream);
     if (e != cudaSuccess) throw CudaError(std::string("ffsl_hflx: ") + cudaGetErrorString(e));
     CK(cudaStreamSynchronize(stream));
   }
 
-  // Bytes of the scratch of one horizontal FFSL flux: four fields, the size the
-  // no-allocation entry point documents; the flux keeps its intermediates qx,
-  // qy in the last two.
-  size_t ffsl_scratch_bytes() const override { return 4 * full3() * sizeof(R); }
+  // Bytes of the scratch of one horizontal FFSL flux: its intermediates qx, qy
+  // (two cell fields), the size the no-allocation entry point documents.
+  size_t ffsl_scratch_bytes() const override { return 2 * full3() * sizeof(R); }
 
   // The same flux with the scratch supplied by the caller (no allocation).
   void ffsl_hflx_in(const gmc_ffsl_fields &f, double dt, void *scratch) override {
@@ -830,7 +842,7 @@ struct Engine : EngineBase {
     BatchView<R> b{};
     b.u = (const R *)f.u; b.v = (const R *)f.v; b.mfx = (const R *)f.mfx; b.mfy = (const R *)f.mfy;
     b.cflx = (const R *)f.cflx; b.cfly = (const R *)f.cfly; b.divx = (const R *)f.divx; b.divy = (const R *)f.divy;
-    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr + 2 * n, scr + 3 * n, (R *)f.qmfx, (R *)f.qmfy, dt);
+    launch_ffsl_hflx<R>(dg, L, b, (const R *)f.q, scr, scr + n, (R *)f.qmfx, (R *)f.qmfy, dt);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
   }
@@ -1054,6 +1066,7 @@ struct Engine : EngineBase {
       const Slot<R> &s = slots[m * 3 + old_i];
       launch_filter_prologue<R>(dg, L, s);
       launch_surface_rel<R>(dg, L, s);
+      launch_check_columns<R>(dg, L, s);   // calc_m of the prologue's operators_prepare
       if (ntr > 0) {
         // the prologue's copy_old_m sees the layer mass before operators_prepare
         CK(cudaMemsetAsync(tb[m].old_phs_f, 0, two_d() * sizeof(double), stream));
@@ -1064,6 +1077,13 @@ struct Engine : EngineBase {
         if (m + 1 < nm) { uv_step = save_uv; mf_step = save_mf; we_step = save_we; }
       }
       forward_prepare(m, s, grid.cfg.dt_dyn);   // operators_prepare(blocks, old, dt_dyn)
+      if (grid.cfg.baroclinic) {
+        // calc_mf's accum_uv_cell of the mass batch (operators_mod.F90:556): the
+        // prologue checks its Courant numbers as the reference does; every
+        // forward pass recomputes them
+        Work<R> &w = work[m];
+        launch_batch_cfl<R>(dg, L, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, grid.cfg.dt_dyn);
+      }
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
@@ -1545,12 +1565,17 @@ struct Engine : EngineBase {
     out->te = out->te_ke + out->te_ie + out->te_pe;
   }
 
+  // The first error raised on the device since the last read (the error
+  // words are cleared): err[1] holds the first bit, err[0] all of them.
   unsigned read_error() override {
-    unsigned h = 0;
-    CK(cudaMemcpyAsync(&h, err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    unsigned h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, err, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    if (h) CK(cudaMemsetAsync(err, 0, sizeof(unsigned), stream));
-    return h;
+    if (h[0] | h[1]) {
+      CK(cudaMemsetAsync(err, 0, 2 * sizeof(unsigned), stream));
+      CK(cudaStreamSynchronize(stream));
+    }
+    return h[1] ? h[1] : h[0];
   }
 };
 
@@ -1693,7 +1718,13 @@ int noalloc_scratch_address(int dev, void **out, std::string &err) {
     }
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (cur != dev) cudaSetDevice(cur);
+    if (cur != dev) {
+      const cudaError_t r = cudaSetDevice(cur);   // the caller's device, restored before anything is cached
+      if (r != cudaSuccess) {
+        err = std::string("cudaSetDevice (restoring the caller's device): ") + cudaGetErrorString(r);
+        return GMC_ECUDA;
+      }
+    }
     if (e != cudaSuccess || !p) {
       err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
       return GMC_ECUDA;
@@ -1874,7 +1905,7 @@ int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt) {
   if (need > kNoAllocScratchBytes)
     return fail(ctx, GMC_EINVAL, "gmc_ffsl_hflx_noalloc: grid needs " + std::to_string(need) +
                                      " scratch bytes, the fixed scratch holds " + std::to_string(kNoAllocScratchBytes) +
-                                     " (4 x nlon x nlat x nlev values); use gmc_ffsl_hflx");
+                                     " (2 x nlon x nlat x nlev values); use gmc_ffsl_hflx");
   return guarded(ctx, [&]() {
     void *scr = nullptr;
     std::string err;

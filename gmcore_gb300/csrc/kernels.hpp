@@ -82,6 +82,8 @@ template <class R> void launch_update_uv(const DGrid &g, const Launch &L, const 
 template <class R> void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s);
 // FP32 form: psr = phs_f - ptop of a slot (no-op in the FP64 form).
 template <class R> void launch_surface_rel(const DGrid &g, const Launch &L, const Slot<R> &s);
+// non-finite or non-monotonic columns of a slot's filtered surface pressure (ERR_NAN, ERR_NONMONO)
+template <class R> void launch_check_columns(const DGrid &g, const Launch &L, const Slot<R> &s);
 template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, double *partial, double *out);
 
 // Divergence damping of order 2 or 4 (div_damp_run, div_damp_mod.F90:89-139);

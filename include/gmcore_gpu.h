@@ -10,13 +10,17 @@
  * (src/dynamics/gmcore_mod.F90:97-135) and the conservation monitor
  * `diagnose` (src/dynamics/gmcore_mod.F90:213-341).  A Fortran host keeps
  * its namelist, initial conditions, output and restart code and calls these
- * functions through iso_c_binding (see INTEGRATION.md for the shim).
+ * functions through iso_c_binding (module gmcore_gpu_mod in
+ * include/gmcore_gpu_mod.F90 binds every entry point).
  *
  * Conventions
  *  - Every function returns an int status: GMC_OK (0) or a negative code.
  *    A message for the last failure is available from gmc_last_error().
  *    The library never aborts the process (the reference stops through
- *    log_error / MPI_ABORT instead).
+ *    log_error / MPI_ABORT instead).  Kernels record errors in a device
+ *    error word; gmc_prepare and gmc_step return the first error raised in
+ *    launch order (the one at which the reference would have stopped) after
+ *    all requested steps ran.
  *  - Host arrays are described by gmc_view: a base pointer plus Fortran
  *    lower/upper bounds per dimension, column-major (i fastest), so a
  *    Fortran array with halos can be passed as c_loc(a) with lbound/ubound.
@@ -44,7 +48,8 @@ extern "C" {
                                 (adv_batch_mod.F90:284-287, 331-333, 538-601) */
 #define GMC_ENONMONO    -3   /* pressure levels not monotonic (operators_mod.F90:493-500) */
 #define GMC_ENEGTRACER  -4   /* negative tracer not fixable (adv_mod.F90:251-253, 290-292) */
-#define GMC_ENAN        -5   /* non-finite value in the prognostic state     */
+#define GMC_ENAN        -5   /* non-finite value in the prognostic state (surface
+                                pressure, potential temperature or gz, winds) */
 #define GMC_ETIMEDOUT   -6   /* a bounded device wait gave up                */
 #define GMC_ECUDA       -7   /* CUDA runtime error                           */
 #define GMC_ENOMEM      -8   /* device allocation failed                     */
@@ -190,22 +195,24 @@ typedef struct gmc_ffsl_fields {
 /* Horizontal FFSL flux of one field (inner advective operators, intermediate
  * qx/qy, outer flux-form operators), the reference's adv_calc_tracer_hflx_cell
  * plugin (adv_mod.F90:109, ffsl_calc_tracer_hflx_cell ffsl_mod.F90:318-413).
- * Its four scratch fields are allocated from the device pool for the call. */
+ * Its two scratch fields are allocated from the device pool for the call. */
 int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
 
 /* gmc_ffsl_hflx without any device allocation.  No counterpart in the
- * reference: it exists for callers that must not allocate at the moment of
- * the call -- code running while a CUDA graph is being captured, a host that
- * reserved all device memory for its own pool at start-up, or a real-time
- * loop where a cudaMalloc would synchronise the device.  Its four scratch
- * fields live in one fixed 32 MiB device array compiled into the library
- * (every GPU that loads the library keeps it until the process exits), so it
- * accepts grids with 4 x nlon x nlat x nlev x sizeof(value) <= 32 MiB and
- * returns GMC_EINVAL beyond that.  The first call on a device looks up the
- * array's device address (make that first call before any stream capture).
- * All calls share the one array: nothing in it needs to start at zero, and
- * calls whose kernels overlap on the GPU (two contexts on different streams
- * at the same time) race on it.  Results equal gmc_ffsl_hflx's. */
+ * reference: it exists for callers that cannot allocate device memory at the
+ * moment of the call -- a host model that reserved all device memory for its
+ * own pool at start-up (so a cudaMalloc would fail), or a time-critical loop
+ * where an allocation would synchronise the device or take an unbounded
+ * time.  Its two scratch fields (the intermediates qx, qy) live in one fixed
+ * 32 MiB device array compiled into the library (every GPU that loads the
+ * library keeps it until the process exits), so it accepts grids with
+ * 2 x nlon x nlat x nlev x sizeof(value) <= 32 MiB and returns GMC_EINVAL
+ * beyond that.  The call runs on the context's stream, waits for it and
+ * reads the device error word, like gmc_ffsl_hflx.  The first call on a
+ * device looks up the array's device address.  All calls share the one
+ * array: nothing in it needs to start at zero, and calls whose kernels
+ * overlap on the GPU (two contexts on different host threads at the same
+ * time) race on it.  Results equal gmc_ffsl_hflx's. */
 int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
 
 /* Tangent-linear and adjoint of nsteps model steps (the benchmark spec's

@@ -1709,6 +1709,22 @@ void *orc_create(const gmc_config *cfg, char *errbuf, int errlen) {
 
 void orc_destroy(void *h) { delete (orc::Model *)h; }
 
+// The seeded synthetic initial state of a benchmark configuration, from the
+// oracle's own build of the host set-up code (so that a CPU-only caller, such
+// as the timed CPU baseline, needs no other library).  Arguments as
+// gmc_make_ic: kind 1 shallow water, kind 2 baroclinic; interior arrays in C
+// order [k][j][i]; a null pointer skips that field.
+int orc_make_ic(const gmc_config *cfg, int kind, uint64_t seed, double noise_k, double *u_lon, double *v_lat,
+                double *pt_or_gz, double *phs, double *gzs, double *q) {
+  if (!cfg) return GMC_EINVAL;
+  gmc_config cc = *cfg;
+  if (!cc.baroclinic) cc.ke_scheme = 1;
+  if (!(cc.dt_adv > 0)) cc.dt_adv = cc.dt_dyn;
+  gmc::Grid g;
+  if (!g.build(cc).empty()) return GMC_EINVAL;
+  return gmc::make_ic(g, kind, seed, noise_k, u_lon, v_lat, pt_or_gz, phs, gzs, q).empty() ? GMC_OK : GMC_EINVAL;
+}
+
 int orc_lon_halo_width(void *h) { return ((orc::Model *)h)->mesh.hx; }
 
 static orc::Arr *orc_field(orc::Model *m, orc::State &s, const char *name, int &nrow, int &k0, int &k1) {

@@ -52,12 +52,40 @@ def load(variant="parity"):
     lib.orc_get_tracer_level.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.orc_tracer_piece.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.orc_ffsl_hflx.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 9 + [C.c_double] + [C.POINTER(C.c_double)] * 2
+    lib.orc_make_ic.argtypes = [C.POINTER(Config), C.c_int, C.c_uint64, C.c_double] + [C.POINTER(C.c_double)] * 6
     _LIBS[variant] = lib
     return lib
 
 
 def _ptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_ic(cfg, kind, seed, noise_k=1.0, variant="parity"):
+    """The seeded synthetic initial state from the oracle's own build (the
+    same generator as the library's gmc_make_ic): a dict of C-ordered float64
+    arrays u_lon, v_lat, gz | (pt, phs), gzs and, with tracers, q."""
+    lib = load(variant)
+    nlon, nlat, nlev = cfg.nlon, cfg.nlat, cfg.nlev
+    u = np.zeros((nlev, nlat, nlon))
+    v = np.zeros((nlev, nlat - 1, nlon))
+    gzs = np.zeros((nlat, nlon))
+    if kind == 1:
+        h = np.zeros((nlat, nlon))
+        rc = lib.orc_make_ic(C.byref(cfg), 1, seed, noise_k, _ptr(u), _ptr(v), _ptr(h), None, _ptr(gzs), None)
+        out = {"u_lon": u, "v_lat": v, "gz": h, "gzs": gzs}
+    else:
+        pt = np.zeros((nlev, nlat, nlon))
+        phs = np.zeros((nlat, nlon))
+        q = np.zeros((max(cfg.ntracer, 0), nlev, nlat, nlon))
+        rc = lib.orc_make_ic(C.byref(cfg), 2, seed, noise_k, _ptr(u), _ptr(v), _ptr(pt), _ptr(phs), _ptr(gzs),
+                             _ptr(q) if cfg.ntracer > 0 else None)
+        out = {"u_lon": u, "v_lat": v, "pt": pt, "phs": phs, "gzs": gzs}
+        if cfg.ntracer > 0:
+            out["q"] = q
+    if rc:
+        raise ValueError(f"orc_make_ic failed ({rc})")
+    return out
 
 
 FIELD_SHAPES = {
