@@ -1,5 +1,5 @@
-"""bench.py parses and its command line answers without a GPU (the driver
-runs it at round end; a syntax error there would lose the measurement)."""
+"""bench.py parses and its command line answers without a GPU (a syntax
+error there would lose the measurement)."""
 import os
 import subprocess
 import sys
@@ -46,3 +46,33 @@ def test_host_register_checks_its_argument_before_cuda():
     a = np.zeros((4, 6))[:, ::2]   # not contiguous
     with pytest.raises(ValueError):
         g.host_register(a)
+
+
+def test_cpu_baseline_leg_loads_only_the_oracle():
+    """The CPU baseline (and the reference arm built on it) builds its initial
+    state with the oracle's own generator and times steps that advect the
+    tracers; no library of the product is loaded in its process.  Run on a
+    small grid in a fresh interpreter."""
+    code = r'''
+import importlib.util, json, sys
+spec = importlib.util.spec_from_file_location("bench_mod", sys.argv[1])
+b = importlib.util.module_from_spec(spec)
+spec.loader.exec_module(b)
+from gmcore_gb300 import abi
+b.workload_config = lambda prec: abi.default_config(
+    nlon=72, nlat=37, nlev=32, baroclinic=1, dt_dyn=180.0, vert_coord_template=abi.VCOORD_WRF_L32,
+    time_scheme=abi.TIME_WRFRK3, max_wave_speed=400.0, ntracer=4, precision=prec)
+class A:
+    steps, warmup = 2, 1
+r = b.cpu_baseline(A(), sample_steps=2, warm=1)
+maps = open("/proc/self/maps").read()
+print(json.dumps({"r": r, "product": "libgmcore_gpu" in maps, "oracle": "liboracle_omp" in maps}))
+'''
+    import json
+    r = subprocess.run([sys.executable, "-c", code, os.path.join(ROOT, "bench.py")], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["oracle"] and not out["product"], out
+    assert out["r"]["kind"] == "port" and out["r"]["value"] > 0
+    assert "advects the tracers" in out["r"]["sample"]

@@ -1,9 +1,13 @@
-"""gmc_ffsl_hflx_noalloc: the FFSL flux entry point for callers that must not
-allocate device memory during the call (graph capture, a host that owns all
-device memory, real-time loops).  It must give the same fluxes as
-gmc_ffsl_hflx, call after call, while its scratch lives in the library's
-fixed device array; grids that do not fit that array are refused.  Kept in
-its own file so that pytest collects it last."""
+"""gmc_ffsl_hflx_noalloc: the FFSL flux entry point for callers that cannot
+allocate device memory during the call (a host model that reserved all device
+memory for its own pool, or a time-critical loop that must not wait on an
+allocation).  It must give the same fluxes as gmc_ffsl_hflx, call after call,
+while its scratch lives in the library's fixed device array; it must not
+allocate (the device's default memory pool and its free memory stay as they
+were); grids that do not fit that array are refused.  Kept in its own file so
+that pytest collects it last."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -38,6 +42,38 @@ def on_device(f, dtype):
     return dev, out, ptrs
 
 
+class DevicePool:
+    """The current device's default memory pool (the one cudaMallocAsync
+    draws from) and the device's free memory, read through the CUDA driver
+    API: the used-memory high-water mark can be reset and read back."""
+
+    USED_MEM_HIGH = 8   # CU_MEMPOOL_ATTR_USED_MEM_HIGH
+
+    def __init__(self):
+        self.cu = C.CDLL("libcuda.so.1")
+        assert self.cu.cuInit(0) == 0
+        ctx = C.c_void_p()
+        assert self.cu.cuCtxGetCurrent(C.byref(ctx)) == 0 and ctx.value, "no current CUDA context"
+        dev = C.c_int()
+        assert self.cu.cuCtxGetDevice(C.byref(dev)) == 0
+        self.pool = C.c_void_p()
+        assert self.cu.cuDeviceGetDefaultMemPool(C.byref(self.pool), dev) == 0
+
+    def reset_high(self):
+        zero = C.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, self.USED_MEM_HIGH, C.byref(zero)) == 0
+
+    def used_high(self):
+        v = C.c_uint64(0)
+        assert self.cu.cuMemPoolGetAttribute(self.pool, self.USED_MEM_HIGH, C.byref(v)) == 0
+        return v.value
+
+    def free_bytes(self):
+        free, total = C.c_size_t(), C.c_size_t()
+        assert self.cu.cuMemGetInfo_v2(C.byref(free), C.byref(total)) == 0
+        return free.value
+
+
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
 def test_noalloc_matches_allocating_entry_point_twice(precision):
     torch = pytest.importorskip("torch")
@@ -58,10 +94,33 @@ def test_noalloc_matches_allocating_entry_point_twice(precision):
     model.close()
 
 
+def test_noalloc_allocates_nothing():
+    torch = pytest.importorskip("torch")
+    cfg = baroclinic_config(precision=abi.PREC_FP64)
+    model = Model(cfg)
+    f = inputs(cfg, 13, model.lon_halo_width)
+    _, out, ptrs = on_device(f, torch.float64)
+    model.ffsl_hflx_noalloc(ptrs, 120.0)   # first call on the device: looks up the scratch address
+    pool = DevicePool()
+    # the allocating entry point draws its scratch from the default pool ...
+    pool.reset_high()
+    model.ffsl_hflx(ptrs, 120.0)
+    assert pool.used_high() >= 2 * cfg.nlon * cfg.nlat * cfg.nlev * 8
+    # ... the no-allocation one leaves it and the device's free memory alone
+    torch.cuda.synchronize()
+    pool.reset_high()
+    free0 = pool.free_bytes()
+    for _ in range(2):
+        model.ffsl_hflx_noalloc(ptrs, 120.0)
+    assert pool.used_high() == 0
+    assert pool.free_bytes() == free0
+    model.close()
+
+
 def test_noalloc_refuses_grids_beyond_its_scratch():
     pytest.importorskip("torch")
-    # 360 x 180 x 32 FP64 needs 4 x 2,073,600 x 8 bytes = 66 MB > 32 MiB
-    cfg = baroclinic_config(nlon=360, nlat=180, nlev=32, dt=60.0)
+    # 360 x 180 x 64 FP64 needs 2 x 4,147,200 x 8 bytes = 66 MB > 32 MiB
+    cfg = baroclinic_config(nlon=360, nlat=180, nlev=64, dt=60.0)
     model = Model(cfg)
     fields = {k: 0 for k in ("q", "u", "v", "mfx", "mfy", "cflx", "cfly", "divx", "divy", "qmfx", "qmfy")}
     with pytest.raises(GmcError) as e:
