@@ -65,6 +65,14 @@ def workload_config(precision):
                               max_wave_speed=400.0, ntracer=NTRACER, precision=precision)
 
 
+def workload_keys():
+    """The `config` object of both arms' JSON lines: the workload only (the
+    arithmetic each arm computes in is its `dtype`/`precision`)."""
+    return {"workload": "hydrostatic baroclinic 0.5deg 720x360 L32 (wrf_l32), 4 FFSL tracers, dt=180 s",
+            "time_scheme": "wrfrk3", "max_wave_speed": 400.0, "steps_per_sim_day": 480,
+            "l2": "inputs larger than L2 (state ~1.5 GB mixed, ~3 GB FP64)"}
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -264,47 +272,46 @@ def run_ours(args):
         a[...] = x
         return a
 
-    host = {k: paged(v) for k, v in st.items()}
-    out = {k: g.page_aligned(v.shape) for k, v in host.items() if k != "q"}   # touched: no page faults when timed
-    qout = g.page_aligned(host["q"].shape)
-    e2e_steps = max(2, min(args.steps, 10))
-
-    def e2e_run():
-        nonlocal host, out, qout
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            for name in ("u_lon", "v_lat", "pt", "phs"):
-                model.set_field(name, host[name])
-            for l in range(NTRACER):
-                model.set_tracer(l, host["q"][l])
-            model.step(1)
-            for name in ("u_lon", "v_lat", "pt", "phs"):
-                model.get_field(name, out=out[name])
-            for l in range(NTRACER):
-                model.get_tracer(l, out=qout[l])
-            # the step's result is the next step's input
-            for name in ("u_lon", "v_lat", "pt", "phs"):
-                host[name], out[name] = out[name], host[name]
-            host["q"], qout = qout, host["q"]
-        barrier()
-        return max_over_ranks(time.perf_counter() - t0)
-
-    # pageable host arrays: gathered and converted on host cores into the
-    # library's pinned staging buffer
-    e2e_staged_s = e2e_run()
-    # the same arrays page-locked once (gmc_host_register, outside the timed
-    # region): gathered, scattered and converted by device kernels over the
-    # host link
-    pinned_arrays = list(host.values()) + list(out.values()) + [qout]
-    for a in pinned_arrays:
-        g.host_register(a)
-    try:
-        e2e_s = e2e_run()
-    finally:
+    def e2e_run(m, nsteps, registered):
+        """Wall time of nsteps steps through the public calls with host float64
+        arrays: each step sets u, v, pt, phs and the tracers from the host,
+        steps once and reads them back; the result feeds the next step.
+        registered: the arrays are page-locked once (gmc_host_register, outside
+        the timed region) and gathered/scattered/converted by device kernels
+        over the host link; otherwise they are pageable and staged on host cores
+        through the library's pinned buffer."""
+        host = {k: paged(v) for k, v in st.items()}
+        out = {k: g.page_aligned(v.shape) for k, v in host.items() if k != "q"}   # touched: no page faults when timed
+        qout = g.page_aligned(host["q"].shape)
+        pinned_arrays = list(host.values()) + list(out.values()) + [qout] if registered else []
         for a in pinned_arrays:
-            g.host_unregister(a)
-    h2d = sum(host[k].nbytes for k in ("u_lon", "v_lat", "pt", "phs", "q"))
+            g.host_register(a)
+        try:
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(nsteps):
+                for name in ("u_lon", "v_lat", "pt", "phs"):
+                    m.set_field(name, host[name])
+                for l in range(NTRACER):
+                    m.set_tracer(l, host["q"][l])
+                m.step(1)
+                for name in ("u_lon", "v_lat", "pt", "phs"):
+                    m.get_field(name, out=out[name])
+                for l in range(NTRACER):
+                    m.get_tracer(l, out=qout[l])
+                for name in ("u_lon", "v_lat", "pt", "phs"):
+                    host[name], out[name] = out[name], host[name]
+                host["q"], qout = qout, host["q"]
+            barrier()
+            t = max_over_ranks(time.perf_counter() - t0)
+        finally:
+            for a in pinned_arrays:
+                g.host_unregister(a)
+        return t, sum(host[k].nbytes for k in ("u_lon", "v_lat", "pt", "phs", "q"))
+
+    e2e_steps = max(2, min(args.steps, 10))
+    e2e_staged_s, _ = e2e_run(model, e2e_steps, registered=False)
+    e2e_s, h2d = e2e_run(model, e2e_steps, registered=True)
     e2e_value = DT * e2e_steps / e2e_s * WORLD
     e2e_staged_value = DT * e2e_steps / e2e_staged_s * WORLD
 
@@ -334,6 +341,24 @@ def run_ours(args):
             ncu_bytes += tb * cnt / 3.0
             covered_ms += ms / 3.0
     ncell = cfg.nlon * cfg.nlat * cfg.nlev
+
+    # ---- one simulated day (480 steps) of the mixed form, device-timed ----
+    one_day = None
+    if not args.quick:
+        m1 = g.Model(cfg)
+        m1.set_state(st)
+        m1.prepare()
+        m1.step(args.warmup)
+        clocks_day = ClockSampler(PHYS_GPU)
+        barrier()
+        clocks_day.start()
+        m1.step(480)
+        barrier()
+        clk_day = clocks_day.stop()
+        day_ms = max_over_ranks(m1.stats()["step_ms"])
+        m1.close()
+        one_day = {"steps": 480, "device_s": day_ms / 1000.0, "ms_per_step": day_ms / 480,
+                   "value": DT * 480 / (day_ms / 1000.0) * WORLD, "unit": "sim days/wall-day", "clocks": clk_day}
     model.close()
 
     # ---- FP64 form on the same initial state ----
@@ -351,15 +376,22 @@ def run_ours(args):
         scale = 100.0 if name == "phs" else 1.0   # phs in hPa
         errors[name] = {"rms": float(np.sqrt(np.mean(d * d)) / scale), "max": float(np.max(np.abs(d)) / scale),
                         "unit": "hPa" if name == "phs" else ("K" if name == "pt" else "m/s")}
-    m64.close()
     ps_rms_hpa = errors["phs"]["rms"]
+    # the FP64 form end to end through the same calls (like-for-like with the
+    # FP64 CPU reference arm)
+    e2e64_steps = 5
+    e2e64_s, _ = e2e_run(m64, e2e64_steps, registered=True)
+    e2e64_value = DT * e2e64_steps / e2e64_s * WORLD
+    m64.close()
 
     adj = adjoint_cost() if RANK == 0 else None
     ens = ensemble_throughput() if RANK == 0 else None
 
+    c5 = c5_leg(args) if RANK == 0 and not args.quick else None
+
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, sample_steps=1)
+        cpu = cpu_baseline(args, sample_steps=3, warm=1)
 
     if RANK == 0:
         line = {
@@ -375,13 +407,15 @@ def run_ours(args):
             "vs_baseline": None,
             "dtype": "f32 bulk + f64 (rings, column sweeps, integrals, filter weights)",
             "data": "synthetic (seeded isothermal 300 K + balanced 35 m/s jet + 1 K noise, 4 Gaussian-blob tracers)",
-            "config": {"workload": "hydrostatic baroclinic 0.5deg 720x360 L32 (wrf_l32), 4 FFSL tracers, dt=180 s",
-                       "time_scheme": "wrfrk3", "max_wave_speed": 400.0, "precision": "mixed",
-                       "parallelism": f"replicas x{WORLD}" if WORLD > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (state ~1.5 GB)"},
+            "config": workload_keys(),
+            "precision": "mixed",
+            "parallelism": f"replicas x{WORLD}" if WORLD > 1 else "single GPU",
             "fp64": {"ms_per_step": ms64, "value": DT / (ms64 / 1000.0) * WORLD,
                      "mixed_speedup": ms64 / ms_per_step, "ps_rms_diff_hpa_after_steps": ps_rms_hpa,
-                     "steps_compared": args.warmup + args.steps, "mixed_minus_fp64": errors},
+                     "steps_compared": args.warmup + args.steps, "mixed_minus_fp64": errors,
+                     "e2e": {"value": e2e64_value, "unit": "sim days/wall-day", "steps": e2e64_steps,
+                             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                             "path": "the registered-array path of e2e, FP64 form"}},
             "e2e": {"value": e2e_value, "unit": "sim days/wall-day", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
                     "path": "gmc_set_field/gmc_set_tracer + gmc_step(1) + gmc_get_field/gmc_get_tracer, host float64 "
@@ -412,6 +446,10 @@ def run_ours(args):
             line["ensemble"] = ens
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if one_day is not None:
+            line["one_day"] = one_day
+        if c5 is not None:
+            line["c5"] = c5
         print(json.dumps(line), flush=True)
     ranks.close()
 
@@ -483,16 +521,18 @@ def ensemble_throughput(steps=10, warmup=3):
     return out
 
 
-def cpu_baseline(args, sample_steps=1, warm=0):
+def cpu_baseline(args, sample_steps=3, warm=1):
     """FP64 CPU restatement of the reference (the oracle, OpenMP build) on
-    the same workload, timed on the host cores."""
-    import gmcore_gb300 as g
-    from gmcore_gb300 import abi
+    the same workload, timed on the host cores.  Its initial state comes from
+    the oracle's own build, so this leg loads no library of the product.  The
+    first step after the prologue skips tracer advection (adv_mod.F90:166), so
+    `warm` >= 1 untimed steps put every timed step on the full path."""
+    from gmcore_gb300 import abi   # ctypes structures only
     import oracle as orc_mod
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     cfg = workload_config(abi.PREC_FP64)
-    st = g.make_ic(cfg, 2, SEED, 1.0)
+    st = orc_mod.make_ic(cfg, 2, SEED, 1.0, variant="omp")
     o = orc_mod.Oracle(cfg, variant="omp")
     for name, a in st.items():
         if name == "q":
@@ -508,14 +548,16 @@ def cpu_baseline(args, sample_steps=1, warm=0):
     dt_s = time.perf_counter() - t0
     o.close()
     return {"value": DT * sample_steps / dt_s, "unit": "sim days/wall-day", "cores": int(os.environ["OMP_NUM_THREADS"]),
-            "kind": "port", "sample": f"{sample_steps} step(s) of the same 0.5deg L32 4-tracer workload after the run prologue",
+            "kind": "port",
+            "sample": f"{sample_steps} step(s) of the same 0.5deg L32 4-tracer workload after the run prologue and "
+                      f"{warm} untimed step(s), so every timed step advects the tracers",
             "s_per_step": dt_s / sample_steps}
 
 
 def run_reference(args):
     if RANK != 0:
         return
-    cpu = cpu_baseline(args, sample_steps=args.steps, warm=args.warmup)
+    cpu = cpu_baseline(args, sample_steps=args.steps, warm=max(1, args.warmup))
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -530,20 +572,22 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded isothermal 300 K + balanced 35 m/s jet + 1 K noise, 4 Gaussian-blob tracers)",
-        "config": {"workload": "hydrostatic baroclinic 0.5deg 720x360 L32 (wrf_l32), 4 FFSL tracers, dt=180 s",
-                   "time_scheme": "wrfrk3", "max_wave_speed": 400.0, "precision": "fp64",
-                   "implementation": "FP64 C++ restatement of the reference (the reference's Fortran/MPI build "
-                                     "cannot be compiled here)"},
+        "config": workload_keys(),
+        "precision": "fp64",
+        "implementation": "FP64 C++ restatement of the reference, OpenMP on the host cores (the reference's "
+                          "Fortran/MPI build cannot be compiled here)",
         "cpu_baseline": cpu,
         "e2e": {"value": cpu["value"], "unit": "sim days/wall-day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_c5(args):
+def c5_leg(args, steps=10):
     """The high-resolution case (0.25 degrees 1440x720, 64 levels wrf_l64,
-    8 FFSL tracers, dt = 60 s): mixed form device-timed over --steps steps,
-    the FP64 form over 3 steps, and their differences after those 3 steps."""
+    8 FFSL tracers, dt = 60 s): the mixed form device-timed over `steps` steps
+    after 3 warm-up steps, the FP64 form over 3 steps, and their RMS
+    differences after those 3 steps (the mixed state is read after its warm-up
+    steps)."""
     import gmcore_gb300 as g
     from gmcore_gb300 import abi
 
@@ -552,38 +596,41 @@ def run_c5(args):
                                   vert_coord_template=abi.VCOORD_WRF_L64, time_scheme=abi.TIME_WRFRK3,
                                   max_wave_speed=400.0, ntracer=8, precision=prec)
     st = g.make_ic(cfg_of(abi.PREC_MIXED), 2, SEED, 1.0)
-    res = {}
-    for prec, steps in ((abi.PREC_MIXED, args.steps), (abi.PREC_FP64, 3)):
-        m = g.Model(cfg_of(prec))
-        m.set_state(st)
-        m.prepare()
-        m.step(3 if prec == abi.PREC_MIXED else 0)
-        m.step(steps)
-        ms = m.stats()["step_ms"] / steps
-        if prec == abi.PREC_MIXED:   # state after 3 steps for the comparison
-            m2 = g.Model(cfg_of(prec))
-            m2.set_state(st)
-            m2.prepare()
-            m2.step(3)
-            state = {f: m2.get_field(f) for f in ("phs", "u_lon", "pt")}
-            m2.close()
-        else:
-            state = {f: m.get_field(f) for f in ("phs", "u_lon", "pt")}
-        m.close()
-        res[prec] = (ms, state)
-    ms_m, s_m = res[abi.PREC_MIXED]
-    ms_d, s_d = res[abi.PREC_FP64]
-    n = 1440 * 720 * 64
-    line = {"metric": "sim days/wall-day at 0.25°L64, 8 tracers: mixed vs FP64 GPU", "value": 60.0 / (ms_m / 1000.0),
-            "unit": "sim days/wall-day", "n_gpus": 1, "steps": args.steps, "ms_per_step": ms_m, "higher_is_better": True,
-            "dtype": "f32 bulk + f64 (rings, surface pressure, integrals)", "data": "synthetic (seeded)",
-            "config": {"workload": "hydrostatic baroclinic 0.25deg 1440x720 L64 (wrf_l64), 8 FFSL tracers, dt=60 s",
-                       "time_scheme": "wrfrk3", "max_wave_speed": 400.0},
-            "fp64": {"ms_per_step": ms_d, "mixed_speedup": ms_d / ms_m,
-                     "mixed_minus_fp64_after_3_steps": {f: float(np.sqrt(np.mean((s_m[f] - s_d[f]) ** 2))) for f in s_m}},
+    fields = ("phs", "u_lon", "pt")
+    m = g.Model(cfg_of(abi.PREC_MIXED))
+    m.set_state(st)
+    m.prepare()
+    m.step(3)
+    s_m = {f: m.get_field(f) for f in fields}
+    m.step(steps)
+    ms_m = m.stats()["step_ms"] / steps
+    m.close()
+    m = g.Model(cfg_of(abi.PREC_FP64))
+    m.set_state(st)
+    m.prepare()
+    m.step(3)
+    ms_d = m.stats()["step_ms"] / 3
+    s_d = {f: m.get_field(f) for f in fields}
+    m.close()
+    n, h = 1440 * 720 * 64, 1440 * 720
+    b_step = n * 4 * (48 + 2 * 8 + 10) + 18 * h * 8
+    return {"workload": "hydrostatic baroclinic 0.25deg 1440x720 L64 (wrf_l64), 8 FFSL tracers, dt=60 s, wrfrk3, "
+                        "max_wave_speed 400",
+            "value": 60.0 / (ms_m / 1000.0), "unit": "sim days/wall-day", "steps": steps, "ms_per_step": ms_m,
             "cell_updates_per_s": n / (ms_m / 1000.0),
-            "step_roofline": {"compulsory_bytes_per_step": n * 4 * (48 + 2 * 8 + 10) + 18 * 1440 * 720 * 8}}
-    line["step_roofline"]["frac"] = line["step_roofline"]["compulsory_bytes_per_step"] / (ms_m / 1000.0) / 1e9 / measured_peaks()[0]
+            "fp64": {"ms_per_step": ms_d, "value": 60.0 / (ms_d / 1000.0), "mixed_speedup": ms_d / ms_m},
+            "mixed_minus_fp64_rms_after_3_steps": {f: float(np.sqrt(np.mean((s_m[f] - s_d[f]) ** 2))) for f in fields},
+            "step_roofline": {"compulsory_bytes_per_step": b_step,
+                              "frac": b_step / (ms_m / 1000.0) / 1e9 / measured_peaks()[0]}}
+
+
+def run_c5(args):
+    """The high-resolution case alone, as its own JSON line."""
+    c5 = c5_leg(args, steps=args.steps)
+    line = {"metric": "sim days/wall-day at 0.25°L64, 8 tracers: mixed vs FP64 GPU", "value": c5["value"],
+            "unit": "sim days/wall-day", "n_gpus": 1, "steps": args.steps, "ms_per_step": c5["ms_per_step"],
+            "higher_is_better": True, "dtype": "f32 bulk + f64 (rings, surface pressure, integrals)",
+            "data": "synthetic (seeded)", "config": {"workload": c5["workload"]}, "c5": c5}
     print(json.dumps(line), flush=True)
 
 
@@ -598,6 +645,8 @@ def main():
                     help="time only the device-resident mixed step (the case profiled under ncu)")
     ap.add_argument("--workload", choices=("c2", "c5"), default="c2",
                     help="c2: 0.5deg L32 4 tracers (headline); c5: 0.25deg L64 8 tracers")
+    ap.add_argument("--quick", action="store_true",
+                    help="leave out the one-day and 0.25deg legs (extra keys of the headline line)")
     args = ap.parse_args()
     if args.workload == "c5":
         run_c5(args)

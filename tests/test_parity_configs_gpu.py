@@ -1,0 +1,145 @@
+"""GPU FP64 form against the FP64 oracle on the benchmark configurations
+themselves, at their full sizes, on the same seeded initial states.
+
+  1 degree shallow water (360 x 180, predict-correct, dt = 60 s): 100 steps,
+      <= 1e-12 after one step and <= 1e-9 after 100.
+  0.5 degree L32 baroclinic core with 4 FFSL tracers (720 x 360 x 32, WRF-RK3,
+      dt = 180 s, max_wave_speed 400): <= 1e-12 after one step and <= 1e-10
+      after four, tracers included (tracer advection starts at the second
+      step); the mixed form against the same oracle run within the mixed
+      form's stated tolerances.
+  The ensemble grids, L26: one member at 2 degrees (180 x 90, dt = 600 s) for
+      100 steps and one at 1 degree (360 x 180, dt = 300 s) for 3, each run
+      inside a 2-member context whose other member has different noise.
+
+Errors are max-norm relative to the oracle field's maximum.  The oracle runs
+its OpenMP build (bit-identical to the parity build) so that the full-size
+cases take seconds per step on the host cores.
+"""
+import numpy as np
+import pytest
+
+from gmcore_gb300 import Model, abi, make_ic
+from oracle import Oracle
+
+from helpers import BC_FIELDS, SWM_FIELDS, compare, initial_state, load_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+SEED = 20240601
+
+
+def oracle_of(cfg, st):
+    o = Oracle(cfg, variant="omp")
+    load_state(o, st)
+    o.prepare()
+    return o
+
+
+def model_of(cfg, st):
+    m = Model(cfg)
+    load_state(m, st)
+    m.prepare()
+    return m
+
+
+def test_c1_shallow_water_100_steps():
+    cfg = abi.default_config(nlon=360, nlat=180, nlev=1, baroclinic=0, dt_dyn=60.0, time_scheme=abi.TIME_PC2)
+    st = initial_state(cfg, SEED, 0.0)
+    orc, gpu = oracle_of(cfg, st), model_of(cfg, st)
+    orc.step(1)
+    gpu.step(1)
+    e1 = compare(gpu, orc, SWM_FIELDS)
+    orc.step(99)
+    gpu.step(99)
+    e100 = compare(gpu, orc, SWM_FIELDS)
+    print("C1 after 1 step", e1, "after 100", e100)
+    assert max(e1.values()) <= 1e-12, e1
+    assert max(e100.values()) <= 1e-9, e100
+    # diagnose's total mass and energy after the 100 steps
+    dg, do = gpu.diagnose(), orc.diagnose()
+    for k in ("tm", "te"):
+        assert abs(dg[k] - do[k]) <= 1e-11 * abs(do[k]), (k, dg[k], do[k])
+    gpu.close()
+    orc.close()
+
+
+def c2_config(precision):
+    return abi.default_config(nlon=720, nlat=360, nlev=32, baroclinic=1, dt_dyn=180.0,
+                              vert_coord_template=abi.VCOORD_WRF_L32, time_scheme=abi.TIME_WRFRK3,
+                              max_wave_speed=400.0, ntracer=4, precision=precision)
+
+
+@pytest.fixture(scope="module")
+def c2_oracle_run():
+    """The oracle's C2 state after 1 and after 4 steps (fields and tracers)."""
+    cfg = c2_config(abi.PREC_FP64)
+    st = make_ic(cfg, 2, SEED, 1.0)
+    orc = oracle_of(cfg, st)
+    out = {}
+    for n, tag in ((1, 1), (3, 4)):
+        orc.step(n)
+        out[tag] = ({f: orc.get_field(f) for f in BC_FIELDS}, [orc.get_tracer(l) for l in range(4)])
+    orc.close()
+    return st, out
+
+
+def test_c2_full_size_fp64(c2_oracle_run):
+    st, ref = c2_oracle_run
+    gpu = model_of(c2_config(abi.PREC_FP64), st)
+    errs = {}
+    for n, tag in ((1, 1), (3, 4)):
+        gpu.step(n)
+        fields, tracers = ref[tag]
+        e = {f: rel_err(gpu.get_field(f), fields[f]) for f in BC_FIELDS}
+        e["q"] = max(rel_err(gpu.get_tracer(l), tracers[l]) for l in range(4))
+        errs[tag] = e
+    gpu.close()
+    print("C2 FP64 vs oracle after 1 step", errs[1], "after 4", errs[4])
+    assert max(errs[1].values()) <= 1e-12, errs[1]
+    assert max(errs[4].values()) <= 1e-10, errs[4]
+
+
+def test_c2_full_size_mixed_within_stated_error(c2_oracle_run):
+    st, ref = c2_oracle_run
+    gpu = model_of(c2_config(abi.PREC_MIXED), st)
+    gpu.step(4)
+    fields, tracers = ref[4]
+    e = {f: rel_err(gpu.get_field(f), fields[f]) for f in BC_FIELDS}
+    d = gpu.get_field("phs") - fields["phs"]
+    ps_rms_hpa = float(np.sqrt(np.mean(d * d))) / 100.0
+    e_q = max(rel_err(gpu.get_tracer(l), tracers[l]) for l in range(4))
+    gpu.close()
+    print("C2 mixed vs oracle after 4 steps", e, "q", e_q, "ps rms hPa", ps_rms_hpa)
+    assert e["phs"] <= 1e-6 and e["pt"] <= 1e-5, e
+    assert max(e.values()) <= 5e-3, e
+    assert e_q <= 1e-3, e_q
+    assert ps_rms_hpa <= 0.05
+
+
+def ensemble_config(nlon, nlat, dt, members):
+    return abi.default_config(nlon=nlon, nlat=nlat, nlev=26, baroclinic=1, dt_dyn=dt,
+                              vert_coord_template=abi.VCOORD_TEST_L26, time_scheme=abi.TIME_WRFRK3,
+                              max_wave_speed=400.0, n_members=members)
+
+
+@pytest.mark.parametrize("nlon,nlat,dt,nsteps", [(180, 90, 600.0, 100), (360, 180, 300.0, 3)])
+def test_ensemble_member_against_oracle(nlon, nlat, dt, nsteps):
+    one = ensemble_config(nlon, nlat, dt, 1)
+    states = [make_ic(one, 2, SEED + m, 0.1) for m in range(2)]
+    gpu = Model(ensemble_config(nlon, nlat, dt, 2))
+    for m, st in enumerate(states):
+        for name, a in st.items():
+            gpu.set_field(name, a, member=m)
+    gpu.prepare()
+    gpu.step(nsteps)
+    worst = 0.0
+    for m in range(2):
+        orc = oracle_of(one, states[m])
+        orc.step(nsteps)
+        e = {f: rel_err(gpu.get_field(f, member=m), orc.get_field(f)) for f in BC_FIELDS}
+        orc.close()
+        print(f"ensemble {nlon}x{nlat} member {m} after {nsteps} steps", e)
+        worst = max(worst, max(e.values()))
+    gpu.close()
+    assert worst <= (1e-9 if nsteps >= 100 else 1e-11), worst
