@@ -30,6 +30,7 @@ EXPORTED = (
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
     "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs", "gmc_host_register", "gmc_host_unregister",
+    "gmc_fp64_fma_peak", "gmc_set_member_layout",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -84,8 +85,19 @@ def load(build_if_missing=True):
     lib.gmc_kernel_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double), P(C.c_int64)]
     lib.gmc_host_register.argtypes = [C.c_void_p, C.c_size_t]
     lib.gmc_host_unregister.argtypes = [C.c_void_p]
+    lib.gmc_fp64_fma_peak.argtypes = [P(C.c_double)]
+    lib.gmc_set_member_layout.argtypes = [C.c_void_p, C.c_int32]
     _lib = lib
     return lib
+
+
+def fp64_fma_peak():
+    """Measured FP64 FMA throughput of the current GPU in TFLOP/s."""
+    out = C.c_double()
+    rc = load().gmc_fp64_fma_peak(C.byref(out))
+    if rc != 0:
+        raise GmcError(rc, "gmc_fp64_fma_peak")
+    return out.value
 
 
 def page_aligned(shape):
@@ -328,7 +340,13 @@ class Model:
         the last step() call."""
         st = Stats()
         self._check(self.lib.gmc_get_stats(self.h, C.byref(st)))
-        return {"step_ms": st.step_ms, "steps": st.steps, "kernel_launches": st.kernel_launches}
+        return {"step_ms": st.step_ms, "steps": st.steps, "kernel_launches": st.kernel_launches,
+                "member_layout": st.member_layout, "layout_tuned": bool(st.layout_tuned)}
+
+    def set_member_layout(self, layout):
+        """Ensemble launch layout: -1 autotune (default), 0 per-member streams,
+        G > 0 member-batched launches in G groups."""
+        self._check(self.lib.gmc_set_member_layout(self.h, layout))
 
     def set_profiling(self, on):
         self._check(self.lib.gmc_set_profiling(self.h, 1 if on else 0))

@@ -71,7 +71,8 @@ class Diag(C.Structure):
 
 
 class Stats(C.Structure):
-    _fields_ = [("step_ms", C.c_double), ("steps", C.c_int64), ("kernel_launches", C.c_int64)]
+    _fields_ = [("step_ms", C.c_double), ("steps", C.c_int64), ("kernel_launches", C.c_int64),
+                ("member_layout", C.c_int32), ("layout_tuned", C.c_int32)]
 
 
 class FfslFields(C.Structure):

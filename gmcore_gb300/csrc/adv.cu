@@ -24,121 +24,128 @@ namespace {
 //   u, v  : advecting velocities (or mass fluxes for the outer operator)
 //   mx    : field reconstructed along x;  my : field reconstructed along y.
 // Along x a block takes one full row: the row is staged in shared memory
-// (one barrier) and each face forms the PPM slope and limited coefficients
-// of its upwind cell from the five cells around it.  Along y a block takes a
-// strip of kHflxRows half rows: each thread loads its column of the strip
-// (plus the stencil's rows) into registers and forms each slope once.  Pole
-// halo rows are read as the reference's fill_halo leaves them (mirrored row
-// shifted by nlon/2).
-constexpr int kHflxRows = 4;
+// with wrapped ends, each cell's slope formed once, and each face forms the
+// limited coefficients of its upwind cell.  Along y each thread marches one
+// column north through a band of rows with a rolling window in registers
+// (YMarch).  Pole halo rows are read as the reference's fill_halo leaves them
+// (mirrored row shifted by nlon/2).
 
 // x fluxes of full row j (2 .. nlat-1) at level k of NF fields that share the
 // Courant numbers cflx: field f is fld[f] advected by the multiplier mul[f]
-// (a velocity or a mass flux); out(i, o, flux[NF]) per face.  xs: NF * nlon
-// values of shared memory.  The upwind cell, the whole-cell count and the
-// fractional Courant number are formed once per face for all fields.
+// (a velocity or a mass flux); out(i0, o, flux[NF]) per face i0 (0-based; the
+// face east of cell i0) at 32-bit offset o.  Shared memory: xs holds the NF
+// rows with wrapped cells beyond both ends, X_f[l] = xs[f * (nlon + 5) + 2 + l]
+// for l = -2 .. nlon+2, and ss their limited slopes, S_f[l] = ss[f * (nlon + 3)
+// + 1 + l] for l = -1 .. nlon+1, so no face indexes modulo nlon.  Each cell's
+// slope (slope_mono, ffsl_mod.F90:1183-1194) is formed once and read by the
+// faces whose upwind cell or neighbour it is; the upwind cell, the whole-cell
+// count and the fractional Courant number are formed once per face for all
+// fields.  Row offsets are 32-bit (grids are validated to < 2^31 cells).
 template <int NF, class R, class Out>
 __device__ __forceinline__ void hflx_xrows(const DGrid &g, int j, int k, const R *const (&mul)[NF],
-                                           const R *__restrict__ cflx, const R *const (&fld)[NF], R *xs, Out out) {
-  const int nlat = g.nlat, nlon = g.nlon, lim = g.limiter;
-  auto W = [nlon](int l) { return l < 0 ? l + nlon : (l >= nlon ? l - nlon : l); };   // one wrap, 0-based
+                                           const R *__restrict__ cflx, const R *const (&fld)[NF], R *xs, R *ss,
+                                           Out out) {
+  const int nlon = g.nlon, lim = g.limiter, xw = nlon + 5, sw = nlon + 3;
   auto Wg = [nlon](int l) {   // any l (a Courant number may exceed nlon on coarse grids)
     if (l >= 0 && l < nlon) return l;
     l %= nlon;
     return l < 0 ? l + nlon : l;
   };
+  const unsigned ro = (unsigned)ix3(g.nlat, nlon, 1, j, k);
   // face inputs of this thread's first faces are requested before the rows
   // are staged so that their latency overlaps it
   constexpr int kPre = 3;
   R cpre[kPre], mpre[NF][kPre];
 #pragma unroll
   for (int t = 0; t < kPre; ++t) {
-    const int i = 1 + threadIdx.x + t * blockDim.x;
-    if (i <= nlon) {
-      const size_t o = ix3(nlat, nlon, i, j, k);
-      cpre[t] = cflx[o];
+    const int i0 = threadIdx.x + t * blockDim.x;
+    if (i0 < nlon) {
+      cpre[t] = cflx[ro + i0];
 #pragma unroll
-      for (int f = 0; f < NF; ++f) mpre[f][t] = mul[f][o];
+      for (int f = 0; f < NF; ++f) mpre[f][t] = mul[f][ro + i0];
     }
   }
-  const size_t ro = ix3(nlat, nlon, 1, j, k);
   __syncthreads();   // xs may still be read by a previous use
 #pragma unroll
-  for (int f = 0; f < NF; ++f)
-    for (int l = threadIdx.x; l < nlon; l += blockDim.x) xs[f * nlon + l] = fld[f][ro + l];
+  for (int f = 0; f < NF; ++f) {
+    R *X = xs + f * xw + 2;
+    for (int l = threadIdx.x; l < nlon; l += blockDim.x) X[l] = fld[f][ro + l];
+    if (threadIdx.x < 5) {   // wrapped cells -2, -1 and nlon .. nlon+2
+      const int l = threadIdx.x < 2 ? (int)threadIdx.x - 2 : nlon + (int)threadIdx.x - 2;
+      X[l] = fld[f][ro + (threadIdx.x < 2 ? l + nlon : l - nlon)];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const R *X = xs + f * xw + 2;
+    R *S = ss + f * sw + 1;
+    for (int l = (int)threadIdx.x - 1; l <= nlon + 1; l += blockDim.x) S[l] = slope(lim, X[l - 1], X[l], X[l + 1]);
+  }
   __syncthreads();
   const bool vl = g.flux_type == GMC_FLUX_VAN_LEER;
-  // PPM coefficients of cell l (0-based) of row x from cells l-2 .. l+2; the
-  // same operations as ppm() on the slopes of cells l-1, l, l+1
-  auto coef = [&](const R *x, int l, R &fl, R &df, R &f6) {
-    const R a = x[W(l - 2)], b = x[W(l - 1)], c = x[l], d = x[W(l + 1)], e = x[W(l + 2)];
-    const R sm = slope(lim, a, b, c), s0 = slope(lim, b, c, d), sp = slope(lim, c, d, e);
-    ppm_cell(c, s0, ppm_edge(b, c, sm, s0), ppm_edge(c, d, s0, sp), fl, df, f6);
-  };
   const R hxr = (R)g.hx;
-  int t = 0;
-  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x, ++t) {
-    const size_t o = ro + (i - 1);
-    R c, mo[NF];
-    if (t < kPre) {
-#pragma unroll
-      for (int q = 0; q < kPre; ++q)
-        if (q == t) {
-          c = cpre[q];
-#pragma unroll
-          for (int f = 0; f < NF; ++f) mo[f] = mpre[f][q];
-        }
-    } else {
-      c = cflx[o];
-#pragma unroll
-      for (int f = 0; f < NF; ++f) mo[f] = mul[f][o];
-    }
+  // the flux through face i0 (between cells i0 and i0 + 1, 0-based) with
+  // Courant number c and multipliers mo
+  auto face = [&](int i0, R c, const R (&mo)[NF]) {
     R flux[NF];
     if (fabs(c) > hxr) {   // |cflx| beyond the reach the reference allows: error, no flux (NaN: no flux below)
       raise_err(g, ERR_CFLX);
 #pragma unroll
       for (int f = 0; f < NF; ++f) flux[f] = 0;
     } else {
+      // c > 0: upwind cell i - ci (1-based face i = i0 + 1), whole cells
+      // i+1-ci .. i, parabola over [1 - cf, 1]; c < 0: upwind cell i + 1 - ci,
+      // whole cells i+1 .. i-ci, parabola over [0, -cf] and the flux's sign
+      // reversed (hflx_ppm_cell, ffsl_mod.F90:833-875).  Both directions run
+      // the same instructions, so a warp whose faces differ in sign does not
+      // diverge; |c| < 1 needs no whole cells and no modulo.
       const int ci = (int)c;
       const R cf = c - (R)ci;
-      if (c > 0) {
-        const int iu = Wg(i - ci - 1);   // 0-based upwind cell
+      const bool pos = c > 0;
+      const int i = i0 + 1;
+      const int iu = ci == 0 ? (pos ? i0 : i0 + 1) : Wg(pos ? i - ci - 1 : i - ci);   // 0-based upwind cell, 0 .. nlon
+      const R s1 = pos ? (R)1 - cf : (R)0, s2 = pos ? (R)1 : -cf;
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          const R *x = xs + f * nlon;
-          R sum = 0;
-          for (int l = i + 1 - ci; l <= i; ++l) sum = sum + x[Wg(l - 1)];
-          if (vl) {   // hflx_van_leer_cell (ffsl_mod.F90:585-590)
-            const R su = slope(lim, x[W(iu - 1)], x[iu], x[W(iu + 1)]);
-            flux[f] = fdiv(mo[f] * (cf * (x[iu] + su * (R)0.5 * ((R)1 - cf)) + sum), c);
-          } else {
-            R fl, df, f6;
-            coef(x, iu, fl, df, f6);
-            flux[f] = fdiv(mo[f] * ppm_tail(sum, fl, df, f6, (R)1 - cf, (R)1), c);
-          }
+      for (int f = 0; f < NF; ++f) {
+        const R *X = xs + f * xw + 2, *S = ss + f * sw + 1;
+        R sum = 0;
+        if (ci != 0) {
+          const int l0 = pos ? i + 1 - ci : i + 1, l1 = pos ? i : i - ci;
+          for (int l = l0; l <= l1; ++l) sum = sum + X[Wg(l - 1)];
         }
-      } else if (c < 0) {
-        const int iu = Wg(i - ci);       // 0-based upwind cell (i - ci + 1 in 1-based)
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          const R *x = xs + f * nlon;
-          R sum = 0;
-          for (int l = i + 1; l <= i - ci; ++l) sum = sum + x[Wg(l - 1)];
-          if (vl) {   // (ffsl_mod.F90:591-594)
-            const R su = slope(lim, x[W(iu - 1)], x[iu], x[W(iu + 1)]);
-            flux[f] = fdiv(mo[f] * (cf * (x[iu] - su * (R)0.5 * ((R)1 + cf)) - sum), c);
-          } else {
-            R fl, df, f6;
-            coef(x, iu, fl, df, f6);
-            flux[f] = fdiv(-mo[f] * ppm_tail(sum, fl, df, f6, (R)0, -cf), c);
-          }
+        R num;
+        if (vl) {   // hflx_van_leer_cell (ffsl_mod.F90:585-594)
+          const R su = S[iu];
+          num = mo[f] * (pos ? cf * (X[iu] + su * (R)0.5 * ((R)1 - cf)) + sum
+                             : cf * (X[iu] - su * (R)0.5 * ((R)1 + cf)) - sum);
+        } else {
+          // PPM coefficients of the upwind cell: ppm() on the slopes of cells iu-1, iu, iu+1
+          const R b = X[iu - 1], cc = X[iu], d = X[iu + 1], sm = S[iu - 1], s0 = S[iu], sp = S[iu + 1];
+          R fl, df, f6;
+          ppm_cell(cc, s0, ppm_edge(b, cc, sm, s0), ppm_edge(cc, d, s0, sp), fl, df, f6);
+          num = (pos ? mo[f] : -mo[f]) * ppm_tail(sum, fl, df, f6, s1, s2);
         }
-      } else {
-#pragma unroll
-        for (int f = 0; f < NF; ++f) flux[f] = 0;
+        flux[f] = c != 0 ? fdiv(num, c) : (R)0;
       }
     }
-    out(i, o, flux);
+    out(i0, ro + i0, flux);
+  };
+#pragma unroll
+  for (int t = 0; t < kPre; ++t) {
+    const int i0 = threadIdx.x + t * blockDim.x;
+    if (i0 < nlon) {
+      R mo[NF];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) mo[f] = mpre[f][t];
+      face(i0, cpre[t], mo);
+    }
+  }
+  for (int i0 = threadIdx.x + kPre * blockDim.x; i0 < nlon; i0 += blockDim.x) {
+    R mo[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) mo[f] = mul[f][ro + i0];
+    face(i0, cflx[ro + i0], mo);
   }
 }
 
@@ -154,71 +161,116 @@ __device__ __forceinline__ const R *halo_row(const DGrid &g, const R *f, int jj,
   return f + ix3(g.nlat, g.nlon, 1, jj, k);
 }
 
-// y flux through half row j with the column window y[t-1 .. t+2] = Y(j-1 .. j+2)
-// and slopes sl[t-1 .. t+2] at those rows.
+// y flux through half row f (between full rows f and f+1) from the values
+// y(f), y(f+1), limited slopes s(f), s(f+1) and PPM edge values e(f), e(f+1),
+// e(f+2) (e(r) = ppm_edge(y(r-1), y(r), s(r-1), s(r)), shared by the faces on
+// both sides of a row) (hflx_ppm_cell along y, ffsl_mod.F90:841-875).  c > 0
+// takes upwind row f, c < 0 row f + 1; both run the same instructions
+// (selects), so a warp with faces of both signs does not diverge.
 template <class R>
-__device__ __forceinline__ R hflx_yface(const DGrid &g, R c, R vv, const R *y, const R *sl, int t) {
-  if (fabs(c) > (R)1) {   // a NaN Courant number falls through to a zero flux
+__device__ __forceinline__ R yface(const DGrid &g, R c, R vv, R y0, R y1, R s0, R s1, R e0, R e1, R e2) {
+  if (fabs(c) > (R)1) {   // a NaN Courant number falls through to a NaN flux
     raise_err(g, ERR_CFLY);
     return 0;
   }
+  const bool pos = c > 0;
   if (g.flux_type == GMC_FLUX_VAN_LEER) {   // hflx_van_leer_cell (ffsl_mod.F90:603-610)
-    const R yu = c > 0 ? y[t] : y[t + 1], su = c > 0 ? sl[t] : sl[t + 1];   // upwind cell j (c > 0) or j + 1
+    const R yu = pos ? y0 : y1, su = pos ? s0 : s1;   // upwind cell f (c > 0) or f + 1
     return vv * (yu + su * (R)0.5 * (fsign((R)1, c) - c));
   }
+  const R yc = pos ? y0 : y1, sc = pos ? s0 : s1;
+  const R el = pos ? e0 : e1, er = pos ? e1 : e2;
   R fl, df, f6;
-  if (c > 0) {   // upwind cell j
-    ppm_cell(y[t], sl[t], ppm_edge(y[t - 1], y[t], sl[t - 1], sl[t]), ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]), fl, df,
-             f6);
-    return fdiv(vv * ppm_tail((R)0, fl, df, f6, (R)1 - c, (R)1), c);
-  }
-  if (c < 0) {   // upwind cell j + 1
-    ppm_cell(y[t + 1], sl[t + 1], ppm_edge(y[t], y[t + 1], sl[t], sl[t + 1]),
-             ppm_edge(y[t + 1], y[t + 2], sl[t + 1], sl[t + 2]), fl, df, f6);
-    return fdiv(-vv * ppm_tail((R)0, fl, df, f6, (R)0, -c), c);
-  }
-  return 0;
+  ppm_cell(yc, sc, el, er, fl, df, f6);
+  const R num = (pos ? vv : -vv) * ppm_tail((R)0, fl, df, f6, pos ? (R)1 - c : (R)0, pos ? (R)1 : -c);
+  return c != 0 ? fdiv(num, c) : (R)0;
 }
 
-// Outer pass: fluxes fy of qx along y with the meridional mass flux (strips).
+// One column (0-based longitude i, level k) of a full-latitude field marching
+// north one half row at a time, for the y passes.  At face f it holds the
+// rows y(f-1 .. f+3), the limited slopes s(f-1 .. f+2) and the edge values
+// e(f .. f+2); each advance reads one new row and forms one slope and one
+// edge, so every row's slope and edges are formed once.  Rows beyond the
+// poles are read as the reference's fill_halo leaves them.
 template <class R>
-__global__ void GMC_BOUNDS(R, 6) k_hflx_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ my,
-                         R *__restrict__ fy) {
-  const int k = blockIdx.y + 1;
-  const int nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
-  const int j0 = blockIdx.x * kHflxRows + 1;
-  if (j0 > nhalf) return;
-  constexpr int NV = kHflxRows + 5;   // rows j0-2 .. j0+kHflxRows+2
-  const int nf = min(kHflxRows, nhalf - j0 + 1);
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-    R y[NV], sl[NV];
-#pragma unroll
-    for (int t = 0; t < NV; ++t) {
-      if (t < nf + 5) {
-        int sh;
-        const R *p = halo_row(g, my, j0 - 2 + t, k, sh);
-        int l = i + sh;
-        y[t] = p[l >= nlon ? l - nlon : l];
-      } else {
-        y[t] = 0;
-      }
+struct YMarch {
+  const DGrid &g;
+  const R *fld;
+  int k, i, f;
+  R y0, y1, y2, y3, y4;   // y(f-1) .. y(f+3)
+  R s0, s1, s2, s3;       // s(f-1) .. s(f+2)
+  R e0, e1, e2;           // e(f) .. e(f+2)
+  R p0, p1;               // rows f+4, f+5, requested ahead of their use (rows
+                          // past the field's end read valid halo rows, unused)
+  __device__ __forceinline__ R row(int jj) const {
+    int sh;
+    const R *p = halo_row(g, fld, jj, k, sh);
+    const int l = i + sh;
+    return p[l >= g.nlon ? l - g.nlon : l];
+  }
+  __device__ __forceinline__ YMarch(const DGrid &g_, const R *fld_, int k_, int i_, int f0)
+      : g(g_), fld(fld_), k(k_), i(i_), f(f0) {
+    const int lim = g.limiter;
+    const R ym = row(f0 - 2);
+    y0 = row(f0 - 1); y1 = row(f0); y2 = row(f0 + 1); y3 = row(f0 + 2); y4 = row(f0 + 3);
+    p0 = row(f0 + 4);
+    p1 = row(f0 + 5);
+    s0 = slope(lim, ym, y0, y1);
+    s1 = slope(lim, y0, y1, y2);
+    s2 = slope(lim, y1, y2, y3);
+    s3 = slope(lim, y2, y3, y4);
+    e0 = ppm_edge(y0, y1, s0, s1);
+    e1 = ppm_edge(y1, y2, s1, s2);
+    e2 = ppm_edge(y2, y3, s2, s3);
+  }
+  __device__ __forceinline__ R flux(R c, R vv) const { return yface(g, c, vv, y1, y2, s1, s2, e0, e1, e2); }
+  // f -> f + 1
+  __device__ __forceinline__ void advance() {
+    const R y5 = p0;
+    p0 = p1;
+    p1 = row(f + 6);
+    const R s4 = slope(g.limiter, y3, y4, y5);   // s(f+3)
+    const R e3 = ppm_edge(y3, y4, s3, s4);        // e(f+3)
+    y0 = y1; y1 = y2; y2 = y3; y3 = y4; y4 = y5;
+    s0 = s1; s1 = s2; s2 = s3; s3 = s4;
+    e0 = e1; e1 = e2; e2 = e3;
+    ++f;
+  }
+};
+
+// Rows (or half rows) per band of the y passes: each thread marches one
+// column through a band.
+constexpr int kYBand = 20;
+constexpr int kYThreads = 128;
+
+// Outer pass: fluxes fy of qx along y with the meridional mass flux, one
+// column per thread marching north through a band of half rows.
+template <class R, bool MB>
+__global__ void __launch_bounds__(kYThreads) k_hflx_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly,
+                                                      const R *__restrict__ my, R *__restrict__ fy) {
+  if constexpr (MB) {   // grid z = member x level
+    const size_t mo = (size_t)(blockIdx.z / g.nlev) * g.mstride;
+    v = mshift(v, mo); cfly = mshift(cfly, mo); my = mshift(my, mo); fy = mshift(fy, mo);
+  }
+  const int k = blockIdx.z % g.nlev + 1;
+  const int nhalf = g.nhalf, nlon = g.nlon;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int fb = blockIdx.y * kYBand + 1, fe = min(nhalf, fb + kYBand - 1);
+  if (i >= nlon || fb > nhalf) return;
+  YMarch<R> ym(g, my, k, i, fb);
+  unsigned o = (unsigned)ix3(nhalf, nlon, i + 1, fb, k);
+  R c = cfly[o], vv = v[o];
+  for (int f = fb;; ++f, o += nlon) {
+    R cn = 0, vn = 0;
+    if (f < fe) {   // the next face's inputs, requested before this face's arithmetic
+      cn = cfly[o + nlon];
+      vn = v[o + nlon];
     }
-    R cy[kHflxRows], vy[kHflxRows];
-#pragma unroll
-    for (int f = 0; f < kHflxRows; ++f) {
-      if (f < nf) {
-        const size_t o = ix3(nhalf, nlon, i + 1, j0 + f, k);
-        cy[f] = cfly[o];
-        vy[f] = v[o];
-      }
-    }
-#pragma unroll
-    for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
-#pragma unroll
-    for (int f = 0; f < kHflxRows; ++f) {
-      if (f >= nf) break;
-      fy[ix3(nhalf, nlon, i + 1, j0 + f, k)] = hflx_yface(g, cy[f], vy[f], y, sl, f + 2);
-    }
+    fy[o] = ym.flux(c, vv);
+    if (f == fe) break;
+    ym.advance();
+    c = cn;
+    vv = vn;
   }
 }
 
@@ -229,11 +281,12 @@ __global__ void GMC_BOUNDS(R, 6) k_hflx_y(DGrid g, const R *__restrict__ v, cons
 // x: one full row per block, together with the outer x pass (fluxes fx of qy
 // with the zonal mass flux), which shares the Courant numbers; qy comes from
 // the y inner pass launched before.
-template <class R>
+template <class R, bool MB>
 __global__ void GMC_BOUNDS(R, 6) k_ffsl_x2(DGrid g, const R *__restrict__ u, const R *__restrict__ mfx,
                                            const R *__restrict__ cflx, const R *__restrict__ q,
                                            const R *__restrict__ qy, const R *__restrict__ divx, R *__restrict__ qx,
-                                           R *__restrict__ fx, double dt) {
+                                           R *__restrict__ fx, R dt) {
+  if constexpr (MB) { const size_t mo = member_offset(g); u = mshift(u, mo); mfx = mshift(mfx, mo); cflx = mshift(cflx, mo); q = mshift(q, mo); qy = mshift(qy, mo); divx = mshift(divx, mo); qx = mshift(qx, mo); fx = mshift(fx, mo); }
   extern __shared__ double sh_raw[];
   const int k = blockIdx.y + 1, j = blockIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon;
@@ -245,108 +298,68 @@ __global__ void GMC_BOUNDS(R, 6) k_ffsl_x2(DGrid g, const R *__restrict__ u, con
     }
     return;
   }
-  R *xs = reinterpret_cast<R *>(sh_raw);   // [2][nlon]: q, qy
-  R *frow = xs + 2 * nlon;
+  R *xs = reinterpret_cast<R *>(sh_raw);   // [2][nlon + 5]: q, qy with wrapped ends
+  R *ss = xs + 2 * (nlon + 5);             // [2][nlon + 3]: their limited slopes
+  R *fr = ss + 2 * (nlon + 3) + 1;         // inner fluxes of q, fr[-1 .. nlon-1]
   const R *mul[2] = {u, mfx};
   const R *fld[2] = {q, qy};
-  hflx_xrows<2, R>(g, j, k, mul, cflx, fld, xs, [&](int i, size_t o, const R (&f)[2]) {
-    frow[i - 1] = f[0];
+  hflx_xrows<2, R>(g, j, k, mul, cflx, fld, xs, ss, [&](int i0, unsigned o, const R (&f)[2]) {
+    fr[i0] = f[0];
+    if (i0 == nlon - 1) fr[-1] = f[0];
     fx[o] = f[1];
   });
   __syncthreads();
   const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j);
-  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-    const size_t o = ix3(nlat, nlon, i, j, k);
-    const R qv = xs[i - 1];
-    const R fxe = frow[i - 1], fxw = frow[i == 1 ? nlon - 1 : i - 2];
-    qx[o] = qv - (R)0.5 * (fdiv((fxe - fxw) * lel, ac) - divx[o] * qv) * hdt;
+  const unsigned ro = (unsigned)ix3(nlat, nlon, 1, j, k);
+  const R *X = xs + 2;
+  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+    const R qv = X[i0];
+    qx[ro + i0] = qv - (R)0.5 * (fdiv((fr[i0] - fr[i0 - 1]) * lel, ac) - divx[ro + i0] * qv) * hdt;
   }
 }
 
-// y: strips whose faces start one half row below the strip, so that every
-// full row of the strip has both of its faces.
-template <class R>
-__global__ void GMC_BOUNDS(R, 5) k_ffsl_inner_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly, const R *__restrict__ q,
-                               const R *__restrict__ divy, R *__restrict__ qy, double dt) {
-  __shared__ double red[32];
-  extern __shared__ double sh_faces[];
-  R *face_sh = reinterpret_cast<R *>(sh_faces);   // polar face fluxes [2][nlon] (strips with a pole)
-  const int k = blockIdx.y + 1;
-  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, lim = g.limiter;
-  const R hdt = (R)dt;
-  const int j0 = blockIdx.x * kHflxRows + 1;
-  if (j0 > nhalf) return;
-  constexpr int NF = kHflxRows + 1;   // faces j0-1 .. j0+kHflxRows-1
-  constexpr int NV = kHflxRows + 6;   // rows j0-3 .. j0+kHflxRows+2
-  const int fl0 = j0 >= 2 ? 0 : 1;                       // first existing face
-  const int nfe = min(kHflxRows, nhalf - j0 + 1) + 1;    // faces up to nhalf
-  const bool has_s = j0 == 1, has_n = j0 <= nhalf && nhalf <= j0 + kHflxRows - 1;
-  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-    R y[NV], sl[NV];
-#pragma unroll
-    for (int t = 0; t < NV; ++t) {
-      if (t < nfe + 5) {
-        int sh;
-        const R *p = halo_row(g, q, j0 - 3 + t, k, sh);
-        int l = i + sh;
-        y[t] = p[l >= nlon ? l - nlon : l];
-      } else {
-        y[t] = 0;
-      }
-    }
-    R cy[NF], vy[NF];
-#pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      if (f >= fl0 && f < nfe) {
-        const size_t o = ix3(nhalf, nlon, i + 1, j0 - 1 + f, k);
-        cy[f] = cfly[o];
-        vy[f] = v[o];
-      }
-    }
-#pragma unroll
-    for (int t = 1; t < NV - 1; ++t) sl[t] = slope(lim, y[t - 1], y[t], y[t + 1]);
-    // faces in order; full row j0+f-1 is finished once face f (its north face) is known
-    R prev = 0, face_s = 0, face_n = 0;
-#pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      R cur = 0;
-      if (f >= fl0 && f < nfe) cur = hflx_yface(g, cy[f], vy[f], y, sl, f + 2);
-      const int jf = j0 - 1 + f;   // half row of face f
-      if (jf == 1) face_s = cur;
-      if (jf == nhalf) face_n = cur;
-      const int j = jf;            // full row whose north face is jf
-      if (f >= 1 && j >= 2 && j <= nlat - 1 && f < nfe) {
-        const size_t o = ix3(nlat, nlon, i + 1, j, k);
-        const R la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1), ac = ROWR(R, area_cell, j);
-        const R qv = y[f + 2];   // y[t] = Y(j0 - 3 + t)
-        qy[o] = qv - (R)0.5 * ((cur * la0 - prev * la1) / ac - divy[o] * qv) * hdt;
-      }
-      prev = cur;
-    }
-    // the polar faces' fluxes wait in shared memory for the FP64 ring sums
-    // below, so the column loop holds no FP64 arithmetic
-    if (has_s) face_sh[i] = face_s;
-    if (has_n) face_sh[nlon + i] = face_n;
+// y: one column per thread marching north through a band of full rows
+// 2 .. nlat-1 (the faces from the band's first south face on).  The pole rows
+// get no qy: the outer x pass, its only reader, skips them (hflx on full
+// latitudes without the poles, ffsl_mod.F90:787-829).
+template <class R, bool MB>
+__global__ void __launch_bounds__(kYThreads) k_ffsl_inner_y(DGrid g, const R *__restrict__ v, const R *__restrict__ cfly,
+                                                            const R *__restrict__ q, const R *__restrict__ divy,
+                                                            R *__restrict__ qy, R dt) {
+  if constexpr (MB) {   // grid z = member x level
+    const size_t mo = (size_t)(blockIdx.z / g.nlev) * g.mstride;
+    v = mshift(v, mo); cfly = mshift(cfly, mo); q = mshift(q, mo); divy = mshift(divy, mo); qy = mshift(qy, mo);
   }
-  // pole rows from the ring of their polar half row
-  for (int side = 0; side < 2; ++side) {
-    const bool has = side == 0 ? has_s : has_n;
-    if (!has) continue;
-    const int j = side == 0 ? 1 : nlat, jv = side == 0 ? 1 : nhalf;
-    __syncthreads();
-    double ring = 0;   // each thread its columns in order, then the fixed-order block sum
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) ring += (double)face_sh[side * nlon + i];
-    double p = block_sum(ring, red);
-    p = p * ROW(g.le_lat, jv) / nlon / ROW(g.area_cell, j);
-    const R pole = (R)p;
-    for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-      const size_t o = ix3(nlat, nlon, i, j, k);
-      const R qv = q[o];
-      if (j == 1)
-        qy[o] = qv - (R)0.5 * (pole - divy[o] * qv) * hdt;
-      else
-        qy[o] = qv + (R)0.5 * (pole - divy[o] * qv) * hdt;
+  const int k = blockIdx.z % g.nlev + 1;
+  const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int jb = blockIdx.y * kYBand + 2, je = min(nlat - 1, jb + kYBand - 1);
+  if (i >= nlon || jb > nlat - 1) return;
+  const R hdt = dt;
+  YMarch<R> ym(g, q, k, i, jb - 1);
+  unsigned of = (unsigned)ix3(nhalf, nlon, i + 1, jb - 1, k);   // face jb-1
+  unsigned oc = (unsigned)ix3(nlat, nlon, i + 1, jb, k);        // cell (i, jb)
+  R prev = ym.flux(cfly[of], v[of]);
+  R la1 = ROWR(R, le_lat, jb - 1);
+  of += nlon;
+  R c = cfly[of], vv = v[of], dy = divy[oc];
+  for (int j = jb; j <= je; ++j, oc += nlon, of += nlon) {
+    R cn = 0, vn = 0, dn = 0;
+    if (j < je) {   // the next row's inputs, requested before this row's arithmetic
+      cn = cfly[of + nlon];
+      vn = v[of + nlon];
+      dn = divy[oc + nlon];
     }
+    ym.advance();
+    const R cur = ym.flux(c, vv);
+    const R la0 = ROWR(R, le_lat, j), ac = ROWR(R, area_cell, j);
+    const R qv = ym.y1;   // y(j)
+    qy[oc] = qv - (R)0.5 * ((cur * la0 - prev * la1) / ac - dy * qv) * hdt;
+    prev = cur;
+    la1 = la0;
+    c = cn;
+    vv = vn;
+    dy = dn;
   }
 }
 
@@ -462,8 +475,9 @@ struct VRoll {
 
 // calc_grad_ptf tail (operators_mod.F90:1034-1098) with the tendency
 // assembly dpt = -(dptf/dlon + dptf/dlat + dptf/dlev) (gmcore_mod.F90:491-495).
-template <class R>
+template <class R, bool MB>
 __global__ void k_pt_tendency(DGrid g, Slot<R> s, Work<R> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   extern __shared__ double sh[];
   double *red = sh, *ring = sh + 32;
   const int j = blockIdx.y + 1;
@@ -569,7 +583,9 @@ __device__ R vflx_tile(const DGrid &g, const R *C, const R *FL, const R *DF, con
 // extrapolated ghost levels, slopes, limited cell coefficients and interface
 // fluxes are built in shared memory phase by phase, each phase parallel over
 // (column, level).
+template <bool MB>
 __global__ void GMC_BOUNDS_F(8) k_pt_tendency_f(DGrid g, Slot<float> s, Work<float> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   extern __shared__ double shd[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev, lim = g.limiter;
   const int j = blockIdx.y + 1;
@@ -742,7 +758,7 @@ __global__ void k_half_level_mass(DGrid g, SurfP<R> sp, R *m_lev, int mode, doub
 }
 
 template <class R>
-__global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, double dt) {
+__global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, R dt) {
   extern __shared__ float colsh[];
   const int j = blockIdx.y + 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -918,7 +934,7 @@ __global__ void k_tracer_vertical(DGrid g, R *q, const R *cflz, const R *we, Sur
 // memory, the update parallel over (column, level); the vertical fixer walks
 // a column in order and runs only in blocks that hold a negative value.
 __global__ void GMC_BOUNDS_F(6) k_tracer_vertical_f(DGrid g, float *q, const float *cflz, const float *we, SurfP<float> sp,
-                                    double dt_adv) {
+                                    float dt_adv) {
   extern __shared__ float shf[];
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev, lim = g.limiter;
   const int j = blockIdx.y + 1;
@@ -1044,20 +1060,21 @@ __global__ void k_tracer_lon_damp(DGrid g, R *q) {
 
 template <class R>
 void launch_ffsl_inner_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, R *qy, double dt) {
-  const dim3 strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
-  k_ffsl_inner_y<R><<<strips, L.threads, 2 * g.nlon * sizeof(R), L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt);
+  // blocks: (column chunk, band of rows, level x member)
+  const dim3 grid((g.nlon + kYThreads - 1) / kYThreads, (g.nlat - 2 + kYBand - 1) / kYBand, g.nlev * L.members);
+  mb_launch(L, [&](auto mb) { k_ffsl_inner_y<R, decltype(mb)::value><<<grid, kYThreads, 0, L.stream>>>(g, b.v, b.cfly, q, b.divy, qy, dt); });
 }
 template <class R>
 void launch_ffsl_x2(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *q, const R *qy, R *qx, R *fx,
                     double dt) {
-  const size_t smem_x = (size_t)3 * g.nlon * sizeof(R);
-  if (smem_x > 48 * 1024) cudaFuncSetAttribute(k_ffsl_x2<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x);
-  k_ffsl_x2<R><<<dim3(g.nlat, g.nlev), L.threads, smem_x, L.stream>>>(g, b.u, b.mfx, b.cflx, q, qy, b.divx, qx, fx, dt);
+  const size_t smem_x = (size_t)(5 * g.nlon + 17) * sizeof(R);   // padded rows, slopes, inner fluxes
+  if (smem_x > 48 * 1024) { cudaFuncSetAttribute(k_ffsl_x2<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x); cudaFuncSetAttribute(k_ffsl_x2<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x); }
+  mb_launch(L, [&](auto mb) { k_ffsl_x2<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, smem_x, L.stream>>>(g, b.u, b.mfx, b.cflx, q, qy, b.divx, qx, fx, dt); });
 }
 template <class R>
 void launch_hflx_y(const DGrid &g, const Launch &L, const BatchView<R> &b, const R *qx, R *fy) {
-  const dim3 strips((g.nhalf + kHflxRows - 1) / kHflxRows, g.nlev);
-  k_hflx_y<R><<<strips, L.threads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy);
+  const dim3 grid((g.nlon + kYThreads - 1) / kYThreads, (g.nhalf + kYBand - 1) / kYBand, g.nlev * L.members);
+  mb_launch(L, [&](auto mb) { k_hflx_y<R, decltype(mb)::value><<<grid, kYThreads, 0, L.stream>>>(g, b.mfy, b.cfly, qx, fy); });
 }
 
 // One horizontal FFSL flux evaluation (fx, fy of q; qx, qy scratch): the y
@@ -1074,13 +1091,13 @@ template <class R>
 void launch_pt_tendency(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
   if constexpr (std::is_same<R, float>::value) {
     const size_t smem = g.nlev * sizeof(double) + (size_t)(6 * g.nlev + 7) * (kTileI + 1) * sizeof(float);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_pt_tendency_f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_pt_tendency_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w);
+    if (smem > 48 * 1024) { cudaFuncSetAttribute(k_pt_tendency_f<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); cudaFuncSetAttribute(k_pt_tendency_f<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
+    mb_launch(L, [&](auto mb) { k_pt_tendency_f<decltype(mb)::value><<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat, L.members), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w); });
     return;
   }
   const int bt = 64;
   size_t smem = (32 + g.nlev + 2) * sizeof(double);
-  k_pt_tendency<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, s, w);
+  mb_launch(L, [&](auto mb) { k_pt_tendency<R, decltype(mb)::value><<<dim3((g.nlon + bt - 1) / bt, g.nlat, L.members), bt, smem, L.stream>>>(g, s, w); });
 }
 
 template void launch_ffsl_hflx<double>(const DGrid &, const Launch &, const BatchView<double> &, const double *, double *,

@@ -58,6 +58,9 @@ struct DGrid {
   double ke_cell_wgt;
   int pv_scheme, upwind_order_pv, pv_pole_stokes, coriolis_scheme, limiter;
   double upwind_wgt_pv;
+  // FP32 copies of scalar constants read by the FP32 form (no per-thread
+  // FP64 -> FP32 conversion on the FP64 pipe)
+  float ke_cell_wgt_f, upwind_wgt_pv_f, kappa_f, Rd_f, g_f;
   const double *area_cell, *area_subcell1, *area_subcell2;
   const double *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
   const double *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
@@ -90,6 +93,7 @@ struct DGrid {
   const double *div_c_lon, *div_c_lat;                             // [(k-1)*n + j-1]
   FilterDev big, small1, small2;
   unsigned *err;                                                   // device error words [2] (raise_err)
+  size_t mstride;                                                  // bytes between ensemble members' fields
 };
 
 // Raise an error from a kernel: err[0] collects every bit raised, err[1]
@@ -114,6 +118,18 @@ struct RowSel<float> {
   static __device__ __forceinline__ const float *pick(const double *, const float *f) { return f; }
 };
 #define ROWR(R, name, j) (RowSel<R>::pick(g.name, g.f.name)[(j) + 1])
+// Scalar constant `name` of DGrid in the form's type (name_f in FP32).
+template <class R>
+struct ScalarSel;
+template <>
+struct ScalarSel<double> {
+  static __device__ __forceinline__ double pick(double d, float) { return d; }
+};
+template <>
+struct ScalarSel<float> {
+  static __device__ __forceinline__ float pick(double, float f) { return f; }
+};
+#define SCALR(R, name) (ScalarSel<R>::pick(g.name, g.name##_f))
 
 // Surface pressure as the layer-mass formula of each form reads it: the FP64
 // form takes phs_f, the FP32 form psr = phs_f - ptop rounded once to FP32.
@@ -140,6 +156,10 @@ struct SurfP<float> {
 // thread. The FP64 forms are capped at 128 registers.
 #define GMC_BOUNDS(R, NB) __launch_bounds__(256, sizeof(R) == 4 ? NB : 2)
 #define GMC_BOUNDS_F(NB) __launch_bounds__(256, NB)
+// The member-batched variant of a kernel (MB) keeps its member offset in
+// registers: one resident block fewer per SM (a few more registers) there.
+#define GMC_BOUNDS_MB(R, NB, MB) __launch_bounds__(256, sizeof(R) == 4 ? ((MB) ? (NB) - 2 : (NB)) : 2)
+#define GMC_BOUNDS_FMB(NB, NB_MB, MB) __launch_bounds__(256, (MB) ? (NB_MB) : (NB))
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); }
 

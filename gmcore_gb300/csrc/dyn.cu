@@ -32,8 +32,9 @@ __device__ __forceinline__ LevMass<R> lev_mass(const DGrid &g, const Slot<R> &s,
   return LevMass<R>(g, s.surf(), s.gz, s.gzs, k);
 }
 
-template <class R>
+template <class R, bool MB>
 __global__ void GMC_BOUNDS(R, 8) k_mass_flux(DGrid g, Slot<R> s) {
+  if constexpr (MB) { to_member(g, s); }   // member-batched launches
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const LevMass<R> M = lev_mass(g, s, k);
@@ -54,8 +55,9 @@ __global__ void GMC_BOUNDS(R, 8) k_mass_flux(DGrid g, Slot<R> s) {
 }
 
 // Tangential mass fluxes and winds (operators_mod.F90:585-605).
-template <class R>
-__global__ void GMC_BOUNDS(R, 8) k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
+template <class R, bool MB>
+__global__ void GMC_BOUNDS_MB(R, 8, MB) k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const LevMass<R> M = lev_mass(g, s, k);
@@ -87,8 +89,9 @@ __global__ void GMC_BOUNDS(R, 8) k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) 
 
 // calc_ke (operators_mod.F90:234-352): cell KE, optionally blended with the
 // four vertex KEs (ke_scheme 2); pole cells take the ring mean of v^2.
-template <class R>
+template <class R, bool MB>
 __global__ void GMC_BOUNDS(R, 6) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const R *u = s.u_f, *v = s.v_f;
@@ -110,7 +113,7 @@ __global__ void GMC_BOUNDS(R, 6) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w)
   const unsigned uc = (unsigned)ix3(nlat, nlon, 1, j, k), us = uc - nlon, un = uc + nlon;
   const unsigned vc = (unsigned)ix3(nhalf, nlon, 1, j, k), vs = vc - nlon;
   const bool vtx = g.ke_scheme == 2;
-  const R cw = (R)g.ke_cell_wgt;
+  const R cw = SCALR(R, ke_cell_wgt);
   const R ate = ROWR(R, area_lat_east, j), atw = ROWR(R, area_lat_west, j), ate1 = ROWR(R, area_lat_east, j - 1),
           atw1 = ROWR(R, area_lat_west, j - 1);
   const R aon = ROWR(R, area_lon_north, j), aon1 = ROWR(R, area_lon_north, j - 1), aos = ROWR(R, area_lon_south, j),
@@ -134,8 +137,9 @@ __global__ void GMC_BOUNDS(R, 6) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w)
 
 // calc_vor + calc_pv (operators_mod.F90:612-703) with the vertex mass of
 // interp_cell_to_vtx (interp_mod.F90:438-463).
-template <class R>
+template <class R, bool MB>
 __global__ void GMC_BOUNDS(R, 6) k_pv(DGrid g, Slot<R> s, Work<R> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
@@ -181,12 +185,13 @@ __device__ __forceinline__ PvRow pv_row(const DGrid &g, int jj, int k) {
   return {(unsigned)ix3(g.nhalf, g.nlon, 1, jj, k), sh};
 }
 
-template <class R>
-__global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, double dt) {
+template <class R, bool MB>
+__global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, R dt) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const R eps = (R)2.220446049250313e-16;
-  const R wgt = (R)g.upwind_wgt_pv;
+  const R wgt = SCALR(R, upwind_wgt_pv);
   const R *__restrict__ pv = s.pv;
   const bool tvd = g.pv_scheme == GMC_PV_TVD, mid_only = g.pv_scheme == GMC_PV_MIDPOINT, up3 = g.upwind_order_pv == 3;
   // pv at 0-based longitude l (l + shift in [-nlon, 2 nlon)) of a resolved row
@@ -248,8 +253,9 @@ __global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, doubl
 // adv_batch_accum_uv_cell, CFL part (adv_batch_mod.F90:252-373): RK4
 // departure points along each axis give the Courant numbers; divx/divy are
 // the axis-split divergences (pole rows: ring sums).
-template <class R>
-__global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt_) {
+template <class R, bool MB>
+__global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, R dt_) {
+  if constexpr (MB) { const size_t mo = member_offset(g); u = mshift(u, mo); v = mshift(v, mo); cflx = mshift(cflx, mo); cfly = mshift(cfly, mo); divx = mshift(divx, mo); divy = mshift(divy, mo); }
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
@@ -383,8 +389,9 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
 
 // calc_grad_mf + calc_dphsdt + calc_we_lev + the mass batch's accum_we_lev
 // for one column (operators_mod.F90:939-1006, 1120-1143, 192-226).
-template <class R>
-__global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
+template <class R, bool MB>
+__global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, R dt) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   extern __shared__ double sh[];
   double *red = sh, *ring = sh + 32;
   const int j = blockIdx.y + 1;
@@ -498,7 +505,9 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, double dt) {
 // FP32 form of k_column_mass over column tiles: layer divergences, their
 // prefix sums along the column (warp scans), we_lev, dphs and the vertical
 // Courant numbers, each phase parallel over (column, level).
-__global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, double dt) {
+template <bool MB>
+__global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, float dt) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   extern __shared__ double shd[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
   const int j = blockIdx.y + 1;
@@ -579,8 +588,9 @@ __global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<flo
 // du = qhv - dke/dlon - we du/dlev, dv = -qhu - dke/dlat - we dv/dlev with the
 // energy-conserving Coriolis term (calc_coriolis, operators_mod.F90:846-906),
 // the KE gradient (:908-937) and SB81 vertical advection (:1145-1216).
-template <class R>
+template <class R, bool MB>
 __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
   const MassField<R> M = mass_of(g, s);
@@ -664,12 +674,14 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
 // passed as non-aliasing kernel arguments addressed by 32-bit row offsets (the
 // base pointers stay in the parameter bank, so the kernel fits in 32
 // registers) and the divisions taken as reciprocal products (fdiv).
-__global__ void GMC_BOUNDS_F(8) k_momentum_f(DGrid g, const float *__restrict__ mfx, const float *__restrict__ mfy,
+template <bool MB>
+__global__ void GMC_BOUNDS_FMB(8, 5, MB) k_momentum_f(DGrid g, const float *__restrict__ mfx, const float *__restrict__ mfy,
                                              const float *__restrict__ pvlon, const float *__restrict__ pvlat,
                                              const float *__restrict__ ke, const float *__restrict__ we,
                                              const float *__restrict__ uf, const float *__restrict__ vf,
                                              const float *__restrict__ psr, float *__restrict__ du,
                                              float *__restrict__ dv) {
+  if constexpr (MB) { const size_t mo = member_offset(g); mfx = mshift(mfx, mo); mfy = mshift(mfy, mo); pvlon = mshift(pvlon, mo); pvlat = mshift(pvlat, mo); ke = mshift(ke, mo); we = mshift(we, mo); uf = mshift(uf, mo); vf = mshift(vf, mo); psr = mshift(psr, mo); du = mshift(du, mo); dv = mshift(dv, mo); }
   const int k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
   const bool cor1 = g.coriolis_scheme == 1;
@@ -729,8 +741,9 @@ __global__ void GMC_BOUNDS_F(8) k_momentum_f(DGrid g, const float *__restrict__ 
 
 // Shallow-water thickness tendency dgz = -(dmf/dlon + dmf/dlat) g
 // (gmcore_mod.F90:520-524) with the pole ring of calc_grad_mf.
-template <class R>
+template <class R, bool MB>
 __global__ void k_swm_dgz(DGrid g, Slot<R> s, Work<R> w) {
+  if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   __shared__ double red[32];
   const int j = blockIdx.x + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
@@ -746,7 +759,7 @@ __global__ void k_swm_dgz(DGrid g, Slot<R> s, Work<R> w) {
   for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
     R dlon = (s.mfx_lon[ix3(nlat, nlon, i, j, 1)] - s.mfx_lon[ix3(nlat, nlon, wrap(i - 1, nlon), j, 1)]) * lel / ac;
     R dlat = (s.mfy_lat[ix3(nhalf, nlon, i, j, 1)] * la0 - s.mfy_lat[ix3(nhalf, nlon, i, j - 1, 1)] * la1) / ac;
-    w.dgz[ix3(nlat, nlon, i, j, 1)] = -(dlon + dlat) * (R)g.g;
+    w.dgz[ix3(nlat, nlon, i, j, 1)] = -(dlon + dlat) * SCALR(R, g);
   }
 }
 
@@ -779,8 +792,9 @@ __device__ __forceinline__ void check_column(const DGrid &g, double phs, double 
 }
 
 // phs = phs_old + dt dphs; phs_f = big filter(phs)   (:134-143)
-template <class R>
+template <class R, bool MB>
 __global__ void k_update_phs(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+  if constexpr (MB) { to_member(g, o); to_member(g, n); to_member(g, w); }   // member-batched launches
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, nlon = g.nlon;
   double *row = sh, *ext = sh + nlon;
@@ -844,8 +858,9 @@ __global__ void k_surface_rel(const double *phs_f, float *psr, size_t n, double 
 template <class R>
 constexpr int kPtLevels = std::is_same<R, float>::value ? 2 : 1;
 
-template <class R>
-__global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+template <class R, bool MB>
+__global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
+  if constexpr (MB) { to_member(g, o); to_member(g, n); to_member(g, w); }   // member-batched launches
   constexpr int KB = kPtLevels<R>;
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, k0 = blockIdx.y * KB + 1, nlon = g.nlon, nlat = g.nlat, nlev = g.nlev;
@@ -879,8 +894,9 @@ __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
 }
 
 // Shallow water: gz = gz_old + dt dgz; gz_f = big(gz); gz = small1(gz) (:178-192)
-template <class R>
-__global__ void k_update_gz(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+template <class R, bool MB>
+__global__ void k_update_gz(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
+  if constexpr (MB) { to_member(g, o); to_member(g, n); to_member(g, w); }   // member-batched launches
   extern __shared__ double sh[];
   const int j = blockIdx.x + 1, nlon = g.nlon;
   R *row = reinterpret_cast<R *>(sh), *row2 = row + nlon, *ext = row2 + nlon;
@@ -906,8 +922,9 @@ __global__ void k_update_gz(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt)
 // operators_mod.F90:124-131): hybrid pressures and their Exner power
 // (calc_ph :136-168), temperature (calc_t :170-190) and the hydrostatic
 // geopotential integrated upward from the surface (calc_gz_lev :433-469).
-template <class R>
+template <class R, bool MB>
 __global__ void k_column_backward(DGrid g, Slot<R> n, Work<R> w) {
+  if constexpr (MB) { to_member(g, n); to_member(g, w); }   // member-batched launches
   const int j = blockIdx.y + 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int nlat = g.nlat, nlon = g.nlon, nlev = g.nlev;
@@ -924,7 +941,7 @@ __global__ void k_column_backward(DGrid g, Slot<R> n, Work<R> w) {
     // Every FP32 quantity is either small or relative, and the geopotential
     // is summed upward as an unevaluated (hi, lo) FP32 pair, so differences
     // between neighbours keep ~1e-7 relative accuracy without FP64 issue.
-    const float kap = (float)g.kappa, Rd = (float)g.Rd;
+    const float kap = g.kappa_f, Rd = g.Rd_f;
     const float dps = (float)(phs - g.ps_ref);
     float hi = (float)gzs;
     float lo = (float)(gzs - (double)hi);
@@ -1042,8 +1059,9 @@ __device__ __forceinline__ bool filter_on(const FilterDev &f, bool full_lat, int
 template <class R>
 constexpr int kUvLevels = std::is_same<R, float>::value ? 2 : 1;
 
-template <class R>
-__global__ void GMC_BOUNDS(R, 6) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, double dt) {
+template <class R, bool MB>
+__global__ void GMC_BOUNDS_MB(R, 6, MB) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
+  if constexpr (MB) { to_member(g, o); to_member(g, n); to_member(g, w); }   // member-batched launches
   constexpr int KB = kUvLevels<R>;
   extern __shared__ double sh[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
@@ -1258,87 +1276,87 @@ inline size_t filter_smem(const DGrid &g, int rows, size_t elem) {
 // ---------------------------------------------------------------------------
 template <class R>
 void launch_mass_flux(const DGrid &g, const Launch &L, const Slot<R> &s) {
-  k_mass_flux<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s);
+  mb_launch(L, [&](auto mb) { k_mass_flux<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s); });
 }
 template <class R>
 void launch_tangent_winds(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  k_tangent_winds<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+  mb_launch(L, [&](auto mb) { k_tangent_winds<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_kinetic_energy(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  k_kinetic_energy<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+  mb_launch(L, [&](auto mb) { k_kinetic_energy<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  k_pv<R><<<dim3(g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+  mb_launch(L, [&](auto mb) { k_pv<R, decltype(mb)::value><<<dim3(g.nhalf, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
-  k_pv_edges<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w, dt);
+  mb_launch(L, [&](auto mb) { k_pv_edges<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w, dt); });
 }
 template <class R>
 void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt) {
   const size_t smem = std::is_same<R, float>::value ? g.nlon * sizeof(float) : 0;
-  k_batch_cfl<R><<<dim3(g.nlat, g.nlev), L.threads, smem, L.stream>>>(g, u, v, cflx, cfly, divx, divy, dt);
+  mb_launch(L, [&](auto mb) { k_batch_cfl<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, smem, L.stream>>>(g, u, v, cflx, cfly, divx, divy, dt); });
 }
 template <class R>
 void launch_column_mass(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
   if constexpr (std::is_same<R, float>::value) {
     const size_t smem = g.nlev * sizeof(double) + (size_t)(2 * g.nlev + 1) * (kTileI + 1) * sizeof(float) +
                         (size_t)(3 * g.nlev + 1) * sizeof(float);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_column_mass_f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_column_mass_f<<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w, dt);
+    if (smem > 48 * 1024) { cudaFuncSetAttribute(k_column_mass_f<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); cudaFuncSetAttribute(k_column_mass_f<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
+    mb_launch(L, [&](auto mb) { k_column_mass_f<decltype(mb)::value><<<dim3((g.nlon + kTileI - 1) / kTileI, g.nlat, L.members), dim3(kTileI, kTileK), smem, L.stream>>>(g, s, w, dt); });
     return;
   }
   const int bt = 64;
   size_t smem = (32 + g.nlev + 2) * sizeof(double);
-  k_column_mass<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, smem, L.stream>>>(g, s, w, dt);
+  mb_launch(L, [&](auto mb) { k_column_mass<R, decltype(mb)::value><<<dim3((g.nlon + bt - 1) / bt, g.nlat, L.members), bt, smem, L.stream>>>(g, s, w, dt); });
 }
 template <class R>
 void launch_momentum_tend(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
   if constexpr (std::is_same<R, float>::value) {
     if (g.baroclinic) {
-      k_momentum_f<<<dim3(g.nlat - 2 + g.nhalf, g.nlev), 256, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
-                                                              s.u_f, s.v_f, s.psr, w.du, w.dv);
+      mb_launch(L, [&](auto mb) { k_momentum_f<decltype(mb)::value><<<dim3(g.nlat - 2 + g.nhalf, g.nlev, L.members), 256, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
+                                                              s.u_f, s.v_f, s.psr, w.du, w.dv); });
       return;
     }
   }
-  k_momentum_tend<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, s, w);
+  mb_launch(L, [&](auto mb) { k_momentum_tend<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_swm_dgz(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  k_swm_dgz<R><<<dim3(g.nlat, 1), L.threads, 0, L.stream>>>(g, s, w);
+  mb_launch(L, [&](auto mb) { k_swm_dgz<R, decltype(mb)::value><<<dim3(g.nlat, 1, L.members), L.threads, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_update_phs(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
-  allow_smem(k_update_phs<R>, filter_smem(g, 1, sizeof(double)));
-  k_update_phs<R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 1, sizeof(double)), L.stream>>>(g, o, n, w, dt);
+  allow_smem(k_update_phs<R, false>, filter_smem(g, 1, sizeof(double))); allow_smem(k_update_phs<R, true>, filter_smem(g, 1, sizeof(double)));
+  mb_launch(L, [&](auto mb) { k_update_phs<R, decltype(mb)::value><<<dim3(g.nlat, 1, L.members), L.threads, filter_smem(g, 1, sizeof(double)), L.stream>>>(g, o, n, w, dt); });
 }
 template <class R>
 void launch_update_pt(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
   constexpr int KB = kPtLevels<R>;
   const int hmax = (g.big.max_taps - 1) / 2;
   const size_t smem = (size_t)KB * (g.nlon + g.nlon + 2 * hmax + 8) * sizeof(R);
-  allow_smem(k_update_pt<R>, smem);
-  k_update_pt<R><<<dim3(g.nlat, (g.nlev + KB - 1) / KB), L.threads, smem, L.stream>>>(g, o, n, w, dt);
+  allow_smem(k_update_pt<R, false>, smem); allow_smem(k_update_pt<R, true>, smem);
+  mb_launch(L, [&](auto mb) { k_update_pt<R, decltype(mb)::value><<<dim3(g.nlat, (g.nlev + KB - 1) / KB, L.members), L.threads, smem, L.stream>>>(g, o, n, w, dt); });
 }
 template <class R>
 void launch_update_gz(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
-  allow_smem(k_update_gz<R>, filter_smem(g, 2, sizeof(R)));
-  k_update_gz<R><<<dim3(g.nlat, 1), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt);
+  allow_smem(k_update_gz<R, false>, filter_smem(g, 2, sizeof(R))); allow_smem(k_update_gz<R, true>, filter_smem(g, 2, sizeof(R)));
+  mb_launch(L, [&](auto mb) { k_update_gz<R, decltype(mb)::value><<<dim3(g.nlat, 1, L.members), L.threads, filter_smem(g, 2, sizeof(R)), L.stream>>>(g, o, n, w, dt); });
 }
 template <class R>
 void launch_column_backward(const DGrid &g, const Launch &L, const Slot<R> &n, const Work<R> &w) {
   const int bt = 64;
-  k_column_backward<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, n, w);
+  mb_launch(L, [&](auto mb) { k_column_backward<R, decltype(mb)::value><<<dim3((g.nlon + bt - 1) / bt, g.nlat, L.members), bt, 0, L.stream>>>(g, n, w); });
 }
 template <class R>
 void launch_update_uv(const DGrid &g, const Launch &L, const Slot<R> &o, const Slot<R> &n, const Work<R> &w, double dt) {
   constexpr int KB = kUvLevels<R>;
   const int hmax = (g.big.max_taps - 1) / 2;
   const size_t smem = (size_t)KB * (2 * g.nlon + g.nlon + 2 * hmax + 8) * sizeof(R);
-  allow_smem(k_update_uv<R>, smem);
-  k_update_uv<R><<<dim3(g.nlat + g.nhalf, (g.nlev + KB - 1) / KB), L.threads, smem, L.stream>>>(g, o, n, w, dt);
+  allow_smem(k_update_uv<R, false>, smem); allow_smem(k_update_uv<R, true>, smem);
+  mb_launch(L, [&](auto mb) { k_update_uv<R, decltype(mb)::value><<<dim3(g.nlat + g.nhalf, (g.nlev + KB - 1) / KB, L.members), L.threads, smem, L.stream>>>(g, o, n, w, dt); });
 }
 template <class R>
 void launch_filter_prologue(const DGrid &g, const Launch &L, const Slot<R> &s) {
@@ -1398,8 +1416,9 @@ namespace gmc {
 namespace {
 
 // calc_div, order-2 branch (operators_mod.F90:354-412), on the filtered wind.
-template <class R>
+template <class R, bool MB>
 __global__ void k_div(DGrid g, Slot<R> n, R *div) {
+  if constexpr (MB) { to_member(g, n); div = mshift(div, member_offset(g)); }   // member-batched launches
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
@@ -1421,8 +1440,9 @@ __global__ void k_div(DGrid g, Slot<R> n, R *div) {
 
 // div2 = Laplacian of div on non-pole rows (operators_mod.F90:412-425); pole
 // rows stay zero as the reference's zero-initialised array leaves them.
-template <class R>
+template <class R, bool MB>
 __global__ void k_div2(DGrid g, const R *div, R *div2) {
+  if constexpr (MB) { const size_t mo = member_offset(g); div = mshift(div, mo); div2 = mshift(div2, mo); }
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nlon = g.nlon;
   if (j == 1 || j == nlat) {
@@ -1440,8 +1460,9 @@ __global__ void k_div2(DGrid g, const R *div, R *div2) {
 }
 
 // order 2: u += c (div(i+1) - div(i)) / de; order 4: u -= c (div2(i+1) - div2(i)) / de
-template <class R>
+template <class R, bool MB>
 __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
+  if constexpr (MB) { to_member(g, n); div = mshift(div, member_offset(g)); }   // member-batched launches
   const R sgn = g.div_damp_order == 4 ? (R)-1 : (R)1;
   const int k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
@@ -1467,12 +1488,12 @@ __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
 
 template <class R>
 void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, R *div2) {
-  k_div<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
+  mb_launch(L, [&](auto mb) { k_div<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, n, div); });
   if (g.div_damp_order == 4) {
-    k_div2<R><<<dim3(g.nlat, g.nlev), L.threads, 0, L.stream>>>(g, div, div2);
-    k_div_damp<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, n, div2);
+    mb_launch(L, [&](auto mb) { k_div2<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, div, div2); });
+    mb_launch(L, [&](auto mb) { k_div_damp<R, decltype(mb)::value><<<dim3(g.nlat + g.nhalf, g.nlev, L.members), L.threads, 0, L.stream>>>(g, n, div2); });
   } else {
-    k_div_damp<R><<<dim3(g.nlat + g.nhalf, g.nlev), L.threads, 0, L.stream>>>(g, n, div);
+    mb_launch(L, [&](auto mb) { k_div_damp<R, decltype(mb)::value><<<dim3(g.nlat + g.nhalf, g.nlev, L.members), L.threads, 0, L.stream>>>(g, n, div); });
   }
 }
 template void launch_div_damp<double>(const DGrid &, const Launch &, const Slot<double> &, double *, double *);

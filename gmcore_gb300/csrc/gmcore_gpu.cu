@@ -12,6 +12,7 @@
 #include <memory>
 #include <tuple>
 #include <map>
+#include <set>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -255,6 +256,9 @@ struct EngineBase {
   virtual void tlm(int nsteps, const double *const dx0[3], double *const dxn[3]) = 0;
   virtual void adjoint(int nsteps, int ckpt, const double *const lam_n[3], double *const lam_0[3]) = 0;
   virtual void set_graphs(bool on) = 0;
+  virtual int layout_in_use() const = 0;
+  virtual bool set_layout(int lay) = 0;
+  virtual bool layout_is_tuned() const = 0;
   long time_step = 0;
   int device = 0;   // device current when the context was created
   // timing and profiling
@@ -420,6 +424,44 @@ struct Engine : EngineBase {
     }
   }
 
+  // Members sharing this grid step in member-batched launches (grid z =
+  // member) when every member-owned pointer of member m is member 0's plus m
+  // times one stride; the arena carves the members identically, and the
+  // check below confirms it pointer by pointer.
+  bool batched_members = false;
+  void member_batching_setup() {
+    dg.mstride = 0;
+    if (nm <= 1) return;
+    const uintptr_t stride = (uintptr_t)gzs[1] - (uintptr_t)gzs[0];
+    bool ok = stride > 0;
+    auto same = [&](const void *p0, const void *pm, int m) {
+      if (!p0 && !pm) return;
+      ok = ok && p0 && pm && (uintptr_t)pm - (uintptr_t)p0 == stride * (uintptr_t)m;
+    };
+    for (int m = 1; m < nm && ok; ++m) {
+      for (int t = 0; t < 3; ++t) {
+        const Slot<R> &a = slots[t], &b = slots[m * 3 + t];
+        for (auto pp : {std::make_pair((const void *)a.u_lon, (const void *)b.u_lon), {a.v_lat, b.v_lat}, {a.u_f, b.u_f},
+                        {a.v_f, b.v_f}, {a.pt, b.pt}, {a.gz, b.gz}, {a.gz_f, b.gz_f}, {a.phs, b.phs}, {a.phs_f, b.phs_f},
+                        {a.psr, b.psr}, {a.mfx_lon, b.mfx_lon}, {a.mfy_lat, b.mfy_lat}, {a.pv, b.pv},
+                        {a.pv_lon, b.pv_lon}, {a.pv_lat, b.pv_lat}, {a.we_lev, b.we_lev}, {a.gzs, b.gzs}})
+          same(pp.first, pp.second, m);
+      }
+      const Work<R> &a = work[0], &b = work[m];
+      for (auto pp : {std::make_pair((const void *)a.u_lat, (const void *)b.u_lat), {a.v_lon, b.v_lon}, {a.ke, b.ke},
+                      {a.cflx, b.cflx}, {a.cfly, b.cfly}, {a.cflz, b.cflz}, {a.divx, b.divx}, {a.divy, b.divy},
+                      {a.qmfx, b.qmfx}, {a.qmfy, b.qmfy}, {a.qx, b.qx}, {a.qy, b.qy}, {a.ptf_lon, b.ptf_lon},
+                      {a.ptf_lat, b.ptf_lat}, {a.du, b.du}, {a.dv, b.dv}, {a.dpt, b.dpt}, {a.dgz, b.dgz},
+                      {a.dphs, b.dphs}, {a.ph_exn_lev, b.ph_exn_lev}, {a.gz_lev, b.gz_lev}, {a.pea, b.pea},
+                      {a.gzhl, b.gzhl}, {a.gzs, b.gzs}})
+        same(pp.first, pp.second, m);
+    }
+    if (ok) {
+      dg.mstride = stride;
+      batched_members = true;
+    }
+  }
+
   explicit Engine(const gmc_config &cfg) {
     try {
       construct(cfg);
@@ -458,8 +500,10 @@ struct Engine : EngineBase {
     cnt.take<R>(std::max(lev3(), full3()));
     arena.reserve(cnt.used + 4096);
     for (int m = 0; m < nm; ++m) carve_member(arena, m, bc);
+    member_batching_setup();
     diag_partial = arena.take<double>(8 * nblk);
     member_streams();
+    setup_layouts();
     if (nm == 1 && bc) {
       CK(cudaStreamCreateWithFlags(&dside, cudaStreamNonBlocking));
       for (cudaEvent_t *e : {&dfork_ev, &dmf_ev, &dcm_ev, &dpt_ev}) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
@@ -657,6 +701,8 @@ struct Engine : EngineBase {
     dg.ke_scheme = c.ke_scheme; dg.ke_cell_wgt = c.ke_cell_wgt;
     dg.pv_scheme = c.pv_scheme; dg.upwind_order_pv = c.upwind_order_pv; dg.pv_pole_stokes = c.pv_pole_stokes;
     dg.coriolis_scheme = c.coriolis_scheme; dg.limiter = c.limiter_type; dg.upwind_wgt_pv = c.upwind_wgt_pv;
+    dg.ke_cell_wgt_f = (float)c.ke_cell_wgt; dg.upwind_wgt_pv_f = (float)c.upwind_wgt_pv;
+    dg.kappa_f = (float)(c.Rd / c.cpd); dg.Rd_f = (float)c.Rd; dg.g_f = (float)c.g;
     dg.flux_type = c.ffsl_flux_type; dg.tvd_limiter = c.tvd_limiter_type; dg.div_damp_order = c.div_damp_order;
   }
 
@@ -1408,9 +1454,9 @@ struct Engine : EngineBase {
   // While a graph is replayed the host logic of the step still runs (dry
   // mode: launches skipped, counters advanced).
   struct GraphKey {
-    int o, n, su, sm, sw, adv, qo;
+    int o, n, su, sm, sw, adv, qo, layout;
     bool operator<(const GraphKey &b) const {
-      return std::tie(o, n, su, sm, sw, adv, qo) < std::tie(b.o, b.n, b.su, b.sm, b.sw, b.adv, b.qo);
+      return std::tie(o, n, su, sm, sw, adv, qo, layout) < std::tie(b.o, b.n, b.su, b.sm, b.sw, b.adv, b.qo, b.layout);
     }
   };
   std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -1435,8 +1481,139 @@ struct Engine : EngineBase {
     CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
   }
 
-  // the launches of one step (all members)
-  void step_body(int o, int n, bool ring) {
+  // Launch layouts of an ensemble step, all with identical results:
+  // layout 0 launches each member's kernels separately, the members spread
+  // over up to 8 streams; layout G > 0 splits the members into G groups of
+  // consecutive members, each group one member-batched launch per operator
+  // (grid z = member) on its own stream, so that G kernels of different kinds
+  // overlap.  The autotuner below times them on the first steps of a context
+  // and keeps the fastest.
+  std::vector<int> layouts;     // candidates, in tuning order
+  int layout = 0;               // in use
+  bool tuned = true;            // false while candidates are being timed
+  struct LayoutTiming { double ms = 0; int n = 0, queued = 0; };   // queued: timed, not yet read
+  std::vector<LayoutTiming> layout_ms;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> tune_pending;
+
+  int layout_in_use() const override { return layout; }
+  bool set_layout(int lay) override {
+    if (lay < 0) {
+      setup_layouts();
+      return true;
+    }
+    if (std::find(layouts.begin(), layouts.end(), lay) == layouts.end()) return false;
+    layout = lay;
+    tuned = true;
+    return true;
+  }
+  bool layout_is_tuned() const override { return tuned; }
+  void setup_layouts() {
+    layouts.clear();
+    layouts.push_back(0);
+    if (batched_members)
+      for (int G : {1, 2, 4, 8})
+        if (G <= nm && (G == 1 || nm / G >= 2)) layouts.push_back(G);
+    layout = 0;
+    tuned = layouts.size() <= 1;
+    layout_ms.assign(layouts.size(), LayoutTiming{});
+  }
+  // the candidate to run next while tuning: each is timed twice on replayed
+  // graphs (its first step captures the graph and is not timed)
+  int next_tuning_layout(bool &timed) {
+    for (size_t c = 0; c < layouts.size(); ++c)
+      if (layout_ms[c].n + layout_ms[c].queued < 2) {
+        timed = captured_layouts.count(layouts[c]) > 0;
+        return (int)c;
+      }
+    timed = false;
+    return -1;
+  }
+  std::set<int> captured_layouts;
+  void collect_tuning() {
+    for (auto &p : tune_pending) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+      layout_ms[p.first].ms += ms;
+      layout_ms[p.first].n += 1;
+      layout_ms[p.first].queued -= 1;
+      event_pool.push_back(p.second.first);
+      event_pool.push_back(p.second.second);
+    }
+    tune_pending.clear();
+    bool done = true;
+    for (const LayoutTiming &t : layout_ms) done = done && t.n >= 2;
+    if (!done) return;
+    size_t best = 0;
+    for (size_t c = 1; c < layouts.size(); ++c)
+      if (layout_ms[c].ms / layout_ms[c].n < layout_ms[best].ms / layout_ms[best].n) best = c;
+    layout = layouts[best];
+    tuned = true;
+  }
+
+  // The dynamics of one step for all members in member-batched launches, in
+  // G groups on their own streams, then each member's tracer advection.
+  void step_body_batched(int o, int n, bool ring, int G) {
+    const double dt = grid.cfg.dt_dyn;
+    const int t3 = 3 - o - n;
+    const int su = uv_step, sm = mf_step, sw = we_step;
+    const bool fork = G > 1 && !prof;
+    if (fork && !dry) {
+      CK(cudaEventRecord(fork_ev, stream));
+      for (int t = 0; t < G; ++t) CK(cudaStreamWaitEvent(mstreams[t], fork_ev, 0));
+    }
+    const int per = (nm + G - 1) / G;
+    try {
+      for (int gi = 0; gi < G; ++gi) {
+        const int m0 = gi * per, cnt = std::min(per, nm - m0);
+        if (cnt <= 0) continue;
+        L.members = cnt;
+        if (fork) L.stream = mstreams[gi];
+        switch (grid.cfg.time_scheme) {
+          case GMC_TIME_EULER:
+            stage(m0, o, o, n, dt);
+            break;
+          case GMC_TIME_PC2:
+            stage(m0, o, o, n, dt / 2.0);
+            stage(m0, o, n, t3, dt / 2.0);
+            stage(m0, o, t3, n, dt);
+            break;
+          default:
+            stage(m0, o, o, n, dt / 3.0);
+            stage(m0, o, n, t3, dt / 2.0);
+            stage(m0, o, t3, n, dt);
+            break;
+        }
+        if (grid.cfg.use_div_damp)
+          K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2,
+            [&] { launch_div_damp<R>(dg, L, slots[m0 * 3 + n], work[m0].ke, work[m0].du); });
+      }
+    } catch (...) {
+      L.members = 1;
+      L.stream = stream;
+      throw;
+    }
+    L.members = 1;
+    L.stream = stream;
+    if (fork && !dry) {
+      for (int t = 0; t < G; ++t) {
+        CK(cudaEventRecord(mevents[t], mstreams[t]));
+        CK(cudaStreamWaitEvent(stream, mevents[t], 0));
+      }
+    }
+    if (ntr > 0) {
+      for (int m = 0; m < nm; ++m) {
+        uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
+        adv_run(m, slots[m * 3 + n], ring && time_step > 0);
+      }
+    }
+  }
+
+  // the launches of one step (all members) in launch layout `lay`
+  void step_body(int o, int n, bool ring, int lay) {
+    if (lay > 0) {
+      step_body_batched(o, n, ring, lay);
+      return;
+    }
     const double dt = grid.cfg.dt_dyn;
     const int t3 = 3 - o - n;
     const int su = uv_step, sm = mf_step, sw = we_step;
@@ -1498,14 +1675,22 @@ struct Engine : EngineBase {
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
       const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
       if (ring) alert_ring = true;
+      // the launch layout of this step: the tuned one, or while tuning the next
+      // candidate (all layouts give identical results)
+      int lay = layout, cand = -1;
+      bool timed = false;
+      if (!tuned && use_graphs) {
+        cand = next_tuning_layout(timed);
+        if (cand >= 0) lay = layouts[cand];
+      }
       if (use_graphs) {
-        const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old};
+        const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old, lay};
         auto gi = graphs.find(key);
         if (gi == graphs.end()) {
           cudaGraph_t gr = nullptr;
           CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
           try {
-            step_body(o, n, ring);
+            step_body(o, n, ring, lay);
           } catch (...) {
             cudaStreamEndCapture(stream, &gr);
             if (gr) cudaGraphDestroy(gr);
@@ -1517,19 +1702,32 @@ struct Engine : EngineBase {
           cudaGraphDestroy(gr);
           if (e != cudaSuccess) throw CudaError(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
           gi = graphs.emplace(key, ex).first;
+          timed = false;   // a capture step is not timed
         } else {
           dry = true;
           try {
-            step_body(o, n, ring);
+            step_body(o, n, ring, lay);
           } catch (...) {
             dry = false;
             throw;
           }
           dry = false;
         }
+        cudaEvent_t ta = nullptr, tb_ = nullptr;
+        if (cand >= 0 && timed) {
+          ta = take_event();
+          tb_ = take_event();
+          CK(cudaEventRecord(ta, stream));
+        }
         CK(cudaGraphLaunch(gi->second, stream));
+        if (ta) {
+          CK(cudaEventRecord(tb_, stream));
+          tune_pending.push_back({cand, {ta, tb_}});
+          layout_ms[cand].queued += 1;
+        }
+        if (cand >= 0) captured_layouts.insert(lay);
       } else {
-        step_body(o, n, ring);
+        step_body(o, n, ring, lay);
       }
       if (ntr > 0 && ring && time_step > 0) q_old = 1 - q_old;
       if (alert_ring) { alert_last = curr_time; alert_ring = false; }
@@ -1546,6 +1744,7 @@ struct Engine : EngineBase {
     last_steps = nsteps;
     last_launches = launches - launches0;
     if (prof) prof_collect();
+    if (!tune_pending.empty()) collect_tuning();
   }
 
   void diagnose(int m, gmc_diag *out) override {
@@ -2030,6 +2229,14 @@ int gmc_get_stats(const gmc_ctx *ctx, gmc_stats *out) {
   out->step_ms = ctx->eng->last_step_ms;
   out->steps = ctx->eng->last_steps;
   out->kernel_launches = ctx->eng->last_launches;
+  out->member_layout = ctx->eng->layout_in_use();
+  out->layout_tuned = ctx->eng->layout_is_tuned() ? 1 : 0;
+  return GMC_OK;
+}
+
+int gmc_set_member_layout(gmc_ctx *ctx, int32_t layout) {
+  if (!ctx || !ctx->eng) return GMC_EINVAL;
+  if (!ctx->eng->set_layout(layout)) return fail(ctx, GMC_EINVAL, "launch layout not available for this context");
   return GMC_OK;
 }
 

@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace gmc {
@@ -60,8 +62,50 @@ inline void allow_smem(Kern k, size_t bytes) {
 
 struct Launch {
   cudaStream_t stream;
-  int threads;   // block size for row kernels
+  int threads;       // block size for row kernels
+  int members = 1;   // ensemble members of one launch (grid z; member-batched kernels)
 };
+
+// Launch f(std::true_type) when the launch covers several members (the
+// member-batched kernel variant, which moves its pointers by the member's
+// offset) and f(std::false_type) otherwise (the single-member variant, whose
+// pointers stay in the parameter bank).
+template <class F>
+inline void mb_launch(const Launch &L, F &&f) {
+  if (L.members > 1) f(std::true_type{});
+  else f(std::false_type{});
+}
+
+// Member-batched launches: blockIdx.z selects the ensemble member.  The
+// members' arena blocks are carved identically one after the other, so every
+// member-owned pointer of member m is member 0's plus m * g.mstride bytes.
+__device__ __forceinline__ size_t member_offset(const DGrid &g) { return (size_t)blockIdx.z * g.mstride; }
+template <class T>
+__device__ __forceinline__ T *mshift(T *p, size_t mo) {
+  return p ? reinterpret_cast<T *>(reinterpret_cast<uintptr_t>(p) + mo) : p;
+}
+template <class R>
+__device__ __forceinline__ void to_member(const DGrid &g, Slot<R> &s) {
+  const size_t mo = member_offset(g);
+  s.u_lon = mshift(s.u_lon, mo); s.v_lat = mshift(s.v_lat, mo); s.u_f = mshift(s.u_f, mo); s.v_f = mshift(s.v_f, mo);
+  s.pt = mshift(s.pt, mo); s.gz = mshift(s.gz, mo); s.gz_f = mshift(s.gz_f, mo);
+  s.phs = mshift(s.phs, mo); s.phs_f = mshift(s.phs_f, mo); s.psr = mshift(s.psr, mo);
+  s.mfx_lon = mshift(s.mfx_lon, mo); s.mfy_lat = mshift(s.mfy_lat, mo);
+  s.pv = mshift(s.pv, mo); s.pv_lon = mshift(s.pv_lon, mo); s.pv_lat = mshift(s.pv_lat, mo);
+  s.we_lev = mshift(s.we_lev, mo); s.gzs = mshift(s.gzs, mo);
+}
+template <class R>
+__device__ __forceinline__ void to_member(const DGrid &g, Work<R> &w) {
+  const size_t mo = member_offset(g);
+  w.u_lat = mshift(w.u_lat, mo); w.v_lon = mshift(w.v_lon, mo); w.ke = mshift(w.ke, mo);
+  w.cflx = mshift(w.cflx, mo); w.cfly = mshift(w.cfly, mo); w.cflz = mshift(w.cflz, mo);
+  w.divx = mshift(w.divx, mo); w.divy = mshift(w.divy, mo);
+  w.qmfx = mshift(w.qmfx, mo); w.qmfy = mshift(w.qmfy, mo); w.qx = mshift(w.qx, mo); w.qy = mshift(w.qy, mo);
+  w.ptf_lon = mshift(w.ptf_lon, mo); w.ptf_lat = mshift(w.ptf_lat, mo);
+  w.du = mshift(w.du, mo); w.dv = mshift(w.dv, mo); w.dpt = mshift(w.dpt, mo); w.dgz = mshift(w.dgz, mo);
+  w.dphs = mshift(w.dphs, mo); w.ph_exn_lev = mshift(w.ph_exn_lev, mo); w.gz_lev = mshift(w.gz_lev, mo);
+  w.pea = mshift(w.pea, mo); w.gzhl = mshift(w.gzhl, mo); w.gzs = mshift(w.gzs, mo);
+}
 
 // ---- dynamics (dyn.cu) ----------------------------------------------------
 template <class R> void launch_mass_flux(const DGrid &g, const Launch &L, const Slot<R> &s);

@@ -255,13 +255,26 @@ int gmc_host_unregister(void *ptr);
 
 /* Timing of the last gmc_step call: device time between CUDA events
  * recorded on the context's stream around the whole call, and the number
- * of kernels it launched. */
+ * of kernels it launched.  An ensemble context (n_members > 1) times its
+ * launch layouts on its first steps and keeps the fastest: layout 0 launches
+ * each member's kernels separately over up to 8 streams; layout G > 0 runs G
+ * groups of members, each group one member-batched launch per operator on its
+ * own stream.  All layouts give identical results. */
 typedef struct gmc_stats {
   double step_ms;           /* device time of the last gmc_step, all steps  */
   int64_t steps;            /* steps in that call                            */
   int64_t kernel_launches;  /* kernels launched by that call                 */
+  int32_t member_layout;    /* launch layout in use (see above)              */
+  int32_t layout_tuned;     /* 1 once the layout is chosen                   */
 } gmc_stats;
 int gmc_get_stats(const gmc_ctx *ctx, gmc_stats *out);
+
+/* Launch layout of an ensemble context (see gmc_stats): -1 times the
+ * candidates on the next steps and keeps the fastest (the default), 0 or
+ * G = 1, 2, 4, 8 (at most n_members) fixes it.  Results do not depend on the
+ * layout.  GMC_EINVAL for a layout this context cannot run.  No reference
+ * counterpart (a launch option). */
+int gmc_set_member_layout(gmc_ctx *ctx, int32_t layout);
 
 /* Per-kernel device timing: when enabled, every kernel launch is bracketed
  * by CUDA events on the context stream and its duration accumulated under
@@ -298,6 +311,12 @@ int gmc_filter_taps(const gmc_config *cfg, int32_t which, int32_t lat, int32_t *
 int gmc_make_ic(const gmc_config *cfg, int32_t kind, uint64_t seed, double noise_k,
                 double *u_lon, double *v_lat, double *pt_or_gz, double *phs,
                 double *gzs, double *q);
+
+/* Measured FP64 fused multiply-add throughput of the current device, in
+ * TFLOP/s: independent FMA chains over every SM, timed with CUDA events (no
+ * clock or other setting of the GPU is changed).  No reference counterpart:
+ * it is the peak against which the FP64 form's kernels are placed. */
+int gmc_fp64_fma_peak(double *tflops);
 
 #ifdef __cplusplus
 }

@@ -86,6 +86,8 @@ module gmcore_gpu_mod
     real(c_double)     :: step_ms
     integer(c_int64_t) :: steps
     integer(c_int64_t) :: kernel_launches
+    integer(c_int32_t) :: member_layout
+    integer(c_int32_t) :: layout_tuned
   end type gmc_stats
 
   interface
@@ -216,6 +218,12 @@ module gmcore_gpu_mod
       type(gmc_stats), intent(out) :: out
     end function gmc_get_stats
 
+    integer(c_int) function gmc_set_member_layout(ctx, layout) bind(c, name='gmc_set_member_layout')
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: layout
+    end function gmc_set_member_layout
+
     integer(c_int) function gmc_set_profiling(ctx, on) bind(c, name='gmc_set_profiling')
       import
       type(c_ptr), value :: ctx
@@ -269,6 +277,12 @@ module gmcore_gpu_mod
       real(c_double), value :: noise_k
       type(c_ptr), value :: u_lon, v_lat, pt_or_gz, phs, gzs, q
     end function gmc_make_ic
+
+    ! measured FP64 FMA throughput of the current device (TFLOP/s)
+    integer(c_int) function gmc_fp64_fma_peak(tflops) bind(c, name='gmc_fp64_fma_peak')
+      import
+      real(c_double), intent(out) :: tflops
+    end function gmc_fp64_fma_peak
 
     integer(c_size_t) function c_strlen(s) bind(c, name='strlen')
       import
