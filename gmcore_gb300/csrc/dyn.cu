@@ -675,7 +675,7 @@ __global__ void k_momentum_tend(DGrid g, Slot<R> s, Work<R> w) {
 // base pointers stay in the parameter bank, so the kernel fits in 32
 // registers) and the divisions taken as reciprocal products (fdiv).
 template <bool MB>
-__global__ void GMC_BOUNDS_FMB(8, 5, MB) k_momentum_f(DGrid g, const float *__restrict__ mfx, const float *__restrict__ mfy,
+__global__ void GMC_BOUNDS_FMB(5, 5, MB) k_momentum_f(DGrid g, const float *__restrict__ mfx, const float *__restrict__ mfy,
                                              const float *__restrict__ pvlon, const float *__restrict__ pvlat,
                                              const float *__restrict__ ke, const float *__restrict__ we,
                                              const float *__restrict__ uf, const float *__restrict__ vf,
@@ -687,6 +687,20 @@ __global__ void GMC_BOUNDS_FMB(8, 5, MB) k_momentum_f(DGrid g, const float *__re
   const bool cor1 = g.coriolis_scheme == 1;
   const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
   const unsigned lf = (unsigned)nlat * nlon, lh = (unsigned)nhalf * nlon;   // level strides
+  // Each thread takes two neighbouring points i0, i0 + 1 (nlon is even and
+  // row offsets are multiples of nlon, so the pair is one aligned 8-byte
+  // load) and the stencil's third column as one more value: three values of a
+  // row for two points where the single-point form loads four.
+  struct T3 { float a, b, c; };
+  auto east = [nlon](const float *__restrict__ p, unsigned o, int i0) {   // values at i0, i0+1, i0+2
+    const float2 t = *reinterpret_cast<const float2 *>(p + o + i0);
+    return T3{t.x, t.y, p[o + (i0 + 2 == nlon ? 0 : i0 + 2)]};
+  };
+  auto west = [nlon](const float *__restrict__ p, unsigned o, int i0) {   // values at i0-1, i0, i0+1
+    const float2 t = *reinterpret_cast<const float2 *>(p + o + i0);
+    return T3{p[o + (i0 == 0 ? nlon - 1 : i0 - 1)], t.x, t.y};
+  };
+  auto pair = [](const float *__restrict__ p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o); };
   // blocks 0 .. nlat-3: du on full rows 2 .. nlat-1; then dv on half rows 1 .. nhalf
   const bool urow = (int)blockIdx.x < nlat - 2;
   const int j = urow ? blockIdx.x + 2 : blockIdx.x - (nlat - 2) + 1;
@@ -695,22 +709,34 @@ __global__ void GMC_BOUNDS_FMB(8, 5, MB) k_momentum_f(DGrid g, const float *__re
     const float aw = ROWR(float, area_lon_west, j), ae = ROWR(float, area_lon_east, j), al = ROWR(float, area_lon, j);
     const unsigned hs = (unsigned)ix3(nhalf, nlon, 1, j - 1, k), hn = hs + nlon;   // half rows j-1, j
     const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k), po = (unsigned)(j - 1) * nlon;
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
-      const int ip = i0 + 1 == nlon ? 0 : i0 + 1;
-      const float pl = pvlon[fo + i0];
-      float qhv;
-      if (cor1)
-        qhv = (t1 * (mfy[hs + i0] * (pl + pvlat[hs + i0]) + mfy[hs + ip] * (pl + pvlat[hs + ip])) +
-               t2 * (mfy[hn + i0] * (pl + pvlat[hn + i0]) + mfy[hn + ip] * (pl + pvlat[hn + ip]))) * 0.5f;
-      else
-        qhv = (t1 * (mfy[hs + i0] + mfy[hs + ip]) + t2 * (mfy[hn + i0] + mfy[hn + ip])) * pl;
-      const float d = qhv - fdiv(ke[fo + ip] - ke[fo + i0], de);
-      const float m_lon = (fmaf(dB, psr[po + i0], dA) + fmaf(dB, psr[po + ip], dA)) * 0.5f;
-      const float u0 = uf[fo + i0];
-      float wd = 0;
-      if (k < nlev) wd = fdiv(aw * we[fo + lf + i0] + ae * we[fo + lf + ip], al) * (uf[fo + lf + i0] - u0);
-      if (k > 1) wd += fdiv(aw * we[fo + i0] + ae * we[fo + ip], al) * (u0 - uf[fo - lf + i0]);
-      du[fo + i0] = d - fdiv(wd, m_lon) * 0.5f;
+    for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+      const float2 pl2 = pair(pvlon, fo + i0), u2 = pair(uf, fo + i0);
+      const T3 ms = east(mfy, hs, i0), ps = east(pvlat, hs, i0), mn = east(mfy, hn, i0), pn = east(pvlat, hn, i0);
+      const T3 ke3 = east(ke, fo, i0), pr = east(psr, po, i0);
+      T3 wu{0, 0, 0}, wl{0, 0, 0};
+      float2 uu = make_float2(0, 0), ul = make_float2(0, 0);
+      if (k < nlev) { wl = east(we, fo + lf, i0); ul = pair(uf, fo + lf + i0); }
+      if (k > 1) { wu = east(we, fo, i0); uu = pair(uf, fo - lf + i0); }
+      float out[2];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {   // point i0 + p: its own column and the next (ip)
+        const float pl = p ? pl2.y : pl2.x;
+        const float ms0 = p ? ms.b : ms.a, ms1 = p ? ms.c : ms.b, ps0 = p ? ps.b : ps.a, ps1 = p ? ps.c : ps.b;
+        const float mn0 = p ? mn.b : mn.a, mn1 = p ? mn.c : mn.b, pn0 = p ? pn.b : pn.a, pn1 = p ? pn.c : pn.b;
+        float qhv;
+        if (cor1)
+          qhv = (t1 * (ms0 * (pl + ps0) + ms1 * (pl + ps1)) + t2 * (mn0 * (pl + pn0) + mn1 * (pl + pn1))) * 0.5f;
+        else
+          qhv = (t1 * (ms0 + ms1) + t2 * (mn0 + mn1)) * pl;
+        const float d = qhv - fdiv((p ? ke3.c : ke3.b) - (p ? ke3.b : ke3.a), de);
+        const float m_lon = (fmaf(dB, p ? pr.b : pr.a, dA) + fmaf(dB, p ? pr.c : pr.b, dA)) * 0.5f;
+        const float u0 = p ? u2.y : u2.x;
+        float wd = 0;
+        if (k < nlev) wd = fdiv(aw * (p ? wl.b : wl.a) + ae * (p ? wl.c : wl.b), al) * ((p ? ul.y : ul.x) - u0);
+        if (k > 1) wd += fdiv(aw * (p ? wu.b : wu.a) + ae * (p ? wu.c : wu.b), al) * (u0 - (p ? uu.y : uu.x));
+        out[p] = d - fdiv(wd, m_lon) * 0.5f;
+      }
+      *reinterpret_cast<float2 *>(du + fo + i0) = make_float2(out[0], out[1]);
     }
     return;
   }
@@ -719,22 +745,34 @@ __global__ void GMC_BOUNDS_FMB(8, 5, MB) k_momentum_f(DGrid g, const float *__re
     const float an = ROWR(float, area_lat_north, j), as = ROWR(float, area_lat_south, j), al = ROWR(float, area_lat, j);
     const unsigned fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon;   // full rows j, j+1
     const unsigned ho = (unsigned)ix3(nhalf, nlon, 1, j, k), ps = (unsigned)(j - 1) * nlon, pn = ps + nlon;
-    for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
-      const int im = i0 == 0 ? nlon - 1 : i0 - 1;
-      const float pl = pvlat[ho + i0];
-      float qhu;
-      if (cor1)
-        qhu = (t1 * (mfx[fs + im] * (pl + pvlon[fs + im]) + mfx[fs + i0] * (pl + pvlon[fs + i0])) +
-               t2 * (mfx[fn + im] * (pl + pvlon[fn + im]) + mfx[fn + i0] * (pl + pvlon[fn + i0]))) * 0.5f;
-      else
-        qhu = (t1 * (mfx[fs + im] + mfx[fs + i0]) + t2 * (mfx[fn + im] + mfx[fn + i0])) * pl;
-      const float d = -qhu - fdiv(ke[fn + i0] - ke[fs + i0], de);
-      const float m_lat = (fmaf(dB, psr[ps + i0], dA) + fmaf(dB, psr[pn + i0], dA)) * 0.5f;
-      const float v0 = vf[ho + i0];
-      float wd = 0;
-      if (k < nlev) wd = fdiv(an * we[fn + lf + i0] + as * we[fs + lf + i0], al) * (vf[ho + lh + i0] - v0);
-      if (k > 1) wd += fdiv(an * we[fn + i0] + as * we[fs + i0], al) * (v0 - vf[ho - lh + i0]);
-      dv[ho + i0] = d - fdiv(wd, m_lat) * 0.5f;
+    for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+      const float2 pl2 = pair(pvlat, ho + i0), v2 = pair(vf, ho + i0);
+      const T3 xs = west(mfx, fs, i0), qs = west(pvlon, fs, i0), xn = west(mfx, fn, i0), qn = west(pvlon, fn, i0);
+      const float2 kn = pair(ke, fn + i0), ks = pair(ke, fs + i0), rs = pair(psr, ps + i0), rn = pair(psr, pn + i0);
+      float2 wnl = make_float2(0, 0), wsl = make_float2(0, 0), wnu = make_float2(0, 0), wsu = make_float2(0, 0);
+      float2 vl = make_float2(0, 0), vu = make_float2(0, 0);
+      if (k < nlev) { wnl = pair(we, fn + lf + i0); wsl = pair(we, fs + lf + i0); vl = pair(vf, ho + lh + i0); }
+      if (k > 1) { wnu = pair(we, fn + i0); wsu = pair(we, fs + i0); vu = pair(vf, ho - lh + i0); }
+      float out[2];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {   // point i0 + p: the previous column (im) and its own
+        const float pl = p ? pl2.y : pl2.x;
+        const float xs0 = p ? xs.b : xs.a, xs1 = p ? xs.c : xs.b, qs0 = p ? qs.b : qs.a, qs1 = p ? qs.c : qs.b;
+        const float xn0 = p ? xn.b : xn.a, xn1 = p ? xn.c : xn.b, qn0 = p ? qn.b : qn.a, qn1 = p ? qn.c : qn.b;
+        float qhu;
+        if (cor1)
+          qhu = (t1 * (xs0 * (pl + qs0) + xs1 * (pl + qs1)) + t2 * (xn0 * (pl + qn0) + xn1 * (pl + qn1))) * 0.5f;
+        else
+          qhu = (t1 * (xs0 + xs1) + t2 * (xn0 + xn1)) * pl;
+        const float d = -qhu - fdiv((p ? kn.y : kn.x) - (p ? ks.y : ks.x), de);
+        const float m_lat = (fmaf(dB, p ? rs.y : rs.x, dA) + fmaf(dB, p ? rn.y : rn.x, dA)) * 0.5f;
+        const float v0 = p ? v2.y : v2.x;
+        float wd = 0;
+        if (k < nlev) wd = fdiv(an * (p ? wnl.y : wnl.x) + as * (p ? wsl.y : wsl.x), al) * ((p ? vl.y : vl.x) - v0);
+        if (k > 1) wd += fdiv(an * (p ? wnu.y : wnu.x) + as * (p ? wsu.y : wsu.x), al) * (v0 - (p ? vu.y : vu.x));
+        out[p] = d - fdiv(wd, m_lat) * 0.5f;
+      }
+      *reinterpret_cast<float2 *>(dv + ho + i0) = make_float2(out[0], out[1]);
     }
   }
 }
@@ -1316,7 +1354,7 @@ template <class R>
 void launch_momentum_tend(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
   if constexpr (std::is_same<R, float>::value) {
     if (g.baroclinic) {
-      mb_launch(L, [&](auto mb) { k_momentum_f<decltype(mb)::value><<<dim3(g.nlat - 2 + g.nhalf, g.nlev, L.members), 256, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
+      mb_launch(L, [&](auto mb) { k_momentum_f<decltype(mb)::value><<<dim3(g.nlat - 2 + g.nhalf, g.nlev, L.members), 128, 0, L.stream>>>(g, s.mfx_lon, s.mfy_lat, s.pv_lon, s.pv_lat, w.ke, s.we_lev,
                                                               s.u_f, s.v_f, s.psr, w.du, w.dv); });
       return;
     }
