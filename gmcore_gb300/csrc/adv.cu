@@ -303,6 +303,16 @@ __global__ void GMC_BOUNDS(R, 6) k_ffsl_x2(DGrid g, const R *__restrict__ u, con
   R *fr = ss + 2 * (nlon + 3) + 1;         // inner fluxes of q, fr[-1 .. nlon-1]
   const R *mul[2] = {u, mfx};
   const R *fld[2] = {q, qy};
+  const unsigned ro = (unsigned)ix3(nlat, nlon, 1, j, k);
+  // divx of this thread's first cells, requested now: it is read only after
+  // the fluxes, behind two barriers
+  constexpr int kPreD = 3;
+  R dpre[kPreD];
+#pragma unroll
+  for (int t = 0; t < kPreD; ++t) {
+    const int i0 = threadIdx.x + t * blockDim.x;
+    dpre[t] = i0 < nlon ? divx[ro + i0] : (R)0;
+  }
   hflx_xrows<2, R>(g, j, k, mul, cflx, fld, xs, ss, [&](int i0, unsigned o, const R (&f)[2]) {
     fr[i0] = f[0];
     if (i0 == nlon - 1) fr[-1] = f[0];
@@ -310,12 +320,17 @@ __global__ void GMC_BOUNDS(R, 6) k_ffsl_x2(DGrid g, const R *__restrict__ u, con
   });
   __syncthreads();
   const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j);
-  const unsigned ro = (unsigned)ix3(nlat, nlon, 1, j, k);
   const R *X = xs + 2;
-  for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
+  auto update = [&](int i0, R dv) {
     const R qv = X[i0];
-    qx[ro + i0] = qv - (R)0.5 * (fdiv((fr[i0] - fr[i0 - 1]) * lel, ac) - divx[ro + i0] * qv) * hdt;
+    qx[ro + i0] = qv - (R)0.5 * (fdiv((fr[i0] - fr[i0 - 1]) * lel, ac) - dv * qv) * hdt;
+  };
+#pragma unroll
+  for (int t = 0; t < kPreD; ++t) {
+    const int i0 = threadIdx.x + t * blockDim.x;
+    if (i0 < nlon) update(i0, dpre[t]);
   }
+  for (int i0 = threadIdx.x + kPreD * blockDim.x; i0 < nlon; i0 += blockDim.x) update(i0, divx[ro + i0]);
 }
 
 // y: one column per thread marching north through a band of full rows

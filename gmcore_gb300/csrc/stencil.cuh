@@ -278,7 +278,8 @@ __device__ __forceinline__ bool filter_rows(const FilterDev &f, bool full_lat, i
       e0[kk] = (A)ext[kk * es + b];
       e1[kk] = (A)ext[kk * es + b + 1];
     }
-    for (int t = 0; t < n; ++t) {
+#pragma unroll 4
+    for (int t = 0; t < n; ++t) {   // unrolled: the weights of four taps are requested together
       const A wt = w[t];
 #pragma unroll
       for (int kk = 0; kk < KB; ++kk) {
