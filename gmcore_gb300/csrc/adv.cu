@@ -837,7 +837,34 @@ __global__ void GMC_BOUNDS(R, 8) k_tracer_horizontal(DGrid g, const R *q_old, R 
   const R lel = ROWR(R, le_lon, j), ac = ROWR(R, area_cell, j), la0 = ROWR(R, le_lat, j), la1 = ROWR(R, le_lat, j - 1);
   const R dta = (R)dt_adv;
   bool neg = false;
-  for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (!is_pole) {
+      // Two points per thread (0-based i0, i0+1): paired loads of q_old, the
+      // fluxes and the surface pressures, the west flux column as one scalar;
+      // the per-point arithmetic is the loop's below.
+      const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k), hn = (unsigned)ix3(nhalf, nlon, 1, j, k), hs = hn - nlon;
+      const unsigned po = (unsigned)(j - 1) * nlon;
+      const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
+      for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+        auto P2 = [&](const float *p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o + i0); };
+        const float2 qo = P2(q_old, fo), fx2 = P2(fx, fo), fyn = P2(fy, hn), fys = P2(fy, hs);
+        const float2 pso = P2(old_sp.psr, po), psn = P2(sp.psr, po);
+        const float fxw = fx[fo + (i0 == 0 ? nlon - 1 : i0 - 1)];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const float om = fmaf(dB, p ? pso.y : pso.x, dA), m = fmaf(dB, p ? psn.y : psn.x, dA);
+          const float a = ((p ? fx2.y : fx2.x) - (p ? fx2.x : fxw)) * lel;
+          const float b = (p ? fyn.y : fyn.x) * la0 - (p ? fys.y : fys.x) * la1;
+          float qn = om * (p ? qo.y : qo.x) - (a + b) / ac * dta;
+          qn = qn / m;
+          row[i0 + 1 + p] = qn;
+          mrow[i0 + 1 + p] = m;
+          neg |= qn < 0;
+        }
+      }
+    }
+  }
+  for (int i = 1 + threadIdx.x; i <= nlon && !(std::is_same<R, float>::value && !is_pole); i += blockDim.x) {
     const size_t o = ix3(nlat, nlon, i, j, k);
     const size_t c2 = (size_t)(j - 1) * nlon + (i - 1);
     R om = Mass<R>::layer(g, k, old_sp.at(c2));
@@ -1169,7 +1196,8 @@ template <class R>
 void launch_tracer_horizontal(const DGrid &g, const Launch &L, const R *q_old, R *q_new, const R *fx, const R *fy,
                               const SurfP<R> &old_sp, const SurfP<R> &sp, double dt_adv) {
   size_t smem = 32 * sizeof(double) + 2 * (g.nlon + 2) * sizeof(R) + 16;
-  k_tracer_horizontal<R><<<dim3(g.nlat, g.nlev), L.threads, smem, L.stream>>>(g, q_old, q_new, fx, fy, old_sp, sp, dt_adv);
+  const int bt = std::is_same<R, float>::value ? 128 : L.threads;   // FP32: two points per thread
+  k_tracer_horizontal<R><<<dim3(g.nlat, g.nlev), bt, smem, L.stream>>>(g, q_old, q_new, fx, fy, old_sp, sp, dt_adv);
 }
 
 template <class R>

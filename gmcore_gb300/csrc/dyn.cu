@@ -90,7 +90,7 @@ __global__ void GMC_BOUNDS_MB(R, 8, MB) k_tangent_winds(DGrid g, Slot<R> s, Work
 // calc_ke (operators_mod.F90:234-352): cell KE, optionally blended with the
 // four vertex KEs (ke_scheme 2); pole cells take the ring mean of v^2.
 template <class R, bool MB>
-__global__ void GMC_BOUNDS(R, 6) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
+__global__ void GMC_BOUNDS(R, 5) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w) {
   if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   __shared__ double red[32];
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
@@ -120,6 +120,38 @@ __global__ void GMC_BOUNDS(R, 6) k_kinetic_energy(DGrid g, Slot<R> s, Work<R> w)
           aosn = ROWR(R, area_lon_south, j + 1);
   const R av = ROWR(R, area_vtx, j), av1 = ROWR(R, area_vtx, j - 1), as2 = ROWR(R, area_subcell2, j),
           as1 = ROWR(R, area_subcell1, j);
+  if constexpr (std::is_same<R, float>::value) {
+    // Two points per thread (i0, i0+1): each row's columns i0-1 .. i0+2 as one
+    // paired load and the scalars around it; the per-point arithmetic below is
+    // the single-point form's.
+    for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+      const int im = i0 == 0 ? nlon - 1 : i0 - 1, i2 = i0 + 2 == nlon ? 0 : i0 + 2;
+      auto P2 = [&](const float *p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o + i0); };
+      const float2 uc2 = P2(u, uc), un2 = P2(u, un), us2 = P2(u, us), vc2 = P2(v, vc), vs2 = P2(v, vs);
+      const float ucw = u[uc + im], unw = u[un + im], usw = u[us + im];
+      const float vcw = v[vc + im], vsw = v[vs + im], vce = v[vc + i2], vse = v[vs + i2];
+      float out[2];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        // columns im, i0, ip of point i0 + p
+        const float uw = p ? uc2.x : ucw, ue = p ? uc2.y : uc2.x;
+        const float vsc = p ? vs2.y : vs2.x, vnc = p ? vc2.y : vc2.x;
+        float ke = fdiv(alw * sq(uw) + ale * sq(ue) + aln * sq(vsc) + als * sq(vnc), ac);
+        if (vtx) {
+          const float v_cm = p ? vc2.x : vcw, v_sm = p ? vs2.x : vsw, v_sp = p ? vse : vs2.y, v_cp = p ? vce : vc2.y;
+          const float u_nm = p ? un2.x : unw, u_sm = p ? us2.x : usw, u_s0 = p ? us2.y : us2.x, u_n0 = p ? un2.y : un2.x;
+          const float k1 = fdiv(ate * sq(v_cm) + atw * sq(vnc) + aon * sq(uw) + aosn * sq(u_nm), av);
+          const float k2 = fdiv(ate1 * sq(v_sm) + atw1 * sq(vsc) + aon1 * sq(u_sm) + aos * sq(uw), av1);
+          const float k3 = fdiv(ate1 * sq(vsc) + atw1 * sq(v_sp) + aon1 * sq(u_s0) + aos * sq(ue), av1);
+          const float k4 = fdiv(ate * sq(vnc) + atw * sq(v_cp) + aon * sq(ue) + aosn * sq(u_n0), av);
+          ke = fdiv((1.0f - cw) * ((k1 + k4) * as2 + (k2 + k3) * as1), ac) + cw * ke;
+        }
+        out[p] = ke;
+      }
+      *reinterpret_cast<float2 *>(w.ke + uc + i0) = make_float2(out[0], out[1]);
+    }
+    return;
+  }
   for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
     const int im = i0 == 0 ? nlon - 1 : i0 - 1, ip = i0 + 1 == nlon ? 0 : i0 + 1;
     const R uw = u[uc + im], ue = u[uc + i0], vsc = v[vs + i0], vnc = v[vc + i0];
@@ -1090,6 +1122,20 @@ __device__ __forceinline__ bool filter_on(const FilterDev &f, bool full_lat, int
   return (full_lat ? f.ntaps_full[j - 1] : f.ntaps_half[j - 1]) > 1;
 }
 
+// FP32 Lin97 pressure-gradient force at two neighbouring edges, pgf_pq(p, q)
+// and pgf_pq(p2, q2), from the Exner pressures and geopotentials at the four
+// distinct points p, p2 (= p + 1 along a row) and q, q2 of a level and the
+// level below (lf further); pa_* / gz_* hold those values.  The same
+// operations as two pgf_pq calls.
+__device__ __forceinline__ float pgf_from(float pa_p, float pa_q, float pa_pl, float pa_ql, float2 gz_p, float2 gz_q,
+                                          float2 gz_pl, float2 gz_ql, float dref, float inv_d) {
+  const float dph1 = dref + (pa_ql - pa_p);
+  const float dph2 = dref + (pa_pl - pa_q);
+  const float dgz1 = hl_diff(gz_pl, gz_q);
+  const float dgz2 = hl_diff(gz_p, gz_ql);
+  return fdiv(-(dph1 * dgz1 + dph2 * dgz2) * inv_d, dph1 + dph2);
+}
+
 // Each row is staged in shared memory (also where no filter touches it: the
 // stores then do not order the next points' loads behind them).  A block takes
 // one row at kUvLevels(R) consecutive levels, so that the filters load each
@@ -1147,8 +1193,34 @@ __global__ void GMC_BOUNDS_MB(R, 6, MB) k_update_uv(DGrid g, Slot<R> o, Slot<R> 
       return o.u_lon[c0 + i0] + dtr * (w.du[c0 + i0] - p);
     };
     const bool small = bc && filter_on(g.small2, true, j), big = filter_on(g.big, true, j);
-    for (int kk = 0; kk < nk; ++kk)
-      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[kk * nlon + i0] = val(kk, i0);
+    bool done = false;
+    if constexpr (std::is_same<R, float>::value) {
+      if (bc) {   // two points per thread: the pairs (i0, i0+1) and column i0+2 of each row, paired loads
+        const float *__restrict__ pa = w.pea;
+        const float2 *__restrict__ gz = w.gzhl;
+        for (int kk = 0; kk < nk; ++kk) {
+          const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k0 + kk);
+          for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+            const unsigned a = c0 + i0, e = c0 + (i0 + 2 == nlon ? 0 : i0 + 2);
+            const float2 pk = *reinterpret_cast<const float2 *>(pa + a), pl = *reinterpret_cast<const float2 *>(pa + a + lf);
+            const float pke = pa[e], ple = pa[e + lf];
+            const float4 gk = *reinterpret_cast<const float4 *>(gz + a), gl = *reinterpret_cast<const float4 *>(gz + a + lf);
+            const float2 gke = gz[e], gle = gz[e + lf];
+            const float2 u2 = *reinterpret_cast<const float2 *>(o.u_lon + a), d2 = *reinterpret_cast<const float2 *>(w.du + a);
+            const float p0 = pgf_from(pk.x, pk.y, pl.x, pl.y, make_float2(gk.x, gk.y), make_float2(gk.z, gk.w),
+                                      make_float2(gl.x, gl.y), make_float2(gl.z, gl.w), dref[kk], inv_d);
+            const float p1 = pgf_from(pk.y, pke, pl.y, ple, make_float2(gk.z, gk.w), gke, make_float2(gl.z, gl.w), gle,
+                                      dref[kk], inv_d);
+            *reinterpret_cast<float2 *>(row + kk * nlon + i0) =
+                make_float2(u2.x + dtr * (d2.x - p0), u2.y + dtr * (d2.y - p1));
+          }
+        }
+        done = true;
+      }
+    }
+    if (!done)
+      for (int kk = 0; kk < nk; ++kk)
+        for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) row[kk * nlon + i0] = val(kk, i0);
     if (small) filt(g.small2, true, j, row);
     __syncthreads();
     for (int kk = 0; kk < nk; ++kk) {
@@ -1185,8 +1257,38 @@ __global__ void GMC_BOUNDS_MB(R, 6, MB) k_update_uv(DGrid g, Slot<R> o, Slot<R> 
   };
   auto load_v = [&](int jj, R *dst) {
     const R inv_d = (R)1 / ROWR(R, de_lat, jj);
-    for (int kk = 0; kk < nk; ++kk)
-      for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) dst[kk * nlon + i0] = vval(kk, jj, inv_d, i0);
+    bool done = false;
+    if constexpr (std::is_same<R, float>::value) {
+      if (bc) {   // two points per thread, paired loads of the full rows jj, jj+1 at both levels
+        const float *__restrict__ pa = w.pea;
+        const float2 *__restrict__ gz = w.gzhl;
+        for (int kk = 0; kk < nk; ++kk) {
+          const int k = k0 + kk;
+          const unsigned cv = (unsigned)ix3(nhalf, nlon, 1, jj, k), ps = (unsigned)ix3(nlat, nlon, 1, jj, k);
+          for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+            const unsigned pp = ps + i0, qq = pp + nlon;
+            const float2 ap = *reinterpret_cast<const float2 *>(pa + pp), aq = *reinterpret_cast<const float2 *>(pa + qq);
+            const float2 apl = *reinterpret_cast<const float2 *>(pa + pp + lf),
+                         aql = *reinterpret_cast<const float2 *>(pa + qq + lf);
+            const float4 gp = *reinterpret_cast<const float4 *>(gz + pp), gq = *reinterpret_cast<const float4 *>(gz + qq);
+            const float4 gpl = *reinterpret_cast<const float4 *>(gz + pp + lf),
+                         gql = *reinterpret_cast<const float4 *>(gz + qq + lf);
+            const float2 v2 = *reinterpret_cast<const float2 *>(o.v_lat + cv + i0),
+                         d2 = *reinterpret_cast<const float2 *>(w.dv + cv + i0);
+            const float p0 = pgf_from(ap.x, aq.x, apl.x, aql.x, make_float2(gp.x, gp.y), make_float2(gq.x, gq.y),
+                                      make_float2(gpl.x, gpl.y), make_float2(gql.x, gql.y), dref[kk], inv_d);
+            const float p1 = pgf_from(ap.y, aq.y, apl.y, aql.y, make_float2(gp.z, gp.w), make_float2(gq.z, gq.w),
+                                      make_float2(gpl.z, gpl.w), make_float2(gql.z, gql.w), dref[kk], inv_d);
+            *reinterpret_cast<float2 *>(dst + kk * nlon + i0) =
+                make_float2(v2.x + dtr * (d2.x - p0), v2.y + dtr * (d2.y - p1));
+          }
+        }
+        done = true;
+      }
+    }
+    if (!done)
+      for (int kk = 0; kk < nk; ++kk)
+        for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) dst[kk * nlon + i0] = vval(kk, jj, inv_d, i0);
     if (bc) filt(g.small2, false, jj, dst);
     __syncthreads();
   };
@@ -1322,7 +1424,9 @@ void launch_tangent_winds(const DGrid &g, const Launch &L, const Slot<R> &s, con
 }
 template <class R>
 void launch_kinetic_energy(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  mb_launch(L, [&](auto mb) { k_kinetic_energy<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
+  // FP32: two points per thread, so smaller blocks
+  const int bt = std::is_same<R, float>::value ? 128 : L.threads;
+  mb_launch(L, [&](auto mb) { k_kinetic_energy<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), bt, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
