@@ -594,6 +594,10 @@ __device__ R vflx_tile(const DGrid &g, const R *C, const R *FL, const R *DF, con
   return 0;
 }
 
+// Interfaces per thread whose vertical inputs the column-tile kernels request
+// at their start (levels are spread over kTileK thread rows: 5 covers 39 levels).
+constexpr int kColPre = 5;
+
 // FP32 form of k_pt_tendency over column tiles: the pt column with its
 // extrapolated ghost levels, slopes, limited cell coefficients and interface
 // fluxes are built in shared memory phase by phase, each phase parallel over
@@ -618,6 +622,19 @@ __global__ void GMC_BOUNDS_F(8) k_pt_tendency_f(DGrid g, Slot<float> s, Work<flo
   float *FZ = F6 + nlev * ld;                             // interface flux k at [(k-1)*ld], k = 1 .. nlev+1
   if (pole) tile_pole_ring(g, j, ring, [&](int ii, int jv, int k) { return w.ptf_lat[ix3(nhalf, nlon, ii, jv, k)]; });
   for (int k = 1 + kt; k <= nlev; k += KT) C[(k + 1) * ld] = s.pt[ix3(nlat, nlon, ic, j, k)];
+  // the Courant numbers and mass fluxes of this thread's interfaces, requested
+  // with the column so that their latency overlaps the reconstruction below
+  float cz[kColPre], wz[kColPre];
+#pragma unroll
+  for (int m = 0; m < kColPre; ++m) {
+    const int k = 1 + kt + m * KT;
+    cz[m] = wz[m] = 0;
+    if (k >= 2 && k <= nlev) {
+      const size_t ol = ix3(nlat, nlon, ic, j, k);
+      cz[m] = w.cflz[ol];
+      wz[m] = s.we_lev[ol];
+    }
+  }
   __syncthreads();
   if (kt == 0) {   // ghost levels by linear extrapolation
     C[1 * ld] = 2.0f * C[2 * ld] - C[3 * ld];                         // C(0)
@@ -638,25 +655,35 @@ __global__ void GMC_BOUNDS_F(8) k_pt_tendency_f(DGrid g, Slot<float> s, Work<flo
     F6[(l - 1) * ld] = f6;
   }
   __syncthreads();
-  for (int k = 1 + kt; k <= nlev + 1; k += KT) {
+  // vertical flux at interface k (2 .. nlev) with Courant number c and mass flux wv
+  auto flux_at = [&](int k, float c, float wv) {
     float fz = 0;
-    if (k != 1 && k != nlev + 1) {
-      const size_t ol = ix3(nlat, nlon, ic, j, k);
-      const float c = w.cflz[ol], wv = s.we_lev[ol];
-      if (fabsf(c) < 1.0f && g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 or k
-        if (c > 0) fz = fdiv(wv * (c * (C[k * ld] + S[(k - 1) * ld] * 0.5f * (1.0f - c))), c);
-        else if (c < 0) fz = fdiv(wv * (c * (C[(k + 1) * ld] - S[k * ld] * 0.5f * (1.0f + c))), c);
-      } else if (fabsf(c) < 1.0f) {
-        if (c > 0) {
-          const int u = k - 2;   // cell k-1
-          fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
-        } else if (c < 0) {
-          const int u = k - 1;   // cell k
-          fz = fdiv(-wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 0.0f, -c), c);
-        }
-      } else if (valid) {
-        fz = vflx_tile<float>(g, C, FL, DF, F6, ld, k, c, wv);
+    if (fabsf(c) < 1.0f && g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 or k
+      if (c > 0) fz = fdiv(wv * (c * (C[k * ld] + S[(k - 1) * ld] * 0.5f * (1.0f - c))), c);
+      else if (c < 0) fz = fdiv(wv * (c * (C[(k + 1) * ld] - S[k * ld] * 0.5f * (1.0f + c))), c);
+    } else if (fabsf(c) < 1.0f) {
+      if (c > 0) {
+        const int u = k - 2;   // cell k-1
+        fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
+      } else if (c < 0) {
+        const int u = k - 1;   // cell k
+        fz = fdiv(-wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 0.0f, -c), c);
       }
+    } else if (valid) {
+      fz = vflx_tile<float>(g, C, FL, DF, F6, ld, k, c, wv);
+    }
+    return fz;
+  };
+#pragma unroll
+  for (int m = 0; m < kColPre; ++m) {
+    const int k = 1 + kt + m * KT;
+    if (k <= nlev + 1) FZ[(k - 1) * ld] = k != 1 && k != nlev + 1 ? flux_at(k, cz[m], wz[m]) : 0.0f;
+  }
+  for (int k = 1 + kt + kColPre * KT; k <= nlev + 1; k += KT) {
+    float fz = 0;
+    if (k != nlev + 1) {
+      const size_t ol = ix3(nlat, nlon, ic, j, k);
+      fz = flux_at(k, w.cflz[ol], s.we_lev[ol]);
     }
     FZ[(k - 1) * ld] = fz;
   }
@@ -997,6 +1024,19 @@ __global__ void GMC_BOUNDS_F(6) k_tracer_vertical_f(DGrid g, float *q, const flo
     C[(k + 1) * ld] = q[ix3(nlat, nlon, ic, j, k)];
     M[(k - 1) * ld] = Mass<float>::layer(g, k, psr);
   }
+  // the Courant numbers and mass fluxes of this thread's interfaces, requested
+  // with the column so that their latency overlaps the reconstruction below
+  float cz[kColPre], wz[kColPre];
+#pragma unroll
+  for (int m = 0; m < kColPre; ++m) {
+    const int k = 1 + kt + m * KT;
+    cz[m] = wz[m] = 0;
+    if (k >= 2 && k <= nlev) {
+      const size_t ol = ix3(nlat, nlon, ic, j, k);
+      cz[m] = cflz[ol];
+      wz[m] = we[ol];
+    }
+  }
   __syncthreads();
   if (kt == 0) {   // ghost levels copy the end levels
     C[0] = C[1 * ld] = C[2 * ld];
@@ -1015,25 +1055,34 @@ __global__ void GMC_BOUNDS_F(6) k_tracer_vertical_f(DGrid g, float *q, const flo
     F6[(l - 1) * ld] = f6;
   }
   __syncthreads();
-  for (int k = 1 + kt; k <= nlev + 1; k += KT) {
+  auto flux_at = [&](int k, float c, float wv) {   // interface k (2 .. nlev)
     float fz = 0;
-    if (k != 1 && k != nlev + 1) {
-      const size_t ol = ix3(nlat, nlon, ic, j, k);
-      const float c = cflz[ol], wv = we[ol];
-      if (fabsf(c) < 1.0f && g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 or k
-        if (c > 0) fz = fdiv(wv * (c * (C[k * ld] + S[(k - 1) * ld] * 0.5f * (1.0f - c))), c);
-        else if (c < 0) fz = fdiv(wv * (c * (C[(k + 1) * ld] - S[k * ld] * 0.5f * (1.0f + c))), c);
-      } else if (fabsf(c) < 1.0f) {
-        if (c > 0) {
-          const int u = k - 2;
-          fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
-        } else if (c < 0) {
-          const int u = k - 1;
-          fz = fdiv(-wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 0.0f, -c), c);
-        }
-      } else if (valid) {
-        fz = vflx_tile<float>(g, C, FL, DF, F6, ld, k, c, wv);
+    if (fabsf(c) < 1.0f && g.flux_type == GMC_FLUX_VAN_LEER) {   // upwind cell k-1 or k
+      if (c > 0) fz = fdiv(wv * (c * (C[k * ld] + S[(k - 1) * ld] * 0.5f * (1.0f - c))), c);
+      else if (c < 0) fz = fdiv(wv * (c * (C[(k + 1) * ld] - S[k * ld] * 0.5f * (1.0f + c))), c);
+    } else if (fabsf(c) < 1.0f) {
+      if (c > 0) {
+        const int u = k - 2;
+        fz = fdiv(wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 1.0f - c, 1.0f), c);
+      } else if (c < 0) {
+        const int u = k - 1;
+        fz = fdiv(-wv * ppm_tail(0.0f, FL[u * ld], DF[u * ld], F6[u * ld], 0.0f, -c), c);
       }
+    } else if (valid) {
+      fz = vflx_tile<float>(g, C, FL, DF, F6, ld, k, c, wv);
+    }
+    return fz;
+  };
+#pragma unroll
+  for (int m = 0; m < kColPre; ++m) {
+    const int k = 1 + kt + m * KT;
+    if (k <= nlev + 1) FZ[(k - 1) * ld] = k != 1 && k != nlev + 1 ? flux_at(k, cz[m], wz[m]) : 0.0f;
+  }
+  for (int k = 1 + kt + kColPre * KT; k <= nlev + 1; k += KT) {
+    float fz = 0;
+    if (k != nlev + 1) {
+      const size_t ol = ix3(nlat, nlon, ic, j, k);
+      fz = flux_at(k, cflz[ol], we[ol]);
     }
     FZ[(k - 1) * ld] = fz;
   }

@@ -40,6 +40,29 @@ __global__ void GMC_BOUNDS(R, 8) k_mass_flux(DGrid g, Slot<R> s) {
   const LevMass<R> M = lev_mass(g, s, k);
   const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k), ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
   const unsigned mo = (unsigned)(j - 1) * nlon;   // cell row j of the 2D mass field
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.baroclinic) {   // two points per thread, paired loads (layer mass dA + dB psr)
+      const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
+      for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+        const float2 p0 = *reinterpret_cast<const float2 *>(s.psr + mo + i0);
+        const float m0 = fmaf(dB, p0.x, dA), m1 = fmaf(dB, p0.y, dA);
+        if (j == 1 || j == nlat) {
+          *reinterpret_cast<float2 *>(s.mfx_lon + fo + i0) = make_float2(0.0f, 0.0f);
+        } else {
+          const float m2 = fmaf(dB, s.psr[mo + (i0 + 2 == nlon ? 0 : i0 + 2)], dA);
+          const float2 u2 = *reinterpret_cast<const float2 *>(s.u_f + fo + i0);
+          *reinterpret_cast<float2 *>(s.mfx_lon + fo + i0) = make_float2((m0 + m1) * 0.5f * u2.x, (m1 + m2) * 0.5f * u2.y);
+        }
+        if (j <= nhalf) {
+          const float2 pn = *reinterpret_cast<const float2 *>(s.psr + mo + nlon + i0);
+          const float2 v2 = *reinterpret_cast<const float2 *>(s.v_f + ho + i0);
+          *reinterpret_cast<float2 *>(s.mfy_lat + ho + i0) =
+              make_float2((m0 + fmaf(dB, pn.x, dA)) * 0.5f * v2.x, (m1 + fmaf(dB, pn.y, dA)) * 0.5f * v2.y);
+        }
+      }
+      return;
+    }
+  }
   if (j == 1 || j == nlat) {
     for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) s.mfx_lon[fo + i0] = (R)0;
   } else {
@@ -62,6 +85,46 @@ __global__ void GMC_BOUNDS_MB(R, 8, MB) k_tangent_winds(DGrid g, Slot<R> s, Work
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
   const LevMass<R> M = lev_mass(g, s, k);
   const unsigned mo = (unsigned)(j - 1) * nlon;
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.baroclinic) {   // two points per thread, paired loads
+      const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
+      auto P2 = [](const float *p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o); };
+      if (j <= nhalf) {
+        const float w1 = ROWR(float, htw1, j), w2 = ROWR(float, htw2, j);
+        const unsigned fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon, ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+          const unsigned im = i0 == 0 ? nlon - 1 : i0 - 1;
+          const float2 xs = P2(s.mfx_lon, fs + i0), xn = P2(s.mfx_lon, fn + i0);
+          const float xsw = s.mfx_lon[fs + im], xnw = s.mfx_lon[fn + im];
+          const float2 ps = P2(s.psr, mo + i0), pn = P2(s.psr, mo + nlon + i0);
+          const float mf0 = w1 * (xsw + xs.x) + w2 * (xnw + xn.x), mf1 = w1 * (xs.x + xs.y) + w2 * (xn.x + xn.y);
+          const float ml0 = (fmaf(dB, ps.x, dA) + fmaf(dB, pn.x, dA)) * 0.5f;
+          const float ml1 = (fmaf(dB, ps.y, dA) + fmaf(dB, pn.y, dA)) * 0.5f;
+          *reinterpret_cast<float2 *>(w.u_lat + ho + i0) = make_float2(fdiv(mf0, ml0), fdiv(mf1, ml1));
+        }
+      }
+      const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k);
+      if (j == 1 || j == nlat) {
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x)
+          *reinterpret_cast<float2 *>(w.v_lon + fo + i0) = make_float2(0.0f, 0.0f);
+      } else {
+        const float w1 = ROWR(float, ftw1, j), w2 = ROWR(float, ftw2, j);
+        const unsigned hn = (unsigned)ix3(nhalf, nlon, 1, j, k), hs = hn - nlon;
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+          const unsigned i2 = i0 + 2 == nlon ? 0 : i0 + 2;
+          const float2 ys = P2(s.mfy_lat, hs + i0), yn = P2(s.mfy_lat, hn + i0);
+          const float yse = s.mfy_lat[hs + i2], yne = s.mfy_lat[hn + i2];
+          const float2 pc = P2(s.psr, mo + i0);
+          const float pe = s.psr[mo + i2];
+          const float mf0 = w1 * (ys.x + ys.y) + w2 * (yn.x + yn.y), mf1 = w1 * (ys.y + yse) + w2 * (yn.y + yne);
+          const float ml0 = (fmaf(dB, pc.x, dA) + fmaf(dB, pc.y, dA)) * 0.5f;
+          const float ml1 = (fmaf(dB, pc.y, dA) + fmaf(dB, pe, dA)) * 0.5f;
+          *reinterpret_cast<float2 *>(w.v_lon + fo + i0) = make_float2(fdiv(mf0, ml0), fdiv(mf1, ml1));
+        }
+      }
+      return;
+    }
+  }
   if (j <= nhalf) {
     const R w1 = ROWR(R, htw1, j), w2 = ROWR(R, htw2, j);
     const unsigned fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon, ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
@@ -188,6 +251,31 @@ __global__ void GMC_BOUNDS(R, 6) k_pv(DGrid g, Slot<R> s, Work<R> w) {
   const LevMass<R> LM = lev_mass(g, s, k);
   const unsigned us = (unsigned)ix3(nlat, nlon, 1, j, k), un = us + nlon, ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
   const unsigned ms = (unsigned)(j - 1) * nlon, mn = ms + nlon;
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.baroclinic) {   // two points per thread, paired loads
+      const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
+      auto P2 = [](const float *p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o); };
+      for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+        const unsigned i2 = i0 + 2 == nlon ? 0 : i0 + 2;
+        const float2 vv = P2(s.v_f, ho + i0);
+        const float ve = s.v_f[ho + i2];
+        float vor0, vor1;
+        if (pole) {
+          vor0 = vor1 = (float)pole_vor;
+        } else {
+          const float2 u0 = P2(s.u_f, us + i0), u1 = P2(s.u_f, un + i0);
+          vor0 = fdiv(u0.x * dl0 - u1.x * dl1 + vv.y * dt - vv.x * dt, av);
+          vor1 = fdiv(u0.y * dl0 - u1.y * dl1 + ve * dt - vv.y * dt, av);
+        }
+        const float2 a2 = P2(s.psr, ms + i0), b2 = P2(s.psr, mn + i0);
+        const float ae = fmaf(dB, s.psr[ms + i2], dA), be = fmaf(dB, s.psr[mn + i2], dA);
+        const float a0 = fmaf(dB, a2.x, dA), a1 = fmaf(dB, a2.y, dA), b0 = fmaf(dB, b2.x, dA), b1 = fmaf(dB, b2.y, dA);
+        const float mv0 = fdiv((a0 + a1) * as2 + (b0 + b1) * as1, av), mv1 = fdiv((a1 + ae) * as2 + (b1 + be) * as1, av);
+        *reinterpret_cast<float2 *>(s.pv + ho + i0) = make_float2(fdiv(vor0 + f, mv0), fdiv(vor1 + f, mv1));
+      }
+      return;
+    }
+  }
   for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) {
     const int ip = i0 + 1 == nlon ? 0 : i0 + 1;
     R vor;
@@ -376,13 +464,22 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       // A departure more than one row away (|cfly| > 1, flagged below) keeps v1.
       const float cdy = (float)dt_ / ROWR(float, de_lat, j);
       const float *A = g.cfl_yoff + (size_t)(j - 1) * 4;   // l = j-1 .. j+2
+      // the four offsets and, per column, the four rows a departure can use
+      // (j-1 .. j+2) are loaded before the RK4 stages, which then select among
+      // them: no load waits on a computed row
+      const float A0 = A[0], A1 = A[1], A2 = A[2], A3 = A[3];
+      auto Asel = [&](int t) { return t == 0 ? A0 : t == 1 ? A1 : t == 2 ? A2 : A3; };
       for (int i = 1 + threadIdx.x; i <= nlon; i += blockDim.x) {
-        auto Vl = [&](int l) { return v[ix3(nhalf, nlon, i, l, k)]; };
-        const float v1 = Vl(j);
+        const unsigned ov = (unsigned)ix3(nhalf, nlon, i, j, k);
+        const float v1 = v[ov];
+        const float vm = j >= 2 ? v[ov - nlon] : 0.0f, vp = j + 1 <= nhalf ? v[ov + nlon] : 0.0f,
+                    vp2 = j + 2 <= nhalf ? v[ov + 2 * nlon] : 0.0f;
+        auto Vsel = [&](int t) { return t == 0 ? vm : t == 1 ? v1 : t == 2 ? vp : vp2; };   // row j-1+t
         auto at = [&](float b) {
           int l = (int)floorf((float)j + b);
           if (l < 1 || l > nhalf - 1 || l < j - 1 || l > j + 1) return v1;
-          return (A[l + 2 - j] - b) * Vl(l) + (b - A[l + 1 - j]) * Vl(l + 1);
+          const int t = l - j + 1;   // 0 .. 2
+          return (Asel(t + 1) - b) * Vsel(t) + (b - Asel(t)) * Vsel(t + 1);
         };
         const float v2 = at(0.5f * cdy * v1);
         const float v3 = at(0.5f * cdy * v2);
@@ -1416,11 +1513,13 @@ inline size_t filter_smem(const DGrid &g, int rows, size_t elem) {
 // ---------------------------------------------------------------------------
 template <class R>
 void launch_mass_flux(const DGrid &g, const Launch &L, const Slot<R> &s) {
-  mb_launch(L, [&](auto mb) { k_mass_flux<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s); });
+  const int bt = std::is_same<R, float>::value && g.baroclinic ? 128 : L.threads;   // FP32: two points per thread
+  mb_launch(L, [&](auto mb) { k_mass_flux<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), bt, 0, L.stream>>>(g, s); });
 }
 template <class R>
 void launch_tangent_winds(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  mb_launch(L, [&](auto mb) { k_tangent_winds<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
+  const int bt = std::is_same<R, float>::value && g.baroclinic ? 128 : L.threads;   // FP32: two points per thread
+  mb_launch(L, [&](auto mb) { k_tangent_winds<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), bt, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_kinetic_energy(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
@@ -1430,7 +1529,8 @@ void launch_kinetic_energy(const DGrid &g, const Launch &L, const Slot<R> &s, co
 }
 template <class R>
 void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w) {
-  mb_launch(L, [&](auto mb) { k_pv<R, decltype(mb)::value><<<dim3(g.nhalf, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w); });
+  const int bt = std::is_same<R, float>::value && g.baroclinic ? 128 : L.threads;   // FP32: two points per thread
+  mb_launch(L, [&](auto mb) { k_pv<R, decltype(mb)::value><<<dim3(g.nhalf, g.nlev, L.members), bt, 0, L.stream>>>(g, s, w); });
 }
 template <class R>
 void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
