@@ -320,6 +320,50 @@ __global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, R dt)
     l = l < 0 ? l + nlon : (l >= nlon ? l - nlon : l);
     return pv[r.off + l];
   };
+  if constexpr (std::is_same<R, float>::value) {
+    // Default options (upwind, order 3) in FP32: two points per thread with
+    // paired loads.  A pv row beyond a pole is read shifted by nlon/2, which
+    // keeps a pair aligned (and wrapping together) when nlon/2 is even.
+    if (!tvd && !mid_only && up3 && (g.half & 1) == 0) {
+      auto P2 = [](const float *p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o); };
+      // pv of a resolved row at 0-based columns i0, i0+1
+      auto Q2 = [&](const PvRow &r, int i0) {
+        int l = i0 + r.sh;
+        l = l >= nlon ? l - nlon : l;
+        return P2(pv, r.off + l);
+      };
+      auto face = [&](float pm, float pc, float p3, float p0, float un, float vt) {   // one edge
+        const float bb = fdiv(fabsf(vt), sqrtf(un * un + vt * vt) + eps);
+        const float dir = fsign(1.0f, vt);
+        const float up = upwind3(dir, wgt, p0, pm, pc, p3);
+        return bb * up + (1.0f - bb) * 0.5f * (pm + pc);
+      };
+      if (j == 1 || j == nlat) {
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x)
+          *reinterpret_cast<float2 *>(s.pv_lon + ix3(nlat, nlon, i0 + 1, j, k)) = make_float2(0.0f, 0.0f);
+      } else {
+        const PvRow r0 = pv_row(g, j - 2, k), r1 = pv_row(g, j - 1, k), r2 = pv_row(g, j, k), r3 = pv_row(g, j + 1, k);
+        const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k);
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+          const float2 a0 = Q2(r0, i0), a1 = Q2(r1, i0), a2 = Q2(r2, i0), a3 = Q2(r3, i0);
+          const float2 un = P2(s.u_f, fo + i0), vt = P2(w.v_lon, fo + i0);
+          *reinterpret_cast<float2 *>(s.pv_lon + fo + i0) =
+              make_float2(face(a1.x, a2.x, a3.x, a0.x, un.x, vt.x), face(a1.y, a2.y, a3.y, a0.y, un.y, vt.y));
+        }
+      }
+      if (j <= nhalf) {   // pv_lat: pv of half row j at columns i-2 .. i+1 (0-based i0-2 .. i0+2 for the pair)
+        const unsigned ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
+          const float2 w2 = P2(pv, ho + (i0 == 0 ? nlon - 2 : i0 - 2)), c2 = P2(pv, ho + i0);
+          const float e = pv[ho + (i0 + 2 == nlon ? 0 : i0 + 2)];
+          const float2 ut = P2(w.u_lat, ho + i0), vn = P2(s.v_f, ho + i0);
+          *reinterpret_cast<float2 *>(s.pv_lat + ho + i0) =
+              make_float2(face(w2.y, c2.x, c2.y, w2.x, vn.x, ut.x), face(c2.x, c2.y, e, w2.y, vn.y, ut.y));
+        }
+      }
+      return;
+    }
+  }
   // pv_lon on full row j: pv of half rows j-2 .. j+1 at the same longitude
   if (j == 1 || j == nlat) {
     for (int i0 = threadIdx.x; i0 < nlon; i0 += blockDim.x) s.pv_lon[ix3(nlat, nlon, i0 + 1, j, k)] = (R)0;
@@ -1534,7 +1578,8 @@ void launch_pv(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> 
 }
 template <class R>
 void launch_pv_edges(const DGrid &g, const Launch &L, const Slot<R> &s, const Work<R> &w, double dt) {
-  mb_launch(L, [&](auto mb) { k_pv_edges<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), L.threads, 0, L.stream>>>(g, s, w, dt); });
+  const int bt = std::is_same<R, float>::value && g.baroclinic ? 128 : L.threads;   // FP32: two points per thread
+  mb_launch(L, [&](auto mb) { k_pv_edges<R, decltype(mb)::value><<<dim3(g.nlat, g.nlev, L.members), bt, 0, L.stream>>>(g, s, w, dt); });
 }
 template <class R>
 void launch_batch_cfl(const DGrid &g, const Launch &L, const R *u, const R *v, R *cflx, R *cfly, R *divx, R *divy, double dt) {
