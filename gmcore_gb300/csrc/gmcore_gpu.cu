@@ -1053,11 +1053,12 @@ struct Engine : EngineBase {
     K("momentum_tend", 1, [&] { launch_momentum_tend<R>(dg, L, s, w); });
   }
 
-  // The same launches as forward_w on two streams.  Side: batch_cfl, then
-  // (after mass_flux) column_mass, ffsl_hflx_pt, pt_tendency.  Context:
-  // mass_flux, tangent_winds, kinetic_energy, pv, pv_edges, then (after
-  // column_mass) momentum_tend; the context stream joins the side stream
-  // before the backward pass.  The two chains write disjoint work fields.
+  // The same launches as forward_w on two streams.  Side: batch_cfl, the y
+  // inner pass, (after mass_flux) the x passes and the y outer pass, (after
+  // column_mass) pt_tendency.  Context: mass_flux, column_mass, tangent_winds,
+  // kinetic_energy, pv, pv_edges, momentum_tend; the context stream joins the
+  // side stream before the backward pass.  The two chains write disjoint work
+  // fields.
   void forward_split(Work<R> &w, const Slot<R> &s, double dt) {
     Launch Ls = L;
     Ls.stream = dside;
@@ -1067,22 +1068,31 @@ struct Engine : EngineBase {
       CK(cudaStreamWaitEvent(to, e, 0));
     };
     edge(dfork_ev, L.stream, dside);
+    // side stream: the potential-temperature transport, which needs the
+    // Courant numbers first, the mass fluxes from the x passes on and the
+    // column quantities last
     K("batch_cfl", 1, [&] { launch_batch_cfl<R>(dg, Ls, s.u_f, s.v_f, w.cflx, w.cfly, w.divx, w.divy, dt); });
-    K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
-    edge(dmf_ev, L.stream, dside);
-    K("column_mass", 1, [&] { launch_column_mass<R>(dg, Ls, s, w, dt); });
-    if (!dry) CK(cudaEventRecord(dcm_ev, dside));
     BatchView<R> b{};
     b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
     b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
-    ffsl3(Ls, b, s.pt, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt);
+    K("ffsl_inner_y", 1, [&] { launch_ffsl_inner_y<R>(dg, Ls, b, s.pt, w.qy, dt); });
+    // context stream: mass fluxes, then the column sweep (which the pt
+    // tendency needs) ahead of the PV chain, so that the two chains are of
+    // about equal length
+    K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
+    if (!dry) CK(cudaEventRecord(dmf_ev, L.stream));
+    K("column_mass", 1, [&] { launch_column_mass<R>(dg, L, s, w, dt); });
+    if (!dry) CK(cudaEventRecord(dcm_ev, L.stream));
+    if (!dry) CK(cudaStreamWaitEvent(dside, dmf_ev, 0));
+    K("ffsl_x2", 1, [&] { launch_ffsl_x2<R>(dg, Ls, b, s.pt, w.qy, w.qx, w.ptf_lon, dt); });
+    K("ffsl_hflx_y", 1, [&] { launch_hflx_y<R>(dg, Ls, b, w.qx, w.ptf_lat); });
+    if (!dry) CK(cudaStreamWaitEvent(dside, dcm_ev, 0));
     K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, Ls, s, w); });
     if (!dry) CK(cudaEventRecord(dpt_ev, dside));
     K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
     K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
     K("pv", 1, [&] { launch_pv<R>(dg, L, s, w); });
     K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w, dt); });
-    if (!dry) CK(cudaStreamWaitEvent(L.stream, dcm_ev, 0));
     K("momentum_tend", 1, [&] { launch_momentum_tend<R>(dg, L, s, w); });
     if (!dry) CK(cudaStreamWaitEvent(L.stream, dpt_ev, 0));
   }
