@@ -182,6 +182,16 @@ def measured_traffic(name):
         return None
 
 
+def fp64_flops_per_cell(name):
+    """FP64 FLOP per cell of one launch of a kernel group of the FP64 form, from
+    the committed ncu op counts (profiles/fp64_flops_c2.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_flops_c2.json")) as f:
+            return json.load(f)["groups"].get(name)
+    except Exception:
+        return None
+
+
 def state_bytes(state):
     return sum(a.nbytes for a in state.values())
 
@@ -382,7 +392,27 @@ def run_ours(args):
     e2e64_steps = 5
     e2e64_s, _ = e2e_run(m64, e2e64_steps, registered=True)
     e2e64_value = DT * e2e64_steps / e2e64_s * WORLD
+    # the FP64 form's roofline: FP64 issue (its kernels keep the FP64 pipe
+    # busy, profiles/fp64_form_c2.md); the dominant kernel's FLOP per launch
+    # over its in-bench launch time, against the FMA peak measured now
+    m64.set_profiling(True)
+    m64.step(1)
+    prof64 = m64.kernel_profile()
+    m64.set_profiling(False)
     m64.close()
+    fp64_roof = None
+    singles64 = {k: v for k, v in prof64.items() if k not in MULTI_KERNEL}
+    top64, (t64, n64) = max(singles64.items(), key=lambda kv: kv[1][0])
+    fpc = fp64_flops_per_cell(top64)
+    if fpc is not None:
+        peak64 = g.fp64_fma_peak()
+        flop = fpc["fp64_flop_per_cell"] * ncell
+        ach64 = flop / (t64 / n64 / 1000.0) / 1e12
+        fp64_roof = {"bound": "fp64", "kernel": top64, "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": ach64 / peak64, "fp64_flop_per_launch": flop, "avg_launch_ms": t64 / n64,
+                     "fp64_pipe_busy_pct_ncu": fpc["fp64_pipe_pct"],
+                     "peak_source": "gmc_fp64_fma_peak (measured in this run)",
+                     "flop_source": "profiles/fp64_flops_c2.json (ncu FP64 op counts)"}
 
     adj = adjoint_cost() if RANK == 0 else None
     ens = ensemble_throughput() if RANK == 0 else None
@@ -415,7 +445,8 @@ def run_ours(args):
                      "steps_compared": args.warmup + args.steps, "mixed_minus_fp64": errors,
                      "e2e": {"value": e2e64_value, "unit": "sim days/wall-day", "steps": e2e64_steps,
                              "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                             "path": "the registered-array path of e2e, FP64 form"}},
+                             "path": "the registered-array path of e2e, FP64 form"},
+                     "roofline": fp64_roof},
             "e2e": {"value": e2e_value, "unit": "sim days/wall-day", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
                     "path": "gmc_set_field/gmc_set_tracer + gmc_step(1) + gmc_get_field/gmc_get_tracer, host float64 "
