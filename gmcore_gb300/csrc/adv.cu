@@ -799,6 +799,27 @@ __global__ void k_half_level_mass(DGrid g, SurfP<R> sp, R *m_lev, int mode, doub
   }
 }
 
+// FP32 form of k_half_level_mass, elementwise over (half level, cell): half
+// level k (1 .. nlev+1) takes (m(k-1) + m(k)) / 2 of the FP32 layer masses with
+// m(0) = m(nlev+1) = 0, the same values as the column loop.
+__global__ void __launch_bounds__(256) k_half_level_mass_f(DGrid g, const float *__restrict__ psr,
+                                                           float *__restrict__ m_lev, int mode, float divisor) {
+  const int H = g.nlat * g.nlon, k = blockIdx.y + 1;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= H) return;
+  float ml = 0;
+  if (psr) {
+    const float ps = psr[c];
+    const float mu = k > 1 ? fmaf(g.dmB[k - 2], ps, g.dmA[k - 2]) : 0.0f;          // layer k-1
+    const float md = k <= g.nlev ? fmaf(g.dmB[k - 1], ps, g.dmA[k - 1]) : 0.0f;   // layer k
+    ml = 0.5f * (mu + md);
+  }
+  float *o = m_lev + (size_t)(k - 1) * H + c;
+  if (mode == 0) *o = ml;
+  else if (mode == 1) *o = *o + ml;
+  else *o = (*o + ml) / divisor;
+}
+
 template <class R>
 __global__ void k_batch_cflz(DGrid g, const R *we_in, const R *ml_in, R *cflz, R dt) {
   extern __shared__ float colsh[];
@@ -1230,6 +1251,14 @@ template void launch_accum_multi<float>(const Launch &, const AccumSet<float> &)
 
 template <class R>
 void launch_half_level_mass(const DGrid &g, const Launch &L, const SurfP<R> &sp, R *m_lev, int mode, double divisor) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.baroclinic) {
+      const int H = g.nlat * g.nlon;
+      k_half_level_mass_f<<<dim3((H + 255) / 256, g.nlev + 1), 256, 0, L.stream>>>(
+          g, sp.phs_f ? sp.psr : nullptr, m_lev, mode, (float)divisor);
+      return;
+    }
+  }
   const int bt = 64;
   k_half_level_mass<R><<<dim3((g.nlon + bt - 1) / bt, g.nlat), bt, 0, L.stream>>>(g, sp, m_lev, mode, divisor);
 }

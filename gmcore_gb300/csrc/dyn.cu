@@ -1081,11 +1081,22 @@ __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
   const R dtr = (R)dt;
   const SurfP<R> so = o.surf(), sn = n.surf();
   const unsigned m0 = (unsigned)(j - 1) * nlon;
+  constexpr bool kPair = std::is_same<R, float>::value;   // FP32: two points per thread, paired loads
   for (int kk = 0; kk < nk; ++kk) {
     const int k = k0 + kk;
     const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x)
-      row[kk * nlon + i] = o.pt[c0 + i] * Mass<R>::layer(g, k, so.at(m0 + i)) + dtr * w.dpt[c0 + i];
+    if constexpr (kPair) {
+      for (int i = 2 * threadIdx.x; i < nlon; i += 2 * blockDim.x) {
+        const float2 p = *reinterpret_cast<const float2 *>(so.psr + m0 + i);
+        const float2 t = *reinterpret_cast<const float2 *>(o.pt + c0 + i);
+        const float2 d = *reinterpret_cast<const float2 *>(w.dpt + c0 + i);
+        *reinterpret_cast<float2 *>(row + kk * nlon + i) = make_float2(
+            t.x * Mass<float>::layer(g, k, p.x) + dtr * d.x, t.y * Mass<float>::layer(g, k, p.y) + dtr * d.y);
+      }
+    } else {
+      for (int i = threadIdx.x; i < nlon; i += blockDim.x)
+        row[kk * nlon + i] = o.pt[c0 + i] * Mass<R>::layer(g, k, so.at(m0 + i)) + dtr * w.dpt[c0 + i];
+    }
   }
   if (nk == KB) {
     filter_rows<KB, R, R>(g.small1, true, j, nlon, row, nlon, ext, es);
@@ -1096,10 +1107,20 @@ __global__ void k_update_pt(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
   for (int kk = 0; kk < nk; ++kk) {
     const int k = k0 + kk;
     const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
-    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
-      const R v = row[kk * nlon + i] / Mass<R>::layer(g, k, sn.at(m0 + i));
-      n.pt[c0 + i] = v;
-      if (!isfinite(v)) raise_err(g, ERR_NAN);
+    if constexpr (kPair) {
+      for (int i = 2 * threadIdx.x; i < nlon; i += 2 * blockDim.x) {
+        const float2 p = *reinterpret_cast<const float2 *>(sn.psr + m0 + i);
+        const float2 r = *reinterpret_cast<const float2 *>(row + kk * nlon + i);
+        const float2 v = make_float2(r.x / Mass<float>::layer(g, k, p.x), r.y / Mass<float>::layer(g, k, p.y));
+        *reinterpret_cast<float2 *>(n.pt + c0 + i) = v;
+        if (!isfinite(v.x) || !isfinite(v.y)) raise_err(g, ERR_NAN);
+      }
+    } else {
+      for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+        const R v = row[kk * nlon + i] / Mass<R>::layer(g, k, sn.at(m0 + i));
+        n.pt[c0 + i] = v;
+        if (!isfinite(v)) raise_err(g, ERR_NAN);
+      }
     }
   }
 }
