@@ -12,7 +12,6 @@ GMC_ECFL = -2
 GMC_ENONMONO = -3
 GMC_ENEGTRACER = -4
 GMC_ENAN = -5
-GMC_ETIMEDOUT = -6
 GMC_ECUDA = -7
 GMC_ENOMEM = -8
 GMC_ESTATE = -9
@@ -20,7 +19,7 @@ GMC_ESTATE = -9
 STATUS_NAMES = {
     GMC_OK: "GMC_OK", GMC_EINVAL: "GMC_EINVAL", GMC_ECFL: "GMC_ECFL",
     GMC_ENONMONO: "GMC_ENONMONO", GMC_ENEGTRACER: "GMC_ENEGTRACER", GMC_ENAN: "GMC_ENAN",
-    GMC_ETIMEDOUT: "GMC_ETIMEDOUT", GMC_ECUDA: "GMC_ECUDA", GMC_ENOMEM: "GMC_ENOMEM",
+    GMC_ECUDA: "GMC_ECUDA", GMC_ENOMEM: "GMC_ENOMEM",
     GMC_ESTATE: "GMC_ESTATE",
 }
 

@@ -50,8 +50,8 @@ extern "C" {
 #define GMC_ENEGTRACER  -4   /* negative tracer not fixable (adv_mod.F90:251-253, 290-292) */
 #define GMC_ENAN        -5   /* non-finite value in the prognostic state (surface
                                 pressure, potential temperature or gz, winds) */
-#define GMC_ETIMEDOUT   -6   /* a bounded device wait gave up                */
-#define GMC_ECUDA       -7   /* CUDA runtime error                           */
+/* -6 is not used: no kernel of the library waits on another */
+#define GMC_ECUDA       -7  /* CUDA runtime error                           */
 #define GMC_ENOMEM      -8   /* device allocation failed                     */
 #define GMC_ESTATE      -9   /* call out of order (e.g. step before prepare) */
 

@@ -24,7 +24,7 @@ module gmcore_gpu_mod
 
   ! status codes
   integer(c_int), parameter :: GMC_OK = 0, GMC_EINVAL = -1, GMC_ECFL = -2, GMC_ENONMONO = -3, &
-                               GMC_ENEGTRACER = -4, GMC_ENAN = -5, GMC_ETIMEDOUT = -6, GMC_ECUDA = -7, &
+                               GMC_ENEGTRACER = -4, GMC_ENAN = -5, GMC_ECUDA = -7, &
                                GMC_ENOMEM = -8, GMC_ESTATE = -9
   ! namelist options (src/utils/namelist_mod.F90)
   integer(c_int32_t), parameter :: GMC_TIME_EULER = 0, GMC_TIME_PC2 = 1, GMC_TIME_WRFRK3 = 2

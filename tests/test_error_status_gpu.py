@@ -126,6 +126,26 @@ def test_clean_state_runs_without_error():
     assert got == want == ("ok", abi.GMC_OK)
 
 
+def test_calls_out_of_order_are_estate():
+    # a step, or the tangent-linear model, before gmc_prepare: GMC_ESTATE, and
+    # the context still prepares and steps afterwards
+    cfg = ec.config()
+    m = Model(cfg)
+    load_state(m, ec.base_state(cfg))
+    with pytest.raises(GmcError) as e:
+        m.step(1)
+    assert e.value.code == abi.GMC_ESTATE
+    swm = abi.default_config(nlon=72, nlat=37, nlev=1, baroclinic=0, dt_dyn=600.0)
+    s = Model(swm)
+    with pytest.raises(GmcError) as e:
+        s.tlm_step(1, {"u_lon": np.zeros((1, 37, 72)), "v_lat": np.zeros((1, 36, 72)), "gz": np.zeros((37, 72))})
+    assert e.value.code == abi.GMC_ESTATE
+    s.close()
+    m.prepare()
+    m.step(1)
+    m.close()
+
+
 def test_device_allocation_failure_is_enomem():
     # 8192 x 4000 x 64 levels in FP64 needs several hundred GB of device memory
     cfg = abi.default_config(nlon=8192, nlat=4000, nlev=64, baroclinic=1, dt_dyn=1.0,
