@@ -192,6 +192,52 @@ def fp64_flops_per_cell(name):
         return None
 
 
+def mixed_ops(name):
+    """Warp instructions, FP32 instructions and FLOP per launch of a kernel
+    group of the mixed form, from the committed ncu counts
+    (profiles/mixed_ops_c2.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "mixed_ops_c2.json")) as f:
+            return json.load(f)["groups"].get(name)
+    except Exception:
+        return None
+
+
+def issue_roof(prof, ms_per_step, sm_mhz, fp32_peak):
+    """The roof that binds the mixed form: instruction issue.  Warp
+    instructions of one step (ncu counts per launch x the launches the
+    in-bench profile saw over its 3 steps) against the GPU's issue rate (4
+    warp instructions per SM per cycle at the SM clock sampled during the
+    timed region), and the step's FP32 FLOP against the measured FP32 FMA
+    peak."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    inst = f32i = flop = covered = 0.0
+    total = sum(ms for ms, _ in prof.values()) / 3.0
+    for name, (ms, cnt) in prof.items():
+        o = mixed_ops(name)
+        if o is None:
+            continue
+        inst += o["warp_inst_per_launch"] * cnt / 3.0
+        f32i += o["fp32_inst_per_launch"] * cnt / 3.0
+        flop += o["fp32_flop_per_launch"] * cnt / 3.0
+        covered += ms / 3.0
+    if not inst:
+        return None
+    peak_issue = sms * 4 * sm_mhz * 1e6
+    s = ms_per_step / 1000.0
+    return {"bound": "issue", "warp_inst_per_step": inst, "achieved_warp_inst_per_s": inst / s,
+            "peak_warp_inst_per_s": peak_issue, "frac": inst / s / peak_issue,
+            "issue_floor_ms_per_step": inst / peak_issue * 1000.0,
+            "fp32_inst_share": f32i / 32.0 / inst,
+            "fp32_flop_per_step": flop, "fp32_tflops": flop / s / 1e12, "fp32_peak_tflops": fp32_peak,
+            "fp32_frac": flop / s / 1e12 / fp32_peak if fp32_peak else None,
+            "kernel_time_covered": covered / total if total else None,
+            "sms": sms, "sm_mhz": sm_mhz,
+            "source": "profiles/mixed_ops_c2.json (ncu instruction and FP32 op counts per launch); "
+                      "peak issue = SMs x 4 x sampled SM clock; FP32 peak = gmc_fp32_fma_peak (measured in this run)"}
+
+
 def state_bytes(state):
     return sum(a.nbytes for a in state.values())
 
@@ -351,6 +397,7 @@ def run_ours(args):
             ncu_bytes += tb * cnt / 3.0
             covered_ms += ms / 3.0
     ncell = cfg.nlon * cfg.nlat * cfg.nlev
+    roof_issue = issue_roof(prof, ms_per_step, clk.get("sm_mhz") or 2070.0, g.fp32_fma_peak())
 
     # ---- one simulated day (480 steps) of the mixed form, device-timed ----
     one_day = None
@@ -466,7 +513,8 @@ def run_ours(args):
                               "ncu_dram_bytes_per_step": ncu_bytes,
                               "redundancy": ncu_bytes / b_step,
                               "kernel_time_weighted_dram_frac": (ncu_bytes / (covered_ms / 1000.0) / 1e9 / peak
-                                                                 if covered_ms else None)},
+                                                                 if covered_ms else None),
+                              "issue": roof_issue},
             "cell_updates_per_s": ncell * args.steps / (dev_ms / 1000.0) * WORLD,
             "kernel_ms_per_step": {k: round(v[0] / 3.0, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clk,

@@ -30,7 +30,7 @@ EXPORTED = (
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
     "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs", "gmc_host_register", "gmc_host_unregister",
-    "gmc_fp64_fma_peak", "gmc_set_member_layout",
+    "gmc_fp64_fma_peak", "gmc_fp32_fma_peak", "gmc_set_member_layout",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -86,6 +86,7 @@ def load(build_if_missing=True):
     lib.gmc_host_register.argtypes = [C.c_void_p, C.c_size_t]
     lib.gmc_host_unregister.argtypes = [C.c_void_p]
     lib.gmc_fp64_fma_peak.argtypes = [P(C.c_double)]
+    lib.gmc_fp32_fma_peak.argtypes = [P(C.c_double)]
     lib.gmc_set_member_layout.argtypes = [C.c_void_p, C.c_int32]
     _lib = lib
     return lib
@@ -97,6 +98,15 @@ def fp64_fma_peak():
     rc = load().gmc_fp64_fma_peak(C.byref(out))
     if rc != 0:
         raise GmcError(rc, "gmc_fp64_fma_peak")
+    return out.value
+
+
+def fp32_fma_peak():
+    """Measured FP32 FMA throughput of the current GPU in TFLOP/s."""
+    out = C.c_double()
+    rc = load().gmc_fp32_fma_peak(C.byref(out))
+    if rc != 0:
+        raise GmcError(rc, "gmc_fp32_fma_peak")
     return out.value
 
 

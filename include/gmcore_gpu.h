@@ -51,7 +51,7 @@ extern "C" {
 #define GMC_ENAN        -5   /* non-finite value in the prognostic state (surface
                                 pressure, potential temperature or gz, winds) */
 /* -6 is not used: no kernel of the library waits on another */
-#define GMC_ECUDA       -7  /* CUDA runtime error                           */
+#define GMC_ECUDA       -7   /* CUDA runtime error                           */
 #define GMC_ENOMEM      -8   /* device allocation failed                     */
 #define GMC_ESTATE      -9   /* call out of order (e.g. step before prepare) */
 
@@ -317,6 +317,9 @@ int gmc_make_ic(const gmc_config *cfg, int32_t kind, uint64_t seed, double noise
  * clock or other setting of the GPU is changed).  No reference counterpart:
  * it is the peak against which the FP64 form's kernels are placed. */
 int gmc_fp64_fma_peak(double *tflops);
+/* The same for FP32 fused multiply-adds: the peak against which the mixed
+ * form's arithmetic per step is placed. */
+int gmc_fp32_fma_peak(double *tflops);
 
 #ifdef __cplusplus
 }

@@ -284,6 +284,12 @@ module gmcore_gpu_mod
       real(c_double), intent(out) :: tflops
     end function gmc_fp64_fma_peak
 
+    ! measured FP32 FMA throughput of the current device (TFLOP/s)
+    integer(c_int) function gmc_fp32_fma_peak(tflops) bind(c, name='gmc_fp32_fma_peak')
+      import
+      real(c_double), intent(out) :: tflops
+    end function gmc_fp32_fma_peak
+
     integer(c_size_t) function c_strlen(s) bind(c, name='strlen')
       import
       type(c_ptr), value :: s
