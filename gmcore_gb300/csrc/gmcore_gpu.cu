@@ -547,6 +547,7 @@ struct Engine : EngineBase {
     tables.release();
     if (tl) {
       tl->drop_graphs();
+      tl->release_streams();
       tl->arena.release();
       tl->zarena.release();
       tl->store.release();
@@ -1164,12 +1165,23 @@ struct Engine : EngineBase {
     Work<double> WF, DW, AW;
     bool ready = false;
     // checkpoint and segment storage of the adjoint, kept for repeated calls
-    // with the same (segments, interval)
+    // with the same (segments, interval); two segment buffers (steps
+    // [b k, b k + k) of xs/ws), so that the next segment is recomputed on
+    // `rs` while the reverse sweep walks the current one
     Arena store;
     int store_nseg = -1, store_k = -1;
     std::vector<double *> cp;
     std::vector<std::array<Slot<double>, 4>> xs;
     std::vector<std::array<Work<double>, 3>> ws;
+    cudaStream_t rs = nullptr;
+    cudaEvent_t ev_fwd = nullptr, ev_rev = nullptr, ev_rec[2] = {nullptr, nullptr};
+    void release_streams() {
+      if (rs) cudaStreamDestroy(rs);
+      for (cudaEvent_t e : {ev_fwd, ev_rev, ev_rec[0], ev_rec[1]})
+        if (e) cudaEventDestroy(e);
+      rs = nullptr;
+      ev_fwd = ev_rev = ev_rec[0] = ev_rec[1] = nullptr;
+    }
     // captured launch sequences keyed by the buffers they touch
     std::map<std::vector<intptr_t>, cudaGraphExec_t> graphs;
     void drop_graphs() {
@@ -1225,11 +1237,11 @@ struct Engine : EngineBase {
       q += f.second;
     }
   }
-  void flat_load(const Slot<R> &d, const R *src) {
+  void flat_load(const Slot<R> &d, const R *src, cudaStream_t on) {
     const R *q = src;
     for (auto f : {std::make_pair(d.u_lon, full3()), std::make_pair(d.u_f, full3()), std::make_pair(d.v_lat, half3()),
                    std::make_pair(d.v_f, half3()), std::make_pair(d.gz, two_d()), std::make_pair(d.gz_f, two_d())}) {
-      CK(cudaMemcpyAsync(f.first, q, f.second * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+      CK(cudaMemcpyAsync(f.first, q, f.second * sizeof(R), cudaMemcpyDeviceToDevice, on));
       q += f.second;
     }
   }
@@ -1262,6 +1274,9 @@ struct Engine : EngineBase {
     for (int t = 0; t < 4; ++t) tl->X[t].gzs = tl->D[t].gzs = tl->A[t].gzs = gzs[0];
     tl->DS.gzs = tl->AS.gzs = gzs[0];
     tl->WF.gzs = tl->DW.gzs = tl->AW.gzs = gzs[0];
+    CK(cudaStreamCreateWithFlags(&tl->rs, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&tl->ev_fwd, &tl->ev_rev, &tl->ev_rec[0], &tl->ev_rec[1]})
+      CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     tl->ready = true;
   }
 
@@ -1331,6 +1346,13 @@ struct Engine : EngineBase {
   // on first use under `key` (graphs off or profiling: launch directly).
   template <class F>
   void replay(const std::vector<intptr_t> &key, F &&f) {
+    replay_on(stream, key, std::forward<F>(f));
+  }
+  // the same, the graph launched on stream `on` (captured on the context
+  // stream, which the capture does not run anything on); without graphs the
+  // work runs on the context stream
+  template <class F>
+  void replay_on(cudaStream_t on, const std::vector<intptr_t> &key, F &&f) {
     if (!graphs_on || prof) {
       f();
       return;
@@ -1354,7 +1376,7 @@ struct Engine : EngineBase {
       if (e != cudaSuccess) throw CudaError(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
       gi = gm.emplace(key, ex).first;
     }
-    CK(cudaGraphLaunch(gi->second, stream));
+    CK(cudaGraphLaunch(gi->second, on));
   }
   static intptr_t ip(const void *p) { return reinterpret_cast<intptr_t>(p); }
 
@@ -1372,15 +1394,16 @@ struct Engine : EngineBase {
       // segment the stage outputs (with the diagnostics forward_prepare left
       // in them when they served as star state) and the forward work of each
       // stage, so the reverse sweep recomputes nothing
+      const int nbuf = nseg > 1 ? 2 : 1;
       if (T.store_nseg != nseg || T.store_k != k) {
         T.drop_graphs();
         T.store.release();
         T.cp.assign(nseg, nullptr);
-        T.xs.assign(k, {});
-        T.ws.assign(k, {});
+        T.xs.assign(nbuf * k, {});
+        T.ws.assign(nbuf * k, {});
         auto carve_store = [&](auto &a) {
           for (int c = 0; c < nseg; ++c) T.cp[c] = a.template take<R>(fc);
-          for (int t = 0; t < k; ++t) {
+          for (int t = 0; t < nbuf * k; ++t) {
             for (int q = 0; q <= nst; ++q) carve(a, T.xs[t][q], false);
             for (int q = 0; q < nst; ++q) carve(a, T.ws[t][q], false);
           }
@@ -1389,23 +1412,28 @@ struct Engine : EngineBase {
         carve_store(cnt);
         T.store.reserve(cnt.used + 4096);
         carve_store(T.store);
-        for (int t = 0; t < k; ++t) {
+        for (int t = 0; t < nbuf * k; ++t) {
           for (int q = 0; q <= nst; ++q) T.xs[t][q].gzs = gzs[0];
           for (int q = 0; q < nst; ++q) T.ws[t][q].gzs = gzs[0];
-          if (t > 0) T.xs[t][0] = T.xs[t - 1][nst];   // a step starts from the previous step's output
+          if (t % k > 0) T.xs[t][0] = T.xs[t - 1][nst];   // a step starts from the previous step's output
         }
         T.store_nseg = nseg;
         T.store_k = k;
       }
       auto &xs = T.xs;
       auto &ws = T.ws;
-      // segment step t: stages of step s0+t into the segment storage (the
-      // final stage's update only when its output is needed)
-      auto seg_step = [&](int t, int last) {
-        replay({2, t, last}, [&] {
-          std::array<Slot<R>, 4> &X = xs[t];
-          for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[t][st], tlad_dt(st));
-          if (last < nst) forward_w(ws[t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
+      // the segment recomputation runs on its own stream while the reverse
+      // sweep walks the other buffer (the graphs replay there; without graphs
+      // everything runs in order on the context stream)
+      const bool overlap = graphs_on && !prof;
+      cudaStream_t rstream = overlap ? T.rs : stream;
+      // segment step t of buffer b: stages of step s0+t into the segment
+      // storage (the final stage's update only when its output is needed)
+      auto seg_step = [&](cudaStream_t on, int b, int t, int last) {
+        replay_on(on, {2, b, t, last}, [&] {
+          std::array<Slot<R>, 4> &X = xs[b * k + t];
+          for (int st = 0; st < last; ++st) stage_io(X[0], X[tlad_star(st)], X[st + 1], ws[b * k + t][st], tlad_dt(st));
+          if (last < nst) forward_w(ws[b * k + t][nst - 1], X[tlad_star(nst - 1)], tlad_dt(nst - 1));
         });
       };
       // forward sweep with checkpoints; the last segment runs straight into
@@ -1419,32 +1447,43 @@ struct Engine : EngineBase {
         });
         std::swap(T.X[0], T.X[nst]);
       }
-      copy_state(xs[0][0], T.X[0]);
-      for (int it = slast; it < nsteps; ++it) seg_step(it - slast, nst);
-      copy_state(slots[old_i], xs[nsteps - 1 - slast][nst]);   // the model ends at step nsteps
+      const int bl = (nseg - 1) % nbuf;   // buffer of segment seg: seg % nbuf
+      copy_state(xs[bl * k][0], T.X[0]);
+      for (int it = slast; it < nsteps; ++it) seg_step(stream, bl, it - slast, nst);
+      copy_state(slots[old_i], xs[bl * k + nsteps - 1 - slast][nst]);   // the model ends at step nsteps
+      CK(cudaEventRecord(T.ev_fwd, stream));   // checkpoints written
       // adjoint of the final state
       for (int t = 0; t <= nst; ++t) zero_state(T.A[t]);
       upload3(T.A[nst], lam_n);
       for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int b = seg % nbuf;
         const int s0 = seg * k, s1 = std::min(nsteps, s0 + k);
-        if (seg < nseg - 1) {   // recompute the segment: xs[t][0] is step s0+t's start state
-          flat_load(xs[0][0], T.cp[seg]);
-          for (int t = 0; t < s1 - s0; ++t) seg_step(t, t + 1 < s1 - s0 ? nst : nst - 1);
+        if (seg >= 1) {
+          // recompute segment seg-1 into the other buffer, once the checkpoints
+          // exist and the reverse sweep of segment seg+1 (the buffer's last
+          // reader) is done: xs[t][0] is step (seg-1) k + t's start state
+          const int bp = (seg - 1) % nbuf;
+          CK(cudaStreamWaitEvent(rstream, seg == nseg - 1 ? T.ev_fwd : T.ev_rev, 0));
+          flat_load(xs[bp * k][0], T.cp[seg - 1], rstream);
+          for (int t = 0; t < k; ++t) seg_step(rstream, bp, t, t + 1 < k ? nst : nst - 1);
+          CK(cudaEventRecord(T.ev_rec[bp], rstream));
         }
+        if (seg < nseg - 1) CK(cudaStreamWaitEvent(stream, T.ev_rec[b], 0));   // segment seg recomputed
         for (int t = s1 - s0 - 1; t >= 0; --t) {
-          replay({3, t, ip(T.A[0].u_lon), ip(T.A[nst].u_lon)}, [&] {
-            std::array<Slot<R>, 4> &X = xs[t];
+          replay({3, b, t, ip(T.A[0].u_lon), ip(T.A[nst].u_lon)}, [&] {
+            std::array<Slot<R>, 4> &X = xs[b * k + t];
             for (int st = nst - 1; st >= 0; --st) {
               const double dt = tlad_dt(st);
               // clears the adjoint work (AS, AW up to AW.du) for the forward-pass adjoint
               ad_update(dg, L, T.A[0], T.A[st + 1], T.AW, T.AS.u_lon, (size_t)(T.AW.du - T.AS.u_lon), dt);
-              ad_forward(dg, L, X[tlad_star(st)], ws[t][st], with_work(T.A[tlad_star(st)], T.AS), T.AW);
+              ad_forward(dg, L, X[tlad_star(st)], ws[b * k + t][st], with_work(T.A[tlad_star(st)], T.AS), T.AW);
             }
           });
           // A[0] is the adjoint of the step's start state: it seeds the step
           // before; every A[st+1] was consumed (zeroed) by its stage's ad_update
           std::swap(T.A[0], T.A[nst]);
         }
+        CK(cudaEventRecord(T.ev_rev, stream));   // buffer b free again
       }
       ad_prologue(dg, L, T.A[nst]);
       CK(cudaGetLastError());
