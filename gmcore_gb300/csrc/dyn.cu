@@ -1306,7 +1306,7 @@ template <class R>
 constexpr int kUvLevels = std::is_same<R, float>::value ? 2 : 1;
 
 template <class R, bool MB>
-__global__ void GMC_BOUNDS_MB(R, 6, MB) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
+__global__ void GMC_BOUNDS_MB(R, 8, MB) k_update_uv(DGrid g, Slot<R> o, Slot<R> n, Work<R> w, R dt) {
   if constexpr (MB) { to_member(g, o); to_member(g, n); to_member(g, w); }   // member-batched launches
   constexpr int KB = kUvLevels<R>;
   extern __shared__ double sh[];
