@@ -240,7 +240,7 @@ struct YMarch {
 
 // Rows (or half rows) per band of the y passes: each thread marches one
 // column through a band.
-constexpr int kYBand = 20;
+constexpr int kYBand = 24;
 constexpr int kYThreads = 128;
 
 // Outer pass: fluxes fy of qx along y with the meridional mass flux, one

@@ -201,6 +201,15 @@ __device__ __forceinline__ void tile_pole_ring(const DGrid &g, int j, float *rin
 // formed once per column instead of once per RK4 interpolation.
 // HL, FD, RFD: half_lev, full_dlev and 1 / full_dlev in FP32 (index [k-1]),
 // from the grid tables or a shared-memory copy of them.
+//
+// Every RK4 position z = z0 + c w lies on the side of z0 = HL[k-1] that the
+// sign of w gives, so the level search (first layer l >= k with z <= HL[l]
+// for w > 0, first l <= k-1 with HL[l-1] <= z otherwise) mostly stops at the
+// layer next to z0, and the displacement mostly stays within one layer.  The
+// two layers k-1 and k and their table values are loaded once; a position or
+// displacement beyond them (or a NaN) takes the general search and walk,
+// which also flags a departure outside the column.  Same operations on the
+// same operands as the general path, so the same values.
 __device__ __forceinline__ float cflz_of_f(const float *HL, const float *FD, const float *RFD, int nlev, const float *wm,
                                            int stride, int k, float dt_, bool &bad) {
   auto W = [&](int l) { return wm[(l - 1) * stride]; };   // l = 1 .. nlev+1
@@ -218,15 +227,34 @@ __device__ __forceinline__ float cflz_of_f(const float *HL, const float *FD, con
     return l;
   };
   auto interp = [&](int l, float z) { return ((HL[l] - z) * W(l) + (z - HL[l - 1]) * W(l + 1)) * RFD[l - 1]; };
-  const float z0 = HL[k - 1];
-  const float w1 = W(k);
+  // layers k-1 (below z0 in eta) and k (above)
+  const float h0 = HL[k - 2], h1 = HL[k - 1], h2 = HL[k];
+  const float wkm = W(k - 1), wk = W(k), wkp = W(k + 1);
+  const float r0 = RFD[k - 2], r1 = RFD[k - 1];
+  auto at = [&](float w, float z) {   // wind at z of an RK4 stage moving with w
+    if (w > 0) {
+      if (z <= h2) return ((h2 - z) * wk + (z - h1) * wkp) * r1;   // layer k
+    } else if (h0 <= z) {
+      return ((h1 - z) * wkm + (z - h0) * wk) * r0;   // layer k-1
+    }
+    return interp(locate(w, z), z);
+  };
+  const float z0 = h1;
+  const float w1 = wk;
   const float z1 = z0 + 0.5f * dt_ * w1;
-  const float w2 = interp(locate(w1, z1), z1);
+  const float w2 = at(w1, z1);
   const float z2 = z0 + 0.5f * dt_ * w2;
-  const float w3 = interp(locate(w2, z2), z2);
+  const float w3 = at(w2, z2);
   const float z3 = z0 + dt_ * w3;
-  const float w4 = interp(locate(w3, z3), z3);
+  const float w4 = at(w3, z3);
   float deta = (w1 + 2.0f * w2 + 2.0f * w3 + w4) * (1.0f / 6.0f) * dt_;
+  if (deta >= 0) {   // within layer k
+    const float d = deta - FD[k - 1];
+    if (d < 0) return (1.0f + d * r1) + 0.0f;
+  } else {           // within layer k-1
+    const float d = fabsf(deta) - FD[k - 2];
+    if (d < 0) return -1.0f * ((1.0f + d * r0) + 0.0f);
+  }
   int ks, ke, s;
   if (deta < 0) { ks = k - 1; ke = 1; s = -1; } else { ks = k; ke = nlev; s = 1; }
   const float sf = deta < 0 ? -1.0f : 1.0f;
