@@ -456,13 +456,18 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
         }
         return us[lw];
       };
+      // the winds at i-1, i, i+1 are loaded once: a departure within one
+      // cell of the face (floor(a) = 0 or -1) interpolates between them, a
+      // longer one indexes the row (the same values either way)
+      const float uw = Ul(i - 1), u1 = Ul(i), ue = Ul(i + 1);
       auto at = [&](float a) {   // wind at i + a
         float fl = floorf(a);
-        int l = i + (int)fl;
         float f = a - fl;
+        if (fl == 0.0f) return (1.0f - f) * u1 + f * ue;
+        if (fl == -1.0f) return (1.0f - f) * uw + f * u1;
+        int l = i + (int)fl;
         return (1.0f - f) * Ul(l) + f * Ul(l + 1);
       };
-      const float u1 = Ul(i);
       const float u2 = at(0.5f * cdx * u1);
       const float u3 = at(0.5f * cdx * u2);
       const float u4 = at(cdx * u3);
@@ -470,7 +475,7 @@ __global__ void k_batch_cfl(DGrid g, const R *u, const R *v, R *cflx, R *cfly, R
       if (fabsf(c) > hx) raise_err(g, ERR_CFLX);   // NaN passes, as abs(cflx) > width does
       size_t o = ix3(nlat, nlon, i, j, k);
       cflx[o] = c;
-      divx[o] = fdiv((u1 - Ul(i - 1)) * lel, ac);
+      divx[o] = fdiv((u1 - uw) * lel, ac);
       divy[o] = fdiv(v[ix3(nhalf, nlon, i, j, k)] * la0 - v[ix3(nhalf, nlon, i, j - 1, k)] * la1, ac);
     }
   } else {
