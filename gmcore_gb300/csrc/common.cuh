@@ -76,6 +76,7 @@ struct DGrid {
   const double *hyai, *hybi, *half_lev, *half_dlev, *full_dlev;   // [k-1]
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
   int f_layer_mass;                                                // 1: the form's layer mass is dmA + dmB psr (FP32)
+  int tangent_inline;   // 1: the FP32 edge PV and pole PV form the tangential winds themselves (no u_lat/v_lon fields)
   const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables
   const float *hybi_f;                                             // FP32 copy of hybi [k-1]
   const float *full_dlev_rf;                                       // FP32 1 / full_dlev [k-1]

@@ -77,6 +77,57 @@ __global__ void GMC_BOUNDS(R, 8) k_mass_flux(DGrid g, Slot<R> s) {
   }
 }
 
+// FP32 tangential winds (operators_mod.F90:585-605) of two neighbouring points
+// (0-based i0, i0+1) of a row at one level, over the edge mass dA + dB psr:
+// v_lon on full row j from the meridional mass fluxes of half rows j-1 (hs) and
+// j (hn); u_lat on half row j from the zonal mass fluxes of full rows j (fs) and
+// j+1 (fn); mo: row j of the 2-D surface pressure.  Shared by the tangent-wind
+// kernel and the edge PV, which forms them itself where each value has one
+// reader (tangent_inline).
+struct TangentRow {
+  float w1, w2, dA, dB;
+  unsigned a, b, mo;   // v_lon: hs, hn; u_lat: fs, fn
+};
+__device__ __forceinline__ float2 vlon_pair(const TangentRow &t, const float *__restrict__ mfy,
+                                            const float *__restrict__ psr, int nlon, int i0) {
+  const unsigned i2 = i0 + 2 == nlon ? 0 : i0 + 2;
+  const float2 ys = *reinterpret_cast<const float2 *>(mfy + t.a + i0), yn = *reinterpret_cast<const float2 *>(mfy + t.b + i0);
+  const float yse = mfy[t.a + i2], yne = mfy[t.b + i2];
+  const float2 pc = *reinterpret_cast<const float2 *>(psr + t.mo + i0);
+  const float pe = psr[t.mo + i2];
+  const float mf0 = t.w1 * (ys.x + ys.y) + t.w2 * (yn.x + yn.y), mf1 = t.w1 * (ys.y + yse) + t.w2 * (yn.y + yne);
+  const float ml0 = (fmaf(t.dB, pc.x, t.dA) + fmaf(t.dB, pc.y, t.dA)) * 0.5f;
+  const float ml1 = (fmaf(t.dB, pc.y, t.dA) + fmaf(t.dB, pe, t.dA)) * 0.5f;
+  return make_float2(fdiv(mf0, ml0), fdiv(mf1, ml1));
+}
+__device__ __forceinline__ float2 ulat_pair(const TangentRow &t, const float *__restrict__ mfx,
+                                            const float *__restrict__ psr, int nlon, int i0) {
+  const unsigned im = i0 == 0 ? nlon - 1 : i0 - 1;
+  const float2 xs = *reinterpret_cast<const float2 *>(mfx + t.a + i0), xn = *reinterpret_cast<const float2 *>(mfx + t.b + i0);
+  const float xsw = mfx[t.a + im], xnw = mfx[t.b + im];
+  const float2 ps = *reinterpret_cast<const float2 *>(psr + t.mo + i0), pn = *reinterpret_cast<const float2 *>(psr + t.mo + nlon + i0);
+  const float mf0 = t.w1 * (xsw + xs.x) + t.w2 * (xnw + xn.x), mf1 = t.w1 * (xs.x + xs.y) + t.w2 * (xn.x + xn.y);
+  const float ml0 = (fmaf(t.dB, ps.x, t.dA) + fmaf(t.dB, pn.x, t.dA)) * 0.5f;
+  const float ml1 = (fmaf(t.dB, ps.y, t.dA) + fmaf(t.dB, pn.y, t.dA)) * 0.5f;
+  return make_float2(fdiv(mf0, ml0), fdiv(mf1, ml1));
+}
+// u_lat at one point (the first component of ulat_pair at i0)
+__device__ __forceinline__ float ulat_at(const TangentRow &t, const float *__restrict__ mfx, const float *__restrict__ psr,
+                                         int nlon, int i0) {
+  const unsigned im = i0 == 0 ? nlon - 1 : i0 - 1;
+  const float mf0 = t.w1 * (mfx[t.a + im] + mfx[t.a + i0]) + t.w2 * (mfx[t.b + im] + mfx[t.b + i0]);
+  const float ml0 = (fmaf(t.dB, psr[t.mo + i0], t.dA) + fmaf(t.dB, psr[t.mo + nlon + i0], t.dA)) * 0.5f;
+  return fdiv(mf0, ml0);
+}
+__device__ __forceinline__ TangentRow vlon_row(const DGrid &g, int j, int k) {
+  const unsigned hn = (unsigned)ix3(g.nhalf, g.nlon, 1, j, k);
+  return {ROWR(float, ftw1, j), ROWR(float, ftw2, j), g.dmA[k - 1], g.dmB[k - 1], hn - g.nlon, hn, (unsigned)(j - 1) * g.nlon};
+}
+__device__ __forceinline__ TangentRow ulat_row(const DGrid &g, int j, int k) {
+  const unsigned fs = (unsigned)ix3(g.nlat, g.nlon, 1, j, k);
+  return {ROWR(float, htw1, j), ROWR(float, htw2, j), g.dmA[k - 1], g.dmB[k - 1], fs, fs + g.nlon, (unsigned)(j - 1) * g.nlon};
+}
+
 // Tangential mass fluxes and winds (operators_mod.F90:585-605).
 template <class R, bool MB>
 __global__ void GMC_BOUNDS_MB(R, 8, MB) k_tangent_winds(DGrid g, Slot<R> s, Work<R> w) {
@@ -87,40 +138,20 @@ __global__ void GMC_BOUNDS_MB(R, 8, MB) k_tangent_winds(DGrid g, Slot<R> s, Work
   const unsigned mo = (unsigned)(j - 1) * nlon;
   if constexpr (std::is_same<R, float>::value) {
     if (g.baroclinic) {   // two points per thread, paired loads
-      const float dA = g.dmA[k - 1], dB = g.dmB[k - 1];
-      auto P2 = [](const float *p, unsigned o) { return *reinterpret_cast<const float2 *>(p + o); };
       if (j <= nhalf) {
-        const float w1 = ROWR(float, htw1, j), w2 = ROWR(float, htw2, j);
-        const unsigned fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon, ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
-        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
-          const unsigned im = i0 == 0 ? nlon - 1 : i0 - 1;
-          const float2 xs = P2(s.mfx_lon, fs + i0), xn = P2(s.mfx_lon, fn + i0);
-          const float xsw = s.mfx_lon[fs + im], xnw = s.mfx_lon[fn + im];
-          const float2 ps = P2(s.psr, mo + i0), pn = P2(s.psr, mo + nlon + i0);
-          const float mf0 = w1 * (xsw + xs.x) + w2 * (xnw + xn.x), mf1 = w1 * (xs.x + xs.y) + w2 * (xn.x + xn.y);
-          const float ml0 = (fmaf(dB, ps.x, dA) + fmaf(dB, pn.x, dA)) * 0.5f;
-          const float ml1 = (fmaf(dB, ps.y, dA) + fmaf(dB, pn.y, dA)) * 0.5f;
-          *reinterpret_cast<float2 *>(w.u_lat + ho + i0) = make_float2(fdiv(mf0, ml0), fdiv(mf1, ml1));
-        }
+        const TangentRow t = ulat_row(g, j, k);
+        const unsigned ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x)
+          *reinterpret_cast<float2 *>(w.u_lat + ho + i0) = ulat_pair(t, s.mfx_lon, s.psr, nlon, i0);
       }
       const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k);
       if (j == 1 || j == nlat) {
         for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x)
           *reinterpret_cast<float2 *>(w.v_lon + fo + i0) = make_float2(0.0f, 0.0f);
       } else {
-        const float w1 = ROWR(float, ftw1, j), w2 = ROWR(float, ftw2, j);
-        const unsigned hn = (unsigned)ix3(nhalf, nlon, 1, j, k), hs = hn - nlon;
-        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
-          const unsigned i2 = i0 + 2 == nlon ? 0 : i0 + 2;
-          const float2 ys = P2(s.mfy_lat, hs + i0), yn = P2(s.mfy_lat, hn + i0);
-          const float yse = s.mfy_lat[hs + i2], yne = s.mfy_lat[hn + i2];
-          const float2 pc = P2(s.psr, mo + i0);
-          const float pe = s.psr[mo + i2];
-          const float mf0 = w1 * (ys.x + ys.y) + w2 * (yn.x + yn.y), mf1 = w1 * (ys.y + yse) + w2 * (yn.y + yne);
-          const float ml0 = (fmaf(dB, pc.x, dA) + fmaf(dB, pc.y, dA)) * 0.5f;
-          const float ml1 = (fmaf(dB, pc.y, dA) + fmaf(dB, pe, dA)) * 0.5f;
-          *reinterpret_cast<float2 *>(w.v_lon + fo + i0) = make_float2(fdiv(mf0, ml0), fdiv(mf1, ml1));
-        }
+        const TangentRow t = vlon_row(g, j, k);
+        for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x)
+          *reinterpret_cast<float2 *>(w.v_lon + fo + i0) = vlon_pair(t, s.mfy_lat, s.psr, nlon, i0);
       }
       return;
     }
@@ -243,7 +274,17 @@ __global__ void GMC_BOUNDS(R, 6) k_pv(DGrid g, Slot<R> s, Work<R> w) {
   if (pole) {
     const double le = ROW(g.le_lat, j);
     const double sgn = j == 1 ? -1.0 : 1.0;
-    double p = ring_sum(nlon, red, [&](int i) { return sgn * (double)w.u_lat[ix3(nhalf, nlon, i, j, k)] * le; });
+    double p;
+    if constexpr (std::is_same<R, float>::value) {
+      if (g.tangent_inline) {   // u_lat of the pole half row, formed here
+        const TangentRow t = ulat_row(g, j, k);
+        p = ring_sum(nlon, red, [&](int i) { return sgn * (double)ulat_at(t, s.mfx_lon, s.psr, nlon, i - 1) * le; });
+      } else {
+        p = ring_sum(nlon, red, [&](int i) { return sgn * (double)w.u_lat[ix3(nhalf, nlon, i, j, k)] * le; });
+      }
+    } else {
+      p = ring_sum(nlon, red, [&](int i) { return sgn * (double)w.u_lat[ix3(nhalf, nlon, i, j, k)] * le; });
+    }
     pole_vor = p / nlon / ROW(g.area_cell, j == 1 ? 1 : nhalf + 1);
   }
   const R dl0 = ROWR(R, de_lon, j), dl1 = ROWR(R, de_lon, j + 1), dt = ROWR(R, de_lat, j), av = ROWR(R, area_vtx, j);
@@ -306,7 +347,7 @@ __device__ __forceinline__ PvRow pv_row(const DGrid &g, int jj, int k) {
 }
 
 template <class R, bool MB>
-__global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, R dt) {
+__global__ void GMC_BOUNDS_MB(R, 6, MB) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, R dt) {
   if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   const int j = blockIdx.x + 1, k = blockIdx.y + 1;
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
@@ -344,19 +385,23 @@ __global__ void GMC_BOUNDS(R, 8) k_pv_edges(DGrid g, Slot<R> s, Work<R> w, R dt)
       } else {
         const PvRow r0 = pv_row(g, j - 2, k), r1 = pv_row(g, j - 1, k), r2 = pv_row(g, j, k), r3 = pv_row(g, j + 1, k);
         const unsigned fo = (unsigned)ix3(nlat, nlon, 1, j, k);
+        const TangentRow tv = vlon_row(g, j, k);
         for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
           const float2 a0 = Q2(r0, i0), a1 = Q2(r1, i0), a2 = Q2(r2, i0), a3 = Q2(r3, i0);
-          const float2 un = P2(s.u_f, fo + i0), vt = P2(w.v_lon, fo + i0);
+          const float2 un = P2(s.u_f, fo + i0);
+          const float2 vt = g.tangent_inline ? vlon_pair(tv, s.mfy_lat, s.psr, nlon, i0) : P2(w.v_lon, fo + i0);
           *reinterpret_cast<float2 *>(s.pv_lon + fo + i0) =
               make_float2(face(a1.x, a2.x, a3.x, a0.x, un.x, vt.x), face(a1.y, a2.y, a3.y, a0.y, un.y, vt.y));
         }
       }
       if (j <= nhalf) {   // pv_lat: pv of half row j at columns i-2 .. i+1 (0-based i0-2 .. i0+2 for the pair)
         const unsigned ho = (unsigned)ix3(nhalf, nlon, 1, j, k);
+        const TangentRow tu = ulat_row(g, j, k);
         for (int i0 = 2 * threadIdx.x; i0 < nlon; i0 += 2 * blockDim.x) {
           const float2 w2 = P2(pv, ho + (i0 == 0 ? nlon - 2 : i0 - 2)), c2 = P2(pv, ho + i0);
           const float e = pv[ho + (i0 + 2 == nlon ? 0 : i0 + 2)];
-          const float2 ut = P2(w.u_lat, ho + i0), vn = P2(s.v_f, ho + i0);
+          const float2 ut = g.tangent_inline ? ulat_pair(tu, s.mfx_lon, s.psr, nlon, i0) : P2(w.u_lat, ho + i0);
+          const float2 vn = P2(s.v_f, ho + i0);
           *reinterpret_cast<float2 *>(s.pv_lat + ho + i0) =
               make_float2(face(w2.y, c2.x, c2.y, w2.x, vn.x, ut.x), face(c2.x, c2.y, e, w2.y, vn.y, ut.y));
         }

@@ -684,6 +684,10 @@ struct Engine : EngineBase {
     dg.dlnp_ref = reinterpret_cast<const float *>(tables.base + offDL);
     dg.ps_ref = ps_ref;
     dg.f_layer_mass = kFP32 ? 1 : 0;
+    // the FP32 edge PV's default path (upwind order 3, pairs aligned beyond the
+    // poles) forms the tangential winds itself: each has one reader there
+    dg.tangent_inline = kFP32 && grid.cfg.baroclinic && grid.cfg.pv_scheme == GMC_PV_UPWIND &&
+                        grid.cfg.upwind_order_pv == 3 && (grid.cfg.nlon / 2) % 2 == 0;
     for (const FFix &x : ff) {
       x.d->ntaps_full = reinterpret_cast<const int *>(tables.base + x.nf);
       x.d->ntaps_half = reinterpret_cast<const int *>(tables.base + x.nh);
@@ -1026,7 +1030,7 @@ struct Engine : EngineBase {
   void forward_prepare(int m, const Slot<R> &s, double dt) { forward_prepare_w(work[m], s, dt); }
   void forward_prepare_w(Work<R> &w, const Slot<R> &s, double dt) {
     K("mass_flux", 1, [&] { launch_mass_flux<R>(dg, L, s); });
-    K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
+    if (!dg.tangent_inline) K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
     K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
     K("pv", 1, [&] { launch_pv<R>(dg, L, s, w); });
     K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w, dt); });
@@ -1090,7 +1094,7 @@ struct Engine : EngineBase {
     if (!dry) CK(cudaStreamWaitEvent(dside, dcm_ev, 0));
     K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, Ls, s, w); });
     if (!dry) CK(cudaEventRecord(dpt_ev, dside));
-    K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
+    if (!dg.tangent_inline) K("tangent_winds", 1, [&] { launch_tangent_winds<R>(dg, L, s, w); });
     K("kinetic_energy", 1, [&] { launch_kinetic_energy<R>(dg, L, s, w); });
     K("pv", 1, [&] { launch_pv<R>(dg, L, s, w); });
     K("pv_edges", 1, [&] { launch_pv_edges<R>(dg, L, s, w, dt); });
