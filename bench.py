@@ -328,14 +328,16 @@ def run_ours(args):
         a[...] = x
         return a
 
-    def e2e_run(m, nsteps, registered):
+    def e2e_run(m, nsteps, registered, exchange=False):
         """Wall time of nsteps steps through the public calls with host float64
         arrays: each step sets u, v, pt, phs and the tracers from the host,
         steps once and reads them back; the result feeds the next step.
         registered: the arrays are page-locked once (gmc_host_register, outside
         the timed region) and gathered/scattered/converted by device kernels
         over the host link; otherwise they are pageable and staged on host cores
-        through the library's pinned buffer."""
+        through the library's pinned buffer.  exchange: the same exchange as one
+        gmc_step_io call per step (tracer inputs move during the dynamics, the
+        fields move back during the tracer advection)."""
         host = {k: paged(v) for k, v in st.items()}
         out = {k: g.page_aligned(v.shape) for k, v in host.items() if k != "q"}   # touched: no page faults when timed
         qout = g.page_aligned(host["q"].shape)
@@ -346,15 +348,21 @@ def run_ours(args):
             barrier()
             t0 = time.perf_counter()
             for _ in range(nsteps):
-                for name in ("u_lon", "v_lat", "pt", "phs"):
-                    m.set_field(name, host[name])
-                for l in range(NTRACER):
-                    m.set_tracer(l, host["q"][l])
-                m.step(1)
-                for name in ("u_lon", "v_lat", "pt", "phs"):
-                    m.get_field(name, out=out[name])
-                for l in range(NTRACER):
-                    m.get_tracer(l, out=qout[l])
+                if exchange:
+                    m.step_io([(k, host[k]) for k in ("u_lon", "v_lat", "pt", "phs")] +
+                              [(l, host["q"][l]) for l in range(NTRACER)], 1,
+                              [(k, out[k]) for k in ("u_lon", "v_lat", "pt", "phs")] +
+                              [(l, qout[l]) for l in range(NTRACER)])
+                else:
+                    for name in ("u_lon", "v_lat", "pt", "phs"):
+                        m.set_field(name, host[name])
+                    for l in range(NTRACER):
+                        m.set_tracer(l, host["q"][l])
+                    m.step(1)
+                    for name in ("u_lon", "v_lat", "pt", "phs"):
+                        m.get_field(name, out=out[name])
+                    for l in range(NTRACER):
+                        m.get_tracer(l, out=qout[l])
                 for name in ("u_lon", "v_lat", "pt", "phs"):
                     host[name], out[name] = out[name], host[name]
                 host["q"], qout = qout, host["q"]
@@ -367,8 +375,11 @@ def run_ours(args):
 
     e2e_steps = max(2, min(args.steps, 10))
     e2e_staged_s, _ = e2e_run(model, e2e_steps, registered=False)
-    e2e_s, h2d = e2e_run(model, e2e_steps, registered=True)
+    e2e_sep_s, _ = e2e_run(model, e2e_steps, registered=True)
+    e2e_run(model, 1, registered=True, exchange=True)   # captures the exchange's step graphs
+    e2e_s, h2d = e2e_run(model, e2e_steps, registered=True, exchange=True)
     e2e_value = DT * e2e_steps / e2e_s * WORLD
+    e2e_sep_value = DT * e2e_steps / e2e_sep_s * WORLD
     e2e_staged_value = DT * e2e_steps / e2e_staged_s * WORLD
 
     # ---- per-kernel device timing for the roofline ----
@@ -437,7 +448,8 @@ def run_ours(args):
     # the FP64 form end to end through the same calls (like-for-like with the
     # FP64 CPU reference arm)
     e2e64_steps = 5
-    e2e64_s, _ = e2e_run(m64, e2e64_steps, registered=True)
+    e2e_run(m64, 1, registered=True, exchange=True)   # graph capture
+    e2e64_s, _ = e2e_run(m64, e2e64_steps, registered=True, exchange=True)
     e2e64_value = DT * e2e64_steps / e2e64_s * WORLD
     # the FP64 form's roofline: FP64 issue (its kernels keep the FP64 pipe
     # busy, profiles/fp64_form_c2.md); the dominant kernel's FLOP per launch
@@ -492,12 +504,16 @@ def run_ours(args):
                      "steps_compared": args.warmup + args.steps, "mixed_minus_fp64": errors,
                      "e2e": {"value": e2e64_value, "unit": "sim days/wall-day", "steps": e2e64_steps,
                              "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                             "path": "the registered-array path of e2e, FP64 form"},
+                             "path": "the exchange path of e2e (gmc_step_io, registered arrays), FP64 form"},
                      "roofline": fp64_roof},
             "e2e": {"value": e2e_value, "unit": "sim days/wall-day", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
-                    "path": "gmc_set_field/gmc_set_tracer + gmc_step(1) + gmc_get_field/gmc_get_tracer, host float64 "
-                            "arrays page-locked once with gmc_host_register (device-side gather/convert)",
+                    "path": "one gmc_step_io call per step (u, v, pt, phs and the tracers in, the same out; host "
+                            "float64 arrays page-locked once with gmc_host_register): tracer inputs move during the "
+                            "dynamics, the fields move back during the tracer advection",
+                    "separate_calls_value": e2e_sep_value,
+                    "separate_calls_path": "gmc_set_field/gmc_set_tracer + gmc_step(1) + gmc_get_field/gmc_get_tracer "
+                                           "on the same registered arrays (device-side gather/convert)",
                     "pageable_value": e2e_staged_value,
                     "pageable_path": "same calls on pageable host arrays (host-side gather/convert into the "
                                      "library's pinned staging buffer)"},

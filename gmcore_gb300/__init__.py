@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .abi import (Config, Diag, View, Stats, FfslFields, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
+from .abi import (Config, Diag, View, Io, Stats, FfslFields, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
                   TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, PV_TVD, TVD_NONE, TVD_VAN_LEER,
                   TVD_MC, FLUX_PPM, FLUX_VAN_LEER, LIMITER_NONE,
                   LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
@@ -30,7 +30,7 @@ EXPORTED = (
     "gmc_last_error", "gmc_destroy", "gmc_mesh_metric", "gmc_filter_taps", "gmc_make_ic",
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
     "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs", "gmc_host_register", "gmc_host_unregister",
-    "gmc_fp64_fma_peak", "gmc_fp32_fma_peak", "gmc_set_member_layout",
+    "gmc_fp64_fma_peak", "gmc_fp32_fma_peak", "gmc_set_member_layout", "gmc_step_io",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -64,6 +64,7 @@ def load(build_if_missing=True):
     lib.gmc_get_field.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, P(View)]
     lib.gmc_set_tracer.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View)]
     lib.gmc_get_tracer.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(View)]
+    lib.gmc_step_io.argtypes = [C.c_void_p, C.c_int32, P(Io), C.c_int32, C.c_int32, P(Io), C.c_int32]
     lib.gmc_prepare.argtypes = [C.c_void_p]
     lib.gmc_step.argtypes = [C.c_void_p, C.c_int32]
     lib.gmc_diagnose.argtypes = [C.c_void_p, C.c_int32, P(Diag)]
@@ -314,6 +315,31 @@ class Model:
             raise ValueError(f"out has shape {out.shape}, tracer {shape}")
         self._check(self.lib.gmc_get_tracer(self.h, member, l, C.byref(view_of(out))))
         return out
+
+    def step_io(self, inputs, nsteps, outputs, member=0):
+        """gmc_step_io: set `inputs`, advance nsteps, read `outputs` back into
+        the given arrays.  Each item is (name, array) for a field or (l, array)
+        for tracer l; arrays are C-ordered float64 of the field's shape
+        (registered with host_register for the overlapped transfers)."""
+        def items(seq):
+            arr = (Io * max(len(seq), 1))()
+            keep = []
+            for t, (key, a) in enumerate(seq):
+                if isinstance(key, str):
+                    nk = 1 if a.ndim == 2 else None
+                    arr[t].name = key.encode()
+                    arr[t].tracer = -1
+                    arr[t].view = view_of(a, nk)
+                else:
+                    arr[t].name = None
+                    arr[t].tracer = int(key)
+                    arr[t].view = view_of(a)
+                keep.append(a)
+            return arr, keep
+        ain, kin = items(inputs)
+        aout, kout = items(outputs)
+        self._check(self.lib.gmc_step_io(self.h, member, ain, len(inputs), nsteps, aout, len(outputs)))
+        return outputs
 
     def set_state(self, state, member=0):
         for name, a in state.items():

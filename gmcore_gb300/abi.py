@@ -82,6 +82,11 @@ class View(C.Structure):
     _fields_ = [("data", C.POINTER(C.c_double)), ("lb", C.c_int32 * 3), ("ub", C.c_int32 * 3)]
 
 
+class Io(C.Structure):
+    """gmc_io: a field (name) or, with name NULL, a tracer, and its view."""
+    _fields_ = [("name", C.c_char_p), ("tracer", C.c_int32), ("view", View)]
+
+
 def default_config(**overrides):
     """Reference namelist defaults (namelist_mod.F90:10-113) with the
     earth constants of const_mod.F90:56-66; keyword overrides win."""

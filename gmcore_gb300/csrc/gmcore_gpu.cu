@@ -231,6 +231,22 @@ __global__ void k_view_scatter(const T *__restrict__ src, ViewDims d, size_t row
   }
 }
 
+// FP64 staging <-> a field in the form's type (the overlapped transfers of
+// gmc_step_io: the DMA moves FP64 rows, the conversion runs on the device).
+template <class T>
+__global__ void k_from_f64(const double *__restrict__ src, size_t n, T *__restrict__ dst, T *__restrict__ dst2) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const T v = (T)src[t];
+    dst[t] = v;
+    if (dst2) dst2[t] = v;
+  }
+}
+template <class T>
+__global__ void k_to_f64(const T *__restrict__ src, size_t n, double *__restrict__ dst) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    dst[t] = (double)src[t];
+}
+
 inline double *view_row(const gmc_view &v, int nrow, size_t r) {
   const long n0 = v.ub[0] - v.lb[0] + 1, n1 = v.ub[1] - v.lb[1] + 1;
   const int k = (int)(r / nrow) + 1, j = (int)(r % nrow) + 1;
@@ -255,6 +271,15 @@ struct EngineBase {
   // three fields are u_lon, v_lat, gz (host, dense interior arrays)
   virtual void tlm(int nsteps, const double *const dx0[3], double *const dxn[3]) = 0;
   virtual void adjoint(int nsteps, int ckpt, const double *const lam_n[3], double *const lam_0[3]) = 0;
+  // gmc_step_io: inputs set, nsteps steps, outputs read back, with the
+  // transfers overlapped with the step where the dependencies allow; an item
+  // with tracer >= 0 is that tracer, otherwise the named field
+  struct IoItem {
+    std::string name;
+    int tracer;
+    gmc_view view;
+  };
+  virtual void step_io(int member, const std::vector<IoItem> &in, int nsteps, const std::vector<IoItem> &out) = 0;
   virtual void set_graphs(bool on) = 0;
   virtual int layout_in_use() const = 0;
   virtual bool set_layout(int lay) = 0;
@@ -554,6 +579,12 @@ struct Engine : EngineBase {
     }
     if (pinned) cudaFreeHost(pinned);
     pinned = nullptr;
+    if (xstream) cudaStreamDestroy(xstream);
+    if (xin_ev) cudaEventDestroy(xin_ev);
+    if (xdyn_ev) cudaEventDestroy(xdyn_ev);
+    if (xstage) cudaFree(xstage);
+    xstream = nullptr;
+    xstage = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -863,6 +894,189 @@ struct Engine : EngineBase {
     download_view<R>(q[((size_t)m * 2 + q_old) * ntr + l], grid.nlat, grid.nlev, dst);
   }
 
+  // ---- gmc_step_io: transfers overlapped with the step (one member) --------
+  // The dynamics of the first step need only the prognostic fields, so tracer
+  // inputs move over the host link while it runs, and its tracer step waits
+  // for them (xin_ev); the last step's fields are final when its dynamics end
+  // (xdyn_ev), so they move back while its tracer step runs.  The overlapped
+  // transfers are copy-engine DMA of FP64 rows between registered host memory
+  // and a device staging area, converted on the device; other items take the
+  // gmc_set_* / gmc_get_* paths before and after the step.
+  cudaStream_t xstream = nullptr;
+  cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr;
+  bool io_wait = false, io_rec = false;          // requested for this call's first / last step
+  bool cur_io_wait = false, cur_io_rec = false;  // in effect for the step being issued
+  bool io_waited = false;                        // the current step has issued its wait
+  double *xstage = nullptr;
+  size_t xstage_n = 0;
+  std::function<void()> after_last;              // enqueued after the last step's launches
+  void io_streams() {
+    if (xstream) return;
+    CK(cudaStreamCreateWithFlags(&xstream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&xin_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&xdyn_ev, cudaEventDisableTiming));
+  }
+  double *io_stage(size_t n) {
+    if (n > xstage_n) {
+      if (xstage) CK(cudaFree(xstage));
+      xstage = nullptr;
+      xstage_n = 0;
+      if (cudaMalloc(&xstage, n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        throw ApiError{GMC_ENOMEM, "device allocation failed (gmc_step_io staging)"};
+      }
+      xstage_n = n;
+    }
+    return xstage;
+  }
+  // registered host rows of a view with a uniform row pitch (nullptr otherwise)
+  const double *io_rows(const gmc_view &v, int nrow, int nk, size_t &pitch) const {
+    ViewDims vd;
+    const double *row0 = mapped_view(v, nrow, nk, vd);
+    if (!row0 || (nk > 1 && vd.n1 != nrow)) return nullptr;
+    pitch = (size_t)vd.n0 * sizeof(double);
+    return view_row(v, nrow, 0);   // host address: the DMA reads the registered range
+  }
+  static bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cs));
+    return cs == cudaStreamCaptureStatusActive;
+  }
+  void io_dyn_done(cudaStream_t st) {   // after the stages of a step
+    if (!cur_io_rec || dry) return;
+    CK(cudaEventRecordWithFlags(xdyn_ev, st, capturing(st) ? cudaEventRecordExternal : cudaEventRecordDefault));
+  }
+  void io_tracers_ready(cudaStream_t st) {   // before the tracer step reads q
+    if (!cur_io_wait || io_waited) return;
+    io_waited = true;
+    if (dry) return;
+    CK(cudaStreamWaitEvent(st, xin_ev, capturing(st) ? cudaEventWaitExternal : cudaEventWaitDefault));
+  }
+
+  void step_io(int m, const std::vector<IoItem> &in, int nsteps, const std::vector<IoItem> &out) override {
+    const bool overlap = nm == 1 && ntr > 0 && nsteps > 0;
+    const int nlon = grid.nlon;
+    // an overlapped item: registered host rows, the device field (R or FP64)
+    // and, for R fields, a slice of the FP64 staging area
+    struct Xfer {
+      double *host;
+      size_t pitch, rows;
+      R *pr, *pr2;
+      double *pd;
+      size_t stage;   // offset in xstage (R fields)
+      std::string name;
+      int tracer;
+    };
+    std::vector<Xfer> in_main, in_x, out_x, out_main;
+    std::vector<const IoItem *> in_sync, out_sync;
+    size_t nstage = 0;
+    auto plan = [&](const IoItem &x, bool input, std::vector<Xfer> &to) {
+      int nrow = grid.nlat, nk = grid.nlev;
+      if (x.tracer < 0) {
+        FieldInfo f = info(x.name);
+        nrow = f.nrow;
+        nk = f.nk;
+      }
+      size_t pitch = 0;
+      const double *h = overlap ? io_rows(x.view, nrow, nk, pitch) : nullptr;
+      if (!h) return false;
+      Xfer t{const_cast<double *>(h), pitch, (size_t)nrow * nk, nullptr, nullptr, nullptr, 0, x.name, x.tracer};
+      // the device fields of an input; an output's are found again after the
+      // step (download), these give its type
+      if (x.tracer >= 0) {
+        t.pr = q[((size_t)m * 2 + 0) * ntr + x.tracer];
+        if (input) t.pr2 = q[((size_t)m * 2 + 1) * ntr + x.tracer];   // both levels, as gmc_set_tracer
+      }
+      if (t.pr || t.tracer < 0) {
+        if (t.tracer < 0) locate(slots[m * 3 + old_i], m, x.name, &t.pr, &t.pd);
+        if (t.pr) {
+          t.stage = nstage;
+          nstage += t.rows * nlon;
+        }
+      }
+      to.push_back(t);
+      return true;
+    };
+    for (const IoItem &x : in)
+      if (!plan(x, true, x.tracer < 0 ? in_main : in_x)) in_sync.push_back(&x);
+    for (const IoItem &x : out)
+      if (!plan(x, false, x.tracer < 0 ? out_x : out_main)) out_sync.push_back(&x);
+    // the inputs that take the calls' own paths first (each synchronous)
+    for (const IoItem *x : in_sync) {
+      if (x->tracer >= 0) set_tracer(m, x->tracer, x->view);
+      else set_field(m, x->name, x->view);
+    }
+    if (nstage || !in_main.empty() || !in_x.empty() || !out_x.empty() || !out_main.empty()) {
+      io_streams();
+      io_stage(std::max<size_t>(nstage, 1));
+    }
+    auto blocks = [](size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); };
+    auto upload = [&](const Xfer &t, cudaStream_t st) {
+      double *dst = t.pr ? xstage + t.stage : t.pd;
+      CK(cudaMemcpy2DAsync(dst, nlon * sizeof(double), t.host, t.pitch, nlon * sizeof(double), t.rows,
+                           cudaMemcpyHostToDevice, st));
+      if (t.pr) {
+        const size_t n = t.rows * nlon;
+        k_from_f64<R><<<blocks(n), 256, 0, st>>>(xstage + t.stage, n, t.pr, t.pr2);
+        CK(cudaGetLastError());
+      }
+    };
+    auto download = [&](const Xfer &t, cudaStream_t st) {
+      // the state after the step: its new slot and tracer time level
+      R *pr = nullptr;
+      double *pd = nullptr;
+      if (t.tracer >= 0) pr = q[((size_t)m * 2 + q_old) * ntr + t.tracer];
+      else locate(slots[m * 3 + old_i], m, t.name, &pr, &pd);
+      const double *src = pd;
+      if (pr) {
+        const size_t n = t.rows * nlon;
+        k_to_f64<R><<<blocks(n), 256, 0, st>>>(pr, n, xstage + t.stage);
+        CK(cudaGetLastError());
+        src = xstage + t.stage;
+      }
+      CK(cudaMemcpy2DAsync(t.host, t.pitch, src, nlon * sizeof(double), nlon * sizeof(double), t.rows,
+                           cudaMemcpyDeviceToHost, st));
+    };
+    // fields on the context stream ahead of the step; tracers on xstream,
+    // which the first step's tracer advection waits for
+    for (const Xfer &t : in_main) upload(t, stream);
+    if (!in_x.empty()) {
+      // after the fields (the link carries one direction's copies at a time
+      // best; the fields are needed first)
+      CK(cudaEventRecord(xin_ev, stream));
+      CK(cudaStreamWaitEvent(xstream, xin_ev, 0));
+      for (const Xfer &t : in_x) upload(t, xstream);
+      CK(cudaEventRecord(xin_ev, xstream));
+      io_wait = true;
+    }
+    // after the last step's launches: its fields once its dynamics are done
+    // (xstream), the tracers after the step (context stream)
+    if (!out_x.empty() || !out_main.empty()) {
+      io_rec = !out_x.empty();
+      after_last = [&]() {
+        if (!out_x.empty()) {
+          CK(cudaStreamWaitEvent(xstream, xdyn_ev, 0));
+          for (const Xfer &t : out_x) download(t, xstream);
+        }
+        for (const Xfer &t : out_main) download(t, stream);
+      };
+    }
+    struct Reset {
+      Engine *e;
+      ~Reset() {
+        e->io_wait = e->io_rec = false;
+        e->after_last = nullptr;
+        if (e->xstream) cudaStreamSynchronize(e->xstream);
+      }
+    } reset{this};
+    step(nsteps);
+    if (xstream) CK(cudaStreamSynchronize(xstream));
+    for (const IoItem *x : out_sync) {
+      if (x->tracer >= 0) get_tracer(m, x->tracer, x->view);
+      else get_field(m, x->name, x->view);
+    }
+  }
+
   // Operator entry point: one horizontal FFSL flux with pool-allocated scratch.
   void ffsl_hflx(const gmc_ffsl_fields &f, double dt) override {
     if (!f.q || !f.u || !f.v || !f.mfx || !f.mfy || !f.cflx || !f.cfly || !f.divx || !f.divy || !f.qmfx || !f.qmfy)
@@ -938,6 +1152,7 @@ struct Engine : EngineBase {
     const double dt_adv = grid.cfg.dt_adv;
     accum_wind(m, n, false);
     if (advect) {
+      io_tracers_ready(L.stream);   // tracer inputs of gmc_step_io
       BatchView<R> bv{};
       bv.u = b.u; bv.v = b.v; bv.mfx = b.mfx; bv.mfy = b.mfy;
       bv.cflx = b.cflx; bv.cfly = b.cfly; bv.divx = b.divx; bv.divy = b.divy; bv.cflz = b.cflz;
@@ -968,6 +1183,7 @@ struct Engine : EngineBase {
         }
       }
     }
+    io_tracers_ready(L.stream);   // a step without tracer advection still orders them
     // copy_old_m
     if (!dry) {
       CK(cudaMemcpyAsync(b.old_phs_f, n.phs_f, two_d() * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
@@ -1507,9 +1723,10 @@ struct Engine : EngineBase {
   // While a graph is replayed the host logic of the step still runs (dry
   // mode: launches skipped, counters advanced).
   struct GraphKey {
-    int o, n, su, sm, sw, adv, qo, layout;
+    int o, n, su, sm, sw, adv, qo, layout, io;   // io: gmc_step_io's wait (1) and record (2)
     bool operator<(const GraphKey &b) const {
-      return std::tie(o, n, su, sm, sw, adv, qo, layout) < std::tie(b.o, b.n, b.su, b.sm, b.sw, b.adv, b.qo, b.layout);
+      return std::tie(o, n, su, sm, sw, adv, qo, layout, io) <
+             std::tie(b.o, b.n, b.su, b.sm, b.sw, b.adv, b.qo, b.layout, b.io);
     }
   };
   std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -1695,6 +1912,7 @@ struct Engine : EngineBase {
       const Slot<R> &N = slots[m * 3 + n];
       if (grid.cfg.use_div_damp)
         K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke, work[m].du); });
+      io_dyn_done(L.stream);   // the new state's fields are final (gmc_step_io)
       if (ntr > 0) {
         uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
         adv_run(m, N, ring && time_step > 0);
@@ -1725,6 +1943,9 @@ struct Engine : EngineBase {
     const bool use_graphs = graphs_on && !prof;
     for (int it = 0; it < nsteps; ++it) {
       const int o = old_i, n = new_i;
+      cur_io_wait = io_wait && it == 0;
+      cur_io_rec = io_rec && it == nsteps - 1;
+      io_waited = false;
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
       const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
       if (ring) alert_ring = true;
@@ -1737,7 +1958,8 @@ struct Engine : EngineBase {
         if (cand >= 0) lay = layouts[cand];
       }
       if (use_graphs) {
-        const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old, lay};
+        const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old, lay,
+                           (cur_io_wait ? 1 : 0) | (cur_io_rec ? 2 : 0)};
         auto gi = graphs.find(key);
         if (gi == graphs.end()) {
           cudaGraph_t gr = nullptr;
@@ -1788,6 +2010,8 @@ struct Engine : EngineBase {
       std::swap(old_i, new_i);
       ++time_step;
     }
+    cur_io_wait = cur_io_rec = false;
+    if (after_last) after_last();
     CK(cudaEventRecord(ev_b, stream));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
@@ -2104,6 +2328,36 @@ int gmc_step(gmc_ctx *ctx, int32_t nsteps) {
   if (nsteps < 0) return fail(ctx, GMC_EINVAL, "nsteps < 0");
   return guarded(ctx, [&]() {
     ctx->eng->step(nsteps);
+    return error_word_status(ctx, ctx->eng->read_error());
+  });
+}
+
+int gmc_step_io(gmc_ctx *ctx, int32_t member, const gmc_io *in, int32_t n_in, int32_t nsteps, const gmc_io *out,
+                int32_t n_out) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  if (nsteps < 0 || n_in < 0 || n_out < 0 || (n_in > 0 && !in) || (n_out > 0 && !out))
+    return fail(ctx, GMC_EINVAL, "negative count or null item array");
+  return guarded(ctx, [&]() {
+    // every item is checked before anything moves
+    auto items = [&](const gmc_io *a, int n) {
+      std::vector<EngineBase::IoItem> v;
+      for (int t = 0; t < n; ++t) {
+        std::string err;
+        int nrow = ctx->cfg.nlat, nk = ctx->cfg.nlev;
+        if (a[t].name) {
+          field_dims(ctx->cfg, a[t].name, nrow, nk);
+        } else if (a[t].tracer < 0 || a[t].tracer >= ctx->cfg.ntracer) {
+          throw ApiError{GMC_EINVAL, "tracer index out of range"};
+        }
+        if (!check_view(&a[t].view, ctx->cfg.nlon, nrow, nk, err)) throw ApiError{GMC_EINVAL, err};
+        v.push_back({a[t].name ? std::string(a[t].name) : std::string(), a[t].name ? -1 : a[t].tracer, a[t].view});
+      }
+      return v;
+    };
+    const std::vector<EngineBase::IoItem> vin = items(in, n_in), vout = items(out, n_out);
+    ctx->eng->step_io(member, vin, nsteps, vout);
     return error_word_status(ctx, ctx->eng->read_error());
   });
 }

@@ -173,6 +173,25 @@ int gmc_step(gmc_ctx *ctx, int32_t nsteps);
 int gmc_get_field(gmc_ctx *ctx, int32_t member, const char *name, const gmc_view *v);
 int gmc_get_tracer(gmc_ctx *ctx, int32_t member, int32_t tracer, const gmc_view *v);
 
+/* One exchange of a coupled step: the inputs set (as gmc_set_field /
+ * gmc_set_tracer), nsteps steps (as gmc_step), the outputs read back (as
+ * gmc_get_field / gmc_get_tracer), with the same results, status and error
+ * word as those calls in that order.  An item names a field (name) or, with
+ * name NULL, a tracer (tracer).  Where the host arrays lie in registered
+ * ranges (gmc_host_register) with one row pitch, the transfers overlap the
+ * step: tracer inputs move while the first step's dynamics run, and field
+ * outputs while the last step's tracer advection runs (one-member contexts
+ * with tracers); the rest move before and after the step.  No reference
+ * counterpart: the field exchange a driver coupled through host arrays makes
+ * around time_integrate (gmcore_mod.F90:138-139). */
+typedef struct gmc_io {
+  const char *name;   /* field name, or NULL for a tracer        */
+  int32_t tracer;     /* tracer index when name is NULL           */
+  gmc_view view;
+} gmc_io;
+int gmc_step_io(gmc_ctx *ctx, int32_t member, const gmc_io *in, int32_t n_in, int32_t nsteps, const gmc_io *out,
+                int32_t n_out);
+
 /* Global integrals of the current state (gmcore_mod.F90:213-341). */
 int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out);
 

@@ -78,6 +78,13 @@ module gmcore_gpu_mod
     integer(c_int32_t) :: ub(3)
   end type gmc_view
 
+  ! an item of gmc_step_io: a field (name, a C string) or, with name null, a tracer
+  type, bind(c) :: gmc_io
+    type(c_ptr)        :: name
+    integer(c_int32_t) :: tracer
+    type(gmc_view)     :: view
+  end type gmc_io
+
   type, bind(c) :: gmc_ffsl_fields
     type(c_ptr) :: q, u, v, mfx, mfy, cflx, cfly, divx, divy, qmfx, qmfy
   end type gmc_ffsl_fields
@@ -149,6 +156,14 @@ module gmcore_gpu_mod
       integer(c_int32_t), value :: member, tracer
       type(gmc_view), intent(in) :: v
     end function gmc_get_tracer
+
+    integer(c_int) function gmc_step_io(ctx, member, in, n_in, nsteps, out, n_out) bind(c, name='gmc_step_io')
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: member, n_in, nsteps, n_out
+      type(gmc_io), intent(in) :: in(*)
+      type(gmc_io), intent(in) :: out(*)
+    end function gmc_step_io
 
     integer(c_int) function gmc_diagnose(ctx, member, out) bind(c, name='gmc_diagnose')
       import
