@@ -272,9 +272,10 @@ int gmc_set_graphs(gmc_ctx *ctx, int32_t on);
 int gmc_host_register(void *ptr, size_t bytes);
 int gmc_host_unregister(void *ptr);
 
-/* Timing of the last gmc_step call: device time between CUDA events
- * recorded on the context's stream around the whole call, and the number
- * of kernels it launched.  An ensemble context (n_members > 1) times its
+/* Timing of the last gmc_step call (or of the steps of the last gmc_step_io
+ * call, with its tracer outputs): device time between CUDA events recorded on
+ * the context's stream around the whole call, and the number of kernels it
+ * launched.  An ensemble context (n_members > 1) times its
  * launch layouts on its first steps and keeps the fastest: layout 0 launches
  * each member's kernels separately over up to 8 streams; layout G > 0 runs G
  * groups of members, each group one member-batched launch per operator on its
