@@ -929,12 +929,14 @@ struct Engine : EngineBase {
     }
     return xstage;
   }
-  // registered host rows of a view with a uniform row pitch (nullptr otherwise)
-  const double *io_rows(const gmc_view &v, int nrow, int nk, size_t &pitch) const {
+  // registered host rows of a view (nullptr otherwise): the first interior
+  // row, the row pitch and the level stride in bytes
+  const double *io_rows(const gmc_view &v, int nrow, int nk, size_t &pitch, size_t &lstride) const {
     ViewDims vd;
     const double *row0 = mapped_view(v, nrow, nk, vd);
-    if (!row0 || (nk > 1 && vd.n1 != nrow)) return nullptr;
+    if (!row0) return nullptr;
     pitch = (size_t)vd.n0 * sizeof(double);
+    lstride = (size_t)vd.n0 * vd.n1 * sizeof(double);
     return view_row(v, nrow, 0);   // host address: the DMA reads the registered range
   }
   static bool capturing(cudaStream_t st) {
@@ -960,7 +962,8 @@ struct Engine : EngineBase {
     // and, for R fields, a slice of the FP64 staging area
     struct Xfer {
       double *host;
-      size_t pitch, rows;
+      size_t pitch, lstride, rows;
+      int nrow, nk;
       R *pr, *pr2;
       double *pd;
       size_t stage;   // offset in xstage (R fields)
@@ -977,10 +980,11 @@ struct Engine : EngineBase {
         nrow = f.nrow;
         nk = f.nk;
       }
-      size_t pitch = 0;
-      const double *h = overlap ? io_rows(x.view, nrow, nk, pitch) : nullptr;
+      size_t pitch = 0, lstride = 0;
+      const double *h = overlap ? io_rows(x.view, nrow, nk, pitch, lstride) : nullptr;
       if (!h) return false;
-      Xfer t{const_cast<double *>(h), pitch, (size_t)nrow * nk, nullptr, nullptr, nullptr, 0, x.name, x.tracer};
+      Xfer t{const_cast<double *>(h), pitch, lstride, (size_t)nrow * nk, nrow, nk, nullptr, nullptr, nullptr, 0,
+             x.name, x.tracer};
       // the device fields of an input; an output's are found again after the
       // step (download), these give its type
       if (x.tracer >= 0) {
@@ -1011,10 +1015,22 @@ struct Engine : EngineBase {
       io_stage(std::max<size_t>(nstage, 1));
     }
     auto blocks = [](size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); };
+    // the rows of a view: one pitched copy when its levels follow each other
+    // at the row pitch, else one per level
+    auto copy_rows = [&](const Xfer &t, double *dev, bool h2d, cudaStream_t st) {
+      const size_t w = nlon * sizeof(double);
+      const bool one = t.nk == 1 || t.lstride == t.pitch * t.nrow;
+      for (int k = 0; k < (one ? 1 : t.nk); ++k) {
+        double *d = dev + (size_t)k * t.nrow * nlon;
+        char *h = reinterpret_cast<char *>(t.host) + (size_t)k * t.lstride;
+        const size_t rows = one ? t.rows : (size_t)t.nrow;
+        if (h2d) CK(cudaMemcpy2DAsync(d, w, h, t.pitch, w, rows, cudaMemcpyHostToDevice, st));
+        else CK(cudaMemcpy2DAsync(h, t.pitch, d, w, w, rows, cudaMemcpyDeviceToHost, st));
+      }
+    };
     auto upload = [&](const Xfer &t, cudaStream_t st) {
       double *dst = t.pr ? xstage + t.stage : t.pd;
-      CK(cudaMemcpy2DAsync(dst, nlon * sizeof(double), t.host, t.pitch, nlon * sizeof(double), t.rows,
-                           cudaMemcpyHostToDevice, st));
+      copy_rows(t, dst, true, st);
       if (t.pr) {
         const size_t n = t.rows * nlon;
         k_from_f64<R><<<blocks(n), 256, 0, st>>>(xstage + t.stage, n, t.pr, t.pr2);
@@ -1034,8 +1050,7 @@ struct Engine : EngineBase {
         CK(cudaGetLastError());
         src = xstage + t.stage;
       }
-      CK(cudaMemcpy2DAsync(t.host, t.pitch, src, nlon * sizeof(double), nlon * sizeof(double), t.rows,
-                           cudaMemcpyDeviceToHost, st));
+      copy_rows(t, const_cast<double *>(src), false, st);
     };
     // fields on the context stream ahead of the step; tracers on xstream,
     // which the first step's tracer advection waits for

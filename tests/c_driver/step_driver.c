@@ -4,7 +4,10 @@
  * src/dynamics/gmcore_mod.F90:97-144): it keeps its own state arrays in the
  * reference's layout -- column-major, with longitude and latitude halos --
  * hands them to the library through gmc_view, runs the prologue and N steps,
- * reads the state back into the same halo'd arrays and calls diagnose.
+ * reads the state back into the same halo'd arrays and calls diagnose.  The
+ * time loop is that of a driver coupled through its host arrays: the arrays
+ * are registered (gmc_host_register) and each step is one gmc_step_io
+ * exchange that sets the state from them and reads it back into them.
  *
  *   step_driver KIND NLON NLAT NLEV DT SCHEME NTRACER PRECISION NSTEPS SEED OUT
  *
@@ -14,6 +17,7 @@
  * eight diagnose values.  Exit status 0 on success, else the failing call's
  * status with its message on stderr.
  */
+#define _POSIX_C_SOURCE 200112L /* posix_memalign */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -25,6 +29,7 @@
 
 typedef struct {
   double *data;
+  size_t bytes; /* whole pages, so that each array registers on its own */
   int lb[3], ub[3];
 } Arr;
 
@@ -34,7 +39,10 @@ static Arr arr_new(int ni, int nj, int nk) {
   a.lb[1] = 1 - HY; a.ub[1] = nj + HY;
   a.lb[2] = 1;      a.ub[2] = nk;
   size_t n = (size_t)(a.ub[0] - a.lb[0] + 1) * (a.ub[1] - a.lb[1] + 1) * nk;
-  a.data = (double *)malloc(n * sizeof(double));
+  a.bytes = (n * sizeof(double) + 4095) / 4096 * 4096;
+  void *p = NULL;
+  if (posix_memalign(&p, 4096, a.bytes) != 0) exit(7);
+  a.data = (double *)p;
   for (size_t t = 0; t < n; ++t) a.data[t] = -9.99e33; /* halo fill: must never be read */
   return a;
 }
@@ -139,7 +147,26 @@ int main(int argc, char **argv) {
   }
 
   check(ctx, gmc_prepare(ctx), "gmc_prepare");
-  for (int s = 0; s < nsteps; ++s) check(ctx, gmc_step(ctx, 1), "gmc_step"); /* the driver's time loop */
+  /* the driver's time loop: one exchange per step through the registered arrays */
+  gmc_io io[16];
+  int nio = 0;
+  const char *names[4] = {"u_lon", "v_lat", bc ? "pt" : "gz", "phs"};
+  Arr *arrs[4] = {&A_u, &A_v, &A_t, &A_phs};
+  for (int f = 0; f < (bc ? 4 : 3); ++f) {
+    check(ctx, gmc_host_register(arrs[f]->data, arrs[f]->bytes), "gmc_host_register");
+    io[nio].name = names[f];
+    io[nio].tracer = -1;
+    io[nio].view = view_of(arrs[f]);
+    ++nio;
+  }
+  for (int l = 0; bc && l < ntr; ++l) {
+    check(ctx, gmc_host_register(A_q[l].data, A_q[l].bytes), "gmc_host_register");
+    io[nio].name = NULL;
+    io[nio].tracer = l;
+    io[nio].view = view_of(&A_q[l]);
+    ++nio;
+  }
+  for (int s = 0; s < nsteps; ++s) check(ctx, gmc_step_io(ctx, 0, io, nio, 1, io, nio), "gmc_step_io");
   int64_t ts = -1;
   check(ctx, gmc_time_step(ctx, &ts), "gmc_time_step");
   if (ts != nsteps) {
@@ -162,6 +189,8 @@ int main(int argc, char **argv) {
   }
   gmc_diag d;
   check(ctx, gmc_diagnose(ctx, 0, &d), "gmc_diagnose");
+  for (int f = 0; f < (bc ? 4 : 3); ++f) check(ctx, gmc_host_unregister(arrs[f]->data), "gmc_host_unregister");
+  for (int l = 0; bc && l < ntr; ++l) check(ctx, gmc_host_unregister(A_q[l].data), "gmc_host_unregister");
 
   FILE *f = fopen(argv[11], "wb");
   if (!f) {

@@ -1,8 +1,10 @@
 """A non-Python caller of the C ABI: tests/c_driver/step_driver.c, a plain C
 host program built with gcc against include/gmcore_gpu.h and linked to the
 library, runs the seeded state through create / set (halo'd column-major
-arrays) / prepare / N steps / get / diagnose.  Its output must match the FP64
-oracle run on the same state, as the Python-driven parity tests do."""
+arrays) / prepare / N steps / get / diagnose, each step one gmc_step_io
+exchange through its registered halo'd arrays (the overlapped transfers with
+row pitch and level stride).  Its output must match the FP64 oracle run on the
+same state, as the Python-driven parity tests do."""
 import os
 import subprocess
 
