@@ -19,7 +19,7 @@ from .abi import (Config, Diag, View, Io, Stats, FfslFields, default_config, STA
                   TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, PV_TVD, TVD_NONE, TVD_VAN_LEER,
                   TVD_MC, FLUX_PPM, FLUX_VAN_LEER, LIMITER_NONE,
                   LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
-                  VCOORD_WRF_L64, PREC_FP64, PREC_MIXED)
+                  VCOORD_WRF_L64, PREC_FP64, PREC_MIXED, FORCING_NONE, FORCING_HELD_SUAREZ)
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libgmcore_gpu.so")

@@ -30,6 +30,7 @@ FLUX_PPM, FLUX_VAN_LEER = 0, 1
 LIMITER_NONE, LIMITER_MONO, LIMITER_PD = 0, 1, 2
 VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32, VCOORD_WRF_L64 = 0, 26, 32, 64
 PREC_FP64, PREC_MIXED = 0, 1
+FORCING_NONE, FORCING_HELD_SUAREZ = 0, 1
 
 
 class Config(C.Structure):
@@ -55,7 +56,7 @@ class Config(C.Structure):
         ("n_members", C.c_int32),
         ("radius", C.c_double), ("omega", C.c_double), ("g", C.c_double), ("Rd", C.c_double),
         ("cpd", C.c_double), ("p0", C.c_double),
-        ("tvd_limiter_type", C.c_int32), ("div_damp_coef4", C.c_double),
+        ("tvd_limiter_type", C.c_int32), ("div_damp_coef4", C.c_double), ("forcing", C.c_int32),
     ]
 
     def as_dict(self):
@@ -113,6 +114,7 @@ def default_config(**overrides):
     pi = math.atan(1.0) * 4.0
     c.radius, c.omega, c.g, c.Rd, c.cpd, c.p0 = 6.37122e6, 2 * pi / 86400.0, 9.80616, 287.04, 1004.0, 1.0e5
     c.tvd_limiter_type, c.div_damp_coef4 = TVD_VAN_LEER, 0.01
+    c.forcing = FORCING_NONE
     for k, v in overrides.items():
         if not hasattr(c, k):
             raise KeyError(k)

@@ -44,7 +44,7 @@ struct RowF {
   const float *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
   const float *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
   const float *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
-  const float *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat, *half_cos_lat;
+  const float *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat, *half_cos_lat, *full_sin_lat;
 };
 
 // Grid constants and 1-D metric tables (device pointers).  Row tables are
@@ -65,7 +65,7 @@ struct DGrid {
   const double *area_lon, *area_lon_west, *area_lon_east, *area_lon_north, *area_lon_south;
   const double *area_lat, *area_lat_west, *area_lat_east, *area_lat_north, *area_lat_south;
   const double *area_vtx, *de_lon, *le_lon, *de_lat, *le_lat, *full_f, *half_f;
-  const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat, *half_cos_lat;
+  const double *ftw1, *ftw2, *htw1, *htw2, *full_cos_lat, *half_lat, *half_cos_lat, *full_sin_lat;
   RowF f;
   int flux_type;        // GMC_FLUX_*
   int tvd_limiter;      // GMC_TVD_* (pv_scheme = tvd)
@@ -77,6 +77,9 @@ struct DGrid {
   const float *dmA, *dmB;                                          // FP32 layer-mass coefficients [k-1]
   int f_layer_mass;                                                // 1: the form's layer mass is dmA + dmB psr (FP32)
   int tangent_inline;   // 1: the FP32 edge PV and pole PV form the tangential winds themselves (no u_lat/v_lon fields)
+  int forcing;                  // GMC_FORCING_*
+  const double *full_lev;       // eta at full levels [k-1]
+  const float *ph_lev_a;        // FP32 hyai(k) (p0 - ptop) + ptop [k-1]: ph_lev = a + hybi psr
   const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables
   const float *hybi_f;                                             // FP32 copy of hybi [k-1]
   const float *full_dlev_rf;                                       // FP32 1 / full_dlev [k-1]

@@ -1842,6 +1842,58 @@ __global__ void k_div_damp(DGrid g, Slot<R> n, const R *div) {
   }
 }
 
+// Held-Suarez forcing of the new state after the integrator (test_forcing_run,
+// gmcore_mod.F90:586; held_suarez_test_apply_forcing,
+// held_suarez_test_mod.F90:74-112): Rayleigh friction kv(sigma) of u (no pole
+// rows) and v below sigma_b = 0.7, and Newtonian relaxation of pt at rate
+// kt(sigma, lat) toward the equilibrium temperature Teq(p, lat).  The pressure
+// is the full-level mean of the half levels from phs_f and the temperature
+// pt (p/p0)^kappa, as calc_ph and calc_t (operators_mod.F90:136-190) leave
+// them in the new state.  Blocks 0 .. nlat-1 take the full rows (u and pt),
+// the rest the half rows (v).
+template <class R, bool MB>
+__global__ void k_held_suarez(DGrid g, Slot<R> n, double dt) {
+  if constexpr (MB) { to_member(g, n); }   // member-batched launches
+  const int k = blockIdx.y + 1, nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  constexpr double sig_b = 0.7, kf = 1.0 / 86400.0, ka = 0.025 / 86400.0, ks = 0.25 / 86400.0;
+  constexpr double dt_lat = 60.0, dpt_lev = 10.0, p0 = 1.0e5;   // K, K, Pa
+  const double sfac = fmax(0.0, (g.full_lev[k - 1] - sig_b) / (1.0 - sig_b));
+  const R ckv = (R)(dt * (kf * sfac));
+  if ((int)blockIdx.x >= nlat) {
+    const int j = blockIdx.x - nlat + 1;
+    const unsigned c0 = (unsigned)ix3(nhalf, nlon, 1, j, k);
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_lat[c0 + i] = n.v_lat[c0 + i] - ckv * n.v_lat[c0 + i];
+    return;
+  }
+  const int j = blockIdx.x + 1;
+  const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k), m0 = (unsigned)(j - 1) * nlon;
+  if (j != 1 && j != nlat)
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_lon[c0 + i] = n.u_lon[c0 + i] - ckv * n.u_lon[c0 + i];
+  const double c = ROW(g.full_cos_lat, j), sn = ROW(g.full_sin_lat, j), c2 = c * c;
+  const double kt = ka + (ks - ka) * sfac * (c2 * c2);
+  if constexpr (std::is_same<R, double>::value) {
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const double phs = n.phs_f[m0 + i];
+      const double ph = 0.5 * (ph_lev(g, k, phs) + ph_lev(g, k + 1, phs));
+      const double p_p0 = ph / p0, pw = pow(p_p0, g.kappa);
+      const double pt = n.pt[c0 + i], t = pt * pw;
+      const double teq = fmax(200.0, (315.0 - dt_lat * (sn * sn) - dpt_lev * log(p_p0) * c2) * pw);
+      n.pt[c0 + i] = pt - dt * kt * pt * (1.0 - teq / t);
+    }
+  } else {   // FP32: pressure from psr = phs_f - ptop
+    const float a0 = g.ph_lev_a[k - 1], a1 = g.ph_lev_a[k], b0 = g.hybi_f[k - 1], b1 = g.hybi_f[k];
+    const float s2 = (float)(dt_lat * (sn * sn)), d2 = (float)(dpt_lev * c2), ckt = (float)(dt * kt);
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const float psr = n.psr[m0 + i];
+      const float ph = 0.5f * (fmaf(b0, psr, a0) + fmaf(b1, psr, a1));
+      const float p_p0 = ph * (float)(1.0 / p0), pw = powf(p_p0, g.kappa_f);
+      const float pt = n.pt[c0 + i], t = pt * pw;
+      const float teq = fmaxf(200.0f, (315.0f - s2 - d2 * logf(p_p0)) * pw);
+      n.pt[c0 + i] = pt - ckt * pt * (1.0f - teq / t);
+    }
+  }
+}
+
 }  // namespace
 
 template <class R>
@@ -1856,5 +1908,12 @@ void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, 
 }
 template void launch_div_damp<double>(const DGrid &, const Launch &, const Slot<double> &, double *, double *);
 template void launch_div_damp<float>(const DGrid &, const Launch &, const Slot<float> &, float *, float *);
+
+template <class R>
+void launch_held_suarez(const DGrid &g, const Launch &L, const Slot<R> &n, double dt) {
+  mb_launch(L, [&](auto mb) { k_held_suarez<R, decltype(mb)::value><<<dim3(g.nlat + g.nhalf, g.nlev, L.members), L.threads, 0, L.stream>>>(g, n, dt); });
+}
+template void launch_held_suarez<double>(const DGrid &, const Launch &, const Slot<double> &, double);
+template void launch_held_suarez<float>(const DGrid &, const Launch &, const Slot<float> &, double);
 
 }  // namespace gmc

@@ -618,8 +618,16 @@ struct Engine : EngineBase {
     row(g.full_tangent_wgt1, &dg.ftw1, &dg.f.ftw1); row(g.full_tangent_wgt2, &dg.ftw2, &dg.f.ftw2);
     row(g.half_tangent_wgt1, &dg.htw1, &dg.f.htw1); row(g.half_tangent_wgt2, &dg.htw2, &dg.f.htw2);
     row(g.full_cos_lat, &dg.full_cos_lat, &dg.f.full_cos_lat); row(g.half_cos_lat, &dg.half_cos_lat, &dg.f.half_cos_lat); row(g.half_lat, &dg.half_lat, &dg.f.half_lat);
+    row(g.full_sin_lat, &dg.full_sin_lat, &dg.f.full_sin_lat);
     vec(g.hyai, &dg.hyai); vec(g.hybi, &dg.hybi); vec(g.half_lev, &dg.half_lev); vec(g.half_dlev, &dg.half_dlev);
     vec(g.full_dlev, &dg.full_dlev); vec(g.lon_damp_wgt_full, &dg.lon_damp_full);
+    vec(g.full_lev, &dg.full_lev);
+    {   // FP32 hybrid pressure coefficients of the half levels (Held-Suarez forcing)
+      std::vector<float> pa(g.nlev + 2, 0.f);
+      for (int k = 0; k <= g.nlev && g.cfg.baroclinic; ++k)
+        pa[k] = (float)(g.hyai[k] * (g.cfg.hybrid_coord_p0 - g.local_ptop) + g.local_ptop);
+      fixes.push_back({push(pa.data(), pa.size() * 4), (const void **)&dg.ph_lev_a});
+    }
     vec(g.div_c_lon, &dg.div_c_lon); vec(g.div_c_lat, &dg.div_c_lat);
     {
       std::vector<float> yo((size_t)g.nhalf * 4, 0.f);
@@ -715,6 +723,7 @@ struct Engine : EngineBase {
     dg.dlnp_ref = reinterpret_cast<const float *>(tables.base + offDL);
     dg.ps_ref = ps_ref;
     dg.f_layer_mass = kFP32 ? 1 : 0;
+    dg.forcing = grid.cfg.forcing;
     // the FP32 edge PV's default path (upwind order 3, pairs aligned beyond the
     // poles) forms the tangential winds itself: each has one reader there
     dg.tangent_inline = kFP32 && grid.cfg.baroclinic && grid.cfg.pv_scheme == GMC_PV_UPWIND &&
@@ -1868,6 +1877,8 @@ struct Engine : EngineBase {
             stage(m0, o, t3, n, dt);
             break;
         }
+        if (grid.cfg.forcing == GMC_FORCING_HELD_SUAREZ)   // test_forcing_run (gmcore_mod.F90:586)
+          K("held_suarez", 1, [&] { launch_held_suarez<R>(dg, L, slots[m0 * 3 + n], dt); });
         if (grid.cfg.use_div_damp)
           K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2,
             [&] { launch_div_damp<R>(dg, L, slots[m0 * 3 + n], work[m0].ke, work[m0].du); });
@@ -1925,6 +1936,8 @@ struct Engine : EngineBase {
           break;
       }
       const Slot<R> &N = slots[m * 3 + n];
+      if (grid.cfg.forcing == GMC_FORCING_HELD_SUAREZ)   // test_forcing_run (gmcore_mod.F90:586)
+        K("held_suarez", 1, [&] { launch_held_suarez<R>(dg, L, N, dt); });
       if (grid.cfg.use_div_damp)
         K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke, work[m].du); });
       io_dyn_done(L.stream);   // the new state's fields are final (gmc_step_io)
@@ -2253,6 +2266,7 @@ void gmc_config_default(gmc_config *c) {
   c->radius = 6.37122e6; c->omega = 2 * pi / 86400.0; c->g = 9.80616; c->Rd = 287.04; c->cpd = 1004.0; c->p0 = 1.0e5;
   c->tvd_limiter_type = GMC_TVD_VAN_LEER;
   c->div_damp_coef4 = 0.01;
+  c->forcing = GMC_FORCING_NONE;
 }
 
 int gmc_create(const gmc_config *cfg, gmc_ctx **out) {

@@ -246,6 +246,8 @@ std::string validate_config(const gmc_config &c) {
   if (c.n_members < 1) return "n_members must be >= 1";
   if (c.use_div_damp && c.div_damp_order != 2 && c.div_damp_order != 4) return "div_damp_order must be 2 or 4";
   if (c.lon_halo_width < 1) return "lon_halo_width must be >= 1";
+  if (c.forcing != GMC_FORCING_NONE && c.forcing != GMC_FORCING_HELD_SUAREZ) return "bad forcing";
+  if (c.forcing == GMC_FORCING_HELD_SUAREZ && !c.baroclinic) return "held_suarez forcing needs the baroclinic model";
   // device kernels index one field with 32-bit arithmetic
   if ((double)(c.nlev + 1) * c.nlat * c.nlon >= 2147483647.0) return "grid too large: (nlev+1)*nlat*nlon must be < 2^31";
   return "";

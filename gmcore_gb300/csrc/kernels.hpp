@@ -133,6 +133,7 @@ template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const S
 // Divergence damping of order 2 or 4 (div_damp_run, div_damp_mod.F90:89-139);
 // div and div2 are scratch cell fields.
 template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, R *div2);
+template <class R> void launch_held_suarez(const DGrid &g, const Launch &L, const Slot<R> &n, double dt);
 
 // ---- advection (adv.cu) ---------------------------------------------------
 // Horizontal FFSL flux of q (ffsl_calc_tracer_hflx_cell): inner advective

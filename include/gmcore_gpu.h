@@ -80,6 +80,9 @@ extern "C" {
 #define GMC_VCOORD_WRF_L32   32   /* hybrid_coord_wrf_l32  (hybrid_coord_test_mod.F90:565) */
 #define GMC_VCOORD_WRF_L64   64   /* hybrid_coord_wrf_l64  (hybrid_coord_test_mod.F90:734) */
 
+#define GMC_FORCING_NONE         0  /* test_case without forcing                   */
+#define GMC_FORCING_HELD_SUAREZ  1  /* test_case = 'held_suarez' (test_forcing_mod.F90:24-25) */
+
 #define GMC_PREC_FP64     0  /* FP64 everywhere                               */
 #define GMC_PREC_MIXED    1  /* FP32 bulk stencils/advection, FP64 pole rings,
                                 column sweeps, integrals and filter weights   */
@@ -115,6 +118,8 @@ typedef struct gmc_config {
   double  radius, omega, g, Rd, cpd, p0;   /* const_mod.F90:51-85 ('earth')     */
   int32_t tvd_limiter_type;        /* GMC_TVD_* (pv_scheme = tvd)                */
   double  div_damp_coef4;          /* namelist div_damp_coef4 (order 4)          */
+  int32_t forcing;                 /* GMC_FORCING_*: test forcing applied after the
+                                      integrator, before damping (gmcore_mod.F90:586) */
 } gmc_config;
 
 /* Diagnostics of gmcore_mod.F90:213-341 (FP64, compensated sums). */

@@ -35,6 +35,7 @@ module gmcore_gpu_mod
   integer(c_int32_t), parameter :: GMC_VCOORD_NONE = 0, GMC_VCOORD_TEST_L26 = 26, GMC_VCOORD_WRF_L32 = 32, &
                                    GMC_VCOORD_WRF_L64 = 64
   integer(c_int32_t), parameter :: GMC_PREC_FP64 = 0, GMC_PREC_MIXED = 1
+  integer(c_int32_t), parameter :: GMC_FORCING_NONE = 0, GMC_FORCING_HELD_SUAREZ = 1
 
   type, bind(c) :: gmc_config
     integer(c_int32_t) :: nlon, nlat, nlev
@@ -66,6 +67,7 @@ module gmcore_gpu_mod
     real(c_double)     :: radius, omega, g, Rd, cpd, p0
     integer(c_int32_t) :: tvd_limiter_type
     real(c_double)     :: div_damp_coef4
+    integer(c_int32_t) :: forcing
   end type gmc_config
 
   type, bind(c) :: gmc_diag

@@ -1615,6 +1615,40 @@ struct Model {
     for (int q = 0; q < 8; ++q) out[q] = v[q] / a;
   }
 
+  // held_suarez_test_apply_forcing (held_suarez_test_mod.F90:74-112) on the
+  // new state, whose ph and t the last stage's backward pass left
+  void held_suarez_forcing(State &s, double dt) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
+    const gmc::Grid &g = G();
+    const double sig_b = 0.7, kf = 1.0 / 86400.0, ka = 0.025 / 86400.0, ks = 0.25 / 86400.0;
+    const double dt_lat = 60.0, dpt_lev = 10.0, p0 = 1.0e5;
+    for (int k = 1; k <= nlev; ++k) {
+      const double kv = kf * std::max(0.0, (g.full_lev[k - 1] - sig_b) / (1.0 - sig_b));
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i) s.u_lon(i, j, k) = s.u_lon(i, j, k) - dt * kv * s.u_lon(i, j, k);
+    }
+    fill_halo(s.u_lon, true);
+    for (int k = 1; k <= nlev; ++k) {
+      const double kv = kf * std::max(0.0, (g.full_lev[k - 1] - sig_b) / (1.0 - sig_b));
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i) s.v_lat(i, j, k) = s.v_lat(i, j, k) - dt * kv * s.v_lat(i, j, k);
+    }
+    fill_halo(s.v_lat, false);
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nlat; ++j) {
+        const double c = g.full_cos_lat[j], sn = g.full_sin_lat[j];
+        const double c2 = c * c, c4 = c2 * c2;   // cos**2, cos**4
+        const double kt = ka + (ks - ka) * std::max(0.0, (g.full_lev[k - 1] - sig_b) / (1.0 - sig_b)) * c4;
+        for (int i = 1; i <= nlon; ++i) {
+          const double p_p0 = s.ph(i, j, k) / p0;
+          const double teq = std::max(200.0, (315.0 - dt_lat * (sn * sn) - dpt_lev * std::log(p_p0) * c2) *
+                                                 std::pow(p_p0, Rd_o_cpd));
+          s.pt(i, j, k) = s.pt(i, j, k) - dt * kt * s.pt(i, j, k) * (1.0 - teq / s.t(i, j, k));
+        }
+      }
+    fill_halo(s.pt, true);
+  }
+
   void time_integrate() {
     const double dt = cfg.dt_dyn;
     const int o = old_i, n = new_i, t3 = 3 - o - n;
@@ -1633,6 +1667,7 @@ struct Model {
         step_fb(o, t3, n, o, n, dt);
         break;
     }
+    if (cfg.forcing == GMC_FORCING_HELD_SUAREZ) held_suarez_forcing(state[n], dt);   // test_forcing_run (gmcore_mod.F90:586)
     if (cfg.use_div_damp) div_damp_run(state[n]);   // damp_run (damp_mod.F90:49-63)
     adv_run(state[n]);
     // time_advance (time_mod.F90:128-159)
