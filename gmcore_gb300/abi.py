@@ -57,6 +57,7 @@ class Config(C.Structure):
         ("radius", C.c_double), ("omega", C.c_double), ("g", C.c_double), ("Rd", C.c_double),
         ("cpd", C.c_double), ("p0", C.c_double),
         ("tvd_limiter_type", C.c_int32), ("div_damp_coef4", C.c_double), ("forcing", C.c_int32),
+        ("use_smag_damp", C.c_int32), ("smag_damp_coef", C.c_double),
     ]
 
     def as_dict(self):
@@ -115,6 +116,7 @@ def default_config(**overrides):
     c.radius, c.omega, c.g, c.Rd, c.cpd, c.p0 = 6.37122e6, 2 * pi / 86400.0, 9.80616, 287.04, 1004.0, 1.0e5
     c.tvd_limiter_type, c.div_damp_coef4 = TVD_VAN_LEER, 0.01
     c.forcing = FORCING_NONE
+    c.use_smag_damp, c.smag_damp_coef = 0, 0.1
     for k, v in overrides.items():
         if not hasattr(c, k):
             raise KeyError(k)

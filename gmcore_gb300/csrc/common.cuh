@@ -78,6 +78,7 @@ struct DGrid {
   int f_layer_mass;                                                // 1: the form's layer mass is dmA + dmB psr (FP32)
   int tangent_inline;   // 1: the FP32 edge PV and pole PV form the tangential winds themselves (no u_lat/v_lon fields)
   int forcing;                  // GMC_FORCING_*
+  double smag_coef;             // smag_damp_coef
   const double *full_lev;       // eta at full levels [k-1]
   const float *ph_lev_a;        // FP32 hyai(k) (p0 - ptop) + ptop [k-1]: ph_lev = a + hybi psr
   const float *half_lev_f, *half_dlev_f, *full_dlev_f;             // FP32 copies of the eta tables

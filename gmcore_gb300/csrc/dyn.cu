@@ -1894,7 +1894,119 @@ __global__ void k_held_suarez(DGrid g, Slot<R> n, double dt) {
   }
 }
 
+// Smagorinsky damping (smag_damp_run, smag_damp_mod.F90:52-190, with
+// decay_from_top = 1 as smag_damp_init leaves it, :36): horizontal tension at
+// cells (full rows 2 .. nlat-1; the pole rows hold the zero the reference's
+// working array was allocated with) and shear at vertices.  Blocks 0 .. nlat-1
+// take the full rows, the rest the half rows.
+template <class R, bool MB>
+__global__ void k_smag_ts(DGrid g, Slot<R> n, R *st, R *ss) {
+  if constexpr (MB) { to_member(g, n); const size_t mo = member_offset(g); st = mshift(st, mo); ss = mshift(ss, mo); }
+  const int k = blockIdx.y + 1, nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const R *u = n.u_lon, *v = n.v_lat;
+  if ((int)blockIdx.x < nlat) {
+    const int j = blockIdx.x + 1;
+    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
+    if (j == 1 || j == nlat) {
+      for (int i = threadIdx.x; i < nlon; i += blockDim.x) st[c0 + i] = (R)0;
+      return;
+    }
+    const unsigned hn = (unsigned)ix3(nhalf, nlon, 1, j, k), hs = hn - nlon;
+    const R dx = ROWR(R, de_lon, j), ly = ROWR(R, le_lon, j), fc = ROWR(R, full_cos_lat, j);
+    const R hcn = ROWR(R, half_cos_lat, j), hcs = ROWR(R, half_cos_lat, j - 1);
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const int iw = i == 0 ? nlon - 1 : i - 1;
+      st[c0 + i] = (u[c0 + i] - u[c0 + iw]) / dx - (v[hn + i] * hcn - v[hs + i] * hcs) / ly / fc;
+    }
+    return;
+  }
+  const int j = blockIdx.x - nlat + 1;
+  const unsigned h0 = (unsigned)ix3(nhalf, nlon, 1, j, k), fs = (unsigned)ix3(nlat, nlon, 1, j, k), fn = fs + nlon;
+  const R lx = ROWR(R, le_lat, j), dy = ROWR(R, de_lat, j), hc = ROWR(R, half_cos_lat, j);
+  const R fcs = ROWR(R, full_cos_lat, j), fcn = ROWR(R, full_cos_lat, j + 1);
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    const int ie = i + 1 == nlon ? 0 : i + 1;
+    ss[h0 + i] = (v[h0 + ie] - v[h0 + i]) / lx + (u[fn + i] * fcn - u[fs + i] * fcs) / dy / hc;
+  }
+}
+
+// The damping tendencies with the eddy viscosities at the u and v points
+// formed from the tension and shear around them (kmh_lon, kmh_lat).
+template <class R, bool MB>
+__global__ void k_smag_tend(DGrid g, Slot<R> n, const R *st, const R *ss, R *du, R *dv) {
+  if constexpr (MB) {
+    to_member(g, n);
+    const size_t mo = member_offset(g);
+    st = mshift(st, mo); ss = mshift(ss, mo); du = mshift(du, mo); dv = mshift(dv, mo);
+  }
+  const int k = blockIdx.y + 1, nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  const R *u = n.u_lon, *v = n.v_lat;
+  const R coef = (R)g.smag_coef;
+  auto sq = [](R x) { return x * x; };
+  if ((int)blockIdx.x < nlat) {
+    const int j = blockIdx.x + 1;
+    if (j == 1 || j == nlat) return;
+    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k), hn = (unsigned)ix3(nhalf, nlon, 1, j, k), hs = hn - nlon;
+    const R dx = ROWR(R, de_lon, j), ly = ROWR(R, le_lon, j), fc = ROWR(R, full_cos_lat, j);
+    const R dyn = ROWR(R, de_lat, j), dys = ROWR(R, de_lat, j - 1), hcn = ROWR(R, half_cos_lat, j),
+            hcs = ROWR(R, half_cos_lat, j - 1);
+    const R ls2 = coef / ((R)1 / sq(dx) + (R)1 / sq(ly));
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+      const int iw = i == 0 ? nlon - 1 : i - 1, ie = i + 1 == nlon ? 0 : i + 1;
+      const R kmh = ls2 * sqrt((R)0.5 * (sq(st[c0 + i]) + sq(st[c0 + ie])) + (R)0.5 * (sq(ss[hn + i]) + sq(ss[hs + i])));
+      const R uc = u[c0 + i];
+      du[c0 + i] = kmh * ((u[c0 + iw] - (R)2 * uc + u[c0 + ie]) / sq(dx) +
+                          ((u[c0 + nlon + i] - uc) / dyn * hcn - (uc - u[c0 - nlon + i]) / dys * hcs) / ly / fc);
+    }
+    return;
+  }
+  const int j = blockIdx.x - nlat + 1;
+  const unsigned h0 = (unsigned)ix3(nhalf, nlon, 1, j, k), fs = (unsigned)ix3(nlat, nlon, 1, j, k);
+  const R lx = ROWR(R, le_lat, j), dy = ROWR(R, de_lat, j), hc = ROWR(R, half_cos_lat, j);
+  const R ls2 = coef / ((R)1 / sq(lx) + (R)1 / sq(dy));
+  const bool edge = j == 1 || j == nhalf;
+  const R lyn = ROWR(R, le_lon, j + 1), lys = ROWR(R, le_lon, j), fcn = ROWR(R, full_cos_lat, j + 1),
+          fcs = ROWR(R, full_cos_lat, j);
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    const int iw = i == 0 ? nlon - 1 : i - 1, ie = i + 1 == nlon ? 0 : i + 1;
+    const R kmh = ls2 * sqrt((R)0.5 * (sq(st[fs + i]) + sq(st[fs + nlon + i])) + (R)0.5 * (sq(ss[h0 + i]) + sq(ss[h0 + iw])));
+    const R vc = v[h0 + i];
+    R t = (v[h0 + iw] - (R)2 * vc + v[h0 + ie]) / sq(lx);
+    if (!edge) t = t + ((v[h0 + nlon + i] - vc) / lyn * fcn - (vc - v[h0 - nlon + i]) / lys * fcs) / dy / hc;
+    dv[h0 + i] = kmh * t;
+  }
+}
+
+// u += dt dudt (rows 2 .. nlat-1), v += dt dvdt
+template <class R, bool MB>
+__global__ void k_smag_update(DGrid g, Slot<R> n, const R *du, const R *dv, R dt) {
+  if constexpr (MB) { to_member(g, n); const size_t mo = member_offset(g); du = mshift(du, mo); dv = mshift(dv, mo); }
+  const int k = blockIdx.y + 1, nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon;
+  if ((int)blockIdx.x < nlat) {
+    const int j = blockIdx.x + 1;
+    if (j == 1 || j == nlat) return;
+    const unsigned c0 = (unsigned)ix3(nlat, nlon, 1, j, k);
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.u_lon[c0 + i] = n.u_lon[c0 + i] + dt * du[c0 + i];
+    return;
+  }
+  const int j = blockIdx.x - nlat + 1;
+  const unsigned h0 = (unsigned)ix3(nhalf, nlon, 1, j, k);
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) n.v_lat[h0 + i] = n.v_lat[h0 + i] + dt * dv[h0 + i];
+}
+
 }  // namespace
+
+template <class R>
+void launch_smag_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *st, R *ss, R *du, R *dv, double dt) {
+  const dim3 grid(g.nlat + g.nhalf, g.nlev, L.members);
+  mb_launch(L, [&](auto mb) { k_smag_ts<R, decltype(mb)::value><<<grid, L.threads, 0, L.stream>>>(g, n, st, ss); });
+  mb_launch(L, [&](auto mb) { k_smag_tend<R, decltype(mb)::value><<<grid, L.threads, 0, L.stream>>>(g, n, st, ss, du, dv); });
+  mb_launch(L, [&](auto mb) { k_smag_update<R, decltype(mb)::value><<<grid, L.threads, 0, L.stream>>>(g, n, du, dv, (R)dt); });
+}
+template void launch_smag_damp<double>(const DGrid &, const Launch &, const Slot<double> &, double *, double *, double *,
+                                       double *, double);
+template void launch_smag_damp<float>(const DGrid &, const Launch &, const Slot<float> &, float *, float *, float *,
+                                      float *, double);
 
 template <class R>
 void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, R *div2) {

@@ -724,6 +724,7 @@ struct Engine : EngineBase {
     dg.ps_ref = ps_ref;
     dg.f_layer_mass = kFP32 ? 1 : 0;
     dg.forcing = grid.cfg.forcing;
+    dg.smag_coef = grid.cfg.smag_damp_coef;
     // the FP32 edge PV's default path (upwind order 3, pairs aligned beyond the
     // poles) forms the tangential winds itself: each has one reader there
     dg.tangent_inline = kFP32 && grid.cfg.baroclinic && grid.cfg.pv_scheme == GMC_PV_UPWIND &&
@@ -1882,6 +1883,10 @@ struct Engine : EngineBase {
         if (grid.cfg.use_div_damp)
           K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2,
             [&] { launch_div_damp<R>(dg, L, slots[m0 * 3 + n], work[m0].ke, work[m0].du); });
+        if (grid.cfg.use_smag_damp)   // damp_run (damp_mod.F90:59-61)
+          K("smag_damp", 3, [&] {
+            launch_smag_damp<R>(dg, L, slots[m0 * 3 + n], work[m0].ke, work[m0].u_lat, work[m0].du, work[m0].dv, dt);
+          });
       }
     } catch (...) {
       L.members = 1;
@@ -1940,6 +1945,8 @@ struct Engine : EngineBase {
         K("held_suarez", 1, [&] { launch_held_suarez<R>(dg, L, N, dt); });
       if (grid.cfg.use_div_damp)
         K("div_damp", grid.cfg.div_damp_order == 4 ? 3 : 2, [&] { launch_div_damp<R>(dg, L, N, work[m].ke, work[m].du); });
+      if (grid.cfg.use_smag_damp)   // damp_run (damp_mod.F90:59-61)
+        K("smag_damp", 3, [&] { launch_smag_damp<R>(dg, L, N, work[m].ke, work[m].u_lat, work[m].du, work[m].dv, dt); });
       io_dyn_done(L.stream);   // the new state's fields are final (gmc_step_io)
       if (ntr > 0) {
         uv_step = su; mf_step = sm; we_step = sw;   // every member runs the same cadence
@@ -2267,6 +2274,8 @@ void gmc_config_default(gmc_config *c) {
   c->tvd_limiter_type = GMC_TVD_VAN_LEER;
   c->div_damp_coef4 = 0.01;
   c->forcing = GMC_FORCING_NONE;
+  c->use_smag_damp = 0;
+  c->smag_damp_coef = 0.1;
 }
 
 int gmc_create(const gmc_config *cfg, gmc_ctx **out) {

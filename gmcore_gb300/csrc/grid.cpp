@@ -248,6 +248,7 @@ std::string validate_config(const gmc_config &c) {
   if (c.lon_halo_width < 1) return "lon_halo_width must be >= 1";
   if (c.forcing != GMC_FORCING_NONE && c.forcing != GMC_FORCING_HELD_SUAREZ) return "bad forcing";
   if (c.forcing == GMC_FORCING_HELD_SUAREZ && !c.baroclinic) return "held_suarez forcing needs the baroclinic model";
+  if (c.use_smag_damp && !(c.smag_damp_coef >= 0)) return "smag_damp_coef must be >= 0";
   // device kernels index one field with 32-bit arithmetic
   if ((double)(c.nlev + 1) * c.nlat * c.nlon >= 2147483647.0) return "grid too large: (nlev+1)*nlat*nlon must be < 2^31";
   return "";

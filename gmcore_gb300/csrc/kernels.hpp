@@ -134,6 +134,8 @@ template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const S
 // div and div2 are scratch cell fields.
 template <class R> void launch_div_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *div, R *div2);
 template <class R> void launch_held_suarez(const DGrid &g, const Launch &L, const Slot<R> &n, double dt);
+template <class R> void launch_smag_damp(const DGrid &g, const Launch &L, const Slot<R> &n, R *st, R *ss, R *du, R *dv,
+                                         double dt);
 
 // ---- advection (adv.cu) ---------------------------------------------------
 // Horizontal FFSL flux of q (ffsl_calc_tracer_hflx_cell): inner advective

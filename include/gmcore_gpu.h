@@ -120,6 +120,8 @@ typedef struct gmc_config {
   double  div_damp_coef4;          /* namelist div_damp_coef4 (order 4)          */
   int32_t forcing;                 /* GMC_FORCING_*: test forcing applied after the
                                       integrator, before damping (gmcore_mod.F90:586) */
+  int32_t use_smag_damp;           /* namelist use_smag_damp (damp_mod.F90:59-61) */
+  double  smag_damp_coef;          /* namelist smag_damp_coef                    */
 } gmc_config;
 
 /* Diagnostics of gmcore_mod.F90:213-341 (FP64, compensated sums). */

@@ -68,6 +68,8 @@ module gmcore_gpu_mod
     integer(c_int32_t) :: tvd_limiter_type
     real(c_double)     :: div_damp_coef4
     integer(c_int32_t) :: forcing
+    integer(c_int32_t) :: use_smag_damp
+    real(c_double)     :: smag_damp_coef
   end type gmc_config
 
   type, bind(c) :: gmc_diag

@@ -114,6 +114,7 @@ struct State {
   Arr u_lon, v_lon, u_f, u_lat, v_lat, v_f, we_lev, we_lev_lon, we_lev_lat, gz, gz_lev, m, m_vtx, m_lon,
       m_lat, m_lev, mfx_lon, mfy_lon, mfy_lat, mfx_lat, pv, pv_lon, pv_lat, ke, pt, ptf_lon, ptf_lat,
       ptf_lev, t, ph, ph_lev, ph_exn_lev, phs, phs_f, vor, gz_f, div, div2;
+  Arr smag_t, smag_s, kmh_lon, kmh_lat, smag_dudt, smag_dvdt;   // smag_damp_run working arrays
 };
 
 struct Tend {
@@ -252,6 +253,10 @@ struct Model {
     F.lon3(s.ptf_lon); F.lat3(s.ptf_lat); F.lev3(s.ptf_lev); F.cell3(s.t); F.cell3(s.ph);
     F.lev3(s.ph_lev); F.lev3(s.ph_exn_lev); F.cell2(s.phs); F.cell2(s.phs_f); F.vtx3(s.vor); F.cell3(s.div);
     F.cell3(s.div2);   // zero at allocation, pole rows never written (allocator_mod.F90:198)
+    if (cfg.use_smag_damp) {   // state_mod.F90:185-191, zero at allocation
+      F.cell3(s.smag_t); F.vtx3(s.smag_s); F.lon3(s.kmh_lon); F.lat3(s.kmh_lat);
+      F.lon3(s.smag_dudt); F.lat3(s.smag_dvdt);
+    }
     if (!baroclinic) F.cell3(s.gz_f);
   }
   void alloc_tend(Tend &t) {
@@ -1615,6 +1620,71 @@ struct Model {
     for (int q = 0; q < 8; ++q) out[q] = v[q] / a;
   }
 
+  // smag_damp_run (smag_damp_mod.F90:52-190); decay_from_top = 1 (:36)
+  void smag_damp_run(State &s, double dt) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
+    const gmc::Grid &g = G();
+    Arr &u = s.u_lon, &v = s.v_lat, &st = s.smag_t, &ss = s.smag_s, &kl = s.kmh_lon, &kt = s.kmh_lat;
+    Arr &du = s.smag_dudt, &dv = s.smag_dvdt;
+    const double coef = cfg.smag_damp_coef, decay = 1.0;
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i)
+          st(i, j, k) = (u(i, j, k) - u(i - 1, j, k)) / g.de_lon[j] -
+                        (v(i, j, k) * g.half_cos_lat[j] - v(i, j - 1, k) * g.half_cos_lat[j - 1]) / g.le_lon[j] /
+                            g.full_cos_lat[j];
+    fill_halo(st, true, false, true, false, true);
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i)
+          ss(i, j, k) = (v(i + 1, j, k) - v(i, j, k)) / g.le_lat[j] +
+                        (u(i, j + 1, k) * g.full_cos_lat[j + 1] - u(i, j, k) * g.full_cos_lat[j]) / g.de_lat[j] /
+                            g.half_cos_lat[j];
+    fill_halo(ss, false, true, false, true, false);
+    auto sq = [](double x) { return x * x; };
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 2; j <= nlat - 1; ++j) {
+        const double ls2 = coef / (1 / sq(g.de_lon[j]) + 1 / sq(g.le_lon[j])) * decay;
+        for (int i = 1; i <= nlon; ++i)
+          kl(i, j, k) = ls2 * std::sqrt(0.5 * (sq(st(i, j, k)) + sq(st(i + 1, j, k))) +
+                                        0.5 * (sq(ss(i, j, k)) + sq(ss(i, j - 1, k))));
+      }
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nhalf; ++j) {
+        const double ls2 = coef / (1 / sq(g.le_lat[j]) + 1 / sq(g.de_lat[j])) * decay;
+        for (int i = 1; i <= nlon; ++i)
+          kt(i, j, k) = ls2 * std::sqrt(0.5 * (sq(st(i, j, k)) + sq(st(i, j + 1, k))) +
+                                        0.5 * (sq(ss(i, j, k)) + sq(ss(i - 1, j, k))));
+      }
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i)
+          du(i, j, k) = kl(i, j, k) * ((u(i - 1, j, k) - 2 * u(i, j, k) + u(i + 1, j, k)) / sq(g.de_lon[j]) +
+                                       ((u(i, j + 1, k) - u(i, j, k)) / g.de_lat[j] * g.half_cos_lat[j] -
+                                        (u(i, j, k) - u(i, j - 1, k)) / g.de_lat[j - 1] * g.half_cos_lat[j - 1]) /
+                                           g.le_lon[j] / g.full_cos_lat[j]);
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 1; i <= nlon; ++i) u(i, j, k) = u(i, j, k) + dt * du(i, j, k);
+    fill_halo(u, true);
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nhalf; ++j) {
+        const bool edge = j == 1 || j == nhalf;
+        for (int i = 1; i <= nlon; ++i) {
+          double t = (v(i - 1, j, k) - 2 * v(i, j, k) + v(i + 1, j, k)) / sq(g.le_lat[j]);
+          if (!edge)
+            t = t + ((v(i, j + 1, k) - v(i, j, k)) / g.le_lon[j + 1] * g.full_cos_lat[j + 1] -
+                     (v(i, j, k) - v(i, j - 1, k)) / g.le_lon[j] * g.full_cos_lat[j]) /
+                        g.de_lat[j] / g.half_cos_lat[j];
+          dv(i, j, k) = kt(i, j, k) * t;
+        }
+      }
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i) v(i, j, k) = v(i, j, k) + dt * dv(i, j, k);
+    fill_halo(v, false);
+  }
+
   // held_suarez_test_apply_forcing (held_suarez_test_mod.F90:74-112) on the
   // new state, whose ph and t the last stage's backward pass left
   void held_suarez_forcing(State &s, double dt) {
@@ -1669,6 +1739,7 @@ struct Model {
     }
     if (cfg.forcing == GMC_FORCING_HELD_SUAREZ) held_suarez_forcing(state[n], dt);   // test_forcing_run (gmcore_mod.F90:586)
     if (cfg.use_div_damp) div_damp_run(state[n]);   // damp_run (damp_mod.F90:49-63)
+    if (cfg.use_smag_damp) smag_damp_run(state[n], dt);
     adv_run(state[n]);
     // time_advance (time_mod.F90:128-159)
     if (alert_ringing) { alert_last_time = curr_time; alert_ringing = false; }
