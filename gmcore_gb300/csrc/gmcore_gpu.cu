@@ -966,6 +966,14 @@ struct Engine : EngineBase {
   }
 
   void step_io(int m, const std::vector<IoItem> &in, int nsteps, const std::vector<IoItem> &out) override {
+    // every field name is known before anything moves
+    for (const std::vector<IoItem> *v : {&in, &out})
+      for (const IoItem &x : *v)
+        if (x.tracer < 0) {
+          R *pr;
+          double *pd;
+          locate(slots[m * 3 + old_i], m, x.name, &pr, &pd);
+        }
     const bool overlap = nm == 1 && ntr > 0 && nsteps > 0;
     const int nlon = grid.nlon;
     // an overlapped item: registered host rows, the device field (R or FP64)

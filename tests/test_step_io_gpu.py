@@ -88,4 +88,8 @@ def test_exchange_rejects_a_bad_item_before_moving_anything():
     assert np.array_equal(m.get_field("pt"), before)
     with pytest.raises(GmcError):
         m.step_io([], 1, [("nonsense", np.zeros((cfg.nlat, cfg.nlon)))])
+    # an unknown output name stops the call before its inputs are set
+    with pytest.raises(GmcError):
+        m.step_io([("pt", before * 2.0)], 1, [("nonsense", np.zeros((cfg.nlev, cfg.nlat, cfg.nlon)))])
+    assert np.array_equal(m.get_field("pt"), before)
     m.close()
