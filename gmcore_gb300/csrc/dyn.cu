@@ -729,7 +729,7 @@ __global__ void k_column_mass(DGrid g, Slot<R> s, Work<R> w, R dt) {
 // prefix sums along the column (warp scans), we_lev, dphs and the vertical
 // Courant numbers, each phase parallel over (column, level).
 template <bool MB>
-__global__ void GMC_BOUNDS_F(6) k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, float dt) {
+__global__ void GMC_BOUNDS_FMB(8, 6, MB) k_column_mass_f(DGrid g, Slot<float> s, Work<float> w, float dt) {
   if constexpr (MB) { to_member(g, s); to_member(g, w); }   // member-batched launches
   extern __shared__ double shd[];
   const int nlat = g.nlat, nhalf = g.nhalf, nlon = g.nlon, nlev = g.nlev;
