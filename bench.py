@@ -475,6 +475,7 @@ def run_ours(args):
 
     adj = adjoint_cost() if RANK == 0 else None
     ens = ensemble_throughput() if RANK == 0 else None
+    files = file_io(cfg, st) if RANK == 0 and not args.quick else None
 
     c5 = c5_leg(args) if RANK == 0 and not args.quick else None
 
@@ -543,10 +544,50 @@ def run_ours(args):
             line["cpu_baseline"] = cpu
         if one_day is not None:
             line["one_day"] = one_day
+        if files is not None:
+            line["files"] = files
         if c5 is not None:
             line["c5"] = c5
         print(json.dumps(line), flush=True)
     ranks.close()
+
+
+def file_io(cfg, st, reps=3):
+    """History and restart files of the workload's state (0.5 deg L32, 4
+    tracers, mixed form): wall time of gmc_restart_write, gmc_restart_read
+    and gmc_history_write (best of `reps`; each moves the state over the host
+    link, converts it to FP64 big-endian and writes or reads the netCDF file
+    in the host's temporary directory), and the file sizes."""
+    import shutil
+    import tempfile
+    import gmcore_gb300 as g
+    m = g.Model(cfg)
+    m.set_state(st)
+    m.prepare()
+    m.step(3)
+    d = tempfile.mkdtemp(prefix="gmc_files_")
+    r0, h0 = os.path.join(d, "c2.r0.nc"), os.path.join(d, "c2.h0.nc")
+
+    def best(f):
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    try:
+        tw = best(lambda: m.restart_write(r0, 540.0))
+        th = best(lambda: m.history_write(h0, 540.0))
+        tr = best(lambda: m.restart_read(r0))
+        rb, hb = os.path.getsize(r0), os.path.getsize(h0)
+    finally:
+        m.close()
+        shutil.rmtree(d, ignore_errors=True)
+    return {"restart_bytes": rb, "restart_write_s": tw, "restart_write_gbs": rb / tw / 1e9,
+            "restart_read_s": tr, "restart_read_gbs": rb / tr / 1e9,
+            "history_bytes": hb, "history_write_s": th, "history_write_gbs": hb / th / 1e9,
+            "where": "netCDF classic (CDF-2) files in the host's temporary directory, best of %d" % reps}
 
 
 def adjoint_cost():

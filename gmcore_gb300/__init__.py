@@ -15,7 +15,8 @@ import os
 
 import numpy as np
 
-from .abi import (Config, Diag, View, Io, Stats, FfslFields, default_config, STATUS_NAMES, GMC_OK,  # noqa: F401
+from .abi import (Config, Diag, View, Io, Stats, FfslFields, FileOpts, RestartArrays,  # noqa: F401
+                  default_config, STATUS_NAMES, GMC_OK,
                   TIME_EULER, TIME_PC2, TIME_WRFRK3, PV_MIDPOINT, PV_UPWIND, PV_TVD, TVD_NONE, TVD_VAN_LEER,
                   TVD_MC, FLUX_PPM, FLUX_VAN_LEER, LIMITER_NONE,
                   LIMITER_MONO, LIMITER_PD, VCOORD_NONE, VCOORD_TEST_L26, VCOORD_WRF_L32,
@@ -31,6 +32,7 @@ EXPORTED = (
     "gmc_get_stats", "gmc_set_profiling", "gmc_kernel_profile", "gmc_ffsl_hflx", "gmc_ffsl_hflx_noalloc",
     "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs", "gmc_host_register", "gmc_host_unregister",
     "gmc_fp64_fma_peak", "gmc_fp32_fma_peak", "gmc_set_member_layout", "gmc_step_io",
+    "gmc_restart_write", "gmc_restart_read", "gmc_history_write", "gmc_restart_write_host", "gmc_restart_read_host",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -89,6 +91,13 @@ def load(build_if_missing=True):
     lib.gmc_fp64_fma_peak.argtypes = [P(C.c_double)]
     lib.gmc_fp32_fma_peak.argtypes = [P(C.c_double)]
     lib.gmc_set_member_layout.argtypes = [C.c_void_p, C.c_int32]
+    lib.gmc_restart_write.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_double, P(FileOpts)]
+    lib.gmc_restart_read.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, P(FileOpts), P(C.c_double)]
+    lib.gmc_history_write.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_double, C.c_int32, P(FileOpts)]
+    lib.gmc_restart_write_host.argtypes = [P(Config), C.c_char_p, C.c_double, P(FileOpts), P(RestartArrays),
+                                           C.c_char_p, C.c_int32]
+    lib.gmc_restart_read_host.argtypes = [P(Config), C.c_char_p, P(FileOpts), P(C.c_double), P(RestartArrays),
+                                          C.c_char_p, C.c_int32]
     _lib = lib
     return lib
 
@@ -215,6 +224,62 @@ def make_ic(cfg, kind, seed, noise_k=1.0):
     if rc:
         raise GmcError(rc, "make_ic")
     return out
+
+
+def file_opts(time_units=None, start_time=None, tracer_names=None, restart_interval=None):
+    """gmc_file_opts from keywords (None: the library's default)."""
+    enc = lambda x: x.encode() if isinstance(x, str) else x
+    if isinstance(tracer_names, (list, tuple)):
+        tracer_names = ",".join(tracer_names)
+    return FileOpts(enc(time_units), enc(start_time), enc(tracer_names), enc(restart_interval))
+
+
+def _restart_arrays(cfg, state):
+    """RestartArrays over the C-ordered float64 arrays of a state dict."""
+    a = RestartArrays()
+    for key, name in (("u_lon", "u_lon"), ("v_lat", "v_lat"), ("pt", "pt"), ("phs", "phs"), ("gz", "gz"),
+                      ("gzs", "gzs"), ("q", "q")):
+        x = state.get(key)
+        if x is not None:
+            if x.dtype != np.float64 or not x.flags.c_contiguous:
+                raise ValueError(f"{key} must be a C-contiguous float64 array")
+            setattr(a, name, x.ctypes.data_as(C.POINTER(C.c_double)))
+    return a
+
+
+def restart_write_host(cfg, path, elapsed_seconds, state, **opts):
+    """Restart file of a host state (dict of dense float64 arrays as make_ic
+    returns them), without a GPU."""
+    lib = load()
+    err = C.create_string_buffer(512)
+    o = file_opts(**opts)
+    rc = lib.gmc_restart_write_host(C.byref(cfg), os.fsencode(path), elapsed_seconds, C.byref(o),
+                                    C.byref(_restart_arrays(cfg, state)), err, len(err))
+    if rc:
+        raise GmcError(rc, err.value.decode())
+
+
+def restart_read_host(cfg, path, **opts):
+    """(elapsed seconds, state dict) of a restart file, without a GPU."""
+    lib = load()
+    nlon, nlat, nlev = cfg.nlon, cfg.nlat, cfg.nlev
+    st = {"u_lon": np.zeros((nlev, nlat, nlon)), "v_lat": np.zeros((nlev, nlat - 1, nlon)),
+          "gzs": np.zeros((nlat, nlon))}
+    if cfg.baroclinic:
+        st["pt"] = np.zeros((nlev, nlat, nlon))
+        st["phs"] = np.zeros((nlat, nlon))
+    else:
+        st["gz"] = np.zeros((nlat, nlon))
+    if cfg.ntracer > 0:
+        st["q"] = np.full((cfg.ntracer, nlev, nlat, nlon), np.nan)
+    err = C.create_string_buffer(512)
+    t = C.c_double()
+    o = file_opts(**opts)
+    rc = lib.gmc_restart_read_host(C.byref(cfg), os.fsencode(path), C.byref(o), C.byref(t),
+                                   C.byref(_restart_arrays(cfg, st)), err, len(err))
+    if rc:
+        raise GmcError(rc, err.value.decode())
+    return t.value, st
 
 
 class Model:
@@ -354,6 +419,25 @@ class Model:
 
     def step(self, n=1):
         self._check(self.lib.gmc_step(self.h, n))
+
+    def restart_write(self, path, elapsed_seconds, member=0, **opts):
+        """Restart file of the state (gmc_restart_write)."""
+        o = file_opts(**opts)
+        self._check(self.lib.gmc_restart_write(self.h, member, os.fsencode(path), elapsed_seconds, C.byref(o)))
+
+    def restart_read(self, path, member=0, **opts):
+        """Sets the state from a restart file; returns its elapsed seconds
+        (gmc_restart_read; prepare() follows)."""
+        o = file_opts(**opts)
+        t = C.c_double()
+        self._check(self.lib.gmc_restart_read(self.h, member, os.fsencode(path), C.byref(o), C.byref(t)))
+        return t.value
+
+    def history_write(self, path, elapsed_seconds, append=False, member=0, **opts):
+        """One history record of the state (gmc_history_write)."""
+        o = file_opts(**opts)
+        self._check(self.lib.gmc_history_write(self.h, member, os.fsencode(path), elapsed_seconds, int(append),
+                                               C.byref(o)))
 
     def diagnose(self, member=0):
         d = Diag()

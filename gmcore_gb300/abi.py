@@ -15,12 +15,13 @@ GMC_ENAN = -5
 GMC_ECUDA = -7
 GMC_ENOMEM = -8
 GMC_ESTATE = -9
+GMC_EIO = -10
 
 STATUS_NAMES = {
     GMC_OK: "GMC_OK", GMC_EINVAL: "GMC_EINVAL", GMC_ECFL: "GMC_ECFL",
     GMC_ENONMONO: "GMC_ENONMONO", GMC_ENEGTRACER: "GMC_ENEGTRACER", GMC_ENAN: "GMC_ENAN",
     GMC_ECUDA: "GMC_ECUDA", GMC_ENOMEM: "GMC_ENOMEM",
-    GMC_ESTATE: "GMC_ESTATE",
+    GMC_ESTATE: "GMC_ESTATE", GMC_EIO: "GMC_EIO",
 }
 
 TIME_EULER, TIME_PC2, TIME_WRFRK3 = 0, 1, 2
@@ -87,6 +88,18 @@ class View(C.Structure):
 class Io(C.Structure):
     """gmc_io: a field (name) or, with name NULL, a tracer, and its view."""
     _fields_ = [("name", C.c_char_p), ("tracer", C.c_int32), ("view", View)]
+
+
+class FileOpts(C.Structure):
+    """gmc_file_opts: time axis, tracer names and restart attribute of the
+    history and restart files (NULL members take the defaults)."""
+    _fields_ = [("time_units", C.c_char_p), ("start_time", C.c_char_p), ("tracer_names", C.c_char_p),
+                ("restart_interval", C.c_char_p)]
+
+
+class RestartArrays(C.Structure):
+    """gmc_restart_arrays: dense FP64 host arrays of a restart."""
+    _fields_ = [(n, C.POINTER(C.c_double)) for n in ("u_lon", "v_lat", "pt", "phs", "gz", "gzs", "q")]
 
 
 def default_config(**overrides):

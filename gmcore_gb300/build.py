@@ -18,9 +18,9 @@ OUT_DIR = os.path.join(PKG, "lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libgmcore_gpu.so")
 
-CUDA_SOURCES = ["dyn.cu", "adv.cu", "tlad.cu", "gmcore_gpu.cu", "peak.cu"]
-CXX_SOURCES = ["grid.cpp"]
-HEADERS = ["common.cuh", "stencil.cuh", "kernels.hpp", "grid.hpp"]
+CUDA_SOURCES = ["dyn.cu", "adv.cu", "tlad.cu", "gmcore_gpu.cu", "peak.cu", "out.cu"]
+CXX_SOURCES = ["grid.cpp", "ncfile.cpp", "output.cpp"]
+HEADERS = ["common.cuh", "stencil.cuh", "kernels.hpp", "grid.hpp", "ncfile.hpp", "output.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -22,6 +22,7 @@
 #include "gmcore_gpu.h"
 #include "grid.hpp"
 #include "kernels.hpp"
+#include "output.hpp"
 
 using namespace gmc;
 
@@ -280,6 +281,11 @@ struct EngineBase {
     gmc_view view;
   };
   virtual void step_io(int member, const std::vector<IoItem> &in, int nsteps, const std::vector<IoItem> &out) = 0;
+  // FP64 history diagnostics of a member's state into dense host arrays:
+  // ph, t, z, div [nlev][nlat][nlon] and vor [nlev][nlat-1][nlon] (shallow
+  // water: z and div [nlat][nlon], ph, t and vor unused and may be null)
+  virtual void output_diag(int member, double *ph, double *t, double *z, double *div, double *vor) = 0;
+  virtual const Grid &host_grid() const = 0;
   virtual void set_graphs(bool on) = 0;
   virtual int layout_in_use() const = 0;
   virtual bool set_layout(int lay) = 0;
@@ -2084,6 +2090,31 @@ struct Engine : EngineBase {
     out->te = out->te_ke + out->te_ie + out->te_pe;
   }
 
+  void output_diag(int m, double *ph, double *t, double *z, double *div, double *vor) override {
+    const Slot<R> &s = slots[m * 3 + old_i];
+    const bool bc = grid.cfg.baroclinic != 0;
+    const size_t nf = full3(), nh = half3(), n2 = two_d();
+    const size_t ncell = bc ? nf : n2;   // cell fields of the layout
+    double *buf = nullptr;
+    CK(cudaMallocAsync((void **)&buf, (4 * ncell + nh) * sizeof(double), stream));
+    double *dph = buf, *dt = buf + ncell, *dz = buf + 2 * ncell, *ddiv = buf + 3 * ncell, *dvor = buf + 4 * ncell;
+    launch_output_diag<R>(dg, stream, s, dph, dt, dz, ddiv, dvor);
+    CK(cudaGetLastError());
+    auto back = [&](double *host, const double *dev, size_t n) {
+      if (host) CK(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    };
+    if (bc) {
+      back(ph, dph, nf);
+      back(t, dt, nf);
+      back(vor, dvor, nh);
+    }
+    back(z, dz, ncell);
+    back(div, ddiv, ncell);
+    CK(cudaFreeAsync(buf, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  const Grid &host_grid() const override { return grid; }
+
   // The first error raised on the device since the last read (the error
   // words are cleared): err[1] holds the first bit, err[0] all of them.
   unsigned read_error() override {
@@ -2252,6 +2283,74 @@ int noalloc_scratch_address(int dev, void **out, std::string &err) {
   }
   *out = g_noalloc_addr[dev];
   return GMC_OK;
+}
+
+// A dense host array [nk][nrow][nlon] as a view.
+gmc_view dense_view(double *p, int nlon, int nrow, int nk) {
+  gmc_view v;
+  v.data = p;
+  v.lb[0] = v.lb[1] = v.lb[2] = 1;
+  v.ub[0] = nlon;
+  v.ub[1] = nrow;
+  v.ub[2] = nk;
+  return v;
+}
+
+// Host copies of a member's restart variables (FP64, dense interior).
+struct HostState {
+  std::vector<double> u, v, pt, phs, gz, gzs, q;
+  HostState(const gmc_config &c) {
+    const size_t n3 = (size_t)c.nlev * c.nlat * c.nlon, h3 = (size_t)c.nlev * (c.nlat - 1) * c.nlon,
+                 n2 = (size_t)c.nlat * c.nlon;
+    u.resize(n3);
+    v.resize(h3);
+    gzs.resize(n2);
+    if (c.baroclinic) {
+      pt.resize(n3);
+      phs.resize(n2);
+    } else {
+      gz.resize(n2);
+    }
+    q.resize((size_t)c.ntracer * n3);
+  }
+  out::State view(const gmc_config &c) {
+    out::State s;
+    s.u = u.data();
+    s.v = v.data();
+    s.gzs = gzs.data();
+    if (c.baroclinic) {
+      s.pt = pt.data();
+      s.phs = phs.data();
+    } else {
+      s.gz = gz.data();
+    }
+    const size_t n3 = (size_t)c.nlev * c.nlat * c.nlon;
+    for (int l = 0; l < c.ntracer; ++l) s.q.push_back(q.data() + l * n3);
+    return s;
+  }
+};
+
+// The prognostic fields of a member into h.
+void gather_state(EngineBase &e, const gmc_config &c, int m, HostState &h) {
+  const int nlon = c.nlon, nlat = c.nlat, nlev = c.nlev;
+  e.get_field(m, "u_lon", dense_view(h.u.data(), nlon, nlat, nlev));
+  e.get_field(m, "v_lat", dense_view(h.v.data(), nlon, nlat - 1, nlev));
+  e.get_field(m, "gzs", dense_view(h.gzs.data(), nlon, nlat, 1));
+  if (c.baroclinic) {
+    e.get_field(m, "pt", dense_view(h.pt.data(), nlon, nlat, nlev));
+    e.get_field(m, "phs", dense_view(h.phs.data(), nlon, nlat, 1));
+  } else {
+    e.get_field(m, "gz", dense_view(h.gz.data(), nlon, nlat, 1));
+  }
+  const size_t n3 = (size_t)nlev * nlat * nlon;
+  for (int l = 0; l < c.ntracer; ++l) e.get_tracer(m, l, dense_view(h.q.data() + l * n3, nlon, nlat, nlev));
+}
+
+void copy_err(char *buf, int32_t len, const std::string &msg) {
+  if (!buf || len <= 0) return;
+  const size_t n = std::min(msg.size(), (size_t)len - 1);
+  std::memcpy(buf, msg.data(), n);
+  buf[n] = 0;
 }
 
 }  // namespace
@@ -2655,6 +2754,178 @@ int gmc_make_ic(const gmc_config *cfg, int32_t kind, uint64_t seed, double noise
     return e.empty() ? GMC_OK : GMC_EINVAL;
   } catch (...) {
     return GMC_EINVAL;
+  }
+}
+
+int gmc_restart_write(gmc_ctx *ctx, int32_t member, const char *path, double elapsed_seconds,
+                      const gmc_file_opts *opts) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!path) return fail(ctx, GMC_EINVAL, "null path");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  return guarded(ctx, [&]() {
+    const gmc_config &c = ctx->cfg;
+    out::Opts o;
+    std::string e = out::parse_opts(opts, c.ntracer, o);
+    if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    HostState h(c);
+    gather_state(*ctx->eng, c, member, h);
+    e = out::write_restart(ctx->eng->host_grid(), path, elapsed_seconds, o, h.view(c));
+    if (!e.empty()) throw ApiError{GMC_EIO, e};
+    return GMC_OK;
+  });
+}
+
+int gmc_restart_read(gmc_ctx *ctx, int32_t member, const char *path, const gmc_file_opts *opts,
+                     double *elapsed_seconds) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!path) return fail(ctx, GMC_EINVAL, "null path");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  return guarded(ctx, [&]() {
+    const gmc_config &c = ctx->cfg;
+    out::Opts o;
+    std::string e = out::parse_opts(opts, c.ntracer, o);
+    if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    HostState h(c);
+    out::State st = h.view(c);
+    std::vector<bool> found;
+    double t = 0;
+    e = out::read_restart(ctx->eng->host_grid(), path, o, t, st, found);
+    if (!e.empty()) throw ApiError{GMC_EIO, e};
+    // the whole file is read before the state changes
+    const int nlon = c.nlon, nlat = c.nlat, nlev = c.nlev;
+    EngineBase &eng = *ctx->eng;
+    eng.set_field(member, "u_lon", dense_view(h.u.data(), nlon, nlat, nlev));
+    eng.set_field(member, "v_lat", dense_view(h.v.data(), nlon, nlat - 1, nlev));
+    eng.set_field(member, "gzs", dense_view(h.gzs.data(), nlon, nlat, 1));
+    if (c.baroclinic) {
+      eng.set_field(member, "pt", dense_view(h.pt.data(), nlon, nlat, nlev));
+      eng.set_field(member, "phs", dense_view(h.phs.data(), nlon, nlat, 1));
+    } else {
+      eng.set_field(member, "gz", dense_view(h.gz.data(), nlon, nlat, 1));
+    }
+    const size_t n3 = (size_t)nlev * nlat * nlon;
+    for (int l = 0; l < c.ntracer; ++l)
+      if (found[(size_t)l]) eng.set_tracer(member, l, dense_view(h.q.data() + l * n3, nlon, nlat, nlev));
+    if (elapsed_seconds) *elapsed_seconds = t;
+    return GMC_OK;
+  });
+}
+
+int gmc_history_write(gmc_ctx *ctx, int32_t member, const char *path, double elapsed_seconds, int32_t append,
+                      const gmc_file_opts *opts) {
+  if (!ctx) return GMC_EINVAL;
+  if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
+  if (!path) return fail(ctx, GMC_EINVAL, "null path");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  return guarded(ctx, [&]() {
+    const gmc_config &c = ctx->cfg;
+    out::Opts o;
+    std::string e = out::parse_opts(opts, c.ntracer, o);
+    if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    EngineBase &eng = *ctx->eng;
+    HostState h(c);
+    gather_state(eng, c, member, h);
+    const size_t n3 = (size_t)c.nlev * c.nlat * c.nlon, h3 = (size_t)c.nlev * (c.nlat - 1) * c.nlon;
+    std::vector<double> ph, t, z(n3), div(n3), vor, pv;
+    if (c.baroclinic) {
+      ph.resize(n3);
+      t.resize(n3);
+      vor.resize(h3);
+    } else {
+      pv.resize(h3);
+      eng.get_field(member, "pv", dense_view(pv.data(), c.nlon, c.nlat - 1, 1));
+    }
+    eng.output_diag(member, ph.empty() ? nullptr : ph.data(), t.empty() ? nullptr : t.data(), z.data(), div.data(),
+                    vor.empty() ? nullptr : vor.data());
+    out::History hv;
+    const out::State st = h.view(c);
+    hv.u = st.u;
+    hv.v = st.v;
+    hv.pt = st.pt;
+    hv.phs = st.phs;
+    hv.gz = st.gz;
+    hv.gzs = st.gzs;
+    hv.ph = ph.empty() ? nullptr : ph.data();
+    hv.t = t.empty() ? nullptr : t.data();
+    hv.z = z.data();
+    hv.div = div.data();
+    hv.vor = vor.empty() ? nullptr : vor.data();
+    hv.pv = pv.empty() ? nullptr : pv.data();
+    for (double *q : st.q) hv.q.push_back(q);
+    eng.diagnose(member, &hv.diag);
+    e = out::write_history(eng.host_grid(), path, elapsed_seconds, append != 0, o, hv);
+    if (!e.empty()) throw ApiError{GMC_EIO, e};
+    return GMC_OK;
+  });
+}
+
+namespace {
+// Grid of a configuration for the host-array file calls.
+int host_grid_of(const gmc_config *cfg, Grid &g, char *errbuf, int32_t errlen) {
+  if (!cfg) { copy_err(errbuf, errlen, "null configuration"); return GMC_EINVAL; }
+  const gmc_config c = normalised(*cfg);
+  std::string e = validate_config(c);
+  if (e.empty()) e = g.build(c);
+  if (!e.empty()) { copy_err(errbuf, errlen, e); return GMC_EINVAL; }
+  return GMC_OK;
+}
+out::State host_state(const gmc_config &c, const gmc_restart_arrays *a) {
+  out::State s;
+  s.u = a->u_lon;
+  s.v = a->v_lat;
+  s.pt = a->pt;
+  s.phs = a->phs;
+  s.gz = a->gz;
+  s.gzs = a->gzs;
+  const size_t n3 = (size_t)c.nlev * c.nlat * c.nlon;
+  for (int l = 0; l < c.ntracer; ++l) s.q.push_back(a->q ? a->q + l * n3 : nullptr);
+  return s;
+}
+}  // namespace
+
+int gmc_restart_write_host(const gmc_config *cfg, const char *path, double elapsed_seconds, const gmc_file_opts *opts,
+                           const gmc_restart_arrays *a, char *errbuf, int32_t errlen) {
+  try {
+    Grid g;
+    int rc = host_grid_of(cfg, g, errbuf, errlen);
+    if (rc != GMC_OK) return rc;
+    if (!path || !a) { copy_err(errbuf, errlen, "null path or arrays"); return GMC_EINVAL; }
+    out::Opts o;
+    std::string e = out::parse_opts(opts, g.cfg.ntracer, o);
+    if (!e.empty()) { copy_err(errbuf, errlen, e); return GMC_EINVAL; }
+    out::State s = host_state(g.cfg, a);
+    if (g.cfg.ntracer > 0 && !a->q) { copy_err(errbuf, errlen, "null tracer array"); return GMC_EINVAL; }
+    e = out::write_restart(g, path, elapsed_seconds, o, s);
+    if (!e.empty()) { copy_err(errbuf, errlen, e); return GMC_EIO; }
+    return GMC_OK;
+  } catch (const std::bad_alloc &) {
+    copy_err(errbuf, errlen, "host allocation failed");
+    return GMC_ENOMEM;
+  }
+}
+
+int gmc_restart_read_host(const gmc_config *cfg, const char *path, const gmc_file_opts *opts,
+                          double *elapsed_seconds, const gmc_restart_arrays *a, char *errbuf, int32_t errlen) {
+  try {
+    Grid g;
+    int rc = host_grid_of(cfg, g, errbuf, errlen);
+    if (rc != GMC_OK) return rc;
+    if (!path || !a) { copy_err(errbuf, errlen, "null path or arrays"); return GMC_EINVAL; }
+    out::Opts o;
+    std::string e = out::parse_opts(opts, g.cfg.ntracer, o);
+    if (!e.empty()) { copy_err(errbuf, errlen, e); return GMC_EINVAL; }
+    out::State s = host_state(g.cfg, a);
+    std::vector<bool> found;
+    double t = 0;
+    e = out::read_restart(g, path, o, t, s, found);
+    if (!e.empty()) { copy_err(errbuf, errlen, e); return GMC_EIO; }
+    if (elapsed_seconds) *elapsed_seconds = t;
+    return GMC_OK;
+  } catch (const std::bad_alloc &) {
+    copy_err(errbuf, errlen, "host allocation failed");
+    return GMC_ENOMEM;
   }
 }
 

@@ -129,6 +129,11 @@ template <class R> void launch_surface_rel(const DGrid &g, const Launch &L, cons
 // non-finite or non-monotonic columns of a slot's filtered surface pressure (ERR_NAN, ERR_NONMONO)
 template <class R> void launch_check_columns(const DGrid &g, const Launch &L, const Slot<R> &s);
 template <class R> void launch_diagnose(const DGrid &g, const Launch &L, const Slot<R> &s, double *partial, double *out);
+// FP64 history diagnostics of a slot (out.cu): ph, t, z at full levels
+// (baroclinic; z = gz / g in shallow water, ph and t unused), div at cells,
+// vor at vertices; dense [k][j][i] device arrays.
+template <class R> void launch_output_diag(const DGrid &g, cudaStream_t st, const Slot<R> &s, double *ph, double *t,
+                                           double *z, double *div, double *vor);
 
 // Divergence damping of order 2 or 4 (div_damp_run, div_damp_mod.F90:89-139);
 // div and div2 are scratch cell fields.

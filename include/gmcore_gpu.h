@@ -54,6 +54,7 @@ extern "C" {
 #define GMC_ECUDA       -7   /* CUDA runtime error                           */
 #define GMC_ENOMEM      -8   /* device allocation failed                     */
 #define GMC_ESTATE      -9   /* call out of order (e.g. step before prepare) */
+#define GMC_EIO        -10   /* a history or restart file could not be written or read */
 
 /* ---- option enums (namelist strings of src/utils/namelist_mod.F90) ------ */
 #define GMC_TIME_EULER    0  /* time_scheme = 'euler'  */
@@ -204,6 +205,54 @@ int gmc_diagnose(gmc_ctx *ctx, int32_t member, gmc_diag *out);
 
 /* Number of steps taken since gmc_prepare. */
 int gmc_time_step(const gmc_ctx *ctx, int64_t *out);
+
+/* ---- history and restart files --------------------------------------------
+ * netCDF classic files (64-bit offset format, readable by any netCDF reader)
+ * with the reference's dimensions (time, lon, lat, ilon, ilat, lev, ilev),
+ * variable names, long names and units.  netCDF lists dimensions slowest
+ * first, so the reference's u(ilon, lat, lev, time) is stored as
+ * u(time, lev, lat, ilon): the library's own [k][j][i] order.
+ *   restart (r0): time_step_size, u, v, phs, pt (baroclinic) or u, v, gz
+ *     (shallow water), gzs, and the tracers  (restart_mod.F90:54-151; the
+ *     reference's restart holds no tracers)
+ *   history (h0): tm, te, tpe, te_ke, te_ie, te_pe, zs, phs, u, v, pt, t, z,
+ *     ph, vor, div and the tracers (hydrostatic, history_mod.F90:194-240,
+ *     519-580); tm, te, tpe, u, v, z, pv, div, zs (shallow water, :125-150,
+ *     398-444).  t, z, ph, vor and div are diagnosed in FP64 on the device
+ *     from the state (calc_ph, calc_t, calc_gz_lev, calc_vor, calc_div). */
+typedef struct gmc_file_opts {
+  const char *time_units;        /* "days", "hours", "minutes", "seconds"; NULL: "hours" */
+  const char *start_time;        /* origin of the time axis; NULL: "2000-01-01 00:00:00" */
+  const char *tracer_names;      /* comma-separated tracer variable names; NULL: q1, q2, ... */
+  const char *restart_interval;  /* restart file attribute restart_interval; NULL: none  */
+} gmc_file_opts;
+
+/* Host arrays of a restart (FP64, dense interior [k][j][i]): u_lon, v_lat,
+ * pt, phs (baroclinic) or gz (shallow water), gzs, and q with the ntracer
+ * tracers one after the other.  Unused pointers may be NULL; on reading, a
+ * NULL destination is skipped. */
+typedef struct gmc_restart_arrays {
+  double *u_lon, *v_lat, *pt, *phs, *gz, *gzs, *q;
+} gmc_restart_arrays;
+
+/* Restart file of a member's state at elapsed_seconds since the start. */
+int gmc_restart_write(gmc_ctx *ctx, int32_t member, const char *path, double elapsed_seconds,
+                      const gmc_file_opts *opts);
+/* Sets a member's state from the first record of a restart file (then
+ * gmc_prepare, as restart_read precedes the run's operators_prepare) and
+ * returns its time.  Tracers the file lacks are left as they are. */
+int gmc_restart_read(gmc_ctx *ctx, int32_t member, const char *path, const gmc_file_opts *opts,
+                     double *elapsed_seconds);
+/* History record of a member's state: a new file, or with append != 0 one
+ * more record of the history file at path (created when absent). */
+int gmc_history_write(gmc_ctx *ctx, int32_t member, const char *path, double elapsed_seconds, int32_t append,
+                      const gmc_file_opts *opts);
+/* The same restart files from and into host arrays, without a context or a
+ * GPU.  errbuf (may be NULL) receives the message of a failure. */
+int gmc_restart_write_host(const gmc_config *cfg, const char *path, double elapsed_seconds, const gmc_file_opts *opts,
+                           const gmc_restart_arrays *a, char *errbuf, int32_t errlen);
+int gmc_restart_read_host(const gmc_config *cfg, const char *path, const gmc_file_opts *opts,
+                          double *elapsed_seconds, const gmc_restart_arrays *a, char *errbuf, int32_t errlen);
 
 /* ---- operator entry points -----------------------------------------------
  * Device pointers, interior layout [k][j][i] (i fastest), in the context's

@@ -25,7 +25,7 @@ module gmcore_gpu_mod
   ! status codes
   integer(c_int), parameter :: GMC_OK = 0, GMC_EINVAL = -1, GMC_ECFL = -2, GMC_ENONMONO = -3, &
                                GMC_ENEGTRACER = -4, GMC_ENAN = -5, GMC_ECUDA = -7, &
-                               GMC_ENOMEM = -8, GMC_ESTATE = -9
+                               GMC_ENOMEM = -8, GMC_ESTATE = -9, GMC_EIO = -10
   ! namelist options (src/utils/namelist_mod.F90)
   integer(c_int32_t), parameter :: GMC_TIME_EULER = 0, GMC_TIME_PC2 = 1, GMC_TIME_WRFRK3 = 2
   integer(c_int32_t), parameter :: GMC_PV_MIDPOINT = 0, GMC_PV_UPWIND = 1, GMC_PV_TVD = 2
@@ -88,6 +88,16 @@ module gmcore_gpu_mod
     integer(c_int32_t) :: tracer
     type(gmc_view)     :: view
   end type gmc_io
+
+  ! history and restart file options: C strings (c_null_ptr: the default)
+  type, bind(c) :: gmc_file_opts
+    type(c_ptr) :: time_units, start_time, tracer_names, restart_interval
+  end type gmc_file_opts
+
+  ! dense FP64 host arrays of a restart (c_loc of contiguous arrays, or c_null_ptr)
+  type, bind(c) :: gmc_restart_arrays
+    type(c_ptr) :: u_lon, v_lat, pt, phs, gz, gzs, q
+  end type gmc_restart_arrays
 
   type, bind(c) :: gmc_ffsl_fields
     type(c_ptr) :: q, u, v, mfx, mfy, cflx, cfly, divx, divy, qmfx, qmfy
@@ -168,6 +178,62 @@ module gmcore_gpu_mod
       type(gmc_io), intent(in) :: in(*)
       type(gmc_io), intent(in) :: out(*)
     end function gmc_step_io
+
+    ! history and restart files (restart_write / restart_read / history_write_h0;
+    ! path is a null-terminated C string, e.g. trim(file) // c_null_char)
+    integer(c_int) function gmc_restart_write(ctx, member, path, elapsed_seconds, opts) &
+        bind(c, name='gmc_restart_write')
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: member
+      character(kind=c_char), intent(in) :: path(*)
+      real(c_double), value :: elapsed_seconds
+      type(gmc_file_opts), intent(in) :: opts
+    end function gmc_restart_write
+
+    integer(c_int) function gmc_restart_read(ctx, member, path, opts, elapsed_seconds) &
+        bind(c, name='gmc_restart_read')
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: member
+      character(kind=c_char), intent(in) :: path(*)
+      type(gmc_file_opts), intent(in) :: opts
+      real(c_double), intent(out) :: elapsed_seconds
+    end function gmc_restart_read
+
+    integer(c_int) function gmc_history_write(ctx, member, path, elapsed_seconds, append, opts) &
+        bind(c, name='gmc_history_write')
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: member, append
+      character(kind=c_char), intent(in) :: path(*)
+      real(c_double), value :: elapsed_seconds
+      type(gmc_file_opts), intent(in) :: opts
+    end function gmc_history_write
+
+    integer(c_int) function gmc_restart_write_host(cfg, path, elapsed_seconds, opts, a, errbuf, errlen) &
+        bind(c, name='gmc_restart_write_host')
+      import
+      type(gmc_config), intent(in) :: cfg
+      character(kind=c_char), intent(in) :: path(*)
+      real(c_double), value :: elapsed_seconds
+      type(gmc_file_opts), intent(in) :: opts
+      type(gmc_restart_arrays), intent(in) :: a
+      character(kind=c_char), intent(out) :: errbuf(*)
+      integer(c_int32_t), value :: errlen
+    end function gmc_restart_write_host
+
+    integer(c_int) function gmc_restart_read_host(cfg, path, opts, elapsed_seconds, a, errbuf, errlen) &
+        bind(c, name='gmc_restart_read_host')
+      import
+      type(gmc_config), intent(in) :: cfg
+      character(kind=c_char), intent(in) :: path(*)
+      type(gmc_file_opts), intent(in) :: opts
+      real(c_double), intent(out) :: elapsed_seconds
+      type(gmc_restart_arrays), intent(in) :: a
+      character(kind=c_char), intent(out) :: errbuf(*)
+      integer(c_int32_t), value :: errlen
+    end function gmc_restart_read_host
 
     integer(c_int) function gmc_diagnose(ctx, member, out) bind(c, name='gmc_diagnose')
       import

@@ -645,15 +645,7 @@ struct Model {
       for (int j = 1; j <= nhalf; ++j)
         for (int i = 1; i <= nlon + 1; ++i) s.mfy_lat(i, j, k) = s.m_lat(i, j, k) * s.v_f(i, j, k);
     if (baroclinic) accum_mf_cell(mass, s.mfx_lon, s.mfy_lat);
-    #pragma omp parallel for schedule(static)
-    for (int k = 1; k <= nlev; ++k)
-      for (int j = 1; j <= nhalf; ++j)
-        for (int i = 1; i <= nlon; ++i) {
-          s.mfx_lat(i, j, k) = g.half_tangent_wgt1[j] * (s.mfx_lon(i - 1, j, k) + s.mfx_lon(i, j, k)) +
-                               g.half_tangent_wgt2[j] * (s.mfx_lon(i - 1, j + 1, k) + s.mfx_lon(i, j + 1, k));
-          s.u_lat(i, j, k) = s.mfx_lat(i, j, k) / s.m_lat(i, j, k);
-        }
-    fill_halo(s.u_lat, false);
+    calc_u_lat(s);
     #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
       for (int j = 2; j <= nlat - 1; ++j)
@@ -665,8 +657,34 @@ struct Model {
     fill_halo(s.v_lon, true);
   }
 
+  // tangential mass flux and wind on the half rows (calc_mf, operators_mod.F90:585-597)
+  void calc_u_lat(State &s) {
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf;
+    const gmc::Grid &g = G();
+    #pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i) {
+          s.mfx_lat(i, j, k) = g.half_tangent_wgt1[j] * (s.mfx_lon(i - 1, j, k) + s.mfx_lon(i, j, k)) +
+                               g.half_tangent_wgt2[j] * (s.mfx_lon(i - 1, j + 1, k) + s.mfx_lon(i, j + 1, k));
+          s.u_lat(i, j, k) = s.mfx_lat(i, j, k) / s.m_lat(i, j, k);
+        }
+    fill_halo(s.u_lat, false);
+  }
+
   void calc_pv(State &s) {   // calc_vor + calc_pv, operators_mod.F90:612-703
-    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf, nlat = mesh.nlat;
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf;
+    const gmc::Grid &g = G();
+    calc_vor(s);
+    #pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nlev; ++k)
+      for (int j = 1; j <= nhalf; ++j)
+        for (int i = 1; i <= nlon; ++i) s.pv(i, j, k) = (s.vor(i, j, k) + g.half_f[j]) / s.m_vtx(i, j, k);
+    fill_halo(s.pv, false);
+  }
+
+  void calc_vor(State &s) {   // operators_mod.F90:612-680
+    const int nlon = mesh.nlon, nlev = mesh.nlev, nhalf = mesh.nhalf;
     const gmc::Grid &g = G();
     Arr &u = s.u_f, &v = s.v_f, &vor = s.vor;
     #pragma omp parallel for schedule(static)
@@ -686,12 +704,30 @@ struct Model {
         for (int i = 1; i <= nlon; ++i) vor(i, nhalf, k) = p;
       }
     }
-    (void)nlat;
+  }
+
+  // The fields a history record holds beside the state (history_mod.F90:519-580
+  // writes state%ph, t, gz / g, vor and div): recomputed on a copy of
+  // state(old) by calc_ph, calc_m, calc_t, calc_gz_lev, the zonal and
+  // tangential mass fluxes of calc_mf (without its batch accumulation),
+  // calc_vor and calc_div.
+  State output_state() {
+    State d = state[old_i];
+    const int nlon = mesh.nlon, nlat = mesh.nlat, nlev = mesh.nlev;
+    if (baroclinic) calc_ph(d);
+    calc_m(d);
+    if (baroclinic) {
+      calc_t(d);
+      calc_gz_lev(d);
+    }
     #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nlev; ++k)
-      for (int j = 1; j <= nhalf; ++j)
-        for (int i = 1; i <= nlon; ++i) s.pv(i, j, k) = (vor(i, j, k) + g.half_f[j]) / s.m_vtx(i, j, k);
-    fill_halo(s.pv, false);
+      for (int j = 2; j <= nlat - 1; ++j)
+        for (int i = 0; i <= nlon; ++i) d.mfx_lon(i, j, k) = d.m_lon(i, j, k) * d.u_f(i, j, k);
+    calc_u_lat(d);
+    calc_vor(d);
+    calc_div(d);
+    return d;
   }
 
   static double upwind1(double dir, double wgt, double f1, double f2) {
@@ -2083,6 +2119,32 @@ int orc_tracer_piece(void *h, int which, double *q, const double *mass) {
 
 int orc_diagnose(void *h, double *out) {
   ((orc::Model *)h)->diagnose(out);
+  return GMC_OK;
+}
+
+// History diagnostics of state(old), interior-only [k][j][i] (null: skipped):
+// ph, t, z = gz / g and div at cells, vor at vertices (half rows).  Shallow
+// water: z = gz / g of the state, div and vor; ph and t unused.
+int orc_output_diag(void *h, double *ph, double *t, double *z, double *div, double *vor) {
+  orc::Model *m = (orc::Model *)h;
+  orc::State d = m->output_state();
+  const int nlon = m->mesh.nlon, nlat = m->mesh.nlat, nhalf = m->mesh.nhalf, nlev = m->mesh.nlev;
+  const double g = m->cfg.g;
+  size_t o = 0, ov = 0;
+  for (int k = 1; k <= nlev; ++k)
+    for (int j = 1; j <= nlat; ++j)
+      for (int i = 1; i <= nlon; ++i, ++o) {
+        if (m->baroclinic) {
+          if (ph) ph[o] = d.ph(i, j, k);
+          if (t) t[o] = d.t(i, j, k);
+        }
+        if (z) z[o] = d.gz(i, j, k) / g;
+        if (div) div[o] = d.div(i, j, k);
+      }
+  for (int k = 1; k <= nlev; ++k)
+    for (int j = 1; j <= nhalf; ++j)
+      for (int i = 1; i <= nlon; ++i, ++ov)
+        if (vor) vor[ov] = d.vor(i, j, k);
   return GMC_OK;
 }
 

@@ -41,6 +41,7 @@ def load(variant="parity"):
     lib.orc_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     lib.orc_step.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
     lib.orc_diagnose.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.orc_output_diag.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 5
     lib.orc_space_identities.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.orc_metric.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int]
     lib.orc_filter_taps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]
@@ -170,6 +171,18 @@ class Oracle:
         out = np.zeros(8)
         self.lib.orc_diagnose(self.h, _ptr(out))
         return dict(zip(("tm", "te", "te_ke", "te_ie", "te_pe", "tav", "tpe", "tpt"), out))
+
+    def output_diag(self):
+        """History diagnostics of the current state: {ph, t, z, div, vor}
+        (shallow water: {z, div, vor})."""
+        c = self.cfg
+        cell = np.zeros((c.nlev, c.nlat, c.nlon))
+        out = {"z": cell.copy(), "div": cell.copy(), "vor": np.zeros((c.nlev, c.nlat - 1, c.nlon))}
+        if c.baroclinic:
+            out["ph"], out["t"] = cell.copy(), cell.copy()
+        p = lambda k: _ptr(out[k]) if k in out else None
+        self.lib.orc_output_diag(self.h, p("ph"), p("t"), p("z"), p("div"), p("vor"))
+        return out
 
     def space_identities(self):
         """Inner products of debug_check_space_operators at state(old)
