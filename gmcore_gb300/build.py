@@ -63,7 +63,7 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD_DIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fno-fast-math", *inc, "-c", s, "-o", o])
+            cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-fno-fast-math", *inc, "-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -76,7 +76,7 @@ def build(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=max(1, min(len(cmds), os.cpu_count() or 1))) as ex:
         list(ex.map(run, cmds))
     if force or cmds or _stale(LIB, objs):
-        libs = ["-lquadmath"] if platform.machine() in ("x86_64", "AMD64") else []
+        libs = (["-lquadmath"] if platform.machine() in ("x86_64", "AMD64") else []) + ["-lpthread"]
         run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, *libs])
     return LIB
 

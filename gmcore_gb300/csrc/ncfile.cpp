@@ -3,12 +3,16 @@
 // the same on little- and big-endian hosts.
 #include "ncfile.hpp"
 
+#include <fcntl.h>
+#include <sys/stat.h>
 #include <sys/types.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cerrno>
 #include <cstring>
 #include <limits>
+#include <thread>
 
 namespace gmc {
 namespace nc {
@@ -354,48 +358,101 @@ std::string Header::decode(const uint8_t *p, size_t n, Header &h, size_t &need) 
 }
 
 File::~File() {
-  if (f_) close();
+  if (fd_ >= 0) close();
 }
 
+namespace {
+
+// Whole-buffer positioned write and read (retrying short transfers).
+bool pwrite_all(int fd, const uint8_t *p, size_t n, uint64_t off) {
+  while (n > 0) {
+    const ssize_t w = ::pwrite(fd, p, n, (off_t)off);
+    if (w < 0 && errno == EINTR) continue;
+    if (w <= 0) return false;
+    p += w;
+    n -= (size_t)w;
+    off += (uint64_t)w;
+  }
+  return true;
+}
+bool pread_all(int fd, uint8_t *p, size_t n, uint64_t off) {
+  while (n > 0) {
+    const ssize_t r = ::pread(fd, p, n, (off_t)off);
+    if (r < 0 && errno == EINTR) continue;
+    if (r <= 0) return false;
+    p += r;
+    n -= (size_t)r;
+    off += (uint64_t)r;
+  }
+  return true;
+}
+
+// Runs body(a, b) over [0, n) split into contiguous parts, one per thread:
+// host threads convert and move large variables in parallel.
+template <class F>
+bool par_ranges(uint64_t n, uint64_t bytes, F body) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min(nt, 16u));
+  if (bytes < (8u << 20)) nt = 1;
+  if (nt == 1) return body(uint64_t(0), n);
+  std::vector<std::thread> th;
+  std::vector<char> ok(nt, 1);
+  const uint64_t per = (n + nt - 1) / nt;
+  for (unsigned t = 0; t < nt; ++t) {
+    const uint64_t a = std::min(n, t * per), b = std::min(n, a + per);
+    th.emplace_back([&, t, a, b]() { ok[t] = body(a, b) ? 1 : 0; });
+  }
+  for (std::thread &x : th) x.join();
+  return std::all_of(ok.begin(), ok.end(), [](char c) { return c != 0; });
+}
+
+constexpr uint64_t kChunk = 1 << 17;   // values converted per transfer
+
+}  // namespace
+
 std::string File::create(const std::string &path, Header hdr) {
-  if (f_) return "file already open";
+  if (fd_ >= 0) return "file already open";
   std::string e = hdr.layout();
   if (!e.empty()) return e;
   h = std::move(hdr);
   h.numrecs = 0;
-  f_ = std::fopen(path.c_str(), "w+b");
-  if (!f_) return "cannot create '" + path + "': " + std::strerror(errno);
+  fd_ = ::open(path.c_str(), O_RDWR | O_CREAT | O_TRUNC, 0644);
+  if (fd_ < 0) return "cannot create '" + path + "': " + std::strerror(errno);
   path_ = path;
   write_ = true;
   const std::vector<uint8_t> b = h.encode();
-  if (std::fwrite(b.data(), 1, b.size(), f_) != b.size()) return "cannot write the header of '" + path + "'";
+  if (!pwrite_all(fd_, b.data(), b.size(), 0)) return "cannot write the header of '" + path + "'";
   dirty_ = true;
   return "";
 }
 
 std::string File::open(const std::string &path, bool update) {
-  if (f_) return "file already open";
-  f_ = std::fopen(path.c_str(), update ? "r+b" : "rb");
-  if (!f_) return "cannot open '" + path + "': " + std::strerror(errno);
+  if (fd_ >= 0) return "file already open";
+  fd_ = ::open(path.c_str(), update ? O_RDWR : O_RDONLY);
+  if (fd_ < 0) return "cannot open '" + path + "': " + std::strerror(errno);
   path_ = path;
   write_ = update;
-  std::vector<uint8_t> buf(4096);
-  size_t got = std::fread(buf.data(), 1, buf.size(), f_);
+  struct stat sb;
+  if (fstat(fd_, &sb) != 0) return "cannot stat '" + path + "'";
+  const uint64_t size = (uint64_t)sb.st_size;
+  std::vector<uint8_t> buf((size_t)std::min<uint64_t>(size, 4096));
   for (;;) {
+    if (!buf.empty() && !pread_all(fd_, buf.data(), buf.size(), 0)) {
+      ::close(fd_);
+      fd_ = -1;
+      return "cannot read '" + path + "'";
+    }
     size_t need = 0;
-    std::string e = Header::decode(buf.data(), got, h, need);
+    std::string e = Header::decode(buf.data(), buf.size(), h, need);
     if (e.empty()) break;
-    if (need == 0 || got < buf.size()) {
-      std::fclose(f_);
-      f_ = nullptr;
+    if (need == 0 || buf.size() >= size) {
+      ::close(fd_);
+      fd_ = -1;
       return "'" + path + "': " + e;
     }
-    buf.resize(std::max(buf.size() * 2, got + need));
-    got += std::fread(buf.data() + got, 1, buf.size() - got, f_);
+    buf.resize((size_t)std::min<uint64_t>(size, std::max<uint64_t>(buf.size() * 2, buf.size() + need)));
   }
   if (h.numrecs == 0xFFFFFFFFull) {   // streaming: count the records present
-    fseeko(f_, 0, SEEK_END);
-    const uint64_t size = (uint64_t)ftello(f_);
     uint64_t first = size;
     for (const Var &v : h.vars)
       if (v.record) first = std::min(first, v.begin);
@@ -405,26 +462,28 @@ std::string File::open(const std::string &path, bool update) {
 }
 
 std::string File::put(const std::string &name, uint64_t rec, const double *src) {
-  if (!f_ || !write_) return "file not open for writing";
+  if (fd_ < 0 || !write_) return "file not open for writing";
   const int vi = h.var(name);
   if (vi < 0) return "no variable '" + name + "' in '" + path_ + "'";
   const Var &v = h.vars[(size_t)vi];
   if (rec > 0xFFFFFFFEull) return "record index out of range";
   const uint64_t off = v.begin + (v.record ? rec * h.recsize : 0);
-  if (fseeko(f_, (off_t)off, SEEK_SET) != 0) return "seek failed in '" + path_ + "'";
   const size_t es = type_size(v.type);
-  constexpr size_t kChunk = 1 << 17;   // values per write
-  std::vector<uint8_t> buf(std::min<uint64_t>(v.count, kChunk) * es + 4);
-  for (uint64_t at = 0; at < v.count; at += kChunk) {
-    const size_t n = (size_t)std::min<uint64_t>(kChunk, v.count - at);
-    for (size_t k = 0; k < n; ++k) store_value(v.type, src[at + k], &buf[k * es]);
-    size_t bytes = n * es;
-    if (at + n == v.count && !(v.record && h.recsize == v.count * es)) {   // pad the last chunk to 4 bytes
-      const size_t padded = (size_t)pad4(v.count * es) - (size_t)(at * es);
-      std::fill(buf.begin() + (long)bytes, buf.begin() + (long)padded, 0);
-      bytes = padded;
+  const bool ok = par_ranges(v.count, v.count * es, [&](uint64_t a, uint64_t b) {
+    std::vector<uint8_t> buf((size_t)std::min<uint64_t>(b - a, kChunk) * es);
+    for (uint64_t at = a; at < b; at += kChunk) {
+      const size_t n = (size_t)std::min<uint64_t>(kChunk, b - at);
+      for (size_t k = 0; k < n; ++k) store_value(v.type, src[at + k], &buf[k * es]);
+      if (!pwrite_all(fd_, buf.data(), n * es, off + at * es)) return false;
     }
-    if (std::fwrite(buf.data(), 1, bytes, f_) != bytes) return "write failed in '" + path_ + "'";
+    return true;
+  });
+  if (!ok) return "write failed in '" + path_ + "'";
+  // zero padding to the next 4 bytes (none when a single record variable fills the record)
+  const uint64_t pad = pad4(v.count * es) - v.count * es;
+  if (pad && !(v.record && h.recsize == v.count * es)) {
+    const uint8_t z[4] = {0, 0, 0, 0};
+    if (!pwrite_all(fd_, z, (size_t)pad, off + v.count * es)) return "write failed in '" + path_ + "'";
   }
   if (v.record && rec + 1 > h.numrecs) {
     h.numrecs = rec + 1;
@@ -434,34 +493,36 @@ std::string File::put(const std::string &name, uint64_t rec, const double *src) 
 }
 
 std::string File::get(const std::string &name, uint64_t rec, double *dst) {
-  if (!f_) return "file not open";
+  if (fd_ < 0) return "file not open";
   const int vi = h.var(name);
   if (vi < 0) return "no variable '" + name + "' in '" + path_ + "'";
   const Var &v = h.vars[(size_t)vi];
   if (v.record && rec >= h.numrecs) return "record " + std::to_string(rec) + " of '" + name + "' not in '" + path_ + "'";
   const uint64_t off = v.begin + (v.record ? rec * h.recsize : 0);
-  if (fseeko(f_, (off_t)off, SEEK_SET) != 0) return "seek failed in '" + path_ + "'";
   const size_t es = type_size(v.type);
-  constexpr size_t kChunk = 1 << 17;
-  std::vector<uint8_t> buf(std::min<uint64_t>(v.count, kChunk) * es);
-  for (uint64_t at = 0; at < v.count; at += kChunk) {
-    const size_t n = (size_t)std::min<uint64_t>(kChunk, v.count - at);
-    if (std::fread(buf.data(), 1, n * es, f_) != n * es) return "'" + path_ + "' ends inside variable '" + name + "'";
-    for (size_t k = 0; k < n; ++k) dst[at + k] = load_value(v.type, &buf[k * es]);
-  }
+  const bool ok = par_ranges(v.count, v.count * es, [&](uint64_t a, uint64_t b) {
+    std::vector<uint8_t> buf((size_t)std::min<uint64_t>(b - a, kChunk) * es);
+    for (uint64_t at = a; at < b; at += kChunk) {
+      const size_t n = (size_t)std::min<uint64_t>(kChunk, b - at);
+      if (!pread_all(fd_, buf.data(), n * es, off + at * es)) return false;
+      for (size_t k = 0; k < n; ++k) dst[at + k] = load_value(v.type, &buf[k * es]);
+    }
+    return true;
+  });
+  if (!ok) return "'" + path_ + "' ends inside variable '" + name + "'";
   return "";
 }
 
 std::string File::close() {
-  if (!f_) return "";
+  if (fd_ < 0) return "";
   std::string e;
   if (write_ && dirty_) {
     uint8_t b[4];
     put_be(b, (uint32_t)h.numrecs, 4);
-    if (fseeko(f_, 4, SEEK_SET) != 0 || std::fwrite(b, 1, 4, f_) != 4) e = "cannot update the record count of '" + path_ + "'";
+    if (!pwrite_all(fd_, b, 4, 4)) e = "cannot update the record count of '" + path_ + "'";
   }
-  if (std::fclose(f_) != 0 && e.empty()) e = "closing '" + path_ + "' failed";
-  f_ = nullptr;
+  if (::close(fd_) != 0 && e.empty()) e = "closing '" + path_ + "' failed";
+  fd_ = -1;
   dirty_ = false;
   return e;
 }

@@ -12,7 +12,6 @@
 #pragma once
 
 #include <cstdint>
-#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -89,7 +88,7 @@ class File {
   std::string close();
 
  private:
-  FILE *f_ = nullptr;
+  int fd_ = -1;
   bool write_ = false;
   bool dirty_ = false;
   std::string path_;
