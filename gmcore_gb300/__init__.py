@@ -33,6 +33,7 @@ EXPORTED = (
     "gmc_tlm_step", "gmc_adjoint", "gmc_set_graphs", "gmc_host_register", "gmc_host_unregister",
     "gmc_fp64_fma_peak", "gmc_fp32_fma_peak", "gmc_set_member_layout", "gmc_step_io",
     "gmc_restart_write", "gmc_restart_read", "gmc_history_write", "gmc_restart_write_host", "gmc_restart_read_host",
+    "gmc_output_wait",
 )
 # state fields of the tangent-linear and adjoint entry points, in ABI order
 TLAD_FIELDS = ("u_lon", "v_lat", "gz")
@@ -91,6 +92,7 @@ def load(build_if_missing=True):
     lib.gmc_fp64_fma_peak.argtypes = [P(C.c_double)]
     lib.gmc_fp32_fma_peak.argtypes = [P(C.c_double)]
     lib.gmc_set_member_layout.argtypes = [C.c_void_p, C.c_int32]
+    lib.gmc_output_wait.argtypes = [C.c_void_p]
     lib.gmc_restart_write.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_double, P(FileOpts)]
     lib.gmc_restart_read.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, P(FileOpts), P(C.c_double)]
     lib.gmc_history_write.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_double, C.c_int32, P(FileOpts)]
@@ -226,12 +228,12 @@ def make_ic(cfg, kind, seed, noise_k=1.0):
     return out
 
 
-def file_opts(time_units=None, start_time=None, tracer_names=None, restart_interval=None):
+def file_opts(time_units=None, start_time=None, tracer_names=None, restart_interval=None, background=False):
     """gmc_file_opts from keywords (None: the library's default)."""
     enc = lambda x: x.encode() if isinstance(x, str) else x
     if isinstance(tracer_names, (list, tuple)):
         tracer_names = ",".join(tracer_names)
-    return FileOpts(enc(time_units), enc(start_time), enc(tracer_names), enc(restart_interval))
+    return FileOpts(enc(time_units), enc(start_time), enc(tracer_names), enc(restart_interval), int(background))
 
 
 def _restart_arrays(cfg, state):
@@ -433,8 +435,13 @@ class Model:
         self._check(self.lib.gmc_restart_read(self.h, member, os.fsencode(path), C.byref(o), C.byref(t)))
         return t.value
 
+    def output_wait(self):
+        """Waits for a background history or restart write (gmc_output_wait)."""
+        self._check(self.lib.gmc_output_wait(self.h))
+
     def history_write(self, path, elapsed_seconds, append=False, member=0, **opts):
-        """One history record of the state (gmc_history_write)."""
+        """One history record of the state (gmc_history_write); background=True
+        returns after a device snapshot and writes while the steps go on."""
         o = file_opts(**opts)
         self._check(self.lib.gmc_history_write(self.h, member, os.fsencode(path), elapsed_seconds, int(append),
                                                C.byref(o)))

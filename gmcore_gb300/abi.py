@@ -94,7 +94,7 @@ class FileOpts(C.Structure):
     """gmc_file_opts: time axis, tracer names and restart attribute of the
     history and restart files (NULL members take the defaults)."""
     _fields_ = [("time_units", C.c_char_p), ("start_time", C.c_char_p), ("tracer_names", C.c_char_p),
-                ("restart_interval", C.c_char_p)]
+                ("restart_interval", C.c_char_p), ("background", C.c_int32)]
 
 
 class RestartArrays(C.Structure):

@@ -286,6 +286,23 @@ struct EngineBase {
   // water: z and div [nlat][nlon], ph, t and vor unused and may be null)
   virtual void output_diag(int member, double *ph, double *t, double *z, double *div, double *vor) = 0;
   virtual const Grid &host_grid() const = 0;
+  // Device copies of a member's output fields, for a file written in the
+  // background while the steps go on: the state and tracers (and, for a
+  // history record, the FP64 diagnostics and the integrals), taken in stream
+  // order after the steps issued so far, in one stream-ordered allocation
+  // that the writer frees.  Field pointers are in the form's storage type
+  // (float when fp32), phs, gzs and the diagnostics in double.
+  struct OutSnap {
+    bool fp32 = false;
+    char *block = nullptr;
+    const void *u = nullptr, *v = nullptr, *pt = nullptr, *gz = nullptr, *pv = nullptr;
+    const double *phs = nullptr, *gzs = nullptr;
+    std::vector<const void *> q;
+    const double *ph = nullptr, *t = nullptr, *z = nullptr, *div = nullptr, *vor = nullptr;
+    gmc_diag diag{};
+    cudaEvent_t ready = nullptr;   // recorded after the copies
+  };
+  virtual OutSnap snapshot(int member, bool history) = 0;
   virtual void set_graphs(bool on) = 0;
   virtual int layout_in_use() const = 0;
   virtual bool set_layout(int lay) = 0;
@@ -2115,6 +2132,75 @@ struct Engine : EngineBase {
   }
   const Grid &host_grid() const override { return grid; }
 
+  OutSnap snapshot(int m, bool history) override {
+    const Slot<R> &s = slots[m * 3 + old_i];
+    const bool bc = grid.cfg.baroclinic != 0;
+    const size_t nf = full3(), nh = half3(), n2 = two_d(), ncell = bc ? nf : n2;
+    size_t bytes = 0;
+    auto add = [&](size_t n, size_t es) {
+      const size_t off = bytes;
+      bytes += (n * es + 255) & ~(size_t)255;
+      return off;
+    };
+    const size_t o_u = add(nf, sizeof(R)), o_v = add(nh, sizeof(R)), o_gzs = add(n2, sizeof(double));
+    const size_t o_pt = bc ? add(nf, sizeof(R)) : 0, o_phs = bc ? add(n2, sizeof(double)) : 0;
+    const size_t o_gz = bc ? 0 : add(n2, sizeof(R)), o_pv = !bc && history ? add(nh, sizeof(R)) : 0;
+    std::vector<size_t> o_q;
+    for (int l = 0; l < ntr; ++l) o_q.push_back(add(nf, sizeof(R)));
+    size_t o_d[5] = {0, 0, 0, 0, 0};   // ph, t, z, div, vor
+    if (history) {
+      for (int d = 0; d < 4; ++d) o_d[d] = add(ncell, sizeof(double));
+      o_d[4] = add(nh, sizeof(double));
+    }
+    OutSnap o;
+    o.fp32 = kFP32;
+    CK(cudaMallocAsync((void **)&o.block, bytes, stream));
+    try {
+      fill_snapshot(o, s, m, history, bc, nf, nh, n2, o_u, o_v, o_gzs, o_pt, o_phs, o_gz, o_pv, o_q, o_d);
+    } catch (...) {
+      cudaFreeAsync(o.block, stream);
+      if (o.ready) cudaEventDestroy(o.ready);
+      throw;
+    }
+    return o;
+  }
+  void fill_snapshot(OutSnap &o, const Slot<R> &s, int m, bool history, bool bc, size_t nf, size_t nh, size_t n2,
+                     size_t o_u, size_t o_v, size_t o_gzs, size_t o_pt, size_t o_phs, size_t o_gz, size_t o_pv,
+                     const std::vector<size_t> &o_q, const size_t (&o_d)[5]) {
+    char *b = o.block;
+    auto copy = [&](size_t off, const void *src, size_t n) {
+      CK(cudaMemcpyAsync(b + off, src, n, cudaMemcpyDeviceToDevice, stream));
+      return (const void *)(b + off);
+    };
+    o.u = copy(o_u, s.u_lon, nf * sizeof(R));
+    o.v = copy(o_v, s.v_lat, nh * sizeof(R));
+    o.gzs = (const double *)copy(o_gzs, s.gzs, n2 * sizeof(double));
+    if (bc) {
+      o.pt = copy(o_pt, s.pt, nf * sizeof(R));
+      o.phs = (const double *)copy(o_phs, s.phs, n2 * sizeof(double));
+    } else {
+      o.gz = copy(o_gz, s.gz, n2 * sizeof(R));
+      if (history) o.pv = copy(o_pv, s.pv, nh * sizeof(R));
+    }
+    for (int l = 0; l < ntr; ++l) o.q.push_back(copy(o_q[(size_t)l], q[((size_t)m * 2 + q_old) * ntr + l], nf * sizeof(R)));
+    if (history) {
+      double *d[5];
+      for (int k = 0; k < 5; ++k) d[k] = reinterpret_cast<double *>(b + o_d[k]);
+      launch_output_diag<R>(dg, stream, s, d[0], d[1], d[2], d[3], d[4]);
+      CK(cudaGetLastError());
+      if (bc) {
+        o.ph = d[0];
+        o.t = d[1];
+        o.vor = d[4];
+      }
+      o.z = d[2];
+      o.div = d[3];
+      diagnose(m, &o.diag);
+    }
+    CK(cudaEventCreateWithFlags(&o.ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(o.ready, stream));
+  }
+
   // The first error raised on the device since the last read (the error
   // words are cleared): err[1] holds the first bit, err[0] all of them.
   unsigned read_error() override {
@@ -2137,6 +2223,14 @@ struct gmc_ctx {
   std::unique_ptr<EngineBase> eng;
   std::string last_error;
   int lon_halo_width = 0;
+  // the history or restart file being written in the background, and the
+  // status it ended with (read after the join)
+  std::thread bg;
+  int bg_rc = GMC_OK;
+  std::string bg_msg;
+  ~gmc_ctx() {
+    if (bg.joinable()) bg.join();
+  }
 };
 
 namespace {
@@ -2351,6 +2445,128 @@ void copy_err(char *buf, int32_t len, const std::string &msg) {
   const size_t n = std::min(msg.size(), (size_t)len - 1);
   std::memcpy(buf, msg.data(), n);
   buf[n] = 0;
+}
+
+// Waits for the context's background file write; its status (GMC_OK when
+// there was none), with its message as the context's last error.
+int join_background(gmc_ctx *ctx) {
+  if (ctx->bg.joinable()) ctx->bg.join();
+  const int rc = ctx->bg_rc;
+  if (rc != GMC_OK) ctx->last_error = ctx->bg_msg;
+  ctx->bg_rc = GMC_OK;
+  ctx->bg_msg.clear();
+  return rc;
+}
+
+// Body of a background write (a host thread): waits for the snapshot's
+// copies, moves it to host FP64 arrays on a stream of its own, frees it, and
+// writes the history record or restart file.
+void write_snapshot(gmc_ctx *ctx, EngineBase::OutSnap o, int device, bool history, std::string path, double elapsed,
+                    bool append, out::Opts opts) {
+  int rc = GMC_OK;
+  std::string msg;
+  cudaStream_t st = nullptr;
+  try {
+    const gmc_config &c = ctx->cfg;
+    const Grid &grid = ctx->eng->host_grid();
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CK(cudaEventSynchronize(o.ready));
+    const size_t n3 = (size_t)c.nlev * c.nlat * c.nlon, h3 = (size_t)c.nlev * (c.nlat - 1) * c.nlon,
+                 n2 = (size_t)c.nlat * c.nlon, ncell = c.baroclinic ? n3 : n2;
+    std::vector<float> f32;
+    // a field of the form's storage type, or a double array (dbl)
+    auto get = [&](const void *src, size_t n, std::vector<double> &dst, bool dbl) {
+      dst.resize(n);
+      if (!src) return;
+      if (o.fp32 && !dbl) {
+        f32.resize(n);
+        CK(cudaMemcpyAsync(f32.data(), src, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (size_t k = 0; k < n; ++k) dst[k] = (double)f32[k];
+      } else {
+        CK(cudaMemcpyAsync(dst.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+      }
+    };
+    HostState h(c);
+    get(o.u, n3, h.u, false);
+    get(o.v, h3, h.v, false);
+    get(o.gzs, n2, h.gzs, true);
+    if (c.baroclinic) {
+      get(o.pt, n3, h.pt, false);
+      get(o.phs, n2, h.phs, true);
+    } else {
+      get(o.gz, n2, h.gz, false);
+    }
+    std::vector<double> tmp;
+    for (size_t l = 0; l < o.q.size(); ++l) {
+      get(o.q[l], n3, tmp, false);
+      std::copy(tmp.begin(), tmp.end(), h.q.begin() + (long)(l * n3));
+    }
+    std::vector<double> ph, t, z, div, vor, pv;
+    if (history) {
+      if (c.baroclinic) {
+        get(o.ph, n3, ph, true);
+        get(o.t, n3, t, true);
+        get(o.vor, h3, vor, true);
+      } else {
+        get(o.pv, h3, pv, false);
+      }
+      get(o.z, ncell, z, true);
+      get(o.div, ncell, div, true);
+    }
+    CK(cudaFreeAsync(o.block, st));
+    o.block = nullptr;
+    CK(cudaStreamSynchronize(st));
+    const out::State sv = h.view(c);
+    std::string e;
+    if (history) {
+      out::History hv;
+      hv.u = sv.u;
+      hv.v = sv.v;
+      hv.pt = sv.pt;
+      hv.phs = sv.phs;
+      hv.gz = sv.gz;
+      hv.gzs = sv.gzs;
+      if (c.baroclinic) {
+        hv.ph = ph.data();
+        hv.t = t.data();
+        hv.vor = vor.data();
+      } else {
+        hv.pv = pv.data();
+      }
+      hv.z = z.data();
+      hv.div = div.data();
+      for (double *q : sv.q) hv.q.push_back(q);
+      hv.diag = o.diag;
+      e = out::write_history(grid, path, elapsed, append, opts, hv);
+    } else {
+      e = out::write_restart(grid, path, elapsed, opts, sv);
+    }
+    if (!e.empty()) {
+      rc = GMC_EIO;
+      msg = e;
+    }
+  } catch (const CudaError &e) {
+    rc = GMC_ECUDA;
+    msg = e.msg;
+  } catch (const std::bad_alloc &) {
+    rc = GMC_ENOMEM;
+    msg = "host allocation failed";
+  }
+  if (o.block) cudaFree(o.block);
+  if (o.ready) cudaEventDestroy(o.ready);
+  if (st) cudaStreamDestroy(st);
+  ctx->bg_rc = rc;
+  ctx->bg_msg = msg;
+}
+
+// Starts the background write of a member's history record or restart file.
+void start_background(gmc_ctx *ctx, int member, bool history, const char *path, double elapsed, bool append,
+                      const out::Opts &o) {
+  EngineBase::OutSnap snap = ctx->eng->snapshot(member, history);
+  ctx->bg = std::thread(write_snapshot, ctx, snap, ctx->eng->device, history, std::string(path), elapsed, append, o);
 }
 
 }  // namespace
@@ -2713,6 +2929,11 @@ const char *gmc_last_error(const gmc_ctx *ctx) { return ctx ? ctx->last_error.c_
 
 void gmc_destroy(gmc_ctx *ctx) { delete ctx; }
 
+int gmc_output_wait(gmc_ctx *ctx) {
+  if (!ctx) return GMC_EINVAL;
+  return join_background(ctx);
+}
+
 int gmc_mesh_metric(const gmc_config *cfg, const char *name, double *out, size_t n) {
   if (!cfg || !name || !out) return GMC_EINVAL;
   try {
@@ -2763,11 +2984,16 @@ int gmc_restart_write(gmc_ctx *ctx, int32_t member, const char *path, double ela
   if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
   if (!path) return fail(ctx, GMC_EINVAL, "null path");
   if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  if (const int prev = join_background(ctx)) return prev;   // the previous background write first
   return guarded(ctx, [&]() {
     const gmc_config &c = ctx->cfg;
     out::Opts o;
     std::string e = out::parse_opts(opts, c.ntracer, o);
     if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    if (opts && opts->background) {
+      start_background(ctx, member, false, path, elapsed_seconds, false, o);
+      return GMC_OK;
+    }
     HostState h(c);
     gather_state(*ctx->eng, c, member, h);
     e = out::write_restart(ctx->eng->host_grid(), path, elapsed_seconds, o, h.view(c));
@@ -2782,6 +3008,7 @@ int gmc_restart_read(gmc_ctx *ctx, int32_t member, const char *path, const gmc_f
   if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
   if (!path) return fail(ctx, GMC_EINVAL, "null path");
   if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  if (const int prev = join_background(ctx)) return prev;   // the previous background write first
   return guarded(ctx, [&]() {
     const gmc_config &c = ctx->cfg;
     out::Opts o;
@@ -2819,11 +3046,16 @@ int gmc_history_write(gmc_ctx *ctx, int32_t member, const char *path, double ela
   if (!ctx->eng) return fail(ctx, GMC_ESTATE, "context has no engine");
   if (!path) return fail(ctx, GMC_EINVAL, "null path");
   if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, GMC_EINVAL, "member out of range");
+  if (const int prev = join_background(ctx)) return prev;   // the previous background write first
   return guarded(ctx, [&]() {
     const gmc_config &c = ctx->cfg;
     out::Opts o;
     std::string e = out::parse_opts(opts, c.ntracer, o);
     if (!e.empty()) throw ApiError{GMC_EINVAL, e};
+    if (opts && opts->background) {
+      start_background(ctx, member, true, path, elapsed_seconds, append != 0, o);
+      return GMC_OK;
+    }
     EngineBase &eng = *ctx->eng;
     HostState h(c);
     gather_state(eng, c, member, h);

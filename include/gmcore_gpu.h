@@ -29,7 +29,9 @@
  *    the ranges the caller registers with gmc_host_register.
  *    The library owns device memory; model state stays resident in HBM
  *    between calls.
- *  - One host thread per context at a time.  All calls are synchronous.
+ *  - One host thread per context at a time.  All calls are synchronous, but
+ *    for history and restart files written in the background
+ *    (gmc_file_opts.background, gmc_output_wait).
  */
 #ifndef GMCORE_GPU_H
 #define GMCORE_GPU_H
@@ -225,6 +227,10 @@ typedef struct gmc_file_opts {
   const char *start_time;        /* origin of the time axis; NULL: "2000-01-01 00:00:00" */
   const char *tracer_names;      /* comma-separated tracer variable names; NULL: q1, q2, ... */
   const char *restart_interval;  /* restart file attribute restart_interval; NULL: none  */
+  int32_t background;            /* nonzero: gmc_history_write / gmc_restart_write copy the
+                                    member's fields on the device (in stream order after the
+                                    steps so far) and return; a host thread moves and writes
+                                    them while the caller steps on; gmc_output_wait ends it */
 } gmc_file_opts;
 
 /* Host arrays of a restart (FP64, dense interior [k][j][i]): u_lon, v_lat,
@@ -247,6 +253,11 @@ int gmc_restart_read(gmc_ctx *ctx, int32_t member, const char *path, const gmc_f
  * more record of the history file at path (created when absent). */
 int gmc_history_write(gmc_ctx *ctx, int32_t member, const char *path, double elapsed_seconds, int32_t append,
                       const gmc_file_opts *opts);
+/* Waits for the context's background file write (gmc_file_opts.background)
+ * and returns its status; GMC_OK when none is in flight.  Every file call and
+ * gmc_destroy wait for it first; a failed background write is reported by the
+ * next of them. */
+int gmc_output_wait(gmc_ctx *ctx);
 /* The same restart files from and into host arrays, without a context or a
  * GPU.  errbuf (may be NULL) receives the message of a failure. */
 int gmc_restart_write_host(const gmc_config *cfg, const char *path, double elapsed_seconds, const gmc_file_opts *opts,

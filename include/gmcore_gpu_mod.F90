@@ -92,6 +92,7 @@ module gmcore_gpu_mod
   ! history and restart file options: C strings (c_null_ptr: the default)
   type, bind(c) :: gmc_file_opts
     type(c_ptr) :: time_units, start_time, tracer_names, restart_interval
+    integer(c_int32_t) :: background
   end type gmc_file_opts
 
   ! dense FP64 host arrays of a restart (c_loc of contiguous arrays, or c_null_ptr)
@@ -210,6 +211,11 @@ module gmcore_gpu_mod
       real(c_double), value :: elapsed_seconds
       type(gmc_file_opts), intent(in) :: opts
     end function gmc_history_write
+
+    integer(c_int) function gmc_output_wait(ctx) bind(c, name='gmc_output_wait')
+      import
+      type(c_ptr), value :: ctx
+    end function gmc_output_wait
 
     integer(c_int) function gmc_restart_write_host(cfg, path, elapsed_seconds, opts, a, errbuf, errlen) &
         bind(c, name='gmc_restart_write_host')

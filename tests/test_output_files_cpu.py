@@ -169,6 +169,7 @@ def test_restart_continues_the_run_bit_for_bit_on_the_oracle(tmp_path, steps_bef
 
 
 def test_file_structs_match_the_header():
-    assert C.sizeof(abi.FileOpts) == 4 * C.sizeof(C.c_void_p)
+    assert C.sizeof(abi.FileOpts) == 5 * C.sizeof(C.c_void_p)   # four strings, an int32 and padding
+    assert abi.FileOpts.background.offset == 4 * C.sizeof(C.c_void_p)
     assert C.sizeof(abi.RestartArrays) == 7 * C.sizeof(C.c_void_p)
     assert abi.STATUS_NAMES[abi.GMC_EIO] == "GMC_EIO"

@@ -158,3 +158,47 @@ def test_restart_errors(tmp_path):
         m.history_write(tmp_path / "h.nc", 0.0, tracer_names="just_one")
     assert e.value.code == abi.GMC_EINVAL
     m.close()
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_background_writes_equal_synchronous_ones(tmp_path, precision):
+    """A background write captures the state at the call: the steps taken
+    while it runs do not reach the file, which equals, byte for byte, the file
+    a synchronous write of the same state makes."""
+    cfg = bc_config(precision)
+    st = g.make_ic(cfg, 2, 13, 1.0)
+    a, b = started(cfg, st, 2), started(cfg, st, 2)
+    a.history_write(tmp_path / "bg.h0.nc", 1200.0, background=True)
+    a.step(3)                                   # overlaps the write
+    a.restart_write(tmp_path / "bg.r0.nc", 3000.0, background=True)   # waits for the history write first
+    a.step(1)
+    a.output_wait()
+    b.history_write(tmp_path / "fg.h0.nc", 1200.0)
+    b.step(3)
+    b.restart_write(tmp_path / "fg.r0.nc", 3000.0)
+    for name in ("h0", "r0"):
+        assert (tmp_path / f"bg.{name}.nc").read_bytes() == (tmp_path / f"fg.{name}.nc").read_bytes(), name
+    b.step(1)
+    for k in DYN:
+        assert np.array_equal(a.get_field(k), b.get_field(k)), k
+    a.output_wait()                             # nothing in flight: OK
+    a.close()
+    b.close()
+
+
+def test_background_write_failure_is_reported(tmp_path):
+    cfg = bc_config(abi.PREC_MIXED)
+    m = started(cfg, g.make_ic(cfg, 2, 9, 1.0), 1)
+    m.history_write(tmp_path / "no_such_dir" / "h.nc", 0.0, background=True)
+    m.step(1)
+    with pytest.raises(GmcError) as e:
+        m.output_wait()
+    assert e.value.code == abi.GMC_EIO
+    m.output_wait()                             # reported once
+    # a failed background write is reported by the next file call
+    m.restart_write(tmp_path / "no_such_dir" / "r.nc", 0.0, background=True)
+    with pytest.raises(GmcError) as e:
+        m.restart_write(tmp_path / "r.nc", 0.0)
+    assert e.value.code == abi.GMC_EIO
+    m.restart_write(tmp_path / "r.nc", 0.0)
+    m.close()
