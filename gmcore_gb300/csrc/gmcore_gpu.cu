@@ -603,6 +603,8 @@ struct Engine : EngineBase {
     if (pinned) cudaFreeHost(pinned);
     pinned = nullptr;
     if (xstream) cudaStreamDestroy(xstream);
+    if (qstream) cudaStreamDestroy(qstream);
+    for (cudaEvent_t e : qev) cudaEventDestroy(e);
     if (xin_ev) cudaEventDestroy(xin_ev);
     if (xdyn_ev) cudaEventDestroy(xdyn_ev);
     if (xstage) cudaFree(xstage);
@@ -935,10 +937,17 @@ struct Engine : EngineBase {
   // transfers are copy-engine DMA of FP64 rows between registered host memory
   // and a device staging area, converted on the device; other items take the
   // gmc_set_* / gmc_get_* paths before and after the step.
-  cudaStream_t xstream = nullptr;
+  // Tracer outputs of registered arrays are pipelined with the last step's
+  // tracer advection: the tracers then advect one after the other on the
+  // context stream, each recording qev[l] when done, and tracer l moves back
+  // on qstream while the next ones advect.
+  cudaStream_t xstream = nullptr, qstream = nullptr;
   cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr;
+  std::vector<cudaEvent_t> qev;                  // [tracer]
   bool io_wait = false, io_rec = false;          // requested for this call's first / last step
   bool cur_io_wait = false, cur_io_rec = false;  // in effect for the step being issued
+  bool io_qout = false, cur_io_qout = false;     // tracer outputs pipelined with the last step
+  bool q_piped = false;                          // the last step advected its tracers pipelined
   bool io_waited = false;                        // the current step has issued its wait
   double *xstage = nullptr;
   size_t xstage_n = 0;
@@ -946,8 +955,11 @@ struct Engine : EngineBase {
   void io_streams() {
     if (xstream) return;
     CK(cudaStreamCreateWithFlags(&xstream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&qstream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&xin_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xdyn_ev, cudaEventDisableTiming));
+    qev.resize((size_t)ntr);
+    for (cudaEvent_t &e : qev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   double *io_stage(size_t n) {
     if (n > xstage_n) {
@@ -1109,24 +1121,34 @@ struct Engine : EngineBase {
     // (xstream), the tracers after the step (context stream)
     if (!out_x.empty() || !out_main.empty()) {
       io_rec = !out_x.empty();
+      io_qout = !out_main.empty();
       after_last = [&]() {
         if (!out_x.empty()) {
           CK(cudaStreamWaitEvent(xstream, xdyn_ev, 0));
           for (const Xfer &t : out_x) download(t, xstream);
         }
-        for (const Xfer &t : out_main) download(t, stream);
+        for (const Xfer &t : out_main) {
+          if (q_piped) {   // each tracer once its own advection is done
+            CK(cudaStreamWaitEvent(qstream, qev[(size_t)t.tracer], 0));
+            download(t, qstream);
+          } else {
+            download(t, stream);
+          }
+        }
       };
     }
     struct Reset {
       Engine *e;
       ~Reset() {
-        e->io_wait = e->io_rec = false;
+        e->io_wait = e->io_rec = e->io_qout = e->q_piped = false;
         e->after_last = nullptr;
         if (e->xstream) cudaStreamSynchronize(e->xstream);
+        if (e->qstream) cudaStreamSynchronize(e->qstream);
       }
     } reset{this};
     step(nsteps);
     if (xstream) CK(cudaStreamSynchronize(xstream));
+    if (qstream) CK(cudaStreamSynchronize(qstream));
     for (const IoItem *x : out_sync) {
       if (x->tracer >= 0) get_tracer(m, x->tracer, x->view);
       else get_field(m, x->name, x->view);
@@ -1213,8 +1235,10 @@ struct Engine : EngineBase {
       bv.u = b.u; bv.v = b.v; bv.mfx = b.mfx; bv.mfy = b.mfy;
       bv.cflx = b.cflx; bv.cfly = b.cfly; bv.divx = b.divx; bv.divy = b.divy; bv.cflz = b.cflz;
       // tracers on their own streams unless profiling (whose events time
-      // the context stream)
-      const bool tfork = tracer_streams() && !prof;
+      // the context stream) or pipelined with their transfers back
+      const bool qpipe = cur_io_qout;
+      if (qpipe) q_piped = true;
+      const bool tfork = tracer_streams() && !prof && !qpipe;
       if (tfork && !dry) {
         CK(cudaEventRecord(tfork_ev, L.stream));
         for (cudaStream_t st : tstreams) CK(cudaStreamWaitEvent(st, tfork_ev, 0));
@@ -1231,6 +1255,9 @@ struct Engine : EngineBase {
         K("tracer_horizontal", 1, [&] { launch_tracer_horizontal<R>(dg, Lt, qo, qn, fx, fy, b.old_surf(), n.surf(), dt_adv); });
         K("tracer_vertical", 1, [&] { launch_tracer_vertical<R>(dg, Lt, qn, b.cflz, b.we, n.surf(), dt_adv); });
         K("tracer_lon_damp", 1, [&] { launch_tracer_lon_damp<R>(dg, Lt, qn); });
+        if (qpipe && !dry)
+          CK(cudaEventRecordWithFlags(qev[(size_t)l], Lt.stream,
+                                      capturing(Lt.stream) ? cudaEventRecordExternal : cudaEventRecordDefault));
       }
       if (tfork && !dry) {
         for (int t = 0; t < ntr; ++t) {
@@ -2011,6 +2038,7 @@ struct Engine : EngineBase {
       const int o = old_i, n = new_i;
       cur_io_wait = io_wait && it == 0;
       cur_io_rec = io_rec && it == nsteps - 1;
+      cur_io_qout = io_qout && it == nsteps - 1;
       io_waited = false;
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
       const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
@@ -2025,7 +2053,7 @@ struct Engine : EngineBase {
       }
       if (use_graphs) {
         const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old, lay,
-                           (cur_io_wait ? 1 : 0) | (cur_io_rec ? 2 : 0)};
+                           (cur_io_wait ? 1 : 0) | (cur_io_rec ? 2 : 0) | (cur_io_qout ? 4 : 0)};
         auto gi = graphs.find(key);
         if (gi == graphs.end()) {
           cudaGraph_t gr = nullptr;
@@ -2076,7 +2104,7 @@ struct Engine : EngineBase {
       std::swap(old_i, new_i);
       ++time_step;
     }
-    cur_io_wait = cur_io_rec = false;
+    cur_io_wait = cur_io_rec = cur_io_qout = false;
     if (after_last) after_last();
     CK(cudaEventRecord(ev_b, stream));
     CK(cudaGetLastError());
