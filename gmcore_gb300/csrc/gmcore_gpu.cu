@@ -607,6 +607,8 @@ struct Engine : EngineBase {
     for (cudaEvent_t e : qev) cudaEventDestroy(e);
     if (xin_ev) cudaEventDestroy(xin_ev);
     if (xdyn_ev) cudaEventDestroy(xdyn_ev);
+    if (xpt_ev) cudaEventDestroy(xpt_ev);
+    if (xlate_ev) cudaEventDestroy(xlate_ev);
     if (xstage) cudaFree(xstage);
     xstream = nullptr;
     xstage = nullptr;
@@ -941,8 +943,15 @@ struct Engine : EngineBase {
   // tracer advection: the tracers then advect one after the other on the
   // context stream, each recording qev[l] when done, and tracer l moves back
   // on qstream while the next ones advect.
+  // The first step's first stage reads pt from its potential-temperature
+  // transport on, and u_lon, v_lat, phs only in its update kernels, so those
+  // inputs cross the link on xstream while the stage's forward pass starts:
+  // pt first (xpt_ev, waited before the first transport kernel), then the
+  // others (xlate_ev, waited before the updates), then the tracers.
   cudaStream_t xstream = nullptr, qstream = nullptr;
-  cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr;
+  cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr, xpt_ev = nullptr, xlate_ev = nullptr;
+  bool io_pt = false, io_late = false, cur_io_pt = false, cur_io_late = false, pt_waited = false,
+       late_waited = false;
   std::vector<cudaEvent_t> qev;                  // [tracer]
   bool io_wait = false, io_rec = false;          // requested for this call's first / last step
   bool cur_io_wait = false, cur_io_rec = false;  // in effect for the step being issued
@@ -958,6 +967,8 @@ struct Engine : EngineBase {
     CK(cudaStreamCreateWithFlags(&qstream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&xin_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xdyn_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&xpt_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&xlate_ev, cudaEventDisableTiming));
     qev.resize((size_t)ntr);
     for (cudaEvent_t &e : qev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
@@ -992,6 +1003,18 @@ struct Engine : EngineBase {
   void io_dyn_done(cudaStream_t st) {   // after the stages of a step
     if (!cur_io_rec || dry) return;
     CK(cudaEventRecordWithFlags(xdyn_ev, st, capturing(st) ? cudaEventRecordExternal : cudaEventRecordDefault));
+  }
+  void io_pt_ready(cudaStream_t st) {   // before the first stage reads pt
+    if (!cur_io_pt || pt_waited) return;
+    pt_waited = true;
+    if (dry) return;
+    CK(cudaStreamWaitEvent(st, xpt_ev, capturing(st) ? cudaEventWaitExternal : cudaEventWaitDefault));
+  }
+  void io_late_ready(cudaStream_t st) {   // before the first stage's updates read u_lon, v_lat, phs
+    if (!cur_io_late || late_waited) return;
+    late_waited = true;
+    if (dry) return;
+    CK(cudaStreamWaitEvent(st, xlate_ev, capturing(st) ? cudaEventWaitExternal : cudaEventWaitDefault));
   }
   void io_tracers_ready(cudaStream_t st) {   // before the tracer step reads q
     if (!cur_io_wait || io_waited) return;
@@ -1105,14 +1128,32 @@ struct Engine : EngineBase {
       }
       copy_rows(t, const_cast<double *>(src), false, st);
     };
-    // fields on the context stream ahead of the step; tracers on xstream,
-    // which the first step's tracer advection waits for
-    for (const Xfer &t : in_main) upload(t, stream);
-    if (!in_x.empty()) {
-      // after the fields (the link carries one direction's copies at a time
-      // best; the fields are needed first)
+    // pt, then u_lon, v_lat, phs on xstream while the first stage starts
+    // (see xpt_ev); other fields on the context stream ahead of the step;
+    // then the tracers on xstream, which the first step's tracer advection
+    // waits for
+    std::vector<Xfer> in_pt, in_late, in_early;
+    for (const Xfer &t : in_main) {
+      if (t.name == "pt") in_pt.push_back(t);
+      else if (t.name == "u_lon" || t.name == "v_lat" || t.name == "phs") in_late.push_back(t);
+      else in_early.push_back(t);
+    }
+    for (const Xfer &t : in_early) upload(t, stream);
+    if (!in_pt.empty() || !in_late.empty() || !in_x.empty()) {
       CK(cudaEventRecord(xin_ev, stream));
       CK(cudaStreamWaitEvent(xstream, xin_ev, 0));
+    }
+    if (!in_pt.empty()) {
+      for (const Xfer &t : in_pt) upload(t, xstream);
+      CK(cudaEventRecord(xpt_ev, xstream));
+      io_pt = true;
+    }
+    if (!in_late.empty()) {
+      for (const Xfer &t : in_late) upload(t, xstream);
+      CK(cudaEventRecord(xlate_ev, xstream));
+      io_late = true;
+    }
+    if (!in_x.empty()) {
       for (const Xfer &t : in_x) upload(t, xstream);
       CK(cudaEventRecord(xin_ev, xstream));
       io_wait = true;
@@ -1140,7 +1181,7 @@ struct Engine : EngineBase {
     struct Reset {
       Engine *e;
       ~Reset() {
-        e->io_wait = e->io_rec = e->io_qout = e->q_piped = false;
+        e->io_wait = e->io_rec = e->io_qout = e->q_piped = e->io_pt = e->io_late = false;
         e->after_last = nullptr;
         if (e->xstream) cudaStreamSynchronize(e->xstream);
         if (e->qstream) cudaStreamSynchronize(e->qstream);
@@ -1349,6 +1390,7 @@ struct Engine : EngineBase {
       BatchView<R> b{};
       b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
       b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
+      io_pt_ready(L.stream);   // pt of gmc_step_io
       ffsl3(L, b, s.pt, w.qx, w.qy, w.ptf_lon, w.ptf_lat, dt);
       K("pt_tendency", 1, [&] { launch_pt_tendency<R>(dg, L, s, w); });
     } else {
@@ -1379,6 +1421,7 @@ struct Engine : EngineBase {
     BatchView<R> b{};
     b.u = s.u_f; b.v = s.v_f; b.mfx = s.mfx_lon; b.mfy = s.mfy_lat;
     b.cflx = w.cflx; b.cfly = w.cfly; b.divx = w.divx; b.divy = w.divy; b.cflz = w.cflz;
+    io_pt_ready(dside);   // pt of gmc_step_io
     K("ffsl_inner_y", 1, [&] { launch_ffsl_inner_y<R>(dg, Ls, b, s.pt, w.qy, dt); });
     // context stream: mass fluxes, then the column sweep (which the pt
     // tendency needs) ahead of the PV chain, so that the two chains are of
@@ -1407,6 +1450,7 @@ struct Engine : EngineBase {
   }
   void stage_io(const Slot<R> &O, const Slot<R> &S, const Slot<R> &N, Work<R> &w, double dt) {
     forward_w(w, S, dt);
+    io_late_ready(L.stream);   // u_lon, v_lat, phs of gmc_step_io
     if (grid.cfg.baroclinic) {
       K("update_phs", 1, [&] { launch_update_phs<R>(dg, L, O, N, w, dt); });
       K("update_pt", 1, [&] { launch_update_pt<R>(dg, L, O, N, w, dt); });
@@ -2039,7 +2083,9 @@ struct Engine : EngineBase {
       cur_io_wait = io_wait && it == 0;
       cur_io_rec = io_rec && it == nsteps - 1;
       cur_io_qout = io_qout && it == nsteps - 1;
-      io_waited = false;
+      cur_io_pt = io_pt && it == 0;
+      cur_io_late = io_late && it == 0;
+      io_waited = pt_waited = late_waited = false;
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
       const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
       if (ring) alert_ring = true;
@@ -2053,7 +2099,8 @@ struct Engine : EngineBase {
       }
       if (use_graphs) {
         const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old, lay,
-                           (cur_io_wait ? 1 : 0) | (cur_io_rec ? 2 : 0) | (cur_io_qout ? 4 : 0)};
+                           (cur_io_wait ? 1 : 0) | (cur_io_rec ? 2 : 0) | (cur_io_qout ? 4 : 0) |
+                               (cur_io_pt ? 8 : 0) | (cur_io_late ? 16 : 0)};
         auto gi = graphs.find(key);
         if (gi == graphs.end()) {
           cudaGraph_t gr = nullptr;
@@ -2104,7 +2151,7 @@ struct Engine : EngineBase {
       std::swap(old_i, new_i);
       ++time_step;
     }
-    cur_io_wait = cur_io_rec = cur_io_qout = false;
+    cur_io_wait = cur_io_rec = cur_io_qout = cur_io_pt = cur_io_late = false;
     if (after_last) after_last();
     CK(cudaEventRecord(ev_b, stream));
     CK(cudaGetLastError());

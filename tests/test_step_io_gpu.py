@@ -52,8 +52,12 @@ def test_exchange_equals_separate_calls(precision, registered, nsteps):
         g.host_register(a)
     try:
         for _ in range(3):
-            # perturb the host state between exchanges, as a coupled driver would
+            # perturb every input between exchanges, as a coupled driver would,
+            # so that an input read before its transfer ends would show
             host["pt"] *= 1.0 + 1e-6
+            host["u_lon"] *= 1.0 + 1e-6
+            host["v_lat"] *= 1.0 - 1e-6
+            host["phs"] += 0.5
             host["q"][0] *= 0.999
             for k in FIELDS:
                 ref.set_field(k, host[k])
