@@ -205,6 +205,17 @@ int main(int argc, char **argv) {
   const double dv[8] = {d.tm, d.te, d.te_ke, d.te_ie, d.te_pe, d.tav, d.tpe, d.tpt};
   fwrite(dv, sizeof(double), 8, f);
   fclose(f);
+  /* history (in the background, overlapping one more exchange-free call) and
+   * restart files of the final state: OUT.h0.nc, OUT.r0.nc */
+  char path[4096];
+  const double elapsed = dt * nsteps;
+  gmc_file_opts fo = {"hours", "2000-01-01 00:00:00", NULL, "1 days", 1};
+  snprintf(path, sizeof path, "%s.h0.nc", argv[11]);
+  check(ctx, gmc_history_write(ctx, 0, path, elapsed, 0, &fo), "gmc_history_write");
+  check(ctx, gmc_output_wait(ctx), "gmc_output_wait");
+  fo.background = 0;
+  snprintf(path, sizeof path, "%s.r0.nc", argv[11]);
+  check(ctx, gmc_restart_write(ctx, 0, path, elapsed, &fo), "gmc_restart_write");
   gmc_destroy(ctx);
   printf("step_driver ok: %d steps\n", nsteps);
   return 0;

@@ -3,8 +3,10 @@ host program built with gcc against include/gmcore_gpu.h and linked to the
 library, runs the seeded state through create / set (halo'd column-major
 arrays) / prepare / N steps / get / diagnose, each step one gmc_step_io
 exchange through its registered halo'd arrays (the overlapped transfers with
-row pitch and level stride).  Its output must match the FP64 oracle run on the
-same state, as the Python-driven parity tests do."""
+row pitch and level stride), then writes a history record (in the background)
+and a restart file.  Its output must match the FP64 oracle run on the same
+state, as the Python-driven parity tests do, and its files must hold that
+output."""
 import os
 import subprocess
 
@@ -75,3 +77,16 @@ def test_c_driver_matches_oracle(tmp_path, case):
     print(case, errs)
     assert max(errs.values()) <= 1e-11, errs
     assert abs(diag[0] - d["tm"]) <= 1e-11 * abs(d["tm"])
+    # the history and restart files it wrote through the C ABI hold its final state
+    from scipy.io import netcdf_file
+    out = os.path.join(tmp, "state.bin")
+    file_names = {"u_lon": "u", "v_lat": "v", "pt": "pt", "phs": "phs", "gz": "gz"}
+    with netcdf_file(out + ".r0.nc", "r", mmap=False) as f:
+        assert f.variables["time"][0] == dt * nsteps / 3600 and f.restart_interval == b"1 days"
+        for name, shape in names:
+            assert np.array_equal(f.variables[file_names[name]][0].reshape(shape), got[name]), name
+        for l in range(ntr):
+            assert np.array_equal(f.variables[f"q{l + 1}"][0], q[l])
+    with netcdf_file(out + ".h0.nc", "r", mmap=False) as f:
+        assert f.variables["te"][0] == diag[1] and f.variables["tpe"][0] == diag[6]
+        assert np.array_equal(f.variables["u"][0].reshape(got["u_lon"].shape), got["u_lon"])
