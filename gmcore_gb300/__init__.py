@@ -12,6 +12,7 @@ and fails with an exception when it is missing or has no GPU.
 """
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -290,6 +291,7 @@ class Model:
     def __init__(self, cfg):
         self.lib = load()
         self.cfg = cfg
+        self._io_cache = {}
         h = C.c_void_p()
         rc = self.lib.gmc_create(C.byref(cfg), C.byref(h))
         self.h = h.value
@@ -390,7 +392,6 @@ class Model:
         (registered with host_register for the overlapped transfers)."""
         def items(seq):
             arr = (Io * max(len(seq), 1))()
-            keep = []
             for t, (key, a) in enumerate(seq):
                 if isinstance(key, str):
                     nk = 1 if a.ndim == 2 else None
@@ -401,10 +402,20 @@ class Model:
                     arr[t].name = None
                     arr[t].tracer = int(key)
                     arr[t].view = view_of(a)
-                keep.append(a)
-            return arr, keep
-        ain, kin = items(inputs)
-        aout, kout = items(outputs)
+            return arr
+        # a driver exchanges the same arrays call after call: their item
+        # arrays are kept (with weak references to the arrays, so that a
+        # dead array's id is never taken for a live one)
+        key = (tuple((k, id(a)) for k, a in inputs), tuple((k, id(a)) for k, a in outputs))
+        hit = self._io_cache.get(key)
+        if hit is not None and all(r() is a for r, (_, a) in zip(hit[2], list(inputs) + list(outputs))):
+            ain, aout = hit[0], hit[1]
+        else:
+            ain, aout = items(inputs), items(outputs)
+            refs = [weakref.ref(a) for _, a in list(inputs) + list(outputs)]
+            if len(self._io_cache) >= 8:
+                self._io_cache.pop(next(iter(self._io_cache)))
+            self._io_cache[key] = (ain, aout, refs)
         self._check(self.lib.gmc_step_io(self.h, member, ain, len(inputs), nsteps, aout, len(outputs)))
         return outputs
 
