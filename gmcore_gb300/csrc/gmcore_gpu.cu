@@ -609,6 +609,7 @@ struct Engine : EngineBase {
     if (xdyn_ev) cudaEventDestroy(xdyn_ev);
     if (xpt_ev) cudaEventDestroy(xpt_ev);
     if (xlate_ev) cudaEventDestroy(xlate_ev);
+    if (xptf_ev) cudaEventDestroy(xptf_ev);
     if (xstage) cudaFree(xstage);
     xstream = nullptr;
     xstage = nullptr;
@@ -950,6 +951,12 @@ struct Engine : EngineBase {
   // others (xlate_ev, waited before the updates), then the tracers.
   cudaStream_t xstream = nullptr, qstream = nullptr;
   cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr, xpt_ev = nullptr, xlate_ev = nullptr;
+  // Without test forcing (which changes pt after the integrator) the last
+  // stage's update_pt leaves pt and phs final, so they move back from there
+  // (xptf_ev) while the column sweep and the wind update still run.
+  cudaEvent_t xptf_ev = nullptr;
+  bool stage_last = false;   // the stage being issued is the step's last
+  bool ptf_recorded = false;
   bool io_pt = false, io_late = false, cur_io_pt = false, cur_io_late = false, pt_waited = false,
        late_waited = false;
   std::vector<cudaEvent_t> qev;                  // [tracer]
@@ -969,6 +976,7 @@ struct Engine : EngineBase {
     CK(cudaEventCreateWithFlags(&xdyn_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xpt_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xlate_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&xptf_ev, cudaEventDisableTiming));
     qev.resize((size_t)ntr);
     for (cudaEvent_t &e : qev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
@@ -1165,8 +1173,18 @@ struct Engine : EngineBase {
       io_qout = !out_main.empty();
       after_last = [&]() {
         if (!out_x.empty()) {
+          // pt and phs first, from the last stage's update_pt on when recorded
+          auto early = [&](const Xfer &t) { return ptf_recorded && (t.name == "pt" || t.name == "phs"); };
+          bool any_early = false;
+          for (const Xfer &t : out_x) any_early = any_early || early(t);
+          if (any_early) {
+            CK(cudaStreamWaitEvent(xstream, xptf_ev, 0));
+            for (const Xfer &t : out_x)
+              if (early(t)) download(t, xstream);
+          }
           CK(cudaStreamWaitEvent(xstream, xdyn_ev, 0));
-          for (const Xfer &t : out_x) download(t, xstream);
+          for (const Xfer &t : out_x)
+            if (!early(t)) download(t, xstream);
         }
         for (const Xfer &t : out_main) {
           if (q_piped) {   // each tracer once its own advection is done
@@ -1181,7 +1199,7 @@ struct Engine : EngineBase {
     struct Reset {
       Engine *e;
       ~Reset() {
-        e->io_wait = e->io_rec = e->io_qout = e->q_piped = e->io_pt = e->io_late = false;
+        e->io_wait = e->io_rec = e->io_qout = e->q_piped = e->io_pt = e->io_late = e->ptf_recorded = false;
         e->after_last = nullptr;
         if (e->xstream) cudaStreamSynchronize(e->xstream);
         if (e->qstream) cudaStreamSynchronize(e->qstream);
@@ -1454,6 +1472,12 @@ struct Engine : EngineBase {
     if (grid.cfg.baroclinic) {
       K("update_phs", 1, [&] { launch_update_phs<R>(dg, L, O, N, w, dt); });
       K("update_pt", 1, [&] { launch_update_pt<R>(dg, L, O, N, w, dt); });
+      if (stage_last && cur_io_rec && grid.cfg.forcing == GMC_FORCING_NONE) {   // pt, phs final (xptf_ev)
+        ptf_recorded = true;
+        if (!dry)
+          CK(cudaEventRecordWithFlags(xptf_ev, L.stream,
+                                      capturing(L.stream) ? cudaEventRecordExternal : cudaEventRecordDefault));
+      }
       K("column_backward", 1, [&] { launch_column_backward<R>(dg, L, N, w); });
     } else {
       K("update_gz", 1, [&] { launch_update_gz<R>(dg, L, O, N, w, dt); });
@@ -2029,19 +2053,23 @@ struct Engine : EngineBase {
       if (fork) L.stream = mstreams[m % mstreams.size()];
       switch (grid.cfg.time_scheme) {
         case GMC_TIME_EULER:
+          stage_last = true;
           stage(m, o, o, n, dt);
           break;
         case GMC_TIME_PC2:
           stage(m, o, o, n, dt / 2.0);
           stage(m, o, n, t3, dt / 2.0);
+          stage_last = true;
           stage(m, o, t3, n, dt);
           break;
         default:
           stage(m, o, o, n, dt / 3.0);
           stage(m, o, n, t3, dt / 2.0);
+          stage_last = true;
           stage(m, o, t3, n, dt);
           break;
       }
+      stage_last = false;
       const Slot<R> &N = slots[m * 3 + n];
       if (grid.cfg.forcing == GMC_FORCING_HELD_SUAREZ)   // test_forcing_run (gmcore_mod.F90:586)
         K("held_suarez", 1, [&] { launch_held_suarez<R>(dg, L, N, dt); });
