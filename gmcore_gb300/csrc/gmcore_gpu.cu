@@ -970,8 +970,12 @@ struct Engine : EngineBase {
   std::function<void()> after_last;              // enqueued after the last step's launches
   void io_streams() {
     if (xstream) return;
-    CK(cudaStreamCreateWithFlags(&xstream, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&qstream, cudaStreamNonBlocking));
+    // the transfer streams' conversion kernels are small and gate the step's
+    // readers (or the end of the call): they go ahead of the step's blocks
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CK(cudaStreamCreateWithPriority(&xstream, cudaStreamNonBlocking, hi));
+    CK(cudaStreamCreateWithPriority(&qstream, cudaStreamNonBlocking, hi));
     CK(cudaEventCreateWithFlags(&xin_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xdyn_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xpt_ev, cudaEventDisableTiming));
