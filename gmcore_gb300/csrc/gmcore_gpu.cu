@@ -610,6 +610,7 @@ struct Engine : EngineBase {
     if (xpt_ev) cudaEventDestroy(xpt_ev);
     if (xlate_ev) cudaEventDestroy(xlate_ev);
     if (xptf_ev) cudaEventDestroy(xptf_ev);
+    if (xphs_ev) cudaEventDestroy(xphs_ev);
     if (xstage) cudaFree(xstage);
     xstream = nullptr;
     xstage = nullptr;
@@ -950,7 +951,7 @@ struct Engine : EngineBase {
   // pt first (xpt_ev, waited before the first transport kernel), then the
   // others (xlate_ev, waited before the updates), then the tracers.
   cudaStream_t xstream = nullptr, qstream = nullptr;
-  cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr, xpt_ev = nullptr, xlate_ev = nullptr;
+  cudaEvent_t xin_ev = nullptr, xdyn_ev = nullptr, xpt_ev = nullptr, xlate_ev = nullptr, xphs_ev = nullptr;
   // Without test forcing (which changes pt after the integrator) the last
   // stage's update_pt leaves pt and phs final, so they move back from there
   // (xptf_ev) while the column sweep and the wind update still run.
@@ -959,6 +960,7 @@ struct Engine : EngineBase {
   bool ptf_recorded = false;
   bool io_pt = false, io_late = false, cur_io_pt = false, cur_io_late = false, pt_waited = false,
        late_waited = false;
+  bool io_phs = false, cur_io_phs = false, phs_waited = false;   // phs ahead of u_lon, v_lat (xphs_ev)
   std::vector<cudaEvent_t> qev;                  // [tracer]
   bool io_wait = false, io_rec = false;          // requested for this call's first / last step
   bool cur_io_wait = false, cur_io_rec = false;  // in effect for the step being issued
@@ -981,6 +983,7 @@ struct Engine : EngineBase {
     CK(cudaEventCreateWithFlags(&xpt_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xlate_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&xptf_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&xphs_ev, cudaEventDisableTiming));
     qev.resize((size_t)ntr);
     for (cudaEvent_t &e : qev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
@@ -1022,7 +1025,13 @@ struct Engine : EngineBase {
     if (dry) return;
     CK(cudaStreamWaitEvent(st, xpt_ev, capturing(st) ? cudaEventWaitExternal : cudaEventWaitDefault));
   }
-  void io_late_ready(cudaStream_t st) {   // before the first stage's updates read u_lon, v_lat, phs
+  void io_phs_ready(cudaStream_t st) {   // before the first stage's update_phs reads phs
+    if (!cur_io_phs || phs_waited) return;
+    phs_waited = true;
+    if (dry) return;
+    CK(cudaStreamWaitEvent(st, xphs_ev, capturing(st) ? cudaEventWaitExternal : cudaEventWaitDefault));
+  }
+  void io_late_ready(cudaStream_t st) {   // before the first stage's update_uv reads u_lon, v_lat
     if (!cur_io_late || late_waited) return;
     late_waited = true;
     if (dry) return;
@@ -1144,14 +1153,15 @@ struct Engine : EngineBase {
     // (see xpt_ev); other fields on the context stream ahead of the step;
     // then the tracers on xstream, which the first step's tracer advection
     // waits for
-    std::vector<Xfer> in_pt, in_late, in_early;
+    std::vector<Xfer> in_pt, in_phs, in_late, in_early;
     for (const Xfer &t : in_main) {
       if (t.name == "pt") in_pt.push_back(t);
-      else if (t.name == "u_lon" || t.name == "v_lat" || t.name == "phs") in_late.push_back(t);
+      else if (t.name == "phs") in_phs.push_back(t);
+      else if (t.name == "u_lon" || t.name == "v_lat") in_late.push_back(t);
       else in_early.push_back(t);
     }
     for (const Xfer &t : in_early) upload(t, stream);
-    if (!in_pt.empty() || !in_late.empty() || !in_x.empty()) {
+    if (!in_pt.empty() || !in_phs.empty() || !in_late.empty() || !in_x.empty()) {
       CK(cudaEventRecord(xin_ev, stream));
       CK(cudaStreamWaitEvent(xstream, xin_ev, 0));
     }
@@ -1159,6 +1169,11 @@ struct Engine : EngineBase {
       for (const Xfer &t : in_pt) upload(t, xstream);
       CK(cudaEventRecord(xpt_ev, xstream));
       io_pt = true;
+    }
+    if (!in_phs.empty()) {
+      for (const Xfer &t : in_phs) upload(t, xstream);
+      CK(cudaEventRecord(xphs_ev, xstream));
+      io_phs = true;
     }
     if (!in_late.empty()) {
       for (const Xfer &t : in_late) upload(t, xstream);
@@ -1204,6 +1219,7 @@ struct Engine : EngineBase {
       Engine *e;
       ~Reset() {
         e->io_wait = e->io_rec = e->io_qout = e->q_piped = e->io_pt = e->io_late = e->ptf_recorded = false;
+        e->io_phs = false;
         e->after_last = nullptr;
         if (e->xstream) cudaStreamSynchronize(e->xstream);
         if (e->qstream) cudaStreamSynchronize(e->qstream);
@@ -1472,7 +1488,7 @@ struct Engine : EngineBase {
   }
   void stage_io(const Slot<R> &O, const Slot<R> &S, const Slot<R> &N, Work<R> &w, double dt) {
     forward_w(w, S, dt);
-    io_late_ready(L.stream);   // u_lon, v_lat, phs of gmc_step_io
+    io_phs_ready(L.stream);    // phs of gmc_step_io
     if (grid.cfg.baroclinic) {
       K("update_phs", 1, [&] { launch_update_phs<R>(dg, L, O, N, w, dt); });
       K("update_pt", 1, [&] { launch_update_pt<R>(dg, L, O, N, w, dt); });
@@ -1486,6 +1502,7 @@ struct Engine : EngineBase {
     } else {
       K("update_gz", 1, [&] { launch_update_gz<R>(dg, L, O, N, w, dt); });
     }
+    io_late_ready(L.stream);   // u_lon, v_lat of gmc_step_io
     K("update_uv", 1, [&] { launch_update_uv<R>(dg, L, O, N, w, dt); });
   }
 
@@ -2117,7 +2134,8 @@ struct Engine : EngineBase {
       cur_io_qout = io_qout && it == nsteps - 1;
       cur_io_pt = io_pt && it == 0;
       cur_io_late = io_late && it == 0;
-      io_waited = pt_waited = late_waited = false;
+      cur_io_phs = io_phs && it == 0;
+      io_waited = pt_waited = late_waited = phs_waited = false;
       // tracer alert: time_is_alerted(name) .and. time_step > 0 (adv_mod.F90:166, time_mod.F90:270-291)
       const bool ring = ntr > 0 && alert_last + grid.cfg.dt_adv <= curr_time + 1e-9 * grid.cfg.dt_adv;
       if (ring) alert_ring = true;
@@ -2132,7 +2150,7 @@ struct Engine : EngineBase {
       if (use_graphs) {
         const GraphKey key{o, n, uv_step, mf_step, we_step, (ring && time_step > 0) ? 1 : 0, q_old, lay,
                            (cur_io_wait ? 1 : 0) | (cur_io_rec ? 2 : 0) | (cur_io_qout ? 4 : 0) |
-                               (cur_io_pt ? 8 : 0) | (cur_io_late ? 16 : 0)};
+                               (cur_io_pt ? 8 : 0) | (cur_io_late ? 16 : 0) | (cur_io_phs ? 32 : 0)};
         auto gi = graphs.find(key);
         if (gi == graphs.end()) {
           cudaGraph_t gr = nullptr;
@@ -2183,7 +2201,7 @@ struct Engine : EngineBase {
       std::swap(old_i, new_i);
       ++time_step;
     }
-    cur_io_wait = cur_io_rec = cur_io_qout = cur_io_pt = cur_io_late = false;
+    cur_io_wait = cur_io_rec = cur_io_qout = cur_io_pt = cur_io_late = cur_io_phs = false;
     if (after_last) after_last();
     CK(cudaEventRecord(ev_b, stream));
     CK(cudaGetLastError());
