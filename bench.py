@@ -376,8 +376,12 @@ def run_ours(args):
     e2e_steps = max(2, min(args.steps, 10))
     e2e_staged_s, _ = e2e_run(model, e2e_steps, registered=False)
     e2e_sep_s, _ = e2e_run(model, e2e_steps, registered=True)
-    e2e_run(model, 1, registered=True, exchange=True)   # captures the exchange's step graphs
-    e2e_s, h2d = e2e_run(model, e2e_steps, registered=True, exchange=True)
+    # the exchange's step graphs (one per tracer-cadence phase) are captured
+    # by untimed exchanges first; then the median of three timed runs, so that
+    # one run that meets a host stall does not stand for the path
+    e2e_run(model, 12, registered=True, exchange=True)
+    runs = [e2e_run(model, e2e_steps, registered=True, exchange=True) for _ in range(3)]
+    e2e_s, h2d = sorted(runs)[1]
     e2e_value = DT * e2e_steps / e2e_s * WORLD
     e2e_sep_value = DT * e2e_steps / e2e_sep_s * WORLD
     e2e_staged_value = DT * e2e_steps / e2e_staged_s * WORLD
@@ -508,7 +512,7 @@ def run_ours(args):
                              "path": "the exchange path of e2e (gmc_step_io, registered arrays), FP64 form"},
                      "roofline": fp64_roof},
             "e2e": {"value": e2e_value, "unit": "sim days/wall-day", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": h2d, "steps": e2e_steps,
+                    "d2h_bytes_per_step": h2d, "steps": e2e_steps, "runs": "median of 3",
                     "path": "one gmc_step_io call per step (u, v, pt, phs and the tracers in, the same out; host "
                             "float64 arrays page-locked once with gmc_host_register): tracer inputs move during the "
                             "dynamics, the fields move back during the tracer advection",
