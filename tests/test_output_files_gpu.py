@@ -202,3 +202,42 @@ def test_background_write_failure_is_reported(tmp_path):
     assert e.value.code == abi.GMC_EIO
     m.restart_write(tmp_path / "r.nc", 0.0)
     m.close()
+
+
+@pytest.mark.parametrize("background", [False, True])
+def test_ensemble_member_files_equal_single_runs(tmp_path, background):
+    """Member 1 of a two-member context writes the restart and history files
+    that a one-member context holding the same state writes, byte for byte."""
+    one = bc_config(abi.PREC_MIXED)
+    ens_cfg = bc_config(abi.PREC_MIXED)
+    ens_cfg.n_members = 2
+    states = [g.make_ic(one, 2, 40 + k, 0.5) for k in range(2)]
+    ens = g.Model(ens_cfg)
+    for k, st in enumerate(states):
+        ens.set_state(st, member=k)
+    ens.prepare()
+    ens.step(2)
+    single = started(one, states[1], 2)
+    for name, call in (("r0", "restart_write"), ("h0", "history_write")):
+        getattr(ens, call)(tmp_path / f"ens.{name}.nc", 1200.0, member=1, background=background)
+        ens.output_wait()
+        getattr(single, call)(tmp_path / f"one.{name}.nc", 1200.0)
+        assert (tmp_path / f"ens.{name}.nc").read_bytes() == (tmp_path / f"one.{name}.nc").read_bytes(), name
+    ens.close()
+    single.close()
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_shallow_water_restart_continues_bit_for_bit(tmp_path, precision):
+    cfg = swm_config(precision)
+    a = started(cfg, g.make_ic(cfg, 1, 5, 1.0), 4)
+    a.restart_write(tmp_path / "swm.r0.nc", 2400.0)
+    b = g.Model(cfg)
+    assert b.restart_read(tmp_path / "swm.r0.nc") == 2400.0
+    b.prepare()
+    a.step(5)
+    b.step(5)
+    for k in ("u_lon", "v_lat", "gz"):
+        assert np.array_equal(a.get_field(k), b.get_field(k)), k
+    a.close()
+    b.close()
