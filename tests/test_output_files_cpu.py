@@ -87,21 +87,34 @@ def test_shallow_water_restart_round_trip(tmp_path):
     assert all(np.array_equal(back[k], st[k]) for k in st)
 
 
-def test_restart_written_by_scipy_is_read(tmp_path):
-    """A restart another netCDF writer made (CDF-2 with several record
-    variables, time in days) is read; a tracer the file lacks is left alone."""
+@pytest.mark.parametrize("version", [1, 2])
+def test_restart_written_by_scipy_is_read(tmp_path, version):
+    """A restart another netCDF writer made (CDF-1 or CDF-2, several record
+    variables and two records, time in days, variables and attributes the
+    library does not use) is read from its first record; a tracer the file
+    lacks is left alone."""
     cfg = bc_config()
     st = g.make_ic(cfg, 2, 5, 1.0)
     path = str(tmp_path / "other.nc")
-    with netcdf(path, "w", version=2) as w:
+    with netcdf(path, "w", version=version) as w:
+        w.title = "written by another netCDF writer"
         for d, n in (("time", None), ("lon", 72), ("lat", 37), ("ilon", 72), ("ilat", 36), ("lev", 26)):
             w.createDimension(d, n)
         tv = w.createVariable("time", "d", ("time",))
         tv.units = "days since 1990-01-01"
         tv[0] = 1.25
+        tv[1] = 2.5
+        extra = w.createVariable("unused", "f", ("lat", "lon"))
+        extra.scale = np.float32(2.0)
+        extra[:] = 1.0
+        w.createVariable("counts", "i", ("time",))[:] = [3, 4]
         for name, (key, dims, _, _) in RESTART_BC.items():
-            w.createVariable(name, "d", dims)[0] = st[key] * 1.5
-        w.createVariable("q2", "d", ("time", "lev", "lat", "lon"))[0] = st["q"][1] * 2
+            var = w.createVariable(name, "d", dims)
+            var[0] = st[key] * 1.5
+            var[1] = st[key] * 9.0   # a second record, not read
+        qv = w.createVariable("q2", "d", ("time", "lev", "lat", "lon"))
+        qv[0] = st["q"][1] * 2
+        qv[1] = 0.0
     t, back = g.restart_read_host(cfg, path)
     assert t == 1.25 * 86400
     for name, (key, _, _, _) in RESTART_BC.items():
