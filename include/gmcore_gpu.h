@@ -301,8 +301,8 @@ int gmc_ffsl_hflx(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
  * time) race on it.  Results equal gmc_ffsl_hflx's. */
 int gmc_ffsl_hflx_noalloc(gmc_ctx *ctx, const gmc_ffsl_fields *f, double dt);
 
-/* Tangent-linear and adjoint of nsteps model steps (the benchmark spec's
- * differentiation path; the reference, a forward-only model, has no
+/* Tangent-linear and adjoint of nsteps model steps (the differentiation
+ * path for variational data assimilation; the reference, a forward-only model, has no
  * counterpart: its closest interface is time_integrate,
  * gmcore_mod.F90:577-591, whose derivative these are).  Both start from the
  * prepared state (call right after gmc_prepare) and leave the model at step
