@@ -53,6 +53,20 @@ def test_null_arguments():
     assert lib.gmc_step(None, 1) == abi.GMC_EINVAL
     assert lib.gmc_prepare(None) == abi.GMC_EINVAL
     assert lib.gmc_last_error(None) == b"null context"
+    # the file calls
+    assert lib.gmc_restart_write(None, 0, b"x.nc", 0.0, None) == abi.GMC_EINVAL
+    assert lib.gmc_restart_read(None, 0, b"x.nc", None, None) == abi.GMC_EINVAL
+    assert lib.gmc_history_write(None, 0, b"x.nc", 0.0, 0, None) == abi.GMC_EINVAL
+    assert lib.gmc_output_wait(None) == abi.GMC_EINVAL
+    err = C.create_string_buffer(128)
+    assert lib.gmc_restart_write_host(None, b"x.nc", 0.0, None, None, err, len(err)) == abi.GMC_EINVAL
+    assert err.value == b"null configuration"
+    cfg = abi.default_config(nlon=36, nlat=19, nlev=1, baroclinic=0, dt_dyn=600.0)
+    assert lib.gmc_restart_write_host(C.byref(cfg), None, 0.0, None, None, err, len(err)) == abi.GMC_EINVAL
+    assert lib.gmc_restart_read_host(C.byref(cfg), None, None, None, None, None, 0) == abi.GMC_EINVAL
+    bad = abi.default_config(nlon=7, nlat=19, nlev=1, baroclinic=0, dt_dyn=600.0)
+    assert lib.gmc_restart_read_host(C.byref(bad), b"x.nc", None, None, None, err, len(err)) == abi.GMC_EINVAL
+    assert b"nlon" in err.value
 
 
 def test_no_gpu_means_an_error_not_a_fallback():
