@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kOutThreads) k_out_div(DGrid g, const R *__res
 }
 
 // Layer mass at cell (i0, row j) of level k: ph_lev(k+1) - ph_lev(k)
-// (baroclinic) or (gz - gzs) / g (calc_m, operators_mod.F90:471-503).
+// (baroclinic) or (gz - gzs) / g (calc_m, operators_mod.F90:471-531).
 template <class R>
 __device__ __forceinline__ double out_mass(const DGrid &g, const Slot<R> &s, int i0, int j, int k) {
   const size_t c = (size_t)(j - 1) * g.nlon + i0;
