@@ -2375,6 +2375,8 @@ int guarded(gmc_ctx *ctx, F f) {
     return fail(ctx, GMC_ECUDA, e.msg);
   } catch (const std::bad_alloc &) {
     return fail(ctx, GMC_ENOMEM, "host allocation failed");
+  } catch (const std::exception &e) {   // nothing crosses the C ABI as an exception
+    return fail(ctx, GMC_EINVAL, std::string("unexpected error: ") + e.what());
   }
 }
 
@@ -2691,7 +2693,14 @@ void write_snapshot(gmc_ctx *ctx, EngineBase::OutSnap o, int device, bool histor
 void start_background(gmc_ctx *ctx, int member, bool history, const char *path, double elapsed, bool append,
                       const out::Opts &o) {
   EngineBase::OutSnap snap = ctx->eng->snapshot(member, history);
-  ctx->bg = std::thread(write_snapshot, ctx, snap, ctx->eng->device, history, std::string(path), elapsed, append, o);
+  try {
+    ctx->bg = std::thread(write_snapshot, ctx, snap, ctx->eng->device, history, std::string(path), elapsed, append, o);
+  } catch (const std::exception &e) {   // no thread: the snapshot is released here
+    cudaEventSynchronize(snap.ready);
+    cudaFree(snap.block);
+    cudaEventDestroy(snap.ready);
+    throw ApiError{GMC_EIO, std::string("cannot start the background writer: ") + e.what()};
+  }
 }
 
 }  // namespace
